@@ -1,0 +1,106 @@
+"""File formats and drivers for the oracle (test infrastructure only -- never on the product path).
+
+* model file (``DNLM``): written by :func:`write_model`, read by ``ref_harness`` (oracle/ref_harness.C)
+* state file (``DNST``): nodal + integration-point state injected by ``ref_harness forces``
+* record file: the harness' output, a sequence of named float64 arrays (:func:`read_records`)
+
+:func:`run_reference` runs the compiled reference (``oracle/_ref/ref_harness``), which exists only
+where the reference sources could be compiled (this container, not the GPU machine).
+"""
+
+from __future__ import annotations
+
+import os
+import struct
+import subprocess
+import tempfile
+from typing import Dict, Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
+
+MODEL_MAGIC = 0x4D4C4E44  # "DNLM"
+STATE_MAGIC = 0x54534E44  # "DNST"
+
+
+def write_model(path: str, m) -> None:
+    """Serialise a :class:`redynela_gb300.meshes.Model` for the harness."""
+    with open(path, "wb") as f:
+        f.write(struct.pack("<4q", MODEL_MAGIC, m.etype, m.N, m.E))
+        f.write(np.ascontiguousarray(m.coords, dtype="<f8").tobytes())
+        f.write(np.ascontiguousarray(m.conn, dtype="<i8").tobytes())
+        f.write(struct.pack("<6d", m.young, m.poisson, m.density, m.A, m.B, m.n))
+        f.write(struct.pack("<3d", *m.v0))
+        f.write(struct.pack("<q", len(m.bcs)))
+        for g in m.bcs:
+            f.write(struct.pack("<q3dq", g.kind, *g.val, len(g.nodes)))
+            f.write(np.ascontiguousarray(g.nodes, dtype="<i8").tobytes())
+        f.write(struct.pack("<6d", m.tend, m.rho_b, m.safety, float(m.freq), float(m.method),
+                            float(m.nsaves)))
+
+
+def write_state(path: str, coords, du, v, a, disp, S, Eps, EpsPlas, p, evp, dt) -> None:
+    """Nodal arrays are (N, 3); tensors are (E, nip, 3, 3); p, evp are (E, nip)."""
+    N = coords.shape[0]
+    node = np.concatenate([coords, du, v, a, disp], axis=1).reshape(N, 15)
+    E, nip = p.shape
+    ip = np.concatenate([S.reshape(E, nip, 9), Eps.reshape(E, nip, 9), EpsPlas.reshape(E, nip, 9),
+                         p.reshape(E, nip, 1), evp.reshape(E, nip, 1)], axis=2)
+    with open(path, "wb") as f:
+        f.write(struct.pack("<q", STATE_MAGIC))
+        f.write(np.ascontiguousarray(node, dtype="<f8").tobytes())
+        f.write(np.ascontiguousarray(ip, dtype="<f8").tobytes())
+        f.write(struct.pack("<d", dt))
+
+
+def read_records(path: str) -> Dict[str, np.ndarray]:
+    out = {}
+    with open(path, "rb") as f:
+        data = f.read()
+    pos = 0
+    while pos < len(data):
+        (ln,) = struct.unpack_from("<q", data, pos)
+        pos += 8
+        name = data[pos:pos + ln].decode()
+        pos += ln
+        (cnt,) = struct.unpack_from("<q", data, pos)
+        pos += 8
+        out[name] = np.frombuffer(data, dtype="<f8", count=cnt, offset=pos).copy()
+        pos += 8 * cnt
+    return out
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_HARNESS)
+
+
+def run_reference(cmd: str, model, *extra, state: Optional[dict] = None, threads: int = 1,
+                  timeout: float = 3600.0) -> Dict[str, np.ndarray]:
+    """Run ``ref_harness <cmd>`` on ``model`` in a scratch directory and return its records."""
+    if not reference_available():
+        raise RuntimeError("compiled reference not found: run `make -C oracle ref` first")
+    with tempfile.TemporaryDirectory(prefix="dnlref_") as tmp:
+        mpath = os.path.join(tmp, "model.dnlm")
+        out = os.path.join(tmp, "out.rec")
+        write_model(mpath, model)
+        args = [REF_HARNESS, cmd, mpath]
+        if cmd == "forces":
+            spath = os.path.join(tmp, "state.dnst")
+            write_state(spath, **state)
+            args += [spath, out]
+        else:
+            args += [out] + [str(x) for x in extra]
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads), OMP_DYNAMIC="FALSE")
+        env.pop("computeInternalForces", None)
+        r = subprocess.run(args, cwd=tmp, env=env, capture_output=True, text=True,
+                           timeout=timeout)
+        if r.returncode != 0:
+            raise RuntimeError(f"ref_harness {cmd} failed ({r.returncode}):\n{r.stderr[-2000:]}")
+        rec = read_records(out)
+        plot = os.path.join(tmp, "dnlref.plot")
+        if os.path.exists(plot):
+            rows = [ln.split() for ln in open(plot) if ln.strip() and not ln.startswith("#")]
+            rec["plot"] = np.array(rows, dtype=np.float64).reshape(-1, 4) if rows else np.zeros((0, 4))
+        return rec

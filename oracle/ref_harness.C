@@ -1,0 +1,525 @@
+// Driver for the reference DynELA numerical core (test infrastructure only, never shipped).
+//
+// It builds a model through the same Structure/Material/Boundary/Solver calls a .dyn deck makes
+// (Samples/Taylor/Taylor_Axi_Parametric.dyn:40-125 shows that sequence), because the .dyn
+// interpreter needs bison/flex, which this machine lacks.  Everything it computes is the
+// reference's own code: Domain::computeInternalForces (finiteElement/Domain.C:130-738),
+// ExplicitSolverCH (finiteElement/ExplicitSolverCH.C:115-567), Solver::computeTimeStep
+// (finiteElement/Solver.C:220-267), ...
+//
+// Commands (file formats are defined in oracle/dnl_io.py):
+//   ref_harness run    <model> <out>          full solve via Structure::solve(), final state
+//   ref_harness steps  <model> <out> <K>      the ExplicitSolverCH loop step by step (its private
+//                                             methods, same order as ExplicitSolverCH.C:179-274),
+//                                             recording Fint and dt for the first K steps
+//   ref_harness forces <model> <state> <out>  inject nodal + integration-point state, then one
+//                                             computeInternalMatrices + computeInternalForces
+//   ref_harness bench  <model> <out> <K>      K steps of the loop, wall time only
+//
+// Run it with OMP_NUM_THREADS=1 for golden data: strategy 0 of Domain::computeInternalForces sums
+// element forces under `omp critical`, so with several threads the summation order (and the last
+// bits of Fint) depends on scheduling.
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cstdarg>
+#include <cmath>
+#include <chrono>
+#include <iostream>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+#include <map>
+#include <list>
+#include <algorithm>
+#include <omp.h>
+#include <unistd.h>
+#include <sys/types.h>
+#include <sys/stat.h>
+
+// The harness reads solver internals (increment counters, private steps of ExplicitSolverCH).
+#define private public
+#define protected public
+#include <Structure.h>
+#include <Domain.h>
+#include <Node.h>
+#include <NodalField.h>
+#include <Element.h>
+#include <ElQua4nAx.h>
+#include <ElHex8n3D.h>
+#include <Material.h>
+#include <IsoHardElastoplastic.h>
+#include <Boundary.h>
+#include <Select.h>
+#include <Solver.h>
+#include <ExplicitSolverCH.h>
+#include <IntegrationPoint.h>
+#include <io_Structure.h>
+#undef private
+#undef protected
+
+// ------------------------------------------------------------------------------------ file IO
+struct Reader
+{
+  FILE *f;
+  explicit Reader(const char *path)
+  {
+    f = fopen(path, "rb");
+    if (!f)
+    {
+      fprintf(stderr, "ref_harness: cannot open %s\n", path);
+      exit(2);
+    }
+  }
+  ~Reader() { fclose(f); }
+  long i64()
+  {
+    long v;
+    if (fread(&v, 8, 1, f) != 1)
+      fail();
+    return v;
+  }
+  double f64()
+  {
+    double v;
+    if (fread(&v, 8, 1, f) != 1)
+      fail();
+    return v;
+  }
+  void f64s(double *p, size_t n)
+  {
+    if (n && fread(p, 8, n, f) != n)
+      fail();
+  }
+  void fail()
+  {
+    fprintf(stderr, "ref_harness: truncated input\n");
+    exit(2);
+  }
+};
+
+// Output: a sequence of named float64 records: [i64 name_len][name][i64 count][count doubles].
+struct Writer
+{
+  FILE *f;
+  explicit Writer(const std::string &path)
+  {
+    f = fopen(path.c_str(), "wb");
+    if (!f)
+    {
+      fprintf(stderr, "ref_harness: cannot write %s\n", path.c_str());
+      exit(2);
+    }
+  }
+  ~Writer() { fclose(f); }
+  void rec(const std::string &name, const double *p, size_t n)
+  {
+    long len = (long)name.size(), cnt = (long)n;
+    fwrite(&len, 8, 1, f);
+    fwrite(name.data(), 1, name.size(), f);
+    fwrite(&cnt, 8, 1, f);
+    if (n)
+      fwrite(p, 8, n, f);
+  }
+  void rec(const std::string &name, const std::vector<double> &v) { rec(name, v.data(), v.size()); }
+  void scalar(const std::string &name, double v) { rec(name, &v, 1); }
+};
+
+struct BCGroup
+{
+  long kind; // 0 restrain (val = 0/1 mask), 1 imposed speed
+  double val[3];
+  std::vector<long> nodes;
+};
+
+struct Model
+{
+  long etype; // 0 ElQua4nAx, 1 ElHex8n3D
+  long N, E, nen;
+  std::vector<double> coords; // N*3
+  std::vector<long> conn;     // E*nen, 0-based
+  double mat[6];              // E, nu, rho, A, B, n
+  double v0[3];               // initial speed of every node
+  std::vector<BCGroup> bcs;
+  double tend, rho_b, safety, freq, method, nsaves;
+};
+
+static const long MODEL_MAGIC = 0x4d4c4e44; // "DNLM"
+
+static Model readModel(const char *path)
+{
+  Reader r(path);
+  Model m;
+  if (r.i64() != MODEL_MAGIC)
+  {
+    fprintf(stderr, "ref_harness: %s is not a model file\n", path);
+    exit(2);
+  }
+  m.etype = r.i64();
+  m.N = r.i64();
+  m.E = r.i64();
+  m.nen = (m.etype == 0 ? 4 : 8);
+  m.coords.resize(m.N * 3);
+  r.f64s(m.coords.data(), m.coords.size());
+  m.conn.resize(m.E * m.nen);
+  for (size_t i = 0; i < m.conn.size(); i++)
+    m.conn[i] = r.i64();
+  r.f64s(m.mat, 6);
+  r.f64s(m.v0, 3);
+  long nbc = r.i64();
+  for (long b = 0; b < nbc; b++)
+  {
+    BCGroup g;
+    g.kind = r.i64();
+    r.f64s(g.val, 3);
+    long cnt = r.i64();
+    g.nodes.resize(cnt);
+    for (long i = 0; i < cnt; i++)
+      g.nodes[i] = r.i64();
+    m.bcs.push_back(g);
+  }
+  m.tend = r.f64();
+  m.rho_b = r.f64();
+  m.safety = r.f64();
+  m.freq = r.f64();
+  m.method = r.f64();
+  m.nsaves = r.f64();
+  return m;
+}
+
+// ------------------------------------------------------------------------------ model build
+struct Built
+{
+  Structure *st;
+  Domain *dom;
+  ExplicitSolverCH *solver;
+};
+
+static Built build(const Model &m)
+{
+  Built b;
+  Structure *st = new Structure; // registers itself as Global_Structure
+  for (long n = 0; n < m.N; n++)
+    st->createNode(n + 1, m.coords[3 * n], m.coords[3 * n + 1], m.coords[3 * n + 2]);
+
+  Element *proto = (m.etype == 0 ? (Element *)new ElQua4nAx(0) : (Element *)new ElHex8n3D(0));
+  st->setDefaultElement(proto);
+  ElementSet *els = new ElementSet;
+  for (long e = 0; e < m.E; e++)
+  {
+    const long *c = &m.conn[e * m.nen];
+    if (m.nen == 4)
+      st->createElement(e + 1, (int)c[0] + 1, (int)c[1] + 1, (int)c[2] + 1, (int)c[3] + 1);
+    else
+      st->createElement(e + 1, (int)c[0] + 1, (int)c[1] + 1, (int)c[2] + 1, (int)c[3] + 1,
+                        (int)c[4] + 1, (int)c[5] + 1, (int)c[6] + 1, (int)c[7] + 1);
+    els->add(e + 1);
+  }
+
+  Material *mat = new Material;
+  IsoHardElastoplastic *hard = new IsoHardElastoplastic;
+  hard->setYieldStress(m.mat[3]);
+  hard->setHardParameter(m.mat[4]);
+  hard->setHardExponent(m.mat[5]);
+  st->addMaterial(mat);
+  mat->setYoung(m.mat[0]);
+  mat->setPoisson(m.mat[1]);
+  mat->setDensity(m.mat[2]);
+  mat->setHardening(hard);
+  st->attachMaterialToElements(mat, els);
+
+  NodeSet *all = new NodeSet;
+  for (long n = 0; n < m.N; n++)
+    all->add(n + 1);
+  BoundarySpeed *ini = new BoundarySpeed;
+  ini->set(m.v0[0], m.v0[1], m.v0[2]);
+  st->attachInitialBC(ini, all);
+
+  for (size_t g = 0; g < m.bcs.size(); g++)
+  {
+    NodeSet *ns = new NodeSet;
+    for (size_t i = 0; i < m.bcs[g].nodes.size(); i++)
+      ns->add(m.bcs[g].nodes[i] + 1);
+    Boundary *bnd;
+    if (m.bcs[g].kind == 0)
+    {
+      BoundaryRestrain *r = new BoundaryRestrain;
+      r->set(m.bcs[g].val[0], m.bcs[g].val[1], m.bcs[g].val[2]);
+      bnd = r;
+    }
+    else
+    {
+      BoundarySpeed *s = new BoundarySpeed;
+      s->set(m.bcs[g].val[0], m.bcs[g].val[1], m.bcs[g].val[2]);
+      bnd = s;
+    }
+    st->attachConstantBC(bnd, ns);
+  }
+
+  ExplicitSolverCH *solver = new ExplicitSolverCH;
+  solver->setTimes(0, m.tend);
+  st->setSaveTimes(0, m.tend, m.tend / m.nsaves);
+  st->addSolver(solver);
+  solver->setTimeStepMethod(m.method == 0 ? "Courant" : "Pulse");
+  if (m.rho_b != 0.8182)
+    solver->setDissipation(m.rho_b);
+  solver->setTimeStepSafetyFactor(m.safety);
+  solver->setComputeTimeStepFrequency((Indice)m.freq);
+
+  st->initSolve();
+  // as DynELA_solve's main (Applications/DynELA_solve/main.C:100-101)
+  st->resultFile->setMode(Write);
+  st->resultFile->incrementalFile() = True;
+  b.st = st;
+  b.dom = st->domains(0);
+  b.solver = solver;
+  return b;
+}
+
+// ------------------------------------------------------------------------------ state dumps
+static void dumpNodes(Writer &w, Domain *d, const char *prefix)
+{
+  long N = d->nodes.size();
+  std::vector<double> x(3 * N), du(3 * N), v(3 * N), a(3 * N), disp(3 * N), mass(N);
+  for (long n = 0; n < N; n++)
+  {
+    Node *p = d->nodes(n);
+    for (int j = 0; j < 3; j++)
+    {
+      x[3 * n + j] = p->coords(j);
+      du[3 * n + j] = p->Current->delta_disp(j);
+      v[3 * n + j] = p->Current->mat_speed(j);
+      a[3 * n + j] = p->Current->dmat_speed(j);
+      disp[3 * n + j] = p->Current->disp(j);
+    }
+    mass[n] = p->mass;
+  }
+  std::string s(prefix);
+  w.rec(s + "coords", x);
+  w.rec(s + "du", du);
+  w.rec(s + "v", v);
+  w.rec(s + "a", a);
+  w.rec(s + "disp", disp);
+  w.rec(s + "mass", mass);
+}
+
+static void dumpIPs(Writer &w, Domain *d, const char *prefix)
+{
+  long E = d->elements.size();
+  std::vector<double> S, Eps, EpsPlas, p, evp, Sig, dEps, R, detJ;
+  for (long e = 0; e < E; e++)
+  {
+    Element *pel = d->elements(e);
+    for (long pt = 0; pt < pel->getNumberOfIntegrationPoints(); pt++)
+    {
+      pel->getIntegrationPoint(pt);
+      IntegrationPoint *ip = pel->ref;
+      for (int k = 0; k < 9; k++)
+      {
+        S.push_back(ip->S(k / 3, k % 3));
+        Eps.push_back(ip->Eps(k / 3, k % 3));
+        EpsPlas.push_back(ip->EpsPlas(k / 3, k % 3));
+        Sig.push_back(ip->Sig(k / 3, k % 3));
+        dEps.push_back(ip->dEps(k / 3, k % 3));
+        R.push_back(ip->R(k / 3, k % 3));
+      }
+      p.push_back(ip->p);
+      evp.push_back(ip->evp);
+      detJ.push_back(ip->detJ);
+    }
+  }
+  std::string s(prefix);
+  w.rec(s + "S", S);
+  w.rec(s + "Eps", Eps);
+  w.rec(s + "EpsPlas", EpsPlas);
+  w.rec(s + "p", p);
+  w.rec(s + "evp", evp);
+  w.rec(s + "Sig", Sig);
+  w.rec(s + "dEps", dEps);
+  w.rec(s + "R", R);
+  w.rec(s + "detJ", detJ);
+}
+
+static void dumpFint(Writer &w, Domain *d, const std::string &name)
+{
+  std::vector<double> f(d->Fint.size());
+  for (long i = 0; i < (long)f.size(); i++)
+    f[i] = d->Fint(i);
+  w.rec(name, f);
+}
+
+// ------------------------------------------------------------------------------ commands
+static int cmdRun(const Model &m, const std::string &out)
+{
+  Built b = build(m);
+  auto t0 = std::chrono::steady_clock::now();
+  b.st->solve();
+  auto t1 = std::chrono::steady_clock::now();
+  Writer w(out);
+  dumpNodes(w, b.dom, "final_");
+  dumpIPs(w, b.dom, "final_");
+  w.scalar("time", b.dom->currentTime);
+  w.scalar("increments", (double)b.solver->increment);
+  w.scalar("wall_s", std::chrono::duration<double>(t1 - t0).count());
+  w.scalar("threads", (double)omp_get_max_threads());
+  return 0;
+}
+
+// The body of ExplicitSolverCH::solve (ExplicitSolverCH.C:115-278), same calls in the same order,
+// with per-step records.  The history .plot line of endStep is written by the reference itself.
+static int cmdSteps(const Model &m, const std::string &out, long K, bool record)
+{
+  Built b = build(m);
+  Domain *d = b.dom;
+  ExplicitSolverCH *s = b.solver;
+  Writer w(out);
+
+  // Domain::solve prologue (Domain.C:1237-1288): history file, solver selection.
+  d->history_file = fopen("dnlref.plot", "w");
+  d->currentSolver = s;
+  s->upTime = m.tend;
+  if (!s->betweenTimeBounds())
+    return 1;
+
+  d->computeInternalMatrices();
+  d->computeMassMatrix();
+  d->computeInternalForces();
+  s->computeTimeStep(True);
+  if (record)
+  {
+    std::vector<double> mass(d->Mass.rows());
+    for (long i = 0; i < (long)mass.size(); i++)
+      mass[i] = d->Mass(i);
+    w.rec("mass", mass);
+    w.scalar("dt0", s->timeStep);
+  }
+
+  std::vector<double> dts, times, kin;
+  double wall = 0;
+  long k = 0;
+  bool run = true;
+  while (run && k < K)
+  {
+    auto t0 = std::chrono::steady_clock::now();
+    s->initStep();
+    s->computePredictions();
+    s->initIteration();
+    if (record)
+    {
+      char nm[64];
+      sprintf(nm, "fint_%06ld", k);
+      dumpFint(w, d, nm);
+      dts.push_back(s->timeStep);
+    }
+    s->explicitSolve();
+    // kinetic energy of the New field, as endStep writes it to the .plot file (ExplicitSolverCH.C:459-461)
+    double ke = record ? d->getTotalKineticEnergy() : 0.0;
+    s->endStep();
+    if (!s->betweenTimeBounds())
+      run = false;
+    if (run)
+    {
+      d->computeInternalMatrices();
+      s->computeTimeStep();
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    wall += std::chrono::duration<double>(t1 - t0).count();
+    if (record)
+    {
+      times.push_back(d->currentTime);
+      kin.push_back(ke);
+    }
+    k++;
+  }
+  if (record)
+  {
+    w.rec("dt", dts);
+    w.rec("time", times);
+    w.rec("kinetic", kin);
+    dumpNodes(w, d, "final_");
+    dumpIPs(w, d, "final_");
+  }
+  w.scalar("steps", (double)k);
+  w.scalar("wall_s", wall);
+  w.scalar("threads", (double)omp_get_max_threads());
+  w.scalar("elements", (double)d->elements.size());
+  return 0;
+}
+
+// State file: per node coords(3) du(3) v(3) a(3) disp(3); per element, per IP: S(9) Eps(9)
+// EpsPlas(9) p evp; then the solver timeStep.
+static int cmdForces(const Model &m, const char *statePath, const std::string &out)
+{
+  Built b = build(m);
+  Domain *d = b.dom;
+  Reader r(statePath);
+  if (r.i64() != 0x54534e44) // "DNST"
+  {
+    fprintf(stderr, "ref_harness: %s is not a state file\n", statePath);
+    return 2;
+  }
+  for (long n = 0; n < d->nodes.size(); n++)
+  {
+    Node *p = d->nodes(n);
+    double buf[15];
+    r.f64s(buf, 15);
+    for (int j = 0; j < 3; j++)
+    {
+      p->coords(j) = buf[j];
+      p->Current->delta_disp(j) = buf[3 + j];
+      p->Current->mat_speed(j) = buf[6 + j];
+      p->Current->dmat_speed(j) = buf[9 + j];
+      p->Current->disp(j) = buf[12 + j];
+    }
+  }
+  for (long e = 0; e < d->elements.size(); e++)
+  {
+    Element *pel = d->elements(e);
+    for (long pt = 0; pt < pel->getNumberOfIntegrationPoints(); pt++)
+    {
+      pel->getIntegrationPoint(pt);
+      IntegrationPoint *ip = pel->ref;
+      double buf[29];
+      r.f64s(buf, 29);
+      for (int k = 0; k < 9; k++)
+      {
+        ip->S(k / 3, k % 3) = buf[k];
+        ip->Eps(k / 3, k % 3) = buf[9 + k];
+        ip->EpsPlas(k / 3, k % 3) = buf[18 + k];
+      }
+      ip->p = buf[27];
+      ip->evp = buf[28];
+    }
+  }
+  d->currentSolver = b.solver;
+  b.solver->timeStep = r.f64();
+  d->computeInternalMatrices();
+  d->computeInternalForces();
+  Writer w(out);
+  dumpFint(w, d, "fint");
+  dumpIPs(w, d, "out_");
+  return 0;
+}
+
+int main(int argc, char **argv)
+{
+  if (argc < 4)
+  {
+    fprintf(stderr, "usage: ref_harness run|steps|forces|bench <model> ...\n");
+    return 2;
+  }
+  std::string cmd = argv[1];
+  Model m = readModel(argv[2]);
+  if (cmd == "run")
+    return cmdRun(m, argv[3]);
+  if (cmd == "steps" && argc >= 5)
+    return cmdSteps(m, argv[3], atol(argv[4]), true);
+  if (cmd == "bench" && argc >= 5)
+    return cmdSteps(m, argv[3], atol(argv[4]), false);
+  if (cmd == "forces" && argc >= 5)
+    return cmdForces(m, argv[3], argv[4]);
+  fprintf(stderr, "ref_harness: bad command\n");
+  return 2;
+}

@@ -1,0 +1,176 @@
+"""Model descriptions for the explicit-dynamics step: meshes, material, boundary conditions, solver.
+
+A :class:`Model` holds what a DynELA ``.dyn`` deck declares before ``END PREPROCESSOR``: nodes,
+``ElQua4nAx`` / ``ElHex8n3D`` connectivity, one ``IsoHardElastoplastic`` material, an initial
+``BoundarySpeed`` on every node, constant ``BoundaryRestrain`` / ``BoundarySpeed`` groups and the
+``ExplicitSolverCH`` settings.  Node and element order is creation order, which the reference
+keeps as its internal ``Id`` (finiteElement/Domain.C:1159-1160).
+
+Generators:
+
+* :func:`taylor_axi` -- the axisymmetric Taylor bar of Samples/Taylor/Taylor_Axi_Parametric.dyn:
+  nodes row by row, radial index fastest (:45-50), elements (:64-74), initial speed (0, -v, 0)
+  (:105-107), base restrained in y (:110-112), axis restrained in x and z (:115-117),
+  ExplicitSolverCH with Courant time step (:120-125).
+* :func:`taylor_hex` -- the 3D counterpart with ``ElHex8n3D``: a 40x40 Cartesian cross-section grid
+  over the bar's bounding square, keeping the cells whose centre lies inside the radius, extruded in
+  z; base restrained in z; Pulse time step (hex8 has no Courant length in the reference,
+  finiteElement/ElHex8n3D.C:188-192).
+* :func:`taylor_batch` -- seeded parameter draws for many independent axisymmetric Taylor bars.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import List, Sequence
+
+import numpy as np
+
+ELQUA4NAX = 0
+ELHEX8N3D = 1
+
+COURANT = 0
+PULSE = 1
+
+RESTRAIN = 0
+SPEED = 1
+
+
+@dataclass
+class BCGroup:
+    """One constant boundary condition attached to a node set (Structure::attachConstantBC).
+
+    kind RESTRAIN: ``val`` is the 0/1 mask of restrained components (BoundaryRestrain::set).
+    kind SPEED: ``val`` is the imposed velocity; components equal to 0 are left free
+    (BoundarySpeed::applyConstant, finiteElement/Boundary.C:478-525).
+    """
+
+    kind: int
+    val: Sequence[float]
+    nodes: np.ndarray
+
+
+@dataclass
+class Model:
+    etype: int
+    coords: np.ndarray  # (N, 3) float64
+    conn: np.ndarray  # (E, nen) int64, 0-based node indices
+    young: float = 117e9
+    poisson: float = 0.35
+    density: float = 8930.0
+    A: float = 90e6
+    B: float = 292e6
+    n: float = 0.31
+    v0: Sequence[float] = (0.0, 0.0, 0.0)
+    bcs: List[BCGroup] = field(default_factory=list)
+    tend: float = 80e-6
+    rho_b: float = 0.8182
+    safety: float = 0.9
+    freq: int = 10
+    method: int = COURANT
+    nsaves: int = 1
+
+    @property
+    def N(self) -> int:
+        return int(self.coords.shape[0])
+
+    @property
+    def E(self) -> int:
+        return int(self.conn.shape[0])
+
+    @property
+    def dim(self) -> int:
+        return 2 if self.etype == ELQUA4NAX else 3
+
+    @property
+    def nen(self) -> int:
+        return 4 if self.etype == ELQUA4NAX else 8
+
+    @property
+    def nip(self) -> int:
+        return 4 if self.etype == ELQUA4NAX else 8
+
+
+def taylor_axi(nr: int = 5, nz: int = 50, radius: float = 3.2e-3, length: float = 32.4e-3,
+               speed: float = 227.0, A: float = 90e6, B: float = 292e6, n: float = 0.31,
+               young: float = 117e9, poisson: float = 0.35, density: float = 8930.0,
+               tend: float = 80e-6, freq: int = 10, safety: float = 0.9,
+               rho_b: float = 0.8182) -> Model:
+    """Axisymmetric Taylor bar, nr radial x nz axial ElQua4nAx elements (x radial, y axial)."""
+    dx = radius / nr
+    dy = length / nz
+    jj, ii = np.meshgrid(np.arange(nz + 1, dtype=np.float64), np.arange(nr + 1, dtype=np.float64),
+                         indexing="ij")
+    coords = np.zeros(((nr + 1) * (nz + 1), 3))
+    coords[:, 0] = (ii * dx).ravel()
+    coords[:, 1] = (jj * dy).ravel()
+    j, i = np.meshgrid(np.arange(nz), np.arange(nr), indexing="ij")
+    n0 = (i + j * (nr + 1)).ravel()
+    conn = np.stack([n0, n0 + 1, n0 + nr + 2, n0 + nr + 1], axis=1).astype(np.int64)
+    base = np.arange(nr + 1, dtype=np.int64)
+    axis = np.arange(0, (nr + 1) * (nz + 1), nr + 1, dtype=np.int64)
+    bcs = [BCGroup(RESTRAIN, (0.0, 1.0, 0.0), base), BCGroup(RESTRAIN, (1.0, 0.0, 1.0), axis)]
+    return Model(ELQUA4NAX, coords, conn, young, poisson, density, A, B, n,
+                 (0.0, -speed, 0.0), bcs, tend, rho_b, safety, freq, COURANT)
+
+
+def taylor_hex(ncross: int = 40, nz: int = 400, radius: float = 3.2e-3, length: float = 32.4e-3,
+               speed: float = 227.0, A: float = 90e6, B: float = 292e6, n: float = 0.31,
+               young: float = 117e9, poisson: float = 0.35, density: float = 8930.0,
+               tend: float = 80e-6, freq: int = 10, safety: float = 0.9,
+               rho_b: float = 0.8182) -> Model:
+    """3D Taylor bar of ElHex8n3D: ncross x ncross cells over [-R, R]^2, cells with centre inside R.
+
+    For ncross=40, nz=400 this gives 1264 cells per layer, 505,600 elements and 538,137 nodes.
+    Nodes are numbered layer by layer (z slowest), then y, then x; only nodes used by a kept cell
+    exist.  Hex node order follows ElHex8n3D (bottom face counter-clockwise, then top face).
+    """
+    h = 2.0 * radius / ncross
+    ci = (np.arange(ncross) + 0.5) * h - radius
+    cy, cx = np.meshgrid(ci, ci, indexing="ij")
+    keep = (cx * cx + cy * cy) <= radius * radius
+    # node grid (ncross+1)^2 per layer; mark the used ones
+    used = np.zeros((ncross + 1, ncross + 1), dtype=bool)
+    ky, kx = np.nonzero(keep)
+    for dy_, dx_ in ((0, 0), (0, 1), (1, 1), (1, 0)):
+        used[ky + dy_, kx + dx_] = True
+    layer_id = -np.ones((ncross + 1, ncross + 1), dtype=np.int64)
+    uy, ux = np.nonzero(used)
+    nlayer = uy.size
+    layer_id[uy, ux] = np.arange(nlayer)
+    gx = ux * h - radius
+    gy = uy * h - radius
+    dz = length / nz
+    coords = np.zeros((nlayer * (nz + 1), 3))
+    for k in range(nz + 1):
+        coords[k * nlayer:(k + 1) * nlayer, 0] = gx
+        coords[k * nlayer:(k + 1) * nlayer, 1] = gy
+        coords[k * nlayer:(k + 1) * nlayer, 2] = k * dz
+    quad = np.stack([layer_id[ky, kx], layer_id[ky, kx + 1], layer_id[ky + 1, kx + 1],
+                     layer_id[ky + 1, kx]], axis=1)
+    ncell = quad.shape[0]
+    conn = np.zeros((ncell * nz, 8), dtype=np.int64)
+    for k in range(nz):
+        conn[k * ncell:(k + 1) * ncell, :4] = quad + k * nlayer
+        conn[k * ncell:(k + 1) * ncell, 4:] = quad + (k + 1) * nlayer
+    base = np.arange(nlayer, dtype=np.int64)
+    bcs = [BCGroup(RESTRAIN, (0.0, 0.0, 1.0), base)]
+    return Model(ELHEX8N3D, coords, conn, young, poisson, density, A, B, n,
+                 (0.0, 0.0, -speed), bcs, tend, rho_b, safety, freq, PULSE)
+
+
+def taylor_batch(count: int = 256, seed: int = 0, nr_range=(4, 40), nz_range=(40, 400),
+                 v_range=(150.0, 300.0), A_range=(60e6, 150e6), B_range=(200e6, 400e6),
+                 n_range=(0.2, 0.5), tend: float = 80e-6) -> List[Model]:
+    """Seeded draws of independent axisymmetric Taylor bars with uneven meshes."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        nr = int(rng.integers(nr_range[0], nr_range[1] + 1))
+        nz = int(rng.integers(nz_range[0], nz_range[1] + 1))
+        v = float(rng.uniform(*v_range))
+        A = float(rng.uniform(*A_range))
+        B = float(rng.uniform(*B_range))
+        nn = float(rng.uniform(*n_range))
+        out.append(taylor_axi(nr, nz, speed=v, A=A, B=B, n=nn, tend=tend))
+    return out
