@@ -1,0 +1,165 @@
+/*
+ * dnl_gpu.h -- C ABI of libdnlgpu.so, the GB300 (sm_103a) FP64 implementation of DynELA's
+ * explicit-dynamics step: element internal forces with J2 radial return, deterministic nodal
+ * assembly, critical time step and Chung-Hulbert nodal update.
+ *
+ * Plain C types only.  Every function returns a status code (DNL_OK = 0).  One handle owns all
+ * device memory of one mesh and a CUDA stream of its own; a handle is used by one host thread at a
+ * time.  Host arrays passed in are borrowed for the duration of the call and copied.
+ *
+ * Reference interfaces replaced (pantale/ReDynELA, paths under Sources/Libraries/):
+ *   dnl_internal_forces  -> Domain::computeInternalForces()        finiteElement/Domain.h:103,
+ *                           Domain.C:130-738 (a new strategy next to the OpenMP cases 0-7) and the
+ *                           Element::computeInternalForces/computeStress it calls, Element.C:164-403
+ *   dnl_create           -> Domain::initSolve()                     Domain.C:1018-1226
+ *   dnl_step / dnl_run   -> ExplicitSolverCH::solve(Real upTime)     ExplicitSolverCH.C:115-278,
+ *                           the virtual Solver::solve of finiteElement/Solver.h:126
+ *   dnl_time_step        -> Solver::computeTimeStep(Boolean)        Solver.C:220-267
+ *   dnl_get/set_state    -> the Node / NodalField / IntegrationPoint members the reference keeps on
+ *                           the host (Node.h:66-171, NodalField.h:36-97, IntegrationPoint.h:68-75)
+ */
+#ifndef DNL_GPU_H
+#define DNL_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------------------- statuses */
+enum dnl_status {
+  DNL_OK = 0,
+  DNL_ERR_NEG_DETJ = 1,      /* negative Jacobian determinant (Element2D.C:101-109) */
+  DNL_ERR_RR_NOCONV = 2,     /* radial return > 2000 iterations (Element.C:327-330) */
+  DNL_ERR_JACOBI_NOCONV = 3, /* polar decomposition, 29 Jacobi sweeps (Tensor2.C:1257-1258) */
+  DNL_ERR_PULSE_NOCONV = 4,  /* power iteration > 1000 iterations (Domain.C:936-939) */
+  DNL_ERR_DT = 5,            /* time step not positive or not finite */
+  DNL_ERR_ARG = 6,           /* invalid argument */
+  DNL_ERR_CUDA = 7,          /* CUDA runtime error; dnl_error_string() has the detail */
+  DNL_ERR_SINGULAR = 8,      /* singular element Jacobian (Matrix.C:1680-1690) */
+  DNL_ERR_TIMEOUT = 9        /* a bounded device-side wait ran out */
+};
+
+/* element types */
+#define DNL_ELQUA4NAX 0 /* ElQua4nAx: 4-node axisymmetric quad, 2x2 Gauss points */
+#define DNL_ELHEX8N3D 1 /* ElHex8n3D: 8-node hexahedron, 2x2x2 Gauss points */
+
+/* time-step methods (Solver::setTimeStepMethod, Solver.C:312-321) */
+#define DNL_COURANT 0
+#define DNL_PULSE 1
+
+/* boundary-condition kinds */
+#define DNL_BC_RESTRAIN 0 /* BoundaryRestrain: val[i] == 1 restrains component i */
+#define DNL_BC_SPEED 1    /* BoundarySpeed (constant): val[i] != 0 imposes velocity val[i] */
+
+/* handle flags */
+#define DNL_FLAG_STEP_TENSORS 1 /* keep each step's dEps and R per integration point */
+
+typedef struct dnl_handle dnl_handle;
+
+/* Mesh and boundary conditions (Structure::createNode/createElement, attachInitialBC,
+ * attachConstantBC).  Node and element order is the reference's Id order. */
+typedef struct {
+  int etype;            /* DNL_ELQUA4NAX or DNL_ELHEX8N3D */
+  int num_nodes;        /* N */
+  int num_elements;     /* E */
+  const double *coords; /* N*3, node-major (x, y, z) like Node::coords */
+  const int *conn;      /* E*nen, 0-based node indices, reference local node order */
+  double v0[3];         /* initial speed of every node (BoundarySpeed::applyInitial_V0) */
+  int num_bc;           /* constant BC groups, applied in this order */
+  const int *bc_kind;   /* num_bc: DNL_BC_RESTRAIN or DNL_BC_SPEED */
+  const double *bc_val; /* num_bc*3 */
+  const int *bc_start;  /* num_bc+1 offsets into bc_nodes */
+  const int *bc_nodes;  /* node indices of each group */
+} dnl_mesh_desc;
+
+/* Material + IsoHardElastoplastic: sigma_y = A + B * evp^n (IsoHardElastoplastic.C:171-184) */
+typedef struct {
+  double young, poisson, density;
+  double A, B, n;
+} dnl_material;
+
+/* ExplicitSolverCH settings (setTimes, setDissipation, setTimeStepSafetyFactor,
+ * setComputeTimeStepFrequency, setTimeStepMethod) */
+typedef struct {
+  double end_time;     /* solver end time; the run starts at 0 */
+  double rho_b;        /* spectral radius, reference default 0.8182 */
+  double safety;       /* time-step safety factor, default 0.9 */
+  int frequency;       /* recompute the critical time step every `frequency` increments (10) */
+  int method;          /* DNL_COURANT or DNL_PULSE */
+  int flags;           /* DNL_FLAG_* */
+} dnl_solver_params;
+
+/* Host-side view of the state.  NULL members are skipped.  Tensors are full 3x3 row-major per
+ * integration point, (E, nip, 9), like Tensor2; they are stored symmetric on the device. */
+typedef struct {
+  double *coords;  /* N*3 current coordinates */
+  double *du;      /* N*3 Current delta_disp */
+  double *v;       /* N*3 Current mat_speed */
+  double *a;       /* N*3 Current dmat_speed */
+  double *disp;    /* N*3 Current disp */
+  double *S;       /* E*nip*9 deviatoric stress */
+  double *Eps;     /* E*nip*9 strain */
+  double *EpsPlas; /* E*nip*9 plastic strain */
+  double *p;       /* E*nip pressure */
+  double *evp;     /* E*nip cumulated plastic strain */
+  double *Sig;     /* E*nip*9 stress S + p I (read only) */
+  double *mass;    /* N lumped nodal mass (read only) */
+} dnl_state_view;
+
+/* Time integration scalars (Solver members) */
+typedef struct {
+  double time;          /* Domain::currentTime */
+  double time_step;     /* Solver::timeStep */
+  double computed_step; /* Solver::computedTimeStep */
+  double kinetic;       /* Domain::getTotalKineticEnergy() of the last step */
+  long long increment;  /* Solver::increment */
+  int done;             /* 1 once the end time is reached */
+  int status;           /* first error recorded on the device */
+  int bad_element;      /* element of that error, or -1 */
+} dnl_time_info;
+
+/* ------------------------------------------------------------------------------ single mesh */
+/* Domain::initSolve (Domain.C:1018-1226): uploads the mesh, sets evp = 1e-10
+ * (IntegrationPoint.C:117), applies the initial speed and computes the reference configuration's
+ * shape-function derivatives. */
+int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_solver_params *sp,
+               dnl_handle **out);
+int dnl_destroy(dnl_handle *h);
+
+int dnl_set_state(dnl_handle *h, const dnl_state_view *s);
+int dnl_get_state(dnl_handle *h, dnl_state_view *s);
+/* dEps and R of the last element pass, (E, nip, 9); needs DNL_FLAG_STEP_TENSORS */
+int dnl_get_step_tensors(dnl_handle *h, double *dEps, double *R);
+
+/* The drop-in of Domain::computeInternalForces(): one pass of the element loop (kinematics,
+ * polar decomposition, radial return, RFI rotation, B^T sigma) and the assembly of Fint, with the
+ * reference's side effects on the integration-point state.  coords / du (N*3, may be NULL to keep
+ * the device copies) are the current coordinates and Current delta_disp; dt is Solver::timeStep;
+ * fint (dim*N, index Id*dim+j, may be NULL) receives Domain::Fint. */
+int dnl_internal_forces(dnl_handle *h, const double *coords, const double *du, double dt,
+                        double *fint);
+
+/* ExplicitSolverCH::solve prologue (ExplicitSolverCH.C:131-172): internal matrices, lumped mass,
+ * one internal-force pass, computeTimeStep(True).  dnl_step/dnl_run call it when needed. */
+int dnl_prologue(dnl_handle *h);
+/* up to nsteps passes of the ExplicitSolverCH loop, all on the device; stops at the end time */
+int dnl_step(dnl_handle *h, int nsteps, int *steps_done);
+/* the whole run to end_time */
+int dnl_run(dnl_handle *h, int *steps_done);
+/* nsteps steps captured once into a CUDA graph and replayed (same results as dnl_step) */
+int dnl_step_graph(dnl_handle *h, int nsteps, int *steps_done);
+int dnl_time_step(dnl_handle *h, double *dt);
+int dnl_get_time_info(dnl_handle *h, dnl_time_info *info);
+/* nodal internal forces of the last element pass, dim*N */
+int dnl_get_fint(dnl_handle *h, double *fint);
+
+/* --------------------------------------------------------------------------------- misc */
+const char *dnl_error_string(int status);
+int dnl_device_count(int *count);
+/* number of kernels this library launched (all handles), for launch accounting */
+long long dnl_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

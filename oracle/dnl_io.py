@@ -72,6 +72,14 @@ def read_records(path: str) -> Dict[str, np.ndarray]:
     return out
 
 
+def reference_tables() -> Dict[str, np.ndarray]:
+    """Shape-function tables of the reference elements (ref_harness tables)."""
+    with tempfile.TemporaryDirectory(prefix="dnlref_") as tmp:
+        out = os.path.join(tmp, "tables.rec")
+        subprocess.run([REF_HARNESS, "tables", out], cwd=tmp, check=True, capture_output=True)
+        return read_records(out)
+
+
 def reference_available() -> bool:
     return os.path.exists(REF_HARNESS)
 
@@ -99,8 +107,9 @@ def run_reference(cmd: str, model, *extra, state: Optional[dict] = None, threads
         if r.returncode != 0:
             raise RuntimeError(f"ref_harness {cmd} failed ({r.returncode}):\n{r.stderr[-2000:]}")
         rec = read_records(out)
-        plot = os.path.join(tmp, "dnlref.plot")
-        if os.path.exists(plot):
+        plots = [f for f in os.listdir(tmp) if f.endswith(".plot")]
+        plot = os.path.join(tmp, plots[0]) if plots else ""
+        if plot and os.path.exists(plot):
             rows = [ln.split() for ln in open(plot) if ln.strip() and not ln.startswith("#")]
             rec["plot"] = np.array(rows, dtype=np.float64).reshape(-1, 4) if rows else np.zeros((0, 4))
         return rec

@@ -1135,6 +1135,23 @@ int dnlo_set(dnlo *h, const char *nm, double value)
 
 int dnlo_bad_element(dnlo *h) { return h->bad_elem; }
 
+/* the element tables built by build_tables, for comparison with the reference's */
+int dnlo_tables(int etype, double *N, double *dN)
+{
+  dnlo t;
+  memset(&t, 0, sizeof t);
+  t.etype = etype;
+  t.dim = etype == 0 ? 2 : 3;
+  t.nen = t.nip = etype == 0 ? 4 : 8;
+  build_tables(&t);
+  for (int pt = 0; pt < t.nip; pt++)
+    for (int k = 0; k < t.nen; k++) {
+      N[pt * t.nen + k] = t.Nt[pt][k];
+      for (int c = 0; c < t.dim; c++) dN[(pt * t.nen + k) * t.dim + c] = t.dNxi[pt][k][c];
+    }
+  return 0;
+}
+
 void dnlo_set_threads(int n)
 {
 #ifdef _OPENMP

@@ -51,6 +51,7 @@ int dnlo_max_frequency(dnlo *h, double *fmax);
 int dnlo_prologue(dnlo *h);
 int dnlo_steps(dnlo *h, long nsteps, long *done);
 int dnlo_bad_element(dnlo *h);
+int dnlo_tables(int etype, double *N, double *dN);
 void dnlo_set_threads(int n);
 int dnlo_get_threads(void);
 

@@ -49,8 +49,19 @@ def lib():
         L.dnlo_max_frequency.argtypes = [C.c_void_p, dp]
         L.dnlo_steps.argtypes = [C.c_void_p, C.c_long, lp]
         L.dnlo_set_threads.argtypes = [C.c_int]
+        L.dnlo_tables.argtypes = [C.c_int, dp, dp]
         _lib = L
     return _lib
+
+
+def tables(etype: int):
+    """(N, dN/dxi) tables the oracle builds: (nip, nen) and (nip, nen, dim)."""
+    nen = 4 if etype == 0 else 8
+    dim = 2 if etype == 0 else 3
+    N = np.zeros((nen, nen))
+    dN = np.zeros((nen, nen, dim))
+    lib().dnlo_tables(etype, _dp(N), _dp(dN))
+    return N, dN
 
 
 def _dp(a):

@@ -15,6 +15,7 @@
 //   ref_harness forces <model> <state> <out>  inject nodal + integration-point state, then one
 //                                             computeInternalMatrices + computeInternalForces
 //   ref_harness bench  <model> <out> <K>      K steps of the loop, wall time only
+//   ref_harness tables <out>                  element tables of ElQua4nAx and ElHex8n3D
 //
 // Run it with OMP_NUM_THREADS=1 for golden data: strategy 0 of Domain::computeInternalForces sums
 // element forces under `omp critical`, so with several threads the summation order (and the last
@@ -503,8 +504,39 @@ static int cmdForces(const Model &m, const char *statePath, const std::string &o
   return 0;
 }
 
+// Element tables of ElQua4nAx / ElHex8n3D (ElQua4nAx.C:31-101, ElHex8n3D.C:26-161): per Gauss
+// point its weight, N_k and dN_k/dxi_c.
+static int cmdTables(const std::string &out)
+{
+  Writer w(out);
+  const ElementData *tabs[2] = {&ElQua4nAx::elementData, &ElHex8n3D::elementData};
+  const char *names[2] = {"axi", "hex"};
+  for (int t = 0; t < 2; t++)
+  {
+    const ElementData *d = tabs[t];
+    std::vector<double> wgt, N, dN;
+    for (int pt = 0; pt < d->numberOfIntegrationPoints; pt++)
+    {
+      const ElementIntegrationPoint &ip = d->integrationPoint[pt];
+      wgt.push_back(ip.weight);
+      for (int k = 0; k < d->numberOfNodes; k++)
+      {
+        N.push_back(ip.shapeFunction(k));
+        for (int c = 0; c < d->numberOfDimensions; c++)
+          dN.push_back(ip.derShapeFunction(k, c));
+      }
+    }
+    w.rec(std::string(names[t]) + "_weight", wgt);
+    w.rec(std::string(names[t]) + "_N", N);
+    w.rec(std::string(names[t]) + "_dN", dN);
+  }
+  return 0;
+}
+
 int main(int argc, char **argv)
 {
+  if (argc == 3 && std::string(argv[1]) == "tables")
+    return cmdTables(argv[2]);
   if (argc < 4)
   {
     fprintf(stderr, "usage: ref_harness run|steps|forces|bench <model> ...\n");

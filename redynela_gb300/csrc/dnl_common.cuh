@@ -1,0 +1,169 @@
+// Shared definitions of libdnlgpu: element traits, device-side time state, kernel argument packs
+// and the handle.  All arithmetic is FP64.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dnl_gpu.h"
+
+namespace dnl {
+
+// ------------------------------------------------------------------------ constants
+// basicTools/Math.h:36-46 (decimal literals, rounded to the nearest double like the reference)
+constexpr double kPi = 3.1415926535897932384626433832795;
+constexpr double kDeuxPi = 6.283185307179586476925286766559;
+constexpr double kSqrt23 = 0.8164965809277260327324280249019;
+constexpr double kSqrt32 = 1.2247448713915890490986420373529;
+// linearAlgebra/Tensor2.C:34 and finiteElement/DefaultValues.h:24-36
+constexpr double kPolarPrecision = 10.0E-10;
+constexpr int kPolarMaxIt = 30;
+constexpr double kRadialReturnPrecision = 1.0E-8;
+constexpr int kRadialReturnMaxIt = 2000;
+constexpr int kPulseMaxIt = 1000;
+constexpr double kPulseConvergence = 1e-4;
+
+// ------------------------------------------------------------------------ element traits
+template <int ET> struct Elem;
+template <> struct Elem<DNL_ELQUA4NAX> {
+  static constexpr int DIM = 2, NEN = 4, NIP = 4;
+  static constexpr int NS = 4;  // symmetric tensor components stored: xx yy zz xy
+};
+template <> struct Elem<DNL_ELHEX8N3D> {
+  static constexpr int DIM = 3, NEN = 8, NIP = 8;
+  static constexpr int NS = 6;  // xx yy zz xy xz yz
+};
+
+// integration-point state, component-major: ip[comp * nIP + (e * NIP + pt)]
+//   S[NS] | Eps[NS] | EpsPlas[NS] | p | evp | evpn (= evp^n, cached yield term)
+template <int ET> struct IpLayout {
+  static constexpr int NS = Elem<ET>::NS;
+  static constexpr int S = 0, EPS = NS, EPSP = 2 * NS, P = 3 * NS, EVP = 3 * NS + 1,
+                       EVPN = 3 * NS + 2, NCOMP = 3 * NS + 3;
+};
+
+// ------------------------------------------------------------------------ device time state
+// Mirrors the Solver / Domain members that drive ExplicitSolverCH::solve.
+struct DevTime {
+  double timeStep, currentTime, nextTime, upTime, endTime, startTime;
+  double computedTimeStep, lastTimeStep, tsDate, lastTsDate;
+  double kinetic;
+  double fmax, fmax0;                // Pulse: last frequency, Domain::fmax0
+  unsigned long long lenMinBits;     // Courant: min element length (bits of a positive double)
+  long long increment;
+  int done;
+  int status;
+  int badElem;
+  int pulseDone;                     // Pulse: power iteration converged
+  int pulseIter;
+  int pad[3];
+};
+
+// ------------------------------------------------------------------------ kernel arguments
+struct Material {
+  double young, nu, rho, A, B, n;
+  double K;          // bulk modulus E / (3 (1 - 2 nu))            (Element.C:232)
+  double G2, G3;     // 2 G and 3 G with G = E / (2 (1 + nu))      (Material.h:167-172)
+  double nB;         // n B
+  double dfun0;      // Sqrt32 * 2.0 * G, first term of dfun      (Element.C:309)
+  double Cs;         // Courant sound speed with the mean nodal density (Element.C:607-621)
+};
+
+struct NodeFields {  // one NodalField bank, SoA, 3 components each
+  double *du[3], *v[3], *a[3], *disp[3];
+};
+
+struct ElemArgs {
+  int E, N;
+  int gate;            // 1: skip the pass once the run is done or an error is recorded
+  const int *conn;     // [NEN][E]
+  double *x[3];        // current coordinates
+  const double *du[3]; // Current delta_disp
+  double *ip;          // integration-point state
+  double *fe;          // element forces [DIM][E*NEN]
+  double *detJ;        // [E*NIP] (written)
+  double *stepT;       // optional dEps|R per IP, [18][E*NIP] or nullptr
+  DevTime *tm;
+  Material mat;
+};
+
+struct GatherArgs {
+  int N, EN;              // EN = E*NEN
+  const int *start;       // node -> CSR offsets, N+1
+  const int *entry;       // entries e*NEN+k, ascending e within a node
+  const double *fe;       // [DIM][EN]
+  double *fint;           // [N*DIM], Id*dim+j
+};
+
+struct NodeArgs {
+  int N, EN;
+  const int *start, *entry;
+  const double *fe;
+  const double *mass;
+  NodeFields cur, nxt;
+  double *x[3];
+  const int *bcIdx;       // per node: -1 or index into bcCode/bcSpeed
+  const int *bcCode;      // 2 bits per component: 0 none, 1 restrained, 2 imposed speed
+  const double *bcSpeed;  // 3 per BC node
+  double *fint;           // optional [N*DIM] copy of the assembled forces
+  DevTime *tm;
+  double alphaM, beta, gamma;
+};
+
+// ------------------------------------------------------------------------ handle
+struct GraphEntry {
+  int nsteps, parity, phase;
+  cudaGraphExec_t exec;
+};
+
+}  // namespace dnl
+
+struct dnl_handle {
+  int etype, dim, nen, nip, N, E, nIP;
+  int flags;
+  cudaStream_t stream;
+  // mesh
+  int *conn;                  // [NEN][E]
+  double *x[3];
+  int *n2eStart, *n2e;        // node -> element entries
+  double *mass;               // N
+  // nodal fields, two banks (Node::Current / Node::New swap by index)
+  double *fieldMem;
+  dnl::NodeFields bank[2];
+  int cur;
+  // integration points
+  double *ip;
+  double *detJ;
+  double *stepT;
+  double *fe;                 // [DIM][E*NEN]
+  double *fint;               // [N*DIM]
+  // boundary conditions
+  int nbcNodes;
+  int *bcIdx, *bcCode, *bcNodeList;
+  double *bcSpeed;
+  bool hasSpeedBC;
+  // Pulse
+  double *ev, *ev0;
+  // time
+  dnl::DevTime *tm;
+  dnl::Material mat;
+  double alphaM, beta, gamma, omegaS, safetyOmega;
+  double endTime, rhoB, safety;
+  int freq, method;
+  bool prologueDone;
+  long long hostIncrement;    // host copy of tm->increment, valid between calls
+  // graphs
+  dnl::GraphEntry graphs[8];
+  int ngraphs;
+  char lastError[256];
+};
+
+namespace dnl {
+// launchers implemented in dnl_elem.cu
+int launch_elem(dnl_handle *h, cudaStream_t s, int gate);
+int launch_mass(dnl_handle *h, cudaStream_t s, double *me);
+int launch_courant(dnl_handle *h, cudaStream_t s);
+int launch_pulse(dnl_handle *h, cudaStream_t s);
+void set_shape_tables();
+long long &launch_counter();
+}  // namespace dnl

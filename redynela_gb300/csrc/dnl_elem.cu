@@ -1,0 +1,711 @@
+// Element kernels of libdnlgpu (sm_103a, FP64).
+//
+// k_elem<ET>   one pass of Domain::computeInternalMatrices + Domain::computeInternalForces:
+//              per integration point the shape-function gradients (Element2D.C:53-126,
+//              Element3D.C:53-113), the incremental F of the Current delta_disp
+//              (ElementAx.C:114-136, Element3D.C:182-205), the Jacobi polar decomposition
+//              (Tensor2.C:1154-1259), the J2 radial return (Element.C:245-345), the element-mean
+//              pressure and RFI rotation (Element.C:351-401) and B^T sigma (Element.C:164-214).
+// k_mass<ET>   Element::computeMassMatrix (Element.C:411-454).
+// k_courant    ElQua4nAx::getLength (ElQua4nAx.C:131-143) min-reduced (Domain.C:1613-1646).
+//
+// Threading: one thread per integration point; the NIP threads of an element are adjacent lanes
+// of one warp (32 % NIP == 0), so the element-mean pressure and the force sum over integration
+// points are warp-local (shuffles and a per-warp shared-memory transpose), and the
+// integration-point state, stored component-major, is read and written with coalesced accesses.
+//
+// Rounding: GB300 executes FP64 at a small fraction of its other rates, so the kernels are written
+// to minimise FP64 instructions and let the compiler fuse multiply-adds -- except along the chain
+// whose last bits decide the strain increment: F = I + sum dN du is accumulated onto 1 with
+// separately rounded products and sums, and C = F^T F, the Jacobi rotation angle and the rotated
+// diagonal use __dmul_rn/__dadd_rn in the reference's association order, so the eigenvalues that
+// enter ln(U) carry the same rounding as the reference.  Elsewhere results differ from the
+// reference by a few units in the last place.
+#include <cstdio>
+
+#include "dnl_common.cuh"
+
+namespace dnl {
+
+#define RMUL __dmul_rn
+#define RADD __dadd_rn
+#define RSUB __dsub_rn
+
+// Shape-function values at the Gauss points, formed by the same constant expressions as
+// ElQua4nAx.C:43-67 and ElHex8n3D.C:73-104 (e.g. (2.0 + sqrt(3.0)) / 6.0).
+struct ShapeConst {
+  double axN[3], axD[2];  // axi: N by number of sign disagreements, dN/dxi by the other axis
+  double hxN[4], hxD[3];  // hex: likewise over three axes
+};
+__constant__ ShapeConst c_shape;
+
+void set_shape_tables()
+{
+  ShapeConst s;
+  s.axN[0] = (2.0 + sqrt(3.0)) / 6.0;
+  s.axN[1] = 1.0 / 6.0;
+  s.axN[2] = (2.0 - sqrt(3.0)) / 6.0;
+  s.axD[0] = (3.0 + sqrt(3.0)) / 12.0;
+  s.axD[1] = (3.0 - sqrt(3.0)) / 12.0;
+  s.hxN[0] = (9.0 + 5.0 * sqrt(3.0)) / 36.0;
+  s.hxN[1] = (3.0 + sqrt(3.0)) / 36.0;
+  s.hxN[2] = (3.0 - sqrt(3.0)) / 36.0;
+  s.hxN[3] = (9.0 - 5.0 * sqrt(3.0)) / 36.0;
+  s.hxD[0] = (2.0 + sqrt(3.0)) / 12.0;
+  s.hxD[1] = 1.0 / 12.0;
+  s.hxD[2] = (2.0 - sqrt(3.0)) / 12.0;
+  cudaMemcpyToSymbol(c_shape, &s, sizeof s);
+}
+
+long long &launch_counter()
+{
+  static long long n = 0;
+  return n;
+}
+
+// Node / Gauss-point signs: xi = bit0^bit1, eta = bit1, zeta = bit2 of the local index
+// (ElQua4nAx and ElHex8n3D number nodes counter-clockwise per face, bottom face first, and list
+// Gauss points in the same pattern).
+__device__ __forceinline__ int sgx(int k) { return (k ^ (k >> 1)) & 1; }
+__device__ __forceinline__ int sgy(int k) { return (k >> 1) & 1; }
+__device__ __forceinline__ int sgz(int k) { return (k >> 2) & 1; }
+
+template <int ET> struct Shape;
+template <> struct Shape<DNL_ELQUA4NAX> {
+  __device__ __forceinline__ static double N(int pt, int k)
+  {
+    const int d = (sgx(k) ^ sgx(pt)) + (sgy(k) ^ sgy(pt));
+    return d == 0 ? c_shape.axN[0] : (d == 1 ? c_shape.axN[1] : c_shape.axN[2]);
+  }
+  __device__ __forceinline__ static double dN(int pt, int k, int c)
+  {
+    const int other = c == 0 ? (sgy(k) ^ sgy(pt)) : (sgx(k) ^ sgx(pt));
+    const double v = other ? c_shape.axD[1] : c_shape.axD[0];
+    const int s = c == 0 ? sgx(k) : sgy(k);
+    return s ? v : -v;
+  }
+};
+template <> struct Shape<DNL_ELHEX8N3D> {
+  __device__ __forceinline__ static double N(int pt, int k)
+  {
+    const int d = (sgx(k) ^ sgx(pt)) + (sgy(k) ^ sgy(pt)) + (sgz(k) ^ sgz(pt));
+    return d == 0 ? c_shape.hxN[0] : (d == 1 ? c_shape.hxN[1] : (d == 2 ? c_shape.hxN[2] : c_shape.hxN[3]));
+  }
+  __device__ __forceinline__ static double dN(int pt, int k, int c)
+  {
+    const int dx = sgx(k) ^ sgx(pt), dy = sgy(k) ^ sgy(pt), dz = sgz(k) ^ sgz(pt);
+    const int d = c == 0 ? dy + dz : (c == 1 ? dx + dz : dx + dy);
+    const double v = d == 0 ? c_shape.hxD[0] : (d == 1 ? c_shape.hxD[1] : c_shape.hxD[2]);
+    const int s = c == 0 ? sgx(k) : (c == 1 ? sgy(k) : sgz(k));
+    return s ? v : -v;
+  }
+};
+
+__device__ __forceinline__ void record_error(DevTime *tm, int code, int e)
+{
+  if (atomicCAS(&tm->status, 0, code) == 0) tm->badElem = e;
+}
+
+// ----------------------------------------------------------------------------- Jacobi rotation
+// One rotation of Tensor2::polarDecomposeLnU (Tensor2.C:1183-1240) on pivot (P, Q): f <- R^T f R
+// with R the plane rotation (c, s), written with the reference's association order and its exact
+// zero/one terms dropped (x + 0 and 1 * x are exact), and Rot <- Rot R.
+template <int P, int Q>
+__device__ __forceinline__ void jacobi_rotate(double f[3][3], double rot[3][3], double c, double s)
+{
+  constexpr int O = 3 - P - Q;
+  const double ms = -s;
+  double pp[3], pq[3];  // P(m, P), P(m, Q) with P(m, j) = sum_k f(k, m) r(k, j)
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    pp[m] = RADD(RMUL(f[P][m], c), RMUL(f[Q][m], ms));
+    pq[m] = RADD(RMUL(f[P][m], s), RMUL(f[Q][m], c));
+  }
+  auto col = [&](int m, int j) -> double { return j == P ? pp[m] : (j == Q ? pq[m] : f[O][m]); };
+  auto U = [&](int i, int j) -> double {
+    if (i == O) return col(O, j);
+    if (i == P) return RADD(RMUL(c, col(P, j)), RMUL(ms, col(Q, j)));
+    return RADD(RMUL(s, col(P, j)), RMUL(c, col(Q, j)));
+  };
+  const double u00 = U(0, 0), u01 = U(0, 1), u02 = U(0, 2), u11 = U(1, 1), u12 = U(1, 2), u22 = U(2, 2);
+  f[0][0] = u00; f[0][1] = u01; f[0][2] = u02;
+  f[1][0] = u01; f[1][1] = u11; f[1][2] = u12;
+  f[2][0] = u02; f[2][1] = u12; f[2][2] = u22;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const double rp = rot[i][P], rq = rot[i][Q];
+    rot[i][P] = fma(rp, c, rq * ms);
+    rot[i][Q] = fma(rp, s, rq * c);
+  }
+}
+
+// Rotation angle of Tensor2.C:1195-1208, IEEE operations in the reference's order.
+__device__ __forceinline__ void jacobi_angle(double fpp, double fqq, double fpq, double &c, double &s)
+{
+  const double alpha = RSUB(fqq, fpp) / RMUL(2., fpq);
+  double t;
+  if (alpha != 0.) {
+    const double r = sqrt(RADD(RMUL(alpha, alpha), 1.));
+    t = 1. / RADD(alpha, alpha > 0. ? r : -r);
+  } else {
+    t = 1.;
+  }
+  c = 1. / (sqrt(RADD(1., RMUL(t, t))));
+  s = RMUL(t, c);
+}
+
+// ----------------------------------------------------------------------------- element kernel
+template <int ET>
+__global__ void __launch_bounds__(128) k_elem(ElemArgs a)
+{
+  using T = Elem<ET>;
+  using L = IpLayout<ET>;
+  using SH = Shape<ET>;
+  constexpr int NIP = T::NIP, NEN = T::NEN, DIM = T::DIM, NS = T::NS;
+  constexpr bool AXI = ET == DNL_ELQUA4NAX;
+  constexpr int EPW = 32 / NIP;  // elements per warp
+
+  __shared__ double red[128 / 32][EPW][NIP][NEN * DIM];
+
+  if (a.gate && (a.tm->done | a.tm->status)) return;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int warpFirstE = (gtid & ~31) / NIP;
+  if (warpFirstE >= a.E) return;
+  const int eRaw = gtid / NIP;
+  const bool valid = eRaw < a.E;
+  const int e = valid ? eRaw : a.E - 1;
+  const int pt = gtid % NIP;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, slot = lane / NIP;
+  const long nIP = (long)a.E * NIP;
+  const long ipx = (long)e * NIP + pt;
+  const Material &m = a.mat;
+
+  int node[NEN];
+#pragma unroll
+  for (int k = 0; k < NEN; k++) node[k] = __ldg(a.conn + (long)k * a.E + e);
+
+  // ---- kinematics: J = sum_k dN/dxi (x) x_k, then J^-1
+  double J[DIM][DIM];
+#pragma unroll
+  for (int r = 0; r < DIM; r++)
+#pragma unroll
+    for (int c = 0; c < DIM; c++) J[r][c] = 0.;
+  double Rad = 0.;  // axisymmetric radius at the Gauss point, sum N_k x_k
+#pragma unroll
+  for (int k = 0; k < NEN; k++) {
+    double xk[DIM];
+#pragma unroll
+    for (int r = 0; r < DIM; r++) xk[r] = a.x[r][node[k]];
+#pragma unroll
+    for (int r = 0; r < DIM; r++)
+#pragma unroll
+      for (int c = 0; c < DIM; c++) J[r][c] = fma(SH::dN(pt, k, c), xk[r], J[r][c]);
+    if (AXI) Rad = RADD(Rad, RMUL(SH::N(pt, k), xk[0]));
+  }
+  double detJ, Ji[DIM][DIM];
+  if (AXI) {
+    detJ = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    const double r = 1. / detJ;
+    Ji[0][0] = J[1][1] * r;
+    Ji[0][1] = -J[0][1] * r;
+    Ji[1][0] = -J[1][0] * r;
+    Ji[1][1] = J[0][0] * r;
+    if (detJ < 0. && valid) record_error(a.tm, DNL_ERR_NEG_DETJ, e);
+  } else {
+    const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    detJ = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+    const double r = 1. / detJ;
+    Ji[0][0] = c00 * r;
+    Ji[1][0] = c01 * r;
+    Ji[2][0] = c02 * r;
+    Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * r;
+    Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+    Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * r;
+    Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+    Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
+    Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+    if (detJ == 0. && valid) record_error(a.tm, DNL_ERR_SINGULAR, e);
+  }
+
+  // ---- F = I + sum_k dN_k (x) du_k (Current field), diagonal accumulated onto 1 in node order
+  double F[3][3] = {{1., 0., 0.}, {0., 1., 0.}, {0., 0., 1.}};
+  double vR = 0.;
+#pragma unroll
+  for (int k = 0; k < NEN; k++) {
+    double dNk[DIM];
+#pragma unroll
+    for (int c = 0; c < DIM; c++) {
+      double s = 0.;
+#pragma unroll
+      for (int l = 0; l < DIM; l++) s = fma(Ji[l][c], SH::dN(pt, k, l), s);
+      dNk[c] = s;
+    }
+    double uk[DIM];
+#pragma unroll
+    for (int r = 0; r < DIM; r++) uk[r] = a.du[r][node[k]];
+#pragma unroll
+    for (int r = 0; r < DIM; r++)
+#pragma unroll
+      for (int c = 0; c < DIM; c++) {
+        if (r == c)
+          F[r][c] = RADD(F[r][c], RMUL(dNk[c], uk[r]));
+        else
+          F[r][c] = fma(dNk[c], uk[r], F[r][c]);
+      }
+    if (AXI) vR = RADD(vR, RMUL(SH::N(pt, k), uk[0]));
+  }
+  if (AXI) F[2][2] = RADD(F[2][2], vR / Rad);
+
+  // ---- C = F^T F (Tensor2::Transpose then operator*), exact reference rounding
+  double f[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = i; j < 3; j++) {
+      double s;
+      if (AXI && (i == 2) != (j == 2)) {
+        s = 0.;
+      } else if (AXI && i == 2) {
+        s = RMUL(F[2][2], F[2][2]);
+      } else if (AXI) {
+        s = RADD(RMUL(F[0][i], F[0][j]), RMUL(F[1][i], F[1][j]));
+      } else {
+        s = RADD(RADD(RMUL(F[0][i], F[0][j]), RMUL(F[1][i], F[1][j])), RMUL(F[2][i], F[2][j]));
+      }
+      f[i][j] = s;
+      f[j][i] = s;
+    }
+
+  // ---- Jacobi eigen-iteration (at most 29 rotations; Tensor2.C:1169)
+  double rot[3][3] = {{1., 0., 0.}, {0., 1., 0.}, {0., 0., 1.}};
+  bool conv = false;
+  for (int it = 1; it < kPolarMaxIt; it++) {
+    int p, q;
+    if (AXI) {  // C is block diagonal: the pivot is always (0,1)
+      p = 0;
+      q = 1;
+    } else {
+      q = (fabs(f[0][1]) > fabs(f[0][2]) ? 1 : 2);
+      p = (fabs(q == 1 ? f[0][1] : f[0][2]) > fabs(f[1][2]) ? 0 : 1);
+      if (p == 1) q = 2;
+    }
+    const double fpq = p == 0 ? (q == 1 ? f[0][1] : f[0][2]) : f[1][2];
+    if (fabs(fpq) < kPolarPrecision) {
+      conv = true;
+      break;
+    }
+    double c, s;
+    if (AXI || (p == 0 && q == 1)) {
+      jacobi_angle(f[0][0], f[1][1], fpq, c, s);
+      jacobi_rotate<0, 1>(f, rot, c, s);
+    } else if (p == 0) {
+      jacobi_angle(f[0][0], f[2][2], fpq, c, s);
+      jacobi_rotate<0, 2>(f, rot, c, s);
+    } else {
+      jacobi_angle(f[1][1], f[2][2], fpq, c, s);
+      jacobi_rotate<1, 2>(f, rot, c, s);
+    }
+  }
+  if (!conv && valid) record_error(a.tm, DNL_ERR_JACOBI_NOCONV, e);
+
+  // ---- ln U = sum ln(l)/2 v v^T,  R = F sum l^-1/2 v v^T
+  double dE[3][3], Rr[3][3];
+  {
+    double lg[3], il[3];
+#pragma unroll
+    for (int cc = 0; cc < 3; cc++) {
+      lg[cc] = log(f[cc][cc]) / 2.;
+      il[cc] = rsqrt(f[cc][cc]);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = i; j < 3; j++) {
+        double su = 0., sr = 0.;
+        if (AXI && (i == 2 || j == 2)) {
+          if (i == 2 && j == 2) {
+            su = lg[2];
+            sr = il[2];
+          }
+        } else {
+#pragma unroll
+          for (int cc = 0; cc < (AXI ? 2 : 3); cc++) {
+            const double ext = rot[i][cc] * rot[j][cc];
+            su = fma(lg[cc], ext, su);
+            sr = fma(il[cc], ext, sr);
+          }
+        }
+        dE[i][j] = dE[j][i] = su;
+        Rr[i][j] = Rr[j][i] = sr;
+      }
+  }
+  double R[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      if (AXI && (i == 2) != (j == 2)) {
+        R[i][j] = 0.;
+      } else if (AXI && i == 2) {
+        R[i][j] = F[2][2] * Rr[2][2];
+      } else {
+        double s = 0.;
+#pragma unroll
+        for (int k = 0; k < (AXI ? 2 : 3); k++) s = fma(F[i][k], Rr[k][j], s);
+        R[i][j] = s;
+      }
+    }
+
+  // ---- strain, trial stress, J2 radial return (Element.C:245-345)
+  double S[3][3], Ep[3][3], Epl[3][3];
+  {
+    // symmetric component order: xx yy zz xy [xz yz]
+    const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+      const double sv = a.ip[(L::S + k) * nIP + ipx];
+      const double ev = a.ip[(L::EPS + k) * nIP + ipx];
+      const double pv = a.ip[(L::EPSP + k) * nIP + ipx];
+      S[I0[k]][I1[k]] = S[I1[k]][I0[k]] = sv;
+      Ep[I0[k]][I1[k]] = Ep[I1[k]][I0[k]] = ev + dE[I0[k]][I1[k]];
+      Epl[I0[k]][I1[k]] = Epl[I1[k]][I0[k]] = pv;
+    }
+    if (AXI) {
+      S[0][2] = S[2][0] = S[1][2] = S[2][1] = 0.;
+      Ep[0][2] = Ep[2][0] = Ep[1][2] = Ep[2][1] = 0.;
+      Epl[0][2] = Epl[2][0] = Epl[1][2] = Epl[2][1] = 0.;
+    }
+  }
+  const double trace = dE[0][0] + dE[1][1] + dE[2][2];
+  {
+    const double tr3 = trace / 3.0;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = i; j < 3; j++) {
+        if (AXI && (i == 2) != (j == 2)) continue;
+        const double dv = i == j ? dE[i][j] - tr3 : dE[i][j];
+        S[i][j] = fma(m.G2, dv, S[i][j]);
+        S[j][i] = S[i][j];
+      }
+  }
+  double evp = a.ip[L::EVP * nIP + ipx];
+  double evpn = a.ip[L::EVPN * nIP + ipx];
+  bool plastic = false;
+  {
+    double ss = S[0][0] * S[0][0] + S[1][1] * S[1][1] + S[2][2] * S[2][2];
+    double off = S[0][1] * S[0][1];
+    if (!AXI) off = fma(S[0][2], S[0][2], fma(S[1][2], S[1][2], off));
+    ss = fma(2., off, ss);
+    const double normS = sqrt(ss);
+    const double Strial = kSqrt32 * normS;
+    const double Sigv0 = RADD(m.A, RMUL(m.B, evpn));
+    if (Strial > Sigv0) {
+      plastic = true;
+      double h = m.nB * (evpn / evp);
+      double gamma = (normS - kSqrt23 * Sigv0) / (m.G2 * (1.0 + h / m.G3));
+      double xn = evpn;
+      int iteration = 0;
+      for (;;) {
+        const double xv = RADD(evp, RMUL(kSqrt23, gamma));
+        xn = exp(m.n * log(xv));  // xv^n
+        const double Sigv = RADD(m.A, RMUL(m.B, xn));
+        h = m.nB * (xn / xv);  // n B xv^(n-1)
+        const double dfun = fma(kSqrt23, h, m.dfun0);
+        const double fun = dfun * gamma - ((Strial - Sigv) + h * kSqrt23 * gamma);
+        if (fabs(fun / Sigv) > kRadialReturnPrecision) {
+          double dgamma = -fun / dfun;
+          if (dgamma < 0 && fabs(dgamma) > gamma) dgamma = -gamma * 0.9;
+          gamma += dgamma;
+        } else {
+          break;
+        }
+        iteration++;
+        if (iteration > kRadialReturnMaxIt) {
+          if (valid) record_error(a.tm, DNL_ERR_RR_NOCONV, e);
+          break;
+        }
+      }
+      const double inv = 1. / normS;
+      evp = RADD(evp, RMUL(kSqrt23, gamma));
+      evpn = xn;
+      const double c2 = m.G2 * gamma;
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = i; j < 3; j++) {
+          if (AXI && (i == 2) != (j == 2)) continue;
+          const double n1 = S[i][j] * inv;
+          S[i][j] = fma(-c2, n1, S[i][j]);
+          Epl[i][j] = fma(gamma, n1, Epl[i][j]);
+          S[j][i] = S[i][j];
+          Epl[j][i] = Epl[i][j];
+        }
+    }
+  }
+
+  // ---- element-mean pressure: sum of the NIP traces in Gauss-point order (Element.C:254, 351)
+  double pressure = 0.0;
+  {
+    const int base = lane - pt;
+#pragma unroll
+    for (int k = 0; k < NIP; k++) pressure += __shfl_sync(0xffffffffu, trace, base + k);
+    pressure /= NIP;
+  }
+  const double p = fma(m.K, pressure, a.ip[L::P * nIP + ipx]);
+
+  // ---- RFI: X <- R X R^T for S, Eps, EpsPlas (Element.C:386-388)
+  auto rfi = [&](double X[3][3]) {
+    if (AXI) {
+      double Tm[2][2];
+#pragma unroll
+      for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 2; j++) Tm[i][j] = fma(X[i][0], R[j][0], X[i][1] * R[j][1]);
+      const double y00 = fma(R[0][0], Tm[0][0], R[0][1] * Tm[1][0]);
+      const double y01 = fma(R[0][0], Tm[0][1], R[0][1] * Tm[1][1]);
+      const double y11 = fma(R[1][0], Tm[0][1], R[1][1] * Tm[1][1]);
+      X[0][0] = y00;
+      X[0][1] = X[1][0] = y01;
+      X[1][1] = y11;
+      X[2][2] = R[2][2] * (X[2][2] * R[2][2]);
+    } else {
+      double Tm[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) Tm[i][j] = fma(X[i][0], R[j][0], fma(X[i][1], R[j][1], X[i][2] * R[j][2]));
+      double Y[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = i; j < 3; j++) Y[i][j] = fma(R[i][0], Tm[0][j], fma(R[i][1], Tm[1][j], R[i][2] * Tm[2][j]));
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = i; j < 3; j++) X[i][j] = X[j][i] = Y[i][j];
+    }
+  };
+  rfi(S);
+  rfi(Ep);
+  rfi(Epl);
+
+  if (valid) {
+    const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+      a.ip[(L::S + k) * nIP + ipx] = S[I0[k]][I1[k]];
+      a.ip[(L::EPS + k) * nIP + ipx] = Ep[I0[k]][I1[k]];
+      a.ip[(L::EPSP + k) * nIP + ipx] = Epl[I0[k]][I1[k]];
+    }
+    a.ip[L::P * nIP + ipx] = p;
+    if (plastic) {
+      a.ip[L::EVP * nIP + ipx] = evp;
+      a.ip[L::EVPN * nIP + ipx] = evpn;
+    }
+    if (a.stepT) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) {
+        a.stepT[k * nIP + ipx] = dE[k / 3][k % 3];
+        a.stepT[(9 + k) * nIP + ipx] = R[k / 3][k % 3];
+      }
+      a.detJ[ipx] = detJ;
+    }
+  }
+
+  // ---- forces: c_k = dN_k . Sig . W with dN = dN/dxi J^-1, i.e. M = J^-1 Sig W (Element.C:179-212)
+  double W = detJ;
+  double hoop = 0.;
+  if (AXI) {
+    W = W * (kDeuxPi * Rad);
+    hoop = (S[2][2] + p) / Rad * W;
+  }
+  double M[DIM][DIM];
+#pragma unroll
+  for (int l = 0; l < DIM; l++)
+#pragma unroll
+    for (int i = 0; i < DIM; i++) {
+      double s = 0.;
+#pragma unroll
+      for (int j = 0; j < DIM; j++) {
+        const double sig = S[j][i] + (i == j ? p : 0.);
+        s = fma(Ji[l][j], sig, s);
+      }
+      M[l][i] = s * W;
+    }
+  double *row = red[wib][slot][pt];
+#pragma unroll
+  for (int k = 0; k < NEN; k++)
+#pragma unroll
+    for (int i = 0; i < DIM; i++) {
+      double s = 0.;
+#pragma unroll
+      for (int l = 0; l < DIM; l++) s = fma(SH::dN(pt, k, l), M[l][i], s);
+      if (AXI && i == 0) s = fma(SH::N(pt, k), hoop, s);
+      row[k * DIM + i] = s;
+    }
+  __syncwarp();
+  if (valid) {
+    // lane pt assembles node pt of its element (NEN == NIP): Fe = - sum over Gauss points
+#pragma unroll
+    for (int i = 0; i < DIM; i++) {
+      double s = 0.0;
+#pragma unroll
+      for (int q = 0; q < NIP; q++) s -= red[wib][slot][q][pt * DIM + i];
+      a.fe[(long)i * a.E * NEN + (long)e * NEN + pt] = s;
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------- mass kernel
+// Element::computeMassMatrix with the reference's rounding: M_k = sum_pt (rho N_k) W,
+// W = detJ (2 pi R).  Writes me[e*NEN + k]; Domain::computeMassMatrix's assembly is the gather.
+template <int ET>
+__global__ void __launch_bounds__(128) k_mass(ElemArgs a, double *me)
+{
+  using T = Elem<ET>;
+  using SH = Shape<ET>;
+  constexpr int NIP = T::NIP, NEN = T::NEN, DIM = T::DIM;
+  constexpr bool AXI = ET == DNL_ELQUA4NAX;
+  constexpr int EPW = 32 / NIP;
+  __shared__ double red[128 / 32][EPW][NIP][NEN];
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((gtid & ~31) / NIP >= a.E) return;
+  const int eRaw = gtid / NIP;
+  const bool valid = eRaw < a.E;
+  const int e = valid ? eRaw : a.E - 1;
+  const int pt = gtid % NIP;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, slot = lane / NIP;
+  double J[DIM][DIM];
+#pragma unroll
+  for (int r = 0; r < DIM; r++)
+#pragma unroll
+    for (int c = 0; c < DIM; c++) J[r][c] = 0.;
+  double Rad = 0.;
+#pragma unroll
+  for (int k = 0; k < NEN; k++) {
+    const int nd = a.conn[(long)k * a.E + e];
+#pragma unroll
+    for (int r = 0; r < DIM; r++) {
+      const double xr = a.x[r][nd];
+#pragma unroll
+      for (int c = 0; c < DIM; c++) J[r][c] = RADD(J[r][c], RMUL(SH::dN(pt, k, c), xr));
+    }
+    if (AXI) Rad = RADD(Rad, RMUL(SH::N(pt, k), a.x[0][nd]));
+  }
+  double detJ;
+  if (AXI) {
+    detJ = RSUB(RMUL(J[0][0], J[1][1]), RMUL(J[0][1], J[1][0]));
+  } else {
+    detJ = RADD(RADD(RMUL(RMUL(J[0][0], J[1][1]), J[2][2]), RMUL(RMUL(J[1][0], J[2][1]), J[0][2])),
+                RMUL(RMUL(J[2][0], J[0][1]), J[1][2]));
+    detJ = RSUB(detJ, RMUL(RMUL(J[2][0], J[1][1]), J[0][2]));
+    detJ = RSUB(detJ, RMUL(RMUL(J[0][0], J[2][1]), J[1][2]));
+    detJ = RSUB(detJ, RMUL(RMUL(J[1][0], J[0][1]), J[2][2]));
+  }
+  double W = detJ;  // weight 1
+  if (AXI) W = RMUL(W, RMUL(RMUL(2., kPi), Rad));
+#pragma unroll
+  for (int k = 0; k < NEN; k++) red[wib][slot][pt][k] = RMUL(RMUL(a.mat.rho, SH::N(pt, k)), W);
+  __syncwarp();
+  if (valid) {
+    double s = 0.;
+#pragma unroll
+    for (int q = 0; q < NIP; q++) s = RADD(s, red[wib][slot][q][pt]);
+    me[(long)e * NEN + pt] = s;
+  }
+  (void)lane;
+}
+
+// ----------------------------------------------------------------------------- Courant
+// ElQua4nAx::getLength with the reference's rounding; min over elements via an unsigned atomicMin
+// on the bit pattern (positive doubles order like their bits).  A non-positive or NaN length is an
+// error: the reference would turn it into a negative or NaN time step.
+__global__ void __launch_bounds__(256) k_courant(ElemArgs a)
+{
+  if (a.tm->done | a.tm->status) return;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  double len = 1e300;
+  if (e < a.E) {
+    const int n0 = a.conn[e], n1 = a.conn[a.E + e], n2 = a.conn[2L * a.E + e], n3 = a.conn[3L * a.E + e];
+    const double x31 = RSUB(a.x[0][n2], a.x[0][n0]), x24 = RSUB(a.x[0][n1], a.x[0][n3]);
+    const double y42 = RSUB(a.x[1][n3], a.x[1][n1]), y31 = RSUB(a.x[1][n2], a.x[1][n0]);
+    const double num = RADD(RMUL(x31, y42), RMUL(x24, y31));
+    const double sq = RADD(RADD(RADD(RMUL(x24, x24), RMUL(y42, y42)), RMUL(x31, x31)), RMUL(y31, y31));
+    len = num / sqrt(RMUL(2., sq));
+    if (!(len > 0.)) {
+      record_error(a.tm, DNL_ERR_DT, e);
+      len = 1e300;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) len = fmin(len, __shfl_xor_sync(0xffffffffu, len, o));
+  __shared__ double wmin[8];
+  if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = len;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = wmin[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) b = fmin(b, wmin[w]);
+    atomicMin(&a.tm->lenMinBits, (unsigned long long)__double_as_longlong(b));
+  }
+}
+
+// ----------------------------------------------------------------------------- launchers
+static ElemArgs elem_args(dnl_handle *h)
+{
+  ElemArgs a;
+  a.E = h->E;
+  a.N = h->N;
+  a.conn = h->conn;
+  for (int r = 0; r < 3; r++) {
+    a.x[r] = h->x[r];
+    a.du[r] = h->bank[h->cur].du[r];
+  }
+  a.ip = h->ip;
+  a.fe = h->fe;
+  a.detJ = h->detJ;
+  a.stepT = h->stepT;
+  a.tm = h->tm;
+  a.mat = h->mat;
+  a.gate = 1;
+  return a;
+}
+
+int launch_elem(dnl_handle *h, cudaStream_t s, int gate)
+{
+  ElemArgs a = elem_args(h);
+  a.gate = gate;
+  const long threads = (long)h->E * h->nip;
+  const int grid = (int)((threads + 127) / 128);
+  if (h->etype == DNL_ELQUA4NAX)
+    k_elem<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a);
+  else
+    k_elem<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a);
+  launch_counter()++;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
+}
+
+int launch_mass(dnl_handle *h, cudaStream_t s, double *me)
+{
+  ElemArgs a = elem_args(h);
+  const long threads = (long)h->E * h->nip;
+  const int grid = (int)((threads + 127) / 128);
+  if (h->etype == DNL_ELQUA4NAX)
+    k_mass<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a, me);
+  else
+    k_mass<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a, me);
+  launch_counter()++;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
+}
+
+int launch_courant(dnl_handle *h, cudaStream_t s)
+{
+  ElemArgs a = elem_args(h);
+  k_courant<<<(h->E + 255) / 256, 256, 0, s>>>(a);
+  launch_counter()++;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
+}
+
+}  // namespace dnl

@@ -1,0 +1,970 @@
+// Host side of libdnlgpu: the C ABI of include/dnl_gpu.h, the nodal kernels (assembly, Chung-Hulbert
+// update, boundary conditions) and the device-side time-step logic.
+//
+// Kernels:
+//   k_gather     Fint(n*dim+j) = sum of element forces in ascending element order, the order of
+//                Domain::computeInternalForces strategy 0 on one thread (Domain.C:158-195);
+//                a node-centric CSR gather, no atomics, identical from run to run.
+//   k_node       k_gather + ExplicitSolverCH::computePredictions (ExplicitSolverCH.C:387-431),
+//                explicitSolve (:490-545), updateGrid (:555-567) and the constant boundary
+//                conditions (Boundary.C:478-525, 636-665) of one node, with the reference's
+//                rounding (__dmul_rn/__dadd_rn in its operation order).
+//   k_bc_current the boundary conditions' writes to the Current field that computeStress reads
+//                (imposed speed: delta_disp = v * dt with this step's dt).
+//   k_dt         Solver::computeTimeStep (Solver.C:220-267), ExplicitSolverCH::initStep (:434-447),
+//                updateTime and Solver::betweenTimeBounds in one thread, so a run needs no
+//                host round trip per step.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "dnl_common.cuh"
+
+using namespace dnl;
+
+#define RMUL __dmul_rn
+#define RADD __dadd_rn
+#define RSUB __dsub_rn
+
+namespace {
+
+// ----------------------------------------------------------------------------- gather
+template <int DIM>
+__global__ void __launch_bounds__(256) k_gather(GatherArgs g)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= g.N) return;
+  const int b = g.start[n], e = g.start[n + 1];
+  double f[DIM];
+#pragma unroll
+  for (int c = 0; c < DIM; c++) f[c] = 0.0;
+  for (int q = b; q < e; q++) {
+    const int ent = __ldg(g.entry + q);
+#pragma unroll
+    for (int c = 0; c < DIM; c++) f[c] = RADD(f[c], __ldg(g.fe + (long)c * g.EN + ent));
+  }
+#pragma unroll
+  for (int c = 0; c < DIM; c++) g.fint[(long)n * DIM + c] = f[c];
+}
+
+// scalar gather (mass): out[n] = sum of me entries in ascending element order
+__global__ void __launch_bounds__(256) k_gather1(int N, const int *start, const int *entry,
+                                                 const double *me, double *out)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  double s = 0.;
+  for (int q = start[n]; q < start[n + 1]; q++) s = RADD(s, me[entry[q]]);
+  out[n] = s;
+}
+
+// ----------------------------------------------------------------------------- nodal update
+__device__ __forceinline__ void apply_bc(int code, const double *spd, double dt, double cdu[3],
+                                         double ndu[3], double cv[3], double nv[3], double ca[3],
+                                         double na[3])
+{
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const int act = (code >> (2 * i)) & 3;
+    if (act == 1) {
+      cdu[i] = ndu[i] = cv[i] = nv[i] = ca[i] = na[i] = 0.;
+    } else if (act == 2) {
+      ca[i] = na[i] = 0.;
+      cv[i] = nv[i] = spd[i];
+      cdu[i] = RMUL(cv[i], dt);
+      ndu[i] = RMUL(nv[i], dt);
+    }
+  }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(256) k_node(NodeArgs g)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= g.N) return;
+  DevTime *tm = g.tm;
+  if (tm->done | tm->status) return;
+  const double dt = tm->timeStep;
+  double cdu[3], cv[3], ca[3], cd[3], ndu[3], nv[3], na[3], nd[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    cdu[i] = g.cur.du[i][n];
+    cv[i] = g.cur.v[i][n];
+    ca[i] = g.cur.a[i][n];
+    cd[i] = g.cur.disp[i][n];
+  }
+  // computePredictions
+  const double c1 = RMUL(dt, RSUB(0.5, g.beta)), c2 = RMUL(dt, RSUB(1., g.gamma));
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    ndu[i] = RMUL(RADD(RMUL(ca[i], c1), cv[i]), dt);
+    nd[i] = RADD(cd[i], ndu[i]);
+    nv[i] = RADD(RMUL(ca[i], c2), cv[i]);
+    na[i] = 0.0;
+  }
+  const int bc = g.bcIdx[n];
+  int code = 0;
+  const double *spd = nullptr;
+  if (bc >= 0) {
+    code = g.bcCode[bc];
+    spd = g.bcSpeed + 3 * bc;
+    apply_bc(code, spd, dt, cdu, ndu, cv, nv, ca, na);
+  }
+  // assembled internal forces of this node
+  double f[DIM];
+#pragma unroll
+  for (int c = 0; c < DIM; c++) f[c] = 0.0;
+  for (int q = g.start[n]; q < g.start[n + 1]; q++) {
+    const int ent = __ldg(g.entry + q);
+#pragma unroll
+    for (int c = 0; c < DIM; c++) f[c] = RADD(f[c], __ldg(g.fe + (long)c * g.EN + ent));
+  }
+  if (g.fint) {
+#pragma unroll
+    for (int c = 0; c < DIM; c++) g.fint[(long)n * DIM + c] = f[c];
+  }
+  // explicitSolve
+  const double m = g.mass[n];
+#pragma unroll
+  for (int c = 0; c < DIM; c++) na[c] = f[c] / m;
+  const double cg = RMUL(dt, g.gamma), cb = RMUL(RMUL(dt, dt), g.beta);
+  const double oma = RSUB(1.0, g.alphaM);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    na[i] = RSUB(na[i], RMUL(g.alphaM, ca[i]));
+    na[i] = na[i] / oma;
+    nv[i] = RADD(nv[i], RMUL(cg, na[i]));
+    ndu[i] = RADD(ndu[i], RMUL(cb, na[i]));
+  }
+  if (bc >= 0) apply_bc(code, spd, dt, cdu, ndu, cv, nv, ca, na);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    nd[i] = RADD(cd[i], ndu[i]);
+    g.nxt.du[i][n] = ndu[i];
+    g.nxt.v[i][n] = nv[i];
+    g.nxt.a[i][n] = na[i];
+    g.nxt.disp[i][n] = nd[i];
+    g.x[i][n] = RADD(g.x[i][n], ndu[i]);
+  }
+}
+
+// Current-field writes of the constant boundary conditions before the element pass
+__global__ void k_bc_current(int nb, const int *nodes, const int *code, const double *speed,
+                             NodeFields cur, DevTime *tm)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb || (tm->done | tm->status)) return;
+  const int n = nodes[i];
+  const double dt = tm->timeStep;
+  const int cd = code[i];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const int act = (cd >> (2 * c)) & 3;
+    if (act == 1) {
+      cur.du[c][n] = 0.;
+      cur.v[c][n] = 0.;
+      cur.a[c][n] = 0.;
+    } else if (act == 2) {
+      const double s = speed[3 * i + c];
+      cur.a[c][n] = 0.;
+      cur.v[c][n] = s;
+      cur.du[c][n] = RMUL(s, dt);
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------- time step
+enum { DT_FORCE = 1, DT_POST = 2, DT_PRE = 4 };
+
+struct DtArgs {
+  DevTime *tm;
+  int mode, freq, method;
+  double safetyOmega, Cs;
+};
+
+__device__ __forceinline__ bool in_bounds(const DevTime *tm)
+{
+  const double up = tm->endTime < tm->upTime ? tm->endTime : tm->upTime;
+  return tm->currentTime >= tm->startTime && tm->currentTime < up;
+}
+
+__device__ void recompute_dt(const DtArgs &a)
+{
+  DevTime *tm = a.tm;
+  double fmax;
+  if (a.method == DNL_COURANT) {
+    const double crit = __longlong_as_double((long long)tm->lenMinBits) / a.Cs;
+    fmax = 2.0 / crit;
+    tm->lenMinBits = 0x7ff0000000000000ull;  // +inf for the next reduction
+  } else {
+    fmax = tm->fmax;
+  }
+  tm->timeStep = a.safetyOmega / fmax;
+  tm->lastTsDate = tm->tsDate;
+  tm->lastTimeStep = tm->computedTimeStep;
+  tm->tsDate = tm->currentTime;
+  tm->computedTimeStep = tm->timeStep;
+}
+
+__global__ void k_dt(DtArgs a)
+{
+  DevTime *tm = a.tm;
+  if (tm->status) return;
+  if (a.mode & DT_FORCE) recompute_dt(a);
+  if ((a.mode & DT_POST) && !tm->done) {
+    tm->currentTime = RADD(tm->currentTime, tm->timeStep);  // ExplicitSolverCH::updateTime
+    if (!in_bounds(tm)) {
+      tm->done = 1;
+    } else if (tm->increment % a.freq == 0) {
+      recompute_dt(a);
+    } else if (tm->tsDate != tm->lastTsDate) {  // LINEARdbl extrapolation (Math.h:91)
+      const double dx = RSUB(tm->currentTime, tm->lastTsDate) / RSUB(tm->tsDate, tm->lastTsDate);
+      tm->timeStep = RADD(RMUL(dx, tm->computedTimeStep), RMUL(RSUB(1.0, dx), tm->lastTimeStep));
+    }
+  }
+  if ((a.mode & DT_PRE) && !tm->done) {
+    if (!in_bounds(tm)) {
+      tm->done = 1;
+    } else {
+      if (RADD(tm->currentTime, tm->timeStep) > tm->upTime) tm->timeStep = RSUB(tm->upTime, tm->currentTime);
+      tm->nextTime = RADD(tm->currentTime, tm->timeStep);
+      tm->increment++;
+    }
+  }
+  if (!tm->done && !(tm->timeStep > 0. && tm->timeStep < 1e300)) {
+    tm->status = DNL_ERR_DT;
+    tm->badElem = -1;
+  }
+}
+
+// kinetic energy of the Current field (Domain::getTotalKineticEnergy), fixed-order block sums
+__global__ void k_kinetic(int N, NodeFields f, const double *mass, double *partial)
+{
+  __shared__ double sh[256];
+  double s = 0.;
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+    const double v0 = f.v[0][n], v1 = f.v[1][n], v2 = f.v[2][n];
+    s += .5 * mass[n] * (v0 * v0 + v1 * v1 + v2 * v2);
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+// ----------------------------------------------------------------------------- helpers
+#define CK(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t err_ = (call);                                                                \
+    if (err_ != cudaSuccess) {                                                                \
+      snprintf(g_lastError, sizeof g_lastError, "%s: %s", #call, cudaGetErrorString(err_));  \
+      return DNL_ERR_CUDA;                                                                    \
+    }                                                                                         \
+  } while (0)
+
+char g_lastError[256] = "";
+
+int check_launch()
+{
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess) {
+    snprintf(g_lastError, sizeof g_lastError, "kernel launch: %s", cudaGetErrorString(e));
+    return DNL_ERR_CUDA;
+  }
+  return 0;
+}
+
+GatherArgs gather_args(dnl_handle *h)
+{
+  GatherArgs g;
+  g.N = h->N;
+  g.EN = h->E * h->nen;
+  g.start = h->n2eStart;
+  g.entry = h->n2e;
+  g.fe = h->fe;
+  g.fint = h->fint;
+  return g;
+}
+
+int launch_gather(dnl_handle *h)
+{
+  GatherArgs g = gather_args(h);
+  const int grid = (h->N + 255) / 256;
+  if (h->dim == 2)
+    k_gather<2><<<grid, 256, 0, h->stream>>>(g);
+  else
+    k_gather<3><<<grid, 256, 0, h->stream>>>(g);
+  launch_counter()++;
+  return check_launch();
+}
+
+int launch_node(dnl_handle *h, bool keepFint)
+{
+  NodeArgs g;
+  g.N = h->N;
+  g.EN = h->E * h->nen;
+  g.start = h->n2eStart;
+  g.entry = h->n2e;
+  g.fe = h->fe;
+  g.mass = h->mass;
+  g.cur = h->bank[h->cur];
+  g.nxt = h->bank[1 - h->cur];
+  for (int i = 0; i < 3; i++) g.x[i] = h->x[i];
+  g.bcIdx = h->bcIdx;
+  g.bcCode = h->bcCode;
+  g.bcSpeed = h->bcSpeed;
+  g.fint = keepFint ? h->fint : nullptr;
+  g.tm = h->tm;
+  g.alphaM = h->alphaM;
+  g.beta = h->beta;
+  g.gamma = h->gamma;
+  const int grid = (h->N + 255) / 256;
+  if (h->dim == 2)
+    k_node<2><<<grid, 256, 0, h->stream>>>(g);
+  else
+    k_node<3><<<grid, 256, 0, h->stream>>>(g);
+  launch_counter()++;
+  return check_launch();
+}
+
+int launch_dt(dnl_handle *h, int mode)
+{
+  DtArgs a;
+  a.tm = h->tm;
+  a.mode = mode;
+  a.freq = h->freq;
+  a.method = h->method;
+  a.safetyOmega = h->safetyOmega;
+  a.Cs = h->mat.Cs;
+  k_dt<<<1, 1, 0, h->stream>>>(a);
+  launch_counter()++;
+  return check_launch();
+}
+
+int launch_bc_current(dnl_handle *h)
+{
+  if (!h->nbcNodes) return 0;
+  k_bc_current<<<(h->nbcNodes + 127) / 128, 128, 0, h->stream>>>(h->nbcNodes, h->bcNodeList, h->bcCode,
+                                                                  h->bcSpeed, h->bank[h->cur], h->tm);
+  launch_counter()++;
+  return check_launch();
+}
+
+// critical-time-step computation that precedes a DT_FORCE or a due DT_POST
+int launch_time_step_source(dnl_handle *h)
+{
+  if (h->method == DNL_COURANT) return launch_courant(h, h->stream);
+  return launch_pulse(h, h->stream);
+}
+
+int read_time(dnl_handle *h, DevTime *out)
+{
+  CK(cudaMemcpyAsync(out, h->tm, sizeof(DevTime), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int status_of(dnl_handle *h, const DevTime &t)
+{
+  (void)h;
+  return t.status;
+}
+
+// one explicit step's launches; post = complete this step's time update afterwards
+int enqueue_step(dnl_handle *h, long long incAfter, bool last)
+{
+  int r;
+  if (h->hasSpeedBC || h->nbcNodes) {
+    if ((r = launch_bc_current(h))) return r;
+  }
+  if ((r = launch_elem(h, h->stream, 1))) return r;
+  if ((r = launch_node(h, true))) return r;
+  h->cur = 1 - h->cur;  // endStep: Node::transfertNodalField
+  if (incAfter % h->freq == 0) {
+    if ((r = launch_time_step_source(h))) return r;
+  }
+  return launch_dt(h, last ? DT_POST : (DT_POST | DT_PRE));
+}
+
+}  // namespace
+
+// =============================================================================== C ABI
+extern "C" {
+
+const char *dnl_error_string(int status)
+{
+  switch (status) {
+    case DNL_OK: return "ok";
+    case DNL_ERR_NEG_DETJ: return "negative Jacobian determinant";
+    case DNL_ERR_RR_NOCONV: return "radial return did not converge in 2000 iterations";
+    case DNL_ERR_JACOBI_NOCONV: return "polar decomposition did not converge in 29 Jacobi rotations";
+    case DNL_ERR_PULSE_NOCONV: return "power iteration did not converge in 1000 iterations";
+    case DNL_ERR_DT: return "time step not positive or not finite";
+    case DNL_ERR_ARG: return "invalid argument";
+    case DNL_ERR_CUDA: return g_lastError[0] ? g_lastError : "CUDA error";
+    case DNL_ERR_SINGULAR: return "singular element Jacobian";
+    case DNL_ERR_TIMEOUT: return "device-side wait ran out";
+    default: return "unknown status";
+  }
+}
+
+int dnl_device_count(int *count)
+{
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) n = 0;
+  if (count) *count = n;
+  return 0;
+}
+
+long long dnl_kernel_launches(void) { return launch_counter(); }
+
+int dnl_destroy(dnl_handle *h)
+{
+  if (!h) return DNL_ERR_ARG;
+  for (int i = 0; i < h->ngraphs; i++) cudaGraphExecDestroy(h->graphs[i].exec);
+  void *ptrs[] = {h->conn, h->x[0], h->n2eStart, h->n2e, h->mass, h->fieldMem, h->ip, h->detJ,
+                  h->stepT, h->fe, h->fint, h->bcIdx, h->bcCode, h->bcNodeList, h->bcSpeed,
+                  h->ev, h->ev0, h->tm};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return 0;
+}
+
+int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_solver_params *sp,
+               dnl_handle **out)
+{
+  if (!mesh || !mat || !sp || !out) return DNL_ERR_ARG;
+  *out = nullptr;
+  if (mesh->etype != DNL_ELQUA4NAX && mesh->etype != DNL_ELHEX8N3D) return DNL_ERR_ARG;
+  if (mesh->num_nodes <= 0 || mesh->num_elements <= 0 || !mesh->coords || !mesh->conn) return DNL_ERR_ARG;
+  if (sp->frequency < 1 || !(sp->end_time > 0) || !(sp->safety > 0)) return DNL_ERR_ARG;
+  if (sp->method != DNL_COURANT && sp->method != DNL_PULSE) return DNL_ERR_ARG;
+  if (sp->method == DNL_COURANT && mesh->etype != DNL_ELQUA4NAX) return DNL_ERR_ARG;  // ElHex8n3D.C:188-192
+  // Node::Current->ro is set only on one NodalField (Domain.C:1088) and the fields swap every step,
+  // so a Courant recomputation at an odd increment reads a zero density; the reference would then
+  // take a zero time step.  Only even frequencies are accepted with Courant.
+  if (sp->method == DNL_COURANT && (sp->frequency % 2)) return DNL_ERR_ARG;
+  if (mesh->num_bc < 0 || (mesh->num_bc > 0 && (!mesh->bc_kind || !mesh->bc_val || !mesh->bc_start || !mesh->bc_nodes)))
+    return DNL_ERR_ARG;
+  const int N = mesh->num_nodes, E = mesh->num_elements;
+  const int nen = mesh->etype == DNL_ELQUA4NAX ? 4 : 8;
+  for (long i = 0; i < (long)E * nen; i++)
+    if (mesh->conn[i] < 0 || mesh->conn[i] >= N) return DNL_ERR_ARG;
+  for (int g = 0; g < mesh->num_bc; g++)
+    for (int q = mesh->bc_start[g]; q < mesh->bc_start[g + 1]; q++)
+      if (mesh->bc_nodes[q] < 0 || mesh->bc_nodes[q] >= N) return DNL_ERR_ARG;
+
+  static bool tablesSet = false;
+  if (!tablesSet) {
+    set_shape_tables();
+    tablesSet = true;
+  }
+
+  dnl_handle *h = new dnl_handle();
+  memset(h, 0, sizeof(dnl_handle));
+  h->etype = mesh->etype;
+  h->dim = mesh->etype == DNL_ELQUA4NAX ? 2 : 3;
+  h->nen = h->nip = nen;
+  h->N = N;
+  h->E = E;
+  h->nIP = E * h->nip;
+  h->flags = sp->flags;
+  h->freq = sp->frequency;
+  h->method = sp->method;
+  h->endTime = sp->end_time;
+  h->rhoB = sp->rho_b;
+  h->safety = sp->safety;
+  h->cur = 0;
+  *out = h;
+  auto fail = [&](int code) {
+    dnl_destroy(h);
+    *out = nullptr;
+    return code;
+  };
+#define CKF(call)                                                                             \
+  do {                                                                                        \
+    cudaError_t err_ = (call);                                                                \
+    if (err_ != cudaSuccess) {                                                                \
+      snprintf(g_lastError, sizeof g_lastError, "%s: %s", #call, cudaGetErrorString(err_));  \
+      return fail(DNL_ERR_CUDA);                                                              \
+    }                                                                                         \
+  } while (0)
+  CKF(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+
+  // material constants, in the reference's expressions
+  Material m;
+  m.young = mat->young;
+  m.nu = mat->poisson;
+  m.rho = mat->density;
+  m.A = mat->A;
+  m.B = mat->B;
+  m.n = mat->n;
+  m.K = m.young / (3. * (1. - 2. * m.nu));
+  const double G = m.young / (2. * (1. + m.nu));
+  m.G2 = 2.0 * G;
+  m.G3 = 3.0 * G;
+  m.nB = m.n * m.B;
+  m.dfun0 = 1.2247448713915890490986420373529 * 2.0 * G;
+  {
+    double ro = 0.;
+    for (int i = 0; i < 4; i++) ro += m.rho;
+    ro /= 4;
+    const double Nu = m.nu;
+    m.Cs = sqrt((m.young * (1 - Nu)) / (ro * (1 + Nu) * (1 - 2 * Nu)));
+  }
+  h->mat = m;
+  // ExplicitSolverCH::computeIntegrationParameters (ExplicitSolverCH.C:336-343)
+  const double rb = sp->rho_b;
+  h->alphaM = (2.0 * rb - 1.0) / (1.0 + rb);
+  h->beta = (5.0 - 3.0 * rb) / ((1.0 + rb) * (1.0 + rb) * (2.0 - rb));
+  h->gamma = 1.5 - h->alphaM;
+  h->omegaS = sqrt((12.0 * pow((1 + rb), 3) * (2.0 - rb)) / (10 + 15 * rb - rb * rb + pow(rb, 3) - pow(rb, 4)));
+  h->safetyOmega = sp->safety * h->omegaS;
+
+  // ---- mesh
+  std::vector<int> connT((size_t)nen * E);
+  for (int e = 0; e < E; e++)
+    for (int k = 0; k < nen; k++) connT[(size_t)k * E + e] = mesh->conn[(size_t)e * nen + k];
+  CKF(cudaMalloc(&h->conn, sizeof(int) * connT.size()));
+  CKF(cudaMemcpy(h->conn, connT.data(), sizeof(int) * connT.size(), cudaMemcpyHostToDevice));
+  {
+    double *xm;
+    CKF(cudaMalloc(&xm, sizeof(double) * 3 * (size_t)N));
+    std::vector<double> xs(3 * (size_t)N);
+    for (int n = 0; n < N; n++)
+      for (int r = 0; r < 3; r++) xs[(size_t)r * N + n] = mesh->coords[3 * (size_t)n + r];
+    CKF(cudaMemcpy(xm, xs.data(), sizeof(double) * xs.size(), cudaMemcpyHostToDevice));
+    for (int r = 0; r < 3; r++) h->x[r] = xm + (size_t)r * N;
+  }
+  // node -> (element, local node) CSR, ascending element order
+  {
+    std::vector<int> start(N + 1, 0), entry((size_t)E * nen), fill(N, 0);
+    for (long i = 0; i < (long)E * nen; i++) start[mesh->conn[i] + 1]++;
+    for (int n = 0; n < N; n++) start[n + 1] += start[n];
+    for (int e = 0; e < E; e++)
+      for (int k = 0; k < nen; k++) {
+        const int n = mesh->conn[(size_t)e * nen + k];
+        entry[start[n] + fill[n]++] = e * nen + k;
+      }
+    CKF(cudaMalloc(&h->n2eStart, sizeof(int) * (N + 1)));
+    CKF(cudaMalloc(&h->n2e, sizeof(int) * entry.size()));
+    CKF(cudaMemcpy(h->n2eStart, start.data(), sizeof(int) * (N + 1), cudaMemcpyHostToDevice));
+    CKF(cudaMemcpy(h->n2e, entry.data(), sizeof(int) * entry.size(), cudaMemcpyHostToDevice));
+  }
+  // ---- nodal fields: 2 banks x 4 fields x 3 components
+  CKF(cudaMalloc(&h->fieldMem, sizeof(double) * 24 * (size_t)N));
+  CKF(cudaMemset(h->fieldMem, 0, sizeof(double) * 24 * (size_t)N));
+  for (int b = 0; b < 2; b++)
+    for (int c = 0; c < 3; c++) {
+      double *base = h->fieldMem + (size_t)b * 12 * N;
+      h->bank[b].du[c] = base + (size_t)(0 + c) * N;
+      h->bank[b].v[c] = base + (size_t)(3 + c) * N;
+      h->bank[b].a[c] = base + (size_t)(6 + c) * N;
+      h->bank[b].disp[c] = base + (size_t)(9 + c) * N;
+    }
+  {  // BoundarySpeed::applyInitial_V0 on both fields
+    std::vector<double> v(N);
+    for (int b = 0; b < 2; b++)
+      for (int c = 0; c < 3; c++) {
+        for (int n = 0; n < N; n++) v[n] = mesh->v0[c];
+        CKF(cudaMemcpy(h->bank[b].v[c], v.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+      }
+  }
+  CKF(cudaMalloc(&h->mass, sizeof(double) * N));
+  CKF(cudaMemset(h->mass, 0, sizeof(double) * N));
+  // ---- integration points
+  const int ncomp = h->etype == DNL_ELQUA4NAX ? IpLayout<DNL_ELQUA4NAX>::NCOMP : IpLayout<DNL_ELHEX8N3D>::NCOMP;
+  const int ns = h->etype == DNL_ELQUA4NAX ? 4 : 6;
+  CKF(cudaMalloc(&h->ip, sizeof(double) * (size_t)ncomp * h->nIP));
+  CKF(cudaMemset(h->ip, 0, sizeof(double) * (size_t)ncomp * h->nIP));
+  {  // evp = 1e-10 (IntegrationPoint::flush) and its cached power
+    std::vector<double> v(h->nIP, 1e-10);
+    CKF(cudaMemcpy(h->ip + (size_t)(3 * ns + 1) * h->nIP, v.data(), sizeof(double) * h->nIP, cudaMemcpyHostToDevice));
+    const double pn = pow(1e-10, m.n);
+    for (auto &x : v) x = pn;
+    CKF(cudaMemcpy(h->ip + (size_t)(3 * ns + 2) * h->nIP, v.data(), sizeof(double) * h->nIP, cudaMemcpyHostToDevice));
+  }
+  CKF(cudaMalloc(&h->detJ, sizeof(double) * h->nIP));
+  if (h->flags & DNL_FLAG_STEP_TENSORS) {
+    CKF(cudaMalloc(&h->stepT, sizeof(double) * 18 * (size_t)h->nIP));
+    CKF(cudaMemset(h->stepT, 0, sizeof(double) * 18 * (size_t)h->nIP));
+  }
+  CKF(cudaMalloc(&h->fe, sizeof(double) * (size_t)h->dim * E * nen));
+  CKF(cudaMalloc(&h->fint, sizeof(double) * (size_t)h->dim * N));
+  CKF(cudaMemset(h->fint, 0, sizeof(double) * (size_t)h->dim * N));
+  // ---- boundary conditions: final action per node and component (the last group wins, as
+  // each BoundaryCondition::applyConstant overwrites delta_disp, mat_speed and dmat_speed)
+  {
+    std::vector<int> codeN(N, 0);
+    std::vector<double> spdN(3 * (size_t)N, 0.);
+    std::vector<char> has(N, 0);
+    for (int g = 0; g < mesh->num_bc; g++) {
+      for (int q = mesh->bc_start[g]; q < mesh->bc_start[g + 1]; q++) {
+        const int n = mesh->bc_nodes[q];
+        has[n] = 1;
+        for (int c = 0; c < 3; c++) {
+          const double v = mesh->bc_val[3 * g + c];
+          if (mesh->bc_kind[g] == DNL_BC_RESTRAIN) {
+            if (v == 1.) codeN[n] = (codeN[n] & ~(3 << (2 * c))) | (1 << (2 * c));
+          } else if (v != 0.) {
+            codeN[n] = (codeN[n] & ~(3 << (2 * c))) | (2 << (2 * c));
+            spdN[3 * (size_t)n + c] = v;
+            h->hasSpeedBC = true;
+          }
+        }
+      }
+    }
+    std::vector<int> idx(N, -1), nodes, codes;
+    std::vector<double> spds;
+    for (int n = 0; n < N; n++)
+      if (has[n] && codeN[n]) {
+        idx[n] = (int)nodes.size();
+        nodes.push_back(n);
+        codes.push_back(codeN[n]);
+        for (int c = 0; c < 3; c++) spds.push_back(spdN[3 * (size_t)n + c]);
+      }
+    h->nbcNodes = (int)nodes.size();
+    CKF(cudaMalloc(&h->bcIdx, sizeof(int) * N));
+    CKF(cudaMemcpy(h->bcIdx, idx.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    const size_t nb = nodes.size() ? nodes.size() : 1;
+    CKF(cudaMalloc(&h->bcNodeList, sizeof(int) * nb));
+    CKF(cudaMalloc(&h->bcCode, sizeof(int) * nb));
+    CKF(cudaMalloc(&h->bcSpeed, sizeof(double) * 3 * nb));
+    if (nodes.size()) {
+      CKF(cudaMemcpy(h->bcNodeList, nodes.data(), sizeof(int) * nodes.size(), cudaMemcpyHostToDevice));
+      CKF(cudaMemcpy(h->bcCode, codes.data(), sizeof(int) * codes.size(), cudaMemcpyHostToDevice));
+      CKF(cudaMemcpy(h->bcSpeed, spds.data(), sizeof(double) * spds.size(), cudaMemcpyHostToDevice));
+    }
+  }
+  // ---- Pulse vectors
+  if (h->method == DNL_PULSE) {
+    CKF(cudaMalloc(&h->ev, sizeof(double) * (size_t)h->dim * N));
+    CKF(cudaMalloc(&h->ev0, sizeof(double) * (size_t)h->dim * N));
+  }
+  // ---- time state
+  CKF(cudaMalloc(&h->tm, sizeof(DevTime)));
+  {
+    DevTime t;
+    memset(&t, 0, sizeof t);
+    t.upTime = sp->end_time;
+    t.endTime = sp->end_time;
+    t.startTime = 0.;
+    t.lenMinBits = 0x7ff0000000000000ull;
+    t.badElem = -1;
+    CKF(cudaMemcpy(h->tm, &t, sizeof t, cudaMemcpyHostToDevice));
+  }
+  CKF(cudaDeviceSynchronize());
+#undef CKF
+  return 0;
+}
+
+// ------------------------------------------------------------------------------ state access
+int dnl_set_state(dnl_handle *h, const dnl_state_view *s)
+{
+  if (!h || !s) return DNL_ERR_ARG;
+  const int N = h->N;
+  std::vector<double> buf((size_t)N);
+  auto put3 = [&](const double *src, double *const dst[3]) -> int {
+    for (int c = 0; c < 3; c++) {
+      for (int n = 0; n < N; n++) buf[n] = src[3 * (size_t)n + c];
+      CK(cudaMemcpy(dst[c], buf.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+    }
+    return 0;
+  };
+  int r;
+  if (s->coords && (r = put3(s->coords, h->x))) return r;
+  if (s->du && (r = put3(s->du, h->bank[h->cur].du))) return r;
+  if (s->v && (r = put3(s->v, h->bank[h->cur].v))) return r;
+  if (s->a && (r = put3(s->a, h->bank[h->cur].a))) return r;
+  if (s->disp && (r = put3(s->disp, h->bank[h->cur].disp))) return r;
+  const int ns = h->etype == DNL_ELQUA4NAX ? 4 : 6;
+  const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
+  const size_t nIP = h->nIP;
+  std::vector<double> ib(nIP);
+  auto putT = [&](const double *src, int base) -> int {
+    for (int k = 0; k < ns; k++) {
+      for (size_t i = 0; i < nIP; i++) ib[i] = src[9 * i + 3 * I0[k] + I1[k]];
+      CK(cudaMemcpy(h->ip + (size_t)(base + k) * nIP, ib.data(), sizeof(double) * nIP, cudaMemcpyHostToDevice));
+    }
+    return 0;
+  };
+  if (s->S && (r = putT(s->S, 0))) return r;
+  if (s->Eps && (r = putT(s->Eps, ns))) return r;
+  if (s->EpsPlas && (r = putT(s->EpsPlas, 2 * ns))) return r;
+  if (s->p) CK(cudaMemcpy(h->ip + (size_t)(3 * ns) * nIP, s->p, sizeof(double) * nIP, cudaMemcpyHostToDevice));
+  if (s->evp) {
+    CK(cudaMemcpy(h->ip + (size_t)(3 * ns + 1) * nIP, s->evp, sizeof(double) * nIP, cudaMemcpyHostToDevice));
+    for (size_t i = 0; i < nIP; i++) ib[i] = pow(s->evp[i], h->mat.n);
+    CK(cudaMemcpy(h->ip + (size_t)(3 * ns + 2) * nIP, ib.data(), sizeof(double) * nIP, cudaMemcpyHostToDevice));
+  }
+  return 0;
+}
+
+int dnl_get_state(dnl_handle *h, dnl_state_view *s)
+{
+  if (!h || !s) return DNL_ERR_ARG;
+  CK(cudaStreamSynchronize(h->stream));
+  const int N = h->N;
+  std::vector<double> buf((size_t)N);
+  auto get3 = [&](double *dst, double *const src[3]) -> int {
+    for (int c = 0; c < 3; c++) {
+      CK(cudaMemcpy(buf.data(), src[c], sizeof(double) * N, cudaMemcpyDeviceToHost));
+      for (int n = 0; n < N; n++) dst[3 * (size_t)n + c] = buf[n];
+    }
+    return 0;
+  };
+  int r;
+  if (s->coords && (r = get3(s->coords, h->x))) return r;
+  if (s->du && (r = get3(s->du, h->bank[h->cur].du))) return r;
+  if (s->v && (r = get3(s->v, h->bank[h->cur].v))) return r;
+  if (s->a && (r = get3(s->a, h->bank[h->cur].a))) return r;
+  if (s->disp && (r = get3(s->disp, h->bank[h->cur].disp))) return r;
+  if (s->mass) CK(cudaMemcpy(s->mass, h->mass, sizeof(double) * N, cudaMemcpyDeviceToHost));
+  const int ns = h->etype == DNL_ELQUA4NAX ? 4 : 6;
+  const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
+  const size_t nIP = h->nIP;
+  std::vector<double> ib(nIP), pb(nIP);
+  auto getT = [&](double *dst, int base, const double *addP) -> int {
+    for (size_t i = 0; i < 9 * nIP; i++) dst[i] = 0.;
+    for (int k = 0; k < ns; k++) {
+      CK(cudaMemcpy(ib.data(), h->ip + (size_t)(base + k) * nIP, sizeof(double) * nIP, cudaMemcpyDeviceToHost));
+      for (size_t i = 0; i < nIP; i++) {
+        dst[9 * i + 3 * I0[k] + I1[k]] = ib[i];
+        dst[9 * i + 3 * I1[k] + I0[k]] = ib[i];
+      }
+    }
+    if (addP)
+      for (size_t i = 0; i < nIP; i++)
+        for (int d = 0; d < 3; d++) dst[9 * i + 4 * d] += addP[i];
+    return 0;
+  };
+  if (s->S && (r = getT(s->S, 0, nullptr))) return r;
+  if (s->Eps && (r = getT(s->Eps, ns, nullptr))) return r;
+  if (s->EpsPlas && (r = getT(s->EpsPlas, 2 * ns, nullptr))) return r;
+  if (s->p || s->Sig) CK(cudaMemcpy(pb.data(), h->ip + (size_t)(3 * ns) * nIP, sizeof(double) * nIP, cudaMemcpyDeviceToHost));
+  if (s->p) memcpy(s->p, pb.data(), sizeof(double) * nIP);
+  if (s->Sig && (r = getT(s->Sig, 0, pb.data()))) return r;
+  if (s->evp) CK(cudaMemcpy(s->evp, h->ip + (size_t)(3 * ns + 1) * nIP, sizeof(double) * nIP, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int dnl_get_step_tensors(dnl_handle *h, double *dEps, double *R)
+{
+  if (!h || !h->stepT) return DNL_ERR_ARG;
+  CK(cudaStreamSynchronize(h->stream));
+  const size_t nIP = h->nIP;
+  std::vector<double> ib(nIP);
+  for (int k = 0; k < 18; k++) {
+    double *dst = k < 9 ? dEps : R;
+    if (!dst) continue;
+    CK(cudaMemcpy(ib.data(), h->stepT + (size_t)k * nIP, sizeof(double) * nIP, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < nIP; i++) dst[9 * i + (k % 9)] = ib[i];
+  }
+  return 0;
+}
+
+int dnl_get_fint(dnl_handle *h, double *fint)
+{
+  if (!h || !fint) return DNL_ERR_ARG;
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(fint, h->fint, sizeof(double) * (size_t)h->dim * h->N, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+// ------------------------------------------------------------------------------ the drop-in
+int dnl_internal_forces(dnl_handle *h, const double *coords, const double *du, double dt, double *fint)
+{
+  (void)dt;  // read by Element::computeStress (Element.C:225) but unused by the J2 update
+  if (!h) return DNL_ERR_ARG;
+  if (coords || du) {
+    dnl_state_view s;
+    memset(&s, 0, sizeof s);
+    s.coords = const_cast<double *>(coords);
+    s.du = const_cast<double *>(du);
+    int r = dnl_set_state(h, &s);
+    if (r) return r;
+  }
+  const int zero = 0, minus1 = -1;
+  CK(cudaMemcpyAsync(&h->tm->status, &zero, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(&h->tm->badElem, &minus1, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  int r;
+  if ((r = launch_elem(h, h->stream, 0))) return r;
+  if ((r = launch_gather(h))) return r;
+  DevTime t;
+  if ((r = read_time(h, &t))) return r;
+  if (t.status) return t.status;
+  if (fint) CK(cudaMemcpy(fint, h->fint, sizeof(double) * (size_t)h->dim * h->N, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+// ------------------------------------------------------------------------------ time loop
+int dnl_prologue(dnl_handle *h)
+{
+  if (!h) return DNL_ERR_ARG;
+  if (h->prologueDone) return 0;
+  int r;
+  // computeMassMatrix (ExplicitSolverCH.C:145): per-element lumped masses, gathered per node
+  double *me;
+  CK(cudaMalloc(&me, sizeof(double) * (size_t)h->E * h->nen));
+  if ((r = launch_mass(h, h->stream, me))) {
+    cudaFree(me);
+    return r;
+  }
+  k_gather1<<<(h->N + 255) / 256, 256, 0, h->stream>>>(h->N, h->n2eStart, h->n2e, me, h->mass);
+  launch_counter()++;
+  if ((r = check_launch())) {
+    cudaFree(me);
+    return r;
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  cudaFree(me);
+  // computeInternalForces with the initial Current field (:157), then computeTimeStep(True) (:172)
+  if ((r = launch_elem(h, h->stream, 1))) return r;
+  if ((r = launch_gather(h))) return r;
+  if ((r = launch_time_step_source(h))) return r;
+  if ((r = launch_dt(h, DT_FORCE))) return r;
+  DevTime t;
+  if ((r = read_time(h, &t))) return r;
+  h->hostIncrement = t.increment;
+  h->prologueDone = true;
+  return t.status;
+}
+
+int dnl_step(dnl_handle *h, int nsteps, int *steps_done)
+{
+  if (steps_done) *steps_done = 0;
+  if (!h || nsteps < 0) return DNL_ERR_ARG;
+  int r;
+  if (!h->prologueDone && (r = dnl_prologue(h))) return r;
+  if (nsteps == 0) return 0;
+  const long long inc0 = h->hostIncrement;
+  if ((r = launch_dt(h, DT_PRE))) return r;
+  for (int s = 0; s < nsteps; s++)
+    if ((r = enqueue_step(h, inc0 + s + 1, s == nsteps - 1))) return r;
+  DevTime t;
+  if ((r = read_time(h, &t))) return r;
+  if (steps_done) *steps_done = (int)(t.increment - inc0);
+  h->hostIncrement = t.increment;
+  // if the run ended early, the bank parity followed the launches, not the steps done
+  if (t.increment - inc0 != nsteps) {
+    const long long extra = nsteps - (t.increment - inc0);
+    if (extra % 2) h->cur = 1 - h->cur;
+  }
+  return t.status;
+}
+
+int dnl_run(dnl_handle *h, int *steps_done)
+{
+  if (steps_done) *steps_done = 0;
+  if (!h) return DNL_ERR_ARG;
+  int total = 0, r = 0;
+  for (;;) {
+    int done = 0;
+    r = dnl_step(h, 1000, &done);
+    total += done;
+    if (r) break;
+    DevTime t;
+    if ((r = read_time(h, &t))) break;
+    if (t.done) break;
+  }
+  if (steps_done) *steps_done = total;
+  return r;
+}
+
+int dnl_step_graph(dnl_handle *h, int nsteps, int *steps_done)
+{
+  if (steps_done) *steps_done = 0;
+  if (!h || nsteps <= 0) return DNL_ERR_ARG;
+  int r;
+  if (!h->prologueDone && (r = dnl_prologue(h))) return r;
+  const long long inc0 = h->hostIncrement;
+  const int parity = h->cur, phase = (int)(inc0 % h->freq);
+  cudaGraphExec_t exec = nullptr;
+  for (int i = 0; i < h->ngraphs; i++)
+    if (h->graphs[i].nsteps == nsteps && h->graphs[i].parity == parity && h->graphs[i].phase == phase)
+      exec = h->graphs[i].exec;
+  const int curBefore = h->cur;
+  if (!exec) {
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int rr = launch_dt(h, DT_PRE);
+    for (int s = 0; s < nsteps && !rr; s++) rr = enqueue_step(h, inc0 + s + 1, s == nsteps - 1);
+    cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+    if (rr) return rr;
+    if (ce != cudaSuccess) {
+      snprintf(g_lastError, sizeof g_lastError, "graph capture: %s", cudaGetErrorString(ce));
+      return DNL_ERR_CUDA;
+    }
+    CK(cudaGraphInstantiate(&exec, graph, 0));
+    cudaGraphDestroy(graph);
+    if (h->ngraphs < 8) {
+      h->graphs[h->ngraphs++] = GraphEntry{nsteps, parity, phase, exec};
+    }
+  } else {
+    h->cur = (nsteps % 2) ? 1 - curBefore : curBefore;
+  }
+  CK(cudaGraphLaunch(exec, h->stream));
+  launch_counter() += 0;  // kernel launches inside a graph are counted at capture
+  DevTime t;
+  if ((r = read_time(h, &t))) return r;
+  if (steps_done) *steps_done = (int)(t.increment - inc0);
+  h->hostIncrement = t.increment;
+  if (t.increment - inc0 != nsteps) {
+    const long long extra = nsteps - (t.increment - inc0);
+    if (extra % 2) h->cur = 1 - h->cur;
+  }
+  if (h->ngraphs >= 8) {
+    bool cached = false;
+    for (int i = 0; i < h->ngraphs; i++) cached |= h->graphs[i].exec == exec;
+    if (!cached) cudaGraphExecDestroy(exec);
+  }
+  return t.status;
+}
+
+int dnl_time_step(dnl_handle *h, double *dt)
+{
+  if (!h || !dt) return DNL_ERR_ARG;
+  DevTime t;
+  int r = read_time(h, &t);
+  if (r) return r;
+  *dt = t.timeStep;
+  return 0;
+}
+
+int dnl_get_time_info(dnl_handle *h, dnl_time_info *info)
+{
+  if (!h || !info) return DNL_ERR_ARG;
+  DevTime t;
+  int r = read_time(h, &t);
+  if (r) return r;
+  // kinetic energy of the Current field = the New field of the last step before the swap
+  const int blocks = 64;
+  double *part;
+  CK(cudaMalloc(&part, sizeof(double) * blocks));
+  k_kinetic<<<blocks, 256, 0, h->stream>>>(h->N, h->bank[h->cur], h->mass, part);
+  launch_counter()++;
+  double hp[blocks];
+  CK(cudaMemcpyAsync(hp, part, sizeof hp, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  cudaFree(part);
+  double ke = 0.;
+  for (int b = 0; b < blocks; b++) ke += hp[b];
+  info->time = t.currentTime;
+  info->time_step = t.timeStep;
+  info->computed_step = t.computedTimeStep;
+  info->kinetic = ke;
+  info->increment = t.increment;
+  info->done = t.done;
+  info->status = t.status;
+  info->bad_element = t.badElem;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,422 @@
+"""Python binding of libdnlgpu (include/dnl_gpu.h) over ctypes.
+
+Two layers:
+
+* :class:`GpuDomain` -- one handle of the C ABI for a :class:`redynela_gb300.meshes.Model`:
+  ``internal_forces`` (the ``Domain::computeInternalForces`` drop-in), ``step`` / ``run`` /
+  ``step_graph`` (``ExplicitSolverCH::solve`` on the device), state get/set.
+* :class:`Structure` and friends -- the calls a DynELA ``.dyn`` deck makes
+  (``Structure::createNode``, ``createElement``, ``attachInitialBC``, ``attachConstantBC``,
+  ``ExplicitSolverCH::setTimes`` ..., see Samples/Taylor/Taylor_Axi_Parametric.dyn), building the
+  same model and solving it on the GPU.
+
+The library must be built (``python -m redynela_gb300.build``); there is no CPU fallback: a
+missing library or CUDA device raises.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+from . import meshes
+from .meshes import BCGroup, Model
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libdnlgpu.so")
+
+DNL_OK = 0
+STATUS_NAMES = {
+    1: "DNL_ERR_NEG_DETJ", 2: "DNL_ERR_RR_NOCONV", 3: "DNL_ERR_JACOBI_NOCONV",
+    4: "DNL_ERR_PULSE_NOCONV", 5: "DNL_ERR_DT", 6: "DNL_ERR_ARG", 7: "DNL_ERR_CUDA",
+    8: "DNL_ERR_SINGULAR", 9: "DNL_ERR_TIMEOUT",
+}
+FLAG_STEP_TENSORS = 1
+
+
+class DnlError(RuntimeError):
+    def __init__(self, code: int, msg: str, element: int = -1):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}"
+                         + (f" (element {element})" if element >= 0 else ""))
+        self.code = code
+        self.element = element
+
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("etype", C.c_int), ("num_nodes", C.c_int), ("num_elements", C.c_int),
+                ("coords", _dp), ("conn", _ip), ("v0", C.c_double * 3), ("num_bc", C.c_int),
+                ("bc_kind", _ip), ("bc_val", _dp), ("bc_start", _ip), ("bc_nodes", _ip)]
+
+
+class MaterialDesc(C.Structure):
+    _fields_ = [("young", C.c_double), ("poisson", C.c_double), ("density", C.c_double),
+                ("A", C.c_double), ("B", C.c_double), ("n", C.c_double)]
+
+
+class SolverParams(C.Structure):
+    _fields_ = [("end_time", C.c_double), ("rho_b", C.c_double), ("safety", C.c_double),
+                ("frequency", C.c_int), ("method", C.c_int), ("flags", C.c_int)]
+
+
+class StateView(C.Structure):
+    _fields_ = [(n, _dp) for n in ("coords", "du", "v", "a", "disp", "S", "Eps", "EpsPlas", "p",
+                                   "evp", "Sig", "mass")]
+
+
+class TimeInfo(C.Structure):
+    _fields_ = [("time", C.c_double), ("time_step", C.c_double), ("computed_step", C.c_double),
+                ("kinetic", C.c_double), ("increment", C.c_longlong), ("done", C.c_int),
+                ("status", C.c_int), ("bad_element", C.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libdnlgpu.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} not found: run `python -m redynela_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        H = C.c_void_p
+        L.dnl_create.argtypes = [C.POINTER(MeshDesc), C.POINTER(MaterialDesc),
+                                 C.POINTER(SolverParams), C.POINTER(H)]
+        L.dnl_destroy.argtypes = [H]
+        L.dnl_set_state.argtypes = [H, C.POINTER(StateView)]
+        L.dnl_get_state.argtypes = [H, C.POINTER(StateView)]
+        L.dnl_get_step_tensors.argtypes = [H, _dp, _dp]
+        L.dnl_internal_forces.argtypes = [H, _dp, _dp, C.c_double, _dp]
+        L.dnl_prologue.argtypes = [H]
+        L.dnl_step.argtypes = [H, C.c_int, _ip]
+        L.dnl_run.argtypes = [H, _ip]
+        L.dnl_step_graph.argtypes = [H, C.c_int, _ip]
+        L.dnl_time_step.argtypes = [H, _dp]
+        L.dnl_get_time_info.argtypes = [H, C.POINTER(TimeInfo)]
+        L.dnl_get_fint.argtypes = [H, _dp]
+        L.dnl_error_string.restype = C.c_char_p
+        L.dnl_error_string.argtypes = [C.c_int]
+        L.dnl_device_count.argtypes = [_ip]
+        L.dnl_kernel_launches.restype = C.c_longlong
+        _lib = L
+    return _lib
+
+
+def device_count() -> int:
+    n = C.c_int(0)
+    lib().dnl_device_count(C.byref(n))
+    return n.value
+
+
+def kernel_launches() -> int:
+    return int(lib().dnl_kernel_launches())
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+class GpuDomain:
+    """One mesh on the GPU (a ``dnl_handle``)."""
+
+    def __init__(self, model: Model, flags: int = 0):
+        L = lib()
+        if device_count() < 1:
+            raise RuntimeError("libdnlgpu: no CUDA device")
+        m = model
+        self.model = m
+        self._coords = np.ascontiguousarray(m.coords, dtype=np.float64)
+        self._conn = np.ascontiguousarray(m.conn, dtype=np.int32)
+        kinds = np.array([g.kind for g in m.bcs] or [0], dtype=np.int32)
+        vals = np.array([list(g.val) for g in m.bcs] or [[0.0, 0.0, 0.0]], dtype=np.float64)
+        starts = np.zeros(len(m.bcs) + 1, dtype=np.int32)
+        for i, g in enumerate(m.bcs):
+            starts[i + 1] = starts[i] + len(g.nodes)
+        nodes = (np.concatenate([np.asarray(g.nodes) for g in m.bcs]).astype(np.int32)
+                 if m.bcs else np.zeros(1, dtype=np.int32))
+        self._bc = (kinds, vals, starts, nodes)
+        desc = MeshDesc(m.etype, m.N, m.E, self._coords.ctypes.data_as(_dp),
+                        self._conn.ctypes.data_as(_ip), (C.c_double * 3)(*m.v0), len(m.bcs),
+                        kinds.ctypes.data_as(_ip), vals.ctypes.data_as(_dp),
+                        starts.ctypes.data_as(_ip), nodes.ctypes.data_as(_ip))
+        mat = MaterialDesc(m.young, m.poisson, m.density, m.A, m.B, m.n)
+        sp = SolverParams(m.tend, m.rho_b, m.safety, int(m.freq), int(m.method), int(flags))
+        h = C.c_void_p()
+        self._check(L.dnl_create(C.byref(desc), C.byref(mat), C.byref(sp), C.byref(h)))
+        self.h = h
+        self.L = L
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.dnl_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int, element: int = -1):
+        if rc != DNL_OK:
+            raise DnlError(rc, lib().dnl_error_string(rc).decode(), element)
+
+    def _check_run(self, rc: int):
+        if rc != DNL_OK:
+            info = self.time_info() if rc not in (6, 7) else None
+            self._check(rc, info["bad_element"] if info else -1)
+
+    # ------------------------------------------------------------------ state
+    @property
+    def nip(self) -> int:
+        return self.model.nip
+
+    def set_state(self, **arrays) -> None:
+        keep = {}
+        sv = StateView()
+        for k, v in arrays.items():
+            if v is None:
+                continue
+            a = np.ascontiguousarray(v, dtype=np.float64)
+            keep[k] = a
+            setattr(sv, k, a.ctypes.data_as(_dp))
+        self._check(self.L.dnl_set_state(self.h, C.byref(sv)))
+
+    def get_state(self, *names: str) -> Dict[str, np.ndarray]:
+        m = self.model
+        nI = m.E * m.nip
+        shapes = {"coords": (m.N, 3), "du": (m.N, 3), "v": (m.N, 3), "a": (m.N, 3),
+                  "disp": (m.N, 3), "S": (m.E, m.nip, 3, 3), "Eps": (m.E, m.nip, 3, 3),
+                  "EpsPlas": (m.E, m.nip, 3, 3), "Sig": (m.E, m.nip, 3, 3), "p": (m.E, m.nip),
+                  "evp": (m.E, m.nip), "mass": (m.N,)}
+        names = names or tuple(shapes)
+        out = {n: np.zeros(shapes[n]) for n in names}
+        sv = StateView()
+        for n, a in out.items():
+            setattr(sv, n, a.ctypes.data_as(_dp))
+        self._check(self.L.dnl_get_state(self.h, C.byref(sv)))
+        del nI
+        return out
+
+    def step_tensors(self):
+        m = self.model
+        dE = np.zeros((m.E, m.nip, 3, 3))
+        R = np.zeros((m.E, m.nip, 3, 3))
+        self._check(self.L.dnl_get_step_tensors(self.h, _ptr(dE), _ptr(R)))
+        return dE, R
+
+    def fint(self) -> np.ndarray:
+        out = np.zeros(self.model.N * self.model.dim)
+        self._check(self.L.dnl_get_fint(self.h, _ptr(out)))
+        return out
+
+    # ------------------------------------------------------------------ compute
+    def internal_forces(self, coords=None, du=None, dt: float = 0.0) -> np.ndarray:
+        """Domain::computeInternalForces drop-in; returns Fint (dim*N, index Id*dim+j)."""
+        c = np.ascontiguousarray(coords, dtype=np.float64) if coords is not None else None
+        d = np.ascontiguousarray(du, dtype=np.float64) if du is not None else None
+        out = np.zeros(self.model.N * self.model.dim)
+        self._check_run(self.L.dnl_internal_forces(self.h, _ptr(c), _ptr(d), float(dt), _ptr(out)))
+        return out
+
+    def prologue(self) -> None:
+        self._check_run(self.L.dnl_prologue(self.h))
+
+    def step(self, n: int = 1) -> int:
+        done = C.c_int(0)
+        self._check_run(self.L.dnl_step(self.h, int(n), C.byref(done)))
+        return done.value
+
+    def step_graph(self, n: int) -> int:
+        done = C.c_int(0)
+        self._check_run(self.L.dnl_step_graph(self.h, int(n), C.byref(done)))
+        return done.value
+
+    def run(self) -> int:
+        done = C.c_int(0)
+        self._check_run(self.L.dnl_run(self.h, C.byref(done)))
+        return done.value
+
+    def time_step(self) -> float:
+        dt = C.c_double(0)
+        self._check(self.L.dnl_time_step(self.h, C.byref(dt)))
+        return dt.value
+
+    def time_info(self) -> dict:
+        t = TimeInfo()
+        self._check(self.L.dnl_get_time_info(self.h, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in TimeInfo._fields_}
+
+
+# ====================================================================== deck-level mirror
+class Material:
+    """Material (finiteElement/Material.h:61-156): setYoung, setPoisson, setDensity, setHardening."""
+
+    def __init__(self):
+        self.young = 0.0
+        self.poisson = 0.0
+        self.density = 0.0
+        self.hardening = None
+
+    def setYoung(self, v):
+        self.young = float(v)
+
+    def setPoisson(self, v):
+        self.poisson = float(v)
+
+    def setDensity(self, v):
+        self.density = float(v)
+
+    def setHardening(self, h):
+        self.hardening = h
+
+
+class IsoHardElastoplastic:
+    """sigma_y = A + B evp^n (finiteElement/IsoHardElastoplastic.C:171-184)."""
+
+    def __init__(self):
+        self.A = self.B = 0.0
+        self.n = 1.0
+
+    def setYieldStress(self, v):
+        self.A = float(v)
+
+    def setHardParameter(self, v):
+        self.B = float(v)
+
+    def setHardExponent(self, v):
+        self.n = float(v)
+
+
+class NodeSet:
+    def __init__(self):
+        self.numbers: List[int] = []
+
+    def add(self, start, stop=None, inc=1):
+        """NodeSet::add(num) or add(start, stop, inc) with 1-based inclusive numbers."""
+        if stop is None:
+            self.numbers.append(int(start))
+        else:
+            self.numbers.extend(range(int(start), int(stop) + 1, int(inc)))
+
+
+class ElementSet(NodeSet):
+    pass
+
+
+class BoundarySpeed:
+    def __init__(self):
+        self.val = (0.0, 0.0, 0.0)
+
+    def set(self, x, y, z):
+        self.val = (float(x), float(y), float(z))
+
+
+class BoundaryRestrain(BoundarySpeed):
+    pass
+
+
+class ExplicitSolverCH:
+    """ExplicitSolverCH settings (finiteElement/ExplicitSolverCH.C, Solver.C)."""
+
+    def __init__(self):
+        self.start, self.end = 0.0, 0.0
+        self.rho_b = 0.8182
+        self.safety = 0.9
+        self.frequency = 10
+        self.method = meshes.PULSE  # the ExplicitSolverCH constructor's default
+
+    def setTimes(self, start, stop):
+        self.start, self.end = float(start), float(stop)
+
+    def setDissipation(self, v):
+        if not 0.0 <= v <= 1.0:
+            raise ValueError("dissipation value out of range [0.0, 1.0]")
+        self.rho_b = float(v)
+
+    def setTimeStepSafetyFactor(self, v):
+        self.safety = float(v)
+
+    def setComputeTimeStepFrequency(self, v):
+        self.frequency = int(v)
+
+    def setTimeStepMethod(self, name):
+        self.method = {"Courant": meshes.COURANT, "Pulse": meshes.PULSE}[name]
+
+
+ElQua4nAx = meshes.ELQUA4NAX
+ElHex8n3D = meshes.ELHEX8N3D
+
+
+class Structure:
+    """The model-building calls of a .dyn deck (finiteElement/Structure.h), solved on the GPU."""
+
+    def __init__(self):
+        self._nodes: Dict[int, Sequence[float]] = {}
+        self._elements: Dict[int, Sequence[int]] = {}
+        self._etype = None
+        self._material = None
+        self._initial = []
+        self._constant = []
+        self._solver = None
+        self.domain: Optional[GpuDomain] = None
+
+    def createNode(self, num, x, y, z):
+        self._nodes[int(num)] = (float(x), float(y), float(z))
+
+    def setDefaultElement(self, etype):
+        self._etype = etype
+
+    def createElement(self, num, *nodes):
+        self._elements[int(num)] = tuple(int(n) for n in nodes)
+
+    def addMaterial(self, mat):
+        self._material = mat
+
+    def attachMaterialToElements(self, mat, els):
+        self._material = mat
+
+    def attachInitialBC(self, bnd, nodes):
+        self._initial.append((bnd, nodes))
+
+    def attachConstantBC(self, bnd, nodes):
+        self._constant.append((bnd, nodes))
+
+    def addSolver(self, solver):
+        self._solver = solver
+
+    def setSaveTimes(self, start, stop, interval):
+        pass
+
+    def model(self) -> Model:
+        nums = sorted(self._nodes)
+        index = {n: i for i, n in enumerate(nums)}
+        coords = np.array([self._nodes[n] for n in nums], dtype=np.float64)
+        conn = np.array([[index[n] for n in self._elements[e]] for e in sorted(self._elements)],
+                        dtype=np.int64)
+        v0 = (0.0, 0.0, 0.0)
+        for bnd, ns in self._initial:
+            v0 = bnd.val
+        bcs = []
+        for bnd, ns in self._constant:
+            kind = meshes.RESTRAIN if isinstance(bnd, BoundaryRestrain) else meshes.SPEED
+            bcs.append(BCGroup(kind, bnd.val, np.array([index[n] for n in ns.numbers])))
+        mat, hard, s = self._material, self._material.hardening, self._solver
+        return Model(self._etype, coords, conn, mat.young, mat.poisson, mat.density, hard.A,
+                     hard.B, hard.n, v0, bcs, s.end, s.rho_b, s.safety, s.frequency, s.method)
+
+    def initSolve(self, flags: int = 0) -> GpuDomain:
+        self.domain = GpuDomain(self.model(), flags)
+        return self.domain
+
+    def solve(self) -> int:
+        if self.domain is None:
+            self.initSolve()
+        return self.domain.run()

@@ -1,0 +1,70 @@
+"""Regenerate the golden fixtures of tests/golden from the compiled reference.
+
+Needs the reference DynELA numerical core built by ``make -C oracle ref`` (it compiles the
+reference sources where they lie; only possible where those sources exist).  Every fixture is the
+reference's own output on a seeded synthetic model:
+
+* ``tables.npz``        element tables of ElQua4nAx / ElHex8n3D
+* ``forces_axi.npz``    one Domain::computeInternalForces on an injected mid-run state, 3x4 axi bar
+* ``forces_hex.npz``    the same on a 4x4x3 hex bar
+* ``steps_c0.npz``      the 5x50 Taylor bar, first 20 steps: Fint, dt, kinetic energy per step
+* ``run_c0.npz``        the 5x50 Taylor bar to 80 us: final coordinates, plastic strain, pressure
+* ``steps_hex.npz``     a 6x6x8 hex bar with the Pulse time step, first 30 steps
+
+    python tests/golden/make_golden.py
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import dnl_io, states  # noqa: E402
+from redynela_gb300 import meshes  # noqa: E402
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name)
+    np.savez_compressed(path, **arrays)
+    print(f"{name}: {os.path.getsize(path)} bytes")
+
+
+def main():
+    if not dnl_io.reference_available():
+        sys.exit("compiled reference missing: run `make -C oracle ref`")
+    t = dnl_io.reference_tables()
+    save("tables.npz", **t)
+
+    for name, m in (("forces_axi.npz", meshes.taylor_axi(3, 4)),
+                    ("forces_hex.npz", meshes.taylor_hex(4, 3))):
+        st = states.random_state(m, seed=7)
+        r = dnl_io.run_reference("forces", m, state=st)
+        save(name, **{f"in_{k}": np.asarray(v) for k, v in st.items()}, fint=r["fint"],
+             **{k: r[k] for k in r if k.startswith("out_")})
+
+    m = meshes.taylor_axi(5, 50)
+    r = dnl_io.run_reference("steps", m, 20)
+    save("steps_c0.npz", mass=r["mass"], dt0=r["dt0"], dt=r["dt"], time=r["time"],
+         kinetic=r["kinetic"], fint=np.stack([r[f"fint_{k:06d}"] for k in range(20)]),
+         final_coords=r["final_coords"], final_evp=r["final_evp"], final_p=r["final_p"])
+
+    r = dnl_io.run_reference("run", m)
+    save("run_c0.npz", increments=r["increments"], time=r["time"], final_coords=r["final_coords"],
+         final_evp=r["final_evp"], final_p=r["final_p"], final_S=r["final_S"],
+         final_v=r["final_v"])
+
+    m = meshes.taylor_hex(6, 8)
+    r = dnl_io.run_reference("steps", m, 30)
+    save("steps_hex.npz", mass=r["mass"], dt0=r["dt0"], dt=r["dt"], time=r["time"],
+         kinetic=r["kinetic"], fint=np.stack([r[f"fint_{k:06d}"] for k in range(30)]),
+         final_coords=r["final_coords"])
+
+
+if __name__ == "__main__":
+    main()

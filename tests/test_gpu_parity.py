@@ -1,0 +1,153 @@
+"""Parity of the CUDA path (through the C ABI) with the reference outputs (tests/golden) and the
+oracle.  Tolerances, from the specification of this path:
+
+* nodal internal forces of one step from the same state: relative 2-norm error <= 1e-12
+* integration-point state after that step: relative 2-norm error <= 1e-12 per field
+* final nodal positions after a full run: max |dx| / max |x| <= 1e-6
+"""
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import states
+from oracle.oracle import Oracle
+from redynela_gb300 import meshes
+
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL = 1e-12
+STATE_TOL = 1e-12
+POS_TOL = 1e-6
+
+
+def rel(a, b):
+    a, b = np.asarray(a).ravel(), np.asarray(b).ravel()
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / nb if nb > 0 else np.linalg.norm(a - b)
+
+
+def _state_from_golden(g):
+    return {k[3:]: g[k] for k in g.files if k.startswith("in_")}
+
+
+@pytest.mark.parametrize("name,model", [("forces_axi.npz", lambda: meshes.taylor_axi(3, 4)),
+                                        ("forces_hex.npz", lambda: meshes.taylor_hex(4, 3))])
+def test_internal_forces_injected_state(gpu_lib, name, model):
+    """dnl_internal_forces on a mid-run state vs the reference's Domain::computeInternalForces."""
+    g = golden(name)
+    m = model()
+    d = gpu_lib.GpuDomain(m, flags=gpu_lib.FLAG_STEP_TENSORS)
+    st = _state_from_golden(g)
+    d.set_state(S=st["S"], Eps=st["Eps"], EpsPlas=st["EpsPlas"], p=st["p"], evp=st["evp"],
+                v=st["v"], a=st["a"], disp=st["disp"])
+    f = d.internal_forces(coords=st["coords"], du=st["du"], dt=float(st["dt"]))
+    assert rel(f, g["fint"]) <= FORCE_TOL
+    out = d.get_state("S", "Eps", "EpsPlas", "p", "evp", "Sig")
+    for k in ("S", "Eps", "EpsPlas", "p", "evp", "Sig"):
+        assert rel(out[k], g["out_" + k]) <= STATE_TOL, k
+    dE, R = d.step_tensors()
+    assert rel(dE, g["out_dEps"]) <= STATE_TOL
+    assert rel(R, g["out_R"]) <= STATE_TOL
+
+
+@pytest.mark.parametrize("etype,seed", [(0, 11), (1, 12), (0, 13), (1, 14)])
+def test_internal_forces_random_states_vs_oracle(gpu_lib, etype, seed):
+    m = meshes.taylor_axi(12, 40) if etype == 0 else meshes.taylor_hex(10, 12)
+    st = states.random_state(m, seed=seed)
+    o = Oracle(m)
+    o.inject(**st)
+    o.internal_matrices()
+    fo = o.internal_forces()
+    d = gpu_lib.GpuDomain(m)
+    d.set_state(S=st["S"], Eps=st["Eps"], EpsPlas=st["EpsPlas"], p=st["p"], evp=st["evp"])
+    f = d.internal_forces(coords=st["coords"], du=st["du"], dt=st["dt"])
+    assert rel(f, fo) <= FORCE_TOL
+    out = d.get_state("S", "EpsPlas", "evp", "p")
+    for k in out:
+        assert rel(out[k], o.array(k)) <= STATE_TOL, k
+
+
+def test_steps_c0_per_step_forces(gpu_lib):
+    """The 5x50 Taylor bar: each of the first 20 steps' Fint, dt and kinetic energy."""
+    g = golden("steps_c0.npz")
+    d = gpu_lib.GpuDomain(meshes.taylor_axi(5, 50))
+    d.prologue()
+    assert rel(d.get_state("mass")["mass"], g["mass"][::2]) == 0.0
+    assert d.time_step() == g["dt0"][0]
+    for k in range(20):
+        assert d.step(1) == 1
+        f = d.fint()
+        r = g["fint"][k]
+        if np.linalg.norm(r) > 0:
+            assert rel(f, r) <= FORCE_TOL, k
+        info = d.time_info()
+        assert abs(info["time"] - g["time"][k]) <= 1e-15 * g["time"][k]
+        assert abs(info["kinetic"] - g["kinetic"][k]) <= 1e-12 * g["kinetic"][k]
+
+
+def test_full_run_c0_final_positions(gpu_lib):
+    """5x50 Taylor impact to 80 us: final positions within 1e-6 of the reference."""
+    g = golden("run_c0.npz")
+    d = gpu_lib.GpuDomain(meshes.taylor_axi(5, 50))
+    n = d.run()
+    info = d.time_info()
+    assert info["done"] == 1 and info["status"] == 0
+    assert abs(n - int(g["increments"][0])) <= 2
+    x = d.get_state("coords")["coords"].ravel()
+    ref = g["final_coords"]
+    err = np.max(np.abs(x - ref)) / np.max(np.abs(ref))
+    assert err <= POS_TOL, err
+    evp = d.get_state("evp")["evp"].ravel()
+    assert rel(evp, g["final_evp"]) <= 1e-6
+
+
+def test_runs_are_bitwise_deterministic(gpu_lib):
+    m = meshes.taylor_axi(10, 100)
+    out = []
+    for _ in range(2):
+        d = gpu_lib.GpuDomain(m)
+        d.step(300)
+        out.append((d.get_state("coords")["coords"], d.fint()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_graph_replay_equals_stream_steps(gpu_lib):
+    m = meshes.taylor_axi(8, 60)
+    a = gpu_lib.GpuDomain(m)
+    a.step(60)
+    b = gpu_lib.GpuDomain(m)
+    b.prologue()
+    for _ in range(3):
+        assert b.step_graph(20) == 20
+    assert np.array_equal(a.get_state("coords")["coords"], b.get_state("coords")["coords"])
+    assert a.time_info()["time"] == b.time_info()["time"]
+
+
+def test_multi_step_vs_oracle_taylor_fine(gpu_lib):
+    """A finer axi bar (20x200) for 200 steps: positions and plastic strain vs the oracle."""
+    m = meshes.taylor_axi(20, 200)
+    o = Oracle(m)
+    o.prologue()
+    o.steps(200)
+    d = gpu_lib.GpuDomain(m)
+    assert d.step(200) == 200
+    x = d.get_state("coords")["coords"].ravel()
+    assert np.max(np.abs(x - o.array("coords"))) <= 1e-12 * np.max(np.abs(o.array("coords")))
+    assert rel(d.fint(), o.array("fint")) <= 1e-10
+
+
+def test_negative_jacobian_is_reported(gpu_lib):
+    """An inverted element gives DNL_ERR_NEG_DETJ with its index; the context stays usable."""
+    m = meshes.taylor_axi(3, 3)
+    d = gpu_lib.GpuDomain(m)
+    x = m.coords.copy()
+    e = 4
+    n0, n2 = m.conn[e, 0], m.conn[e, 2]
+    x[[n0, n2]] = x[[n2, n0]]
+    with pytest.raises(gpu_lib.DnlError) as ei:
+        d.internal_forces(coords=x, du=np.zeros((m.N, 3)))
+    assert ei.value.code == 1
+    f = d.internal_forces(coords=m.coords, du=np.zeros((m.N, 3)))
+    assert np.all(np.isfinite(f))

@@ -1,0 +1,178 @@
+"""The oracle (oracle/dnl_oracle.c) against the reference's own outputs (tests/golden, generated by
+tests/golden/make_golden.py from the compiled reference) and against known answers.  CPU only."""
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import oracle as orc
+from oracle.oracle import Oracle
+from redynela_gb300 import meshes
+
+
+def _inject(o, g):
+    o.inject(**{k[3:]: (g[k] if k != "in_dt" else float(g[k])) for k in g.files if k.startswith("in_")})
+
+
+def test_tables_match_reference():
+    g = golden("tables.npz")
+    for et, nm in ((0, "axi"), (1, "hex")):
+        N, dN = orc.tables(et)
+        assert np.array_equal(N.ravel(), g[nm + "_N"])
+        assert np.array_equal(dN.ravel(), g[nm + "_dN"])
+        assert np.all(g[nm + "_weight"] == 1.0)
+
+
+@pytest.mark.parametrize("name,model", [("forces_axi.npz", lambda: meshes.taylor_axi(3, 4)),
+                                        ("forces_hex.npz", lambda: meshes.taylor_hex(4, 3))])
+def test_internal_forces_bit_exact(name, model):
+    """One Domain::computeInternalForces on an injected mid-run state: bit for bit."""
+    g = golden(name)
+    m = model()
+    o = Oracle(m)
+    _inject(o, g)
+    o.internal_matrices()
+    f = o.internal_forces()
+    assert np.array_equal(f, g["fint"])
+    for k in ("S", "Eps", "EpsPlas", "p", "evp", "Sig", "dEps", "R"):
+        assert np.array_equal(o.array(k), g["out_" + k]), k
+    # the state exercises both branches of the radial return
+    assert np.any(o.array("evp") != g["in_evp"].ravel())
+    assert np.any(o.array("evp") == g["in_evp"].ravel())
+
+
+def test_steps_c0_bit_exact():
+    g = golden("steps_c0.npz")
+    o = Oracle(meshes.taylor_axi(5, 50))
+    o.prologue()
+    assert np.array_equal(o.array("Mass"), g["mass"])
+    assert o.get("dt") == g["dt0"][0]
+    for k in range(20):
+        assert o.get("dt") == g["dt"][k] or k == 0
+        o.steps(1)
+        assert np.array_equal(o.array("fint"), g["fint"][k]), k
+        assert o.get("kinetic_current") == g["kinetic"][k]
+        assert o.get("time") == g["time"][k]
+    assert np.array_equal(o.array("coords"), g["final_coords"])
+
+
+def test_run_c0_bit_exact():
+    """The full 5x50 Taylor run to 80 us (9722 increments) reproduces the reference bit for bit."""
+    g = golden("run_c0.npz")
+    o = Oracle(meshes.taylor_axi(5, 50))
+    o.prologue()
+    n = o.steps(10 ** 9)
+    assert n == int(g["increments"][0])
+    assert o.get("time") == g["time"][0]
+    assert np.array_equal(o.array("coords"), g["final_coords"])
+    assert np.array_equal(o.array("evp"), g["final_evp"])
+    assert np.array_equal(o.array("S"), g["final_S"])
+
+
+def test_steps_hex_pulse():
+    """Hex8 with the Pulse time step: the power iteration sums K.x in element order where the
+    reference uses its Jobs order, so agreement is to rounding, not bitwise."""
+    g = golden("steps_hex.npz")
+    o = Oracle(meshes.taylor_hex(6, 8))
+    o.prologue()
+    assert np.array_equal(o.array("Mass"), g["mass"])
+    assert abs(o.get("dt") - g["dt0"][0]) <= 1e-14 * g["dt0"][0]
+    for k in range(30):
+        o.steps(1)
+        f, r = o.array("fint"), g["fint"][k]
+        if np.linalg.norm(r) > 0:
+            assert np.linalg.norm(f - r) <= 1e-12 * np.linalg.norm(r), k
+    x = o.array("coords")
+    assert np.max(np.abs(x - g["final_coords"])) <= 1e-12 * np.max(np.abs(g["final_coords"]))
+
+
+# ---------------------------------------------------------------------- known answers
+def test_chung_hulbert_parameters():
+    o = Oracle(meshes.taylor_axi(2, 2))
+    assert abs(o.get("alphaM") - 0.350016) < 1e-6
+    assert abs(o.get("beta") - 0.651521) < 1e-6
+    assert abs(o.get("gamma") - 1.149984) < 1e-6
+    assert abs(o.get("omegaS") - 1.981819) < 1e-6
+
+
+def test_total_mass_axisymmetric():
+    """sum of lumped masses = rho * integral of 2 pi r dA = rho pi R^2 L for the undeformed bar."""
+    m = meshes.taylor_axi(5, 50)
+    o = Oracle(m)
+    o.prologue()
+    total = o.array("mass").sum()
+    exact = m.density * np.pi * 3.2e-3 ** 2 * 32.4e-3
+    assert abs(total - exact) <= 1e-12 * exact
+
+
+def test_total_mass_hex():
+    m = meshes.taylor_hex(8, 4)
+    o = Oracle(m)
+    o.prologue()
+    vol = 0.0
+    x = m.coords[m.conn]
+    for e in range(m.E):
+        ext = x[e].max(axis=0) - x[e].min(axis=0)
+        vol += np.prod(ext)
+    assert abs(o.array("mass").sum() - m.density * vol) <= 1e-10 * m.density * vol
+
+
+def _single_element(F_disp, etype=0):
+    """One element, zero state, Current delta_disp = F_disp applied to the nodes."""
+    m = meshes.taylor_axi(1, 1) if etype == 0 else meshes.taylor_hex(1, 1)
+    m.bcs = []
+    o = Oracle(m)
+    x = m.coords.copy()
+    x[:, 0] += 1e-3  # keep the axisymmetric element off the axis
+    du = np.zeros((m.N, 3))
+    du[:, :m.dim] = F_disp(x)[:, :m.dim]
+    o.inject(coords=x, du=du, v=np.zeros_like(du), a=np.zeros_like(du), disp=np.zeros_like(du),
+             S=np.zeros((m.E, m.nip, 3, 3)), Eps=np.zeros((m.E, m.nip, 3, 3)),
+             EpsPlas=np.zeros((m.E, m.nip, 3, 3)), p=np.zeros((m.E, m.nip)),
+             evp=np.full((m.E, m.nip), 1e-10), dt=1e-8)
+    o.internal_matrices()
+    o.internal_forces()
+    return o, m
+
+
+def test_zero_increment_gives_zero_strain_identity_rotation():
+    o, m = _single_element(lambda x: np.zeros_like(x), etype=1)
+    assert np.all(o.array("dEps") == 0.0)
+    R = o.array("R").reshape(-1, 3, 3)
+    assert np.all(R == np.eye(3))
+
+
+def test_rigid_rotation_gives_no_strain():
+    """delta_u = (Q - I) x: F = Q, so ln U = 0 and R = Q (3D hex)."""
+    th = 0.3
+    Q = np.array([[np.cos(th), -np.sin(th), 0], [np.sin(th), np.cos(th), 0], [0, 0, 1.0]])
+    o, m = _single_element(lambda x: x @ (Q - np.eye(3)).T, etype=1)
+    assert np.max(np.abs(o.array("dEps"))) < 1e-12
+    R = o.array("R").reshape(-1, 3, 3)
+    assert np.max(np.abs(R - Q)) < 1e-12
+
+
+def test_uniaxial_elastic_increment_is_hooke():
+    """A small uniaxial stretch in z (hex): S = 2G dev(eps), p = K tr(eps), with eps = ln(1+e)."""
+    e = 1e-5
+    o, m = _single_element(lambda x: np.stack([0 * x[:, 0], 0 * x[:, 1], e * x[:, 2]], 1), etype=1)
+    E, nu = m.young, m.poisson
+    G, K = E / (2 * (1 + nu)), E / (3 * (1 - 2 * nu))
+    eps = np.log1p(e)
+    S = o.array("S").reshape(-1, 3, 3)
+    p = o.array("p")
+    assert np.allclose(S[:, 2, 2], 2 * G * (eps - eps / 3), rtol=1e-9)
+    assert np.allclose(S[:, 0, 0], 2 * G * (-eps / 3), rtol=1e-9)
+    assert np.allclose(p, K * eps, rtol=1e-9)
+
+
+def test_plastic_step_returns_to_yield_surface():
+    """After a plastic correction the J2 stress equals sigma_y(evp) within the Newton tolerance."""
+    e = 2e-2
+    o, m = _single_element(lambda x: np.stack([0 * x[:, 0], 0 * x[:, 1], e * x[:, 2]], 1), etype=1)
+    S = o.array("S").reshape(-1, 3, 3)
+    evp = o.array("evp")
+    j2 = np.sqrt(1.5 * np.sum(S * S, axis=(1, 2)))
+    sy = m.A + m.B * evp ** m.n
+    assert np.all(evp > 1e-10)
+    assert np.all(np.abs(j2 - sy) <= 1e-8 * sy)
