@@ -1,0 +1,316 @@
+#!/usr/bin/env python3
+"""Element-updates/s of DynELA's explicit step on GB300 (libdnlgpu, FP64).
+
+Workload (default): the 3D Taylor impact bar of ElHex8n3D -- a 40x40 cross-section grid clipped
+to the radius, 400 layers (505,600 elements, 538,137 nodes), copper J2 material
+(A 90 MPa, B 292 MPa, n 0.31), impact speed 227 m/s, Chung-Hulbert explicit integration with the
+Pulse critical time step.  A step is one full explicit increment: element pass (kinematics, polar
+decomposition, radial return, forces), CSR assembly, nodal update and the time-step logic
+(Pulse power iteration every 10 increments).  An element-update is one element through one step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config hex|axi]
+
+`value` is measured with device-resident state (CUDA events on the library's stream);
+`e2e` goes through the C ABI with page-locked host buffers: each step uploads the nodal state the
+caller owns (coordinates, delta_disp, velocity, acceleration, displacement), advances one step and
+reads it back.  The reference arm (--impl reference) times the oracle's CPU restatement of the
+reference (oracle/dnl_oracle.c, OpenMP on all host cores) on a bounded slice of the same bar.
+Multi-GPU: independent replicas, one per rank (the explicit step has no cross-replica exchange).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from redynela_gb300 import meshes  # noqa: E402
+
+# dram__bytes_read.sum + dram__bytes_write.sum per k_elem launch from the ncu capture summarised in
+# profiles/ (k_elem on the 40x40x40 slice, scaled by elements to the full bar); None until captured
+ELEM_TRAFFIC_BYTES_PER_ELEMENT = None
+
+
+def workload(name: str, layers: int = 400):
+    if name == "hex":
+        return meshes.taylor_hex(40, layers), f"taylor_hex_40x40x{layers}"
+    if name == "axi":
+        return meshes.taylor_axi(20, 200), "taylor_axi_20x200"
+    raise SystemExit(f"unknown config {name}")
+
+
+def cpu_sample(name: str, layers: int = 400):
+    """CPU sample: the same bar, timed over a bounded number of steps after its prologue."""
+    m, wname = workload(name, layers)
+    return m, f"{wname} ({m.E:,} elements)"
+
+
+def elem_bytes(m) -> float:
+    """Compulsory HBM bytes of one k_elem launch: integration-point state read (S, Eps, EpsPlas, p,
+    evp, evp^n) and written (S, Eps, EpsPlas, p; evp and evp^n only where plastic, not counted),
+    connectivity, element forces written, node coordinates and delta_disp read once."""
+    ns = 4 if m.etype == meshes.ELQUA4NAX else 6
+    ncomp = 3 * ns + 3
+    per_elem = m.nip * (ncomp * 8 + (3 * ns + 1) * 8) + m.nen * 4 + m.nen * m.dim * 8
+    return m.E * per_elem + m.N * 2 * m.dim * 8
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        if self.path and os.path.exists(self.path):
+            for ln in open(self.path):
+                parts = [p.strip() for p in ln.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        load = [s for s in sm if mx and s > 0.3 * max(mx)] or sm
+        return {"sm_mhz": float(np.median(load)) if load else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def barrier_and_max(value: float, world: int) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_cpu_baseline(model, sample_desc, min_seconds=10.0, max_steps=400, threads=None):
+    from oracle.oracle import Oracle
+    threads = threads or os.cpu_count() or 1
+    o = Oracle(model, threads=threads)
+    o.prologue()
+    o.steps(2)  # warm-up
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < max_steps:
+        steps += o.steps(1)
+        if time.perf_counter() - t0 >= min_seconds:
+            break
+    dt = time.perf_counter() - t0
+    rate = model.E * steps / dt
+    return {"value": rate, "unit": "element-updates/s", "cores": threads, "kind": "port",
+            "sample": f"{sample_desc}, {steps} explicit steps after the prologue, {dt:.1f} s"}
+
+
+def main_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    model, sample = cpu_sample(args.config, args.layers)
+    from oracle.oracle import Oracle
+    threads = os.cpu_count() or 1
+    o = Oracle(model, threads=threads)
+    o.prologue()
+    if args.warmup:
+        o.steps(args.warmup)
+    t0 = time.perf_counter()
+    done = o.steps(args.steps)
+    dt = time.perf_counter() - t0
+    rate = model.E * done / dt
+    name = workload(args.config, args.layers)[1]
+    line = {"impl": "reference", "metric": "element-updates/s", "value": rate,
+            "unit": "element-updates/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(done, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": name, "sample": sample},
+            "cpu_baseline": {"value": rate, "unit": "element-updates/s", "cores": threads,
+                             "kind": "port",
+                             "sample": f"{sample}; the oracle's C restatement of the reference "
+                                       "(the reference's own build needs its sources, absent on "
+                                       "this host)"},
+            "e2e": {"value": rate, "unit": "element-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main_ours(args):
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    from redynela_gb300 import build, dynela
+    build.build()
+    dynela.set_device(local)
+    model, name = workload(args.config, args.layers)
+
+    d = dynela.GpuDomain(model)
+    d.prologue()
+    launches0 = dynela.kernel_launches()
+    d.step(args.warmup)
+
+    # ---- device-resident timed region
+    barrier(world)
+    with ClockSampler(local) as clk:
+        launches0 = dynela.kernel_launches()
+        d.profile_begin()
+        d.timer_mark(0)
+        done = d.step(args.steps)
+        d.timer_mark(1)
+        ms = d.timer_elapsed_ms(0, 1)
+        prof = d.profile_end()
+        launches = dynela.kernel_launches() - launches0
+    clocks = clk.summary()
+    barrier(world)
+    ms_max = barrier_and_max(ms, world)
+    value = world * model.E * done / (ms_max * 1e-3)
+
+    # ---- roofline of the dominant kernel (k_elem)
+    elem_ms, elem_n = prof["elem"]
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    bytes_per_launch = elem_bytes(model)
+    achieved = bytes_per_launch / (elem_ms / elem_n * 1e-3) / 1e9 if elem_n else None
+    traffic = (ELEM_TRAFFIC_BYTES_PER_ELEMENT * model.E) if ELEM_TRAFFIC_BYTES_PER_ELEMENT else None
+    fp64_peak = dynela.fp64_peak_tflops()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak if achieved else None, "traffic": traffic,
+                "kernel": "k_elem<ElHex8n3D>" if model.etype else "k_elem<ElQua4nAx>",
+                "peak_source": peak_src,
+                "algorithmic_bytes_per_launch": bytes_per_launch,
+                "avg_launch_ms": elem_ms / elem_n if elem_n else None,
+                "fp64_dfma_peak_tflops_measured": fp64_peak,
+                "note": "the element pass is FP64-pipe bound on GB300; see profiles/"}
+    kernel_share = {k: round(v[0] / ms, 4) for k, v in prof.items() if v[1]}
+
+    # ---- end to end through the C ABI with page-locked host buffers
+    e2e_steps = min(args.steps, 20)
+    N = model.N
+    host = {k: dynela.PinnedArray((N, 3)) for k in ("coords", "du", "v", "a", "disp")}
+    st = d.get_state(*host.keys())
+    for k, pa in host.items():
+        pa.array[:] = st[k]
+    d.timer_mark(2)
+    e2e_done = 0
+    for _ in range(e2e_steps):
+        d.set_state(**{k: pa.array for k, pa in host.items()})
+        e2e_done += d.step(1)
+        out = {k: pa.array for k, pa in host.items()}
+        sv = dynela.StateView()
+        for k, a in out.items():
+            setattr(sv, k, a.ctypes.data_as(dynela._dp))
+        d._check(d.L.dnl_get_state(d.h, dynela.C.byref(sv)))
+    d.timer_mark(3)
+    e2e_ms = d.timer_elapsed_ms(2, 3)
+    e2e_ms = barrier_and_max(e2e_ms, world)
+    nodal_bytes = 5 * N * 3 * 8
+    e2e = {"value": world * model.E * e2e_done / (e2e_ms * 1e-3), "unit": "element-updates/s",
+           "h2d_bytes_per_step": nodal_bytes, "d2h_bytes_per_step": nodal_bytes,
+           "steps": e2e_done, "path": "dnl_set_state + dnl_step(1) + dnl_get_state per step"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cm, sample = cpu_sample(args.config, args.layers)
+        cpu = run_cpu_baseline(cm, sample, min_seconds=args.cpu_seconds)
+
+    if rank == 0:
+        line = {"metric": "element-updates/s", "value": value, "unit": "element-updates/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ms_max / max(done, 1), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded generator of the reference Taylor deck's geometry)",
+                "config": {"workload": name, "elements": model.E, "nodes": model.N,
+                           "time_step": "Pulse every 10 increments",
+                           "l2": "inputs larger than L2 (integration-point state "
+                                 f"{model.E * model.nip * (3 * (4 if model.etype == 0 else 6) + 3) * 8 / 1e6:.0f} MB)",
+                           "parallelism": f"replicas x{world}"},
+                "gpu_launches": launches, "kernel_time_share": kernel_share,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
+        print(json.dumps(line), flush=True)
+    d.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="hex", choices=["hex", "axi"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--layers", type=int, default=400,
+                    help="axial layers of the hex bar (400 = the benchmark workload; fewer for "
+                         "profiling captures)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        main_reference(args)
+    else:
+        main_ours(args)
+
+
+if __name__ == "__main__":
+    main()

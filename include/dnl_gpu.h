@@ -146,14 +146,43 @@ int dnl_prologue(dnl_handle *h);
 int dnl_step(dnl_handle *h, int nsteps, int *steps_done);
 /* the whole run to end_time */
 int dnl_run(dnl_handle *h, int *steps_done);
-/* nsteps steps captured once into a CUDA graph and replayed (same results as dnl_step) */
+/* nsteps steps captured once into a CUDA graph and replayed (same results as dnl_step);
+ * Courant time step only (the Pulse power iteration checks convergence on the host) */
 int dnl_step_graph(dnl_handle *h, int nsteps, int *steps_done);
 int dnl_time_step(dnl_handle *h, double *dt);
 int dnl_get_time_info(dnl_handle *h, dnl_time_info *info);
 /* nodal internal forces of the last element pass, dim*N */
 int dnl_get_fint(dnl_handle *h, double *fint);
 
+/* -------------------------------------------------------------------------- measurement */
+/* Per-kernel device time: between dnl_profile_begin and dnl_profile_end the library brackets each
+ * of its launches on the handle's stream with CUDA events; dnl_profile_end synchronises and returns
+ * the summed milliseconds and launch counts per kernel class. */
+#define DNL_PROF_ELEM 0    /* k_elem: element pass (kinematics, stress, forces) */
+#define DNL_PROF_NODE 1    /* k_node / k_gather: assembly and nodal update */
+#define DNL_PROF_PULSE 2   /* Pulse power-iteration kernels */
+#define DNL_PROF_COURANT 3 /* Courant length reduction */
+#define DNL_PROF_OTHER 4   /* time-step logic, boundary conditions */
+#define DNL_PROF_KINDS 5
+int dnl_profile_begin(dnl_handle *h);
+int dnl_profile_end(dnl_handle *h, double *ms, long long *launches);
+/* the handle's CUDA stream (a cudaStream_t), e.g. to record timing events around calls */
+int dnl_get_stream(dnl_handle *h, void **stream);
+
+/* Device-time marks on the handle's stream: dnl_timer_mark records CUDA event `slot` (0..7);
+ * dnl_timer_elapsed waits for `to` and returns the milliseconds between the two marks. */
+int dnl_timer_mark(dnl_handle *h, int slot);
+int dnl_timer_elapsed(dnl_handle *h, int from, int to, double *ms);
+/* FP64 fused multiply-add throughput of the current device, measured by a dependent-chain kernel
+ * over all SMs (TFLOP/s, 2 flops per DFMA) */
+int dnl_measure_fp64_peak(double *tflops);
+
 /* --------------------------------------------------------------------------------- misc */
+/* select the CUDA device used by subsequent dnl_create calls of this thread */
+int dnl_set_device(int device);
+/* page-locked host memory for fast host <-> device state transfers */
+int dnl_host_alloc(unsigned long long bytes, void **ptr);
+int dnl_host_free(void *ptr);
 const char *dnl_error_string(int status);
 int dnl_device_count(int *count);
 /* number of kernels this library launched (all handles), for launch accounting */

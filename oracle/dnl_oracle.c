@@ -68,6 +68,7 @@ struct dnlo {
   double computedTimeStep, lastTimeStep, tsDate, lastTsDate;
   double *EV, *Ke, *kx;
   double fmax0;
+  long pulse_iter, pulse_total;
   long *n2e_start, *n2e;
   double Nt[8][8];
   double dNxi[8][8][3];
@@ -776,6 +777,8 @@ int dnlo_max_frequency(dnlo *h, double *out)
     }
   }
   free(EV0);
+  h->pulse_iter = iteration;
+  h->pulse_total += iteration;
   *out = sqrt(fmax);
   return 0;
 }
@@ -1103,6 +1106,8 @@ double dnlo_get(dnlo *h, const char *nm)
   if (!strcmp(nm, "increment")) return (double)h->increment;
   if (!strcmp(nm, "computed_dt")) return h->computedTimeStep;
   if (!strcmp(nm, "fmax0")) return h->fmax0;
+  if (!strcmp(nm, "pulse_iterations")) return (double)h->pulse_iter;
+  if (!strcmp(nm, "pulse_total")) return (double)h->pulse_total;
   if (!strcmp(nm, "alphaM")) return h->alphaM;
   if (!strcmp(nm, "beta")) return h->beta;
   if (!strcmp(nm, "gamma")) return h->gamma;

@@ -48,15 +48,19 @@ struct DevTime {
   double timeStep, currentTime, nextTime, upTime, endTime, startTime;
   double computedTimeStep, lastTimeStep, tsDate, lastTsDate;
   double kinetic;
-  double fmax, fmax0;                // Pulse: last frequency, Domain::fmax0
+  double fmax;                       // Pulse: sqrt of the converged eigenvalue estimate
+  double fmax0;                      // Pulse: Domain::fmax0, last estimate (0 = not started)
+  double pulseScale;                 // Pulse: divisor that normalises the stored vector
+  unsigned long long pulseMaxBits;   // Pulse: max |M^-1 K x| of the running iteration
   unsigned long long lenMinBits;     // Courant: min element length (bits of a positive double)
   long long increment;
+  long long pulseTotal;              // Pulse: power iterations over the run
   int done;
   int status;
   int badElem;
   int pulseDone;                     // Pulse: power iteration converged
-  int pulseIter;
-  int pad[3];
+  int pulseIter;                     // Pulse: iterations of the running call
+  int pad;
 };
 
 // ------------------------------------------------------------------------ kernel arguments
@@ -142,8 +146,9 @@ struct dnl_handle {
   int *bcIdx, *bcCode, *bcNodeList;
   double *bcSpeed;
   bool hasSpeedBC;
-  // Pulse
-  double *ev, *ev0;
+  // Pulse: per Gauss point J^-1, weight x detJ (x 2 pi R) and R; the iterated vector (raw)
+  double *pj, *ev, *kx;
+  double C00, C01, C33;       // Hooke matrix entries (Material::getHookeMatrix)
   // time
   dnl::DevTime *tm;
   dnl::Material mat;
@@ -156,6 +161,11 @@ struct dnl_handle {
   dnl::GraphEntry graphs[8];
   int ngraphs;
   char lastError[256];
+  double *stage;              // N*3 staging buffer for host <-> device nodal vectors
+  cudaEvent_t marks[8];
+  // per-kernel event timing (dnl_profile_begin/end)
+  bool profiling;
+  void *prof;
 };
 
 namespace dnl {
@@ -166,4 +176,7 @@ int launch_courant(dnl_handle *h, cudaStream_t s);
 int launch_pulse(dnl_handle *h, cudaStream_t s);
 void set_shape_tables();
 long long &launch_counter();
+// event brackets around one launch when the handle is profiling
+void prof_begin(dnl_handle *h, cudaStream_t s);
+void prof_end(dnl_handle *h, int kind, cudaStream_t s);
 }  // namespace dnl

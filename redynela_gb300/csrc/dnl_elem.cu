@@ -679,10 +679,12 @@ int launch_elem(dnl_handle *h, cudaStream_t s, int gate)
   a.gate = gate;
   const long threads = (long)h->E * h->nip;
   const int grid = (int)((threads + 127) / 128);
+  prof_begin(h, s);
   if (h->etype == DNL_ELQUA4NAX)
     k_elem<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a);
   else
     k_elem<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a);
+  prof_end(h, DNL_PROF_ELEM, s);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
@@ -703,7 +705,9 @@ int launch_mass(dnl_handle *h, cudaStream_t s, double *me)
 int launch_courant(dnl_handle *h, cudaStream_t s)
 {
   ElemArgs a = elem_args(h);
+  prof_begin(h, s);
   k_courant<<<(h->E + 255) / 256, 256, 0, s>>>(a);
+  prof_end(h, DNL_PROF_COURANT, s);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }

@@ -239,6 +239,37 @@ __global__ void k_dt(DtArgs a)
   }
 }
 
+// node-major (x,y,z) host layout <-> component arrays on the device
+__global__ void k_aos_to_soa(int N, const double *aos, double *c0, double *c1, double *c2)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  c0[n] = aos[3L * n];
+  c1[n] = aos[3L * n + 1];
+  c2[n] = aos[3L * n + 2];
+}
+__global__ void k_soa_to_aos(int N, double *aos, const double *c0, const double *c1, const double *c2)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  aos[3L * n] = c0[n];
+  aos[3L * n + 1] = c1[n];
+  aos[3L * n + 2] = c2[n];
+}
+
+// FP64 throughput probe: 8 independent DFMA chains per thread, ITER rounds
+__global__ void k_fp64_peak(double *out, double a, double b, int iters)
+{
+  double x0 = threadIdx.x * 1e-9, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5,
+         x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; i++) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  const double s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+  if (s == 12345.678) out[0] = s;  // keeps the chains live
+}
+
 // kinetic energy of the Current field (Domain::getTotalKineticEnergy), fixed-order block sums
 __global__ void k_kinetic(int N, NodeFields f, const double *mass, double *partial)
 {
@@ -295,10 +326,12 @@ int launch_gather(dnl_handle *h)
 {
   GatherArgs g = gather_args(h);
   const int grid = (h->N + 255) / 256;
+  prof_begin(h, h->stream);
   if (h->dim == 2)
     k_gather<2><<<grid, 256, 0, h->stream>>>(g);
   else
     k_gather<3><<<grid, 256, 0, h->stream>>>(g);
+  prof_end(h, DNL_PROF_NODE, h->stream);
   launch_counter()++;
   return check_launch();
 }
@@ -324,10 +357,12 @@ int launch_node(dnl_handle *h, bool keepFint)
   g.beta = h->beta;
   g.gamma = h->gamma;
   const int grid = (h->N + 255) / 256;
+  prof_begin(h, h->stream);
   if (h->dim == 2)
     k_node<2><<<grid, 256, 0, h->stream>>>(g);
   else
     k_node<3><<<grid, 256, 0, h->stream>>>(g);
+  prof_end(h, DNL_PROF_NODE, h->stream);
   launch_counter()++;
   return check_launch();
 }
@@ -341,7 +376,9 @@ int launch_dt(dnl_handle *h, int mode)
   a.method = h->method;
   a.safetyOmega = h->safetyOmega;
   a.Cs = h->mat.Cs;
+  prof_begin(h, h->stream);
   k_dt<<<1, 1, 0, h->stream>>>(a);
+  prof_end(h, DNL_PROF_OTHER, h->stream);
   launch_counter()++;
   return check_launch();
 }
@@ -349,8 +386,10 @@ int launch_dt(dnl_handle *h, int mode)
 int launch_bc_current(dnl_handle *h)
 {
   if (!h->nbcNodes) return 0;
+  prof_begin(h, h->stream);
   k_bc_current<<<(h->nbcNodes + 127) / 128, 128, 0, h->stream>>>(h->nbcNodes, h->bcNodeList, h->bcCode,
                                                                   h->bcSpeed, h->bank[h->cur], h->tm);
+  prof_end(h, DNL_PROF_OTHER, h->stream);
   launch_counter()++;
   return check_launch();
 }
@@ -393,6 +432,48 @@ int enqueue_step(dnl_handle *h, long long incAfter, bool last)
 
 }  // namespace
 
+// ------------------------------------------------------------------------------ profiling
+namespace {
+struct ProfRec {
+  int kind;
+  cudaEvent_t a, b;
+};
+struct Prof {
+  std::vector<ProfRec> recs;
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t open;
+};
+cudaEvent_t prof_event(Prof *p)
+{
+  if (!p->pool.empty()) {
+    cudaEvent_t e = p->pool.back();
+    p->pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+}  // namespace
+
+namespace dnl {
+void prof_begin(dnl_handle *h, cudaStream_t s)
+{
+  if (!h->profiling) return;
+  Prof *p = (Prof *)h->prof;
+  p->open = prof_event(p);
+  cudaEventRecord(p->open, s);
+}
+void prof_end(dnl_handle *h, int kind, cudaStream_t s)
+{
+  if (!h->profiling) return;
+  Prof *p = (Prof *)h->prof;
+  cudaEvent_t b = prof_event(p);
+  cudaEventRecord(b, s);
+  p->recs.push_back(ProfRec{kind, p->open, b});
+}
+}  // namespace dnl
+
 // =============================================================================== C ABI
 extern "C" {
 
@@ -423,16 +504,131 @@ int dnl_device_count(int *count)
 
 long long dnl_kernel_launches(void) { return launch_counter(); }
 
+int dnl_profile_begin(dnl_handle *h)
+{
+  if (!h) return DNL_ERR_ARG;
+  if (!h->prof) h->prof = new Prof();
+  ((Prof *)h->prof)->recs.clear();
+  h->profiling = true;
+  return 0;
+}
+
+int dnl_profile_end(dnl_handle *h, double *ms, long long *launches)
+{
+  if (!h || !h->prof) return DNL_ERR_ARG;
+  h->profiling = false;
+  CK(cudaStreamSynchronize(h->stream));
+  Prof *p = (Prof *)h->prof;
+  for (int k = 0; k < DNL_PROF_KINDS; k++) {
+    if (ms) ms[k] = 0.;
+    if (launches) launches[k] = 0;
+  }
+  for (auto &r : p->recs) {
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, r.a, r.b));
+    if (ms) ms[r.kind] += t;
+    if (launches) launches[r.kind]++;
+    p->pool.push_back(r.a);
+    p->pool.push_back(r.b);
+  }
+  p->recs.clear();
+  return 0;
+}
+
+int dnl_timer_mark(dnl_handle *h, int slot)
+{
+  if (!h || slot < 0 || slot >= 8) return DNL_ERR_ARG;
+  if (!h->marks[slot]) CK(cudaEventCreate(&h->marks[slot]));
+  CK(cudaEventRecord(h->marks[slot], h->stream));
+  return 0;
+}
+
+int dnl_timer_elapsed(dnl_handle *h, int from, int to, double *ms)
+{
+  if (!h || !ms || from < 0 || from >= 8 || to < 0 || to >= 8 || !h->marks[from] || !h->marks[to])
+    return DNL_ERR_ARG;
+  CK(cudaEventSynchronize(h->marks[to]));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, h->marks[from], h->marks[to]));
+  *ms = t;
+  return 0;
+}
+
+int dnl_measure_fp64_peak(double *tflops)
+{
+  if (!tflops) return DNL_ERR_ARG;
+  int dev = 0, sms = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  double *out;
+  CK(cudaMalloc(&out, sizeof(double)));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const int threads = 256, blocks = sms * 8, iters = 4096;
+  k_fp64_peak<<<blocks, threads>>>(out, 0.999999, 1e-7, 64);  // warm-up
+  CK(cudaEventRecord(e0));
+  k_fp64_peak<<<blocks, threads>>>(out, 0.999999, 1e-7, iters);
+  CK(cudaEventRecord(e1));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, e0, e1));
+  launch_counter() += 2;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  const double flops = 2.0 * 8.0 * iters * (double)threads * blocks;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return 0;
+}
+
+int dnl_set_device(int device)
+{
+  CK(cudaSetDevice(device));
+  return 0;
+}
+
+int dnl_host_alloc(unsigned long long bytes, void **ptr)
+{
+  if (!ptr) return DNL_ERR_ARG;
+  CK(cudaMallocHost(ptr, bytes));
+  return 0;
+}
+
+int dnl_host_free(void *ptr)
+{
+  if (ptr) CK(cudaFreeHost(ptr));
+  return 0;
+}
+
+int dnl_get_stream(dnl_handle *h, void **stream)
+{
+  if (!h || !stream) return DNL_ERR_ARG;
+  *stream = (void *)h->stream;
+  return 0;
+}
+
 int dnl_destroy(dnl_handle *h)
 {
   if (!h) return DNL_ERR_ARG;
   for (int i = 0; i < h->ngraphs; i++) cudaGraphExecDestroy(h->graphs[i].exec);
   void *ptrs[] = {h->conn, h->x[0], h->n2eStart, h->n2e, h->mass, h->fieldMem, h->ip, h->detJ,
-                  h->stepT, h->fe, h->fint, h->bcIdx, h->bcCode, h->bcNodeList, h->bcSpeed,
-                  h->ev, h->ev0, h->tm};
+                  h->stepT, h->fe, h->fint, h->stage, h->bcIdx, h->bcCode, h->bcNodeList, h->bcSpeed,
+                  h->pj, h->ev, h->kx, h->tm};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  for (int i = 0; i < 8; i++)
+    if (h->marks[i]) cudaEventDestroy(h->marks[i]);
   if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->prof) {
+    Prof *p = (Prof *)h->prof;
+    for (auto &r : p->recs) {
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+    for (auto e : p->pool) cudaEventDestroy(e);
+    delete p;
+  }
   delete h;
   return 0;
 }
@@ -577,6 +773,7 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
         CKF(cudaMemcpy(h->bank[b].v[c], v.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
       }
   }
+  CKF(cudaMalloc(&h->stage, sizeof(double) * 3 * (size_t)N));
   CKF(cudaMalloc(&h->mass, sizeof(double) * N));
   CKF(cudaMemset(h->mass, 0, sizeof(double) * N));
   // ---- integration points
@@ -643,10 +840,18 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
       CKF(cudaMemcpy(h->bcSpeed, spds.data(), sizeof(double) * spds.size(), cudaMemcpyHostToDevice));
     }
   }
-  // ---- Pulse vectors
+  // ---- Pulse: per-Gauss-point kinematics, iterated vector, element products
   if (h->method == DNL_PULSE) {
+    const int npj = h->dim * h->dim + 2;
+    CKF(cudaMalloc(&h->pj, sizeof(double) * (size_t)npj * h->nIP));
     CKF(cudaMalloc(&h->ev, sizeof(double) * (size_t)h->dim * N));
-    CKF(cudaMalloc(&h->ev0, sizeof(double) * (size_t)h->dim * N));
+    CKF(cudaMalloc(&h->kx, sizeof(double) * (size_t)h->dim * E * nen));
+    // Material::getHookeMatrix (Material.C:270-331): entries times E(1-nu)/((1+nu)(1-2nu))
+    const double Nu = m.nu;
+    const double f = (m.young * (1.0 - Nu) / ((1.0 + Nu) * (1.0 - 2.0 * Nu)));
+    h->C00 = 1 * f;
+    h->C01 = (Nu / (1. - Nu)) * f;
+    h->C33 = ((1.0 - 2.0 * Nu) / (2. * (1.0 - Nu))) * f;
   }
   // ---- time state
   CKF(cudaMalloc(&h->tm, sizeof(DevTime)));
@@ -670,13 +875,11 @@ int dnl_set_state(dnl_handle *h, const dnl_state_view *s)
 {
   if (!h || !s) return DNL_ERR_ARG;
   const int N = h->N;
-  std::vector<double> buf((size_t)N);
   auto put3 = [&](const double *src, double *const dst[3]) -> int {
-    for (int c = 0; c < 3; c++) {
-      for (int n = 0; n < N; n++) buf[n] = src[3 * (size_t)n + c];
-      CK(cudaMemcpy(dst[c], buf.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
-    }
-    return 0;
+    CK(cudaMemcpyAsync(h->stage, src, sizeof(double) * 3 * (size_t)N, cudaMemcpyHostToDevice, h->stream));
+    k_aos_to_soa<<<(N + 255) / 256, 256, 0, h->stream>>>(N, h->stage, dst[0], dst[1], dst[2]);
+    launch_counter()++;
+    return check_launch();
   };
   int r;
   if (s->coords && (r = put3(s->coords, h->x))) return r;
@@ -687,6 +890,8 @@ int dnl_set_state(dnl_handle *h, const dnl_state_view *s)
   const int ns = h->etype == DNL_ELQUA4NAX ? 4 : 6;
   const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
   const size_t nIP = h->nIP;
+  CK(cudaStreamSynchronize(h->stream));
+  if (!(s->S || s->Eps || s->EpsPlas || s->p || s->evp)) return 0;
   std::vector<double> ib(nIP);
   auto putT = [&](const double *src, int base) -> int {
     for (int k = 0; k < ns; k++) {
@@ -710,14 +915,13 @@ int dnl_set_state(dnl_handle *h, const dnl_state_view *s)
 int dnl_get_state(dnl_handle *h, dnl_state_view *s)
 {
   if (!h || !s) return DNL_ERR_ARG;
-  CK(cudaStreamSynchronize(h->stream));
   const int N = h->N;
-  std::vector<double> buf((size_t)N);
   auto get3 = [&](double *dst, double *const src[3]) -> int {
-    for (int c = 0; c < 3; c++) {
-      CK(cudaMemcpy(buf.data(), src[c], sizeof(double) * N, cudaMemcpyDeviceToHost));
-      for (int n = 0; n < N; n++) dst[3 * (size_t)n + c] = buf[n];
-    }
+    k_soa_to_aos<<<(N + 255) / 256, 256, 0, h->stream>>>(N, h->stage, src[0], src[1], src[2]);
+    launch_counter()++;
+    if (int r = check_launch()) return r;
+    CK(cudaMemcpyAsync(dst, h->stage, sizeof(double) * 3 * (size_t)N, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
     return 0;
   };
   int r;
@@ -726,7 +930,9 @@ int dnl_get_state(dnl_handle *h, dnl_state_view *s)
   if (s->v && (r = get3(s->v, h->bank[h->cur].v))) return r;
   if (s->a && (r = get3(s->a, h->bank[h->cur].a))) return r;
   if (s->disp && (r = get3(s->disp, h->bank[h->cur].disp))) return r;
+  CK(cudaStreamSynchronize(h->stream));
   if (s->mass) CK(cudaMemcpy(s->mass, h->mass, sizeof(double) * N, cudaMemcpyDeviceToHost));
+  if (!(s->S || s->Eps || s->EpsPlas || s->p || s->evp || s->Sig)) return 0;
   const int ns = h->etype == DNL_ELQUA4NAX ? 4 : 6;
   const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
   const size_t nIP = h->nIP;
@@ -882,6 +1088,7 @@ int dnl_step_graph(dnl_handle *h, int nsteps, int *steps_done)
 {
   if (steps_done) *steps_done = 0;
   if (!h || nsteps <= 0) return DNL_ERR_ARG;
+  if (h->method == DNL_PULSE) return DNL_ERR_ARG;  // Pulse iterates to convergence with host checks
   int r;
   if (!h->prologueDone && (r = dnl_prologue(h))) return r;
   const long long inc0 = h->hostIncrement;

@@ -35,6 +35,7 @@ STATUS_NAMES = {
     8: "DNL_ERR_SINGULAR", 9: "DNL_ERR_TIMEOUT",
 }
 FLAG_STEP_TENSORS = 1
+PROF_KINDS = ("elem", "node", "pulse", "courant", "other")
 
 
 class DnlError(RuntimeError):
@@ -105,6 +106,15 @@ def lib():
         L.dnl_error_string.argtypes = [C.c_int]
         L.dnl_device_count.argtypes = [_ip]
         L.dnl_kernel_launches.restype = C.c_longlong
+        L.dnl_profile_begin.argtypes = [H]
+        L.dnl_profile_end.argtypes = [H, _dp, C.POINTER(C.c_longlong)]
+        L.dnl_get_stream.argtypes = [H, C.POINTER(C.c_void_p)]
+        L.dnl_timer_mark.argtypes = [H, C.c_int]
+        L.dnl_timer_elapsed.argtypes = [H, C.c_int, C.c_int, _dp]
+        L.dnl_measure_fp64_peak.argtypes = [_dp]
+        L.dnl_set_device.argtypes = [C.c_int]
+        L.dnl_host_alloc.argtypes = [C.c_ulonglong, C.POINTER(C.c_void_p)]
+        L.dnl_host_free.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -117,6 +127,39 @@ def device_count() -> int:
 
 def kernel_launches() -> int:
     return int(lib().dnl_kernel_launches())
+
+
+def set_device(device: int) -> None:
+    rc = lib().dnl_set_device(int(device))
+    if rc:
+        raise DnlError(rc, lib().dnl_error_string(rc).decode())
+
+
+def fp64_peak_tflops() -> float:
+    t = C.c_double(0)
+    rc = lib().dnl_measure_fp64_peak(C.byref(t))
+    if rc:
+        raise DnlError(rc, lib().dnl_error_string(rc).decode())
+    return t.value
+
+
+class PinnedArray:
+    """A float64 numpy array in page-locked host memory (dnl_host_alloc)."""
+
+    def __init__(self, shape):
+        n = int(np.prod(shape))
+        p = C.c_void_p()
+        rc = lib().dnl_host_alloc(8 * max(n, 1), C.byref(p))
+        if rc:
+            raise DnlError(rc, lib().dnl_error_string(rc).decode())
+        self._p = p
+        buf = (C.c_double * max(n, 1)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=np.float64, count=n).reshape(shape)
+
+    def __del__(self):
+        if getattr(self, "_p", None) and self._p.value:
+            lib().dnl_host_free(self._p)
+            self._p = None
 
 
 def _ptr(a: Optional[np.ndarray]):
@@ -248,6 +291,30 @@ class GpuDomain:
         dt = C.c_double(0)
         self._check(self.L.dnl_time_step(self.h, C.byref(dt)))
         return dt.value
+
+    def profile_begin(self) -> None:
+        self._check(self.L.dnl_profile_begin(self.h))
+
+    def profile_end(self) -> Dict[str, tuple]:
+        """{kernel class: (milliseconds, launches)} since profile_begin."""
+        ms = np.zeros(len(PROF_KINDS))
+        n = (C.c_longlong * len(PROF_KINDS))()
+        self._check(self.L.dnl_profile_end(self.h, _ptr(ms), n))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(PROF_KINDS)}
+
+    def timer_mark(self, slot: int) -> None:
+        self._check(self.L.dnl_timer_mark(self.h, int(slot)))
+
+    def timer_elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_double(0)
+        self._check(self.L.dnl_timer_elapsed(self.h, int(a), int(b), C.byref(ms)))
+        return ms.value
+
+    def stream(self) -> int:
+        """The handle's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+        p = C.c_void_p()
+        self._check(self.L.dnl_get_stream(self.h, C.byref(p)))
+        return int(p.value or 0)
 
     def time_info(self) -> dict:
         t = TimeInfo()

@@ -10,6 +10,7 @@ reference's own output on a seeded synthetic model:
 * ``steps_c0.npz``      the 5x50 Taylor bar, first 20 steps: Fint, dt, kinetic energy per step
 * ``run_c0.npz``        the 5x50 Taylor bar to 80 us: final coordinates, plastic strain, pressure
 * ``steps_hex.npz``     a 6x6x8 hex bar with the Pulse time step, first 30 steps
+* ``run_hex.npz``       an 8x8x24 hex bar with the Pulse time step to 80 us: final coordinates
 
     python tests/golden/make_golden.py
 """
@@ -64,6 +65,11 @@ def main():
     save("steps_hex.npz", mass=r["mass"], dt0=r["dt0"], dt=r["dt"], time=r["time"],
          kinetic=r["kinetic"], fint=np.stack([r[f"fint_{k:06d}"] for k in range(30)]),
          final_coords=r["final_coords"])
+
+    m = meshes.taylor_hex(8, 24)
+    r = dnl_io.run_reference("run", m)
+    save("run_hex.npz", increments=r["increments"], time=r["time"], final_coords=r["final_coords"],
+         final_evp=r["final_evp"])
 
 
 if __name__ == "__main__":
