@@ -154,6 +154,36 @@ int dnl_get_time_info(dnl_handle *h, dnl_time_info *info);
 /* nodal internal forces of the last element pass, dim*N */
 int dnl_get_fint(dnl_handle *h, double *fint);
 
+/* ------------------------------------------------------------- no device allocation */
+/* Internal forces for callers that cannot allocate device memory: code running inside a CUDA
+ * stream capture, or under a memory manager that owns all device memory and forbids the library
+ * its own cudaMalloc.  No counterpart in the reference (its element loop runs on host objects).
+ *
+ * Same computation and side effects as dnl_internal_forces, but without a handle: the caller
+ * passes every input and output in device memory, and the per-element force scratch
+ * (num_elements * nen * dim doubles) is a fixed array inside the library, at most
+ * DNL_STATIC_MAX_ELEMENT_DOFS doubles (8 MiB; e.g. 43,690 hex8 or 131,072 axisymmetric elements);
+ * larger meshes are rejected with DNL_ERR_ARG.  Every GPU that loads the library holds that array
+ * until the process exits.  The first call on a device resolves the array's address (make it
+ * before any stream capture).  All calls share the array: calls whose GPU work overlaps race and
+ * must be serialised by the caller.  The function synchronises `stream` to read the error word.
+ * It calls no cudaMalloc, cudaFree or allocating library routine. */
+#define DNL_STATIC_MAX_ELEMENT_DOFS (1 << 20)
+typedef struct {
+  int etype, num_nodes, num_elements;
+  const int *conn;       /* [nen][E], node indices (component-major) */
+  const int *node_start; /* N+1 offsets into node_entry */
+  const int *node_entry; /* e*nen + k for each element touching the node, ascending e */
+  const double *coords;  /* [3][N] current coordinates */
+  const double *du;      /* [3][N] Current delta_disp */
+  double *ip;            /* integration-point state, updated in place: [ncomp][E*nip] with the
+                            components S, Eps, EpsPlas (symmetric: xx yy zz xy [xz yz]), p, evp,
+                            evp^n -- 15 components (axisymmetric) or 21 (hex8) */
+  double *fint;          /* out: N*dim, index n*dim + j */
+  dnl_material mat;
+} dnl_static_args;
+int dnl_internal_forces_static(const dnl_static_args *args, void *stream, int *bad_element);
+
 /* -------------------------------------------------------------------------- measurement */
 /* Per-kernel device time: between dnl_profile_begin and dnl_profile_end the library brackets each
  * of its launches on the handle's stream with CUDA events; dnl_profile_end synchronises and returns

@@ -176,6 +176,9 @@ int launch_courant(dnl_handle *h, cudaStream_t s);
 int launch_pulse(dnl_handle *h, cudaStream_t s);
 void set_shape_tables();
 long long &launch_counter();
+// launches on caller-built arguments (no handle)
+int launch_elem_raw(int etype, const ElemArgs &a, cudaStream_t s);
+int launch_gather_raw(int dim, const GatherArgs &g, cudaStream_t s);
 // event brackets around one launch when the handle is profiling
 void prof_begin(dnl_handle *h, cudaStream_t s);
 void prof_end(dnl_handle *h, int kind, cudaStream_t s);

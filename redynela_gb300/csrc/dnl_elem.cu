@@ -689,6 +689,18 @@ int launch_elem(dnl_handle *h, cudaStream_t s, int gate)
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
 
+int launch_elem_raw(int etype, const ElemArgs &a, cudaStream_t s)
+{
+  const long threads = (long)a.E * (etype == DNL_ELQUA4NAX ? 4 : 8);
+  const int grid = (int)((threads + 127) / 128);
+  if (etype == DNL_ELQUA4NAX)
+    k_elem<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a);
+  else
+    k_elem<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a);
+  launch_counter()++;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
+}
+
 int launch_mass(dnl_handle *h, cudaStream_t s, double *me)
 {
   ElemArgs a = elem_args(h);

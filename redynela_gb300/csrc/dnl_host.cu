@@ -432,6 +432,19 @@ int enqueue_step(dnl_handle *h, long long incAfter, bool last)
 
 }  // namespace
 
+namespace dnl {
+int launch_gather_raw(int dim, const GatherArgs &g, cudaStream_t s)
+{
+  const int grid = (g.N + 255) / 256;
+  if (dim == 2)
+    k_gather<2><<<grid, 256, 0, s>>>(g);
+  else
+    k_gather<3><<<grid, 256, 0, s>>>(g);
+  launch_counter()++;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
+}
+}  // namespace dnl
+
 // ------------------------------------------------------------------------------ profiling
 namespace {
 struct ProfRec {
