@@ -10,6 +10,8 @@ decomposition, radial return, forces), CSR assembly, nodal update and the time-s
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config hex|axi]
 
+The timed window starts at t = 10 us of the 80 us impact (reached untimed), when the elastic
+wave has crossed the bar and the impact end is plastic.
 `value` is measured with device-resident state (CUDA events on the library's stream);
 `e2e` goes through the C ABI with page-locked host buffers: each step uploads the nodal state the
 caller owns (coordinates, delta_disp, velocity, acceleration, displacement), advances one step and
@@ -139,11 +141,33 @@ def barrier(world: int):
         dist.barrier()
 
 
-def run_cpu_baseline(model, sample_desc, min_seconds=10.0, max_steps=400, threads=None):
+def run_cpu_baseline(model, sample_desc, min_seconds=10.0, max_steps=400, threads=None,
+                     start=None, start_us=0.0):
+    """The oracle on the host cores.  `start` = (state, time info) of the GPU run at the window
+    start, injected after the oracle's own prologue (which computes the lumped mass on the
+    undeformed mesh, as the reference does once); otherwise the oracle advances to start_us."""
     from oracle.oracle import Oracle
     threads = threads or os.cpu_count() or 1
     o = Oracle(model, threads=threads)
     o.prologue()
+    if start is not None:
+        st, info = start
+        o.inject(coords=st["coords"], du=st["du"], v=st["v"], a=st["a"], disp=st["disp"],
+                 S=st["S"], Eps=st["Eps"], EpsPlas=st["EpsPlas"], p=st["p"], evp=st["evp"],
+                 dt=info["time_step"])
+        o.set("time", info["time"])
+        o.set("increment", info["increment"])
+        o.set("computed_dt", info["computed_step"])
+        o.set("last_dt", info["computed_step"])
+        o.set("ts_date", info["time"])
+        o.set("last_ts_date", info["time"])
+        o.internal_matrices()
+        if model.method == meshes.PULSE:
+            o.max_frequency()  # warm the power-iteration vector like the GPU's
+    else:
+        while o.get("time") < start_us * 1e-6:
+            if o.steps(50) == 0:
+                break
     o.steps(2)  # warm-up
     t0 = time.perf_counter()
     steps = 0
@@ -166,6 +190,9 @@ def main_reference(args):
     threads = os.cpu_count() or 1
     o = Oracle(model, threads=threads)
     o.prologue()
+    while o.get("time") < args.start_us * 1e-6:  # untimed, to the window start
+        if o.steps(50) == 0:
+            break
     if args.warmup:
         o.steps(args.warmup)
     t0 = time.perf_counter()
@@ -177,7 +204,8 @@ def main_reference(args):
             "unit": "element-updates/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(done, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": name, "sample": sample},
+            "data": "synthetic",
+            "config": {"workload": name, "sample": sample, "window_start_us": args.start_us},
             "cpu_baseline": {"value": rate, "unit": "element-updates/s", "cores": threads,
                              "kind": "port",
                              "sample": f"{sample}; the oracle's C restatement of the reference "
@@ -200,7 +228,14 @@ def main_ours(args):
 
     d = dynela.GpuDomain(model)
     d.prologue()
-    launches0 = dynela.kernel_launches()
+    # advance, untimed, to the start of the measured window
+    while d.time_info()["time"] < args.start_us * 1e-6:
+        if d.step(50) == 0:
+            break
+    window = d.time_info()
+    snapshot = None
+    if rank == 0 and not args.no_cpu:
+        snapshot = d.get_state("coords", "du", "v", "a", "disp", "S", "Eps", "EpsPlas", "p", "evp")
     d.step(args.warmup)
 
     # ---- device-resident timed region
@@ -208,9 +243,11 @@ def main_ours(args):
     with ClockSampler(local) as clk:
         launches0 = dynela.kernel_launches()
         d.profile_begin()
+        dynela.range_push("window")
         d.timer_mark(0)
         done = d.step(args.steps)
         d.timer_mark(1)
+        dynela.range_pop()
         ms = d.timer_elapsed_ms(0, 1)
         prof = d.profile_end()
         launches = dynela.kernel_launches() - launches0
@@ -269,7 +306,8 @@ def main_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu:
         cm, sample = cpu_sample(args.config, args.layers)
-        cpu = run_cpu_baseline(cm, sample, min_seconds=args.cpu_seconds)
+        cpu = run_cpu_baseline(cm, sample, min_seconds=args.cpu_seconds,
+                               start=(snapshot, window))
 
     if rank == 0:
         line = {"metric": "element-updates/s", "value": value, "unit": "element-updates/s",
@@ -279,6 +317,8 @@ def main_ours(args):
                 "data": "synthetic (seeded generator of the reference Taylor deck's geometry)",
                 "config": {"workload": name, "elements": model.E, "nodes": model.N,
                            "time_step": "Pulse every 10 increments",
+                           "window": f"{args.steps} steps from t = {window['time'] * 1e6:.2f} us "
+                                     f"(increment {window['increment']}), reached untimed",
                            "l2": "inputs larger than L2 (integration-point state "
                                  f"{model.E * model.nip * (3 * (4 if model.etype == 0 else 6) + 3) * 8 / 1e6:.0f} MB)",
                            "parallelism": f"replicas x{world}"},
@@ -291,14 +331,68 @@ def main_ours(args):
         dist.destroy_process_group()
 
 
+def main_batch(args):
+    """Batched mode: 256 seeded axisymmetric Taylor bars (radial x axial divisions 4-40 x 40-400,
+    v 150-300 m/s, A 60-150 MPa, B 200-400 MPa, n 0.2-0.5), every instance advancing K steps with
+    its own time step in one graph-captured launch sequence per step, against the same bars run
+    one after another through the single-mesh path on the same GPU."""
+    from redynela_gb300 import build, dynela
+    build.build()
+    models = meshes.taylor_batch(args.instances, seed=0)
+    E = sum(m.E for m in models)
+    b = dynela.BatchDomain(models)
+    b.prologue()
+    block = b.autotune(steps=3)
+    b.step_graph(args.steps)  # capture + warm-up
+    for _ in range(max(0, args.warmup - 1)):
+        b.step_graph(args.steps)
+    hv = b.handle_view()
+    with ClockSampler(0) as clk:
+        launches0 = dynela.kernel_launches()
+        hv.timer_mark(0)
+        active = b.step_graph(args.steps)
+        hv.timer_mark(1)
+        ms = hv.timer_elapsed_ms(0, 1)
+        launches = dynela.kernel_launches() - launches0
+    clocks = clk.summary()
+    value = E * args.steps / (ms * 1e-3)
+    # the same bars one at a time through the single-mesh path (stream launches, state resident)
+    plain_ms = 0.0
+    for m in models:
+        d = dynela.GpuDomain(m)
+        d.prologue()
+        d.step(args.warmup)
+        d.timer_mark(0)
+        d.step(args.steps)
+        d.timer_mark(1)
+        plain_ms += d.timer_elapsed_ms(0, 1)
+        d.close()
+    plain = E * args.steps / (plain_ms * 1e-3)
+    line = {"metric": "element-updates/s (batched)", "value": value, "unit": "element-updates/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, numpy default_rng(0))",
+            "config": {"workload": f"taylor_axi_batch_{args.instances}", "elements": E,
+                       "instances": args.instances, "block": block, "active_after": active,
+                       "l2": "inputs larger than L2 (integration-point state "
+                             f"{E * 4 * 15 * 8 / 1e6:.0f} MB)"},
+            "plain_instance_by_instance": {"value": plain, "ms_per_step": plain_ms / args.steps},
+            "batched_over_plain": value / plain, "gpu_launches": launches, "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="hex", choices=["hex", "axi"])
+    ap.add_argument("--config", default="hex", choices=["hex", "axi", "batch"])
+    ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--start-us", type=float, default=10.0,
+                    help="simulated time at which the timed window starts (reached untimed), so "
+                         "the window sees the deformed, partly plastic bar of a real run")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--layers", type=int, default=400,
                     help="axial layers of the hex bar (400 = the benchmark workload; fewer for "
@@ -308,6 +402,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         main_reference(args)
+    elif args.config == "batch":
+        main_batch(args)
     else:
         main_ours(args)
 

@@ -154,6 +154,31 @@ int dnl_get_time_info(dnl_handle *h, dnl_time_info *info);
 /* nodal internal forces of the last element pass, dim*N */
 int dnl_get_fint(dnl_handle *h, double *fint);
 
+/* ------------------------------------------------------------------------------ batches */
+/* Many independent meshes (same element type, Courant time step) advanced together: each keeps
+ * its own material, time step, increment counter and end time (each instance is one
+ * ExplicitSolverCH::solve of its own Domain); every kernel of a step is launched once for all
+ * instances.  No counterpart in the reference, which solves one domain at a time
+ * (Structure::solve, Structure.C:809-897). */
+typedef struct dnl_batch dnl_batch;
+int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material *mats,
+                     const dnl_solver_params *params, dnl_batch **out);
+int dnl_batch_destroy(dnl_batch *b);
+int dnl_batch_prologue(dnl_batch *b);
+/* nsteps increments of every unfinished instance; *active = instances not yet at their end time */
+int dnl_batch_step(dnl_batch *b, int nsteps, int *active);
+/* the same, captured once into a CUDA graph per (nsteps, phase) and replayed */
+int dnl_batch_step_graph(dnl_batch *b, int nsteps, int *active);
+/* time live steps with 64, 128 and 256 threads per element-pass block; keep the fastest */
+int dnl_batch_autotune(dnl_batch *b, int steps_per_candidate, int *block);
+int dnl_batch_set_block(dnl_batch *b, int block);
+int dnl_batch_time_info(dnl_batch *b, int instance, dnl_time_info *info);
+int dnl_batch_get_coords(dnl_batch *b, int instance, double *coords);
+int dnl_batch_get_fint(dnl_batch *b, int instance, double *fint);
+int dnl_batch_sizes(dnl_batch *b, int *elements, int *nodes);
+/* the handle holding the union mesh (profiling, timer marks, stream) -- owned by the batch */
+int dnl_batch_handle(dnl_batch *b, dnl_handle **h);
+
 /* ------------------------------------------------------------- no device allocation */
 /* Internal forces for callers that cannot allocate device memory: code running inside a CUDA
  * stream capture, or under a memory manager that owns all device memory and forbids the library
@@ -203,6 +228,9 @@ int dnl_get_stream(dnl_handle *h, void **stream);
  * dnl_timer_elapsed waits for `to` and returns the milliseconds between the two marks. */
 int dnl_timer_mark(dnl_handle *h, int slot);
 int dnl_timer_elapsed(dnl_handle *h, int from, int to, double *ms);
+/* NVTX ranges around a caller's region (profilers can restrict capture to it) */
+int dnl_range_push(const char *name);
+int dnl_range_pop(void);
 /* FP64 fused multiply-add throughput of the current device, measured by a dependent-chain kernel
  * over all SMs (TFLOP/s, 2 flops per DFMA) */
 int dnl_measure_fp64_peak(double *tflops);

@@ -1134,6 +1134,11 @@ int dnlo_set(dnlo *h, const char *nm, double value)
   if (!strcmp(nm, "dt")) h->timeStep = value;
   else if (!strcmp(nm, "time")) h->currentTime = value;
   else if (!strcmp(nm, "up_time")) h->upTime = value;
+  else if (!strcmp(nm, "increment")) h->increment = (long)value;
+  else if (!strcmp(nm, "computed_dt")) h->computedTimeStep = value;
+  else if (!strcmp(nm, "last_dt")) h->lastTimeStep = value;
+  else if (!strcmp(nm, "ts_date")) h->tsDate = value;
+  else if (!strcmp(nm, "last_ts_date")) h->lastTsDate = value;
   else return DNLO_ERR_ARG;
   return 0;
 }

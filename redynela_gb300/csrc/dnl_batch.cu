@@ -1,0 +1,474 @@
+// Batched explicit dynamics: many independent meshes (e.g. Taylor bars of different sizes and
+// materials) advanced together.
+//
+// The meshes are concatenated into one union mesh (node and element indices offset per instance)
+// stored in an ordinary handle, plus an instance index per element and per node, a material and
+// integration constants per instance and one time record per instance (each instance has its own
+// time step, increment counter and end).  A step is the same five kernels as the single-mesh path,
+// each launched once for all instances: time logic (one thread per instance), boundary conditions,
+// element pass, assembly + nodal update, and every `frequency` increments the Courant reduction
+// into each instance's minimum.  Small meshes that could not fill the GPU alone share its SMs, and
+// the per-step launch cost is paid once for the batch; `dnl_batch_step_graph` captures a run of
+// steps into a CUDA graph and replays it.
+//
+// Tile autotuning: the element pass is launched with 64, 128 or 256 threads per block (16, 32 or
+// 64 axisymmetric elements per block); `dnl_batch_autotune` times live steps with each and keeps
+// the fastest.  Every element's arithmetic is independent of the block size, so the choice does
+// not change results.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "dnl_common.cuh"
+
+using namespace dnl;
+
+struct dnl_batch {
+  int count;
+  dnl_handle *h;  // union mesh
+  int *elemInst, *nodeInst;
+  Material *mats;
+  InstParams *prm;
+  DevTime *tms;
+  std::vector<int> nodeOff, elemOff;  // count+1 offsets
+  std::vector<InstParams> hprm;
+  int freq;
+  int block;
+  long long increment;  // host copy (all instances advance in lockstep until they finish)
+  bool prologueDone;
+  struct Graph {
+    int nsteps, parity, phase;
+    cudaGraphExec_t exec;
+    long long kernels;
+  } graphs[8];
+  int ngraphs;
+};
+
+namespace {
+
+char g_batchError[256] = "";
+
+#define BK(call)                                                                                 \
+  do {                                                                                           \
+    cudaError_t err_ = (call);                                                                   \
+    if (err_ != cudaSuccess) {                                                                   \
+      snprintf(g_batchError, sizeof g_batchError, "%s: %s", #call, cudaGetErrorString(err_));   \
+      return DNL_ERR_CUDA;                                                                       \
+    }                                                                                            \
+  } while (0)
+
+enum { BT_FORCE = 1, BT_POST = 2, BT_PRE = 4 };  // same modes as the single-mesh time kernel
+
+int read_tms(dnl_batch *b, std::vector<DevTime> &t)
+{
+  t.resize(b->count);
+  BK(cudaMemcpyAsync(t.data(), b->tms, sizeof(DevTime) * b->count, cudaMemcpyDeviceToHost, b->h->stream));
+  BK(cudaStreamSynchronize(b->h->stream));
+  return 0;
+}
+
+int first_status(const std::vector<DevTime> &t, int *inst)
+{
+  for (size_t i = 0; i < t.size(); i++)
+    if (t[i].status) {
+      if (inst) *inst = (int)i;
+      return t[i].status;
+    }
+  return 0;
+}
+
+int enqueue_batch_step(dnl_batch *b, long long incAfter, bool last)
+{
+  dnl_handle *h = b->h;
+  int r;
+  if ((r = launch_bc_batch(h, b->tms, b->nodeInst))) return r;
+  ElemArgs a = elem_args_of(h);
+  prof_begin(h, h->stream);
+  r = launch_elem_batch(h->etype, b->block, a, b->elemInst, b->mats, b->tms, h->stream);
+  prof_end(h, DNL_PROF_ELEM, h->stream);
+  if (r) return r;
+  if ((r = launch_node_batch(h, b->nodeInst, b->prm, b->tms))) return r;
+  h->cur = 1 - h->cur;
+  if (incAfter % b->freq == 0) {
+    ElemArgs c = elem_args_of(h);
+    prof_begin(h, h->stream);
+    r = launch_courant_batch(c, b->elemInst, b->tms, h->stream);
+    prof_end(h, DNL_PROF_COURANT, h->stream);
+    if (r) return r;
+  }
+  return launch_dt_batch(h, b->tms, b->prm, b->count, last ? BT_POST : (BT_POST | BT_PRE));
+}
+
+}  // namespace
+
+extern "C" {
+
+int dnl_batch_destroy(dnl_batch *b)
+{
+  if (!b) return DNL_ERR_ARG;
+  for (int i = 0; i < b->ngraphs; i++) cudaGraphExecDestroy(b->graphs[i].exec);
+  void *ptrs[] = {b->elemInst, b->nodeInst, b->mats, b->prm, b->tms};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (b->h) dnl_destroy(b->h);
+  delete b;
+  return 0;
+}
+
+int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material *mats,
+                     const dnl_solver_params *sps, dnl_batch **out)
+{
+  if (!out || count <= 0 || !meshes || !mats || !sps) return DNL_ERR_ARG;
+  *out = nullptr;
+  const int etype = meshes[0].etype;
+  const int nen = etype == DNL_ELQUA4NAX ? 4 : 8;
+  for (int i = 0; i < count; i++) {
+    if (meshes[i].etype != etype) return DNL_ERR_ARG;
+    if (sps[i].method != DNL_COURANT || etype != DNL_ELQUA4NAX) return DNL_ERR_ARG;
+    if (sps[i].frequency != sps[0].frequency || (sps[i].frequency % 2)) return DNL_ERR_ARG;
+    if (meshes[i].num_nodes <= 0 || meshes[i].num_elements <= 0) return DNL_ERR_ARG;
+  }
+  // ---- the union mesh
+  std::vector<int> nodeOff(count + 1, 0), elemOff(count + 1, 0);
+  for (int i = 0; i < count; i++) {
+    nodeOff[i + 1] = nodeOff[i] + meshes[i].num_nodes;
+    elemOff[i + 1] = elemOff[i] + meshes[i].num_elements;
+  }
+  const int N = nodeOff[count], E = elemOff[count];
+  std::vector<double> coords(3 * (size_t)N);
+  std::vector<int> conn((size_t)nen * E), elemInst(E), nodeInst(N);
+  std::vector<int> bcKind, bcStart(1, 0), bcNodes;
+  std::vector<double> bcVal;
+  for (int i = 0; i < count; i++) {
+    const dnl_mesh_desc &m = meshes[i];
+    memcpy(&coords[3 * (size_t)nodeOff[i]], m.coords, sizeof(double) * 3 * m.num_nodes);
+    for (long q = 0; q < (long)m.num_elements * nen; q++) {
+      if (m.conn[q] < 0 || m.conn[q] >= m.num_nodes) return DNL_ERR_ARG;
+      conn[(size_t)elemOff[i] * nen + q] = m.conn[q] + nodeOff[i];
+    }
+    for (int e = 0; e < m.num_elements; e++) elemInst[elemOff[i] + e] = i;
+    for (int n = 0; n < m.num_nodes; n++) nodeInst[nodeOff[i] + n] = i;
+    for (int g = 0; g < m.num_bc; g++) {
+      bcKind.push_back(m.bc_kind[g]);
+      for (int c = 0; c < 3; c++) bcVal.push_back(m.bc_val[3 * g + c]);
+      for (int q = m.bc_start[g]; q < m.bc_start[g + 1]; q++) {
+        if (m.bc_nodes[q] < 0 || m.bc_nodes[q] >= m.num_nodes) return DNL_ERR_ARG;
+        bcNodes.push_back(m.bc_nodes[q] + nodeOff[i]);
+      }
+      bcStart.push_back((int)bcNodes.size());
+    }
+  }
+  dnl_mesh_desc u;
+  memset(&u, 0, sizeof u);
+  u.etype = etype;
+  u.num_nodes = N;
+  u.num_elements = E;
+  u.coords = coords.data();
+  u.conn = conn.data();
+  for (int c = 0; c < 3; c++) u.v0[c] = meshes[0].v0[c];
+  u.num_bc = (int)bcKind.size();
+  u.bc_kind = bcKind.data();
+  u.bc_val = bcVal.data();
+  u.bc_start = bcStart.data();
+  u.bc_nodes = bcNodes.data();
+  dnl_solver_params sp0 = sps[0];
+  dnl_handle *h = nullptr;
+  int r = dnl_create(&u, &mats[0], &sp0, &h);
+  if (r) return r;
+  dnl_batch *b = new dnl_batch();
+  b->count = count;
+  b->h = h;
+  b->nodeOff = nodeOff;
+  b->elemOff = elemOff;
+  b->freq = sps[0].frequency;
+  b->block = 128;
+  b->ngraphs = 0;
+  b->increment = 0;
+  b->prologueDone = false;
+  *out = b;
+  auto fail = [&](int code) {
+    dnl_batch_destroy(b);
+    *out = nullptr;
+    return code;
+  };
+#define BKF(call)                                                                                \
+  do {                                                                                           \
+    cudaError_t err_ = (call);                                                                   \
+    if (err_ != cudaSuccess) {                                                                   \
+      snprintf(g_batchError, sizeof g_batchError, "%s: %s", #call, cudaGetErrorString(err_));   \
+      return fail(DNL_ERR_CUDA);                                                                 \
+    }                                                                                            \
+  } while (0)
+  // ---- per-instance constants, in the reference's expressions (as dnl_create)
+  std::vector<Material> hm(count);
+  b->hprm.resize(count);
+  std::vector<DevTime> ht(count);
+  for (int i = 0; i < count; i++) {
+    Material &m = hm[i];
+    m.young = mats[i].young;
+    m.nu = mats[i].poisson;
+    m.rho = mats[i].density;
+    m.A = mats[i].A;
+    m.B = mats[i].B;
+    m.n = mats[i].n;
+    m.K = m.young / (3. * (1. - 2. * m.nu));
+    const double G = m.young / (2. * (1. + m.nu));
+    m.G2 = 2.0 * G;
+    m.G3 = 3.0 * G;
+    m.nB = m.n * m.B;
+    m.dfun0 = kSqrt32 * 2.0 * G;
+    double ro = 0.;
+    for (int k = 0; k < 4; k++) ro += m.rho;
+    ro /= 4;
+    const double Nu = m.nu;
+    m.Cs = sqrt((m.young * (1 - Nu)) / (ro * (1 + Nu) * (1 - 2 * Nu)));
+    const double rb = sps[i].rho_b;
+    InstParams &p = b->hprm[i];
+    p.alphaM = (2.0 * rb - 1.0) / (1.0 + rb);
+    p.beta = (5.0 - 3.0 * rb) / ((1.0 + rb) * (1.0 + rb) * (2.0 - rb));
+    p.gamma = 1.5 - p.alphaM;
+    const double omegaS = sqrt((12.0 * pow((1 + rb), 3) * (2.0 - rb)) /
+                               (10 + 15 * rb - rb * rb + pow(rb, 3) - pow(rb, 4)));
+    p.safetyOmega = sps[i].safety * omegaS;
+    p.Cs = m.Cs;
+    p.freq = sps[i].frequency;
+    p.method = DNL_COURANT;
+    DevTime &t = ht[i];
+    memset(&t, 0, sizeof t);
+    t.upTime = t.endTime = sps[i].end_time;
+    t.lenMinBits = 0x7ff0000000000000ull;
+    t.badElem = -1;
+  }
+  BKF(cudaMalloc(&b->elemInst, sizeof(int) * E));
+  BKF(cudaMalloc(&b->nodeInst, sizeof(int) * N));
+  BKF(cudaMalloc(&b->mats, sizeof(Material) * count));
+  BKF(cudaMalloc(&b->prm, sizeof(InstParams) * count));
+  BKF(cudaMalloc(&b->tms, sizeof(DevTime) * count));
+  BKF(cudaMemcpy(b->elemInst, elemInst.data(), sizeof(int) * E, cudaMemcpyHostToDevice));
+  BKF(cudaMemcpy(b->nodeInst, nodeInst.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+  BKF(cudaMemcpy(b->mats, hm.data(), sizeof(Material) * count, cudaMemcpyHostToDevice));
+  BKF(cudaMemcpy(b->prm, b->hprm.data(), sizeof(InstParams) * count, cudaMemcpyHostToDevice));
+  BKF(cudaMemcpy(b->tms, ht.data(), sizeof(DevTime) * count, cudaMemcpyHostToDevice));
+  // ---- per-instance initial speed (both fields) and cached evp^n at evp = 1e-10
+  {
+    std::vector<double> v(N);
+    for (int c = 0; c < 3; c++) {
+      for (int i = 0; i < count; i++)
+        for (int n = nodeOff[i]; n < nodeOff[i + 1]; n++) v[n] = meshes[i].v0[c];
+      for (int bk = 0; bk < 2; bk++)
+        BKF(cudaMemcpy(h->bank[bk].v[c], v.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+    }
+    const size_t nIP = (size_t)E * h->nip;
+    std::vector<double> pn(nIP);
+    for (int i = 0; i < count; i++) {
+      const double val = pow(1e-10, mats[i].n);
+      for (size_t q = (size_t)elemOff[i] * h->nip; q < (size_t)elemOff[i + 1] * h->nip; q++) pn[q] = val;
+    }
+    const int ns = 4;
+    BKF(cudaMemcpy(h->ip + (size_t)(3 * ns + 2) * nIP, pn.data(), sizeof(double) * nIP, cudaMemcpyHostToDevice));
+  }
+  BKF(cudaDeviceSynchronize());
+#undef BKF
+  return 0;
+}
+
+int dnl_batch_prologue(dnl_batch *b)
+{
+  if (!b) return DNL_ERR_ARG;
+  if (b->prologueDone) return 0;
+  dnl_handle *h = b->h;
+  double *me;
+  BK(cudaMalloc(&me, sizeof(double) * (size_t)h->E * h->nen));
+  ElemArgs a = elem_args_of(h);
+  int r = launch_mass_batch(h->etype, a, me, b->elemInst, b->mats, h->stream);
+  if (!r) r = launch_gather_mass(h, me);
+  if (r) {
+    cudaFree(me);
+    return r;
+  }
+  BK(cudaStreamSynchronize(h->stream));
+  cudaFree(me);
+  // computeInternalForces with the initial (zero) Current field, then computeTimeStep(True)
+  a = elem_args_of(h);
+  if ((r = launch_elem_batch(h->etype, b->block, a, b->elemInst, b->mats, b->tms, h->stream))) return r;
+  if ((r = launch_courant_batch(a, b->elemInst, b->tms, h->stream))) return r;
+  if ((r = launch_dt_batch(h, b->tms, b->prm, b->count, BT_FORCE))) return r;
+  std::vector<DevTime> t;
+  if ((r = read_tms(b, t))) return r;
+  b->prologueDone = true;
+  return first_status(t, nullptr);
+}
+
+int dnl_batch_step(dnl_batch *b, int nsteps, int *active)
+{
+  if (active) *active = 0;
+  if (!b || nsteps < 0) return DNL_ERR_ARG;
+  int r;
+  if (!b->prologueDone && (r = dnl_batch_prologue(b))) return r;
+  dnl_handle *h = b->h;
+  if (nsteps > 0) {
+    const long long inc0 = b->increment;
+    if ((r = launch_dt_batch(h, b->tms, b->prm, b->count, BT_PRE))) return r;
+    for (int s = 0; s < nsteps; s++)
+      if ((r = enqueue_batch_step(b, inc0 + s + 1, s == nsteps - 1))) return r;
+    b->increment += nsteps;
+  }
+  std::vector<DevTime> t;
+  if ((r = read_tms(b, t))) return r;
+  int n = 0;
+  for (auto &x : t) n += !x.done;
+  if (active) *active = n;
+  return first_status(t, nullptr);
+}
+
+int dnl_batch_step_graph(dnl_batch *b, int nsteps, int *active)
+{
+  if (active) *active = 0;
+  if (!b || nsteps <= 0) return DNL_ERR_ARG;
+  int r;
+  if (!b->prologueDone && (r = dnl_batch_prologue(b))) return r;
+  dnl_handle *h = b->h;
+  const long long inc0 = b->increment;
+  const int parity = h->cur, phase = (int)(inc0 % b->freq);
+  cudaGraphExec_t exec = nullptr;
+  for (int i = 0; i < b->ngraphs; i++)
+    if (b->graphs[i].nsteps == nsteps && b->graphs[i].parity == parity && b->graphs[i].phase == phase)
+      exec = b->graphs[i].exec;
+  if (!exec) {
+    cudaGraph_t graph;
+    const long long k0 = launch_counter();
+    BK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int rr = launch_dt_batch(h, b->tms, b->prm, b->count, BT_PRE);
+    for (int s = 0; s < nsteps && !rr; s++) rr = enqueue_batch_step(b, inc0 + s + 1, s == nsteps - 1);
+    cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+    if (rr) return rr;
+    if (ce != cudaSuccess) {
+      snprintf(g_batchError, sizeof g_batchError, "graph capture: %s", cudaGetErrorString(ce));
+      return DNL_ERR_CUDA;
+    }
+    BK(cudaGraphInstantiate(&exec, graph, 0));
+    cudaGraphDestroy(graph);
+    const long long kernels = launch_counter() - k0;
+    launch_counter() = k0;
+    if (b->ngraphs < 8) b->graphs[b->ngraphs++] = dnl_batch::Graph{nsteps, parity, phase, exec, kernels};
+  } else {
+    h->cur = (nsteps % 2) ? 1 - parity : parity;
+  }
+  for (int i = 0; i < b->ngraphs; i++)
+    if (b->graphs[i].exec == exec) launch_counter() += b->graphs[i].kernels;
+  BK(cudaGraphLaunch(exec, h->stream));
+  b->increment += nsteps;
+  std::vector<DevTime> t;
+  if ((r = read_tms(b, t))) return r;
+  int n = 0;
+  for (auto &x : t) n += !x.done;
+  if (active) *active = n;
+  bool cached = false;
+  for (int i = 0; i < b->ngraphs; i++) cached |= b->graphs[i].exec == exec;
+  if (!cached) cudaGraphExecDestroy(exec);
+  return first_status(t, nullptr);
+}
+
+int dnl_batch_autotune(dnl_batch *b, int steps_per_candidate, int *block)
+{
+  if (!b || steps_per_candidate <= 0) return DNL_ERR_ARG;
+  int r;
+  if (!b->prologueDone && (r = dnl_batch_prologue(b))) return r;
+  const int cands[3] = {64, 128, 256};
+  double best = 1e300;
+  int bestB = b->block;
+  cudaEvent_t e0, e1;
+  BK(cudaEventCreate(&e0));
+  BK(cudaEventCreate(&e1));
+  for (int c = 0; c < 3; c++) {
+    b->block = cands[c];
+    BK(cudaEventRecord(e0, b->h->stream));
+    int active = 0;
+    if ((r = dnl_batch_step(b, steps_per_candidate, &active))) break;
+    BK(cudaEventRecord(e1, b->h->stream));
+    BK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    BK(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best) {
+      best = ms;
+      bestB = cands[c];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->block = bestB;
+  for (int i = 0; i < b->ngraphs; i++) cudaGraphExecDestroy(b->graphs[i].exec);
+  b->ngraphs = 0;
+  if (block) *block = bestB;
+  return r;
+}
+
+int dnl_batch_set_block(dnl_batch *b, int block)
+{
+  if (!b || (block != 64 && block != 128 && block != 256)) return DNL_ERR_ARG;
+  b->block = block;
+  for (int i = 0; i < b->ngraphs; i++) cudaGraphExecDestroy(b->graphs[i].exec);
+  b->ngraphs = 0;
+  return 0;
+}
+
+int dnl_batch_time_info(dnl_batch *b, int inst, dnl_time_info *info)
+{
+  if (!b || !info || inst < 0 || inst >= b->count) return DNL_ERR_ARG;
+  std::vector<DevTime> t;
+  int r = read_tms(b, t);
+  if (r) return r;
+  const DevTime &x = t[inst];
+  info->time = x.currentTime;
+  info->time_step = x.timeStep;
+  info->computed_step = x.computedTimeStep;
+  info->kinetic = 0.;
+  info->increment = x.increment;
+  info->done = x.done;
+  info->status = x.status;
+  info->bad_element = x.badElem >= 0 ? x.badElem - b->elemOff[inst] : -1;
+  return 0;
+}
+
+int dnl_batch_get_coords(dnl_batch *b, int inst, double *coords)
+{
+  if (!b || !coords || inst < 0 || inst >= b->count) return DNL_ERR_ARG;
+  dnl_handle *h = b->h;
+  const int n0 = b->nodeOff[inst], n1 = b->nodeOff[inst + 1];
+  std::vector<double> c(n1 - n0);
+  BK(cudaStreamSynchronize(h->stream));
+  for (int r = 0; r < 3; r++) {
+    BK(cudaMemcpy(c.data(), h->x[r] + n0, sizeof(double) * (n1 - n0), cudaMemcpyDeviceToHost));
+    for (int n = 0; n < n1 - n0; n++) coords[3 * (size_t)n + r] = c[n];
+  }
+  return 0;
+}
+
+int dnl_batch_get_fint(dnl_batch *b, int inst, double *fint)
+{
+  if (!b || !fint || inst < 0 || inst >= b->count) return DNL_ERR_ARG;
+  dnl_handle *h = b->h;
+  BK(cudaStreamSynchronize(h->stream));
+  BK(cudaMemcpy(fint, h->fint + (size_t)h->dim * b->nodeOff[inst],
+                sizeof(double) * h->dim * (b->nodeOff[inst + 1] - b->nodeOff[inst]),
+                cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int dnl_batch_sizes(dnl_batch *b, int *elements, int *nodes)
+{
+  if (!b) return DNL_ERR_ARG;
+  if (elements) *elements = b->h->E;
+  if (nodes) *nodes = b->h->N;
+  return 0;
+}
+
+int dnl_batch_handle(dnl_batch *b, dnl_handle **h)
+{
+  if (!b || !h) return DNL_ERR_ARG;
+  *h = b->h;
+  return 0;
+}
+
+}  // extern "C"

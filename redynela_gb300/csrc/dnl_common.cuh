@@ -114,6 +114,12 @@ struct NodeArgs {
   double alphaM, beta, gamma;
 };
 
+// per-instance constants of a batch
+struct InstParams {
+  double alphaM, beta, gamma, safetyOmega, Cs;
+  int freq, method;
+};
+
 // ------------------------------------------------------------------------ handle
 struct GraphEntry {
   int nsteps, parity, phase;
@@ -176,6 +182,17 @@ int launch_courant(dnl_handle *h, cudaStream_t s);
 int launch_pulse(dnl_handle *h, cudaStream_t s);
 void set_shape_tables();
 long long &launch_counter();
+// batched launches (dnl_batch.cu)
+int launch_elem_batch(int etype, int block, const ElemArgs &a, const int *elemInst,
+                      const Material *mats, DevTime *tms, cudaStream_t s);
+int launch_mass_batch(int etype, const ElemArgs &a, double *me, const int *elemInst,
+                      const Material *mats, cudaStream_t s);
+int launch_courant_batch(const ElemArgs &a, const int *elemInst, DevTime *tms, cudaStream_t s);
+ElemArgs elem_args_of(dnl_handle *h);
+int launch_node_batch(dnl_handle *h, const int *nodeInst, const InstParams *prm, DevTime *tms);
+int launch_dt_batch(dnl_handle *h, DevTime *tms, const InstParams *prm, int count, int mode);
+int launch_bc_batch(dnl_handle *h, DevTime *tms, const int *nodeInst);
+int launch_gather_mass(dnl_handle *h, const double *me);
 // launches on caller-built arguments (no handle)
 int launch_elem_raw(int etype, const ElemArgs &a, cudaStream_t s);
 int launch_gather_raw(int dim, const GatherArgs &g, cudaStream_t s);

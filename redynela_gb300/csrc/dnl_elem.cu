@@ -106,6 +106,27 @@ __device__ __forceinline__ void record_error(DevTime *tm, int code, int e)
   if (atomicCAS(&tm->status, 0, code) == 0) tm->badElem = e;
 }
 
+// |a| > |b| and |a| < |b| on the bit patterns (finite doubles): integer compares keep them off the
+// FP64 pipe, which on GB300 issues 2 thread-instructions per SM per cycle.
+__device__ __forceinline__ unsigned long long abits(double a)
+{
+  return (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ bool abs_gt(double a, double b) { return abits(a) > abits(b); }
+
+// 1/x by Newton-Raphson (r <- r + r (1 - x r), quadratic convergence) from the PTX hardware seed
+// rcp.approx.ftz.f64; two steps give the double result to about an ulp (not correctly rounded).
+// For normal, finite, non-zero x.
+__device__ __forceinline__ double nr_rcp(double x)
+{
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}
+
 // ----------------------------------------------------------------------------- Jacobi rotation
 // One rotation of Tensor2::polarDecomposeLnU (Tensor2.C:1183-1240) on pivot (P, Q): f <- R^T f R
 // with R the plane rotation (c, s), written with the reference's association order and its exact
@@ -139,46 +160,44 @@ __device__ __forceinline__ void jacobi_rotate(double f[3][3], double rot[3][3], 
   }
 }
 
-// Rotation angle of Tensor2.C:1195-1208, IEEE operations in the reference's order.
+// Rotation angle of Tensor2.C:1195-1208.  With d = C_qq - C_pp and e = 2 C_pq the reference's
+// t = 1 / (alpha + sign(alpha) sqrt(alpha^2 + 1)), alpha = d / e, is
+// t = sign(d e) |e| / (|d| + sqrt(d^2 + e^2)) (t = 1 when d = 0); then c = 1/sqrt(1 + t^2),
+// s = t c.  One square root, one division and one reciprocal square root instead of two of each:
+// the same angle to a few ulps, which moves the rotated diagonal by less than an ulp of its
+// stationary value.
 __device__ __forceinline__ void jacobi_angle(double fpp, double fqq, double fpq, double &c, double &s)
 {
-  const double alpha = RSUB(fqq, fpp) / RMUL(2., fpq);
+  const double d = RSUB(fqq, fpp), e = RMUL(2., fpq);
   double t;
-  if (alpha != 0.) {
-    const double r = sqrt(RADD(RMUL(alpha, alpha), 1.));
-    t = 1. / RADD(alpha, alpha > 0. ? r : -r);
+  if (d != 0.) {
+    const double ae = fabs(e);
+    t = ae / (fabs(d) + sqrt(fma(d, d, e * e)));
+    if ((d < 0.) != (e < 0.)) t = -t;
   } else {
     t = 1.;
   }
-  c = 1. / (sqrt(RADD(1., RMUL(t, t))));
-  s = RMUL(t, c);
+  c = rsqrt(fma(t, t, 1.));
+  s = t * c;
 }
 
 // ----------------------------------------------------------------------------- element kernel
+// One Gauss point of one element: lane `pt` of the NIP adjacent lanes that hold element e.  All
+// lanes of a warp must call it (the pressure average and the force sum are warp-collective);
+// lanes with valid == false compute on a clamped element and store nothing.  `red` is this
+// element's NIP x NEN*DIM slice of shared memory; `m` and `tm` are the element's material and
+// time/status record (one per mesh, or per instance in a batch).
 template <int ET>
-__global__ void __launch_bounds__(128) k_elem(ElemArgs a)
+__device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, DevTime *tm, int e,
+                                        int pt, bool valid, int lane, double *red)
 {
   using T = Elem<ET>;
   using L = IpLayout<ET>;
   using SH = Shape<ET>;
   constexpr int NIP = T::NIP, NEN = T::NEN, DIM = T::DIM, NS = T::NS;
   constexpr bool AXI = ET == DNL_ELQUA4NAX;
-  constexpr int EPW = 32 / NIP;  // elements per warp
-
-  __shared__ double red[128 / 32][EPW][NIP][NEN * DIM];
-
-  if (a.gate && (a.tm->done | a.tm->status)) return;
-  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int warpFirstE = (gtid & ~31) / NIP;
-  if (warpFirstE >= a.E) return;
-  const int eRaw = gtid / NIP;
-  const bool valid = eRaw < a.E;
-  const int e = valid ? eRaw : a.E - 1;
-  const int pt = gtid % NIP;
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, slot = lane / NIP;
   const long nIP = (long)a.E * NIP;
   const long ipx = (long)e * NIP + pt;
-  const Material &m = a.mat;
 
   int node[NEN];
 #pragma unroll
@@ -210,7 +229,7 @@ __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
     Ji[0][1] = -J[0][1] * r;
     Ji[1][0] = -J[1][0] * r;
     Ji[1][1] = J[0][0] * r;
-    if (detJ < 0. && valid) record_error(a.tm, DNL_ERR_NEG_DETJ, e);
+    if (detJ < 0. && valid) record_error(tm, DNL_ERR_NEG_DETJ, e);
   } else {
     const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
     const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
@@ -226,7 +245,7 @@ __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
     Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
     Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
     Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
-    if (detJ == 0. && valid) record_error(a.tm, DNL_ERR_SINGULAR, e);
+    if (detJ == 0. && valid) record_error(tm, DNL_ERR_SINGULAR, e);
   }
 
   // ---- F = I + sum_k dN_k (x) du_k (Current field), diagonal accumulated onto 1 in node order
@@ -287,12 +306,12 @@ __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
       p = 0;
       q = 1;
     } else {
-      q = (fabs(f[0][1]) > fabs(f[0][2]) ? 1 : 2);
-      p = (fabs(q == 1 ? f[0][1] : f[0][2]) > fabs(f[1][2]) ? 0 : 1);
+      q = abs_gt(f[0][1], f[0][2]) ? 1 : 2;
+      p = abs_gt(q == 1 ? f[0][1] : f[0][2], f[1][2]) ? 0 : 1;
       if (p == 1) q = 2;
     }
     const double fpq = p == 0 ? (q == 1 ? f[0][1] : f[0][2]) : f[1][2];
-    if (fabs(fpq) < kPolarPrecision) {
+    if (abits(fpq) < abits(kPolarPrecision)) {
       conv = true;
       break;
     }
@@ -308,7 +327,7 @@ __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
       jacobi_rotate<1, 2>(f, rot, c, s);
     }
   }
-  if (!conv && valid) record_error(a.tm, DNL_ERR_JACOBI_NOCONV, e);
+  if (!conv && valid) record_error(tm, DNL_ERR_JACOBI_NOCONV, e);
 
   // ---- ln U = sum ln(l)/2 v v^T,  R = F sum l^-1/2 v v^T
   double dE[3][3], Rr[3][3];
@@ -380,7 +399,7 @@ __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
   }
   const double trace = dE[0][0] + dE[1][1] + dE[2][2];
   {
-    const double tr3 = trace / 3.0;
+    const double tr3 = trace * (1.0 / 3.0);
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -404,19 +423,19 @@ __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
     const double Sigv0 = RADD(m.A, RMUL(m.B, evpn));
     if (Strial > Sigv0) {
       plastic = true;
-      double h = m.nB * (evpn / evp);
-      double gamma = (normS - kSqrt23 * Sigv0) / (m.G2 * (1.0 + h / m.G3));
+      double h = m.nB * evpn * nr_rcp(evp);
+      double gamma = (normS - kSqrt23 * Sigv0) / (m.G2 * fma(h, 1.0 / m.G3, 1.0));
       double xn = evpn;
       int iteration = 0;
       for (;;) {
         const double xv = RADD(evp, RMUL(kSqrt23, gamma));
         xn = exp(m.n * log(xv));  // xv^n
         const double Sigv = RADD(m.A, RMUL(m.B, xn));
-        h = m.nB * (xn / xv);  // n B xv^(n-1)
+        h = m.nB * xn * nr_rcp(xv);  // n B xv^(n-1)
         const double dfun = fma(kSqrt23, h, m.dfun0);
         const double fun = dfun * gamma - ((Strial - Sigv) + h * kSqrt23 * gamma);
-        if (fabs(fun / Sigv) > kRadialReturnPrecision) {
-          double dgamma = -fun / dfun;
+        if (fabs(fun) > kRadialReturnPrecision * Sigv) {  // |fun / Sigv| > 1e-8, Sigv > 0
+          double dgamma = -fun * nr_rcp(dfun);
           if (dgamma < 0 && fabs(dgamma) > gamma) dgamma = -gamma * 0.9;
           gamma += dgamma;
         } else {
@@ -424,7 +443,7 @@ __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
         }
         iteration++;
         if (iteration > kRadialReturnMaxIt) {
-          if (valid) record_error(a.tm, DNL_ERR_RR_NOCONV, e);
+          if (valid) record_error(tm, DNL_ERR_RR_NOCONV, e);
           break;
         }
       }
@@ -452,7 +471,7 @@ __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
     const int base = lane - pt;
 #pragma unroll
     for (int k = 0; k < NIP; k++) pressure += __shfl_sync(0xffffffffu, trace, base + k);
-    pressure /= NIP;
+    pressure *= 1.0 / NIP;  // exact: NIP is a power of two
   }
   const double p = fma(m.K, pressure, a.ip[L::P * nIP + ipx]);
 
@@ -490,7 +509,14 @@ __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
   };
   rfi(S);
   rfi(Ep);
-  rfi(Epl);
+  {  // a point that never yielded has EpsPlas = 0 exactly, and R 0 R^T = 0
+    unsigned long long nz = 0;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = i; j < 3; j++) nz |= abits(Epl[i][j]);
+    if (nz) rfi(Epl);
+  }
 
   if (valid) {
     const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
@@ -530,12 +556,12 @@ __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
       double s = 0.;
 #pragma unroll
       for (int j = 0; j < DIM; j++) {
-        const double sig = S[j][i] + (i == j ? p : 0.);
+        const double sig = i == j ? S[j][i] + p : S[j][i];
         s = fma(Ji[l][j], sig, s);
       }
       M[l][i] = s * W;
     }
-  double *row = red[wib][slot][pt];
+  double *row = red + pt * (NEN * DIM);
 #pragma unroll
   for (int k = 0; k < NEN; k++)
 #pragma unroll
@@ -553,17 +579,55 @@ __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
     for (int i = 0; i < DIM; i++) {
       double s = 0.0;
 #pragma unroll
-      for (int q = 0; q < NIP; q++) s -= red[wib][slot][q][pt * DIM + i];
+      for (int q = 0; q < NIP; q++) s -= red[q * (NEN * DIM) + pt * DIM + i];
       a.fe[(long)i * a.E * NEN + (long)e * NEN + pt] = s;
     }
   }
+}
+
+template <int ET>
+__global__ void __launch_bounds__(128) k_elem(ElemArgs a)
+{
+  constexpr int NIP = Elem<ET>::NIP, NEN = Elem<ET>::NEN, DIM = Elem<ET>::DIM;
+  constexpr int EPW = 32 / NIP;  // elements per warp
+  __shared__ double red[128 / 32][EPW][NIP * NEN * DIM];
+  if (a.gate && (a.tm->done | a.tm->status)) return;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((gtid & ~31) / NIP >= a.E) return;
+  const int eRaw = gtid / NIP;
+  const bool valid = eRaw < a.E;
+  const int lane = threadIdx.x & 31;
+  elem_ip<ET>(a, a.mat, a.tm, valid ? eRaw : a.E - 1, gtid % NIP, valid, lane,
+              red[threadIdx.x >> 5][lane / NIP]);
+}
+
+// Batched element pass over the union of many meshes: element e belongs to instance inst[e],
+// whose material and time record are mats[inst] and tms[inst]; instances that have finished or
+// failed keep their lanes in the warp but store nothing.
+template <int ET, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_elem_batch(ElemArgs a, const int *elemInst,
+                                                      const Material *mats, DevTime *tms)
+{
+  constexpr int NIP = Elem<ET>::NIP, NEN = Elem<ET>::NEN, DIM = Elem<ET>::DIM;
+  constexpr int EPW = 32 / NIP;
+  __shared__ double red[BLOCK / 32][EPW][NIP * NEN * DIM];
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((gtid & ~31) / NIP >= a.E) return;
+  const int eRaw = gtid / NIP;
+  const int e = eRaw < a.E ? eRaw : a.E - 1;
+  const int inst = elemInst[e];
+  DevTime *tm = tms + inst;
+  const bool valid = eRaw < a.E && !(tm->done | tm->status);
+  const int lane = threadIdx.x & 31;
+  elem_ip<ET>(a, mats[inst], tm, e, gtid % NIP, valid, lane, red[threadIdx.x >> 5][lane / NIP]);
 }
 
 // ----------------------------------------------------------------------------- mass kernel
 // Element::computeMassMatrix with the reference's rounding: M_k = sum_pt (rho N_k) W,
 // W = detJ (2 pi R).  Writes me[e*NEN + k]; Domain::computeMassMatrix's assembly is the gather.
 template <int ET>
-__global__ void __launch_bounds__(128) k_mass(ElemArgs a, double *me)
+__global__ void __launch_bounds__(128) k_mass(ElemArgs a, double *me, const int *elemInst,
+                                              const Material *mats)
 {
   using T = Elem<ET>;
   using SH = Shape<ET>;
@@ -608,7 +672,8 @@ __global__ void __launch_bounds__(128) k_mass(ElemArgs a, double *me)
   double W = detJ;  // weight 1
   if (AXI) W = RMUL(W, RMUL(RMUL(2., kPi), Rad));
 #pragma unroll
-  for (int k = 0; k < NEN; k++) red[wib][slot][pt][k] = RMUL(RMUL(a.mat.rho, SH::N(pt, k)), W);
+  const double rho = elemInst ? mats[elemInst[e]].rho : a.mat.rho;
+  for (int k = 0; k < NEN; k++) red[wib][slot][pt][k] = RMUL(RMUL(rho, SH::N(pt, k)), W);
   __syncwarp();
   if (valid) {
     double s = 0.;
@@ -649,6 +714,39 @@ __global__ void __launch_bounds__(256) k_courant(ElemArgs a)
     double b = wmin[0];
     for (int w = 1; w < (int)(blockDim.x >> 5); w++) b = fmin(b, wmin[w]);
     atomicMin(&a.tm->lenMinBits, (unsigned long long)__double_as_longlong(b));
+  }
+}
+
+// Batched Courant lengths: each element folds its length into its instance's minimum; a warp whose
+// lanes all belong to one instance reduces first and issues one atomic.
+__global__ void __launch_bounds__(256) k_courant_batch(ElemArgs a, const int *elemInst, DevTime *tms)
+{
+  const int eRaw = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((eRaw & ~31) >= a.E) return;
+  const int e = eRaw < a.E ? eRaw : a.E - 1;
+  const int inst = elemInst[e];
+  DevTime *tm = tms + inst;
+  double len = 1e300;
+  if (eRaw < a.E && !(tm->done | tm->status)) {
+    const int n0 = a.conn[e], n1 = a.conn[a.E + e], n2 = a.conn[2L * a.E + e], n3 = a.conn[3L * a.E + e];
+    const double x31 = RSUB(a.x[0][n2], a.x[0][n0]), x24 = RSUB(a.x[0][n1], a.x[0][n3]);
+    const double y42 = RSUB(a.x[1][n3], a.x[1][n1]), y31 = RSUB(a.x[1][n2], a.x[1][n0]);
+    const double num = RADD(RMUL(x31, y42), RMUL(x24, y31));
+    const double sq = RADD(RADD(RADD(RMUL(x24, x24), RMUL(y42, y42)), RMUL(x31, x31)), RMUL(y31, y31));
+    len = num / sqrt(RMUL(2., sq));
+    if (!(len > 0.)) {
+      record_error(tm, DNL_ERR_DT, e);
+      len = 1e300;
+    }
+  }
+  const int first = __shfl_sync(0xffffffffu, inst, 0);
+  if (__all_sync(0xffffffffu, inst == first)) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) len = fmin(len, __shfl_xor_sync(0xffffffffu, len, o));
+    if ((threadIdx.x & 31) == 0 && len < 1e300)
+      atomicMin(&tm->lenMinBits, (unsigned long long)__double_as_longlong(len));
+  } else if (len < 1e300) {
+    atomicMin(&tm->lenMinBits, (unsigned long long)__double_as_longlong(len));
   }
 }
 
@@ -707,12 +805,53 @@ int launch_mass(dnl_handle *h, cudaStream_t s, double *me)
   const long threads = (long)h->E * h->nip;
   const int grid = (int)((threads + 127) / 128);
   if (h->etype == DNL_ELQUA4NAX)
-    k_mass<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a, me);
+    k_mass<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a, me, nullptr, nullptr);
   else
-    k_mass<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a, me);
+    k_mass<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a, me, nullptr, nullptr);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
+
+int launch_elem_batch(int etype, int block, const ElemArgs &a, const int *elemInst,
+                      const Material *mats, DevTime *tms, cudaStream_t s)
+{
+  const long threads = (long)a.E * (etype == DNL_ELQUA4NAX ? 4 : 8);
+  const int grid = (int)((threads + block - 1) / block);
+#define DNL_EB(ET, B) k_elem_batch<ET, B><<<grid, B, 0, s>>>(a, elemInst, mats, tms)
+  if (etype == DNL_ELQUA4NAX) {
+    if (block == 64) DNL_EB(DNL_ELQUA4NAX, 64);
+    else if (block == 256) DNL_EB(DNL_ELQUA4NAX, 256);
+    else DNL_EB(DNL_ELQUA4NAX, 128);
+  } else {
+    if (block == 64) DNL_EB(DNL_ELHEX8N3D, 64);
+    else DNL_EB(DNL_ELHEX8N3D, 128);
+  }
+#undef DNL_EB
+  launch_counter()++;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
+}
+
+int launch_mass_batch(int etype, const ElemArgs &a, double *me, const int *elemInst,
+                      const Material *mats, cudaStream_t s)
+{
+  const long threads = (long)a.E * (etype == DNL_ELQUA4NAX ? 4 : 8);
+  const int grid = (int)((threads + 127) / 128);
+  if (etype == DNL_ELQUA4NAX)
+    k_mass<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a, me, elemInst, mats);
+  else
+    k_mass<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a, me, elemInst, mats);
+  launch_counter()++;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
+}
+
+int launch_courant_batch(const ElemArgs &a, const int *elemInst, DevTime *tms, cudaStream_t s)
+{
+  k_courant_batch<<<(a.E + 255) / 256, 256, 0, s>>>(a, elemInst, tms);
+  launch_counter()++;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
+}
+
+ElemArgs elem_args_of(dnl_handle *h) { return elem_args(h); }
 
 int launch_courant(dnl_handle *h, cudaStream_t s)
 {

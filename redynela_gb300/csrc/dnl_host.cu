@@ -20,6 +20,8 @@
 #include <cstring>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "dnl_common.cuh"
 
 using namespace dnl;
@@ -79,14 +81,11 @@ __device__ __forceinline__ void apply_bc(int code, const double *spd, double dt,
   }
 }
 
+// one node of the Chung-Hulbert update; dt and the integration constants of its mesh
 template <int DIM>
-__global__ void __launch_bounds__(256) k_node(NodeArgs g)
+__device__ __forceinline__ void node_update(const NodeArgs &g, int n, double dt, double alphaM,
+                                            double beta, double gamma)
 {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= g.N) return;
-  DevTime *tm = g.tm;
-  if (tm->done | tm->status) return;
-  const double dt = tm->timeStep;
   double cdu[3], cv[3], ca[3], cd[3], ndu[3], nv[3], na[3], nd[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
@@ -96,7 +95,7 @@ __global__ void __launch_bounds__(256) k_node(NodeArgs g)
     cd[i] = g.cur.disp[i][n];
   }
   // computePredictions
-  const double c1 = RMUL(dt, RSUB(0.5, g.beta)), c2 = RMUL(dt, RSUB(1., g.gamma));
+  const double c1 = RMUL(dt, RSUB(0.5, beta)), c2 = RMUL(dt, RSUB(1., gamma));
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     ndu[i] = RMUL(RADD(RMUL(ca[i], c1), cv[i]), dt);
@@ -129,11 +128,11 @@ __global__ void __launch_bounds__(256) k_node(NodeArgs g)
   const double m = g.mass[n];
 #pragma unroll
   for (int c = 0; c < DIM; c++) na[c] = f[c] / m;
-  const double cg = RMUL(dt, g.gamma), cb = RMUL(RMUL(dt, dt), g.beta);
-  const double oma = RSUB(1.0, g.alphaM);
+  const double cg = RMUL(dt, gamma), cb = RMUL(RMUL(dt, dt), beta);
+  const double oma = RSUB(1.0, alphaM);
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    na[i] = RSUB(na[i], RMUL(g.alphaM, ca[i]));
+    na[i] = RSUB(na[i], RMUL(alphaM, ca[i]));
     na[i] = na[i] / oma;
     nv[i] = RADD(nv[i], RMUL(cg, na[i]));
     ndu[i] = RADD(ndu[i], RMUL(cb, na[i]));
@@ -150,12 +149,38 @@ __global__ void __launch_bounds__(256) k_node(NodeArgs g)
   }
 }
 
-// Current-field writes of the constant boundary conditions before the element pass
+template <int DIM>
+__global__ void __launch_bounds__(256) k_node(NodeArgs g)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= g.N) return;
+  DevTime *tm = g.tm;
+  if (tm->done | tm->status) return;
+  node_update<DIM>(g, n, tm->timeStep, g.alphaM, g.beta, g.gamma);
+}
+
+// batched: node n belongs to instance nodeInst[n] with its own time record and constants
+template <int DIM>
+__global__ void __launch_bounds__(256) k_node_batch(NodeArgs g, const int *nodeInst,
+                                                    const InstParams *prm, DevTime *tms)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= g.N) return;
+  const int i = nodeInst[n];
+  const DevTime *tm = tms + i;
+  if (tm->done | tm->status) return;
+  node_update<DIM>(g, n, tm->timeStep, prm[i].alphaM, prm[i].beta, prm[i].gamma);
+}
+
+// Current-field writes of the constant boundary conditions before the element pass; in a batch
+// node n's time record is tm[nodeInst[n]], otherwise tm[0]
 __global__ void k_bc_current(int nb, const int *nodes, const int *code, const double *speed,
-                             NodeFields cur, DevTime *tm)
+                             NodeFields cur, DevTime *tmBase, const int *nodeInst)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nb || (tm->done | tm->status)) return;
+  if (i >= nb) return;
+  const DevTime *tm = tmBase + (nodeInst ? nodeInst[nodes[i]] : 0);
+  if (tm->done | tm->status) return;
   const int n = nodes[i];
   const double dt = tm->timeStep;
   const int cd = code[i];
@@ -190,41 +215,39 @@ __device__ __forceinline__ bool in_bounds(const DevTime *tm)
   return tm->currentTime >= tm->startTime && tm->currentTime < up;
 }
 
-__device__ void recompute_dt(const DtArgs &a)
+__device__ void recompute_dt(DevTime *tm, int method, double safetyOmega, double Cs)
 {
-  DevTime *tm = a.tm;
   double fmax;
-  if (a.method == DNL_COURANT) {
-    const double crit = __longlong_as_double((long long)tm->lenMinBits) / a.Cs;
+  if (method == DNL_COURANT) {
+    const double crit = __longlong_as_double((long long)tm->lenMinBits) / Cs;
     fmax = 2.0 / crit;
     tm->lenMinBits = 0x7ff0000000000000ull;  // +inf for the next reduction
   } else {
     fmax = tm->fmax;
   }
-  tm->timeStep = a.safetyOmega / fmax;
+  tm->timeStep = safetyOmega / fmax;
   tm->lastTsDate = tm->tsDate;
   tm->lastTimeStep = tm->computedTimeStep;
   tm->tsDate = tm->currentTime;
   tm->computedTimeStep = tm->timeStep;
 }
 
-__global__ void k_dt(DtArgs a)
+__device__ void dt_update(DevTime *tm, int mode, int freq, int method, double safetyOmega, double Cs)
 {
-  DevTime *tm = a.tm;
   if (tm->status) return;
-  if (a.mode & DT_FORCE) recompute_dt(a);
-  if ((a.mode & DT_POST) && !tm->done) {
+  if (mode & DT_FORCE) recompute_dt(tm, method, safetyOmega, Cs);
+  if ((mode & DT_POST) && !tm->done) {
     tm->currentTime = RADD(tm->currentTime, tm->timeStep);  // ExplicitSolverCH::updateTime
     if (!in_bounds(tm)) {
       tm->done = 1;
-    } else if (tm->increment % a.freq == 0) {
-      recompute_dt(a);
+    } else if (tm->increment % freq == 0) {
+      recompute_dt(tm, method, safetyOmega, Cs);
     } else if (tm->tsDate != tm->lastTsDate) {  // LINEARdbl extrapolation (Math.h:91)
       const double dx = RSUB(tm->currentTime, tm->lastTsDate) / RSUB(tm->tsDate, tm->lastTsDate);
       tm->timeStep = RADD(RMUL(dx, tm->computedTimeStep), RMUL(RSUB(1.0, dx), tm->lastTimeStep));
     }
   }
-  if ((a.mode & DT_PRE) && !tm->done) {
+  if ((mode & DT_PRE) && !tm->done) {
     if (!in_bounds(tm)) {
       tm->done = 1;
     } else {
@@ -237,6 +260,18 @@ __global__ void k_dt(DtArgs a)
     tm->status = DNL_ERR_DT;
     tm->badElem = -1;
   }
+}
+
+__global__ void k_dt(DtArgs a)
+{
+  dt_update(a.tm, a.mode, a.freq, a.method, a.safetyOmega, a.Cs);
+}
+
+__global__ void k_dt_batch(DevTime *tms, const InstParams *prm, int count, int mode)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  dt_update(tms + i, mode, prm[i].freq, prm[i].method, prm[i].safetyOmega, prm[i].Cs);
 }
 
 // node-major (x,y,z) host layout <-> component arrays on the device
@@ -388,7 +423,8 @@ int launch_bc_current(dnl_handle *h)
   if (!h->nbcNodes) return 0;
   prof_begin(h, h->stream);
   k_bc_current<<<(h->nbcNodes + 127) / 128, 128, 0, h->stream>>>(h->nbcNodes, h->bcNodeList, h->bcCode,
-                                                                  h->bcSpeed, h->bank[h->cur], h->tm);
+                                                                  h->bcSpeed, h->bank[h->cur], h->tm,
+                                                                  nullptr);
   prof_end(h, DNL_PROF_OTHER, h->stream);
   launch_counter()++;
   return check_launch();
@@ -433,6 +469,63 @@ int enqueue_step(dnl_handle *h, long long incAfter, bool last)
 }  // namespace
 
 namespace dnl {
+int launch_node_batch(dnl_handle *h, const int *nodeInst, const InstParams *prm, DevTime *tms)
+{
+  NodeArgs g;
+  g.N = h->N;
+  g.EN = h->E * h->nen;
+  g.start = h->n2eStart;
+  g.entry = h->n2e;
+  g.fe = h->fe;
+  g.mass = h->mass;
+  g.cur = h->bank[h->cur];
+  g.nxt = h->bank[1 - h->cur];
+  for (int i = 0; i < 3; i++) g.x[i] = h->x[i];
+  g.bcIdx = h->bcIdx;
+  g.bcCode = h->bcCode;
+  g.bcSpeed = h->bcSpeed;
+  g.fint = h->fint;
+  g.tm = nullptr;
+  g.alphaM = g.beta = g.gamma = 0.;
+  const int grid = (h->N + 255) / 256;
+  prof_begin(h, h->stream);
+  if (h->dim == 2)
+    k_node_batch<2><<<grid, 256, 0, h->stream>>>(g, nodeInst, prm, tms);
+  else
+    k_node_batch<3><<<grid, 256, 0, h->stream>>>(g, nodeInst, prm, tms);
+  prof_end(h, DNL_PROF_NODE, h->stream);
+  launch_counter()++;
+  return check_launch();
+}
+
+int launch_dt_batch(dnl_handle *h, DevTime *tms, const InstParams *prm, int count, int mode)
+{
+  prof_begin(h, h->stream);
+  k_dt_batch<<<(count + 127) / 128, 128, 0, h->stream>>>(tms, prm, count, mode);
+  prof_end(h, DNL_PROF_OTHER, h->stream);
+  launch_counter()++;
+  return check_launch();
+}
+
+int launch_bc_batch(dnl_handle *h, DevTime *tms, const int *nodeInst)
+{
+  if (!h->nbcNodes) return 0;
+  prof_begin(h, h->stream);
+  k_bc_current<<<(h->nbcNodes + 127) / 128, 128, 0, h->stream>>>(h->nbcNodes, h->bcNodeList, h->bcCode,
+                                                                  h->bcSpeed, h->bank[h->cur], tms,
+                                                                  nodeInst);
+  prof_end(h, DNL_PROF_OTHER, h->stream);
+  launch_counter()++;
+  return check_launch();
+}
+
+int launch_gather_mass(dnl_handle *h, const double *me)
+{
+  k_gather1<<<(h->N + 255) / 256, 256, 0, h->stream>>>(h->N, h->n2eStart, h->n2e, me, h->mass);
+  launch_counter()++;
+  return check_launch();
+}
+
 int launch_gather_raw(int dim, const GatherArgs &g, cudaStream_t s)
 {
   const int grid = (g.N + 255) / 256;
@@ -592,6 +685,18 @@ int dnl_measure_fp64_peak(double *tflops)
   cudaFree(out);
   const double flops = 2.0 * 8.0 * iters * (double)threads * blocks;
   *tflops = flops / (ms * 1e-3) / 1e12;
+  return 0;
+}
+
+int dnl_range_push(const char *name)
+{
+  nvtxRangePushA(name ? name : "dnl");
+  return 0;
+}
+
+int dnl_range_pop(void)
+{
+  nvtxRangePop();
   return 0;
 }
 

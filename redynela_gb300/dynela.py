@@ -115,6 +115,20 @@ def lib():
         L.dnl_set_device.argtypes = [C.c_int]
         L.dnl_host_alloc.argtypes = [C.c_ulonglong, C.POINTER(C.c_void_p)]
         L.dnl_host_free.argtypes = [C.c_void_p]
+        L.dnl_range_push.argtypes = [C.c_char_p]
+        L.dnl_batch_create.argtypes = [C.c_int, C.POINTER(MeshDesc), C.POINTER(MaterialDesc),
+                                       C.POINTER(SolverParams), C.POINTER(H)]
+        L.dnl_batch_destroy.argtypes = [H]
+        L.dnl_batch_prologue.argtypes = [H]
+        L.dnl_batch_step.argtypes = [H, C.c_int, _ip]
+        L.dnl_batch_step_graph.argtypes = [H, C.c_int, _ip]
+        L.dnl_batch_autotune.argtypes = [H, C.c_int, _ip]
+        L.dnl_batch_set_block.argtypes = [H, C.c_int]
+        L.dnl_batch_time_info.argtypes = [H, C.c_int, C.POINTER(TimeInfo)]
+        L.dnl_batch_get_coords.argtypes = [H, C.c_int, _dp]
+        L.dnl_batch_get_fint.argtypes = [H, C.c_int, _dp]
+        L.dnl_batch_sizes.argtypes = [H, _ip, _ip]
+        L.dnl_batch_handle.argtypes = [H, C.POINTER(H)]
         _lib = L
     return _lib
 
@@ -133,6 +147,14 @@ def set_device(device: int) -> None:
     rc = lib().dnl_set_device(int(device))
     if rc:
         raise DnlError(rc, lib().dnl_error_string(rc).decode())
+
+
+def range_push(name: str) -> None:
+    lib().dnl_range_push(name.encode())
+
+
+def range_pop() -> None:
+    lib().dnl_range_pop()
 
 
 def fp64_peak_tflops() -> float:
@@ -320,6 +342,116 @@ class GpuDomain:
         t = TimeInfo()
         self._check(self.L.dnl_get_time_info(self.h, C.byref(t)))
         return {k: getattr(t, k) for k, _ in TimeInfo._fields_}
+
+
+class _HandleView(GpuDomain):
+    """Timer/profiling access to a handle owned by someone else (a batch's union mesh)."""
+
+    def __init__(self, h, model):  # noqa: D401 -- no dnl_create
+        self.h = h
+        self.L = lib()
+        self.model = model
+
+    def close(self):
+        self.h = None
+
+
+class BatchDomain:
+    """Many meshes advanced together (dnl_batch_*)."""
+
+    def __init__(self, models: Sequence[Model]):
+        L = lib()
+        if device_count() < 1:
+            raise RuntimeError("libdnlgpu: no CUDA device")
+        self.models = list(models)
+        n = len(self.models)
+        descs = (MeshDesc * n)()
+        mats = (MaterialDesc * n)()
+        sps = (SolverParams * n)()
+        self._keep = []
+        for i, m in enumerate(self.models):
+            coords = np.ascontiguousarray(m.coords, dtype=np.float64)
+            conn = np.ascontiguousarray(m.conn, dtype=np.int32)
+            kinds = np.array([g.kind for g in m.bcs] or [0], dtype=np.int32)
+            vals = np.array([list(g.val) for g in m.bcs] or [[0.0, 0.0, 0.0]], dtype=np.float64)
+            starts = np.zeros(len(m.bcs) + 1, dtype=np.int32)
+            for j, g in enumerate(m.bcs):
+                starts[j + 1] = starts[j] + len(g.nodes)
+            nodes = (np.concatenate([np.asarray(g.nodes) for g in m.bcs]).astype(np.int32)
+                     if m.bcs else np.zeros(1, dtype=np.int32))
+            self._keep += [coords, conn, kinds, vals, starts, nodes]
+            descs[i] = MeshDesc(m.etype, m.N, m.E, coords.ctypes.data_as(_dp),
+                                conn.ctypes.data_as(_ip), (C.c_double * 3)(*m.v0), len(m.bcs),
+                                kinds.ctypes.data_as(_ip), vals.ctypes.data_as(_dp),
+                                starts.ctypes.data_as(_ip), nodes.ctypes.data_as(_ip))
+            mats[i] = MaterialDesc(m.young, m.poisson, m.density, m.A, m.B, m.n)
+            sps[i] = SolverParams(m.tend, m.rho_b, m.safety, int(m.freq), int(m.method), 0)
+        h = C.c_void_p()
+        rc = L.dnl_batch_create(n, descs, mats, sps, C.byref(h))
+        if rc:
+            raise DnlError(rc, L.dnl_error_string(rc).decode())
+        self.h = h
+        self.L = L
+        E, N = C.c_int(0), C.c_int(0)
+        L.dnl_batch_sizes(h, C.byref(E), C.byref(N))
+        self.E, self.N = E.value, N.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.dnl_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc:
+            raise DnlError(rc, self.L.dnl_error_string(rc).decode())
+
+    def prologue(self):
+        self._check(self.L.dnl_batch_prologue(self.h))
+
+    def step(self, n: int) -> int:
+        act = C.c_int(0)
+        self._check(self.L.dnl_batch_step(self.h, int(n), C.byref(act)))
+        return act.value
+
+    def step_graph(self, n: int) -> int:
+        act = C.c_int(0)
+        self._check(self.L.dnl_batch_step_graph(self.h, int(n), C.byref(act)))
+        return act.value
+
+    def autotune(self, steps: int = 3) -> int:
+        b = C.c_int(0)
+        self._check(self.L.dnl_batch_autotune(self.h, int(steps), C.byref(b)))
+        return b.value
+
+    def set_block(self, block: int):
+        self._check(self.L.dnl_batch_set_block(self.h, int(block)))
+
+    def time_info(self, i: int) -> dict:
+        t = TimeInfo()
+        self._check(self.L.dnl_batch_time_info(self.h, int(i), C.byref(t)))
+        return {k: getattr(t, k) for k, _ in TimeInfo._fields_}
+
+    def coords(self, i: int) -> np.ndarray:
+        out = np.zeros((self.models[i].N, 3))
+        self._check(self.L.dnl_batch_get_coords(self.h, int(i), _ptr(out)))
+        return out
+
+    def fint(self, i: int) -> np.ndarray:
+        out = np.zeros(self.models[i].N * self.models[i].dim)
+        self._check(self.L.dnl_batch_get_fint(self.h, int(i), _ptr(out)))
+        return out
+
+    def handle_view(self) -> GpuDomain:
+        """Timer marks / profiling on the batch's stream."""
+        hh = C.c_void_p()
+        self._check(self.L.dnl_batch_handle(self.h, C.byref(hh)))
+        return _HandleView(hh, self.models[0])
 
 
 # ====================================================================== deck-level mirror
