@@ -209,6 +209,27 @@ typedef struct {
 } dnl_static_args;
 int dnl_internal_forces_static(const dnl_static_args *args, void *stream, int *bad_element);
 
+/* ------------------------------------------------------------------- sensitivities */
+/* Derivatives of a run's final nodal coordinates with respect to four parameters: the hardening
+ * law's A, B, n (sigma_y = A + B evp^n, IsoHardElastoplastic.C:171-184) and the magnitude |v0| of
+ * the initial velocity v0 = |v0| u (BoundarySpeed::applyInitial_V0, Boundary.C:378-385).  The run
+ * is ExplicitSolverCH::solve's loop (ExplicitSolverCH.C:179-274) with the step sizes taken from a
+ * caller's schedule (a parameter-independent dt sequence) instead of Solver::computeTimeStep, from
+ * the handle's initial state (no step taken yet); the end time is not applied.  Computed in
+ * forward mode (four tangent copies of the state advanced with it), which for four parameters
+ * stores no trajectory.  No counterpart in the reference, which has no derivatives. */
+#define DNL_SENS_NPARAM 4 /* A, B, n, |v0| */
+/* nsteps steps with step sizes dts[0..nsteps); coords (3N, node-major, may be NULL) receives the
+ * final coordinates, dcoords (4 x 3N, may be NULL) their derivatives, dcoords[p*3N + 3n + j] */
+int dnl_sens_run(dnl_handle *h, int nsteps, const double *dts, double *coords, double *dcoords);
+/* step-size schedule used by dnl_adjoint */
+int dnl_set_dt_schedule(dnl_handle *h, const double *dts, int nsteps);
+/* gradient of L(x_final) for a given dL/dx_final (3N): grad[p] = sum dL/dx . dx/dp, p = A, B, n,
+ * |v0|, over the schedule set by dnl_set_dt_schedule.  ckpt_stride (>= 0) is accepted for
+ * interface compatibility with checkpointed reverse-mode adjoints and unused: the forward mode
+ * keeps no checkpoints. */
+int dnl_adjoint(dnl_handle *h, const double *dL_dx, double *grad, int ckpt_stride);
+
 /* -------------------------------------------------------------------------- measurement */
 /* Per-kernel device time: between dnl_profile_begin and dnl_profile_end the library brackets each
  * of its launches on the handle's stream with CUDA events; dnl_profile_end synchronises and returns

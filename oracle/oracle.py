@@ -14,13 +14,18 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
+SENS_PATH = os.path.join(HERE, "libsens.so")
 
 _lib = None
+_sens = None
+
+
+def _stale(out, src):
+    return not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(os.path.join(HERE, src))
 
 
 def build(force: bool = False) -> str:
-    if force or not os.path.exists(LIB_PATH) or \
-            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "dnl_oracle.c")):
+    if force or _stale(LIB_PATH, "dnl_oracle.c") or _stale(SENS_PATH, "dnl_sens.cc"):
         subprocess.run(["make", "-C", HERE, "port"], check=True, capture_output=True)
     return LIB_PATH
 
@@ -168,3 +173,81 @@ class Oracle:
         self.array("p")[:] = np.asarray(p).ravel()
         self.array("evp")[:] = np.asarray(evp).ravel()
         self.set("dt", dt)
+
+
+def sens_lib():
+    global _sens
+    if _sens is None:
+        build()
+        L = C.CDLL(SENS_PATH)
+        dp, lp = C.POINTER(C.c_double), C.POINTER(C.c_long)
+        L.dnls_create.restype = C.c_void_p
+        L.dnls_create.argtypes = [C.c_int, C.c_long, C.c_long, dp, lp, dp, dp, dp, C.c_long, lp, dp,
+                                  lp, lp, C.c_double]
+        L.dnls_destroy.argtypes = [C.c_void_p]
+        L.dnls_run.argtypes = [C.c_void_p, C.c_long, dp]
+        L.dnls_coords.argtypes = [C.c_void_p, dp, dp]
+        _sens = L
+    return _sens
+
+
+def _bc_arrays(m):
+    kinds = np.array([g.kind for g in m.bcs] or [0], dtype=np.int64)
+    vals = np.array([list(g.val) for g in m.bcs] or [[0, 0, 0]], dtype=np.float64).ravel()
+    starts = np.zeros(len(m.bcs) + 1, dtype=np.int64)
+    for i, g in enumerate(m.bcs):
+        starts[i + 1] = starts[i] + len(g.nodes)
+    nodes = np.concatenate([np.asarray(g.nodes, dtype=np.int64) for g in m.bcs]) if m.bcs \
+        else np.zeros(1, dtype=np.int64)
+    return kinds, vals, starts, nodes
+
+
+PARAMS = ("A", "B", "n", "v0")
+
+
+class SensOracle:
+    """Forward-mode sensitivities on the CPU (oracle/dnl_sens.cc): a run with a prescribed
+    step-size schedule, carrying d/dp for p = (A, B, n, |v0|) in FP64 dual numbers."""
+
+    def __init__(self, model, mass=None, threads: int = 0):
+        L = sens_lib()
+        if threads:
+            lib().dnlo_set_threads(int(threads))
+        m = model
+        if mass is None:
+            o = Oracle(m)
+            o.prologue()
+            mass = o.array("mass").copy()
+        coords = np.ascontiguousarray(m.coords, dtype=np.float64)
+        conn = np.ascontiguousarray(m.conn, dtype=np.int64)
+        mat = np.array([m.young, m.poisson, m.density, m.A, m.B, m.n], dtype=np.float64)
+        v0 = np.array(m.v0, dtype=np.float64)
+        mass = np.ascontiguousarray(mass, dtype=np.float64)
+        kinds, vals, starts, nodes = _bc_arrays(m)
+        self._keep = (coords, conn, mat, v0, mass, kinds, vals, starts, nodes)
+        self.h = L.dnls_create(m.etype, m.N, m.E, _dp(coords), _lp(conn), _dp(mat), _dp(v0),
+                               _dp(mass), len(m.bcs), _lp(kinds), _dp(vals), _lp(starts),
+                               _lp(nodes), float(m.rho_b))
+        if not self.h:
+            raise ValueError("dnls_create rejected the model")
+        self.model = m
+        self.L = L
+
+    def run(self, dts):
+        dts = np.ascontiguousarray(dts, dtype=np.float64)
+        r = self.L.dnls_run(self.h, len(dts), _dp(dts))
+        if r:
+            raise OracleError(r, -1)
+
+    def coords(self):
+        """(coords (N, 3), d coords / dp (4, N, 3))"""
+        m = self.model
+        x = np.zeros((m.N, 3))
+        dx = np.zeros((4, m.N, 3))
+        self.L.dnls_coords(self.h, _dp(x), _dp(dx))
+        return x, dx
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.dnls_destroy(self.h)
+            self.h = None

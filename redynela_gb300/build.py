@@ -19,8 +19,11 @@ OBJDIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libdnlgpu.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE,
-         "--expt-relaxed-constexpr"]
+# Host code: no contraction of a*b+c into fused multiply-adds (GCC's default on aarch64), so the
+# host-side constants (material moduli, integration parameters) round as the reference's x86
+# build and identically in every translation unit.
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+         "-I" + INCLUDE, "--expt-relaxed-constexpr"]
 
 
 def _sources():
@@ -29,7 +32,7 @@ def _sources():
 
 def _deps():
     return _sources() + sorted(glob.glob(os.path.join(CSRC, "*.cuh"))) + \
-        [os.path.join(INCLUDE, "dnl_gpu.h")]
+        [os.path.join(INCLUDE, "dnl_gpu.h"), os.path.abspath(__file__)]
 
 
 def _stale(target, deps):
@@ -39,9 +42,15 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+# Element kernels: no implicit multiply-add contraction on the device either; the source writes every
+# fused multiply-add it wants as fma(), so each instantiation of the shared element code rounds the
+# same way whatever the inlining context.
+FILE_FLAGS = {"dnl_elem.cu": ["-fmad=false"]}
+
+
 def _compile(src):
     obj = os.path.join(OBJDIR, os.path.basename(src) + ".o")
-    cmd = [NVCC] + ARCH + FLAGS + ["-c", src, "-o", obj]
+    cmd = [NVCC] + ARCH + FLAGS + FILE_FLAGS.get(os.path.basename(src), []) + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed on {src}:\n{r.stderr}")

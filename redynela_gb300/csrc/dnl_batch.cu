@@ -205,24 +205,7 @@ int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material 
   b->hprm.resize(count);
   std::vector<DevTime> ht(count);
   for (int i = 0; i < count; i++) {
-    Material &m = hm[i];
-    m.young = mats[i].young;
-    m.nu = mats[i].poisson;
-    m.rho = mats[i].density;
-    m.A = mats[i].A;
-    m.B = mats[i].B;
-    m.n = mats[i].n;
-    m.K = m.young / (3. * (1. - 2. * m.nu));
-    const double G = m.young / (2. * (1. + m.nu));
-    m.G2 = 2.0 * G;
-    m.G3 = 3.0 * G;
-    m.nB = m.n * m.B;
-    m.dfun0 = kSqrt32 * 2.0 * G;
-    double ro = 0.;
-    for (int k = 0; k < 4; k++) ro += m.rho;
-    ro /= 4;
-    const double Nu = m.nu;
-    m.Cs = sqrt((m.young * (1 - Nu)) / (ro * (1 + Nu) * (1 - 2 * Nu)));
+    hm[i] = make_material(mats[i]);
     const double rb = sps[i].rho_b;
     InstParams &p = b->hprm[i];
     p.alphaM = (2.0 * rb - 1.0) / (1.0 + rb);
@@ -231,7 +214,7 @@ int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material 
     const double omegaS = sqrt((12.0 * pow((1 + rb), 3) * (2.0 - rb)) /
                                (10 + 15 * rb - rb * rb + pow(rb, 3) - pow(rb, 4)));
     p.safetyOmega = sps[i].safety * omegaS;
-    p.Cs = m.Cs;
+    p.Cs = hm[i].Cs;
     p.freq = sps[i].frequency;
     p.method = DNL_COURANT;
     DevTime &t = ht[i];

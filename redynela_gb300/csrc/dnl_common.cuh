@@ -42,6 +42,37 @@ template <int ET> struct IpLayout {
                        EVPN = 3 * NS + 2, NCOMP = 3 * NS + 3;
 };
 
+// Per-integration-point record of the element pass that the tangent pass (forward-mode
+// sensitivities) reads back, component-major [slot][E*NIP].
+template <int ET> struct TapeLayout {
+  static constexpr int DIM = Elem<ET>::DIM, NS = Elem<ET>::NS;
+  static constexpr int JI = 0;              // J^-1 [l][c], DIM x DIM
+  static constexpr int DETJ = JI + DIM * DIM;
+  static constexpr int RAD = DETJ + 1;      // axisymmetric radius of the Gauss point
+  static constexpr int F = RAD + 1;         // F [r][c], 3 x 3
+  static constexpr int V = F + 9;           // eigenvectors of C = F^T F (columns), 3 x 3
+  static constexpr int LAM = V + 9;         // eigenvalues of C
+  static constexpr int LG = LAM + 3;        // ln(l) / 2
+  static constexpr int IL = LG + 3;         // l^-1/2
+  static constexpr int R = IL + 3;          // rotation, 3 x 3
+  static constexpr int STR = R + 9;         // trial deviator (symmetric components)
+  static constexpr int NORMS = STR + NS;    // its norm
+  static constexpr int GAM = NORMS + 1;     // plastic multiplier (0: elastic step)
+  static constexpr int XV = GAM + 1;        // evp + sqrt(2/3) gamma
+  static constexpr int XN = XV + 1;         // XV^n
+  static constexpr int SPRE = XN + 1;       // S, Eps, EpsPlas before the RFI rotation
+  static constexpr int EPRE = SPRE + NS;
+  static constexpr int PPRE = EPRE + NS;
+  static constexpr int NT = PPRE + NS;
+};
+
+// Tangent integration-point state per parameter direction: [dir][comp][E*NIP]
+template <int ET> struct TanLayout {
+  static constexpr int NS = Elem<ET>::NS;
+  static constexpr int S = 0, EPS = NS, EPSP = 2 * NS, P = 3 * NS, EVP = 3 * NS + 1, NCOMP = 3 * NS + 2;
+};
+constexpr int kSensParams = 4;  // A, B, n, |v0|
+
 // ------------------------------------------------------------------------ device time state
 // Mirrors the Solver / Domain members that drive ExplicitSolverCH::solve.
 struct DevTime {
@@ -71,7 +102,35 @@ struct Material {
   double nB;         // n B
   double dfun0;      // Sqrt32 * 2.0 * G, first term of dfun      (Element.C:309)
   double Cs;         // Courant sound speed with the mean nodal density (Element.C:607-621)
+  double rG3;        // 1 / (3 G), for the first radial-return guess (Element.C:298)
 };
+
+// Material constants from the ABI description, in the reference's expressions.
+#include <math.h>
+inline Material make_material(const dnl_material &mt)
+{
+  Material m;
+  m.young = mt.young;
+  m.nu = mt.poisson;
+  m.rho = mt.density;
+  m.A = mt.A;
+  m.B = mt.B;
+  m.n = mt.n;
+  m.K = m.young / (3. * (1. - 2. * m.nu));
+  const double G = m.young / (2. * (1. + m.nu));
+  m.G2 = 2.0 * G;
+  m.G3 = 3.0 * G;
+  m.nB = m.n * m.B;
+  m.dfun0 = kSqrt32 * 2.0 * G;
+  m.rG3 = 1.0 / m.G3;
+  // ElQua4nAx::getLength's sound speed uses the mean of the four nodal densities
+  double ro = 0.;
+  for (int i = 0; i < 4; i++) ro += m.rho;
+  ro /= 4;
+  const double Nu = m.nu;
+  m.Cs = sqrt((m.young * (1 - Nu)) / (ro * (1 + Nu) * (1 - 2 * Nu)));
+  return m;
+}
 
 struct NodeFields {  // one NodalField bank, SoA, 3 components each
   double *du[3], *v[3], *a[3], *disp[3];
@@ -87,6 +146,24 @@ struct ElemArgs {
   double *fe;          // element forces [DIM][E*NEN]
   double *detJ;        // [E*NIP] (written)
   double *stepT;       // optional dEps|R per IP, [18][E*NIP] or nullptr
+  double *tape;        // [TapeLayout::NT][E*NIP], written by the tape instance of k_elem
+  DevTime *tm;
+  Material mat;
+};
+
+// Tangent element pass: the primal pass's inputs and record, the tangents of its inputs
+// (coordinates and Current delta_disp, [dir][3][N]) and of the integration-point state.
+struct SensElemArgs {
+  int E, N;
+  const int *conn;
+  const double *x[3];
+  const double *du[3];
+  const double *ip;    // integration-point state after the primal pass
+  const double *tape;  // [TapeLayout::NT][E*NIP]
+  const double *tx;    // [dir][3][N]
+  const double *tdu;   // [dir][3][N]
+  double *tip;         // [dir][TanLayout::NCOMP][E*NIP]
+  double *tfe;         // [dir][DIM][E*NEN]
   DevTime *tm;
   Material mat;
 };
@@ -172,11 +249,21 @@ struct dnl_handle {
   // per-kernel event timing (dnl_profile_begin/end)
   bool profiling;
   void *prof;
+  // forward-mode sensitivities (dnl_sens.cu)
+  double v0dir[3];            // unit vector of the initial velocity
+  void *sens;
 };
 
 namespace dnl {
 // launchers implemented in dnl_elem.cu
 int launch_elem(dnl_handle *h, cudaStream_t s, int gate);
+int launch_elem_tape(dnl_handle *h, cudaStream_t s, double *tape);
+int launch_elem_tan(int etype, const SensElemArgs &a, cudaStream_t s);
+void sens_free(dnl_handle *h);
+// primal per-step launches (dnl_host.cu) used by the sensitivity run
+int enqueue_bc_current(dnl_handle *h);
+int enqueue_node(dnl_handle *h);
+int read_time_state(dnl_handle *h, DevTime *t);
 int launch_mass(dnl_handle *h, cudaStream_t s, double *me);
 int launch_courant(dnl_handle *h, cudaStream_t s);
 int launch_pulse(dnl_handle *h, cudaStream_t s);

@@ -15,13 +15,16 @@
 // integration-point state, stored component-major, is read and written with coalesced accesses.
 //
 // Rounding: GB300 executes FP64 at a small fraction of its other rates, so the kernels are written
-// to minimise FP64 instructions and let the compiler fuse multiply-adds -- except along the chain
+// to minimise FP64 instructions with explicit fused multiply-adds (this file is compiled with
+// -fmad=false: the compiler fuses nothing by itself, so every instantiation of the element code --
+// single mesh, batch, tape, caller-allocated -- rounds identically) -- except along the chain
 // whose last bits decide the strain increment: F = I + sum dN du is accumulated onto 1 with
 // separately rounded products and sums, and C = F^T F, the Jacobi rotation angle and the rotated
 // diagonal use __dmul_rn/__dadd_rn in the reference's association order, so the eigenvalues that
 // enter ln(U) carry the same rounding as the reference.  Elsewhere results differ from the
 // reference by a few units in the last place.
 #include <cstdio>
+#include <cstring>
 
 #include "dnl_common.cuh"
 
@@ -70,6 +73,12 @@ __device__ __forceinline__ int sgx(int k) { return (k ^ (k >> 1)) & 1; }
 __device__ __forceinline__ int sgy(int k) { return (k >> 1) & 1; }
 __device__ __forceinline__ int sgz(int k) { return (k >> 2) & 1; }
 
+// -x on the bit pattern (integer pipe, not FP64).
+__device__ __forceinline__ double flip_sign(double a)
+{
+  return __longlong_as_double(__double_as_longlong(a) ^ (long long)0x8000000000000000ull);
+}
+
 template <int ET> struct Shape;
 template <> struct Shape<DNL_ELQUA4NAX> {
   __device__ __forceinline__ static double N(int pt, int k)
@@ -82,7 +91,7 @@ template <> struct Shape<DNL_ELQUA4NAX> {
     const int other = c == 0 ? (sgy(k) ^ sgy(pt)) : (sgx(k) ^ sgx(pt));
     const double v = other ? c_shape.axD[1] : c_shape.axD[0];
     const int s = c == 0 ? sgx(k) : sgy(k);
-    return s ? v : -v;
+    return s ? v : flip_sign(v);
   }
 };
 template <> struct Shape<DNL_ELHEX8N3D> {
@@ -97,7 +106,7 @@ template <> struct Shape<DNL_ELHEX8N3D> {
     const int d = c == 0 ? dy + dz : (c == 1 ? dx + dz : dx + dy);
     const double v = d == 0 ? c_shape.hxD[0] : (d == 1 ? c_shape.hxD[1] : c_shape.hxD[2]);
     const int s = c == 0 ? sgx(k) : (c == 1 ? sgy(k) : sgz(k));
-    return s ? v : -v;
+    return s ? v : flip_sign(v);
   }
 };
 
@@ -127,58 +136,77 @@ __device__ __forceinline__ double nr_rcp(double x)
   return fma(r, e, r);
 }
 
-// ----------------------------------------------------------------------------- Jacobi rotation
-// One rotation of Tensor2::polarDecomposeLnU (Tensor2.C:1183-1240) on pivot (P, Q): f <- R^T f R
-// with R the plane rotation (c, s), written with the reference's association order and its exact
-// zero/one terms dropped (x + 0 and 1 * x are exact), and Rot <- Rot R.
-template <int P, int Q>
-__device__ __forceinline__ void jacobi_rotate(double f[3][3], double rot[3][3], double c, double s)
-{
-  constexpr int O = 3 - P - Q;
-  const double ms = -s;
-  double pp[3], pq[3];  // P(m, P), P(m, Q) with P(m, j) = sum_k f(k, m) r(k, j)
-#pragma unroll
-  for (int m = 0; m < 3; m++) {
-    pp[m] = RADD(RMUL(f[P][m], c), RMUL(f[Q][m], ms));
-    pq[m] = RADD(RMUL(f[P][m], s), RMUL(f[Q][m], c));
-  }
-  auto col = [&](int m, int j) -> double { return j == P ? pp[m] : (j == Q ? pq[m] : f[O][m]); };
-  auto U = [&](int i, int j) -> double {
-    if (i == O) return col(O, j);
-    if (i == P) return RADD(RMUL(c, col(P, j)), RMUL(ms, col(Q, j)));
-    return RADD(RMUL(s, col(P, j)), RMUL(c, col(Q, j)));
-  };
-  const double u00 = U(0, 0), u01 = U(0, 1), u02 = U(0, 2), u11 = U(1, 1), u12 = U(1, 2), u22 = U(2, 2);
-  f[0][0] = u00; f[0][1] = u01; f[0][2] = u02;
-  f[1][0] = u01; f[1][1] = u11; f[1][2] = u12;
-  f[2][0] = u02; f[2][1] = u12; f[2][2] = u22;
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    const double rp = rot[i][P], rq = rot[i][Q];
-    rot[i][P] = fma(rp, c, rq * ms);
-    rot[i][Q] = fma(rp, s, rq * c);
-  }
-}
+// |x| and -x on the bit pattern (integer pipe).
+__device__ __forceinline__ double iabs(double a) { return __longlong_as_double((long long)abits(a)); }
+__device__ __forceinline__ double ineg(double a) { return flip_sign(a); }
 
+// ----------------------------------------------------------------------------- Jacobi rotation
 // Rotation angle of Tensor2.C:1195-1208.  With d = C_qq - C_pp and e = 2 C_pq the reference's
-// t = 1 / (alpha + sign(alpha) sqrt(alpha^2 + 1)), alpha = d / e, is
-// t = sign(d e) |e| / (|d| + sqrt(d^2 + e^2)) (t = 1 when d = 0); then c = 1/sqrt(1 + t^2),
-// s = t c.  One square root, one division and one reciprocal square root instead of two of each:
-// the same angle to a few ulps, which moves the rotated diagonal by less than an ulp of its
-// stationary value.
+// t = 1 / (alpha + sign(alpha) sqrt(alpha^2 + 1)), alpha = d / e, is tan(theta) with
+// cos(2 theta) = |d| / sqrt(d^2 + e^2) >= 0 and sign(theta) = sign(d e) (theta = +pi/4 when
+// d = 0).  Half-angle identities give c = sqrt((1 + cos 2theta) / 2) and
+// s = sin(2 theta) / (2 c) = |C_pq| w / c with w = 1 / sqrt(d^2 + e^2): two reciprocal square
+// roots and no division.  The angle agrees with the reference's to a few ulps; the rotated
+// diagonal is stationary in the angle, so it moves by far less than an ulp.
 __device__ __forceinline__ void jacobi_angle(double fpp, double fqq, double fpq, double &c, double &s)
 {
-  const double d = RSUB(fqq, fpp), e = RMUL(2., fpq);
-  double t;
-  if (d != 0.) {
-    const double ae = fabs(e);
-    t = ae / (fabs(d) + sqrt(fma(d, d, e * e)));
-    if ((d < 0.) != (e < 0.)) t = -t;
+  const double d = fqq - fpp;
+  const double w = rsqrt(fma(d, d, (4.0 * fpq) * fpq));
+  const double h = fma(0.5 * iabs(d), w, 0.5);  // cos^2(theta)
+  const double r = rsqrt(h);
+  c = h * r;
+  const double sv = iabs(fpq) * w * r;
+  const bool neg = abits(d) != 0 && ((__double_as_longlong(d) ^ __double_as_longlong(fpq)) < 0);
+  s = neg ? ineg(sv) : sv;
+}
+
+// One rotation of Tensor2::polarDecomposeLnU (Tensor2.C:1183-1240): C <- R^T C R with R the plane
+// rotation (c, s) on pivot (P, Q), Rot <- Rot R.  The pivot is a run-time case k (0: (0,1),
+// 1: (0,2), 2: (1,2); O is the third index) so that the lanes of a warp, which pick different
+// pivots, execute one rotation instead of one per distinct pivot.  The reference stores, for
+// i < j, the (j, i) entry sum_k R_kj (C R)_ki; with its exact zero and one terms dropped
+// (x + 0 and 1 * x are exact) every entry is a two-term sum of products, and such a sum rounds
+// the same in any operand order, so the pivot-generic formulas on a = C_PP, b = C_QQ, x = C_PQ,
+// y = C_PO, z = C_QO give its results bit for bit for the same (c, s).
+// AXI: C is block diagonal and the pivot is always (0, 1).
+template <bool AXI>
+__device__ __forceinline__ void jacobi_rotate(int k, double &f00, double &f11, double &f22, double &f01,
+                                              double &f02, double &f12, double rot[3][3], double x)
+{
+  const double a = k == 2 ? f11 : f00;
+  const double b = k == 0 ? f11 : f22;
+  double c, s;
+  jacobi_angle(a, b, x, c, s);
+  const double ms = ineg(s);
+  const double ppP = RADD(RMUL(a, c), RMUL(x, ms)), ppQ = RADD(RMUL(x, c), RMUL(b, ms));
+  const double pqP = RADD(RMUL(a, s), RMUL(x, c)), pqQ = RADD(RMUL(x, s), RMUL(b, c));
+  const double a2 = RADD(RMUL(c, ppP), RMUL(ms, ppQ));
+  const double b2 = RADD(RMUL(s, pqP), RMUL(c, pqQ));
+  const double x2 = RADD(RMUL(s, ppP), RMUL(c, ppQ));  // stored C_PQ is (R^T C R)_QP
+  if (AXI) {
+    f00 = a2;
+    f11 = b2;
+    f01 = x2;
   } else {
-    t = 1.;
+    const double y = k == 0 ? f02 : f01, z = k == 2 ? f02 : f12;
+    const double y2 = RADD(RMUL(c, y), RMUL(ms, z));
+    const double z2 = RADD(RMUL(s, y), RMUL(c, z));
+    f00 = k == 2 ? f00 : a2;
+    f11 = k == 0 ? b2 : (k == 2 ? a2 : f11);
+    f22 = k == 0 ? f22 : b2;
+    f01 = k == 0 ? x2 : y2;
+    f02 = k == 0 ? y2 : (k == 1 ? x2 : z2);
+    f12 = k == 2 ? x2 : z2;
   }
-  c = rsqrt(fma(t, t, 1.));
-  s = t * c;
+#pragma unroll
+  for (int i = 0; i < (AXI ? 2 : 3); i++) {
+    const double rp = k == 2 ? rot[i][1] : rot[i][0];
+    const double rq = k == 0 ? rot[i][1] : rot[i][2];
+    const double np = fma(rp, c, rq * ms), nq = fma(rp, s, rq * c);
+    rot[i][0] = k == 2 ? rot[i][0] : np;
+    rot[i][1] = k == 0 ? nq : (k == 2 ? np : rot[i][1]);
+    rot[i][2] = k == 0 ? rot[i][2] : nq;
+  }
 }
 
 // ----------------------------------------------------------------------------- element kernel
@@ -187,17 +215,21 @@ __device__ __forceinline__ void jacobi_angle(double fpp, double fqq, double fpq,
 // lanes with valid == false compute on a clamped element and store nothing.  `red` is this
 // element's NIP x NEN*DIM slice of shared memory; `m` and `tm` are the element's material and
 // time/status record (one per mesh, or per instance in a batch).
-template <int ET>
+template <int ET, bool TAPE = false>
 __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, DevTime *tm, int e,
                                         int pt, bool valid, int lane, double *red)
 {
   using T = Elem<ET>;
   using L = IpLayout<ET>;
   using SH = Shape<ET>;
+  using TL = TapeLayout<ET>;
   constexpr int NIP = T::NIP, NEN = T::NEN, DIM = T::DIM, NS = T::NS;
   constexpr bool AXI = ET == DNL_ELQUA4NAX;
   const long nIP = (long)a.E * NIP;
   const long ipx = (long)e * NIP + pt;
+  auto tape = [&](int slot, double v) {
+    if (TAPE && valid) a.tape[(long)slot * nIP + ipx] = v;
+  };
 
   int node[NEN];
 #pragma unroll
@@ -223,7 +255,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
   }
   double detJ, Ji[DIM][DIM];
   if (AXI) {
-    detJ = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    detJ = fma(J[0][0], J[1][1], -J[0][1] * J[1][0]);
     const double r = 1. / detJ;
     Ji[0][0] = J[1][1] * r;
     Ji[0][1] = -J[0][1] * r;
@@ -231,21 +263,29 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     Ji[1][1] = J[0][0] * r;
     if (detJ < 0. && valid) record_error(tm, DNL_ERR_NEG_DETJ, e);
   } else {
-    const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-    const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-    const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-    detJ = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+    const double c00 = fma(J[1][1], J[2][2], -J[1][2] * J[2][1]);
+    const double c01 = fma(J[1][2], J[2][0], -J[1][0] * J[2][2]);
+    const double c02 = fma(J[1][0], J[2][1], -J[1][1] * J[2][0]);
+    detJ = fma(J[0][0], c00, fma(J[0][1], c01, J[0][2] * c02));
     const double r = 1. / detJ;
     Ji[0][0] = c00 * r;
     Ji[1][0] = c01 * r;
     Ji[2][0] = c02 * r;
-    Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * r;
-    Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
-    Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * r;
-    Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
-    Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
-    Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+    Ji[0][1] = fma(J[0][2], J[2][1], -J[0][1] * J[2][2]) * r;
+    Ji[1][1] = fma(J[0][0], J[2][2], -J[0][2] * J[2][0]) * r;
+    Ji[2][1] = fma(J[0][1], J[2][0], -J[0][0] * J[2][1]) * r;
+    Ji[0][2] = fma(J[0][1], J[1][2], -J[0][2] * J[1][1]) * r;
+    Ji[1][2] = fma(J[0][2], J[1][0], -J[0][0] * J[1][2]) * r;
+    Ji[2][2] = fma(J[0][0], J[1][1], -J[0][1] * J[1][0]) * r;
     if (detJ == 0. && valid) record_error(tm, DNL_ERR_SINGULAR, e);
+  }
+  if (TAPE) {
+#pragma unroll
+    for (int l = 0; l < DIM; l++)
+#pragma unroll
+      for (int c = 0; c < DIM; c++) tape(TL::JI + l * DIM + c, Ji[l][c]);
+    tape(TL::DETJ, detJ);
+    tape(TL::RAD, Rad);
   }
 
   // ---- F = I + sum_k dN_k (x) du_k (Current field), diagonal accumulated onto 1 in node order
@@ -276,6 +316,10 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     if (AXI) vR = RADD(vR, RMUL(SH::N(pt, k), uk[0]));
   }
   if (AXI) F[2][2] = RADD(F[2][2], vR / Rad);
+  if (TAPE) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) tape(TL::F + k, F[k / 3][k % 3]);
+  }
 
   // ---- C = F^T F (Tensor2::Transpose then operator*), exact reference rounding
   double f[3][3];
@@ -300,32 +344,28 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
   // ---- Jacobi eigen-iteration (at most 29 rotations; Tensor2.C:1169)
   double rot[3][3] = {{1., 0., 0.}, {0., 1., 0.}, {0., 0., 1.}};
   bool conv = false;
-  for (int it = 1; it < kPolarMaxIt; it++) {
-    int p, q;
-    if (AXI) {  // C is block diagonal: the pivot is always (0,1)
-      p = 0;
-      q = 1;
-    } else {
-      q = abs_gt(f[0][1], f[0][2]) ? 1 : 2;
-      p = abs_gt(q == 1 ? f[0][1] : f[0][2], f[1][2]) ? 0 : 1;
-      if (p == 1) q = 2;
+  {
+    double f00 = f[0][0], f11 = f[1][1], f22 = f[2][2], f01 = f[0][1], f02 = f[0][2], f12 = f[1][2];
+    for (int it = 1; it < kPolarMaxIt; it++) {
+      // pivot of Tensor2.C:1173-1178: q = |C01| > |C02| ? 1 : 2, p = |C0q| > |C12| ? 0 : 1
+      int k = 0;
+      double fpq = f01;
+      if (!AXI) {
+        const bool q1 = abs_gt(f01, f02);
+        const double f0q = q1 ? f01 : f02;
+        const bool p0 = abs_gt(f0q, f12);
+        k = p0 ? (q1 ? 0 : 1) : 2;
+        fpq = p0 ? f0q : f12;
+      }
+      if (abits(fpq) < abits(kPolarPrecision)) {
+        conv = true;
+        break;
+      }
+      jacobi_rotate<AXI>(k, f00, f11, f22, f01, f02, f12, rot, fpq);
     }
-    const double fpq = p == 0 ? (q == 1 ? f[0][1] : f[0][2]) : f[1][2];
-    if (abits(fpq) < abits(kPolarPrecision)) {
-      conv = true;
-      break;
-    }
-    double c, s;
-    if (AXI || (p == 0 && q == 1)) {
-      jacobi_angle(f[0][0], f[1][1], fpq, c, s);
-      jacobi_rotate<0, 1>(f, rot, c, s);
-    } else if (p == 0) {
-      jacobi_angle(f[0][0], f[2][2], fpq, c, s);
-      jacobi_rotate<0, 2>(f, rot, c, s);
-    } else {
-      jacobi_angle(f[1][1], f[2][2], fpq, c, s);
-      jacobi_rotate<1, 2>(f, rot, c, s);
-    }
+    f[0][0] = f00;
+    f[1][1] = f11;
+    f[2][2] = f22;
   }
   if (!conv && valid) record_error(tm, DNL_ERR_JACOBI_NOCONV, e);
 
@@ -335,8 +375,18 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     double lg[3], il[3];
 #pragma unroll
     for (int cc = 0; cc < 3; cc++) {
-      lg[cc] = log(f[cc][cc]) / 2.;
+      lg[cc] = 0.5 * log(f[cc][cc]);
       il[cc] = rsqrt(f[cc][cc]);
+    }
+    if (TAPE) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) tape(TL::V + k, rot[k / 3][k % 3]);
+#pragma unroll
+      for (int cc = 0; cc < 3; cc++) {
+        tape(TL::LAM + cc, f[cc][cc]);
+        tape(TL::LG + cc, lg[cc]);
+        tape(TL::IL + cc, il[cc]);
+      }
     }
 #pragma unroll
     for (int i = 0; i < 3; i++)
@@ -376,6 +426,10 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         R[i][j] = s;
       }
     }
+  if (TAPE) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) tape(TL::R + k, R[k / 3][k % 3]);
+  }
 
   // ---- strain, trial stress, J2 radial return (Element.C:245-345)
   double S[3][3], Ep[3][3], Epl[3][3];
@@ -414,17 +468,26 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
   double evpn = a.ip[L::EVPN * nIP + ipx];
   bool plastic = false;
   {
-    double ss = S[0][0] * S[0][0] + S[1][1] * S[1][1] + S[2][2] * S[2][2];
+    double ss = fma(S[0][0], S[0][0], fma(S[1][1], S[1][1], S[2][2] * S[2][2]));
     double off = S[0][1] * S[0][1];
     if (!AXI) off = fma(S[0][2], S[0][2], fma(S[1][2], S[1][2], off));
     ss = fma(2., off, ss);
     const double normS = sqrt(ss);
     const double Strial = kSqrt32 * normS;
     const double Sigv0 = RADD(m.A, RMUL(m.B, evpn));
-    if (Strial > Sigv0) {
+    if (TAPE) {
+      const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+      for (int k = 0; k < NS; k++) tape(TL::STR + k, S[I0[k]][I1[k]]);
+      tape(TL::NORMS, normS);
+      tape(TL::GAM, 0.);
+      tape(TL::XV, evp);
+      tape(TL::XN, evpn);
+    }
+    if (__double_as_longlong(Strial) > __double_as_longlong(Sigv0)) {  // both >= 0
       plastic = true;
       double h = m.nB * evpn * nr_rcp(evp);
-      double gamma = (normS - kSqrt23 * Sigv0) / (m.G2 * fma(h, 1.0 / m.G3, 1.0));
+      double gamma = fma(-kSqrt23, Sigv0, normS) * nr_rcp(m.G2 * fma(h, m.rG3, 1.0));
       double xn = evpn;
       int iteration = 0;
       for (;;) {
@@ -433,10 +496,11 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         const double Sigv = RADD(m.A, RMUL(m.B, xn));
         h = m.nB * xn * nr_rcp(xv);  // n B xv^(n-1)
         const double dfun = fma(kSqrt23, h, m.dfun0);
-        const double fun = dfun * gamma - ((Strial - Sigv) + h * kSqrt23 * gamma);
-        if (fabs(fun) > kRadialReturnPrecision * Sigv) {  // |fun / Sigv| > 1e-8, Sigv > 0
+        const double fun = fma(dfun, gamma, -fma(h * kSqrt23, gamma, Strial - Sigv));
+        if (abs_gt(fun, kRadialReturnPrecision * Sigv)) {  // |fun / Sigv| > 1e-8, Sigv > 0
           double dgamma = -fun * nr_rcp(dfun);
-          if (dgamma < 0 && fabs(dgamma) > gamma) dgamma = -gamma * 0.9;
+          // dgamma < 0 && |dgamma| > gamma, with gamma > 0
+          if (__double_as_longlong(dgamma) < 0 && abs_gt(dgamma, gamma)) dgamma = -gamma * 0.9;
           gamma += dgamma;
         } else {
           break;
@@ -448,6 +512,9 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         }
       }
       const double inv = 1. / normS;
+      tape(TL::GAM, gamma);
+      tape(TL::XV, RADD(evp, RMUL(kSqrt23, gamma)));
+      tape(TL::XN, xn);
       evp = RADD(evp, RMUL(kSqrt23, gamma));
       evpn = xn;
       const double c2 = m.G2 * gamma;
@@ -474,6 +541,16 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     pressure *= 1.0 / NIP;  // exact: NIP is a power of two
   }
   const double p = fma(m.K, pressure, a.ip[L::P * nIP + ipx]);
+
+  if (TAPE) {
+    const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+      tape(TL::SPRE + k, S[I0[k]][I1[k]]);
+      tape(TL::EPRE + k, Ep[I0[k]][I1[k]]);
+      tape(TL::PPRE + k, Epl[I0[k]][I1[k]]);
+    }
+  }
 
   // ---- RFI: X <- R X R^T for S, Eps, EpsPlas (Element.C:386-388)
   auto rfi = [&](double X[3][3]) {
@@ -585,7 +662,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
   }
 }
 
-template <int ET>
+template <int ET, bool TAPE = false>
 __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
 {
   constexpr int NIP = Elem<ET>::NIP, NEN = Elem<ET>::NEN, DIM = Elem<ET>::DIM;
@@ -597,8 +674,8 @@ __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
   const int eRaw = gtid / NIP;
   const bool valid = eRaw < a.E;
   const int lane = threadIdx.x & 31;
-  elem_ip<ET>(a, a.mat, a.tm, valid ? eRaw : a.E - 1, gtid % NIP, valid, lane,
-              red[threadIdx.x >> 5][lane / NIP]);
+  elem_ip<ET, TAPE>(a, a.mat, a.tm, valid ? eRaw : a.E - 1, gtid % NIP, valid, lane,
+                    red[threadIdx.x >> 5][lane / NIP]);
 }
 
 // Batched element pass over the union of many meshes: element e belongs to instance inst[e],
@@ -621,6 +698,9 @@ __global__ void __launch_bounds__(BLOCK) k_elem_batch(ElemArgs a, const int *ele
   const int lane = threadIdx.x & 31;
   elem_ip<ET>(a, mats[inst], tm, e, gtid % NIP, valid, lane, red[threadIdx.x >> 5][lane / NIP]);
 }
+
+// ----------------------------------------------------------------------------- tangent pass
+#include "dnl_sens_elem.cuh"
 
 // ----------------------------------------------------------------------------- mass kernel
 // Element::computeMassMatrix with the reference's rounding: M_k = sum_pt (rho N_k) W,
@@ -671,8 +751,8 @@ __global__ void __launch_bounds__(128) k_mass(ElemArgs a, double *me, const int 
   }
   double W = detJ;  // weight 1
   if (AXI) W = RMUL(W, RMUL(RMUL(2., kPi), Rad));
-#pragma unroll
   const double rho = elemInst ? mats[elemInst[e]].rho : a.mat.rho;
+#pragma unroll
   for (int k = 0; k < NEN; k++) red[wib][slot][pt][k] = RMUL(RMUL(rho, SH::N(pt, k)), W);
   __syncwarp();
   if (valid) {
@@ -754,6 +834,7 @@ __global__ void __launch_bounds__(256) k_courant_batch(ElemArgs a, const int *el
 static ElemArgs elem_args(dnl_handle *h)
 {
   ElemArgs a;
+  memset(&a, 0, sizeof a);
   a.E = h->E;
   a.N = h->N;
   a.conn = h->conn;
@@ -782,6 +863,24 @@ int launch_elem(dnl_handle *h, cudaStream_t s, int gate)
     k_elem<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a);
   else
     k_elem<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a);
+  prof_end(h, DNL_PROF_ELEM, s);
+  launch_counter()++;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
+}
+
+// the element pass with its per-integration-point record (forward-mode sensitivities)
+int launch_elem_tape(dnl_handle *h, cudaStream_t s, double *tape)
+{
+  ElemArgs a = elem_args(h);
+  a.gate = 1;
+  a.tape = tape;
+  const long threads = (long)h->E * h->nip;
+  const int grid = (int)((threads + 127) / 128);
+  prof_begin(h, s);
+  if (h->etype == DNL_ELQUA4NAX)
+    k_elem<DNL_ELQUA4NAX, true><<<grid, 128, 0, s>>>(a);
+  else
+    k_elem<DNL_ELHEX8N3D, true><<<grid, 128, 0, s>>>(a);
   prof_end(h, DNL_PROF_ELEM, s);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;

@@ -526,6 +526,11 @@ int launch_gather_mass(dnl_handle *h, const double *me)
   return check_launch();
 }
 
+// the primal per-step launches, for the sensitivity run (dnl_sens.cu)
+int enqueue_bc_current(dnl_handle *h) { return (h->hasSpeedBC || h->nbcNodes) ? launch_bc_current(h) : 0; }
+int enqueue_node(dnl_handle *h) { return launch_node(h, true); }
+int read_time_state(dnl_handle *h, DevTime *t) { return read_time(h, t); }
+
 int launch_gather_raw(int dim, const GatherArgs &g, cudaStream_t s)
 {
   const int grid = (g.N + 255) / 256;
@@ -729,6 +734,7 @@ int dnl_get_stream(dnl_handle *h, void **stream)
 int dnl_destroy(dnl_handle *h)
 {
   if (!h) return DNL_ERR_ARG;
+  dnl::sens_free(h);
   for (int i = 0; i < h->ngraphs; i++) cudaGraphExecDestroy(h->graphs[i].exec);
   void *ptrs[] = {h->conn, h->x[0], h->n2eStart, h->n2e, h->mass, h->fieldMem, h->ip, h->detJ,
                   h->stepT, h->fe, h->fint, h->stage, h->bcIdx, h->bcCode, h->bcNodeList, h->bcSpeed,
@@ -813,26 +819,7 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
   CKF(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
 
   // material constants, in the reference's expressions
-  Material m;
-  m.young = mat->young;
-  m.nu = mat->poisson;
-  m.rho = mat->density;
-  m.A = mat->A;
-  m.B = mat->B;
-  m.n = mat->n;
-  m.K = m.young / (3. * (1. - 2. * m.nu));
-  const double G = m.young / (2. * (1. + m.nu));
-  m.G2 = 2.0 * G;
-  m.G3 = 3.0 * G;
-  m.nB = m.n * m.B;
-  m.dfun0 = 1.2247448713915890490986420373529 * 2.0 * G;
-  {
-    double ro = 0.;
-    for (int i = 0; i < 4; i++) ro += m.rho;
-    ro /= 4;
-    const double Nu = m.nu;
-    m.Cs = sqrt((m.young * (1 - Nu)) / (ro * (1 + Nu) * (1 - 2 * Nu)));
-  }
+  const Material m = make_material(*mat);
   h->mat = m;
   // ExplicitSolverCH::computeIntegrationParameters (ExplicitSolverCH.C:336-343)
   const double rb = sp->rho_b;
@@ -884,6 +871,8 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
       h->bank[b].disp[c] = base + (size_t)(9 + c) * N;
     }
   {  // BoundarySpeed::applyInitial_V0 on both fields
+    const double vn = sqrt(mesh->v0[0] * mesh->v0[0] + mesh->v0[1] * mesh->v0[1] + mesh->v0[2] * mesh->v0[2]);
+    for (int c = 0; c < 3; c++) h->v0dir[c] = vn > 0 ? mesh->v0[c] / vn : 0.;
     std::vector<double> v(N);
     for (int b = 0; b < 2; b++)
       for (int c = 0; c < 3; c++) {

@@ -1,0 +1,353 @@
+// Forward-mode sensitivities of an explicit run (dnl_sens_run, dnl_adjoint).
+//
+// The run advances the primal state exactly as dnl_step does (boundary conditions, element pass,
+// nodal Chung-Hulbert update of ExplicitSolverCH.C:387-567), except that the step sizes come from
+// the caller's schedule instead of the Courant/Pulse estimate, and the element pass writes its
+// per-integration-point record.  After each primal launch a tangent launch carries the derivative
+// of the state with respect to the four parameters (A, B, n of IsoHardElastoplastic and the
+// initial-velocity magnitude |v0|) -- four tangent copies of every nodal field and
+// integration-point variable.  Four parameters make the forward mode cheaper than a reverse
+// (adjoint) sweep: no trajectory is stored or recomputed, so no checkpoints are needed.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "dnl_common.cuh"
+
+namespace dnl {
+
+struct SensState {
+  int E, N;
+  double *mem = nullptr;
+  double *tape = nullptr;  // [NT][E*NIP]
+  double *tx = nullptr;    // [dir][3][N]
+  double *tb[2][4];        // [bank][du, v, a, disp] -> [dir][3][N]
+  double *tip = nullptr;   // [dir][NCOMP][E*NIP]
+  double *tfe = nullptr;   // [dir][DIM][E*NEN]
+  double *dts = nullptr;   // step sizes on the device
+  double *out = nullptr;   // N*3 staging for node-major results
+  int dtsCap = 0;
+  std::vector<double> schedule;  // dnl_set_dt_schedule
+};
+
+namespace {
+
+__global__ void k_sens_dt(DevTime *tm, const double *dts, int phase)
+{
+  if (tm->status) return;
+  if (phase == 0) {  // initStep with the scheduled step
+    const double dt = dts[tm->increment];
+    tm->timeStep = dt;
+    tm->nextTime = __dadd_rn(tm->currentTime, dt);
+    tm->increment++;
+  } else {  // updateTime
+    tm->currentTime = __dadd_rn(tm->currentTime, tm->timeStep);
+  }
+}
+
+// constant boundary conditions on the Current tangents: a restrained or imposed-speed component
+// has a parameter-independent value, so its tangents are zero
+__global__ void k_bc_tan(int nb, const int *nodes, const int *code, int N, double *du, double *v,
+                         double *a)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const int n = nodes[i], cd = code[i];
+  for (int dir = 0; dir < kSensParams; dir++)
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+      if ((cd >> (2 * c)) & 3) {
+        const long o = ((long)dir * 3 + c) * N + n;
+        du[o] = 0.;
+        v[o] = 0.;
+        a[o] = 0.;
+      }
+}
+
+struct SensNodeArgs {
+  int N, EN;
+  const int *start, *entry;
+  const double *tfe, *mass;
+  double *cur[4], *nxt[4];  // du, v, a, disp: [dir][3][N]
+  double *tx;
+  const int *bcIdx, *bcCode;
+  const DevTime *tm;
+  double alphaM, beta, gamma;
+};
+
+// tangent of node_update (dnl_host.cu): the predictor, the assembled force, the corrector and the
+// boundary conditions are linear in the state, so the tangents follow the same formulas
+template <int DIM>
+__global__ void __launch_bounds__(256) k_node_tan(SensNodeArgs g)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  const int dir = blockIdx.y;
+  if (n >= g.N || g.tm->status) return;
+  const double dt = g.tm->timeStep;
+  const long N = g.N, base = (long)dir * 3 * N;
+  double cdu[3], cv[3], ca[3], cd[3], ndu[3], nv[3], na[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    cdu[i] = g.cur[0][base + i * N + n];
+    cv[i] = g.cur[1][base + i * N + n];
+    ca[i] = g.cur[2][base + i * N + n];
+    cd[i] = g.cur[3][base + i * N + n];
+  }
+  (void)cdu;
+  const double c1 = dt * (0.5 - g.beta), c2 = dt * (1. - g.gamma);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    ndu[i] = (ca[i] * c1 + cv[i]) * dt;
+    nv[i] = ca[i] * c2 + cv[i];
+    na[i] = 0.;
+  }
+  const int bc = g.bcIdx[n];
+  const int code = bc >= 0 ? g.bcCode[bc] : 0;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    if ((code >> (2 * i)) & 3) ca[i] = cv[i] = ndu[i] = nv[i] = 0.;
+  double f[DIM];
+#pragma unroll
+  for (int c = 0; c < DIM; c++) f[c] = 0.;
+  const double *fe = g.tfe + (long)dir * DIM * g.EN;
+  for (int q = g.start[n]; q < g.start[n + 1]; q++) {
+    const int ent = __ldg(g.entry + q);
+#pragma unroll
+    for (int c = 0; c < DIM; c++) f[c] += __ldg(fe + (long)c * g.EN + ent);
+  }
+  const double m = g.mass[n];
+#pragma unroll
+  for (int c = 0; c < DIM; c++) na[c] = f[c] / m;
+  const double cg = dt * g.gamma, cb = dt * dt * g.beta, oma = 1. - g.alphaM;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    na[i] = (na[i] - g.alphaM * ca[i]) / oma;
+    nv[i] = fma(cg, na[i], nv[i]);
+    ndu[i] = fma(cb, na[i], ndu[i]);
+    if ((code >> (2 * i)) & 3) na[i] = nv[i] = ndu[i] = 0.;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const long o = base + i * N + n;
+    g.nxt[0][o] = ndu[i];
+    g.nxt[1][o] = nv[i];
+    g.nxt[2][o] = na[i];
+    g.nxt[3][o] = cd[i] + ndu[i];
+    g.tx[o] += ndu[i];
+  }
+}
+
+// initial tangents: the initial velocity v0 = |v0| u on both fields, d v / d|v0| = u
+__global__ void k_sens_seed(int N, double *v0bank, double *v1bank, double u0, double u1, double u2)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const long base = 3L * 3 * N;  // direction 3
+  const double u[3] = {u0, u1, u2};
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    v0bank[base + c * (long)N + n] = u[c];
+    v1bank[base + c * (long)N + n] = u[c];
+  }
+}
+
+__global__ void k_to_nodes(int N, double *out, const double *c0, const double *c1, const double *c2)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  out[3L * n] = c0[n];
+  out[3L * n + 1] = c1[n];
+  out[3L * n + 2] = c2[n];
+}
+
+#define CKS(x)                                \
+  do {                                        \
+    if ((x) != cudaSuccess) return DNL_ERR_CUDA; \
+  } while (0)
+
+int sens_alloc(dnl_handle *h, SensState *S)
+{
+  const long nIP = (long)h->E * h->nip, N = h->N;
+  const int NT = h->etype == DNL_ELQUA4NAX ? TapeLayout<DNL_ELQUA4NAX>::NT : TapeLayout<DNL_ELHEX8N3D>::NT;
+  const int NC = h->etype == DNL_ELQUA4NAX ? TanLayout<DNL_ELQUA4NAX>::NCOMP : TanLayout<DNL_ELHEX8N3D>::NCOMP;
+  const long nodal = (long)kSensParams * 3 * N;
+  const long total = NT * nIP + nodal * 9 + (long)kSensParams * NC * nIP +
+                     (long)kSensParams * h->dim * h->E * h->nen + 3 * N;
+  CKS(cudaMalloc(&S->mem, sizeof(double) * total));
+  double *p = S->mem;
+  S->tape = p;
+  p += NT * nIP;
+  S->tx = p;
+  p += nodal;
+  for (int b = 0; b < 2; b++)
+    for (int f = 0; f < 4; f++) {
+      S->tb[b][f] = p;
+      p += nodal;
+    }
+  S->tip = p;
+  p += (long)kSensParams * NC * nIP;
+  S->tfe = p;
+  p += (long)kSensParams * h->dim * h->E * h->nen;
+  S->out = p;
+  S->E = h->E;
+  S->N = h->N;
+  return 0;
+}
+
+}  // namespace
+
+void sens_free(dnl_handle *h)
+{
+  SensState *S = (SensState *)h->sens;
+  if (!S) return;
+  if (S->mem) cudaFree(S->mem);
+  if (S->dts) cudaFree(S->dts);
+  delete S;
+  h->sens = nullptr;
+}
+
+}  // namespace dnl
+
+using namespace dnl;
+
+extern "C" {
+
+int dnl_set_dt_schedule(dnl_handle *h, const double *dts, int nsteps)
+{
+  if (!h || !dts || nsteps <= 0) return DNL_ERR_ARG;
+  for (int k = 0; k < nsteps; k++)
+    if (!(dts[k] > 0. && dts[k] < 1e300)) return DNL_ERR_ARG;
+  if (!h->sens) h->sens = new SensState();
+  ((SensState *)h->sens)->schedule.assign(dts, dts + nsteps);
+  return 0;
+}
+
+int dnl_sens_run(dnl_handle *h, int nsteps, const double *dts, double *coords, double *dcoords)
+{
+  if (!h || nsteps <= 0 || !dts) return DNL_ERR_ARG;
+  for (int k = 0; k < nsteps; k++)
+    if (!(dts[k] > 0. && dts[k] < 1e300)) return DNL_ERR_ARG;
+  if (h->hostIncrement != 0) return DNL_ERR_ARG;  // starts from the initial state
+  int r;
+  if (!h->prologueDone && (r = dnl_prologue(h))) return r;
+  if (!h->sens) h->sens = new SensState();
+  SensState *S = (SensState *)h->sens;
+  if (!S->mem && (r = sens_alloc(h, S))) return r;
+  cudaStream_t s = h->stream;
+  const long nIP = (long)h->E * h->nip, N = h->N;
+  // zero every tangent, then seed d v / d|v0|
+  {
+    const int NT = h->etype == DNL_ELQUA4NAX ? TapeLayout<DNL_ELQUA4NAX>::NT : TapeLayout<DNL_ELHEX8N3D>::NT;
+    const size_t bytes = sizeof(double) * (size_t)((S->out - S->mem) - NT * nIP);
+    CKS(cudaMemsetAsync(S->tx, 0, bytes, s));
+  }
+  k_sens_seed<<<(h->N + 255) / 256, 256, 0, s>>>(h->N, S->tb[0][1], S->tb[1][1], h->v0dir[0], h->v0dir[1],
+                                                  h->v0dir[2]);
+  launch_counter()++;
+  if (S->dtsCap < nsteps) {
+    if (S->dts) cudaFree(S->dts);
+    S->dts = nullptr;
+    S->dtsCap = 0;
+    CKS(cudaMalloc(&S->dts, sizeof(double) * nsteps));
+    S->dtsCap = nsteps;
+  }
+  CKS(cudaMemcpyAsync(S->dts, dts, sizeof(double) * nsteps, cudaMemcpyHostToDevice, s));
+
+  SensElemArgs ea;
+  memset(&ea, 0, sizeof ea);
+  ea.E = h->E;
+  ea.N = h->N;
+  ea.conn = h->conn;
+  for (int c = 0; c < 3; c++) ea.x[c] = h->x[c];
+  ea.ip = h->ip;
+  ea.tape = S->tape;
+  ea.tx = S->tx;
+  ea.tip = S->tip;
+  ea.tfe = S->tfe;
+  ea.tm = h->tm;
+  ea.mat = h->mat;
+  SensNodeArgs na;
+  memset(&na, 0, sizeof na);
+  na.N = h->N;
+  na.EN = h->E * h->nen;
+  na.start = h->n2eStart;
+  na.entry = h->n2e;
+  na.tfe = S->tfe;
+  na.mass = h->mass;
+  na.tx = S->tx;
+  na.bcIdx = h->bcIdx;
+  na.bcCode = h->bcCode;
+  na.tm = h->tm;
+  na.alphaM = h->alphaM;
+  na.beta = h->beta;
+  na.gamma = h->gamma;
+  const dim3 ngrid((h->N + 255) / 256, kSensParams);
+  for (int k = 0; k < nsteps; k++) {
+    k_sens_dt<<<1, 1, 0, s>>>(h->tm, S->dts, 0);
+    launch_counter()++;
+    if ((r = enqueue_bc_current(h))) return r;
+    if (h->nbcNodes) {
+      double **tc = S->tb[h->cur];
+      k_bc_tan<<<(h->nbcNodes + 127) / 128, 128, 0, s>>>(h->nbcNodes, h->bcNodeList, h->bcCode, h->N, tc[0],
+                                                         tc[1], tc[2]);
+      launch_counter()++;
+    }
+    if ((r = launch_elem_tape(h, s, S->tape))) return r;
+    for (int c = 0; c < 3; c++) ea.du[c] = h->bank[h->cur].du[c];
+    ea.tdu = S->tb[h->cur][0];
+    if ((r = launch_elem_tan(h->etype, ea, s))) return r;
+    if ((r = enqueue_node(h))) return r;
+    for (int f = 0; f < 4; f++) {
+      na.cur[f] = S->tb[h->cur][f];
+      na.nxt[f] = S->tb[1 - h->cur][f];
+    }
+    if (h->dim == 2)
+      k_node_tan<2><<<ngrid, 256, 0, s>>>(na);
+    else
+      k_node_tan<3><<<ngrid, 256, 0, s>>>(na);
+    launch_counter()++;
+    h->cur = 1 - h->cur;
+    k_sens_dt<<<1, 1, 0, s>>>(h->tm, S->dts, 1);
+    launch_counter()++;
+    if (cudaPeekAtLastError() != cudaSuccess) return DNL_ERR_CUDA;
+  }
+  DevTime t;
+  if ((r = read_time_state(h, &t))) return r;
+  h->hostIncrement = t.increment;
+  if (t.status) return t.status;
+  const int grid = (h->N + 255) / 256;
+  if (coords) {
+    k_to_nodes<<<grid, 256, 0, s>>>(h->N, S->out, h->x[0], h->x[1], h->x[2]);
+    CKS(cudaMemcpyAsync(coords, S->out, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s));
+    CKS(cudaStreamSynchronize(s));
+  }
+  if (dcoords)
+    for (int dir = 0; dir < kSensParams; dir++) {
+      const double *b = S->tx + (long)dir * 3 * N;
+      k_to_nodes<<<grid, 256, 0, s>>>(h->N, S->out, b, b + N, b + 2 * N);
+      CKS(cudaMemcpyAsync(dcoords + (long)dir * 3 * N, S->out, sizeof(double) * 3 * N,
+                          cudaMemcpyDeviceToHost, s));
+      CKS(cudaStreamSynchronize(s));
+    }
+  return 0;
+}
+
+int dnl_adjoint(dnl_handle *h, const double *dL_dx, double *grad, int ckpt_stride)
+{
+  if (!h || !dL_dx || !grad || ckpt_stride < 0 || !h->sens) return DNL_ERR_ARG;
+  SensState *S = (SensState *)h->sens;
+  if (S->schedule.empty()) return DNL_ERR_ARG;
+  const long n3 = 3L * h->N;
+  std::vector<double> dx((size_t)kSensParams * n3);
+  int r = dnl_sens_run(h, (int)S->schedule.size(), S->schedule.data(), nullptr, dx.data());
+  if (r) return r;
+  for (int p = 0; p < kSensParams; p++) {
+    double s = 0.;
+    for (long i = 0; i < n3; i++) s += dL_dx[i] * dx[(size_t)p * n3 + i];
+    grad[p] = s;
+  }
+  return 0;
+}
+
+}  // extern "C"

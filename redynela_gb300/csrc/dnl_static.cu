@@ -69,20 +69,7 @@ extern "C" int dnl_internal_forces_static(const dnl_static_args *a, void *stream
   // the error word starts at zero on every call; the array itself needs no clearing (fully written)
   if (cudaMemsetAsync(sp->tm, 0, sizeof(DevTime), s) != cudaSuccess) return DNL_ERR_CUDA;
 
-  Material m;
-  m.young = a->mat.young;
-  m.nu = a->mat.poisson;
-  m.rho = a->mat.density;
-  m.A = a->mat.A;
-  m.B = a->mat.B;
-  m.n = a->mat.n;
-  m.K = m.young / (3. * (1. - 2. * m.nu));
-  const double G = m.young / (2. * (1. + m.nu));
-  m.G2 = 2.0 * G;
-  m.G3 = 3.0 * G;
-  m.nB = m.n * m.B;
-  m.dfun0 = kSqrt32 * 2.0 * G;
-  m.Cs = 0.;
+  const Material m = make_material(a->mat);
 
   const int N = a->num_nodes, E = a->num_elements;
   ElemArgs ea;

@@ -129,6 +129,9 @@ def lib():
         L.dnl_batch_get_fint.argtypes = [H, C.c_int, _dp]
         L.dnl_batch_sizes.argtypes = [H, _ip, _ip]
         L.dnl_batch_handle.argtypes = [H, C.POINTER(H)]
+        L.dnl_sens_run.argtypes = [H, C.c_int, _dp, _dp, _dp]
+        L.dnl_set_dt_schedule.argtypes = [H, _dp, C.c_int]
+        L.dnl_adjoint.argtypes = [H, _dp, _dp, C.c_int]
         _lib = L
     return _lib
 
@@ -342,6 +345,68 @@ class GpuDomain:
         t = TimeInfo()
         self._check(self.L.dnl_get_time_info(self.h, C.byref(t)))
         return {k: getattr(t, k) for k, _ in TimeInfo._fields_}
+
+    def sensitivities(self, dts):
+        """dnl_sens_run: the run with step sizes ``dts`` from the initial state; returns the final
+        coordinates (N, 3) and their derivatives (4, N, 3) with respect to SENS_PARAMS."""
+        dts = np.ascontiguousarray(dts, dtype=np.float64)
+        N = self.model.N
+        x = np.zeros((N, 3))
+        dx = np.zeros((SENS_NPARAM, N, 3))
+        self._check_run(self.L.dnl_sens_run(self.h, len(dts), _ptr(dts), _ptr(x), _ptr(dx)))
+        return x, dx
+
+    def adjoint(self, dL_dx, dts, ckpt_stride: int = 0) -> np.ndarray:
+        """dnl_set_dt_schedule + dnl_adjoint: gradient of L(x_final) given dL/dx_final (N, 3)."""
+        dts = np.ascontiguousarray(dts, dtype=np.float64)
+        g = np.ascontiguousarray(dL_dx, dtype=np.float64)
+        assert g.size == 3 * self.model.N
+        self._check(self.L.dnl_set_dt_schedule(self.h, _ptr(dts), len(dts)))
+        grad = np.zeros(SENS_NPARAM)
+        self._check_run(self.L.dnl_adjoint(self.h, _ptr(g), _ptr(grad), int(ckpt_stride)))
+        return grad
+
+
+SENS_NPARAM = 4
+SENS_PARAMS = ("A", "B", "n", "v0")
+
+
+def model_with_params(model: Model, A: float, B: float, n: float, v0: float) -> Model:
+    """The model with hardening (A, B, n) and initial-velocity magnitude v0 (direction kept)."""
+    import dataclasses
+    u = np.asarray(model.v0, dtype=np.float64)
+    nu = float(np.linalg.norm(u))
+    return dataclasses.replace(model, A=float(A), B=float(B), n=float(n),
+                               v0=tuple(u / nu * float(v0)) if nu > 0 else tuple(u))
+
+
+def taylor_autograd():
+    """torch.autograd.Function over the GPU run: forward(params, model, dts) -> final coordinates.
+
+    ``params`` is a float64 tensor (A, B, n, |v0|); the forward pass runs dnl_sens_run, which
+    returns the final coordinates and their derivatives, and the backward pass contracts the
+    incoming gradient with those derivatives (forward-mode Jacobian, reverse-mode interface)."""
+    import torch
+
+    class TaylorRun(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, params, model, dts):
+            A, B, n, v0 = (float(v) for v in params.detach().cpu().tolist())
+            d = GpuDomain(model_with_params(model, A, B, n, v0))
+            try:
+                x, dx = d.sensitivities(dts)
+            finally:
+                d.close()
+            ctx.dx = torch.from_numpy(dx).to(params.device)
+            return torch.from_numpy(x).to(params.device)
+
+        @staticmethod
+        def backward(ctx, grad_x):
+            dx = ctx.dx
+            g = (dx * grad_x.to(dx.dtype).unsqueeze(0)).sum(dim=(1, 2))
+            return g, None, None
+
+    return TaylorRun
 
 
 class _HandleView(GpuDomain):

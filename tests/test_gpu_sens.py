@@ -1,0 +1,100 @@
+"""Forward-mode sensitivities on the GPU (dnl_sens_run / dnl_adjoint) against the sensitivity
+oracle (FP64 dual numbers through the restated run, oracle/dnl_sens.cc), with the same step-size
+schedule.  The GPU differentiates the polar decomposition with the spectral formula and the J2
+return by the implicit function theorem at the converged multiplier; the oracle carries dual
+numbers through the Newton iterations, which stop at a 1e-8 relative residual -- the two
+derivatives agree to that order.  Tolerance on each parameter's derivative field: 1e-5 relative
+(2-norm)."""
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle, SensOracle
+from redynela_gb300 import meshes
+
+pytestmark = pytest.mark.gpu
+
+SENS_TOL = 1e-5
+
+
+def rel(a, b):
+    return np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b))
+
+
+def schedule(m, nsteps):
+    o = Oracle(m)
+    o.prologue()
+    dts = []
+    for _ in range(nsteps):
+        dts.append(o.get("dt"))
+        o.steps(1)
+    return np.array(dts), o.array("coords").reshape(-1, 3).copy(), o.array("mass").copy()
+
+
+@pytest.mark.parametrize("etype,nsteps", [("axi", 300), ("hex", 80)])
+def test_sensitivities_vs_dual_oracle(gpu_lib, etype, nsteps):
+    m = meshes.taylor_axi(5, 50) if etype == "axi" else meshes.taylor_hex(4, 10)
+    dts, x_ref, mass = schedule(m, nsteps)
+    s = SensOracle(m, mass=mass)
+    s.run(dts)
+    xo, dxo = s.coords()
+    d = gpu_lib.GpuDomain(m)
+    x, dx = d.sensitivities(dts)
+    pos_tol = 1e-12 if etype == "axi" else 1e-8
+    assert np.max(np.abs(x - xo)) <= pos_tol * np.max(np.abs(xo))
+    for p in range(4):
+        assert np.linalg.norm(dxo[p]) > 0
+        assert rel(dx[p], dxo[p]) <= SENS_TOL, (p, rel(dx[p], dxo[p]))
+
+
+def test_sens_run_primal_is_the_plain_run(gpu_lib):
+    """The primal part of dnl_sens_run, given the plain run's own step sizes, is the plain run."""
+    m = meshes.taylor_axi(5, 50)
+    d = gpu_lib.GpuDomain(m)
+    d.prologue()
+    dts = []
+    for _ in range(200):
+        dts.append(d.time_info()["time_step"])
+        d.step(1)
+    x_plain = d.get_state("coords")["coords"]
+    x, _ = gpu_lib.GpuDomain(m).sensitivities(np.array(dts))
+    assert np.array_equal(x, x_plain)
+
+
+def test_adjoint_is_the_contraction(gpu_lib):
+    m = meshes.taylor_axi(4, 30)
+    dts, _, _ = schedule(m, 120)
+    rng = np.random.default_rng(3)
+    w = rng.normal(size=(m.N, 3))
+    _, dx = gpu_lib.GpuDomain(m).sensitivities(dts)
+    g = gpu_lib.GpuDomain(m).adjoint(w, dts, ckpt_stride=0)
+    ref = np.einsum("pnj,nj->p", dx, w)
+    assert np.allclose(g, ref, rtol=1e-12, atol=0)
+
+
+def test_torch_autograd_function(gpu_lib):
+    torch = pytest.importorskip("torch")
+    m = meshes.taylor_axi(4, 30)
+    dts, _, _ = schedule(m, 120)
+    run = gpu_lib.taylor_autograd()
+    v0 = float(np.linalg.norm(m.v0))
+    params = torch.tensor([m.A, m.B, m.n, v0], dtype=torch.float64, requires_grad=True)
+    target = torch.from_numpy(m.coords.copy())
+    x = run.apply(params, m, dts)
+    loss = ((x - target) ** 2).sum()
+    loss.backward()
+    # the same gradient from the derivatives directly
+    _, dx = gpu_lib.GpuDomain(m).sensitivities(dts)
+    ref = np.einsum("pnj,nj->p", dx, 2 * (x.detach().numpy() - m.coords))
+    assert np.allclose(params.grad.numpy(), ref, rtol=1e-12, atol=0)
+    # and central differences of the GPU run for the hardening parameters (h = 1e-6 relative)
+    for p in range(3):
+        h = 1e-6 * float(params[p])
+        vals = []
+        for sgn in (1, -1):
+            q = params.detach().clone()
+            q[p] += sgn * h
+            xq = run.apply(q, m, dts)
+            vals.append(float(((xq - target) ** 2).sum()))
+        fd = (vals[0] - vals[1]) / (2 * h)
+        assert abs(fd - float(params.grad[p])) <= 1e-4 * abs(float(params.grad[p])), p
