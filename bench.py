@@ -37,9 +37,10 @@ sys.path.insert(0, ROOT)
 
 from redynela_gb300 import meshes  # noqa: E402
 
-# dram__bytes_read.sum + dram__bytes_write.sum per k_elem launch from the ncu capture summarised in
-# profiles/ (k_elem on the 40x40x40 slice, scaled by elements to the full bar); None until captured
-ELEM_TRAFFIC_BYTES_PER_ELEMENT = None
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_elem launch per element, from the ncu capture
+# summarised in profiles/k_elem_hex_40x40x100_window.md (308.85 MB on the 126,400-element bar's
+# mid-run window); bench.py scales it by the elements of the workload
+ELEM_TRAFFIC_BYTES_PER_ELEMENT = 308.85e6 / 126400
 
 
 def workload(name: str, layers: int = 400):
@@ -116,6 +117,15 @@ class ClockSampler:
         load = [s for s in sm if mx and s > 0.3 * max(mx)] or sm
         return {"sm_mhz": float(np.median(load)) if load else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def peak_hbm():
+    """(HBM GB/s, "measured" | "fallback"): the copy bandwidth in MEASURED_PEAKS.json, else 6.8 TB/s."""
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peaks = json.load(open(pk)) if os.path.exists(pk) else {}
+    if "hbm_gbs" in peaks:
+        return float(peaks["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
 
 
 def dist_env():
@@ -258,12 +268,7 @@ def main_ours(args):
 
     # ---- roofline of the dominant kernel (k_elem)
     elem_ms, elem_n = prof["elem"]
-    peaks = {}
-    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(pk):
-        peaks = json.load(open(pk))
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    hbm_peak, peak_src = peak_hbm()
     bytes_per_launch = elem_bytes(model)
     achieved = bytes_per_launch / (elem_ms / elem_n * 1e-3) / 1e9 if elem_n else None
     traffic = (ELEM_TRAFFIC_BYTES_PER_ELEMENT * model.E) if ELEM_TRAFFIC_BYTES_PER_ELEMENT else None
@@ -381,13 +386,135 @@ def main_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def main_sens(args):
+    """Gradient workload: the 20x200 axisymmetric Taylor bar (4,000 ElQua4nAx elements) advanced
+    with a fixed step-size schedule -- the nominal run's own Courant steps, at most 4,000 -- and
+    L = |x_final(p) - x_target|^2 with x_target the final shape for (A, B, n) = (110 MPa, 310 MPa,
+    0.28).  One gradient = dL/d(A, B, n, |v0|) at the nominal parameters: dnl_reset with the
+    parameters, one forward-mode run (dnl_sens_run: the explicit run plus four tangent copies) and
+    the contraction with dL/dx.  `value`: gradients/s from CUDA events around the device work;
+    `e2e`: wall clock of the whole call sequence a user makes (reset, run, copies, contraction)."""
+    from redynela_gb300 import build, dynela
+    build.build()
+    m = meshes.taylor_axi(20, 200)
+    v0 = float(np.linalg.norm(m.v0))
+    sched = dynela.GpuDomain(m)
+    sched.prologue()
+    dts = []
+    while len(dts) < args.sens_steps:
+        info = sched.time_info()
+        if info["done"]:
+            break
+        dts.append(info["time_step"])
+        if sched.step(1) == 0:
+            break
+    sched.close()
+    dts = np.array(dts)
+    nst = len(dts)
+    target = dynela.model_with_params(m, 110e6, 310e6, 0.28, v0)
+    xt, _ = dynela.GpuDomain(target).sensitivities(dts)
+    d = dynela.GpuDomain(m)
+    surf = meshes.taylor_axi_free_surface(20, 200)  # outer radius and top face nodes
+    w = np.zeros((m.N, 3))
+
+    def gradient():
+        # L = mean over the free-surface nodes of |x - x_target|^2
+        d.reset(m)
+        x, dx = d.sensitivities(dts)
+        w[:] = 0.
+        w[surf] = 2.0 * (x[surf] - xt[surf]) / len(surf)
+        return np.einsum("pnj,nj->p", dx, w), x
+
+    for _ in range(args.warmup):
+        gradient()
+    launches0 = dynela.kernel_launches()
+    dev_ms = 0.0
+    d.profile_begin()
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            d.timer_mark(0)
+            g, x = gradient()
+            d.timer_mark(1)
+            dev_ms += d.timer_elapsed_ms(0, 1)
+        wall = time.perf_counter() - t0
+    prof = d.profile_end()
+    launches = (dynela.kernel_launches() - launches0) // args.steps
+    clocks = clk.summary()
+    value = args.steps / (dev_ms * 1e-3)
+    e2e = args.steps / wall
+    tan_ms, tan_n = prof["tangent"]
+    elem_ms, elem_n = prof["elem"]
+    total_ms = sum(v[0] for v in prof.values())
+    # agreement with the sensitivity oracle (FP64 dual numbers) over a bounded prefix, which is
+    # also the CPU baseline's sample
+    cpu = None
+    agree = None
+    if not args.no_cpu:
+        from oracle.oracle import Oracle, SensOracle
+        threads = os.cpu_count() or 1
+        o = Oracle(m, threads=threads)
+        o.prologue()
+        mass = o.array("mass").copy()
+        probe = 20
+        so = SensOracle(m, mass=mass, threads=threads)
+        t1 = time.perf_counter()
+        so.run(dts[:probe])
+        per_step = (time.perf_counter() - t1) / probe
+        k = int(min(nst, max(probe, args.cpu_seconds / max(per_step, 1e-9))))
+        so = SensOracle(m, mass=mass, threads=threads)
+        t1 = time.perf_counter()
+        so.run(dts[:k])
+        tc = time.perf_counter() - t1
+        _, dxo = so.coords()
+        d.reset(m)
+        _, dxg = d.sensitivities(dts[:k])
+        agree = max(float(np.linalg.norm(dxg[p] - dxo[p]) / np.linalg.norm(dxo[p])) for p in range(4))
+        cpu = {"value": 1.0 / (tc * nst / k), "unit": "gradients/s", "cores": threads, "kind": "port",
+               "sample": f"the sensitivity oracle (FP64 dual numbers, OpenMP) over the first {k} of "
+                         f"the {nst} steps, {tc:.1f} s, scaled to the full schedule"}
+    # tangent element pass: compulsory bytes per launch (tape and state read, tangent state
+    # read + written, element forces written) over its mean launch time
+    nip, ns = 4, 4
+    nt = 4 + 3 + 9 + 9 + 3 * 3 + 9 + ns + 4 + 3 * ns
+    tan_bytes = m.E * nip * 8 * (nt + (ns + 1) + 4 * 2 * (3 * ns + 2)) + m.E * 4 * 8 * 2 * 4
+    line = {"metric": "gradients/s", "value": value, "unit": "gradients/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (the reference Taylor deck's geometry)",
+            "config": {"workload": "taylor_axi_20x200_sensitivities", "elements": m.E,
+                       "explicit_steps": nst, "parameters": ["A", "B", "n", "|v0|"],
+                       "loss": "mean over the free-surface nodes (outer radius, impact-free end) of "
+                               "|x_final - x_final(A=110 MPa, B=310 MPa, n=0.28)|^2",
+                       "step": "one gradient = dnl_reset + dnl_sens_run + contraction",
+                       "l2": "state of 4,000 elements fits L2; each gradient is a 4,000-step run"},
+            "gradient": [float(v) for v in g],
+            "agreement_vs_dual_oracle": agree,
+            "gpu_launches": launches,
+            "kernel_time_share": {k: round(v[0] / total_ms, 4) for k, v in prof.items()} if total_ms else None,
+            "roofline": {"bound": "hbm", "achieved": tan_bytes / (tan_ms / max(tan_n, 1) * 1e-3) / 1e9,
+                         "peak": peak_hbm()[0], "unit": "GB/s",
+                         "frac": tan_bytes / (tan_ms / max(tan_n, 1) * 1e-3) / 1e9 / peak_hbm()[0],
+                         "avg_launch_ms": tan_ms / max(tan_n, 1), "algorithmic_bytes_per_launch": tan_bytes,
+                         "traffic": None, "kernel": "k_elem_tan<ElQua4nAx>",
+                         "peak_source": peak_hbm()[1],
+                         "note": "4,000 elements: launch-latency bound; the tangent pass is FP64 work"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e, "unit": "gradients/s", "h2d_bytes_per_step": 8 * (nst + 9),
+                    "d2h_bytes_per_step": 8 * 3 * m.N * 5},
+            "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="hex", choices=["hex", "axi", "batch"])
+    ap.add_argument("--config", default="hex", choices=["hex", "axi", "batch", "sens"])
+    ap.add_argument("--sens-steps", type=int, default=4000,
+                    help="explicit steps of the gradient workload's schedule")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--start-us", type=float, default=10.0,
@@ -404,6 +531,8 @@ def main():
         main_reference(args)
     elif args.config == "batch":
         main_batch(args)
+    elif args.config == "sens":
+        main_sens(args)
     else:
         main_ours(args)
 

@@ -209,6 +209,14 @@ typedef struct {
 } dnl_static_args;
 int dnl_internal_forces_static(const dnl_static_args *args, void *stream, int *bad_element);
 
+/* Back to the state dnl_create left: time 0, initial coordinates, velocity v0 on both nodal
+ * fields, zero stresses and strains, evp = 1e-10 (IntegrationPoint.C:117); optionally with a new
+ * material and initial velocity (NULL keeps the current ones).  The mesh, boundary conditions,
+ * solver settings and device allocations stay; captured graphs are dropped.  For loops over
+ * parameter sets (optimisation, sensitivities).  No counterpart in the reference, which rebuilds
+ * the Structure from the .dyn deck. */
+int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0);
+
 /* ------------------------------------------------------------------- sensitivities */
 /* Derivatives of a run's final nodal coordinates with respect to four parameters: the hardening
  * law's A, B, n (sigma_y = A + B evp^n, IsoHardElastoplastic.C:171-184) and the magnitude |v0| of
@@ -239,7 +247,8 @@ int dnl_adjoint(dnl_handle *h, const double *dL_dx, double *grad, int ckpt_strid
 #define DNL_PROF_PULSE 2   /* Pulse power-iteration kernels */
 #define DNL_PROF_COURANT 3 /* Courant length reduction */
 #define DNL_PROF_OTHER 4   /* time-step logic, boundary conditions */
-#define DNL_PROF_KINDS 5
+#define DNL_PROF_TANGENT 5 /* sensitivity run: tangent element pass (its nodal pass counts as NODE) */
+#define DNL_PROF_KINDS 6
 int dnl_profile_begin(dnl_handle *h);
 int dnl_profile_end(dnl_handle *h, double *ms, long long *launches);
 /* the handle's CUDA stream (a cudaStream_t), e.g. to record timing events around calls */

@@ -249,6 +249,9 @@ struct dnl_handle {
   // per-kernel event timing (dnl_profile_begin/end)
   bool profiling;
   void *prof;
+  // initial state (dnl_reset)
+  double *x0;                 // initial coordinates [3][N]
+  double v0[3];               // initial velocity
   // forward-mode sensitivities (dnl_sens.cu)
   double v0dir[3];            // unit vector of the initial velocity
   void *sens;

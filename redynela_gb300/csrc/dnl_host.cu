@@ -293,6 +293,12 @@ __global__ void k_soa_to_aos(int N, double *aos, const double *c0, const double 
 }
 
 // FP64 throughput probe: 8 independent DFMA chains per thread, ITER rounds
+__global__ void k_fill(double *p, long n, double v)
+{
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
 __global__ void k_fp64_peak(double *out, double a, double b, int iters)
 {
   double x0 = threadIdx.x * 1e-9, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5,
@@ -738,7 +744,7 @@ int dnl_destroy(dnl_handle *h)
   for (int i = 0; i < h->ngraphs; i++) cudaGraphExecDestroy(h->graphs[i].exec);
   void *ptrs[] = {h->conn, h->x[0], h->n2eStart, h->n2e, h->mass, h->fieldMem, h->ip, h->detJ,
                   h->stepT, h->fe, h->fint, h->stage, h->bcIdx, h->bcCode, h->bcNodeList, h->bcSpeed,
-                  h->pj, h->ev, h->kx, h->tm};
+                  h->pj, h->ev, h->kx, h->tm, h->x0};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; i++)
@@ -754,6 +760,61 @@ int dnl_destroy(dnl_handle *h)
     delete p;
   }
   delete h;
+  return 0;
+}
+
+int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0)
+{
+  if (!h) return DNL_ERR_ARG;
+  cudaStream_t s = h->stream;
+  CK(cudaStreamSynchronize(s));
+  for (int i = 0; i < h->ngraphs; i++) cudaGraphExecDestroy(h->graphs[i].exec);
+  h->ngraphs = 0;  // captured launches hold the old material and state by value
+  if (mat) {
+    h->mat = make_material(*mat);
+    const double Nu = h->mat.nu;
+    const double f = (h->mat.young * (1.0 - Nu) / ((1.0 + Nu) * (1.0 - 2.0 * Nu)));
+    h->C00 = 1 * f;
+    h->C01 = (Nu / (1. - Nu)) * f;
+    h->C33 = ((1.0 - 2.0 * Nu) / (2. * (1.0 - Nu))) * f;
+  }
+  if (v0) {
+    const double vn = sqrt(v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2]);
+    for (int c = 0; c < 3; c++) {
+      h->v0[c] = v0[c];
+      h->v0dir[c] = vn > 0 ? v0[c] / vn : 0.;
+    }
+  }
+  const long N = h->N, nIP = h->nIP;
+  CK(cudaMemcpyAsync(h->x[0], h->x0, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemsetAsync(h->fieldMem, 0, sizeof(double) * 24 * N, s));
+  for (int b = 0; b < 2; b++)
+    for (int c = 0; c < 3; c++) {
+      k_fill<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(h->bank[b].v[c], N, h->v0[c]);
+      launch_counter()++;
+    }
+  const int ncomp = h->etype == DNL_ELQUA4NAX ? IpLayout<DNL_ELQUA4NAX>::NCOMP : IpLayout<DNL_ELHEX8N3D>::NCOMP;
+  const int ns = h->etype == DNL_ELQUA4NAX ? 4 : 6;
+  CK(cudaMemsetAsync(h->ip, 0, sizeof(double) * ncomp * nIP, s));
+  k_fill<<<(unsigned)((nIP + 255) / 256), 256, 0, s>>>(h->ip + (size_t)(3 * ns + 1) * nIP, nIP, 1e-10);
+  k_fill<<<(unsigned)((nIP + 255) / 256), 256, 0, s>>>(h->ip + (size_t)(3 * ns + 2) * nIP, nIP,
+                                                       pow(1e-10, h->mat.n));
+  launch_counter() += 2;
+  CK(cudaMemsetAsync(h->fint, 0, sizeof(double) * h->dim * N, s));
+  if (h->stepT) CK(cudaMemsetAsync(h->stepT, 0, sizeof(double) * 18 * nIP, s));
+  DevTime t;
+  memset(&t, 0, sizeof t);
+  t.upTime = h->endTime;
+  t.endTime = h->endTime;
+  t.startTime = 0.;
+  t.lenMinBits = 0x7ff0000000000000ull;
+  t.badElem = -1;
+  CK(cudaMemcpyAsync(h->tm, &t, sizeof t, cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  if (check_launch()) return DNL_ERR_CUDA;
+  h->cur = 0;
+  h->prologueDone = false;
+  h->hostIncrement = 0;
   return 0;
 }
 
@@ -843,6 +904,8 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
       for (int r = 0; r < 3; r++) xs[(size_t)r * N + n] = mesh->coords[3 * (size_t)n + r];
     CKF(cudaMemcpy(xm, xs.data(), sizeof(double) * xs.size(), cudaMemcpyHostToDevice));
     for (int r = 0; r < 3; r++) h->x[r] = xm + (size_t)r * N;
+    CKF(cudaMalloc(&h->x0, sizeof(double) * 3 * (size_t)N));
+    CKF(cudaMemcpy(h->x0, xm, sizeof(double) * 3 * (size_t)N, cudaMemcpyDeviceToDevice));
   }
   // node -> (element, local node) CSR, ascending element order
   {
@@ -872,7 +935,10 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
     }
   {  // BoundarySpeed::applyInitial_V0 on both fields
     const double vn = sqrt(mesh->v0[0] * mesh->v0[0] + mesh->v0[1] * mesh->v0[1] + mesh->v0[2] * mesh->v0[2]);
-    for (int c = 0; c < 3; c++) h->v0dir[c] = vn > 0 ? mesh->v0[c] / vn : 0.;
+    for (int c = 0; c < 3; c++) {
+      h->v0[c] = mesh->v0[c];
+      h->v0dir[c] = vn > 0 ? mesh->v0[c] / vn : 0.;
+    }
     std::vector<double> v(N);
     for (int b = 0; b < 2; b++)
       for (int c = 0; c < 3; c++) {

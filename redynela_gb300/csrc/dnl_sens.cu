@@ -296,16 +296,21 @@ int dnl_sens_run(dnl_handle *h, int nsteps, const double *dts, double *coords, d
     if ((r = launch_elem_tape(h, s, S->tape))) return r;
     for (int c = 0; c < 3; c++) ea.du[c] = h->bank[h->cur].du[c];
     ea.tdu = S->tb[h->cur][0];
-    if ((r = launch_elem_tan(h->etype, ea, s))) return r;
+    prof_begin(h, s);
+    r = launch_elem_tan(h->etype, ea, s);
+    prof_end(h, DNL_PROF_TANGENT, s);
+    if (r) return r;
     if ((r = enqueue_node(h))) return r;
     for (int f = 0; f < 4; f++) {
       na.cur[f] = S->tb[h->cur][f];
       na.nxt[f] = S->tb[1 - h->cur][f];
     }
+    prof_begin(h, s);
     if (h->dim == 2)
       k_node_tan<2><<<ngrid, 256, 0, s>>>(na);
     else
       k_node_tan<3><<<ngrid, 256, 0, s>>>(na);
+    prof_end(h, DNL_PROF_NODE, s);
     launch_counter()++;
     h->cur = 1 - h->cur;
     k_sens_dt<<<1, 1, 0, s>>>(h->tm, S->dts, 1);

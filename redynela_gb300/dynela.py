@@ -35,7 +35,7 @@ STATUS_NAMES = {
     8: "DNL_ERR_SINGULAR", 9: "DNL_ERR_TIMEOUT",
 }
 FLAG_STEP_TENSORS = 1
-PROF_KINDS = ("elem", "node", "pulse", "courant", "other")
+PROF_KINDS = ("elem", "node", "pulse", "courant", "other", "tangent")
 
 
 class DnlError(RuntimeError):
@@ -132,6 +132,7 @@ def lib():
         L.dnl_sens_run.argtypes = [H, C.c_int, _dp, _dp, _dp]
         L.dnl_set_dt_schedule.argtypes = [H, _dp, C.c_int]
         L.dnl_adjoint.argtypes = [H, _dp, _dp, C.c_int]
+        L.dnl_reset.argtypes = [H, C.POINTER(MaterialDesc), _dp]
         _lib = L
     return _lib
 
@@ -345,6 +346,17 @@ class GpuDomain:
         t = TimeInfo()
         self._check(self.L.dnl_get_time_info(self.h, C.byref(t)))
         return {k: getattr(t, k) for k, _ in TimeInfo._fields_}
+
+    def reset(self, model: Optional[Model] = None) -> None:
+        """dnl_reset: back to the initial state; with ``model`` (same mesh), take its material and
+        initial velocity."""
+        if model is None:
+            self._check(self.L.dnl_reset(self.h, None, None))
+            return
+        mat = MaterialDesc(model.young, model.poisson, model.density, model.A, model.B, model.n)
+        v0 = np.ascontiguousarray(model.v0, dtype=np.float64)
+        self._check(self.L.dnl_reset(self.h, C.byref(mat), _ptr(v0)))
+        self.model = model
 
     def sensitivities(self, dts):
         """dnl_sens_run: the run with step sizes ``dts`` from the initial state; returns the final

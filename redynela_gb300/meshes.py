@@ -114,6 +114,14 @@ def taylor_axi(nr: int = 5, nz: int = 50, radius: float = 3.2e-3, length: float 
                  (0.0, -speed, 0.0), bcs, tend, rho_b, safety, freq, COURANT)
 
 
+def taylor_axi_free_surface(nr: int, nz: int) -> np.ndarray:
+    """Node ids of taylor_axi(nr, nz)'s free surface: the outer radius (i = nr) and the free end
+    (j = nz), node (i, j) = i + j (nr + 1), ascending and without repetition."""
+    outer = nr + np.arange(nz + 1, dtype=np.int64) * (nr + 1)
+    top = nz * (nr + 1) + np.arange(nr + 1, dtype=np.int64)
+    return np.unique(np.concatenate([outer, top]))
+
+
 def taylor_hex(ncross: int = 40, nz: int = 400, radius: float = 3.2e-3, length: float = 32.4e-3,
                speed: float = 227.0, A: float = 90e6, B: float = 292e6, n: float = 0.31,
                young: float = 117e9, poisson: float = 0.35, density: float = 8930.0,

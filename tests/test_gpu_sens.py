@@ -98,3 +98,28 @@ def test_torch_autograd_function(gpu_lib):
             vals.append(float(((xq - target) ** 2).sum()))
         fd = (vals[0] - vals[1]) / (2 * h)
         assert abs(fd - float(params.grad[p])) <= 1e-4 * abs(float(params.grad[p])), p
+
+
+def test_reset_returns_to_the_initial_state(gpu_lib):
+    """dnl_reset: a handle run, reset (with another material and speed) and run again gives what a
+    fresh handle of that model gives, bit for bit -- plain steps and sensitivities."""
+    m = meshes.taylor_axi(4, 30)
+    m2 = gpu_lib.model_with_params(m, 110e6, 310e6, 0.28, 250.0)
+    d = gpu_lib.GpuDomain(m)
+    d.step(80)
+    d.reset()
+    d.step(80)
+    ref = gpu_lib.GpuDomain(m)
+    ref.step(80)
+    assert np.array_equal(d.get_state("coords")["coords"], ref.get_state("coords")["coords"])
+    d.reset(m2)
+    d.step(80)
+    ref2 = gpu_lib.GpuDomain(m2)
+    ref2.step(80)
+    assert np.array_equal(d.get_state("coords")["coords"], ref2.get_state("coords")["coords"])
+    assert np.array_equal(d.get_state("S")["S"], ref2.get_state("S")["S"])
+    dts, _, _ = schedule(m, 60)
+    d.reset(m2)
+    x, dx = d.sensitivities(dts)
+    x2, dx2 = gpu_lib.GpuDomain(m2).sensitivities(dts)
+    assert np.array_equal(x, x2) and np.array_equal(dx, dx2)
