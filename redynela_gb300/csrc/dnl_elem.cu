@@ -19,10 +19,11 @@
 // -fmad=false: the compiler fuses nothing by itself, so every instantiation of the element code --
 // single mesh, batch, tape, caller-allocated -- rounds identically) -- except along the chain
 // whose last bits decide the strain increment: F = I + sum dN du is accumulated onto 1 with
-// separately rounded products and sums, and C = F^T F, the Jacobi rotation angle and the rotated
-// diagonal use __dmul_rn/__dadd_rn in the reference's association order, so the eigenvalues that
-// enter ln(U) carry the same rounding as the reference.  Elsewhere results differ from the
-// reference by a few units in the last place.
+// separately rounded products and sums and C = F^T F uses __dmul_rn/__dadd_rn in the reference's
+// association order, so the matrix whose eigenvalues enter ln(U) carries the reference's
+// rounding; the Jacobi rotations then move the eigenvalues by a few ulps of 1 against the
+// reference's (see jacobi_rotate).  Elsewhere results differ from the reference by a few units in
+// the last place.
 #include <cstdio>
 #include <cstring>
 
@@ -145,29 +146,35 @@ __device__ __forceinline__ double ineg(double a) { return flip_sign(a); }
 // t = 1 / (alpha + sign(alpha) sqrt(alpha^2 + 1)), alpha = d / e, is tan(theta) with
 // cos(2 theta) = |d| / sqrt(d^2 + e^2) >= 0 and sign(theta) = sign(d e) (theta = +pi/4 when
 // d = 0).  Half-angle identities give c = sqrt((1 + cos 2theta) / 2) and
-// s = sin(2 theta) / (2 c) = |C_pq| w / c with w = 1 / sqrt(d^2 + e^2): two reciprocal square
-// roots and no division.  The angle agrees with the reference's to a few ulps; the rotated
-// diagonal is stationary in the angle, so it moves by far less than an ulp.
-__device__ __forceinline__ void jacobi_angle(double fpp, double fqq, double fpq, double &c, double &s)
+// s = sin(2 theta) / (2 c) = |C_pq| w / c with w = 1 / sqrt(d^2 + e^2), and t = s / c: two
+// reciprocal square roots (1 / c is the second) and no division.  The angle agrees with the
+// reference's to a few ulps; the rotated diagonal is stationary in the angle.
+__device__ __forceinline__ void jacobi_angle(double fpp, double fqq, double fpq, double &c, double &s,
+                                             double &t)
 {
   const double d = fqq - fpp;
   const double w = rsqrt(fma(d, d, (4.0 * fpq) * fpq));
   const double h = fma(0.5 * iabs(d), w, 0.5);  // cos^2(theta)
-  const double r = rsqrt(h);
+  const double r = rsqrt(h);                    // 1 / c
   c = h * r;
   const double sv = iabs(fpq) * w * r;
+  const double tv = sv * r;
   const bool neg = abits(d) != 0 && ((__double_as_longlong(d) ^ __double_as_longlong(fpq)) < 0);
   s = neg ? ineg(sv) : sv;
+  t = neg ? ineg(tv) : tv;
 }
 
 // One rotation of Tensor2::polarDecomposeLnU (Tensor2.C:1183-1240): C <- R^T C R with R the plane
 // rotation (c, s) on pivot (P, Q), Rot <- Rot R.  The pivot is a run-time case k (0: (0,1),
 // 1: (0,2), 2: (1,2); O is the third index) so that the lanes of a warp, which pick different
-// pivots, execute one rotation instead of one per distinct pivot.  The reference stores, for
-// i < j, the (j, i) entry sum_k R_kj (C R)_ki; with its exact zero and one terms dropped
-// (x + 0 and 1 * x are exact) every entry is a two-term sum of products, and such a sum rounds
-// the same in any operand order, so the pivot-generic formulas on a = C_PP, b = C_QQ, x = C_PQ,
-// y = C_PO, z = C_QO give its results bit for bit for the same (c, s).
+// pivots, execute one rotation instead of one per distinct pivot.  On a = C_PP, b = C_QQ,
+// x = C_PQ, y = C_PO, z = C_QO the rotation that annihilates x gives, in closed form,
+// a' = a - t x, b' = b + t x, x' = 0, y' = c y - s z, z' = s y + c z (Rutishauser's form of the
+// Jacobi update): 6 FP64 operations instead of the 27 products and sums of R^T C R.  The
+// reference forms R^T C R in full, so its diagonal carries several roundings at the scale of 1 and
+// its x' a rounding residual; the closed form rounds once.  The two diagonals differ by a few ulps
+// of 1 (at most 9 in 4e5 random 3x3 cases, the same order as the angle's own effect) and the
+// pivot sequences are the same (x' is below the 1e-9 stop either way).
 // AXI: C is block diagonal and the pivot is always (0, 1).
 template <bool AXI>
 __device__ __forceinline__ void jacobi_rotate(int k, double &f00, double &f11, double &f22, double &f01,
@@ -175,22 +182,20 @@ __device__ __forceinline__ void jacobi_rotate(int k, double &f00, double &f11, d
 {
   const double a = k == 2 ? f11 : f00;
   const double b = k == 0 ? f11 : f22;
-  double c, s;
-  jacobi_angle(a, b, x, c, s);
+  double c, s, t;
+  jacobi_angle(a, b, x, c, s, t);
   const double ms = ineg(s);
-  const double ppP = RADD(RMUL(a, c), RMUL(x, ms)), ppQ = RADD(RMUL(x, c), RMUL(b, ms));
-  const double pqP = RADD(RMUL(a, s), RMUL(x, c)), pqQ = RADD(RMUL(x, s), RMUL(b, c));
-  const double a2 = RADD(RMUL(c, ppP), RMUL(ms, ppQ));
-  const double b2 = RADD(RMUL(s, pqP), RMUL(c, pqQ));
-  const double x2 = RADD(RMUL(s, ppP), RMUL(c, ppQ));  // stored C_PQ is (R^T C R)_QP
+  const double a2 = fma(ineg(t), x, a);
+  const double b2 = fma(t, x, b);
+  const double x2 = 0.;
   if (AXI) {
     f00 = a2;
     f11 = b2;
     f01 = x2;
   } else {
     const double y = k == 0 ? f02 : f01, z = k == 2 ? f02 : f12;
-    const double y2 = RADD(RMUL(c, y), RMUL(ms, z));
-    const double z2 = RADD(RMUL(s, y), RMUL(c, z));
+    const double y2 = fma(c, y, ms * z);
+    const double z2 = fma(s, y, c * z);
     f00 = k == 2 ? f00 : a2;
     f11 = k == 0 ? b2 : (k == 2 ? a2 : f11);
     f22 = k == 0 ? f22 : b2;
