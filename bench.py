@@ -506,13 +506,114 @@ def main_sens(args):
     print(json.dumps(line), flush=True)
 
 
+def main_necking(args):
+    """Batched sensitivities: 32 parameter sets (A, B, n drawn as for the batched Taylor bars) of
+    the tensile necking bar (ElHex8n3D, gauge radius 6.4 mm, length 53.3 mm, 209,824 elements each,
+    6.7 M in the batch; clamped end, the other pulled at 1 m/s, mass scaling x100) run as one batch
+    with their forward-mode derivatives, over a 30,000-step schedule of 3.55e-7 s.  The timed
+    region is K steps of that schedule (the full run is ~6 h of GPU time); `value` extrapolates
+    to gradients of the whole schedule: instances / (time per step x 30,000).  Loss: the
+    mid-length cross-section, mean over its nodes of x^2 + y^2 (the necking measure)."""
+    from redynela_gb300 import build, dynela
+    build.build()
+    nz = 166
+    models = meshes.necking_batch(args.necking_instances, seed=0, nz=nz)
+    total_steps = 30000
+    dt = models[0].tend / total_steps
+    probe = dynela.GpuDomain(models[0])
+    probe.prologue()
+    dt_stable = probe.time_step()
+    probe.close()
+    E = sum(m.E for m in models)
+    b = dynela.BatchDomain(models)
+    dts = np.full(max(args.warmup, args.steps), dt)
+    b.sensitivities(dts[:args.warmup], outputs=False)  # allocations, first launches
+    b.reset()
+    hv = b.handle_view()
+    launches0 = dynela.kernel_launches()
+    hv.profile_begin()
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        hv.timer_mark(0)
+        b.sensitivities(dts[:args.steps], outputs=False)
+        hv.timer_mark(1)
+        wall = time.perf_counter() - t0
+    ms = hv.timer_elapsed_ms(0, 1)
+    prof = hv.profile_end()
+    launches = dynela.kernel_launches() - launches0
+    clocks = clk.summary()
+    per_step = ms * 1e-3 / args.steps
+    value = len(models) / (per_step * total_steps)
+    tan_ms, tan_n = prof["tangent"]
+    total_ms = sum(v[0] for v in prof.values())
+    nip, ns, nt = 8, 6, 9 + 3 + 9 + 9 + 3 * 3 + 9 + 6 + 4 + 3 * 6
+    tan_bytes = E * nip * 8 * (nt + (ns + 1) + 4 * 2 * (3 * ns + 2)) + E * 8 * 3 * 8 * 4
+    achieved = tan_bytes / (tan_ms / max(tan_n, 1) * 1e-3) / 1e9 if tan_n else None
+    cpu = None
+    agree = None
+    if not args.no_cpu:
+        from oracle.oracle import SensOracle
+        threads = os.cpu_count() or 1
+        m0 = models[0]
+        g = dynela.GpuDomain(m0)
+        g.prologue()
+        mass = g.get_state("mass")["mass"].ravel().copy()  # lumped mass, bit-exact with the oracle's
+        g.close()
+        k = 2
+        so = SensOracle(m0, mass=mass, threads=threads)
+        t1 = time.perf_counter()
+        so.run(dts[:k])
+        tc = (time.perf_counter() - t1) / k
+        _, dxo = so.coords()
+        g = dynela.GpuDomain(m0)
+        _, dxg = g.sensitivities(dts[:k])
+        agree = max(float(np.linalg.norm(dxg[p] - dxo[p]) / np.linalg.norm(dxo[p]))
+                    for p in range(3) if np.linalg.norm(dxo[p]) > 0) if any(
+            np.linalg.norm(dxo[p]) > 0 for p in range(3)) else None
+        cpu = {"value": 1.0 / (tc * total_steps), "unit": "gradients/s", "cores": threads,
+               "kind": "port",
+               "sample": f"the sensitivity oracle (FP64 dual numbers, OpenMP) on one bar "
+                         f"({m0.E:,} elements), {k} steps, {tc:.2f} s per step, scaled to one "
+                         f"gradient of the 30,000-step schedule"}
+    line = {"metric": "gradients/s (batched, 3D)", "value": value, "unit": "gradients/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded parameter sets, numpy default_rng(0))",
+            "config": {"workload": f"necking_hex_batch_{len(models)}", "elements": E,
+                       "instances": len(models), "elements_per_instance": models[0].E,
+                       "schedule": f"{total_steps} steps of {dt:.4g} s (stable step at t=0: "
+                                   f"{dt_stable:.4g} s)",
+                       "timed": f"{args.steps} steps of the schedule, extrapolated to "
+                                f"{total_steps}",
+                       "parameters": ["A", "B", "n", "|v0| (0: starts at rest)"],
+                       "l2": "inputs larger than L2 (tangent state "
+                             f"{E * 8 * 4 * 20 * 8 / 1e9:.0f} GB)"},
+            "element_updates_per_s_with_tangents": E / per_step,
+            "agreement_vs_dual_oracle": agree,
+            "gpu_launches": launches,
+            "kernel_time_share": {k: round(v[0] / total_ms, 4) for k, v in prof.items()} if total_ms else None,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak_hbm()[0], "unit": "GB/s",
+                         "frac": achieved / peak_hbm()[0] if achieved else None, "traffic": None,
+                         "kernel": "k_elem_tan<ElHex8n3D>", "peak_source": peak_hbm()[1],
+                         "avg_launch_ms": tan_ms / max(tan_n, 1),
+                         "algorithmic_bytes_per_launch": tan_bytes,
+                         "note": "the tangent pass is FP64-pipe bound"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": 1.0 / (wall / args.steps * total_steps) * len(models), "unit": "gradients/s",
+                    "h2d_bytes_per_step": 8, "d2h_bytes_per_step": 0},
+            "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="hex", choices=["hex", "axi", "batch", "sens"])
+    ap.add_argument("--config", default="hex", choices=["hex", "axi", "batch", "sens", "necking"])
+    ap.add_argument("--necking-instances", type=int, default=32)
     ap.add_argument("--sens-steps", type=int, default=4000,
                     help="explicit steps of the gradient workload's schedule")
     ap.add_argument("--instances", type=int, default=256)
@@ -533,6 +634,8 @@ def main():
         main_batch(args)
     elif args.config == "sens":
         main_sens(args)
+    elif args.config == "necking":
+        main_necking(args)
     else:
         main_ours(args)
 

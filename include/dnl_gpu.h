@@ -155,11 +155,13 @@ int dnl_get_time_info(dnl_handle *h, dnl_time_info *info);
 int dnl_get_fint(dnl_handle *h, double *fint);
 
 /* ------------------------------------------------------------------------------ batches */
-/* Many independent meshes (same element type, Courant time step) advanced together: each keeps
- * its own material, time step, increment counter and end time (each instance is one
- * ExplicitSolverCH::solve of its own Domain); every kernel of a step is launched once for all
- * instances.  No counterpart in the reference, which solves one domain at a time
- * (Structure::solve, Structure.C:809-897). */
+/* Many independent meshes (same element type) advanced together: each keeps its own material,
+ * time step, increment counter and end time (each instance is one ExplicitSolverCH::solve of its
+ * own Domain); every kernel of a step is launched once for all instances.  dnl_batch_prologue,
+ * _step, _step_graph and _autotune need ElQua4nAx instances with the Courant time step (an even
+ * recomputation frequency) and return DNL_ERR_ARG otherwise; dnl_batch_sens_run (sensitivities,
+ * with a step schedule) takes any.  No counterpart in the reference, which solves one domain at a
+ * time (Structure::solve, Structure.C:809-897). */
 typedef struct dnl_batch dnl_batch;
 int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material *mats,
                      const dnl_solver_params *params, dnl_batch **out);
@@ -237,6 +239,13 @@ int dnl_set_dt_schedule(dnl_handle *h, const double *dts, int nsteps);
  * interface compatibility with checkpointed reverse-mode adjoints and unused: the forward mode
  * keeps no checkpoints. */
 int dnl_adjoint(dnl_handle *h, const double *dL_dx, double *grad, int ckpt_stride);
+/* The same for every instance of a batch at once, all with the schedule dts, from the batch's
+ * initial state; coords (3 x total nodes) and dcoords (4 x 3 x total nodes) in the union's node
+ * order (instance after instance, see dnl_batch_sizes).  A batch created for this may hold
+ * instances of either element type with either time-step method (the schedule replaces it). */
+int dnl_batch_sens_run(dnl_batch *b, int nsteps, const double *dts, double *coords, double *dcoords);
+/* every instance back to its initial state (as dnl_batch_create left it), device buffers kept */
+int dnl_batch_reset(dnl_batch *b);
 
 /* -------------------------------------------------------------------------- measurement */
 /* Per-kernel device time: between dnl_profile_begin and dnl_profile_end the library brackets each

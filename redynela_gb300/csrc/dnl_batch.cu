@@ -37,6 +37,12 @@ struct dnl_batch {
   int block;
   long long increment;  // host copy (all instances advance in lockstep until they finish)
   bool prologueDone;
+  bool massDone;
+  bool canStep;         // axisymmetric Courant instances: dnl_batch_step; any: dnl_batch_sens_run
+  double *v0dir;        // [count][3] unit initial velocity per instance
+  double *v0;           // [count][3] initial velocity per instance (dnl_batch_reset)
+  double *evpn0;        // [count] (1e-10)^n per instance (dnl_batch_reset)
+  std::vector<DevTime> t0;  // initial time records
   struct Graph {
     int nsteps, parity, phase;
     cudaGraphExec_t exec;
@@ -59,6 +65,23 @@ char g_batchError[256] = "";
   } while (0)
 
 enum { BT_FORCE = 1, BT_POST = 2, BT_PRE = 4 };  // same modes as the single-mesh time kernel
+
+// initial nodal velocities and evp^n cache per instance (dnl_batch_reset)
+__global__ void k_batch_init(int N, long nIP, int nip, const int *nodeInst, const int *elemInst,
+                             const double *v0, const double *evpn0, NodeFields b0, NodeFields b1,
+                             double *evp, double *evpn)
+{
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) {
+    const int inst = nodeInst[i];
+#pragma unroll
+    for (int c = 0; c < 3; c++) b0.v[c][i] = b1.v[c][i] = v0[3 * inst + c];
+  }
+  if (i < nIP) {
+    evp[i] = 1e-10;
+    evpn[i] = evpn0[elemInst[i / nip]];
+  }
+}
 
 int read_tms(dnl_batch *b, std::vector<DevTime> &t)
 {
@@ -108,7 +131,7 @@ int dnl_batch_destroy(dnl_batch *b)
 {
   if (!b) return DNL_ERR_ARG;
   for (int i = 0; i < b->ngraphs; i++) cudaGraphExecDestroy(b->graphs[i].exec);
-  void *ptrs[] = {b->elemInst, b->nodeInst, b->mats, b->prm, b->tms};
+  void *ptrs[] = {b->elemInst, b->nodeInst, b->mats, b->prm, b->tms, b->v0dir, b->v0, b->evpn0};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (b->h) dnl_destroy(b->h);
@@ -123,10 +146,13 @@ int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material 
   *out = nullptr;
   const int etype = meshes[0].etype;
   const int nen = etype == DNL_ELQUA4NAX ? 4 : 8;
+  // plain batched stepping needs the axisymmetric Courant step of every instance; sensitivity
+  // runs take a step schedule and accept any element type and time-step method
+  bool canStep = etype == DNL_ELQUA4NAX;
   for (int i = 0; i < count; i++) {
     if (meshes[i].etype != etype) return DNL_ERR_ARG;
-    if (sps[i].method != DNL_COURANT || etype != DNL_ELQUA4NAX) return DNL_ERR_ARG;
-    if (sps[i].frequency != sps[0].frequency || (sps[i].frequency % 2)) return DNL_ERR_ARG;
+    if (sps[i].method != sps[0].method || sps[i].frequency != sps[0].frequency) return DNL_ERR_ARG;
+    if (sps[i].method != DNL_COURANT || (sps[i].frequency % 2)) canStep = false;
     if (meshes[i].num_nodes <= 0 || meshes[i].num_elements <= 0) return DNL_ERR_ARG;
   }
   // ---- the union mesh
@@ -186,6 +212,11 @@ int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material 
   b->ngraphs = 0;
   b->increment = 0;
   b->prologueDone = false;
+  b->massDone = false;
+  b->canStep = canStep;
+  b->v0dir = nullptr;
+  b->v0 = nullptr;
+  b->evpn0 = nullptr;
   *out = b;
   auto fail = [&](int code) {
     dnl_batch_destroy(b);
@@ -233,6 +264,26 @@ int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material 
   BKF(cudaMemcpy(b->mats, hm.data(), sizeof(Material) * count, cudaMemcpyHostToDevice));
   BKF(cudaMemcpy(b->prm, b->hprm.data(), sizeof(InstParams) * count, cudaMemcpyHostToDevice));
   BKF(cudaMemcpy(b->tms, ht.data(), sizeof(DevTime) * count, cudaMemcpyHostToDevice));
+  {
+    std::vector<double> dirs(3 * (size_t)count);
+    for (int i = 0; i < count; i++) {
+      const double *v = meshes[i].v0;
+      const double vn = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+      for (int c = 0; c < 3; c++) dirs[3 * (size_t)i + c] = vn > 0 ? v[c] / vn : 0.;
+    }
+    BKF(cudaMalloc(&b->v0dir, sizeof(double) * 3 * count));
+    BKF(cudaMemcpy(b->v0dir, dirs.data(), sizeof(double) * 3 * count, cudaMemcpyHostToDevice));
+    std::vector<double> v0s(3 * (size_t)count), pn0(count);
+    for (int i = 0; i < count; i++) {
+      for (int c = 0; c < 3; c++) v0s[3 * (size_t)i + c] = meshes[i].v0[c];
+      pn0[i] = pow(1e-10, mats[i].n);
+    }
+    BKF(cudaMalloc(&b->v0, sizeof(double) * 3 * count));
+    BKF(cudaMemcpy(b->v0, v0s.data(), sizeof(double) * 3 * count, cudaMemcpyHostToDevice));
+    BKF(cudaMalloc(&b->evpn0, sizeof(double) * count));
+    BKF(cudaMemcpy(b->evpn0, pn0.data(), sizeof(double) * count, cudaMemcpyHostToDevice));
+    b->t0 = ht;
+  }
   // ---- per-instance initial speed (both fields) and cached evp^n at evp = 1e-10
   {
     std::vector<double> v(N);
@@ -248,7 +299,7 @@ int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material 
       const double val = pow(1e-10, mats[i].n);
       for (size_t q = (size_t)elemOff[i] * h->nip; q < (size_t)elemOff[i + 1] * h->nip; q++) pn[q] = val;
     }
-    const int ns = 4;
+    const int ns = etype == DNL_ELQUA4NAX ? 4 : 6;
     BKF(cudaMemcpy(h->ip + (size_t)(3 * ns + 2) * nIP, pn.data(), sizeof(double) * nIP, cudaMemcpyHostToDevice));
   }
   BKF(cudaDeviceSynchronize());
@@ -256,10 +307,9 @@ int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material 
   return 0;
 }
 
-int dnl_batch_prologue(dnl_batch *b)
+static int batch_mass(dnl_batch *b)
 {
-  if (!b) return DNL_ERR_ARG;
-  if (b->prologueDone) return 0;
+  if (b->massDone) return 0;
   dnl_handle *h = b->h;
   double *me;
   BK(cudaMalloc(&me, sizeof(double) * (size_t)h->E * h->nen));
@@ -272,8 +322,19 @@ int dnl_batch_prologue(dnl_batch *b)
   }
   BK(cudaStreamSynchronize(h->stream));
   cudaFree(me);
+  b->massDone = true;
+  return 0;
+}
+
+int dnl_batch_prologue(dnl_batch *b)
+{
+  if (!b || !b->canStep) return DNL_ERR_ARG;
+  if (b->prologueDone) return 0;
+  dnl_handle *h = b->h;
+  int r;
+  if ((r = batch_mass(b))) return r;
   // computeInternalForces with the initial (zero) Current field, then computeTimeStep(True)
-  a = elem_args_of(h);
+  ElemArgs a = elem_args_of(h);
   if ((r = launch_elem_batch(h->etype, b->block, a, b->elemInst, b->mats, b->tms, h->stream))) return r;
   if ((r = launch_courant_batch(a, b->elemInst, b->tms, h->stream))) return r;
   if ((r = launch_dt_batch(h, b->tms, b->prm, b->count, BT_FORCE))) return r;
@@ -385,6 +446,55 @@ int dnl_batch_autotune(dnl_batch *b, int steps_per_candidate, int *block)
   b->ngraphs = 0;
   if (block) *block = bestB;
   return r;
+}
+
+int dnl_batch_reset(dnl_batch *b)
+{
+  if (!b) return DNL_ERR_ARG;
+  dnl_handle *h = b->h;
+  cudaStream_t s = h->stream;
+  BK(cudaStreamSynchronize(s));
+  for (int i = 0; i < b->ngraphs; i++) cudaGraphExecDestroy(b->graphs[i].exec);
+  b->ngraphs = 0;
+  const long N = h->N, nIP = h->nIP;
+  const int ncomp = h->etype == DNL_ELQUA4NAX ? IpLayout<DNL_ELQUA4NAX>::NCOMP : IpLayout<DNL_ELHEX8N3D>::NCOMP;
+  const int ns = h->etype == DNL_ELQUA4NAX ? 4 : 6;
+  BK(cudaMemcpyAsync(h->x[0], h->x0, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
+  BK(cudaMemsetAsync(h->fieldMem, 0, sizeof(double) * 24 * N, s));
+  BK(cudaMemsetAsync(h->ip, 0, sizeof(double) * ncomp * nIP, s));
+  BK(cudaMemsetAsync(h->fint, 0, sizeof(double) * h->dim * N, s));
+  const long n = N > nIP ? N : nIP;
+  k_batch_init<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+      (int)N, nIP, h->nip, b->nodeInst, b->elemInst, b->v0, b->evpn0, h->bank[0], h->bank[1],
+      h->ip + (size_t)(3 * ns + 1) * nIP, h->ip + (size_t)(3 * ns + 2) * nIP);
+  launch_counter()++;
+  BK(cudaMemcpyAsync(b->tms, b->t0.data(), sizeof(DevTime) * b->count, cudaMemcpyHostToDevice, s));
+  BK(cudaStreamSynchronize(s));
+  BK(cudaGetLastError());
+  h->cur = 0;
+  h->hostIncrement = 0;
+  b->increment = 0;
+  b->prologueDone = false;
+  return 0;
+}
+
+int dnl_batch_sens_run(dnl_batch *b, int nsteps, const double *dts, double *coords, double *dcoords)
+{
+  if (!b || nsteps <= 0 || !dts || b->increment != 0) return DNL_ERR_ARG;
+  int r;
+  if ((r = batch_mass(b))) return r;
+  SensBatch bt;
+  bt.count = b->count;
+  bt.elemInst = b->elemInst;
+  bt.nodeInst = b->nodeInst;
+  bt.mats = b->mats;
+  bt.prm = b->prm;
+  bt.tms = b->tms;
+  bt.v0dir = b->v0dir;
+  r = sens_run(b->h, nsteps, dts, &bt);
+  b->increment = nsteps;
+  if (r) return r;
+  return sens_outputs(b->h, coords, dcoords);
 }
 
 int dnl_batch_set_block(dnl_batch *b, int block)

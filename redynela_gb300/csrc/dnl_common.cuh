@@ -166,6 +166,8 @@ struct SensElemArgs {
   double *tfe;         // [dir][DIM][E*NEN]
   DevTime *tm;
   Material mat;
+  const int *elemInst; // batched: instance of each element (its material), or nullptr
+  const Material *mats;
 };
 
 struct GatherArgs {
@@ -262,6 +264,19 @@ namespace dnl {
 int launch_elem(dnl_handle *h, cudaStream_t s, int gate);
 int launch_elem_tape(dnl_handle *h, cudaStream_t s, double *tape);
 int launch_elem_tan(int etype, const SensElemArgs &a, cudaStream_t s);
+int launch_elem_batch_tape(int etype, const ElemArgs &a, const int *elemInst, const Material *mats,
+                           DevTime *tms, cudaStream_t s);
+// batched instance tables for the sensitivity run (nullptr members: a single mesh)
+struct SensBatch {
+  int count;
+  const int *elemInst, *nodeInst;
+  const Material *mats;
+  const InstParams *prm;
+  DevTime *tms;
+  const double *v0dir;  // [count][3]
+};
+int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt);
+int sens_outputs(dnl_handle *h, double *coords, double *dcoords);
 void sens_free(dnl_handle *h);
 // primal per-step launches (dnl_host.cu) used by the sensitivity run
 int enqueue_bc_current(dnl_handle *h);

@@ -686,7 +686,7 @@ __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
 // Batched element pass over the union of many meshes: element e belongs to instance inst[e],
 // whose material and time record are mats[inst] and tms[inst]; instances that have finished or
 // failed keep their lanes in the warp but store nothing.
-template <int ET, int BLOCK>
+template <int ET, int BLOCK, bool TAPE = false>
 __global__ void __launch_bounds__(BLOCK) k_elem_batch(ElemArgs a, const int *elemInst,
                                                       const Material *mats, DevTime *tms)
 {
@@ -701,7 +701,7 @@ __global__ void __launch_bounds__(BLOCK) k_elem_batch(ElemArgs a, const int *ele
   DevTime *tm = tms + inst;
   const bool valid = eRaw < a.E && !(tm->done | tm->status);
   const int lane = threadIdx.x & 31;
-  elem_ip<ET>(a, mats[inst], tm, e, gtid % NIP, valid, lane, red[threadIdx.x >> 5][lane / NIP]);
+  elem_ip<ET, TAPE>(a, mats[inst], tm, e, gtid % NIP, valid, lane, red[threadIdx.x >> 5][lane / NIP]);
 }
 
 // ----------------------------------------------------------------------------- tangent pass
@@ -931,6 +931,20 @@ int launch_elem_batch(int etype, int block, const ElemArgs &a, const int *elemIn
     else DNL_EB(DNL_ELHEX8N3D, 128);
   }
 #undef DNL_EB
+  launch_counter()++;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
+}
+
+// batched element pass with its per-integration-point record (batched sensitivities)
+int launch_elem_batch_tape(int etype, const ElemArgs &a, const int *elemInst, const Material *mats,
+                           DevTime *tms, cudaStream_t s)
+{
+  const long threads = (long)a.E * (etype == DNL_ELQUA4NAX ? 4 : 8);
+  const int grid = (int)((threads + 127) / 128);
+  if (etype == DNL_ELQUA4NAX)
+    k_elem_batch<DNL_ELQUA4NAX, 128, true><<<grid, 128, 0, s>>>(a, elemInst, mats, tms);
+  else
+    k_elem_batch<DNL_ELHEX8N3D, 128, true><<<grid, 128, 0, s>>>(a, elemInst, mats, tms);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }

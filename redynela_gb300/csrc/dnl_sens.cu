@@ -33,8 +33,11 @@ struct SensState {
 
 namespace {
 
-__global__ void k_sens_dt(DevTime *tm, const double *dts, int phase)
+__global__ void k_sens_dt(DevTime *tms, int count, const double *dts, int phase)
 {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  DevTime *tm = tms + i;
   if (tm->status) return;
   if (phase == 0) {  // initStep with the scheduled step
     const double dt = dts[tm->increment];
@@ -74,6 +77,9 @@ struct SensNodeArgs {
   const int *bcIdx, *bcCode;
   const DevTime *tm;
   double alphaM, beta, gamma;
+  const int *nodeInst;      // batched: instance of each node (its time record and constants)
+  const InstParams *prm;
+  const DevTime *tms;
 };
 
 // tangent of node_update (dnl_host.cu): the predictor, the assembled force, the corrector and the
@@ -83,8 +89,14 @@ __global__ void __launch_bounds__(256) k_node_tan(SensNodeArgs g)
 {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   const int dir = blockIdx.y;
-  if (n >= g.N || g.tm->status) return;
-  const double dt = g.tm->timeStep;
+  if (n >= g.N) return;
+  const int inst = g.nodeInst ? g.nodeInst[n] : 0;
+  const DevTime *tm = g.nodeInst ? g.tms + inst : g.tm;
+  if (tm->status) return;
+  const double dt = tm->timeStep;
+  const double alphaM = g.nodeInst ? g.prm[inst].alphaM : g.alphaM;
+  const double beta = g.nodeInst ? g.prm[inst].beta : g.beta;
+  const double gamma = g.nodeInst ? g.prm[inst].gamma : g.gamma;
   const long N = g.N, base = (long)dir * 3 * N;
   double cdu[3], cv[3], ca[3], cd[3], ndu[3], nv[3], na[3];
 #pragma unroll
@@ -95,7 +107,7 @@ __global__ void __launch_bounds__(256) k_node_tan(SensNodeArgs g)
     cd[i] = g.cur[3][base + i * N + n];
   }
   (void)cdu;
-  const double c1 = dt * (0.5 - g.beta), c2 = dt * (1. - g.gamma);
+  const double c1 = dt * (0.5 - beta), c2 = dt * (1. - gamma);
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     ndu[i] = (ca[i] * c1 + cv[i]) * dt;
@@ -119,10 +131,10 @@ __global__ void __launch_bounds__(256) k_node_tan(SensNodeArgs g)
   const double m = g.mass[n];
 #pragma unroll
   for (int c = 0; c < DIM; c++) na[c] = f[c] / m;
-  const double cg = dt * g.gamma, cb = dt * dt * g.beta, oma = 1. - g.alphaM;
+  const double cg = dt * gamma, cb = dt * dt * beta, oma = 1. - alphaM;
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    na[i] = (na[i] - g.alphaM * ca[i]) / oma;
+    na[i] = (na[i] - alphaM * ca[i]) / oma;
     nv[i] = fma(cg, na[i], nv[i]);
     ndu[i] = fma(cb, na[i], ndu[i]);
     if ((code >> (2 * i)) & 3) na[i] = nv[i] = ndu[i] = 0.;
@@ -138,13 +150,17 @@ __global__ void __launch_bounds__(256) k_node_tan(SensNodeArgs g)
   }
 }
 
-// initial tangents: the initial velocity v0 = |v0| u on both fields, d v / d|v0| = u
-__global__ void k_sens_seed(int N, double *v0bank, double *v1bank, double u0, double u1, double u2)
+// initial tangents: the initial velocity v0 = |v0| u on both fields, d v / d|v0| = u (per
+// instance in a batch: u of the node's instance)
+__global__ void k_sens_seed(int N, double *v0bank, double *v1bank, double u0, double u1, double u2,
+                            const int *nodeInst, const double *v0dir)
 {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
   const long base = 3L * 3 * N;  // direction 3
-  const double u[3] = {u0, u1, u2};
+  double u[3] = {u0, u1, u2};
+  if (nodeInst)
+    for (int c = 0; c < 3; c++) u[c] = v0dir[3 * nodeInst[n] + c];
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     v0bank[base + c * (long)N + n] = u[c];
@@ -197,6 +213,158 @@ int sens_alloc(dnl_handle *h, SensState *S)
 
 }  // namespace
 
+// The sensitivity run on a handle (bt == nullptr) or on a batch's union mesh: zero the tangents,
+// seed d v / d|v0|, then per step the primal launches of the single-mesh or batched path with the
+// scheduled step size, each followed by its tangent launch.
+int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt)
+{
+  for (int k = 0; k < nsteps; k++)
+    if (!(dts[k] > 0. && dts[k] < 1e300)) return DNL_ERR_ARG;
+  int r;
+  if (!h->sens) h->sens = new SensState();
+  SensState *S = (SensState *)h->sens;
+  if (!S->mem && (r = sens_alloc(h, S))) return r;
+  cudaStream_t s = h->stream;
+  const long nIP = (long)h->E * h->nip;
+  {
+    const int NT = h->etype == DNL_ELQUA4NAX ? TapeLayout<DNL_ELQUA4NAX>::NT : TapeLayout<DNL_ELHEX8N3D>::NT;
+    const size_t bytes = sizeof(double) * (size_t)((S->out - S->mem) - NT * nIP);
+    CKS(cudaMemsetAsync(S->tx, 0, bytes, s));
+  }
+  k_sens_seed<<<(h->N + 255) / 256, 256, 0, s>>>(h->N, S->tb[0][1], S->tb[1][1], h->v0dir[0], h->v0dir[1],
+                                                  h->v0dir[2], bt ? bt->nodeInst : nullptr,
+                                                  bt ? bt->v0dir : nullptr);
+  launch_counter()++;
+  if (S->dtsCap < nsteps) {
+    if (S->dts) cudaFree(S->dts);
+    S->dts = nullptr;
+    S->dtsCap = 0;
+    CKS(cudaMalloc(&S->dts, sizeof(double) * nsteps));
+    S->dtsCap = nsteps;
+  }
+  CKS(cudaMemcpyAsync(S->dts, dts, sizeof(double) * nsteps, cudaMemcpyHostToDevice, s));
+
+  DevTime *tms = bt ? bt->tms : h->tm;
+  const int ninst = bt ? bt->count : 1;
+  SensElemArgs ea;
+  memset(&ea, 0, sizeof ea);
+  ea.E = h->E;
+  ea.N = h->N;
+  ea.conn = h->conn;
+  for (int c = 0; c < 3; c++) ea.x[c] = h->x[c];
+  ea.ip = h->ip;
+  ea.tape = S->tape;
+  ea.tx = S->tx;
+  ea.tip = S->tip;
+  ea.tfe = S->tfe;
+  ea.tm = h->tm;
+  ea.mat = h->mat;
+  ea.elemInst = bt ? bt->elemInst : nullptr;
+  ea.mats = bt ? bt->mats : nullptr;
+  SensNodeArgs na;
+  memset(&na, 0, sizeof na);
+  na.N = h->N;
+  na.EN = h->E * h->nen;
+  na.start = h->n2eStart;
+  na.entry = h->n2e;
+  na.tfe = S->tfe;
+  na.mass = h->mass;
+  na.tx = S->tx;
+  na.bcIdx = h->bcIdx;
+  na.bcCode = h->bcCode;
+  na.tm = h->tm;
+  na.alphaM = h->alphaM;
+  na.beta = h->beta;
+  na.gamma = h->gamma;
+  na.nodeInst = bt ? bt->nodeInst : nullptr;
+  na.prm = bt ? bt->prm : nullptr;
+  na.tms = bt ? bt->tms : nullptr;
+  const dim3 ngrid((h->N + 255) / 256, kSensParams);
+  const int tgrid = (ninst + 127) / 128;
+  for (int k = 0; k < nsteps; k++) {
+    k_sens_dt<<<tgrid, 128, 0, s>>>(tms, ninst, S->dts, 0);
+    launch_counter()++;
+    if (bt)
+      r = launch_bc_batch(h, bt->tms, bt->nodeInst);
+    else
+      r = enqueue_bc_current(h);
+    if (r) return r;
+    if (h->nbcNodes) {
+      double **tc = S->tb[h->cur];
+      k_bc_tan<<<(h->nbcNodes + 127) / 128, 128, 0, s>>>(h->nbcNodes, h->bcNodeList, h->bcCode, h->N, tc[0],
+                                                         tc[1], tc[2]);
+      launch_counter()++;
+    }
+    if (bt) {
+      ElemArgs a = elem_args_of(h);
+      a.tape = S->tape;
+      prof_begin(h, s);
+      r = launch_elem_batch_tape(h->etype, a, bt->elemInst, bt->mats, bt->tms, s);
+      prof_end(h, DNL_PROF_ELEM, s);
+    } else {
+      r = launch_elem_tape(h, s, S->tape);
+    }
+    if (r) return r;
+    for (int c = 0; c < 3; c++) ea.du[c] = h->bank[h->cur].du[c];
+    ea.tdu = S->tb[h->cur][0];
+    prof_begin(h, s);
+    r = launch_elem_tan(h->etype, ea, s);
+    prof_end(h, DNL_PROF_TANGENT, s);
+    if (r) return r;
+    if (bt)
+      r = launch_node_batch(h, bt->nodeInst, bt->prm, bt->tms);
+    else
+      r = enqueue_node(h);
+    if (r) return r;
+    for (int f = 0; f < 4; f++) {
+      na.cur[f] = S->tb[h->cur][f];
+      na.nxt[f] = S->tb[1 - h->cur][f];
+    }
+    prof_begin(h, s);
+    if (h->dim == 2)
+      k_node_tan<2><<<ngrid, 256, 0, s>>>(na);
+    else
+      k_node_tan<3><<<ngrid, 256, 0, s>>>(na);
+    prof_end(h, DNL_PROF_NODE, s);
+    launch_counter()++;
+    h->cur = 1 - h->cur;
+    k_sens_dt<<<tgrid, 128, 0, s>>>(tms, ninst, S->dts, 1);
+    launch_counter()++;
+    if (cudaPeekAtLastError() != cudaSuccess) return DNL_ERR_CUDA;
+  }
+  std::vector<DevTime> t(ninst);
+  CKS(cudaMemcpyAsync(t.data(), tms, sizeof(DevTime) * ninst, cudaMemcpyDeviceToHost, s));
+  CKS(cudaStreamSynchronize(s));
+  h->hostIncrement = t[0].increment;
+  for (const DevTime &ti : t)
+    if (ti.status) return ti.status;
+  return 0;
+}
+
+// final coordinates (3N, node-major) and their derivatives (4 x 3N) of the last sensitivity run
+int sens_outputs(dnl_handle *h, double *coords, double *dcoords)
+{
+  SensState *S = (SensState *)h->sens;
+  if (!S || !S->mem) return DNL_ERR_ARG;
+  cudaStream_t s = h->stream;
+  const long N = h->N;
+  const int grid = (h->N + 255) / 256;
+  if (coords) {
+    k_to_nodes<<<grid, 256, 0, s>>>(h->N, S->out, h->x[0], h->x[1], h->x[2]);
+    CKS(cudaMemcpyAsync(coords, S->out, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s));
+    CKS(cudaStreamSynchronize(s));
+  }
+  if (dcoords)
+    for (int dir = 0; dir < kSensParams; dir++) {
+      const double *b = S->tx + (long)dir * 3 * N;
+      k_to_nodes<<<grid, 256, 0, s>>>(h->N, S->out, b, b + N, b + 2 * N);
+      CKS(cudaMemcpyAsync(dcoords + (long)dir * 3 * N, S->out, sizeof(double) * 3 * N,
+                          cudaMemcpyDeviceToHost, s));
+      CKS(cudaStreamSynchronize(s));
+    }
+  return 0;
+}
+
 void sens_free(dnl_handle *h)
 {
   SensState *S = (SensState *)h->sens;
@@ -226,116 +394,11 @@ int dnl_set_dt_schedule(dnl_handle *h, const double *dts, int nsteps)
 int dnl_sens_run(dnl_handle *h, int nsteps, const double *dts, double *coords, double *dcoords)
 {
   if (!h || nsteps <= 0 || !dts) return DNL_ERR_ARG;
-  for (int k = 0; k < nsteps; k++)
-    if (!(dts[k] > 0. && dts[k] < 1e300)) return DNL_ERR_ARG;
   if (h->hostIncrement != 0) return DNL_ERR_ARG;  // starts from the initial state
   int r;
   if (!h->prologueDone && (r = dnl_prologue(h))) return r;
-  if (!h->sens) h->sens = new SensState();
-  SensState *S = (SensState *)h->sens;
-  if (!S->mem && (r = sens_alloc(h, S))) return r;
-  cudaStream_t s = h->stream;
-  const long nIP = (long)h->E * h->nip, N = h->N;
-  // zero every tangent, then seed d v / d|v0|
-  {
-    const int NT = h->etype == DNL_ELQUA4NAX ? TapeLayout<DNL_ELQUA4NAX>::NT : TapeLayout<DNL_ELHEX8N3D>::NT;
-    const size_t bytes = sizeof(double) * (size_t)((S->out - S->mem) - NT * nIP);
-    CKS(cudaMemsetAsync(S->tx, 0, bytes, s));
-  }
-  k_sens_seed<<<(h->N + 255) / 256, 256, 0, s>>>(h->N, S->tb[0][1], S->tb[1][1], h->v0dir[0], h->v0dir[1],
-                                                  h->v0dir[2]);
-  launch_counter()++;
-  if (S->dtsCap < nsteps) {
-    if (S->dts) cudaFree(S->dts);
-    S->dts = nullptr;
-    S->dtsCap = 0;
-    CKS(cudaMalloc(&S->dts, sizeof(double) * nsteps));
-    S->dtsCap = nsteps;
-  }
-  CKS(cudaMemcpyAsync(S->dts, dts, sizeof(double) * nsteps, cudaMemcpyHostToDevice, s));
-
-  SensElemArgs ea;
-  memset(&ea, 0, sizeof ea);
-  ea.E = h->E;
-  ea.N = h->N;
-  ea.conn = h->conn;
-  for (int c = 0; c < 3; c++) ea.x[c] = h->x[c];
-  ea.ip = h->ip;
-  ea.tape = S->tape;
-  ea.tx = S->tx;
-  ea.tip = S->tip;
-  ea.tfe = S->tfe;
-  ea.tm = h->tm;
-  ea.mat = h->mat;
-  SensNodeArgs na;
-  memset(&na, 0, sizeof na);
-  na.N = h->N;
-  na.EN = h->E * h->nen;
-  na.start = h->n2eStart;
-  na.entry = h->n2e;
-  na.tfe = S->tfe;
-  na.mass = h->mass;
-  na.tx = S->tx;
-  na.bcIdx = h->bcIdx;
-  na.bcCode = h->bcCode;
-  na.tm = h->tm;
-  na.alphaM = h->alphaM;
-  na.beta = h->beta;
-  na.gamma = h->gamma;
-  const dim3 ngrid((h->N + 255) / 256, kSensParams);
-  for (int k = 0; k < nsteps; k++) {
-    k_sens_dt<<<1, 1, 0, s>>>(h->tm, S->dts, 0);
-    launch_counter()++;
-    if ((r = enqueue_bc_current(h))) return r;
-    if (h->nbcNodes) {
-      double **tc = S->tb[h->cur];
-      k_bc_tan<<<(h->nbcNodes + 127) / 128, 128, 0, s>>>(h->nbcNodes, h->bcNodeList, h->bcCode, h->N, tc[0],
-                                                         tc[1], tc[2]);
-      launch_counter()++;
-    }
-    if ((r = launch_elem_tape(h, s, S->tape))) return r;
-    for (int c = 0; c < 3; c++) ea.du[c] = h->bank[h->cur].du[c];
-    ea.tdu = S->tb[h->cur][0];
-    prof_begin(h, s);
-    r = launch_elem_tan(h->etype, ea, s);
-    prof_end(h, DNL_PROF_TANGENT, s);
-    if (r) return r;
-    if ((r = enqueue_node(h))) return r;
-    for (int f = 0; f < 4; f++) {
-      na.cur[f] = S->tb[h->cur][f];
-      na.nxt[f] = S->tb[1 - h->cur][f];
-    }
-    prof_begin(h, s);
-    if (h->dim == 2)
-      k_node_tan<2><<<ngrid, 256, 0, s>>>(na);
-    else
-      k_node_tan<3><<<ngrid, 256, 0, s>>>(na);
-    prof_end(h, DNL_PROF_NODE, s);
-    launch_counter()++;
-    h->cur = 1 - h->cur;
-    k_sens_dt<<<1, 1, 0, s>>>(h->tm, S->dts, 1);
-    launch_counter()++;
-    if (cudaPeekAtLastError() != cudaSuccess) return DNL_ERR_CUDA;
-  }
-  DevTime t;
-  if ((r = read_time_state(h, &t))) return r;
-  h->hostIncrement = t.increment;
-  if (t.status) return t.status;
-  const int grid = (h->N + 255) / 256;
-  if (coords) {
-    k_to_nodes<<<grid, 256, 0, s>>>(h->N, S->out, h->x[0], h->x[1], h->x[2]);
-    CKS(cudaMemcpyAsync(coords, S->out, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s));
-    CKS(cudaStreamSynchronize(s));
-  }
-  if (dcoords)
-    for (int dir = 0; dir < kSensParams; dir++) {
-      const double *b = S->tx + (long)dir * 3 * N;
-      k_to_nodes<<<grid, 256, 0, s>>>(h->N, S->out, b, b + N, b + 2 * N);
-      CKS(cudaMemcpyAsync(dcoords + (long)dir * 3 * N, S->out, sizeof(double) * 3 * N,
-                          cudaMemcpyDeviceToHost, s));
-      CKS(cudaStreamSynchronize(s));
-    }
-  return 0;
+  if ((r = sens_run(h, nsteps, dts, nullptr))) return r;
+  return sens_outputs(h, coords, dcoords);
 }
 
 int dnl_adjoint(dnl_handle *h, const double *dL_dx, double *grad, int ckpt_stride)

@@ -28,7 +28,7 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
   constexpr int NIP = T::NIP, NEN = T::NEN, DIM = T::DIM, NS = T::NS;
   constexpr bool AXI = ET == DNL_ELQUA4NAX;
   const long nIP = (long)a.E * NIP, ipx = (long)e * NIP + pt, N = a.N;
-  const Material &m = a.mat;
+  const Material &m = a.elemInst ? a.mats[a.elemInst[e]] : a.mat;
   auto tp = [&](int slot) { return a.tape[(long)slot * nIP + ipx]; };
   const double *tx = a.tx + (long)dir * 3 * N, *tdu = a.tdu + (long)dir * 3 * N;
   double *tip = a.tip + (long)dir * TN::NCOMP * nIP;
@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(128) k_elem_tan(SensElemArgs a)
   constexpr int NIP = Elem<ET>::NIP, NEN = Elem<ET>::NEN, DIM = Elem<ET>::DIM;
   constexpr int GPW = 32 / NIP;  // (element, direction) groups per warp
   __shared__ double red[128 / 32][GPW][NIP * NEN * DIM];
-  if (a.tm->status) return;
+  if (!a.elemInst && a.tm->status) return;
   const long groups = (long)a.E * kSensParams;
   const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if ((gtid & ~31L) / NIP >= groups) return;

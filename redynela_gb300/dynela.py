@@ -133,6 +133,8 @@ def lib():
         L.dnl_set_dt_schedule.argtypes = [H, _dp, C.c_int]
         L.dnl_adjoint.argtypes = [H, _dp, _dp, C.c_int]
         L.dnl_reset.argtypes = [H, C.POINTER(MaterialDesc), _dp]
+        L.dnl_batch_sens_run.argtypes = [H, C.c_int, _dp, _dp, _dp]
+        L.dnl_batch_reset.argtypes = [H]
         _lib = L
     return _lib
 
@@ -522,6 +524,26 @@ class BatchDomain:
     def fint(self, i: int) -> np.ndarray:
         out = np.zeros(self.models[i].N * self.models[i].dim)
         self._check(self.L.dnl_batch_get_fint(self.h, int(i), _ptr(out)))
+        return out
+
+    def reset(self) -> None:
+        """dnl_batch_reset: every instance back to its initial state."""
+        self._check(self.L.dnl_batch_reset(self.h))
+
+    def sensitivities(self, dts, outputs: bool = True):
+        """dnl_batch_sens_run: every instance with step sizes ``dts``; returns, per instance, the
+        final coordinates (N_i, 3) and their derivatives (4, N_i, 3) (nothing if not outputs)."""
+        dts = np.ascontiguousarray(dts, dtype=np.float64)
+        if not outputs:
+            self._check(self.L.dnl_batch_sens_run(self.h, len(dts), _ptr(dts), None, None))
+            return None
+        x = np.zeros((self.N, 3))
+        dx = np.zeros((SENS_NPARAM, self.N, 3))
+        self._check(self.L.dnl_batch_sens_run(self.h, len(dts), _ptr(dts), _ptr(x), _ptr(dx)))
+        out, off = [], 0
+        for m in self.models:
+            out.append((x[off:off + m.N].copy(), dx[:, off:off + m.N].copy()))
+            off += m.N
         return out
 
     def handle_view(self) -> GpuDomain:

@@ -21,6 +21,7 @@ Generators:
 
 from __future__ import annotations
 
+import dataclasses
 from dataclasses import dataclass, field
 from typing import List, Sequence
 
@@ -165,6 +166,57 @@ def taylor_hex(ncross: int = 40, nz: int = 400, radius: float = 3.2e-3, length: 
     bcs = [BCGroup(RESTRAIN, (0.0, 0.0, 1.0), base)]
     return Model(ELHEX8N3D, coords, conn, young, poisson, density, A, B, n,
                  (0.0, 0.0, -speed), bcs, tend, rho_b, safety, freq, PULSE)
+
+
+def necking_bar(ncross: int = 40, nz: int = 166, radius: float = 6.4e-3, length: float = 53.3e-3,
+                speed: float = 1.0, A: float = 90e6, B: float = 292e6, n: float = 0.31,
+                young: float = 117e9, poisson: float = 0.35, density: float = 8930.0,
+                mass_scaling: float = 100.0, imperfection: float = 0.005,
+                tend: float = 10.66e-3, freq: int = 10, safety: float = 0.9,
+                rho_b: float = 0.8182) -> Model:
+    """3D tensile bar of ElHex8n3D for necking: the cross-section grid of taylor_hex (gauge radius
+    6.4 mm, length 53.3 mm; ncross=40, nz=166 gives 1264 cells per layer, 209,824 elements), the
+    end z = 0 clamped (BoundaryRestrain 1 1 1), the end z = L pulled at `speed` along z
+    (BoundarySpeed 0 0 speed; x and y free), starting at rest.  The radius is reduced by the
+    relative `imperfection` around mid-length, r(z) = R (1 - imp exp(-((z - L/2) / (0.1 L))^2)),
+    so that the neck forms there.  The density is multiplied by `mass_scaling` (mass scaling: with
+    the default 100 the stable step grows tenfold and 30,000 steps of 3.55e-7 s cover the 10.66 ms
+    it takes to stretch the bar by 20 % at 1 m/s); copper J2 hardening as the Taylor bars.
+    Node numbering as taylor_hex: layer by layer along z."""
+    m = taylor_hex(ncross, nz, radius, length, 0.0, A, B, n, young, poisson, density * mass_scaling,
+                   tend, freq, safety, rho_b)
+    coords = m.coords.copy()
+    z = coords[:, 2]
+    scale = 1.0 - imperfection * np.exp(-(((z - 0.5 * length) / (0.1 * length)) ** 2))
+    coords[:, 0] *= scale
+    coords[:, 1] *= scale
+    nlayer = m.N // (nz + 1)
+    base = np.arange(nlayer, dtype=np.int64)
+    top = nz * nlayer + np.arange(nlayer, dtype=np.int64)
+    bcs = [BCGroup(RESTRAIN, (1.0, 1.0, 1.0), base), BCGroup(SPEED, (0.0, 0.0, speed), top)]
+    return Model(ELHEX8N3D, coords, m.conn, young, poisson, density * mass_scaling, A, B, n,
+                 (0.0, 0.0, 0.0), bcs, tend, rho_b, safety, freq, PULSE)
+
+
+def necking_mid_nodes(model: Model, nz: int) -> np.ndarray:
+    """Node ids of the mid-length layer (z = L/2 for even nz) of a necking_bar(.., nz, ..)."""
+    nlayer = model.N // (nz + 1)
+    k = nz // 2
+    return k * nlayer + np.arange(nlayer, dtype=np.int64)
+
+
+def necking_batch(count: int = 32, seed: int = 0, ncross: int = 40, nz: int = 166,
+                  A_range=(60e6, 150e6), B_range=(200e6, 400e6), n_range=(0.2, 0.5)) -> List[Model]:
+    """Seeded parameter sets (A, B, n drawn as in taylor_batch) on one necking bar mesh."""
+    rng = np.random.default_rng(seed)
+    base = necking_bar(ncross, nz)
+    out = []
+    for _ in range(count):
+        A = float(rng.uniform(*A_range))
+        B = float(rng.uniform(*B_range))
+        nn = float(rng.uniform(*n_range))
+        out.append(dataclasses.replace(base, A=A, B=B, n=nn))
+    return out
 
 
 def taylor_batch(count: int = 256, seed: int = 0, nr_range=(4, 40), nz_range=(40, 400),

@@ -123,3 +123,46 @@ def test_reset_returns_to_the_initial_state(gpu_lib):
     x, dx = d.sensitivities(dts)
     x2, dx2 = gpu_lib.GpuDomain(m2).sensitivities(dts)
     assert np.array_equal(x, x2) and np.array_equal(dx, dx2)
+
+
+def _small_necking(count):
+    base = meshes.necking_bar(6, 12)
+    rng = np.random.default_rng(7)
+    import dataclasses
+    return [dataclasses.replace(base, A=float(rng.uniform(60e6, 150e6)), B=float(rng.uniform(200e6, 400e6)),
+                                n=float(rng.uniform(0.2, 0.5))) for _ in range(count)]
+
+
+@pytest.mark.parametrize("kind", ["hex", "axi"])
+def test_batch_sensitivities_match_single_meshes(gpu_lib, kind):
+    """dnl_batch_sens_run over several instances = dnl_sens_run of each instance alone, bit for
+    bit (hex necking bars with three parameter sets; uneven axisymmetric bars)."""
+    if kind == "hex":
+        models = _small_necking(3)
+        d0 = gpu_lib.GpuDomain(models[0])
+        d0.prologue()  # the Pulse estimate of the stable step
+        dt0 = d0.time_step()
+        dts = np.full(60, 0.5 * dt0)
+    else:
+        models = [meshes.taylor_axi(4, 30), meshes.taylor_axi(6, 40, speed=260.0, A=120e6, n=0.45),
+                  meshes.taylor_axi(5, 20, speed=150.0, B=380e6)]
+        dts, _, _ = schedule(models[0], 60)
+        dts = 0.8 * dts
+    b = gpu_lib.BatchDomain(models)
+    out = b.sensitivities(dts)
+    for i, m in enumerate(models):
+        x, dx = gpu_lib.GpuDomain(m).sensitivities(dts)
+        assert np.array_equal(out[i][0], x), i
+        assert np.array_equal(out[i][1], dx), i
+        if kind == "hex":
+            assert np.linalg.norm(dx[0]) > 0  # the pulled bar yields: dA is not zero
+    b.reset()
+    again = b.sensitivities(dts)
+    for i in range(len(models)):
+        assert np.array_equal(again[i][0], out[i][0]) and np.array_equal(again[i][1], out[i][1])
+
+
+def test_hex_batch_refuses_plain_stepping(gpu_lib):
+    b = gpu_lib.BatchDomain(_small_necking(2))
+    with pytest.raises(gpu_lib.DnlError):
+        b.step(1)
