@@ -43,27 +43,29 @@ template <int ET> struct IpLayout {
 };
 
 // Per-integration-point record of the element pass that the tangent pass (forward-mode
-// sensitivities) reads back, component-major [slot][E*NIP].
+// sensitivities) reads back, component-major [slot][E*NIP].  Symmetric 3x3 matrices are stored
+// as xx yy zz xy xz yz.  Besides the primal quantities it holds the direction-independent
+// factors of the tangent, formed once per point instead of once per parameter: the divided
+// differences of ln(l)/2 and l^-1/2 over the eigenvalues of C, U^-1, and G_u = sum_k du_k dN/dxi_k.
 template <int ET> struct TapeLayout {
   static constexpr int DIM = Elem<ET>::DIM, NS = Elem<ET>::NS;
   static constexpr int JI = 0;              // J^-1 [l][c], DIM x DIM
   static constexpr int DETJ = JI + DIM * DIM;
   static constexpr int RAD = DETJ + 1;      // axisymmetric radius of the Gauss point
-  static constexpr int F = RAD + 1;         // F [r][c], 3 x 3
-  static constexpr int V = F + 9;           // eigenvectors of C = F^T F (columns), 3 x 3
-  static constexpr int LAM = V + 9;         // eigenvalues of C
-  static constexpr int LG = LAM + 3;        // ln(l) / 2
-  static constexpr int IL = LG + 3;         // l^-1/2
-  static constexpr int R = IL + 3;          // rotation, 3 x 3
+  static constexpr int VRR = RAD + 1;       // axisymmetric (sum N_k du_k,r) / radius
+  static constexpr int F = VRR + 1;         // F [r][c], 3 x 3
+  static constexpr int GU = F + 9;          // G_u [r][l] = sum_k du_k[r] dN_k/dxi_l, DIM x DIM
+  static constexpr int V = GU + DIM * DIM;  // eigenvectors of C = F^T F (columns), 3 x 3
+  static constexpr int GD = V + 9;          // divided differences of ln(l)/2, symmetric
+  static constexpr int HD = GD + 6;         // divided differences of l^-1/2, symmetric
+  static constexpr int UI = HD + 6;         // U^-1 = C^-1/2, symmetric
+  static constexpr int R = UI + 6;          // rotation, 3 x 3
   static constexpr int STR = R + 9;         // trial deviator (symmetric components)
   static constexpr int NORMS = STR + NS;    // its norm
   static constexpr int GAM = NORMS + 1;     // plastic multiplier (0: elastic step)
   static constexpr int XV = GAM + 1;        // evp + sqrt(2/3) gamma
   static constexpr int XN = XV + 1;         // XV^n
-  static constexpr int SPRE = XN + 1;       // S, Eps, EpsPlas before the RFI rotation
-  static constexpr int EPRE = SPRE + NS;
-  static constexpr int PPRE = EPRE + NS;
-  static constexpr int NT = PPRE + NS;
+  static constexpr int NT = XN + 1;
 };
 
 // Tangent integration-point state per parameter direction: [dir][comp][E*NIP]

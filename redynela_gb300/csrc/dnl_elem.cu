@@ -296,6 +296,11 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
   // ---- F = I + sum_k dN_k (x) du_k (Current field), diagonal accumulated onto 1 in node order
   double F[3][3] = {{1., 0., 0.}, {0., 1., 0.}, {0., 0., 1.}};
   double vR = 0.;
+  double GU[DIM][DIM];  // tape only: sum_k du_k (x) dN/dxi_k
+#pragma unroll
+  for (int r = 0; r < DIM; r++)
+#pragma unroll
+    for (int l = 0; l < DIM; l++) GU[r][l] = 0.;
 #pragma unroll
   for (int k = 0; k < NEN; k++) {
     double dNk[DIM];
@@ -318,12 +323,23 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         else
           F[r][c] = fma(dNk[c], uk[r], F[r][c]);
       }
+    if (TAPE) {
+#pragma unroll
+      for (int r = 0; r < DIM; r++)
+#pragma unroll
+        for (int l = 0; l < DIM; l++) GU[r][l] = fma(uk[r], SH::dN(pt, k, l), GU[r][l]);
+    }
     if (AXI) vR = RADD(vR, RMUL(SH::N(pt, k), uk[0]));
   }
   if (AXI) F[2][2] = RADD(F[2][2], vR / Rad);
   if (TAPE) {
 #pragma unroll
     for (int k = 0; k < 9; k++) tape(TL::F + k, F[k / 3][k % 3]);
+#pragma unroll
+    for (int r = 0; r < DIM; r++)
+#pragma unroll
+      for (int l = 0; l < DIM; l++) tape(TL::GU + r * DIM + l, GU[r][l]);
+    tape(TL::VRR, AXI ? vR / Rad : 0.);
   }
 
   // ---- C = F^T F (Tensor2::Transpose then operator*), exact reference rounding
@@ -384,13 +400,27 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
       il[cc] = rsqrt(f[cc][cc]);
     }
     if (TAPE) {
+      // eigenvectors and the divided differences of ln(l)/2 and l^-1/2 (Daleckii-Krein factors)
 #pragma unroll
       for (int k = 0; k < 9; k++) tape(TL::V + k, rot[k / 3][k % 3]);
+      const int P0[6] = {0, 1, 2, 0, 0, 1}, P1[6] = {0, 1, 2, 1, 2, 2};
 #pragma unroll
-      for (int cc = 0; cc < 3; cc++) {
-        tape(TL::LAM + cc, f[cc][cc]);
-        tape(TL::LG + cc, lg[cc]);
-        tape(TL::IL + cc, il[cc]);
+      for (int k = 0; k < 6; k++) {
+        const int i = P0[k], j = P1[k];
+        double g, hh;
+        if (i == j) {
+          g = 0.5 * il[i] * il[i];        // 1 / (2 l)
+          hh = -0.5 * il[i] * il[i] * il[i];  // -l^-3/2 / 2
+        } else {
+          const double li = f[i][i], lj = f[j][j];
+          const double mean = 0.5 * (li + lj), q = (li - lj) / mean;
+          // 2 atanh(q/2) / (2 q mean) for near-equal eigenvalues (series to q^4)
+          g = fabs(q) < 1e-3 ? 0.5 * fma(q * q, fma(q * q, 1. / 80., 1. / 12.), 1.) / mean
+                             : (lg[i] - lg[j]) / (li - lj);
+          hh = -il[i] * il[j] / fma(li, il[i], lj * il[j]);
+        }
+        tape(TL::GD + k, g);
+        tape(TL::HD + k, hh);
       }
     }
 #pragma unroll
@@ -414,6 +444,11 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         dE[i][j] = dE[j][i] = su;
         Rr[i][j] = Rr[j][i] = sr;
       }
+    if (TAPE) {
+      const int P0[6] = {0, 1, 2, 0, 0, 1}, P1[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+      for (int k = 0; k < 6; k++) tape(TL::UI + k, Rr[P0[k]][P1[k]]);
+    }
   }
   double R[3][3];
 #pragma unroll
@@ -546,16 +581,6 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     pressure *= 1.0 / NIP;  // exact: NIP is a power of two
   }
   const double p = fma(m.K, pressure, a.ip[L::P * nIP + ipx]);
-
-  if (TAPE) {
-    const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
-#pragma unroll
-    for (int k = 0; k < NS; k++) {
-      tape(TL::SPRE + k, S[I0[k]][I1[k]]);
-      tape(TL::EPRE + k, Ep[I0[k]][I1[k]]);
-      tape(TL::PPRE + k, Epl[I0[k]][I1[k]]);
-    }
-  }
 
   // ---- RFI: X <- R X R^T for S, Eps, EpsPlas (Element.C:386-388)
   auto rfi = [&](double X[3][3]) {

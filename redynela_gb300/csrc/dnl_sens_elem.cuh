@@ -7,12 +7,16 @@
 //   J, J^-1, det J      from the coordinate tangents          (Element2D.C:53-126, Element3D.C:53-113)
 //   F = I + grad du     with the Current delta_disp tangents  (ElementAx.C:114-136, Element3D.C:182-205)
 //   ln U, U^-1, R       spectral derivative at the computed eigenpairs of C = F^T F (Daleckii-Krein:
-//                       d f(C) = V (F o (V^T dC V)) V^T, F_ij divided differences of f)
-//                                                           (Tensor2.C:1154-1259)
+//                       d f(C) = V (F o (V^T dC V)) V^T, F_ij divided differences of f, recorded
+//                       by the primal pass)                 (Tensor2.C:1154-1259)
 //   trial stress, J2 return: implicit-function derivative of the converged return equation
 //                       sqrt(6) G gamma - Strial + sigma_y(evp + sqrt(2/3) gamma; A, B, n) = 0
 //                                                           (Element.C:245-345, IsoHardElastoplastic.C:171-184)
-//   pressure, RFI rotation, B^T sigma                       (Element.C:164-214, 351-401)
+//   pressure, RFI rotation (d(R X R^T) = R dX R^T + Omega X' + (Omega X')^T, Omega = dR R^T,
+//   X' the rotated state the primal pass stored), B^T sigma  (Element.C:164-214, 351-401)
+// Work that does not depend on the parameter (the divided differences, U^-1, G_u) is formed once
+// per point by the primal pass; in the axisymmetric case the 2 + 1 block structure of F, C, V, R
+// skips the identically zero entries.
 // Threading: NIP adjacent lanes per (element, direction) group, the four directions of an element
 // in consecutive groups, so the pressure average and the force sum stay warp-local as in k_elem.
 
@@ -33,7 +37,9 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
   const double *tx = a.tx + (long)dir * 3 * N, *tdu = a.tdu + (long)dir * 3 * N;
   double *tip = a.tip + (long)dir * TN::NCOMP * nIP;
   const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
-  auto sym = [&](double X[3][3], auto get) {
+  // (i, j) entries that are identically zero in the axisymmetric block structure (2 + 1)
+  auto zero = [](int i, int j) { return AXI && ((i == 2) != (j == 2)); };
+  auto symload = [&](double X[3][3], auto get) {
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -46,29 +52,40 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
 #pragma unroll
   for (int k = 0; k < NEN; k++) node[k] = __ldg(a.conn + (long)k * a.E + e);
 
-  // ---- J^-1, det J and their tangents
+  // ---- dJ, dRad from the coordinate tangents; the tangent of G_u from the Current du tangents
+  double dJ[DIM][DIM], GT[DIM][DIM], dRad = 0., dvR = 0.;
+#pragma unroll
+  for (int r = 0; r < DIM; r++)
+#pragma unroll
+    for (int c = 0; c < DIM; c++) dJ[r][c] = GT[r][c] = 0.;
+#pragma unroll
+  for (int k = 0; k < NEN; k++) {
+    double t[DIM], tu[DIM];
+#pragma unroll
+    for (int r = 0; r < DIM; r++) {
+      t[r] = tx[(long)r * N + node[k]];
+      tu[r] = tdu[(long)r * N + node[k]];
+    }
+#pragma unroll
+    for (int r = 0; r < DIM; r++)
+#pragma unroll
+      for (int c = 0; c < DIM; c++) {
+        const double d = SH::dN(pt, k, c);
+        dJ[r][c] = fma(d, t[r], dJ[r][c]);
+        GT[r][c] = fma(d, tu[r], GT[r][c]);
+      }
+    if (AXI) {
+      dRad = fma(SH::N(pt, k), t[0], dRad);
+      dvR = fma(SH::N(pt, k), tu[0], dvR);
+    }
+  }
+  // ---- dJ^-1 = -J^-1 dJ J^-1, d det J = det J tr(J^-1 dJ)
   double Ji[DIM][DIM];
 #pragma unroll
   for (int l = 0; l < DIM; l++)
 #pragma unroll
     for (int c = 0; c < DIM; c++) Ji[l][c] = tp(TL::JI + l * DIM + c);
   const double detJ = tp(TL::DETJ), Rad = tp(TL::RAD);
-  double dJ[DIM][DIM], dRad = 0.;
-#pragma unroll
-  for (int r = 0; r < DIM; r++)
-#pragma unroll
-    for (int c = 0; c < DIM; c++) dJ[r][c] = 0.;
-#pragma unroll
-  for (int k = 0; k < NEN; k++) {
-    double t[DIM];
-#pragma unroll
-    for (int r = 0; r < DIM; r++) t[r] = tx[(long)r * N + node[k]];
-#pragma unroll
-    for (int r = 0; r < DIM; r++)
-#pragma unroll
-      for (int c = 0; c < DIM; c++) dJ[r][c] = fma(SH::dN(pt, k, c), t[r], dJ[r][c]);
-    if (AXI) dRad = fma(SH::N(pt, k), t[0], dRad);
-  }
   double JdJ[DIM][DIM], dJi[DIM][DIM];
 #pragma unroll
   for (int l = 0; l < DIM; l++)
@@ -93,139 +110,145 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
   }
   const double ddetJ = detJ * trJ;
 
-  // ---- F (recorded) and dF
+  // ---- dF = d(G_u J^-1) = G_t J^-1 + G_u dJ^-1  (F - I = G_u J^-1); axisymmetric hoop term
   double F[3][3], dF[3][3];
 #pragma unroll
   for (int k = 0; k < 9; k++) {
     F[k / 3][k % 3] = tp(TL::F + k);
     dF[k / 3][k % 3] = 0.;
   }
-  double vR = 0., dvR = 0.;
-#pragma unroll
-  for (int k = 0; k < NEN; k++) {
-    double dNk[DIM], ddNk[DIM], u[DIM], tu[DIM];
-#pragma unroll
-    for (int c = 0; c < DIM; c++) {
-      double s = 0., ds = 0.;
-#pragma unroll
-      for (int l = 0; l < DIM; l++) {
-        s = fma(Ji[l][c], SH::dN(pt, k, l), s);
-        ds = fma(dJi[l][c], SH::dN(pt, k, l), ds);
-      }
-      dNk[c] = s;
-      ddNk[c] = ds;
-    }
-#pragma unroll
-    for (int r = 0; r < DIM; r++) {
-      u[r] = a.du[r][node[k]];
-      tu[r] = tdu[(long)r * N + node[k]];
-    }
+  {
+    double GU[DIM][DIM];
 #pragma unroll
     for (int r = 0; r < DIM; r++)
 #pragma unroll
-      for (int c = 0; c < DIM; c++) dF[r][c] = fma(ddNk[c], u[r], fma(dNk[c], tu[r], dF[r][c]));
-    if (AXI) {
-      vR = fma(SH::N(pt, k), u[0], vR);
-      dvR = fma(SH::N(pt, k), tu[0], dvR);
-    }
+      for (int l = 0; l < DIM; l++) GU[r][l] = tp(TL::GU + r * DIM + l);
+#pragma unroll
+    for (int r = 0; r < DIM; r++)
+#pragma unroll
+      for (int c = 0; c < DIM; c++) {
+        double s = 0.;
+#pragma unroll
+        for (int l = 0; l < DIM; l++) s = fma(GT[r][l], Ji[l][c], fma(GU[r][l], dJi[l][c], s));
+        dF[r][c] = s;
+      }
   }
-  if (AXI) dF[2][2] = fma(-(vR / Rad), dRad, dvR) / Rad;
+  if (AXI) dF[2][2] = fma(-tp(TL::VRR), dRad, dvR) / Rad;
 
-  // ---- dC, and the spectral derivatives of ln U = ln(C)/2 and U^-1 = C^-1/2
+  // ---- dC = dF^T F + F^T dF (symmetric)
   double dC[3][3];
 #pragma unroll
-  for (int i = 0; i < 3; i++)
+  for (int q = 0; q < 6; q++) {
+    const int i = I0[q], j = I1[q];
+    double s = 0.;
+    if (!zero(i, j)) {
 #pragma unroll
-    for (int j = 0; j < 3; j++) {
-      double s = 0.;
-#pragma unroll
-      for (int k = 0; k < 3; k++) s = fma(dF[k][i], F[k][j], fma(F[k][i], dF[k][j], s));
-      dC[i][j] = s;
+      for (int k = 0; k < 3; k++)
+        if (!zero(k, i) && !zero(k, j)) s = fma(dF[k][i], F[k][j], fma(F[k][i], dF[k][j], s));
     }
-  double V[3][3], lam[3], lg[3], il[3];
+    dC[i][j] = dC[j][i] = s;
+  }
+  // ---- spectral derivative: Ah = V^T dC V; d ln U = V (G o Ah) V^T; d U^-1 = V (H o Ah) V^T
+  double V[3][3];
 #pragma unroll
   for (int k = 0; k < 9; k++) V[k / 3][k % 3] = tp(TL::V + k);
-#pragma unroll
-  for (int c = 0; c < 3; c++) {
-    lam[c] = tp(TL::LAM + c);
-    lg[c] = tp(TL::LG + c);
-    il[c] = tp(TL::IL + c);
-  }
-  double Ah[3][3];  // V^T dC V
+  double Bg[3][3], Bh[3][3];
   {
     double T1[3][3];
 #pragma unroll
-    for (int i = 0; i < 3; i++)
+    for (int k = 0; k < 3; k++)
 #pragma unroll
       for (int j = 0; j < 3; j++) {
         double s = 0.;
 #pragma unroll
-        for (int k = 0; k < 3; k++) s = fma(dC[i][k], V[k][j], s);
-        T1[i][j] = s;
+        for (int l = 0; l < 3; l++)
+          if (!zero(k, l) && !zero(l, j)) s = fma(dC[k][l], V[l][j], s);
+        T1[k][j] = s;
+      }
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+      const int i = I0[q], j = I1[q];
+      double s = 0.;
+      if (!zero(i, j)) {
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+          if (!zero(k, i) && !zero(k, j)) s = fma(V[k][i], T1[k][j], s);
+      }
+      Bg[i][j] = Bg[j][i] = tp(TL::GD + q) * s;
+      Bh[i][j] = Bh[j][i] = tp(TL::HD + q) * s;
+    }
+  }
+  double dLn[3][3], dUi[3][3];
+  {
+    double Tg[3][3], Th[3][3];  // V B
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int l = 0; l < 3; l++) {
+        double sg = 0., sh = 0.;
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+          if (!zero(i, k) && !zero(k, l)) {
+            sg = fma(V[i][k], Bg[k][l], sg);
+            sh = fma(V[i][k], Bh[k][l], sh);
+          }
+        Tg[i][l] = sg;
+        Th[i][l] = sh;
+      }
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+      const int i = I0[q], j = I1[q];
+      double sg = 0., sh = 0.;
+      if (!zero(i, j)) {
+#pragma unroll
+        for (int l = 0; l < 3; l++)
+          if (!zero(i, l) && !zero(j, l)) {
+            sg = fma(Tg[i][l], V[j][l], sg);
+            sh = fma(Th[i][l], V[j][l], sh);
+          }
+      }
+      dLn[i][j] = dLn[j][i] = sg;
+      dUi[i][j] = dUi[j][i] = sh;
+    }
+  }
+  // ---- dR = dF U^-1 + F dU^-1, and Omega = dR R^T
+  double R[3][3], Om[3][3];
+  {
+    double Ui[3][3], dR[3][3];
+#pragma unroll
+    for (int q = 0; q < 6; q++) Ui[I0[q]][I1[q]] = Ui[I1[q]][I0[q]] = tp(TL::UI + q);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        R[i][j] = tp(TL::R + i * 3 + j);
+        double s = 0.;
+        if (!zero(i, j)) {
+#pragma unroll
+          for (int k = 0; k < 3; k++)
+            if (!zero(i, k) && !zero(k, j)) s = fma(dF[i][k], Ui[k][j], fma(F[i][k], dUi[k][j], s));
+        }
+        dR[i][j] = s;
       }
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int j = 0; j < 3; j++) {
         double s = 0.;
+        if (!zero(i, j)) {
 #pragma unroll
-        for (int k = 0; k < 3; k++) s = fma(V[k][i], T1[k][j], s);
-        Ah[i][j] = s;
+          for (int k = 0; k < 3; k++)
+            if (!zero(i, k) && !zero(j, k)) s = fma(dR[i][k], R[j][k], s);
+        }
+        Om[i][j] = s;
       }
   }
-  double Bg[3][3], Bh[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      const double li = lam[i], lj = lam[j];
-      const double mean = 0.5 * (li + lj), q = (li - lj) / mean;
-      // (ln li - ln lj) / (2 (li - lj)); near-equal pair: 2 atanh(q/2) / (2 q mean) series
-      const double g = fabs(q) < 1e-3 ? 0.5 * fma(q * q, fma(q * q, 1. / 80., 1. / 12.), 1.) / mean
-                                       : (lg[i] - lg[j]) / (li - lj);
-      const double hh = -il[i] * il[j] / fma(li, il[i], lj * il[j]);
-      Bg[i][j] = g * Ah[i][j];
-      Bh[i][j] = hh * Ah[i][j];
-    }
-  double dLn[3][3], dUi[3][3], Ui[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      double sg = 0., sh = 0., su = 0.;
-#pragma unroll
-      for (int k = 0; k < 3; k++) {
-        double tg = 0., th = 0.;
-#pragma unroll
-        for (int l = 0; l < 3; l++) {
-          tg = fma(Bg[k][l], V[j][l], tg);
-          th = fma(Bh[k][l], V[j][l], th);
-        }
-        sg = fma(V[i][k], tg, sg);
-        sh = fma(V[i][k], th, sh);
-        su = fma(V[i][k] * il[k], V[j][k], su);
-      }
-      dLn[i][j] = sg;
-      dUi[i][j] = sh;
-      Ui[i][j] = su;
-    }
-  double R[3][3], dR[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      R[i][j] = tp(TL::R + i * 3 + j);
-      double s = 0.;
-#pragma unroll
-      for (int k = 0; k < 3; k++) s = fma(dF[i][k], Ui[k][j], fma(F[i][k], dUi[k][j], s));
-      dR[i][j] = s;
-    }
 
   // ---- strain, trial stress
   double dS[3][3], dE[3][3], dP[3][3];
-  sym(dS, [&](int k) { return tip[(TN::S + k) * nIP + ipx]; });
-  sym(dE, [&](int k) { return tip[(TN::EPS + k) * nIP + ipx]; });
-  sym(dP, [&](int k) { return tip[(TN::EPSP + k) * nIP + ipx]; });
+  symload(dS, [&](int k) { return tip[(TN::S + k) * nIP + ipx]; });
+  symload(dE, [&](int k) { return tip[(TN::EPS + k) * nIP + ipx]; });
+  symload(dP, [&](int k) { return tip[(TN::EPSP + k) * nIP + ipx]; });
   const double dp0 = tip[TN::P * nIP + ipx], devp0 = tip[TN::EVP * nIP + ipx];
   const double dtr = dLn[0][0] + dLn[1][1] + dLn[2][2];
 #pragma unroll
@@ -242,7 +265,7 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
   if (gam > 0.) {
     const double normS = tp(TL::NORMS), xv = tp(TL::XV), xn = tp(TL::XN);
     double nh[3][3];
-    sym(nh, [&](int k) { return tp(TL::STR + k) / normS; });
+    symload(nh, [&](int k) { return tp(TL::STR + k) / normS; });
     double dnorm = 0.;
 #pragma unroll
     for (int i = 0; i < 3; i++)
@@ -274,46 +297,43 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
   }
   const double dpn = fma(m.K, dpres, dp0);
 
-  // ---- RFI: d(R X R^T) = R dX R^T + T + T^T, T = dR X R^T
-  auto rfi_t = [&](int slot, double dX[3][3]) {
-    double X[3][3];
-    sym(X, [&](int k) { return tp(slot + k); });
-    double XRt[3][3], dXRt[3][3];
+  // ---- RFI: X' = R X R^T, d X' = R dX R^T + Omega X' + (Omega X')^T (R^T R = I), with X' the
+  // rotated state the primal pass stored
+  auto rfi_t = [&](int comp, double dX[3][3]) {
+    double Xp[3][3];
+    symload(Xp, [&](int k) { return a.ip[(comp + k) * nIP + ipx]; });
+    double Tm[3][3], dXRt[3][3];
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int j = 0; j < 3; j++) {
         double s = 0., t = 0.;
+        if (!zero(i, j)) {
 #pragma unroll
-        for (int k = 0; k < 3; k++) {
-          s = fma(X[i][k], R[j][k], s);
-          t = fma(dX[i][k], R[j][k], t);
-        }
-        XRt[i][j] = s;
-        dXRt[i][j] = t;
-      }
-    double Tm[3][3], Y[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3; j++) {
-        double s = 0., t = 0.;
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-          s = fma(dR[i][k], XRt[k][j], s);
-          t = fma(R[i][k], dXRt[k][j], t);
+          for (int k = 0; k < 3; k++) {
+            if (!zero(i, k) && !zero(k, j)) s = fma(Om[i][k], Xp[k][j], s);
+            if (!zero(i, k) && !zero(j, k)) t = fma(dX[i][k], R[j][k], t);
+          }
         }
         Tm[i][j] = s;
-        Y[i][j] = t;
+        dXRt[i][j] = t;
       }
 #pragma unroll
-    for (int i = 0; i < 3; i++)
+    for (int q = 0; q < 6; q++) {
+      const int i = I0[q], j = I1[q];
+      double y = 0.;
+      if (!zero(i, j)) {
 #pragma unroll
-      for (int j = 0; j < 3; j++) dX[i][j] = Y[i][j] + Tm[i][j] + Tm[j][i];
+        for (int k = 0; k < 3; k++)
+          if (!zero(i, k) && !zero(k, j)) y = fma(R[i][k], dXRt[k][j], y);
+      }
+      const double v = y + Tm[i][j] + Tm[j][i];
+      dX[i][j] = dX[j][i] = v;
+    }
   };
-  rfi_t(TL::SPRE, dS);
-  rfi_t(TL::EPRE, dE);
-  rfi_t(TL::PPRE, dP);
+  rfi_t(L::S, dS);
+  rfi_t(L::EPS, dE);
+  rfi_t(L::EPSP, dP);
   if (valid) {
 #pragma unroll
     for (int k = 0; k < NS; k++) {
@@ -327,7 +347,7 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
 
   // ---- forces: Fe_k = - sum_pt dN_k . Sig W (+ hoop term)
   double sig[3][3];
-  sym(sig, [&](int k) { return a.ip[(L::S + k) * nIP + ipx]; });
+  symload(sig, [&](int k) { return a.ip[(L::S + k) * nIP + ipx]; });
   const double pf = a.ip[L::P * nIP + ipx];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
