@@ -473,11 +473,11 @@ def main_sens(args):
         cpu = {"value": 1.0 / (tc * nst / k), "unit": "gradients/s", "cores": threads, "kind": "port",
                "sample": f"the sensitivity oracle (FP64 dual numbers, OpenMP) over the first {k} of "
                          f"the {nst} steps, {tc:.1f} s, scaled to the full schedule"}
-    # tangent element pass: compulsory bytes per launch (tape and state read, tangent state
-    # read + written, element forces written) over its mean launch time
-    nip, ns = 4, 4
-    nt = 4 + 3 + 9 + 9 + 3 * 3 + 9 + ns + 4 + 3 * ns
-    tan_bytes = m.E * nip * 8 * (nt + (ns + 1) + 4 * 2 * (3 * ns + 2)) + m.E * 4 * 8 * 2 * 4
+    # tangent element pass: compulsory bytes per launch -- the per-point record (64 doubles,
+    # axisymmetric) and the rotated state (3 tensors + p) read once, the four tangent states read
+    # and written, the element forces written -- over its mean launch time
+    nip, ns, nt = 4, 4, 64
+    tan_bytes = m.E * nip * 8 * (nt + 3 * ns + 1 + 4 * 2 * (3 * ns + 2)) + m.E * 4 * 2 * 8 * 4
     line = {"metric": "gradients/s", "value": value, "unit": "gradients/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -546,8 +546,8 @@ def main_necking(args):
     value = len(models) / (per_step * total_steps)
     tan_ms, tan_n = prof["tangent"]
     total_ms = sum(v[0] for v in prof.values())
-    nip, ns, nt = 8, 6, 9 + 3 + 9 + 9 + 3 * 3 + 9 + 6 + 4 + 3 * 6
-    tan_bytes = E * nip * 8 * (nt + (ns + 1) + 4 * 2 * (3 * ns + 2)) + E * 8 * 3 * 8 * 4
+    nip, ns, nt = 8, 6, 76  # the per-point record of a hex8 Gauss point: 76 doubles
+    tan_bytes = E * nip * 8 * (nt + 3 * ns + 1 + 4 * 2 * (3 * ns + 2)) + E * 8 * 3 * 8 * 4
     achieved = tan_bytes / (tan_ms / max(tan_n, 1) * 1e-3) / 1e9 if tan_n else None
     cpu = None
     agree = None

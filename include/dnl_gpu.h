@@ -219,6 +219,18 @@ int dnl_internal_forces_static(const dnl_static_args *args, void *stream, int *b
  * the Structure from the .dyn deck. */
 int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0);
 
+/* -------------------------------------------------------------- results / restart files */
+/* The reference's binary results file (Structure::writeData, Structure.C:936-952, through
+ * io_Data::structure_write, io_Data.C:486-506): version header, time, per node the coordinates
+ * and the Current NodalField, per integration point p, evp, S, Sig, Eps, dEps, EpsPlas.  Writing
+ * needs the last step's strain increments: a handle created with DNL_FLAG_STEP_TENSORS
+ * (DNL_ERR_ARG otherwise). */
+int dnl_write_results(dnl_handle *h, const char *path);
+/* Load such a file into the handle (same mesh) and continue from its time: coordinates, Current
+ * nodal fields and integration-point state are replaced, the lumped mass stays that of the initial
+ * mesh, and the time step is recomputed on the loaded state (Solver::computeTimeStep(True)). */
+int dnl_read_results(dnl_handle *h, const char *path);
+
 /* ------------------------------------------------------------------- sensitivities */
 /* Derivatives of a run's final nodal coordinates with respect to four parameters: the hardening
  * law's A, B, n (sigma_y = A + B evp^n, IsoHardElastoplastic.C:171-184) and the magnitude |v0| of

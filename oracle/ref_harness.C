@@ -370,7 +370,8 @@ static int cmdRun(const Model &m, const std::string &out)
 
 // The body of ExplicitSolverCH::solve (ExplicitSolverCH.C:115-278), same calls in the same order,
 // with per-step records.  The history .plot line of endStep is written by the reference itself.
-static int cmdSteps(const Model &m, const std::string &out, long K, bool record)
+static int cmdSteps(const Model &m, const std::string &out, long K, bool record,
+                    const char *resultsPath = nullptr)
 {
   Built b = build(m);
   Domain *d = b.dom;
@@ -441,6 +442,14 @@ static int cmdSteps(const Model &m, const std::string &out, long K, bool record)
     w.rec("kinetic", kin);
     dumpNodes(w, d, "final_");
     dumpIPs(w, d, "final_");
+  }
+  if (resultsPath)
+  {
+    // the reference's own binary results file (io_Data::structure_write, io_Data.C:486-506)
+    // Structure::solve sets the structure's time to the domain's before each save (Structure.C:852)
+    b.st->currentTime = d->currentTime;
+    std::ofstream pf(resultsPath);
+    b.st->writeData(pf);
   }
   w.scalar("steps", (double)k);
   w.scalar("wall_s", wall);
@@ -546,6 +555,8 @@ int main(int argc, char **argv)
   Model m = readModel(argv[2]);
   if (cmd == "run")
     return cmdRun(m, argv[3]);
+  if (cmd == "steps" && argc >= 6)
+    return cmdSteps(m, argv[3], atol(argv[4]), true, argv[5]);
   if (cmd == "steps" && argc >= 5)
     return cmdSteps(m, argv[3], atol(argv[4]), true);
   if (cmd == "bench" && argc >= 5)

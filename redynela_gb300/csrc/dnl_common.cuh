@@ -284,6 +284,7 @@ void sens_free(dnl_handle *h);
 int enqueue_bc_current(dnl_handle *h);
 int enqueue_node(dnl_handle *h);
 int read_time_state(dnl_handle *h, DevTime *t);
+int restart_time(dnl_handle *h, double t);
 int launch_mass(dnl_handle *h, cudaStream_t s, double *me);
 int launch_courant(dnl_handle *h, cudaStream_t s);
 int launch_pulse(dnl_handle *h, cudaStream_t s);

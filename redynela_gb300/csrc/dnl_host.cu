@@ -532,6 +532,25 @@ int launch_gather_mass(dnl_handle *h, const double *me)
   return check_launch();
 }
 
+__global__ void k_set_time(DevTime *tm, double t)
+{
+  tm->currentTime = t;
+  tm->tsDate = tm->lastTsDate = t;
+}
+
+// restart at time t from the state already loaded: Solver::computeTimeStep(True) on it
+int restart_time(dnl_handle *h, double t)
+{
+  k_set_time<<<1, 1, 0, h->stream>>>(h->tm, t);
+  launch_counter()++;
+  int r;
+  if ((r = launch_time_step_source(h))) return r;
+  if ((r = launch_dt(h, DT_FORCE))) return r;
+  DevTime tt;
+  if ((r = read_time(h, &tt))) return r;
+  return tt.status;
+}
+
 // the primal per-step launches, for the sensitivity run (dnl_sens.cu)
 int enqueue_bc_current(dnl_handle *h) { return (h->hasSpeedBC || h->nbcNodes) ? launch_bc_current(h) : 0; }
 int enqueue_node(dnl_handle *h) { return launch_node(h, true); }

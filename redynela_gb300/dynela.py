@@ -133,6 +133,8 @@ def lib():
         L.dnl_set_dt_schedule.argtypes = [H, _dp, C.c_int]
         L.dnl_adjoint.argtypes = [H, _dp, _dp, C.c_int]
         L.dnl_reset.argtypes = [H, C.POINTER(MaterialDesc), _dp]
+        L.dnl_write_results.argtypes = [H, C.c_char_p]
+        L.dnl_read_results.argtypes = [H, C.c_char_p]
         L.dnl_batch_sens_run.argtypes = [H, C.c_int, _dp, _dp, _dp]
         L.dnl_batch_reset.argtypes = [H]
         _lib = L
@@ -360,6 +362,14 @@ class GpuDomain:
         self._check(self.L.dnl_reset(self.h, C.byref(mat), _ptr(v0)))
         self.model = model
 
+    def write_results(self, path: str) -> None:
+        """dnl_write_results: the reference's binary results file (needs FLAG_STEP_TENSORS)."""
+        self._check(self.L.dnl_write_results(self.h, os.fsencode(path)))
+
+    def read_results(self, path: str) -> None:
+        """dnl_read_results: load a results file of this mesh and continue from its time."""
+        self._check_run(self.L.dnl_read_results(self.h, os.fsencode(path)))
+
     def sensitivities(self, dts):
         """dnl_sens_run: the run with step sizes ``dts`` from the initial state; returns the final
         coordinates (N, 3) and their derivatives (4, N, 3) with respect to SENS_PARAMS."""
@@ -379,6 +389,31 @@ class GpuDomain:
         grad = np.zeros(SENS_NPARAM)
         self._check_run(self.L.dnl_adjoint(self.h, _ptr(g), _ptr(grad), int(ckpt_stride)))
         return grad
+
+
+def parse_results(path: str, num_nodes: int, num_points: int) -> Dict[str, np.ndarray]:
+    """Decode a results file in the reference's binary format (see dnl_write_results): headers,
+    times, per node coords ro dro e de T v a fe du disp, per integration point p evp S Sig Eps dEps
+    EpsPlas (tensors (n, 3, 3)), separators."""
+    d = np.fromfile(path, dtype=np.float64)
+    expect = 6 + 1 + 6 + 1 + 23 * num_nodes + 3 + 47 * num_points + 3 + 3
+    if d.size != expect:
+        raise ValueError(f"{path}: {d.size} doubles, expected {expect}")
+    out = {"header": d[0:6].copy(), "structure_time": float(d[6]), "domain_header": d[7:13].copy(),
+           "time": float(d[13])}
+    nodes = d[14:14 + 23 * num_nodes].reshape(num_nodes, 23)
+    for name, a, b in (("coords", 0, 3), ("thermal", 3, 8), ("v", 8, 11), ("a", 11, 14),
+                       ("fe", 14, 17), ("du", 17, 20), ("disp", 20, 23)):
+        out[name] = nodes[:, a:b].copy()
+    o = 14 + 23 * num_nodes
+    out["separators"] = [d[o:o + 3].copy()]
+    ips = d[o + 3:o + 3 + 47 * num_points].reshape(num_points, 47)
+    out["p"], out["evp"] = ips[:, 0].copy(), ips[:, 1].copy()
+    for k, name in enumerate(("S", "Sig", "Eps", "dEps", "EpsPlas")):
+        out[name] = ips[:, 2 + 9 * k:11 + 9 * k].reshape(num_points, 3, 3).copy()
+    o += 3 + 47 * num_points
+    out["separators"] += [d[o:o + 3].copy(), d[o + 3:o + 6].copy()]
+    return out
 
 
 SENS_NPARAM = 4

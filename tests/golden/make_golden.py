@@ -11,6 +11,8 @@ reference's own output on a seeded synthetic model:
 * ``run_c0.npz``        the 5x50 Taylor bar to 80 us: final coordinates, plastic strain, pressure
 * ``steps_hex.npz``     a 6x6x8 hex bar with the Pulse time step, first 30 steps
 * ``run_hex.npz``       an 8x8x24 hex bar with the Pulse time step to 80 us: final coordinates
+* ``results_axi.bin``   the reference's binary results file (Structure::writeData) of the 3x4 axi bar
+                        after 13 steps, and ``results_axi.npz`` its state from the harness
 
     python tests/golden/make_golden.py
 """
@@ -36,9 +38,21 @@ def save(name, **arrays):
     print(f"{name}: {os.path.getsize(path)} bytes")
 
 
+def results():
+    """The results-file fixture only: python tests/golden/make_golden.py results"""
+    m = meshes.taylor_axi(3, 4)
+    path = os.path.join(HERE, "results_axi.bin")
+    r = dnl_io.run_reference("steps", m, 13, path)
+    print(f"results_axi.bin: {os.path.getsize(path)} bytes")
+    save("results_axi.npz", **{k: r[k] for k in r if k.startswith("final_")}, time=r["time"])
+
+
 def main():
     if not dnl_io.reference_available():
         sys.exit("compiled reference missing: run `make -C oracle ref`")
+    if sys.argv[1:] == ["results"]:
+        results()
+        return
     t = dnl_io.reference_tables()
     save("tables.npz", **t)
 
@@ -70,6 +84,8 @@ def main():
     r = dnl_io.run_reference("run", m)
     save("run_hex.npz", increments=r["increments"], time=r["time"], final_coords=r["final_coords"],
          final_evp=r["final_evp"])
+
+    results()
 
 
 if __name__ == "__main__":

@@ -89,7 +89,7 @@ def test_torch_autograd_function(gpu_lib):
     assert np.allclose(params.grad.numpy(), ref, rtol=1e-12, atol=0)
     # and central differences of the GPU run for the hardening parameters (h = 1e-6 relative)
     for p in range(3):
-        h = 1e-6 * float(params[p])
+        h = 1e-6 * float(params.detach()[p])
         vals = []
         for sgn in (1, -1):
             q = params.detach().clone()
