@@ -22,6 +22,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
 
 MODEL_MAGIC = 0x4D4C4E44  # "DNLM"
+EXT_MAGIC = 0x584C4E44  # "DNLX": optional block after the solver settings
 STATE_MAGIC = 0x54534E44  # "DNST"
 
 
@@ -39,6 +40,25 @@ def write_model(path: str, m) -> None:
             f.write(np.ascontiguousarray(g.nodes, dtype="<i8").tobytes())
         f.write(struct.pack("<6d", m.tend, m.rho_b, m.safety, float(m.freq), float(m.method),
                             float(m.nsaves)))
+        if getattr(m, "extended", False):
+            # materials / laws, element materials, per-node initial velocities
+            laws = m.material_laws()
+            f.write(struct.pack("<2q", EXT_MAGIC, len(laws)))
+            for ml in laws:
+                prm = list(ml.params) + [0.0] * (8 - len(ml.params))
+                tx = np.zeros(0) if ml.table_x is None else np.asarray(ml.table_x, dtype="<f8")
+                ty = np.zeros(0) if ml.table_y is None else np.asarray(ml.table_y, dtype="<f8")
+                f.write(struct.pack("<3dq8dq", ml.young, ml.poisson, ml.density, ml.law, *prm, tx.size))
+                f.write(tx.tobytes())
+                f.write(ty.tobytes())
+            em = m.elem_material
+            f.write(struct.pack("<q", 0 if em is None else 1))
+            if em is not None:
+                f.write(np.ascontiguousarray(em, dtype="<i8").tobytes())
+            iv = m.initial_velocity
+            f.write(struct.pack("<q", 0 if iv is None else 1))
+            if iv is not None:
+                f.write(np.ascontiguousarray(iv, dtype="<f8").tobytes())
 
 
 def write_state(path: str, coords, du, v, a, disp, S, Eps, EpsPlas, p, evp, dt) -> None:

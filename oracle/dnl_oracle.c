@@ -55,6 +55,14 @@ struct dnlo {
   double *p, *evp, *detJ, *detJ0;
   double *dN; /* (E, nip, nen, 3) */
   double young, nu, rho, A, B, n;
+  /* materials (Structure::attachMaterialToElements): per material E, nu, rho, hardening law and
+   * its parameters / table; material 0 is the one of dnlo_create */
+  int nmat;
+  double *mE, *mNu, *mRho, *mP; /* mP: nmat x 8 (POWER: A B n; METAFOR: P1..P8) */
+  int *mLaw;
+  long *mTab;                   /* nmat + 1 offsets into tabX / tabY */
+  double *tabX, *tabY;
+  int *elemMat;                 /* E material indices, or NULL: material 0 */
   double v0[3];
   long *bcn_start; /* per node: its constant BCs, in attachment order */
   int *bcn_kind;
@@ -408,16 +416,59 @@ static void elem_F(const dnlo *h, long e, int pt, double *F)
   }
 }
 
-/* IsoHardElastoplastic::getIsotropicYieldStress / Hardening (IsoHardElastoplastic.C:171-184) */
-static double yield_stress(const dnlo *h, double evp, double shift)
+#define MATOF(h, e) ((h)->elemMat ? (h)->elemMat[e] : 0)
+
+/* DiscreteFunction::getValue / getSlope (linearAlgebra/DiscreteFunction.C:169-201, 274-297):
+ * the segment ending at the first point with x >= a (the first segment below the table), the
+ * point's own value when x == a, and 0 beyond the last point. */
+static double tab_value(const double *x, const double *y, long n, double a)
 {
-  const double x = evp + DNL_SQRT23 * shift;
-  return (h->A + h->B * pow(x, h->n));
+  for (long i = 1; i < n; i++)
+    if (x[i] >= a) {
+      if (x[i] == a) return y[i];
+      return ((a - x[i - 1]) / (x[i] - x[i - 1])) * (y[i] - y[i - 1]) + y[i - 1];
+    }
+  return 0;
 }
-static double yield_hardening(const dnlo *h, double evp, double shift)
+static double tab_slope(const double *x, const double *y, long n, double a)
+{
+  for (long i = 1; i < n; i++)
+    if (x[i] >= a) return (y[i] - y[i - 1]) / (x[i] - x[i - 1]);
+  return 0;
+}
+
+/* getIsotropicYieldStress / getIsotropicYieldHardening of the material's hardening law at
+ * evp + sqrt(2/3) shift: IsoHardElastoplastic (IsoHardElastoplastic.C:171-184),
+ * IsoHardElastoplasticTabular (IsoHardElastoplasticTabular.C:103-116), IsoHardMetafor
+ * (IsoHardMetafor.C:132-153). */
+static double yield_stress(const dnlo *h, int mi, double evp, double shift)
 {
   const double x = evp + DNL_SQRT23 * shift;
-  return (h->n * h->B * pow(x, (h->n - 1.)));
+  const double *P = h->mP + 8 * mi;
+  switch (h->mLaw[mi]) {
+  case DNLO_HARD_TABULAR:
+    return tab_value(h->tabX + h->mTab[mi], h->tabY + h->mTab[mi], h->mTab[mi + 1] - h->mTab[mi], x);
+  case DNLO_HARD_METAFOR:
+    return (P[1] - P[0]) * (1 - exp(-P[2] * (x))) + P[3] * pow(x, P[4]) + P[0] * pow((1 + P[5] * x), P[6]) + P[7] * x;
+  default:
+    return (P[0] + P[1] * pow(x, P[2]));
+  }
+}
+static double yield_hardening(const dnlo *h, int mi, double evp, double shift)
+{
+  const double x = evp + DNL_SQRT23 * shift;
+  const double *P = h->mP + 8 * mi;
+  switch (h->mLaw[mi]) {
+  case DNLO_HARD_TABULAR:
+    return tab_slope(h->tabX + h->mTab[mi], h->tabY + h->mTab[mi], h->mTab[mi + 1] - h->mTab[mi], x);
+  case DNLO_HARD_METAFOR:
+    if (x > 0.)
+      return ((P[1] - P[0]) * P[2] * exp(-P[2] * (x)) + P[3] * P[4] * pow(x, (P[4] - 1.0)) +
+              P[0] * P[5] * P[6] * pow((1.0 + P[5] * x), (P[6] - 1.0)) + P[7]);
+    return ((P[1] - P[0]) * P[2] * exp(-P[2] * (x)) + P[0] * P[5] * P[6] * pow((1.0 + P[5] * x), (P[6] - 1.0)) + P[7]);
+  default:
+    return (P[2] * P[1] * pow(x, (P[2] - 1.)));
+  }
 }
 
 /* Element::computeStress (Element.C:217-403) followed by Element::computeInternalForces
@@ -425,8 +476,10 @@ static double yield_hardening(const dnlo *h, double evp, double shift)
 static int elem_forces(dnlo *h, long e, double *fe)
 {
   const int nip = h->nip, nen = h->nen, dim = h->dim;
-  const double K = h->young / (3. * (1. - 2. * h->nu));
-  const double G = h->young / (2. * (1. + h->nu)); /* Material::mu(), Material.h:167-172 */
+  const int mi = MATOF(h, e);
+  const double K = h->mE[mi] / (3. * (1. - 2. * h->mNu[mi]));
+  const double G = h->mE[mi] / (2. * (1. + h->mNu[mi])); /* Material::mu(), Material.h:167-172 */
+  const int yields = h->mLaw[mi] != DNLO_HARD_ELASTIC; /* Material::isYield (Material.C:366-371) */
   double pressure = 0.0;
   int err = 0;
   for (int pt = 0; pt < nip; pt++) {
@@ -450,20 +503,20 @@ static int elem_forces(dnlo *h, long e, double *fe)
       for (int k = 0; k < 9; k++) S[k] += g2 * dev[k];
     }
     double gamma = 0.0, h_ = 0.0;
-    {
-      const double Sigv0 = yield_stress(h, h->evp[ix], 0.0);
+    if (yields) {
+      const double Sigv0 = yield_stress(h, mi, h->evp[ix], 0.0);
       double ss = 0.;
       for (int k = 0; k < 9; k++) ss += S[k] * S[k];
       const double Strial = DNL_SQRT32 * sqrt(ss); /* Tensor2::J2, :505-510 */
       if (Strial > Sigv0) {
-        h_ = yield_hardening(h, h->evp[ix], 0.0);
+        h_ = yield_hardening(h, mi, h->evp[ix], 0.0);
         const double normS = sqrt(ss); /* Tensor2::norme, :484-489 */
         gamma = (normS - DNL_SQRT23 * Sigv0) / (2.0 * G * (1.0 + (h_) / (3.0 * G)));
         double dgamma = 0, Sigv, dfun, fun;
         int run = 1, iteration = 0;
         while (run) {
-          Sigv = yield_stress(h, h->evp[ix], gamma);
-          h_ = yield_hardening(h, h->evp[ix], gamma);
+          Sigv = yield_stress(h, mi, h->evp[ix], gamma);
+          h_ = yield_hardening(h, mi, h->evp[ix], gamma);
           dfun = DNL_SQRT32 * 2.0 * G + DNL_SQRT23 * h_;
           fun = dfun * gamma - (Strial - Sigv + h_ * DNL_SQRT23 * gamma);
           if (ABS(fun / Sigv) > DNL_RR_PRECISION) {
@@ -588,7 +641,7 @@ int dnlo_mass(dnlo *h)
         double R = elem_radius(h, e, pt);
         WxdJ *= 2. * DNL_PI * R;
       }
-      for (int i = 0; i < h->nen; i++) Me[i] += h->rho * (h->Nt[pt][i]) * WxdJ;
+      for (int i = 0; i < h->nen; i++) Me[i] += h->mRho[MATOF(h, e)] * (h->Nt[pt][i]) * WxdJ;
     }
     for (int i = 0; i < h->nen; i++) {
       long glob = h->conn[e * h->nen + i];
@@ -614,7 +667,7 @@ static double elem_courant(const dnlo *h, long e)
   double r = 0.;
   for (int i = 0; i < 4; i++) r += ro[cn[i]];
   r /= 4;
-  const double E = h->young, Nu = h->nu;
+  const double E = h->mE[MATOF(h, e)], Nu = h->mNu[MATOF(h, e)];
   const double Cs = sqrt((E * (1 - Nu)) / (r * (1 + Nu) * (1 - 2 * Nu)));
   return len / (Cs);
 }
@@ -636,7 +689,7 @@ double dnlo_courant(dnlo *h)
 static void elem_stiffness(const dnlo *h, long e, double *Ke)
 {
   const int nen = h->nen, dim = h->dim, nd = nen * dim;
-  const double Nu = h->nu, E = h->young;
+  const double Nu = h->mNu[MATOF(h, e)], E = h->mE[MATOF(h, e)];
   double C[6][6];
   memset(C, 0, sizeof C);
   if (h->etype == 0) {
@@ -982,6 +1035,14 @@ dnlo *dnlo_create(int etype, long N, long E, const double *coords, const long *c
   for (long i = 0; i < nI; i++) h->evp[i] = 1e-10; /* IntegrationPoint::flush, IntegrationPoint.C:117 */
   h->young = mat[0]; h->nu = mat[1]; h->rho = mat[2];
   h->A = mat[3]; h->B = mat[4]; h->n = mat[5];
+  h->nmat = 1;
+  h->mE = zalloc(1); h->mNu = zalloc(1); h->mRho = zalloc(1); h->mP = zalloc(8);
+  h->mLaw = (int *)calloc(1, sizeof(int));
+  h->mTab = (long *)calloc(2, sizeof(long));
+  h->tabX = zalloc(1); h->tabY = zalloc(1);
+  h->mE[0] = mat[0]; h->mNu[0] = mat[1]; h->mRho[0] = mat[2];
+  h->mP[0] = mat[3]; h->mP[1] = mat[4]; h->mP[2] = mat[5];
+  h->elemMat = NULL;
   for (int i = 0; i < 3; i++) h->v0[i] = v0[i];
   /* Domain::initSolve: Current->ro = density (Domain.C:1076-1091); initial speed on both fields
    * (BoundarySpeed::applyInitial_V0, Boundary.C:378-385) */
@@ -1057,7 +1118,61 @@ void dnlo_destroy(dnlo *h)
   free(h->bcn_start); free(h->bcn_kind); free(h->bcn_val);
   free(h->EV); free(h->kx); free(h->Ke);
   free(h->n2e_start); free(h->n2e);
+  free(h->mE); free(h->mNu); free(h->mRho); free(h->mP); free(h->mLaw); free(h->mTab);
+  free(h->tabX); free(h->tabY); free(h->elemMat);
   free(h);
+}
+
+/* Several materials (Structure::attachMaterialToElements per ElementSet): props is nmat x 12
+ * {E, nu, rho, law, P1..P8}; material m's table (tabular law) is tab_x/tab_y[tab_start[m] ..
+ * tab_start[m+1]); elem_mat gives each element's material (NULL: all material 0).  The nodal
+ * density on the Current field becomes that of the last element, in element order, that holds the
+ * node (Domain::initSolve, Domain.C:1073-1106).  Before the prologue. */
+int dnlo_set_materials(dnlo *h, int nmat, const double *props, const long *tab_start,
+                       const double *tab_x, const double *tab_y, const long *elem_mat)
+{
+  if (nmat < 1 || !props || h->mass_done) return DNLO_ERR_ARG;
+  if (elem_mat)
+    for (long e = 0; e < h->E; e++)
+      if (elem_mat[e] < 0 || elem_mat[e] >= nmat) return DNLO_ERR_ARG;
+  free(h->mE); free(h->mNu); free(h->mRho); free(h->mP); free(h->mLaw); free(h->mTab);
+  free(h->tabX); free(h->tabY); free(h->elemMat);
+  h->nmat = nmat;
+  h->mE = zalloc(nmat); h->mNu = zalloc(nmat); h->mRho = zalloc(nmat); h->mP = zalloc(8 * nmat);
+  h->mLaw = (int *)calloc(nmat, sizeof(int));
+  h->mTab = (long *)calloc(nmat + 1, sizeof(long));
+  for (int m = 0; m < nmat; m++) {
+    const double *q = props + 12 * m;
+    h->mE[m] = q[0]; h->mNu[m] = q[1]; h->mRho[m] = q[2];
+    h->mLaw[m] = (int)q[3];
+    for (int k = 0; k < 8; k++) h->mP[8 * m + k] = q[4 + k];
+    h->mTab[m + 1] = tab_start ? tab_start[m + 1] : 0;
+  }
+  const long nt = h->mTab[nmat];
+  h->tabX = zalloc(nt); h->tabY = zalloc(nt);
+  for (long i = 0; i < nt; i++) {
+    h->tabX[i] = tab_x[i];
+    h->tabY[i] = tab_y[i];
+  }
+  h->elemMat = NULL;
+  if (elem_mat) {
+    h->elemMat = (int *)malloc(sizeof(int) * h->E);
+    for (long e = 0; e < h->E; e++) h->elemMat[e] = (int)elem_mat[e];
+  }
+  h->young = h->mE[0]; h->nu = h->mNu[0]; h->rho = h->mRho[0];
+  h->A = h->mP[0]; h->B = h->mP[1]; h->n = h->mP[2];
+  for (long e = 0; e < h->E; e++)
+    for (int k = 0; k < h->nen; k++) h->ro[0][h->conn[e * h->nen + k]] = h->mRho[MATOF(h, e)];
+  return 0;
+}
+
+/* Initial velocities per node (BoundarySpeed::applyInitial_V0 on node sets, Boundary.C:378-385):
+ * v (N x 3) on both nodal fields. */
+int dnlo_set_velocity(dnlo *h, const double *v)
+{
+  for (long n = 0; n < h->N; n++)
+    for (int i = 0; i < 3; i++) h->fld[0][1][n * 3 + i] = h->fld[1][1][n * 3 + i] = v[n * 3 + i];
+  return 0;
 }
 
 double *dnlo_array(dnlo *h, const char *nm, long *count)

@@ -27,6 +27,10 @@ enum {
   DNLO_ERR_SINGULAR = 7      /* Matrix.C:1680-1690, exactly singular Jacobian */
 };
 
+/* hardening laws: IsoHardElastoplastic, none (Material::isYield false), IsoHardElastoplasticTabular,
+ * IsoHardMetafor */
+enum { DNLO_HARD_POWER = 0, DNLO_HARD_ELASTIC = 1, DNLO_HARD_TABULAR = 2, DNLO_HARD_METAFOR = 3 };
+
 /* solver[5] = {tend, rho_b, safety, freq, method (0 Courant, 1 Pulse)}
  * mat[6]    = {E, nu, rho, A, B, n}
  * BC groups: kind 0 = BoundaryRestrain (val = 0/1 mask), 1 = BoundarySpeed (val = velocity);
@@ -54,6 +58,10 @@ int dnlo_bad_element(dnlo *h);
 int dnlo_tables(int etype, double *N, double *dN);
 void dnlo_set_threads(int n);
 int dnlo_get_threads(void);
+/* several materials / hardening laws (props nmat x 12: E nu rho law P1..P8), initial velocities */
+int dnlo_set_materials(dnlo *h, int nmat, const double *props, const long *tab_start,
+                       const double *tab_x, const double *tab_y, const long *elem_mat);
+int dnlo_set_velocity(dnlo *h, const double *v);
 
 #ifdef __cplusplus
 }

@@ -55,6 +55,8 @@ def lib():
         L.dnlo_steps.argtypes = [C.c_void_p, C.c_long, lp]
         L.dnlo_set_threads.argtypes = [C.c_int]
         L.dnlo_tables.argtypes = [C.c_int, dp, dp]
+        L.dnlo_set_materials.argtypes = [C.c_void_p, C.c_int, dp, lp, dp, dp, lp]
+        L.dnlo_set_velocity.argtypes = [C.c_void_p, dp]
         _lib = L
     return _lib
 
@@ -113,6 +115,34 @@ class Oracle:
             raise ValueError("dnlo_create rejected the model")
         self.model = m
         self.L = L
+        if getattr(m, "extended", False):
+            self._apply_extensions(m)
+
+    def _apply_extensions(self, m):
+        laws = m.material_laws()
+        props = np.zeros((len(laws), 12))
+        starts = np.zeros(len(laws) + 1, dtype=np.int64)
+        xs, ys = [], []
+        for i, ml in enumerate(laws):
+            props[i, :4] = (ml.young, ml.poisson, ml.density, ml.law)
+            props[i, 4:4 + len(ml.params)] = ml.params
+            tx = np.zeros(0) if ml.table_x is None else np.asarray(ml.table_x, dtype=np.float64)
+            ty = np.zeros(0) if ml.table_y is None else np.asarray(ml.table_y, dtype=np.float64)
+            xs.append(tx)
+            ys.append(ty)
+            starts[i + 1] = starts[i] + tx.size
+        tx = np.concatenate(xs) if starts[-1] else np.zeros(1)
+        ty = np.concatenate(ys) if starts[-1] else np.zeros(1)
+        em = None if m.elem_material is None else np.ascontiguousarray(m.elem_material, dtype=np.int64)
+        self._keep_ext = (props, starts, tx, ty, em)
+        r = self.L.dnlo_set_materials(self.h, len(laws), _dp(props), _lp(starts), _dp(tx), _dp(ty),
+                                      _lp(em) if em is not None else None)
+        if r:
+            raise ValueError(f"dnlo_set_materials: {r}")
+        if m.initial_velocity is not None:
+            v = np.ascontiguousarray(m.initial_velocity, dtype=np.float64)
+            self._keep_v = v
+            self.L.dnlo_set_velocity(self.h, _dp(v))
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -58,6 +58,9 @@
 #include <ExplicitSolverCH.h>
 #include <IntegrationPoint.h>
 #include <io_Structure.h>
+#include <IsoHardElastoplasticTabular.h>
+#include <IsoHardMetafor.h>
+#include <DiscreteFunction.h>
 #undef private
 #undef protected
 
@@ -135,6 +138,14 @@ struct BCGroup
   std::vector<long> nodes;
 };
 
+struct MatLaw
+{
+  double E, nu, rho;
+  long law; // 0 IsoHardElastoplastic, 1 none (elastic), 2 IsoHardElastoplasticTabular, 3 IsoHardMetafor
+  double P[8];
+  std::vector<double> tx, ty;
+};
+
 struct Model
 {
   long etype; // 0 ElQua4nAx, 1 ElHex8n3D
@@ -145,7 +156,13 @@ struct Model
   double v0[3];               // initial speed of every node
   std::vector<BCGroup> bcs;
   double tend, rho_b, safety, freq, method, nsaves;
+  // optional: several materials, element materials, per-node initial velocity
+  std::vector<MatLaw> mats;
+  std::vector<long> elemMat;
+  std::vector<double> vel;
 };
+
+static const long EXT_MAGIC = 0x584c4e44; // "DNLX"
 
 static const long MODEL_MAGIC = 0x4d4c4e44; // "DNLM"
 
@@ -187,6 +204,37 @@ static Model readModel(const char *path)
   m.freq = r.f64();
   m.method = r.f64();
   m.nsaves = r.f64();
+  long magic;
+  if (fread(&magic, 8, 1, r.f) == 1 && magic == EXT_MAGIC)
+  {
+    long nmat = r.i64();
+    for (long i = 0; i < nmat; i++)
+    {
+      MatLaw ml;
+      ml.E = r.f64();
+      ml.nu = r.f64();
+      ml.rho = r.f64();
+      ml.law = r.i64();
+      r.f64s(ml.P, 8);
+      long np = r.i64();
+      ml.tx.resize(np);
+      ml.ty.resize(np);
+      r.f64s(ml.tx.data(), np);
+      r.f64s(ml.ty.data(), np);
+      m.mats.push_back(ml);
+    }
+    if (r.i64())
+    {
+      m.elemMat.resize(m.E);
+      for (long e = 0; e < m.E; e++)
+        m.elemMat[e] = r.i64();
+    }
+    if (r.i64())
+    {
+      m.vel.resize(3 * m.N);
+      r.f64s(m.vel.data(), 3 * m.N);
+    }
+  }
   return m;
 }
 
@@ -219,24 +267,89 @@ static Built build(const Model &m)
     els->add(e + 1);
   }
 
-  Material *mat = new Material;
-  IsoHardElastoplastic *hard = new IsoHardElastoplastic;
-  hard->setYieldStress(m.mat[3]);
-  hard->setHardParameter(m.mat[4]);
-  hard->setHardExponent(m.mat[5]);
-  st->addMaterial(mat);
-  mat->setYoung(m.mat[0]);
-  mat->setPoisson(m.mat[1]);
-  mat->setDensity(m.mat[2]);
-  mat->setHardening(hard);
-  st->attachMaterialToElements(mat, els);
+  if (m.mats.empty())
+  {
+    Material *mat = new Material;
+    IsoHardElastoplastic *hard = new IsoHardElastoplastic;
+    hard->setYieldStress(m.mat[3]);
+    hard->setHardParameter(m.mat[4]);
+    hard->setHardExponent(m.mat[5]);
+    st->addMaterial(mat);
+    mat->setYoung(m.mat[0]);
+    mat->setPoisson(m.mat[1]);
+    mat->setDensity(m.mat[2]);
+    mat->setHardening(hard);
+    st->attachMaterialToElements(mat, els);
+  }
+  else
+  {
+    // one Material per entry, its hardening as a deck builds it (Samples/Traction/Traction.dyn:
+    // DiscreteFunction + IsoHardElastoplasticTabular::setFunction; a material without hardening),
+    // attached to the ElementSet of its elements
+    for (size_t i = 0; i < m.mats.size(); i++)
+    {
+      const MatLaw &ml = m.mats[i];
+      Material *mat = new Material;
+      st->addMaterial(mat);
+      mat->setYoung(ml.E);
+      mat->setPoisson(ml.nu);
+      mat->setDensity(ml.rho);
+      if (ml.law == 0)
+      {
+        IsoHardElastoplastic *hard = new IsoHardElastoplastic;
+        hard->setYieldStress(ml.P[0]);
+        hard->setHardParameter(ml.P[1]);
+        hard->setHardExponent(ml.P[2]);
+        mat->setHardening(hard);
+      }
+      else if (ml.law == 2)
+      {
+        DiscreteFunction *fn = new DiscreteFunction;
+        for (size_t k = 0; k < ml.tx.size(); k++)
+          fn->add(ml.tx[k], ml.ty[k]);
+        IsoHardElastoplasticTabular *hard = new IsoHardElastoplasticTabular;
+        hard->setFunction(fn);
+        mat->setHardening(hard);
+      }
+      else if (ml.law == 3)
+      {
+        IsoHardMetafor *hard = new IsoHardMetafor;
+        for (int k = 0; k < 8; k++)
+          hard->getConstitutiveParameter(k) = ml.P[k];
+        mat->setHardening(hard);
+      }
+      ElementSet *es = new ElementSet;
+      for (long e = 0; e < m.E; e++)
+        if ((m.elemMat.empty() ? 0 : m.elemMat[e]) == (long)i)
+          es->add(e + 1);
+      st->attachMaterialToElements(mat, es);
+    }
+  }
 
-  NodeSet *all = new NodeSet;
-  for (long n = 0; n < m.N; n++)
-    all->add(n + 1);
-  BoundarySpeed *ini = new BoundarySpeed;
-  ini->set(m.v0[0], m.v0[1], m.v0[2]);
-  st->attachInitialBC(ini, all);
+  if (m.vel.empty())
+  {
+    NodeSet *all = new NodeSet;
+    for (long n = 0; n < m.N; n++)
+      all->add(n + 1);
+    BoundarySpeed *ini = new BoundarySpeed;
+    ini->set(m.v0[0], m.v0[1], m.v0[2]);
+    st->attachInitialBC(ini, all);
+  }
+  else
+  {
+    // one BoundarySpeed per node that moves (applyInitial_V0 on node sets)
+    for (long n = 0; n < m.N; n++)
+    {
+      const double *v = &m.vel[3 * n];
+      if (v[0] == 0. && v[1] == 0. && v[2] == 0.)
+        continue;
+      NodeSet *one = new NodeSet;
+      one->add(n + 1);
+      BoundarySpeed *ini = new BoundarySpeed;
+      ini->set(v[0], v[1], v[2]);
+      st->attachInitialBC(ini, one);
+    }
+  }
 
   for (size_t g = 0; g < m.bcs.size(); g++)
   {

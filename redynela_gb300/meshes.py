@@ -23,7 +23,7 @@ from __future__ import annotations
 
 import dataclasses
 from dataclasses import dataclass, field
-from typing import List, Sequence
+from typing import List, Optional, Sequence
 
 import numpy as np
 
@@ -35,6 +35,12 @@ PULSE = 1
 
 RESTRAIN = 0
 SPEED = 1
+# hardening laws: IsoHardElastoplastic (A + B evp^n), no hardening attached (elastic: never
+# yields), IsoHardElastoplasticTabular (DiscreteFunction of evp), IsoHardMetafor (P1..P8)
+HARD_POWER = 0
+HARD_ELASTIC = 1
+HARD_TABULAR = 2
+HARD_METAFOR = 3
 
 
 @dataclass
@@ -49,6 +55,22 @@ class BCGroup:
     kind: int
     val: Sequence[float]
     nodes: np.ndarray
+
+
+@dataclass
+class MaterialLaw:
+    """One Material with its isotropic hardening (Material.h:61-156 + an IsotropicHardening).
+
+    params: POWER (A, B, n); METAFOR (P1, ..., P8); table_x/table_y: TABULAR, the
+    DiscreteFunction's points in ascending evp."""
+
+    young: float
+    poisson: float
+    density: float
+    law: int = HARD_POWER
+    params: Sequence[float] = ()
+    table_x: Optional[np.ndarray] = None
+    table_y: Optional[np.ndarray] = None
 
 
 @dataclass
@@ -70,6 +92,23 @@ class Model:
     freq: int = 10
     method: int = COURANT
     nsaves: int = 1
+    # several materials (Structure::attachMaterialToElements): None = one power-law material from
+    # the fields above; elem_material[e] indexes `materials`
+    materials: Optional[List[MaterialLaw]] = None
+    elem_material: Optional[np.ndarray] = None
+    # initial velocity per node (attachInitialBC on node sets), (N, 3); None = v0 everywhere
+    initial_velocity: Optional[np.ndarray] = None
+
+    def material_laws(self) -> List[MaterialLaw]:
+        if self.materials:
+            return list(self.materials)
+        return [MaterialLaw(self.young, self.poisson, self.density, HARD_POWER,
+                            (self.A, self.B, self.n))]
+
+    @property
+    def extended(self) -> bool:
+        return bool(self.materials) or self.elem_material is not None or \
+            self.initial_velocity is not None
 
     @property
     def N(self) -> int:
@@ -166,6 +205,51 @@ def taylor_hex(ncross: int = 40, nz: int = 400, radius: float = 3.2e-3, length: 
     bcs = [BCGroup(RESTRAIN, (0.0, 0.0, 1.0), base)]
     return Model(ELHEX8N3D, coords, conn, young, poisson, density, A, B, n,
                  (0.0, 0.0, -speed), bcs, tend, rho_b, safety, freq, PULSE)
+
+
+def tabular_table(A: float, B: float, n: float, step: float = 0.1, stop: float = 10.0):
+    """The table a deck builds for IsoHardElastoplasticTabular with a loop
+    ``for (eps = 0; eps < stop; eps += step) f.add(eps, A + B * eps^n)`` (Samples/Traction): the
+    abscissae accumulate by repeated double additions, as the interpreter does."""
+    xs, ys = [], []
+    eps = 0.0
+    while eps < stop:
+        xs.append(eps)
+        ys.append(A + B * eps ** n)
+        eps += step
+    return np.array(xs), np.array(ys)
+
+
+def impact_two_materials(nr: int = 5, nz: int = 50, radius: float = 3.2e-3,
+                         length: float = 32.4e-3, split: float = 0.5, speed: float = 80.0,
+                         tend: float = 40e-6, freq: int = 10) -> Model:
+    """Axisymmetric bar of two bonded materials in the pattern of Samples/Traction/Traction.dyn:
+    the lower part (rows j < split*nz) is the deck's target -- E 74.2 GPa, nu 0.33, rho 2784, an
+    IsoHardElastoplasticTabular law tabulating 360 MPa + 316 MPa eps^0.28 every 0.1 up to 10 -- the
+    upper part its projectile -- E 193.6 GPa, nu 0.3, rho 7800, no hardening attached (elastic),
+    and only the projectile's nodes start at `speed` towards the base; base and axis restrained."""
+    m = taylor_axi(nr, nz, radius, length, 0.0, tend=tend, freq=freq)
+    tx, ty = tabular_table(360e6, 316e6, 0.28)
+    target = MaterialLaw(74.2e9, 0.33, 2784.0, HARD_TABULAR, (), tx, ty)
+    projectile = MaterialLaw(193.6e9, 0.3, 7800.0, HARD_ELASTIC, ())
+    js = int(round(split * nz))
+    row = np.repeat(np.arange(nz), nr)
+    em = (row >= js).astype(np.int64)
+    v = np.zeros((m.N, 3))
+    node_row = np.arange(m.N) // (nr + 1)
+    v[node_row >= js, 1] = -speed
+    return dataclasses.replace(m, young=74.2e9, poisson=0.33, density=2784.0,
+                               materials=[target, projectile], elem_material=em,
+                               initial_velocity=v)
+
+
+def metafor_bar(nr: int = 5, nz: int = 50, speed: float = 227.0, tend: float = 40e-6,
+                P=(90e6, 200e6, 10.0, 50e6, 0.5, 1.0, 0.1, 1e8)) -> Model:
+    """The copper Taylor bar with an IsoHardMetafor law (P1..P8):
+    sigma_y = (P2 - P1)(1 - exp(-P3 evp)) + P4 evp^P5 + P1 (1 + P6 evp)^P7 + P8 evp."""
+    m = taylor_axi(nr, nz, speed=speed, tend=tend)
+    law = MaterialLaw(m.young, m.poisson, m.density, HARD_METAFOR, tuple(P))
+    return dataclasses.replace(m, materials=[law])
 
 
 def necking_bar(ncross: int = 40, nz: int = 166, radius: float = 6.4e-3, length: float = 53.3e-3,

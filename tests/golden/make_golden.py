@@ -11,6 +11,9 @@ reference's own output on a seeded synthetic model:
 * ``run_c0.npz``        the 5x50 Taylor bar to 80 us: final coordinates, plastic strain, pressure
 * ``steps_hex.npz``     a 6x6x8 hex bar with the Pulse time step, first 30 steps
 * ``run_hex.npz``       an 8x8x24 hex bar with the Pulse time step to 80 us: final coordinates
+* ``steps_two.npz``     two bonded materials in the pattern of Samples/Traction (tabular target,
+                        elastic projectile with its own initial velocity), first 40 steps
+* ``steps_metafor.npz`` the 5x50 bar with an IsoHardMetafor law, first 40 steps
 * ``results_axi.bin``   the reference's binary results file (Structure::writeData) of the 3x4 axi bar
                         after 13 steps, and ``results_axi.npz`` its state from the harness
 
@@ -47,11 +50,25 @@ def results():
     save("results_axi.npz", **{k: r[k] for k in r if k.startswith("final_")}, time=r["time"])
 
 
+def laws():
+    """The hardening-law / material fixtures only: python tests/golden/make_golden.py laws"""
+    for name, m in (("steps_two.npz", meshes.impact_two_materials(5, 50)),
+                    ("steps_metafor.npz", meshes.metafor_bar(5, 50))):
+        r = dnl_io.run_reference("steps", m, 40)
+        save(name, mass=r["mass"], dt0=r["dt0"], dt=r["dt"], time=r["time"],
+             fint=np.stack([r[f"fint_{k:06d}"] for k in range(40)]),
+             final_coords=r["final_coords"], final_evp=r["final_evp"], final_S=r["final_S"],
+             final_p=r["final_p"])
+
+
 def main():
     if not dnl_io.reference_available():
         sys.exit("compiled reference missing: run `make -C oracle ref`")
     if sys.argv[1:] == ["results"]:
         results()
+        return
+    if sys.argv[1:] == ["laws"]:
+        laws()
         return
     t = dnl_io.reference_tables()
     save("tables.npz", **t)
@@ -86,6 +103,7 @@ def main():
          final_evp=r["final_evp"])
 
     results()
+    laws()
 
 
 if __name__ == "__main__":
