@@ -219,6 +219,31 @@ int dnl_internal_forces_static(const dnl_static_args *args, void *stream, int *b
  * the Structure from the .dyn deck. */
 int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0);
 
+/* ------------------------------------------------------- materials and hardening laws */
+/* The isotropic hardening attached to a Material (Material::setHardening): */
+#define DNL_HARD_POWER 0   /* IsoHardElastoplastic: sigma_y = A + B evp^n, params = A, B, n
+                              (IsoHardElastoplastic.C:171-184) */
+#define DNL_HARD_ELASTIC 1 /* none attached: the material never yields (Material::isYield,
+                              Material.C:366-371) */
+#define DNL_HARD_TABULAR 2 /* IsoHardElastoplasticTabular: a DiscreteFunction of evp, points in
+                              ascending abscissa (IsoHardElastoplasticTabular.C:103-116,
+                              DiscreteFunction.C:169-201, 274-297) */
+#define DNL_HARD_METAFOR 3 /* IsoHardMetafor: params = P1..P8, sigma_y = (P2-P1)(1-exp(-P3 evp))
+                              + P4 evp^P5 + P1 (1 + P6 evp)^P7 + P8 evp (IsoHardMetafor.C:132-153) */
+typedef struct {
+  double young, poisson, density;
+  int law;                        /* DNL_HARD_* */
+  double params[8];
+  int npoints;                    /* DNL_HARD_TABULAR */
+  const double *table_x, *table_y;
+} dnl_material_law;
+/* Several materials in one mesh (Structure::attachMaterialToElements per ElementSet) and any of
+ * the hardening laws: element e gets mats[elem_material[e]] (elem_material NULL: one material for
+ * all).  As Domain::initSolve, each node's density is that of the last element holding it and the
+ * Courant sound speed of an element averages those densities.  Before the prologue; with the
+ * Pulse time step one material only.  Sensitivity runs need one power-law material. */
+int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, const int *elem_material);
+
 /* -------------------------------------------------------------- results / restart files */
 /* The reference's binary results file (Structure::writeData, Structure.C:936-952, through
  * io_Data::structure_write, io_Data.C:486-506): version header, time, per node the coordinates

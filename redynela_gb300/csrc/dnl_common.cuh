@@ -97,6 +97,15 @@ struct DevTime {
 };
 
 // ------------------------------------------------------------------------ kernel arguments
+// The isotropic hardening attached to a material (DNL_HARD_*), passed by value to the non-power
+// laws' evaluation.
+struct HardLaw {
+  int law;
+  int tabN;          // tabular law: number of points, abscissae tab[0..N), ordinates tab[N..2N)
+  const double *tab; // device
+  double P[8];       // Metafor law: P1..P8
+};
+
 struct Material {
   double young, nu, rho, A, B, n;
   double K;          // bulk modulus E / (3 (1 - 2 nu))            (Element.C:232)
@@ -105,6 +114,7 @@ struct Material {
   double dfun0;      // Sqrt32 * 2.0 * G, first term of dfun      (Element.C:309)
   double Cs;         // Courant sound speed with the mean nodal density (Element.C:607-621)
   double rG3;        // 1 / (3 G), for the first radial-return guess (Element.C:298)
+  HardLaw hard;
 };
 
 // Material constants from the ABI description, in the reference's expressions.
@@ -131,6 +141,30 @@ inline Material make_material(const dnl_material &mt)
   ro /= 4;
   const double Nu = m.nu;
   m.Cs = sqrt((m.young * (1 - Nu)) / (ro * (1 + Nu) * (1 - 2 * Nu)));
+  m.hard.law = DNL_HARD_POWER;
+  m.hard.tabN = 0;
+  m.hard.tab = nullptr;
+  for (int k = 0; k < 8; k++) m.hard.P[k] = 0.;
+  return m;
+}
+
+// A material with any of the hardening laws (the moduli as make_material; power-law parameters
+// from params[0..2]; the tabular law's table already on the device at `tab`).
+inline Material make_material_law(const dnl_material_law &ml, const double *tab)
+{
+  dnl_material mt;
+  mt.young = ml.young;
+  mt.poisson = ml.poisson;
+  mt.density = ml.density;
+  const bool power = ml.law == DNL_HARD_POWER;
+  mt.A = power ? ml.params[0] : 0.;
+  mt.B = power ? ml.params[1] : 0.;
+  mt.n = power ? ml.params[2] : 0.;
+  Material m = make_material(mt);
+  m.hard.law = ml.law;
+  m.hard.tabN = ml.law == DNL_HARD_TABULAR ? ml.npoints : 0;
+  m.hard.tab = tab;
+  for (int k = 0; k < 8; k++) m.hard.P[k] = ml.params[k];
   return m;
 }
 
@@ -151,6 +185,9 @@ struct ElemArgs {
   double *tape;        // [TapeLayout::NT][E*NIP], written by the tape instance of k_elem
   DevTime *tm;
   Material mat;
+  const int *elemMat;       // several materials: material of each element (mats), or nullptr
+  const Material *mats;
+  const double *elemCs;     // several materials: Courant sound speed of each element
 };
 
 // Tangent element pass: the primal pass's inputs and record, the tangents of its inputs
@@ -253,6 +290,14 @@ struct dnl_handle {
   // per-kernel event timing (dnl_profile_begin/end)
   bool profiling;
   void *prof;
+  // several materials (dnl_set_materials)
+  int nmat;
+  int *elemMat;               // device, E, or nullptr (one material: mat)
+  dnl::Material *dmats;       // device, nmat
+  double *elemCs;             // device, E: sound speed with the nodal densities of Domain::initSolve
+  double *matTab;             // device: the tabular laws' points
+  double *evpn0;              // device, nmat: (1e-10)^n of power-law materials (dnl_reset)
+  double *nodeRo;             // host, N: Current ro of the first nodal field (results files)
   // initial state (dnl_reset)
   double *x0;                 // initial coordinates [3][N]
   double v0[3];               // initial velocity

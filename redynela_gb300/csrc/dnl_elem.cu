@@ -137,6 +137,43 @@ __device__ __forceinline__ double nr_rcp(double x)
   return fma(r, e, r);
 }
 
+// Yield stress and hardening slope of the non-power laws at x = evp + sqrt(2/3) gamma:
+// IsoHardElastoplasticTabular through DiscreteFunction::getValue / getSlope (the segment ending at
+// the first abscissa >= x, that point's own ordinate when equal, 0 beyond the table; the table is
+// ascending, so a binary search finds the same segment as the reference's linear one) and
+// IsoHardMetafor (IsoHardMetafor.C:132-153, operations in the reference's order).
+__device__ __noinline__ void hardening_law(const HardLaw m, double x, double &sig, double &h)
+{
+  if (m.law == DNL_HARD_TABULAR) {
+    const double *X = m.tab, *Y = m.tab + m.tabN;
+    int lo = 1, hi = m.tabN;  // first i in [1, N) with X[i] >= x, else N
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (X[mid] >= x)
+        hi = mid;
+      else
+        lo = mid + 1;
+    }
+    if (lo >= m.tabN) {
+      sig = 0.;
+      h = 0.;
+      return;
+    }
+    const double x0 = X[lo - 1], x1 = X[lo], y0 = Y[lo - 1], y1 = Y[lo];
+    sig = x1 == x ? y1 : ((x - x0) / (x1 - x0)) * (y1 - y0) + y0;
+    h = (y1 - y0) / (x1 - x0);
+    return;
+  }
+  const double *P = m.P;  // P1..P8
+  const double e3 = exp(-P[2] * (x)), w = 1 + P[5] * x;
+  sig = (P[1] - P[0]) * (1 - e3) + P[3] * pow(x, P[4]) + P[0] * pow(w, P[6]) + P[7] * x;
+  if (x > 0.)
+    h = ((P[1] - P[0]) * P[2] * e3 + P[3] * P[4] * pow(x, (P[4] - 1.0)) +
+         P[0] * P[5] * P[6] * pow((1.0 + P[5] * x), (P[6] - 1.0)) + P[7]);
+  else
+    h = ((P[1] - P[0]) * P[2] * e3 + P[0] * P[5] * P[6] * pow((1.0 + P[5] * x), (P[6] - 1.0)) + P[7]);
+}
+
 // |x| and -x on the bit pattern (integer pipe).
 __device__ __forceinline__ double iabs(double a) { return __longlong_as_double((long long)abits(a)); }
 __device__ __forceinline__ double ineg(double a) { return flip_sign(a); }
@@ -220,7 +257,8 @@ __device__ __forceinline__ void jacobi_rotate(int k, double &f00, double &f11, d
 // lanes with valid == false compute on a clamped element and store nothing.  `red` is this
 // element's NIP x NEN*DIM slice of shared memory; `m` and `tm` are the element's material and
 // time/status record (one per mesh, or per instance in a batch).
-template <int ET, bool TAPE = false>
+// GENERAL: the material may carry any hardening law (otherwise the power law, compiled alone).
+template <int ET, bool TAPE = false, bool GENERAL = false>
 __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, DevTime *tm, int e,
                                         int pt, bool valid, int lane, double *red)
 {
@@ -514,7 +552,12 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     ss = fma(2., off, ss);
     const double normS = sqrt(ss);
     const double Strial = kSqrt32 * normS;
-    const double Sigv0 = RADD(m.A, RMUL(m.B, evpn));
+    const bool power = !GENERAL || m.hard.law == DNL_HARD_POWER;
+    double Sigv0, h0 = 0.;
+    if (power)
+      Sigv0 = RADD(m.A, RMUL(m.B, evpn));
+    else if (GENERAL)
+      hardening_law(m.hard, evp, Sigv0, h0);
     if (TAPE) {
       const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
 #pragma unroll
@@ -524,7 +567,45 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
       tape(TL::XV, evp);
       tape(TL::XN, evpn);
     }
-    if (__double_as_longlong(Strial) > __double_as_longlong(Sigv0)) {  // both >= 0
+    if (GENERAL && !power && m.hard.law != DNL_HARD_ELASTIC && Strial > Sigv0) {
+      // any other hardening law: the return of Element.C:282-345 with the law's
+      // getIsotropicYieldStress / getIsotropicYieldHardening at evp + sqrt(2/3) gamma
+      plastic = true;
+      double gamma = (normS - kSqrt23 * Sigv0) / (m.G2 * (1.0 + h0 / m.G3));
+      int iteration = 0;
+      for (;;) {
+        double Sigv, h;
+        hardening_law(m.hard, RADD(evp, RMUL(kSqrt23, gamma)), Sigv, h);
+        const double dfun = kSqrt32 * m.G2 + kSqrt23 * h;
+        const double fun = dfun * gamma - (Strial - Sigv + h * kSqrt23 * gamma);
+        if (fabs(fun / Sigv) > kRadialReturnPrecision) {
+          double dgamma = -fun / dfun;
+          if (dgamma < 0 && fabs(dgamma) > gamma) dgamma = -gamma * 0.9;
+          gamma += dgamma;
+        } else {
+          break;
+        }
+        iteration++;
+        if (iteration > kRadialReturnMaxIt) {
+          if (valid) record_error(tm, DNL_ERR_RR_NOCONV, e);
+          break;
+        }
+      }
+      const double inv = 1. / normS;
+      evp = RADD(evp, RMUL(kSqrt23, gamma));
+      const double c2 = m.G2 * gamma;
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = i; j < 3; j++) {
+          if (AXI && (i == 2) != (j == 2)) continue;
+          const double n1 = S[i][j] * inv;
+          S[i][j] = fma(-c2, n1, S[i][j]);
+          Epl[i][j] = fma(gamma, n1, Epl[i][j]);
+          S[j][i] = S[i][j];
+          Epl[j][i] = Epl[i][j];
+        }
+    } else if (power && __double_as_longlong(Strial) > __double_as_longlong(Sigv0)) {  // both >= 0
       plastic = true;
       double h = m.nB * evpn * nr_rcp(evp);
       double gamma = fma(-kSqrt23, Sigv0, normS) * nr_rcp(m.G2 * fma(h, m.rG3, 1.0));
@@ -692,7 +773,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
   }
 }
 
-template <int ET, bool TAPE = false>
+template <int ET, bool TAPE = false, bool GENERAL = false>
 __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
 {
   constexpr int NIP = Elem<ET>::NIP, NEN = Elem<ET>::NEN, DIM = Elem<ET>::DIM;
@@ -704,8 +785,13 @@ __global__ void __launch_bounds__(128) k_elem(ElemArgs a)
   const int eRaw = gtid / NIP;
   const bool valid = eRaw < a.E;
   const int lane = threadIdx.x & 31;
-  elem_ip<ET, TAPE>(a, a.mat, a.tm, valid ? eRaw : a.E - 1, gtid % NIP, valid, lane,
-                    red[threadIdx.x >> 5][lane / NIP]);
+  const int e = valid ? eRaw : a.E - 1;
+  if (GENERAL && a.elemMat)
+    elem_ip<ET, TAPE, true>(a, a.mats[a.elemMat[e]], a.tm, e, gtid % NIP, valid, lane,
+                            red[threadIdx.x >> 5][lane / NIP]);
+  else
+    elem_ip<ET, TAPE, GENERAL>(a, a.mat, a.tm, e, gtid % NIP, valid, lane,
+                               red[threadIdx.x >> 5][lane / NIP]);
 }
 
 // Batched element pass over the union of many meshes: element e belongs to instance inst[e],
@@ -813,6 +899,8 @@ __global__ void __launch_bounds__(256) k_courant(ElemArgs a)
     if (!(len > 0.)) {
       record_error(a.tm, DNL_ERR_DT, e);
       len = 1e300;
+    } else if (a.elemCs) {
+      len = len / a.elemCs[e];  // several materials: the critical time of this element
     }
   }
 #pragma unroll
@@ -878,6 +966,9 @@ static ElemArgs elem_args(dnl_handle *h)
   a.stepT = h->stepT;
   a.tm = h->tm;
   a.mat = h->mat;
+  a.elemMat = h->elemMat;
+  a.mats = h->dmats;
+  a.elemCs = h->elemCs;
   a.gate = 1;
   return a;
 }
@@ -889,10 +980,18 @@ int launch_elem(dnl_handle *h, cudaStream_t s, int gate)
   const long threads = (long)h->E * h->nip;
   const int grid = (int)((threads + 127) / 128);
   prof_begin(h, s);
-  if (h->etype == DNL_ELQUA4NAX)
-    k_elem<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a);
-  else
-    k_elem<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a);
+  const bool general = h->elemMat || h->mat.hard.law != DNL_HARD_POWER;
+  if (h->etype == DNL_ELQUA4NAX) {
+    if (general)
+      k_elem<DNL_ELQUA4NAX, false, true><<<grid, 128, 0, s>>>(a);
+    else
+      k_elem<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a);
+  } else {
+    if (general)
+      k_elem<DNL_ELHEX8N3D, false, true><<<grid, 128, 0, s>>>(a);
+    else
+      k_elem<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a);
+  }
   prof_end(h, DNL_PROF_ELEM, s);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
@@ -934,9 +1033,9 @@ int launch_mass(dnl_handle *h, cudaStream_t s, double *me)
   const long threads = (long)h->E * h->nip;
   const int grid = (int)((threads + 127) / 128);
   if (h->etype == DNL_ELQUA4NAX)
-    k_mass<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a, me, nullptr, nullptr);
+    k_mass<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a, me, h->elemMat, h->dmats);
   else
-    k_mass<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a, me, nullptr, nullptr);
+    k_mass<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a, me, h->elemMat, h->dmats);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }

@@ -299,6 +299,13 @@ __global__ void k_fill(double *p, long n, double v)
   if (i < n) p[i] = v;
 }
 
+// cached evp^n at evp = 1e-10 per element material (several materials)
+__global__ void k_fill_evpn(long nIP, int nip, const int *elemMat, const double *evpn0, double *out)
+{
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nIP) out[i] = evpn0[elemMat[i / nip]];
+}
+
 __global__ void k_fp64_peak(double *out, double a, double b, int iters)
 {
   double x0 = threadIdx.x * 1e-9, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5,
@@ -416,7 +423,7 @@ int launch_dt(dnl_handle *h, int mode)
   a.freq = h->freq;
   a.method = h->method;
   a.safetyOmega = h->safetyOmega;
-  a.Cs = h->mat.Cs;
+  a.Cs = h->elemCs ? 1.0 : h->mat.Cs;  // several materials: k_courant reduced len / Cs per element
   prof_begin(h, h->stream);
   k_dt<<<1, 1, 0, h->stream>>>(a);
   prof_end(h, DNL_PROF_OTHER, h->stream);
@@ -763,7 +770,8 @@ int dnl_destroy(dnl_handle *h)
   for (int i = 0; i < h->ngraphs; i++) cudaGraphExecDestroy(h->graphs[i].exec);
   void *ptrs[] = {h->conn, h->x[0], h->n2eStart, h->n2e, h->mass, h->fieldMem, h->ip, h->detJ,
                   h->stepT, h->fe, h->fint, h->stage, h->bcIdx, h->bcCode, h->bcNodeList, h->bcSpeed,
-                  h->pj, h->ev, h->kx, h->tm, h->x0};
+                  h->pj, h->ev, h->kx, h->tm, h->x0, h->elemMat, h->dmats, h->elemCs,
+                  h->matTab, h->evpn0};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; i++)
@@ -778,13 +786,112 @@ int dnl_destroy(dnl_handle *h)
     for (auto e : p->pool) cudaEventDestroy(e);
     delete p;
   }
+  delete[] h->nodeRo;
   delete h;
+  return 0;
+}
+
+int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, const int *elem_material)
+{
+  if (!h || nmat < 1 || !mats || h->prologueDone) return DNL_ERR_ARG;
+  if (nmat > 1 && !elem_material) return DNL_ERR_ARG;
+  if (nmat > 1 && h->method == DNL_PULSE) return DNL_ERR_ARG;  // one Hooke matrix per handle
+  const long N = h->N, E = h->E, nIP = h->nIP;
+  if (elem_material)
+    for (long e = 0; e < E; e++)
+      if (elem_material[e] < 0 || elem_material[e] >= nmat) return DNL_ERR_ARG;
+  long ntab = 0;
+  for (int i = 0; i < nmat; i++) {
+    const dnl_material_law &ml = mats[i];
+    if (ml.law < DNL_HARD_POWER || ml.law > DNL_HARD_METAFOR) return DNL_ERR_ARG;
+    if (!(ml.young > 0. && ml.density > 0.)) return DNL_ERR_ARG;
+    if (ml.law == DNL_HARD_TABULAR) {
+      if (ml.npoints < 1 || !ml.table_x || !ml.table_y) return DNL_ERR_ARG;
+      for (int k = 1; k < ml.npoints; k++)
+        if (!(ml.table_x[k] >= ml.table_x[k - 1])) return DNL_ERR_ARG;  // ascending (sorted DiscreteFunction)
+      ntab += 2 * ml.npoints;
+    }
+  }
+  // drop an earlier assignment
+  void *old[] = {h->elemMat, h->dmats, h->elemCs, h->matTab, h->evpn0};
+  for (void *p : old)
+    if (p) cudaFree(p);
+  h->elemMat = nullptr;
+  h->dmats = nullptr;
+  h->elemCs = nullptr;
+  h->matTab = nullptr;
+  h->evpn0 = nullptr;
+  delete[] h->nodeRo;
+  h->nodeRo = nullptr;
+  if (ntab) CK(cudaMalloc(&h->matTab, sizeof(double) * ntab));
+  std::vector<Material> hm(nmat);
+  std::vector<double> pn(nmat, 0.);
+  long off = 0;
+  for (int i = 0; i < nmat; i++) {
+    const dnl_material_law &ml = mats[i];
+    const double *tab = nullptr;
+    if (ml.law == DNL_HARD_TABULAR) {
+      CK(cudaMemcpy(h->matTab + off, ml.table_x, sizeof(double) * ml.npoints, cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(h->matTab + off + ml.npoints, ml.table_y, sizeof(double) * ml.npoints, cudaMemcpyHostToDevice));
+      tab = h->matTab + off;
+      off += 2 * ml.npoints;
+    }
+    hm[i] = make_material_law(ml, tab);
+    if (ml.law == DNL_HARD_POWER) pn[i] = pow(1e-10, ml.params[2]);
+  }
+  h->nmat = nmat;
+  h->mat = hm[0];
+  {  // Material::getHookeMatrix of material 0 for the Pulse estimate
+    const double Nu = h->mat.nu;
+    const double f = (h->mat.young * (1.0 - Nu) / ((1.0 + Nu) * (1.0 - 2.0 * Nu)));
+    h->C00 = 1 * f;
+    h->C01 = (Nu / (1. - Nu)) * f;
+    h->C33 = ((1.0 - 2.0 * Nu) / (2. * (1.0 - Nu))) * f;
+  }
+  // nodal densities as Domain::initSolve assigns them: element order, the last element wins
+  std::vector<int> conn((size_t)E * h->nen);
+  CK(cudaMemcpy(conn.data(), h->conn, sizeof(int) * conn.size(), cudaMemcpyDeviceToHost));  // [NEN][E]
+  h->nodeRo = new double[N];
+  for (long n = 0; n < N; n++) h->nodeRo[n] = hm[0].rho;
+  for (long e = 0; e < E; e++) {
+    const int mi = elem_material ? elem_material[e] : 0;
+    for (int k = 0; k < h->nen; k++) h->nodeRo[conn[(size_t)k * E + e]] = hm[mi].rho;
+  }
+  std::vector<double> pnIP(nIP);
+  for (long e = 0; e < E; e++)
+    for (int q = 0; q < h->nip; q++) pnIP[e * h->nip + q] = pn[elem_material ? elem_material[e] : 0];
+  const int ns = h->etype == DNL_ELQUA4NAX ? 4 : 6;
+  CK(cudaMemcpy(h->ip + (size_t)(3 * ns + 2) * nIP, pnIP.data(), sizeof(double) * nIP, cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&h->evpn0, sizeof(double) * nmat));
+  CK(cudaMemcpy(h->evpn0, pn.data(), sizeof(double) * nmat, cudaMemcpyHostToDevice));
+  if (nmat > 1) {
+    // Element::getSoundSpeed: the element's E and nu, the mean of its nodes' densities
+    std::vector<double> cs(E);
+    for (long e = 0; e < E; e++) {
+      const Material &m = hm[elem_material[e]];
+      double ro = 0.;
+      for (int k = 0; k < h->nen; k++) ro += h->nodeRo[conn[(size_t)k * E + e]];
+      ro /= h->nen;
+      const double Nu = m.nu;
+      cs[e] = sqrt((m.young * (1 - Nu)) / (ro * (1 + Nu) * (1 - 2 * Nu)));
+    }
+    std::vector<int> em(elem_material, elem_material + E);
+    CK(cudaMalloc(&h->elemMat, sizeof(int) * E));
+    CK(cudaMemcpy(h->elemMat, em.data(), sizeof(int) * E, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&h->dmats, sizeof(Material) * nmat));
+    CK(cudaMemcpy(h->dmats, hm.data(), sizeof(Material) * nmat, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&h->elemCs, sizeof(double) * E));
+    CK(cudaMemcpy(h->elemCs, cs.data(), sizeof(double) * E, cudaMemcpyHostToDevice));
+  }
+  for (int i = 0; i < h->ngraphs; i++) cudaGraphExecDestroy(h->graphs[i].exec);
+  h->ngraphs = 0;
   return 0;
 }
 
 int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0)
 {
   if (!h) return DNL_ERR_ARG;
+  if (mat && (h->nmat > 1 || h->mat.hard.law != DNL_HARD_POWER)) return DNL_ERR_ARG;
   cudaStream_t s = h->stream;
   CK(cudaStreamSynchronize(s));
   for (int i = 0; i < h->ngraphs; i++) cudaGraphExecDestroy(h->graphs[i].exec);
@@ -816,8 +923,12 @@ int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0)
   const int ns = h->etype == DNL_ELQUA4NAX ? 4 : 6;
   CK(cudaMemsetAsync(h->ip, 0, sizeof(double) * ncomp * nIP, s));
   k_fill<<<(unsigned)((nIP + 255) / 256), 256, 0, s>>>(h->ip + (size_t)(3 * ns + 1) * nIP, nIP, 1e-10);
-  k_fill<<<(unsigned)((nIP + 255) / 256), 256, 0, s>>>(h->ip + (size_t)(3 * ns + 2) * nIP, nIP,
-                                                       pow(1e-10, h->mat.n));
+  if (h->elemMat)
+    k_fill_evpn<<<(unsigned)((nIP + 255) / 256), 256, 0, s>>>(nIP, h->nip, h->elemMat, h->evpn0,
+                                                              h->ip + (size_t)(3 * ns + 2) * nIP);
+  else
+    k_fill<<<(unsigned)((nIP + 255) / 256), 256, 0, s>>>(h->ip + (size_t)(3 * ns + 2) * nIP, nIP,
+                                                         h->mat.hard.law == DNL_HARD_POWER ? pow(1e-10, h->mat.n) : 0.);
   launch_counter() += 2;
   CK(cudaMemsetAsync(h->fint, 0, sizeof(double) * h->dim * N, s));
   if (h->stepT) CK(cudaMemsetAsync(h->stepT, 0, sizeof(double) * 18 * nIP, s));

@@ -116,9 +116,9 @@ int dnl_write_results(dnl_handle *h, const char *path)
   o.put(t.time);
   o.header();
   o.put(t.time);
-  const double ro = h->cur == 0 ? h->mat.rho : 0.;
   for (long n = 0; n < N; n++) {
     o.put(&x[3 * n], 3);
+    const double ro = h->cur != 0 ? 0. : (h->nodeRo ? h->nodeRo[n] : h->mat.rho);
     const double therm[5] = {ro, 0., 0., 0., 0.};  // ro, dro, e, de, T
     o.put(therm, 5);
     o.put(&v[3 * n], 3);

@@ -61,6 +61,12 @@ class MaterialDesc(C.Structure):
                 ("A", C.c_double), ("B", C.c_double), ("n", C.c_double)]
 
 
+class MaterialLawDesc(C.Structure):
+    _fields_ = [("young", C.c_double), ("poisson", C.c_double), ("density", C.c_double),
+                ("law", C.c_int), ("params", C.c_double * 8), ("npoints", C.c_int),
+                ("table_x", C.POINTER(C.c_double)), ("table_y", C.POINTER(C.c_double))]
+
+
 class SolverParams(C.Structure):
     _fields_ = [("end_time", C.c_double), ("rho_b", C.c_double), ("safety", C.c_double),
                 ("frequency", C.c_int), ("method", C.c_int), ("flags", C.c_int)]
@@ -133,6 +139,7 @@ def lib():
         L.dnl_set_dt_schedule.argtypes = [H, _dp, C.c_int]
         L.dnl_adjoint.argtypes = [H, _dp, _dp, C.c_int]
         L.dnl_reset.argtypes = [H, C.POINTER(MaterialDesc), _dp]
+        L.dnl_set_materials.argtypes = [H, C.c_int, C.POINTER(MaterialLawDesc), _ip]
         L.dnl_write_results.argtypes = [H, C.c_char_p]
         L.dnl_read_results.argtypes = [H, C.c_char_p]
         L.dnl_batch_sens_run.argtypes = [H, C.c_int, _dp, _dp, _dp]
@@ -225,6 +232,26 @@ class GpuDomain:
         self._check(L.dnl_create(C.byref(desc), C.byref(mat), C.byref(sp), C.byref(h)))
         self.h = h
         self.L = L
+        if m.materials or m.elem_material is not None:
+            self.set_materials(m.material_laws(), m.elem_material)
+        if m.initial_velocity is not None:
+            self.set_state(v=np.asarray(m.initial_velocity, dtype=np.float64))
+
+    def set_materials(self, laws, elem_material=None) -> None:
+        """dnl_set_materials: materials with their hardening laws, one per element."""
+        arr = (MaterialLawDesc * len(laws))()
+        keep = []
+        for i, ml in enumerate(laws):
+            prm = list(ml.params) + [0.0] * (8 - len(ml.params))
+            tx = np.ascontiguousarray(ml.table_x if ml.table_x is not None else np.zeros(1), dtype=np.float64)
+            ty = np.ascontiguousarray(ml.table_y if ml.table_y is not None else np.zeros(1), dtype=np.float64)
+            keep += [tx, ty]
+            npts = len(ml.table_x) if ml.table_x is not None else 0
+            arr[i] = MaterialLawDesc(ml.young, ml.poisson, ml.density, int(ml.law), (C.c_double * 8)(*prm),
+                                     npts, tx.ctypes.data_as(_dp), ty.ctypes.data_as(_dp))
+        em = None if elem_material is None else np.ascontiguousarray(elem_material, dtype=np.int32)
+        self._check(self.L.dnl_set_materials(self.h, len(laws), arr,
+                                             em.ctypes.data_as(_ip) if em is not None else None))
 
     def close(self):
         if getattr(self, "h", None):
