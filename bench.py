@@ -61,7 +61,7 @@ def elem_bytes(m) -> float:
     """Compulsory HBM bytes of one k_elem launch: integration-point state read (S, Eps, EpsPlas, p,
     evp, evp^n) and written (S, Eps, EpsPlas, p; evp and evp^n only where plastic, not counted),
     connectivity, element forces written, node coordinates and delta_disp read once."""
-    ns = 4 if m.etype == meshes.ELQUA4NAX else 6
+    ns = 6 if m.etype == meshes.ELHEX8N3D else 4
     ncomp = 3 * ns + 3
     per_elem = m.nip * (ncomp * 8 + (3 * ns + 1) * 8) + m.nen * 4 + m.nen * m.dim * 8
     return m.E * per_elem + m.N * 2 * m.dim * 8

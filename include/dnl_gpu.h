@@ -42,6 +42,7 @@ enum dnl_status {
 /* element types */
 #define DNL_ELQUA4NAX 0 /* ElQua4nAx: 4-node axisymmetric quad, 2x2 Gauss points */
 #define DNL_ELHEX8N3D 1 /* ElHex8n3D: 8-node hexahedron, 2x2x2 Gauss points */
+#define DNL_ELQUA4N2D 2 /* ElQua4n2D: 4-node plane-strain quad, 2x2 Gauss points (ElementPlane) */
 
 /* time-step methods (Solver::setTimeStepMethod, Solver.C:312-321) */
 #define DNL_COURANT 0
@@ -59,7 +60,7 @@ typedef struct dnl_handle dnl_handle;
 /* Mesh and boundary conditions (Structure::createNode/createElement, attachInitialBC,
  * attachConstantBC).  Node and element order is the reference's Id order. */
 typedef struct {
-  int etype;            /* DNL_ELQUA4NAX or DNL_ELHEX8N3D */
+  int etype;            /* DNL_ELQUA4NAX, DNL_ELHEX8N3D or DNL_ELQUA4N2D */
   int num_nodes;        /* N */
   int num_elements;     /* E */
   const double *coords; /* N*3, node-major (x, y, z) like Node::coords */

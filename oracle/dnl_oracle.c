@@ -97,7 +97,7 @@ static const int HX_ZETA[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
 
 static void build_tables(dnlo *h)
 {
-  if (h->etype == 0) {
+  if (h->etype != 1) { /* ElQua4nAx and ElQua4n2D share their tables (ElQua4n2D.C:26-70) */
     const double cN[3] = {(2.0 + sqrt(3.0)) / 6.0, 1.0 / 6.0, (2.0 - sqrt(3.0)) / 6.0};
     const double cD[2] = {(3.0 + sqrt(3.0)) / 12.0, (3.0 - sqrt(3.0)) / 12.0};
     for (int pt = 0; pt < 4; pt++) {
@@ -388,8 +388,9 @@ static double elem_radius(const dnlo *h, long e, int pt)
   return R;
 }
 
-/* ElementAx::getF_atIntPoint (ElementAx.C:114-136) / Element3D::getF_atIntPoint
- * (Element3D.C:182-205) with the Current nodal field (Node::getFieldAtTime(0), Node.h:178-183) */
+/* ElementAx::getF_atIntPoint (ElementAx.C:114-136) / ElementPlane::getF_atIntPoint
+ * (ElementPlane.C:83-99, no hoop stretch) / Element3D::getF_atIntPoint (Element3D.C:182-205) with
+ * the Current nodal field (Node::getFieldAtTime(0), Node.h:178-183) */
 static void elem_F(const dnlo *h, long e, int pt, double *F)
 {
   const long *cn = h->conn + e * h->nen;
@@ -405,8 +406,10 @@ static void elem_F(const dnlo *h, long e, int pt, double *F)
       F[4] += DN(h, e, pt, k, 1) * d[1];
       v += h->Nt[pt][k] * d[0];
     }
-    const double R = elem_radius(h, e, pt);
-    F[8] += v / R;
+    if (h->etype == 0) {
+      const double R = elem_radius(h, e, pt);
+      F[8] += v / R;
+    }
   } else {
     for (int k = 0; k < 8; k++) {
       const double *d = du + cn[k] * 3;
@@ -684,7 +687,8 @@ double dnlo_courant(dnlo *h)
 }
 
 /* Element2D::computeElasticStiffnessMatrix (Element2D.C:129-226) and Element3D's
- * (Element3D.C:242-333), full integration, with Material::getHookeMatrix (Material.C:270-331).
+ * (Element3D.C:242-333), full integration, with Material::getHookeMatrix (Material.C:270-331):
+ * the axisymmetric 4x4, the plane-strain 3x3 (its upper-left block) or the 3D 6x6.
  * Ke is row-major (nd x nd). */
 static void elem_stiffness(const dnlo *h, long e, double *Ke)
 {
@@ -692,11 +696,15 @@ static void elem_stiffness(const dnlo *h, long e, double *Ke)
   const double Nu = h->mNu[MATOF(h, e)], E = h->mE[MATOF(h, e)];
   double C[6][6];
   memset(C, 0, sizeof C);
-  if (h->etype == 0) {
-    C[0][0] = 1; C[1][1] = 1; C[3][3] = 1;
+  const int axi = h->etype == 0;
+  if (h->etype != 1) {
+    C[0][0] = 1; C[1][1] = 1;
     C[1][0] = Nu / (1. - Nu); C[0][1] = Nu / (1. - Nu);
-    C[3][0] = Nu / (1. - Nu); C[3][1] = Nu / (1. - Nu);
-    C[0][3] = Nu / (1. - Nu); C[1][3] = Nu / (1. - Nu);
+    if (axi) {
+      C[3][3] = 1;
+      C[3][0] = Nu / (1. - Nu); C[3][1] = Nu / (1. - Nu);
+      C[0][3] = Nu / (1. - Nu); C[1][3] = Nu / (1. - Nu);
+    }
     C[2][2] = (1.0 - 2.0 * Nu) / (2. * (1.0 - Nu));
     const double f = (E * (1.0 - Nu) / ((1.0 + Nu) * (1.0 - 2.0 * Nu)));
     for (int i = 0; i < 4; i++)
@@ -719,9 +727,11 @@ static void elem_stiffness(const dnlo *h, long e, double *Ke)
     const long ix = IPX(h, e, pt);
     double WxdJ = h->weight[pt] * h->detJ[ix];
     double R = 0.;
-    if (h->etype == 0) {
-      R = elem_radius(h, e, pt);
-      WxdJ *= 2 * DNL_PI * R;
+    if (h->etype != 1) {
+      if (axi) {
+        R = elem_radius(h, e, pt);
+        WxdJ *= 2 * DNL_PI * R;
+      }
       for (int i = 0; i < 4; i++) {
         const int I = 2 * i;
         const double d0 = DN(h, e, pt, i, 0), d1 = DN(h, e, pt, i, 1), Ni = h->Nt[pt][i];
@@ -731,6 +741,7 @@ static void elem_stiffness(const dnlo *h, long e, double *Ke)
         CB[0][I + 1] = (C[0][1] * d1 + C[0][2] * d0);
         CB[1][I + 1] = (C[1][1] * d1 + C[1][2] * d0);
         CB[2][I + 1] = (C[2][1] * d1 + C[2][2] * d0);
+        if (!axi) continue;
         CB[3][I] = (C[3][0] * d0 + C[3][2] * d1);
         CB[3][I + 1] = (C[3][1] * d1 + C[3][2] * d0);
         CB[0][I] += C[0][3] * Ni / R;
@@ -746,6 +757,7 @@ static void elem_stiffness(const dnlo *h, long e, double *Ke)
           Ke[I * nd + J + 1] += (d0 * CB[0][J + 1] + d1 * CB[2][J + 1]) * WxdJ;
           Ke[(I + 1) * nd + J] += (d1 * CB[1][J] + d0 * CB[2][J]) * WxdJ;
           Ke[(I + 1) * nd + J + 1] += (d1 * CB[1][J + 1] + d0 * CB[2][J + 1]) * WxdJ;
+          if (!axi) continue;
           Ke[I * nd + J] += CB[3][J] * Ni / R * WxdJ;
           Ke[I * nd + J + 1] += CB[3][J + 1] * Ni / R * WxdJ;
         }
@@ -992,11 +1004,11 @@ dnlo *dnlo_create(int etype, long N, long E, const double *coords, const long *c
                   const double *bc_val, const long *bc_start, const long *bc_nodes,
                   const double *solver)
 {
-  if ((etype != 0 && etype != 1) || N <= 0 || E <= 0) return NULL;
+  if ((etype != 0 && etype != 1 && etype != 2) || N <= 0 || E <= 0) return NULL;
   dnlo *h = (dnlo *)calloc(1, sizeof(dnlo));
   h->etype = etype;
-  h->dim = etype == 0 ? 2 : 3;
-  h->nen = h->nip = etype == 0 ? 4 : 8;
+  h->dim = etype == 1 ? 3 : 2;
+  h->nen = h->nip = etype == 1 ? 8 : 4;
   h->N = N;
   h->E = E;
   h->conn = (long *)malloc(sizeof(long) * E * h->nen);
@@ -1266,8 +1278,8 @@ int dnlo_tables(int etype, double *N, double *dN)
   dnlo t;
   memset(&t, 0, sizeof t);
   t.etype = etype;
-  t.dim = etype == 0 ? 2 : 3;
-  t.nen = t.nip = etype == 0 ? 4 : 8;
+  t.dim = etype == 1 ? 3 : 2;
+  t.nen = t.nip = etype == 1 ? 8 : 4;
   build_tables(&t);
   for (int pt = 0; pt < t.nip; pt++)
     for (int k = 0; k < t.nen; k++) {

@@ -3,8 +3,8 @@
  * Only tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load this library, and
  * only as the checker / the timed CPU baseline.  The product path (libdnlgpu.so) never calls it.
  *
- * Element types: ElQua4nAx (etype 0, 4 nodes, 2x2 Gauss points) and ElHex8n3D (etype 1, 8 nodes,
- * 2x2x2 Gauss points).  Storage mirrors the reference objects: nodal vectors are (N, 3) like Vec3D,
+ * Element types: ElQua4nAx (etype 0, 4 nodes, 2x2 Gauss points), ElHex8n3D (etype 1, 8 nodes,
+ * 2x2x2 Gauss points) and ElQua4n2D (etype 2, plane strain, the tables of ElQua4nAx).  Storage mirrors the reference objects: nodal vectors are (N, 3) like Vec3D,
  * integration-point tensors are (E, nip, 3, 3) row-major like Tensor2 (linearAlgebra/Tensor2.h).
  */
 #ifndef DNL_ORACLE_H

@@ -175,7 +175,7 @@ namespace {
 
 void build_tables(dnls *h)
 {
-  if (h->etype == 0) {
+  if (h->etype != 1) {  // ElQua4nAx and ElQua4n2D share their tables
     const double cN[3] = {(2.0 + sqrt(3.0)) / 6.0, 1.0 / 6.0, (2.0 - sqrt(3.0)) / 6.0};
     const double cD[2] = {(3.0 + sqrt(3.0)) / 12.0, (3.0 - sqrt(3.0)) / 12.0};
     for (int pt = 0; pt < 4; pt++) {
@@ -543,8 +543,10 @@ void elem_F(const dnls *h, long e, int pt, D *F)
       F[4] += DNS(h, e, pt, k, 1) * d[1];
       v += h->Nt[pt][k] * d[0];
     }
-    const D R = elem_radius(h, e, pt);
-    F[8] += v / R;
+    if (h->etype == 0) {  // ElementPlane (etype 2) has no hoop stretch
+      const D R = elem_radius(h, e, pt);
+      F[8] += v / R;
+    }
   } else {
     for (int k = 0; k < 8; k++) {
       const D *d = du + cn[k] * 3;
@@ -776,11 +778,11 @@ dnls *dnls_create(int etype, long N, long E, const double *coords, const long *c
                   const long *bc_kind, const double *bc_val, const long *bc_start,
                   const long *bc_nodes, double rho_b)
 {
-  if ((etype != 0 && etype != 1) || N <= 0 || E <= 0) return nullptr;
+  if ((etype != 0 && etype != 1 && etype != 2) || N <= 0 || E <= 0) return nullptr;
   dnls *h = new dnls();
   h->etype = etype;
-  h->dim = etype == 0 ? 2 : 3;
-  h->nen = h->nip = etype == 0 ? 4 : 8;
+  h->dim = etype == 1 ? 3 : 2;
+  h->nen = h->nip = etype == 1 ? 8 : 4;
   h->N = N;
   h->E = E;
   h->conn.assign(conn, conn + E * h->nen);

@@ -63,8 +63,8 @@ def lib():
 
 def tables(etype: int):
     """(N, dN/dxi) tables the oracle builds: (nip, nen) and (nip, nen, dim)."""
-    nen = 4 if etype == 0 else 8
-    dim = 2 if etype == 0 else 3
+    nen = 8 if etype == 1 else 4
+    dim = 3 if etype == 1 else 2
     N = np.zeros((nen, nen))
     dN = np.zeros((nen, nen, dim))
     lib().dnlo_tables(etype, _dp(N), _dp(dN))

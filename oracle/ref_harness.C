@@ -15,7 +15,7 @@
 //   ref_harness forces <model> <state> <out>  inject nodal + integration-point state, then one
 //                                             computeInternalMatrices + computeInternalForces
 //   ref_harness bench  <model> <out> <K>      K steps of the loop, wall time only
-//   ref_harness tables <out>                  element tables of ElQua4nAx and ElHex8n3D
+//   ref_harness tables <out>                  element tables of ElQua4nAx, ElHex8n3D, ElQua4n2D
 //
 // Run it with OMP_NUM_THREADS=1 for golden data: strategy 0 of Domain::computeInternalForces sums
 // element forces under `omp critical`, so with several threads the summation order (and the last
@@ -49,6 +49,7 @@
 #include <NodalField.h>
 #include <Element.h>
 #include <ElQua4nAx.h>
+#include <ElQua4n2D.h>
 #include <ElHex8n3D.h>
 #include <Material.h>
 #include <IsoHardElastoplastic.h>
@@ -148,7 +149,7 @@ struct MatLaw
 
 struct Model
 {
-  long etype; // 0 ElQua4nAx, 1 ElHex8n3D
+  long etype; // 0 ElQua4nAx, 1 ElHex8n3D, 2 ElQua4n2D
   long N, E, nen;
   std::vector<double> coords; // N*3
   std::vector<long> conn;     // E*nen, 0-based
@@ -178,7 +179,7 @@ static Model readModel(const char *path)
   m.etype = r.i64();
   m.N = r.i64();
   m.E = r.i64();
-  m.nen = (m.etype == 0 ? 4 : 8);
+  m.nen = (m.etype == 1 ? 8 : 4);
   m.coords.resize(m.N * 3);
   r.f64s(m.coords.data(), m.coords.size());
   m.conn.resize(m.E * m.nen);
@@ -253,7 +254,9 @@ static Built build(const Model &m)
   for (long n = 0; n < m.N; n++)
     st->createNode(n + 1, m.coords[3 * n], m.coords[3 * n + 1], m.coords[3 * n + 2]);
 
-  Element *proto = (m.etype == 0 ? (Element *)new ElQua4nAx(0) : (Element *)new ElHex8n3D(0));
+  Element *proto = (m.etype == 0   ? (Element *)new ElQua4nAx(0)
+                    : m.etype == 2 ? (Element *)new ElQua4n2D(0)
+                                   : (Element *)new ElHex8n3D(0));
   st->setDefaultElement(proto);
   ElementSet *els = new ElementSet;
   for (long e = 0; e < m.E; e++)
@@ -626,14 +629,15 @@ static int cmdForces(const Model &m, const char *statePath, const std::string &o
   return 0;
 }
 
-// Element tables of ElQua4nAx / ElHex8n3D (ElQua4nAx.C:31-101, ElHex8n3D.C:26-161): per Gauss
-// point its weight, N_k and dN_k/dxi_c.
+// Element tables of ElQua4nAx / ElHex8n3D / ElQua4n2D (ElQua4nAx.C:31-101, ElHex8n3D.C:26-161,
+// ElQua4n2D.C:26-70): per Gauss point its weight, N_k and dN_k/dxi_c.
 static int cmdTables(const std::string &out)
 {
   Writer w(out);
-  const ElementData *tabs[2] = {&ElQua4nAx::elementData, &ElHex8n3D::elementData};
-  const char *names[2] = {"axi", "hex"};
-  for (int t = 0; t < 2; t++)
+  const ElementData *tabs[3] = {&ElQua4nAx::elementData, &ElHex8n3D::elementData,
+                                &ElQua4n2D::elementData};
+  const char *names[3] = {"axi", "hex", "plane"};
+  for (int t = 0; t < 3; t++)
   {
     const ElementData *d = tabs[t];
     std::vector<double> wgt, N, dN;

@@ -12,10 +12,10 @@ from __future__ import annotations
 import numpy as np
 
 
-def _sym(rng, shape, scale, axi):
+def _sym(rng, shape, scale, two_d):
     t = rng.normal(scale=scale, size=shape + (3, 3))
     t = 0.5 * (t + np.swapaxes(t, -1, -2))
-    if axi:
+    if two_d:
         t[..., 0, 2] = t[..., 2, 0] = t[..., 1, 2] = t[..., 2, 1] = 0.0
     return t
 
@@ -24,6 +24,7 @@ def random_state(model, seed: int = 0, du_scale: float = 2e-3, dt: float = 1e-8)
     rng = np.random.default_rng(seed)
     m = model
     axi = m.etype == 0
+    two_d = m.etype != 1
     dim, N, E, nip = m.dim, m.N, m.E, m.nip
     x = m.coords[m.conn]  # (E, nen, 3)
     h = float(np.min(np.linalg.norm(x[:, 1] - x[:, 0], axis=1)))
@@ -46,16 +47,16 @@ def random_state(model, seed: int = 0, du_scale: float = 2e-3, dt: float = 1e-8)
     evp = rng.uniform(1e-10, 0.4, size=(E, nip))
     evp[rng.uniform(size=(E, nip)) < 0.2] = 1e-10
     sig_y = m.A + m.B * evp ** m.n
-    S = _sym(rng, (E, nip), 1.0, axi)
+    S = _sym(rng, (E, nip), 1.0, two_d)
     tr = np.trace(S, axis1=-2, axis2=-1)[..., None, None] / 3.0
     S = S - tr * np.eye(3)
     nrm = np.sqrt(1.5 * np.sum(S * S, axis=(-1, -2)))
     target = sig_y * rng.uniform(0.7, 1.1, size=(E, nip))
     S *= (target / nrm)[..., None, None]
-    if axi:
+    if two_d:
         S[..., 0, 2] = S[..., 2, 0] = S[..., 1, 2] = S[..., 2, 1] = 0.0
-    Eps = _sym(rng, (E, nip), 2e-2, axi)
-    EpsPlas = _sym(rng, (E, nip), 1e-2, axi)
+    Eps = _sym(rng, (E, nip), 2e-2, two_d)
+    EpsPlas = _sym(rng, (E, nip), 1e-2, two_d)
     p = rng.normal(scale=1e8, size=(E, nip))
     return dict(coords=coords, du=du, v=v, a=a, disp=disp, S=S, Eps=Eps, EpsPlas=EpsPlas, p=p,
                 evp=evp, dt=dt)

@@ -145,10 +145,10 @@ int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material 
   if (!out || count <= 0 || !meshes || !mats || !sps) return DNL_ERR_ARG;
   *out = nullptr;
   const int etype = meshes[0].etype;
-  const int nen = etype == DNL_ELQUA4NAX ? 4 : 8;
+  const int nen = etype == DNL_ELHEX8N3D ? 8 : 4;
   // plain batched stepping needs the axisymmetric Courant step of every instance; sensitivity
   // runs take a step schedule and accept any element type and time-step method
-  bool canStep = etype == DNL_ELQUA4NAX;
+  bool canStep = etype != DNL_ELHEX8N3D;
   for (int i = 0; i < count; i++) {
     if (meshes[i].etype != etype) return DNL_ERR_ARG;
     if (sps[i].method != sps[0].method || sps[i].frequency != sps[0].frequency) return DNL_ERR_ARG;
@@ -299,7 +299,7 @@ int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material 
       const double val = pow(1e-10, mats[i].n);
       for (size_t q = (size_t)elemOff[i] * h->nip; q < (size_t)elemOff[i + 1] * h->nip; q++) pn[q] = val;
     }
-    const int ns = etype == DNL_ELQUA4NAX ? 4 : 6;
+    const int ns = etype == DNL_ELHEX8N3D ? 6 : 4;
     BKF(cudaMemcpy(h->ip + (size_t)(3 * ns + 2) * nIP, pn.data(), sizeof(double) * nIP, cudaMemcpyHostToDevice));
   }
   BKF(cudaDeviceSynchronize());
@@ -457,8 +457,8 @@ int dnl_batch_reset(dnl_batch *b)
   for (int i = 0; i < b->ngraphs; i++) cudaGraphExecDestroy(b->graphs[i].exec);
   b->ngraphs = 0;
   const long N = h->N, nIP = h->nIP;
-  const int ncomp = h->etype == DNL_ELQUA4NAX ? IpLayout<DNL_ELQUA4NAX>::NCOMP : IpLayout<DNL_ELHEX8N3D>::NCOMP;
-  const int ns = h->etype == DNL_ELQUA4NAX ? 4 : 6;
+  const int ncomp = h->etype == DNL_ELHEX8N3D ? IpLayout<DNL_ELHEX8N3D>::NCOMP : IpLayout<DNL_ELQUA4NAX>::NCOMP;
+  const int ns = h->etype == DNL_ELHEX8N3D ? 6 : 4;
   BK(cudaMemcpyAsync(h->x[0], h->x0, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
   BK(cudaMemsetAsync(h->fieldMem, 0, sizeof(double) * 24 * N, s));
   BK(cudaMemsetAsync(h->ip, 0, sizeof(double) * ncomp * nIP, s));

@@ -33,6 +33,10 @@ template <> struct Elem<DNL_ELHEX8N3D> {
   static constexpr int DIM = 3, NEN = 8, NIP = 8;
   static constexpr int NS = 6;  // xx yy zz xy xz yz
 };
+template <> struct Elem<DNL_ELQUA4N2D> {  // plane strain: the quad of ElQua4nAx without the hoop terms
+  static constexpr int DIM = 2, NEN = 4, NIP = 4;
+  static constexpr int NS = 4;
+};
 
 // integration-point state, component-major: ip[comp * nIP + (e * NIP + pt)]
 //   S[NS] | Eps[NS] | EpsPlas[NS] | p | evp | evpn (= evp^n, cached yield term)
@@ -305,6 +309,21 @@ struct dnl_handle {
   double v0dir[3];            // unit vector of the initial velocity
   void *sens;
 };
+
+// CALL instantiated for the handle's element type, as ET (CALL in parentheses when it has commas)
+#define DNL_BY_ETYPE(etype, CALL)                    \
+  do {                                               \
+    if ((etype) == DNL_ELQUA4NAX) {                  \
+      constexpr int ET = DNL_ELQUA4NAX;              \
+      CALL;                                          \
+    } else if ((etype) == DNL_ELQUA4N2D) {           \
+      constexpr int ET = DNL_ELQUA4N2D;              \
+      CALL;                                          \
+    } else {                                         \
+      constexpr int ET = DNL_ELHEX8N3D;              \
+      CALL;                                          \
+    }                                                \
+  } while (0)
 
 namespace dnl {
 // launchers implemented in dnl_elem.cu

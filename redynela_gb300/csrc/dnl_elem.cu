@@ -95,6 +95,7 @@ template <> struct Shape<DNL_ELQUA4NAX> {
     return s ? v : flip_sign(v);
   }
 };
+template <> struct Shape<DNL_ELQUA4N2D> : Shape<DNL_ELQUA4NAX> {};  // same tables (ElQua4n2D.C:31-101)
 template <> struct Shape<DNL_ELHEX8N3D> {
   __device__ __forceinline__ static double N(int pt, int k)
   {
@@ -212,8 +213,8 @@ __device__ __forceinline__ void jacobi_angle(double fpp, double fqq, double fpq,
 // its x' a rounding residual; the closed form rounds once.  The two diagonals differ by a few ulps
 // of 1 (at most 9 in 4e5 random 3x3 cases, the same order as the angle's own effect) and the
 // pivot sequences are the same (x' is below the 1e-9 stop either way).
-// AXI: C is block diagonal and the pivot is always (0, 1).
-template <bool AXI>
+// TWO_D (axisymmetric and plane strain): C is block diagonal and the pivot is always (0, 1).
+template <bool TWO_D>
 __device__ __forceinline__ void jacobi_rotate(int k, double &f00, double &f11, double &f22, double &f01,
                                               double &f02, double &f12, double rot[3][3], double x)
 {
@@ -225,7 +226,7 @@ __device__ __forceinline__ void jacobi_rotate(int k, double &f00, double &f11, d
   const double a2 = fma(ineg(t), x, a);
   const double b2 = fma(t, x, b);
   const double x2 = 0.;
-  if (AXI) {
+  if (TWO_D) {
     f00 = a2;
     f11 = b2;
     f01 = x2;
@@ -241,7 +242,7 @@ __device__ __forceinline__ void jacobi_rotate(int k, double &f00, double &f11, d
     f12 = k == 2 ? x2 : z2;
   }
 #pragma unroll
-  for (int i = 0; i < (AXI ? 2 : 3); i++) {
+  for (int i = 0; i < (TWO_D ? 2 : 3); i++) {
     const double rp = k == 2 ? rot[i][1] : rot[i][0];
     const double rq = k == 0 ? rot[i][1] : rot[i][2];
     const double np = fma(rp, c, rq * ms), nq = fma(rp, s, rq * c);
@@ -267,7 +268,8 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
   using SH = Shape<ET>;
   using TL = TapeLayout<ET>;
   constexpr int NIP = T::NIP, NEN = T::NEN, DIM = T::DIM, NS = T::NS;
-  constexpr bool AXI = ET == DNL_ELQUA4NAX;
+  constexpr bool AXI = ET == DNL_ELQUA4NAX;    // radius, hoop strain and hoop force
+  constexpr bool TWO_D = ET != DNL_ELHEX8N3D;  // the 2 + 1 block structure of F, C, R, S
   const long nIP = (long)a.E * NIP;
   const long ipx = (long)e * NIP + pt;
   auto tape = [&](int slot, double v) {
@@ -297,7 +299,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     if (AXI) Rad = RADD(Rad, RMUL(SH::N(pt, k), xk[0]));
   }
   double detJ, Ji[DIM][DIM];
-  if (AXI) {
+  if (TWO_D) {
     detJ = fma(J[0][0], J[1][1], -J[0][1] * J[1][0]);
     const double r = 1. / detJ;
     Ji[0][0] = J[1][1] * r;
@@ -387,11 +389,11 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
 #pragma unroll
     for (int j = i; j < 3; j++) {
       double s;
-      if (AXI && (i == 2) != (j == 2)) {
+      if (TWO_D && (i == 2) != (j == 2)) {
         s = 0.;
-      } else if (AXI && i == 2) {
+      } else if (TWO_D && i == 2) {
         s = RMUL(F[2][2], F[2][2]);
-      } else if (AXI) {
+      } else if (TWO_D) {
         s = RADD(RMUL(F[0][i], F[0][j]), RMUL(F[1][i], F[1][j]));
       } else {
         s = RADD(RADD(RMUL(F[0][i], F[0][j]), RMUL(F[1][i], F[1][j])), RMUL(F[2][i], F[2][j]));
@@ -409,7 +411,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
       // pivot of Tensor2.C:1173-1178: q = |C01| > |C02| ? 1 : 2, p = |C0q| > |C12| ? 0 : 1
       int k = 0;
       double fpq = f01;
-      if (!AXI) {
+      if (!TWO_D) {
         const bool q1 = abs_gt(f01, f02);
         const double f0q = q1 ? f01 : f02;
         const bool p0 = abs_gt(f0q, f12);
@@ -420,7 +422,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         conv = true;
         break;
       }
-      jacobi_rotate<AXI>(k, f00, f11, f22, f01, f02, f12, rot, fpq);
+      jacobi_rotate<TWO_D>(k, f00, f11, f22, f01, f02, f12, rot, fpq);
     }
     f[0][0] = f00;
     f[1][1] = f11;
@@ -466,14 +468,14 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
 #pragma unroll
       for (int j = i; j < 3; j++) {
         double su = 0., sr = 0.;
-        if (AXI && (i == 2 || j == 2)) {
+        if (TWO_D && (i == 2 || j == 2)) {
           if (i == 2 && j == 2) {
             su = lg[2];
             sr = il[2];
           }
         } else {
 #pragma unroll
-          for (int cc = 0; cc < (AXI ? 2 : 3); cc++) {
+          for (int cc = 0; cc < (TWO_D ? 2 : 3); cc++) {
             const double ext = rot[i][cc] * rot[j][cc];
             su = fma(lg[cc], ext, su);
             sr = fma(il[cc], ext, sr);
@@ -493,14 +495,14 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      if (AXI && (i == 2) != (j == 2)) {
+      if (TWO_D && (i == 2) != (j == 2)) {
         R[i][j] = 0.;
-      } else if (AXI && i == 2) {
+      } else if (TWO_D && i == 2) {
         R[i][j] = F[2][2] * Rr[2][2];
       } else {
         double s = 0.;
 #pragma unroll
-        for (int k = 0; k < (AXI ? 2 : 3); k++) s = fma(F[i][k], Rr[k][j], s);
+        for (int k = 0; k < (TWO_D ? 2 : 3); k++) s = fma(F[i][k], Rr[k][j], s);
         R[i][j] = s;
       }
     }
@@ -523,7 +525,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
       Ep[I0[k]][I1[k]] = Ep[I1[k]][I0[k]] = ev + dE[I0[k]][I1[k]];
       Epl[I0[k]][I1[k]] = Epl[I1[k]][I0[k]] = pv;
     }
-    if (AXI) {
+    if (TWO_D) {
       S[0][2] = S[2][0] = S[1][2] = S[2][1] = 0.;
       Ep[0][2] = Ep[2][0] = Ep[1][2] = Ep[2][1] = 0.;
       Epl[0][2] = Epl[2][0] = Epl[1][2] = Epl[2][1] = 0.;
@@ -536,7 +538,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int j = i; j < 3; j++) {
-        if (AXI && (i == 2) != (j == 2)) continue;
+        if (TWO_D && (i == 2) != (j == 2)) continue;
         const double dv = i == j ? dE[i][j] - tr3 : dE[i][j];
         S[i][j] = fma(m.G2, dv, S[i][j]);
         S[j][i] = S[i][j];
@@ -548,7 +550,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
   {
     double ss = fma(S[0][0], S[0][0], fma(S[1][1], S[1][1], S[2][2] * S[2][2]));
     double off = S[0][1] * S[0][1];
-    if (!AXI) off = fma(S[0][2], S[0][2], fma(S[1][2], S[1][2], off));
+    if (!TWO_D) off = fma(S[0][2], S[0][2], fma(S[1][2], S[1][2], off));
     ss = fma(2., off, ss);
     const double normS = sqrt(ss);
     const double Strial = kSqrt32 * normS;
@@ -598,7 +600,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
       for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int j = i; j < 3; j++) {
-          if (AXI && (i == 2) != (j == 2)) continue;
+          if (TWO_D && (i == 2) != (j == 2)) continue;
           const double n1 = S[i][j] * inv;
           S[i][j] = fma(-c2, n1, S[i][j]);
           Epl[i][j] = fma(gamma, n1, Epl[i][j]);
@@ -643,7 +645,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
       for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int j = i; j < 3; j++) {
-          if (AXI && (i == 2) != (j == 2)) continue;
+          if (TWO_D && (i == 2) != (j == 2)) continue;
           const double n1 = S[i][j] * inv;
           S[i][j] = fma(-c2, n1, S[i][j]);
           Epl[i][j] = fma(gamma, n1, Epl[i][j]);
@@ -665,7 +667,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
 
   // ---- RFI: X <- R X R^T for S, Eps, EpsPlas (Element.C:386-388)
   auto rfi = [&](double X[3][3]) {
-    if (AXI) {
+    if (TWO_D) {
       double Tm[2][2];
 #pragma unroll
       for (int i = 0; i < 2; i++)
@@ -829,6 +831,7 @@ __global__ void __launch_bounds__(128) k_mass(ElemArgs a, double *me, const int 
   using SH = Shape<ET>;
   constexpr int NIP = T::NIP, NEN = T::NEN, DIM = T::DIM;
   constexpr bool AXI = ET == DNL_ELQUA4NAX;
+  constexpr bool TWO_D = ET != DNL_ELHEX8N3D;
   constexpr int EPW = 32 / NIP;
   __shared__ double red[128 / 32][EPW][NIP][NEN];
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -856,7 +859,7 @@ __global__ void __launch_bounds__(128) k_mass(ElemArgs a, double *me, const int 
     if (AXI) Rad = RADD(Rad, RMUL(SH::N(pt, k), a.x[0][nd]));
   }
   double detJ;
-  if (AXI) {
+  if (TWO_D) {
     detJ = RSUB(RMUL(J[0][0], J[1][1]), RMUL(J[0][1], J[1][0]));
   } else {
     detJ = RADD(RADD(RMUL(RMUL(J[0][0], J[1][1]), J[2][2]), RMUL(RMUL(J[1][0], J[2][1]), J[0][2])),
@@ -981,17 +984,10 @@ int launch_elem(dnl_handle *h, cudaStream_t s, int gate)
   const int grid = (int)((threads + 127) / 128);
   prof_begin(h, s);
   const bool general = h->elemMat || h->mat.hard.law != DNL_HARD_POWER;
-  if (h->etype == DNL_ELQUA4NAX) {
-    if (general)
-      k_elem<DNL_ELQUA4NAX, false, true><<<grid, 128, 0, s>>>(a);
-    else
-      k_elem<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a);
-  } else {
-    if (general)
-      k_elem<DNL_ELHEX8N3D, false, true><<<grid, 128, 0, s>>>(a);
-    else
-      k_elem<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a);
-  }
+  if (general)
+    DNL_BY_ETYPE(h->etype, (k_elem<ET, false, true><<<grid, 128, 0, s>>>(a)));
+  else
+    DNL_BY_ETYPE(h->etype, (k_elem<ET><<<grid, 128, 0, s>>>(a)));
   prof_end(h, DNL_PROF_ELEM, s);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
@@ -1006,10 +1002,7 @@ int launch_elem_tape(dnl_handle *h, cudaStream_t s, double *tape)
   const long threads = (long)h->E * h->nip;
   const int grid = (int)((threads + 127) / 128);
   prof_begin(h, s);
-  if (h->etype == DNL_ELQUA4NAX)
-    k_elem<DNL_ELQUA4NAX, true><<<grid, 128, 0, s>>>(a);
-  else
-    k_elem<DNL_ELHEX8N3D, true><<<grid, 128, 0, s>>>(a);
+  DNL_BY_ETYPE(h->etype, (k_elem<ET, true><<<grid, 128, 0, s>>>(a)));
   prof_end(h, DNL_PROF_ELEM, s);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
@@ -1017,12 +1010,9 @@ int launch_elem_tape(dnl_handle *h, cudaStream_t s, double *tape)
 
 int launch_elem_raw(int etype, const ElemArgs &a, cudaStream_t s)
 {
-  const long threads = (long)a.E * (etype == DNL_ELQUA4NAX ? 4 : 8);
+  const long threads = (long)a.E * (etype == DNL_ELHEX8N3D ? 8 : 4);
   const int grid = (int)((threads + 127) / 128);
-  if (etype == DNL_ELQUA4NAX)
-    k_elem<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a);
-  else
-    k_elem<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a);
+  DNL_BY_ETYPE(etype, (k_elem<ET><<<grid, 128, 0, s>>>(a)));
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
@@ -1032,10 +1022,7 @@ int launch_mass(dnl_handle *h, cudaStream_t s, double *me)
   ElemArgs a = elem_args(h);
   const long threads = (long)h->E * h->nip;
   const int grid = (int)((threads + 127) / 128);
-  if (h->etype == DNL_ELQUA4NAX)
-    k_mass<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a, me, h->elemMat, h->dmats);
-  else
-    k_mass<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a, me, h->elemMat, h->dmats);
+  DNL_BY_ETYPE(h->etype, (k_mass<ET><<<grid, 128, 0, s>>>(a, me, h->elemMat, h->dmats)));
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
@@ -1043,11 +1030,15 @@ int launch_mass(dnl_handle *h, cudaStream_t s, double *me)
 int launch_elem_batch(int etype, int block, const ElemArgs &a, const int *elemInst,
                       const Material *mats, DevTime *tms, cudaStream_t s)
 {
-  const long threads = (long)a.E * (etype == DNL_ELQUA4NAX ? 4 : 8);
+  const long threads = (long)a.E * (etype == DNL_ELHEX8N3D ? 8 : 4);
   const int grid = (int)((threads + block - 1) / block);
 #define DNL_EB(ET, B) k_elem_batch<ET, B><<<grid, B, 0, s>>>(a, elemInst, mats, tms)
-  if (etype == DNL_ELQUA4NAX) {
-    if (block == 64) DNL_EB(DNL_ELQUA4NAX, 64);
+  if (etype != DNL_ELHEX8N3D) {
+    if (etype == DNL_ELQUA4N2D) {
+      if (block == 64) DNL_EB(DNL_ELQUA4N2D, 64);
+      else if (block == 256) DNL_EB(DNL_ELQUA4N2D, 256);
+      else DNL_EB(DNL_ELQUA4N2D, 128);
+    } else if (block == 64) DNL_EB(DNL_ELQUA4NAX, 64);
     else if (block == 256) DNL_EB(DNL_ELQUA4NAX, 256);
     else DNL_EB(DNL_ELQUA4NAX, 128);
   } else {
@@ -1063,12 +1054,9 @@ int launch_elem_batch(int etype, int block, const ElemArgs &a, const int *elemIn
 int launch_elem_batch_tape(int etype, const ElemArgs &a, const int *elemInst, const Material *mats,
                            DevTime *tms, cudaStream_t s)
 {
-  const long threads = (long)a.E * (etype == DNL_ELQUA4NAX ? 4 : 8);
+  const long threads = (long)a.E * (etype == DNL_ELHEX8N3D ? 8 : 4);
   const int grid = (int)((threads + 127) / 128);
-  if (etype == DNL_ELQUA4NAX)
-    k_elem_batch<DNL_ELQUA4NAX, 128, true><<<grid, 128, 0, s>>>(a, elemInst, mats, tms);
-  else
-    k_elem_batch<DNL_ELHEX8N3D, 128, true><<<grid, 128, 0, s>>>(a, elemInst, mats, tms);
+  DNL_BY_ETYPE(etype, (k_elem_batch<ET, 128, true><<<grid, 128, 0, s>>>(a, elemInst, mats, tms)));
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
@@ -1076,12 +1064,9 @@ int launch_elem_batch_tape(int etype, const ElemArgs &a, const int *elemInst, co
 int launch_mass_batch(int etype, const ElemArgs &a, double *me, const int *elemInst,
                       const Material *mats, cudaStream_t s)
 {
-  const long threads = (long)a.E * (etype == DNL_ELQUA4NAX ? 4 : 8);
+  const long threads = (long)a.E * (etype == DNL_ELHEX8N3D ? 8 : 4);
   const int grid = (int)((threads + 127) / 128);
-  if (etype == DNL_ELQUA4NAX)
-    k_mass<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a, me, elemInst, mats);
-  else
-    k_mass<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a, me, elemInst, mats);
+  DNL_BY_ETYPE(etype, (k_mass<ET><<<grid, 128, 0, s>>>(a, me, elemInst, mats)));
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }

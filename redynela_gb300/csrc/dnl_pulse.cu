@@ -48,6 +48,14 @@ template <> __device__ __forceinline__ double pdN<DNL_ELQUA4NAX>(int pt, int k, 
   const double v = other ? c_pshape.axD[1] : c_pshape.axD[0];
   return (c == 0 ? psgx(k) : psgy(k)) ? v : -v;
 }
+template <> __device__ __forceinline__ double pN<DNL_ELQUA4N2D>(int pt, int k)
+{
+  return pN<DNL_ELQUA4NAX>(pt, k);
+}
+template <> __device__ __forceinline__ double pdN<DNL_ELQUA4N2D>(int pt, int k, int c)
+{
+  return pdN<DNL_ELQUA4NAX>(pt, k, c);
+}
 template <> __device__ __forceinline__ double pN<DNL_ELHEX8N3D>(int pt, int k)
 {
   const int d = (psgx(k) ^ psgx(pt)) + (psgy(k) ^ psgy(pt)) + (psgz(k) ^ psgz(pt));
@@ -98,7 +106,7 @@ __global__ void __launch_bounds__(128) k_pulse_setup(PulseArgs a)
 {
   using T = Elem<ET>;
   constexpr int NIP = T::NIP, NEN = T::NEN, DIM = T::DIM;
-  constexpr bool AXI = ET == DNL_ELQUA4NAX;
+  constexpr bool AXI = ET == DNL_ELQUA4NAX, TWO_D = ET != DNL_ELHEX8N3D;
   if (a.tm->done | a.tm->status) return;
   const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long nIP = (long)a.E * NIP;
@@ -118,7 +126,7 @@ __global__ void __launch_bounds__(128) k_pulse_setup(PulseArgs a)
     if (AXI) Rad = fma(pN<ET>(pt, k), a.x[0][nd], Rad);
   }
   double Ji[DIM][DIM], detJ;
-  if (AXI) {
+  if (TWO_D) {
     detJ = J[0][0] * J[1][1] - J[0][1] * J[1][0];
     const double r = 1. / detJ;
     Ji[0][0] = J[1][1] * r;
@@ -204,10 +212,11 @@ __global__ void __launch_bounds__(128) k_pulse_kx(PulseArgs a)
       for (int l = 0; l < DIM; l++) s = fma(G[r][l], Ji[l][c], s);
       gr[r][c] = s;
     }
-  // Hooke stress S (symmetric 3x3 of the in-plane components) and, axisymmetric, the hoop stress
+  // Hooke stress S of the in-plane components and, axisymmetric, the hoop stress (plane strain:
+  // the upper-left block of the axisymmetric matrix, no hoop strain)
   double S[DIM][DIM], hoop = 0.;
-  if (AXI) {
-    const double e0 = gr[0][0], e1 = gr[1][1], e2 = gr[0][1] + gr[1][0], e3 = ur / Rad;
+  if (DIM == 2) {
+    const double e0 = gr[0][0], e1 = gr[1][1], e2 = gr[0][1] + gr[1][0], e3 = AXI ? ur / Rad : 0.;
     S[0][0] = a.C00 * e0 + a.C01 * (e1 + e3);
     S[1][1] = a.C00 * e1 + a.C01 * (e0 + e3);
     S[0][1] = S[1][0] = a.C33 * e2;
@@ -372,18 +381,15 @@ int launch_pulse(dnl_handle *h, cudaStream_t s)
   const int gridN = (h->N + 255) / 256;
   prof_begin(h, s);
   k_pulse_begin<<<1, 1, 0, s>>>(h->tm);
-  if (h->etype == DNL_ELQUA4NAX)
-    k_pulse_setup<DNL_ELQUA4NAX><<<gridIP, 128, 0, s>>>(a);
-  else
-    k_pulse_setup<DNL_ELHEX8N3D><<<gridIP, 128, 0, s>>>(a);
+  DNL_BY_ETYPE(h->etype, (k_pulse_setup<ET><<<gridIP, 128, 0, s>>>(a)));
   prof_end(h, DNL_PROF_PULSE, s);
   launch_counter() += 2;
   const int batch = 4;
   for (int round = 0; round < (kPulseMaxIt + batch) / batch + 1; round++) {
     for (int b = 0; b < batch; b++) {
       prof_begin(h, s);
-      if (h->etype == DNL_ELQUA4NAX) {
-        k_pulse_kx<DNL_ELQUA4NAX><<<gridIP, 128, 0, s>>>(a);
+      if (h->etype != DNL_ELHEX8N3D) {
+        DNL_BY_ETYPE(h->etype, (k_pulse_kx<ET><<<gridIP, 128, 0, s>>>(a)));
         k_pulse_gather<2><<<gridN, 256, 0, s>>>(a, h->E * h->nen);
       } else {
         k_pulse_kx<DNL_ELHEX8N3D><<<gridIP, 128, 0, s>>>(a);

@@ -185,8 +185,8 @@ __global__ void k_to_nodes(int N, double *out, const double *c0, const double *c
 int sens_alloc(dnl_handle *h, SensState *S)
 {
   const long nIP = (long)h->E * h->nip, N = h->N;
-  const int NT = h->etype == DNL_ELQUA4NAX ? TapeLayout<DNL_ELQUA4NAX>::NT : TapeLayout<DNL_ELHEX8N3D>::NT;
-  const int NC = h->etype == DNL_ELQUA4NAX ? TanLayout<DNL_ELQUA4NAX>::NCOMP : TanLayout<DNL_ELHEX8N3D>::NCOMP;
+  const int NT = h->etype == DNL_ELHEX8N3D ? TapeLayout<DNL_ELHEX8N3D>::NT : TapeLayout<DNL_ELQUA4NAX>::NT;
+  const int NC = h->etype == DNL_ELHEX8N3D ? TanLayout<DNL_ELHEX8N3D>::NCOMP : TanLayout<DNL_ELQUA4NAX>::NCOMP;
   const long nodal = (long)kSensParams * 3 * N;
   const long total = NT * nIP + nodal * 9 + (long)kSensParams * NC * nIP +
                      (long)kSensParams * h->dim * h->E * h->nen + 3 * N;
@@ -229,7 +229,7 @@ int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt)
   cudaStream_t s = h->stream;
   const long nIP = (long)h->E * h->nip;
   {
-    const int NT = h->etype == DNL_ELQUA4NAX ? TapeLayout<DNL_ELQUA4NAX>::NT : TapeLayout<DNL_ELHEX8N3D>::NT;
+    const int NT = h->etype == DNL_ELHEX8N3D ? TapeLayout<DNL_ELHEX8N3D>::NT : TapeLayout<DNL_ELQUA4NAX>::NT;
     const size_t bytes = sizeof(double) * (size_t)((S->out - S->mem) - NT * nIP);
     CKS(cudaMemsetAsync(S->tx, 0, bytes, s));
   }

@@ -31,6 +31,7 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
   using L = IpLayout<ET>;
   constexpr int NIP = T::NIP, NEN = T::NEN, DIM = T::DIM, NS = T::NS;
   constexpr bool AXI = ET == DNL_ELQUA4NAX;
+  constexpr bool TWO_D = ET != DNL_ELHEX8N3D;
   const long nIP = (long)a.E * NIP, ipx = (long)e * NIP + pt, N = a.N;
   const Material &m = a.elemInst ? a.mats[a.elemInst[e]] : a.mat;
   auto tp = [&](int slot) { return a.tape[(long)slot * nIP + ipx]; };
@@ -38,7 +39,7 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
   double *tip = a.tip + (long)dir * TN::NCOMP * nIP;
   const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
   // (i, j) entries that are identically zero in the axisymmetric block structure (2 + 1)
-  auto zero = [](int i, int j) { return AXI && ((i == 2) != (j == 2)); };
+  auto zero = [](int i, int j) { return TWO_D && ((i == 2) != (j == 2)); };
   auto symload = [&](double X[3][3], auto get) {
 #pragma unroll
     for (int i = 0; i < 3; i++)
@@ -418,12 +419,9 @@ __global__ void __launch_bounds__(128) k_elem_tan(SensElemArgs a)
 
 int launch_elem_tan(int etype, const SensElemArgs &a, cudaStream_t s)
 {
-  const long threads = (long)a.E * kSensParams * (etype == DNL_ELQUA4NAX ? 4 : 8);
+  const long threads = (long)a.E * kSensParams * (etype == DNL_ELHEX8N3D ? 8 : 4);
   const int grid = (int)((threads + 127) / 128);
-  if (etype == DNL_ELQUA4NAX)
-    k_elem_tan<DNL_ELQUA4NAX><<<grid, 128, 0, s>>>(a);
-  else
-    k_elem_tan<DNL_ELHEX8N3D><<<grid, 128, 0, s>>>(a);
+  DNL_BY_ETYPE(etype, (k_elem_tan<ET><<<grid, 128, 0, s>>>(a)));
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }

@@ -56,8 +56,9 @@ extern "C" int dnl_internal_forces_static(const dnl_static_args *a, void *stream
   using namespace dnl;
   if (bad_element) *bad_element = -1;
   if (!a) return DNL_ERR_ARG;
-  if (a->etype != DNL_ELQUA4NAX && a->etype != DNL_ELHEX8N3D) return DNL_ERR_ARG;
-  const int nen = a->etype == DNL_ELQUA4NAX ? 4 : 8, dim = a->etype == DNL_ELQUA4NAX ? 2 : 3;
+  if (a->etype != DNL_ELQUA4NAX && a->etype != DNL_ELHEX8N3D && a->etype != DNL_ELQUA4N2D)
+    return DNL_ERR_ARG;
+  const int nen = a->etype == DNL_ELHEX8N3D ? 8 : 4, dim = a->etype == DNL_ELHEX8N3D ? 3 : 2;
   if (a->num_nodes <= 0 || a->num_elements <= 0) return DNL_ERR_ARG;
   if ((long long)a->num_elements * nen * dim > DNL_STATIC_MAX_ELEMENT_DOFS) return DNL_ERR_ARG;
   if (!a->conn || !a->node_start || !a->node_entry || !a->coords || !a->du || !a->ip || !a->fint)

@@ -713,6 +713,7 @@ class ExplicitSolverCH:
 
 ElQua4nAx = meshes.ELQUA4NAX
 ElHex8n3D = meshes.ELHEX8N3D
+ElQua4n2D = meshes.ELQUA4N2D
 
 
 class Structure:

@@ -29,6 +29,7 @@ import numpy as np
 
 ELQUA4NAX = 0
 ELHEX8N3D = 1
+ELQUA4N2D = 2  # plane strain
 
 COURANT = 0
 PULSE = 1
@@ -120,15 +121,15 @@ class Model:
 
     @property
     def dim(self) -> int:
-        return 2 if self.etype == ELQUA4NAX else 3
+        return 3 if self.etype == ELHEX8N3D else 2
 
     @property
     def nen(self) -> int:
-        return 4 if self.etype == ELQUA4NAX else 8
+        return 8 if self.etype == ELHEX8N3D else 4
 
     @property
     def nip(self) -> int:
-        return 4 if self.etype == ELQUA4NAX else 8
+        return 8 if self.etype == ELHEX8N3D else 4
 
 
 def taylor_axi(nr: int = 5, nz: int = 50, radius: float = 3.2e-3, length: float = 32.4e-3,
@@ -152,6 +153,12 @@ def taylor_axi(nr: int = 5, nz: int = 50, radius: float = 3.2e-3, length: float 
     bcs = [BCGroup(RESTRAIN, (0.0, 1.0, 0.0), base), BCGroup(RESTRAIN, (1.0, 0.0, 1.0), axis)]
     return Model(ELQUA4NAX, coords, conn, young, poisson, density, A, B, n,
                  (0.0, -speed, 0.0), bcs, tend, rho_b, safety, freq, COURANT)
+
+
+def taylor_plane(nr: int = 5, nz: int = 50, **kw) -> Model:
+    """Plane-strain Taylor impact: taylor_axi's mesh and boundary conditions on ElQua4n2D
+    elements, x = 0 a symmetry plane instead of the axis."""
+    return dataclasses.replace(taylor_axi(nr, nz, **kw), etype=ELQUA4N2D)
 
 
 def taylor_axi_free_surface(nr: int, nz: int) -> np.ndarray:

@@ -4,7 +4,7 @@ Needs the reference DynELA numerical core built by ``make -C oracle ref`` (it co
 reference sources where they lie; only possible where those sources exist).  Every fixture is the
 reference's own output on a seeded synthetic model:
 
-* ``tables.npz``        element tables of ElQua4nAx / ElHex8n3D
+* ``tables.npz``        element tables of ElQua4nAx / ElHex8n3D / ElQua4n2D
 * ``forces_axi.npz``    one Domain::computeInternalForces on an injected mid-run state, 3x4 axi bar
 * ``forces_hex.npz``    the same on a 4x4x3 hex bar
 * ``steps_c0.npz``      the 5x50 Taylor bar, first 20 steps: Fint, dt, kinetic energy per step
@@ -16,12 +16,17 @@ reference's own output on a seeded synthetic model:
 * ``steps_metafor.npz`` the 5x50 bar with an IsoHardMetafor law, first 40 steps
 * ``results_axi.bin``   the reference's binary results file (Structure::writeData) of the 3x4 axi bar
                         after 13 steps, and ``results_axi.npz`` its state from the harness
+* ``forces_plane.npz``  one Domain::computeInternalForces on an injected state, 3x4 ElQua4n2D bar
+* ``steps_plane.npz``   the 5x50 bar in plane strain (ElQua4n2D), first 40 steps
+* ``run_plane.npz``     the same bar to 80 us: final coordinates, plastic strain, pressure
+* ``steps_plane_pulse.npz`` the plane-strain bar with the Pulse time step, first 30 steps
 
     python tests/golden/make_golden.py
 """
 
 from __future__ import annotations
 
+import dataclasses
 import os
 import sys
 
@@ -61,6 +66,31 @@ def laws():
              final_p=r["final_p"])
 
 
+def plane():
+    """The plane-strain (ElQua4n2D) fixtures only: python tests/golden/make_golden.py plane"""
+    save("tables.npz", **dnl_io.reference_tables())
+    m = meshes.taylor_plane(3, 4)
+    st = states.random_state(m, seed=7)
+    r = dnl_io.run_reference("forces", m, state=st)
+    save("forces_plane.npz", **{f"in_{k}": np.asarray(v) for k, v in st.items()}, fint=r["fint"],
+         **{k: r[k] for k in r if k.startswith("out_")})
+    m = meshes.taylor_plane(5, 50)
+    r = dnl_io.run_reference("steps", m, 40)
+    save("steps_plane.npz", mass=r["mass"], dt0=r["dt0"], dt=r["dt"], time=r["time"],
+         kinetic=r["kinetic"], fint=np.stack([r[f"fint_{k:06d}"] for k in range(40)]),
+         final_coords=r["final_coords"], final_evp=r["final_evp"], final_S=r["final_S"],
+         final_p=r["final_p"])
+    mp = dataclasses.replace(m, method=meshes.PULSE)
+    r = dnl_io.run_reference("steps", mp, 30)
+    save("steps_plane_pulse.npz", mass=r["mass"], dt0=r["dt0"], dt=r["dt"], time=r["time"],
+         kinetic=r["kinetic"], fint=np.stack([r[f"fint_{k:06d}"] for k in range(30)]),
+         final_coords=r["final_coords"])
+    r = dnl_io.run_reference("run", m)
+    save("run_plane.npz", increments=r["increments"], time=r["time"],
+         final_coords=r["final_coords"], final_evp=r["final_evp"], final_p=r["final_p"],
+         final_S=r["final_S"], final_v=r["final_v"])
+
+
 def main():
     if not dnl_io.reference_available():
         sys.exit("compiled reference missing: run `make -C oracle ref`")
@@ -69,6 +99,9 @@ def main():
         return
     if sys.argv[1:] == ["laws"]:
         laws()
+        return
+    if sys.argv[1:] == ["plane"]:
+        plane()
         return
     t = dnl_io.reference_tables()
     save("tables.npz", **t)
@@ -104,6 +137,7 @@ def main():
 
     results()
     laws()
+    plane()
 
 
 if __name__ == "__main__":

@@ -1,6 +1,8 @@
 """The oracle (oracle/dnl_oracle.c) against the reference's own outputs (tests/golden, generated by
 tests/golden/make_golden.py from the compiled reference) and against known answers.  CPU only."""
 
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -16,7 +18,7 @@ def _inject(o, g):
 
 def test_tables_match_reference():
     g = golden("tables.npz")
-    for et, nm in ((0, "axi"), (1, "hex")):
+    for et, nm in ((0, "axi"), (1, "hex"), (2, "plane")):
         N, dN = orc.tables(et)
         assert np.array_equal(N.ravel(), g[nm + "_N"])
         assert np.array_equal(dN.ravel(), g[nm + "_dN"])
@@ -24,7 +26,8 @@ def test_tables_match_reference():
 
 
 @pytest.mark.parametrize("name,model", [("forces_axi.npz", lambda: meshes.taylor_axi(3, 4)),
-                                        ("forces_hex.npz", lambda: meshes.taylor_hex(4, 3))])
+                                        ("forces_hex.npz", lambda: meshes.taylor_hex(4, 3)),
+                                        ("forces_plane.npz", lambda: meshes.taylor_plane(3, 4))])
 def test_internal_forces_bit_exact(name, model):
     """One Domain::computeInternalForces on an injected mid-run state: bit for bit."""
     g = golden(name)
@@ -67,6 +70,46 @@ def test_run_c0_bit_exact():
     assert np.array_equal(o.array("coords"), g["final_coords"])
     assert np.array_equal(o.array("evp"), g["final_evp"])
     assert np.array_equal(o.array("S"), g["final_S"])
+
+
+def test_plane_strain_steps_and_run_bit_exact():
+    """ElQua4n2D (ElementPlane: no hoop stretch, no 2 pi R weight, no hoop force): 40 steps with
+    their forces, then the full run to 80 us, bit for bit with the reference."""
+    g = golden("steps_plane.npz")
+    m = meshes.taylor_plane(5, 50)
+    o = Oracle(m)
+    o.prologue()
+    assert np.array_equal(o.array("Mass"), g["mass"])
+    assert o.get("dt") == g["dt0"][0]
+    for k in range(40):
+        o.steps(1)
+        assert np.array_equal(o.array("fint"), g["fint"][k]), k
+        assert o.get("kinetic_current") == g["kinetic"][k]
+    assert np.array_equal(o.array("coords"), g["final_coords"])
+    assert np.array_equal(o.array("S"), g["final_S"])
+    g = golden("run_plane.npz")
+    o = Oracle(m)
+    o.prologue()
+    assert o.steps(10 ** 9) == int(g["increments"][0])
+    assert o.get("time") == g["time"][0]
+    assert np.array_equal(o.array("coords"), g["final_coords"])
+    assert np.array_equal(o.array("evp"), g["final_evp"])
+    assert g["final_evp"].max() > 1.0
+
+
+def test_steps_plane_pulse():
+    """ElQua4n2D with the Pulse time step (plane-strain Hooke matrix, Material.C:276-284)."""
+    g = golden("steps_plane_pulse.npz")
+    o = Oracle(dataclasses.replace(meshes.taylor_plane(5, 50), method=meshes.PULSE))
+    o.prologue()
+    assert abs(o.get("dt") - g["dt0"][0]) <= 1e-14 * g["dt0"][0]
+    for k in range(30):
+        o.steps(1)
+        f, r = o.array("fint"), g["fint"][k]
+        if np.linalg.norm(r) > 0:
+            assert np.linalg.norm(f - r) <= 1e-12 * np.linalg.norm(r), k
+    x = o.array("coords")
+    assert np.max(np.abs(x - g["final_coords"])) <= 1e-12 * np.max(np.abs(g["final_coords"]))
 
 
 def test_steps_hex_pulse():

@@ -37,7 +37,7 @@ SYM = [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]
 
 
 def _ip_array(m, st):
-    ns = 4 if m.etype == meshes.ELQUA4NAX else 6
+    ns = 6 if m.etype == meshes.ELHEX8N3D else 4
     nI = m.E * m.nip
     comps = []
     for name in ("S", "Eps", "EpsPlas"):
@@ -94,7 +94,7 @@ def test_static_entry_matches_handle_path_twice(gpu_lib, etype):
     t_fint = torch.zeros(m.N * m.dim, dtype=torch.float64, device=dev)
     L = gpu_lib.lib()
     L.dnl_internal_forces_static.argtypes = [C.POINTER(StaticArgs), C.c_void_p, C.POINTER(C.c_int)]
-    ns = 4 if etype == meshes.ELQUA4NAX else 6
+    ns = 6 if etype == meshes.ELHEX8N3D else 4
     for call, (x, u) in enumerate(((st["coords"], st["du"]), (coords2, du2))):
         t_x = torch.tensor(np.ascontiguousarray(np.asarray(x).T), dtype=torch.float64, device=dev)
         t_u = torch.tensor(np.ascontiguousarray(np.asarray(u).T), dtype=torch.float64, device=dev)
