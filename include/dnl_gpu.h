@@ -43,6 +43,8 @@ enum dnl_status {
 #define DNL_ELQUA4NAX 0 /* ElQua4nAx: 4-node axisymmetric quad, 2x2 Gauss points */
 #define DNL_ELHEX8N3D 1 /* ElHex8n3D: 8-node hexahedron, 2x2x2 Gauss points */
 #define DNL_ELQUA4N2D 2 /* ElQua4n2D: 4-node plane-strain quad, 2x2 Gauss points (ElementPlane) */
+#define DNL_ELTET4N3D 3 /* ElTet4n3D: 4-node tetrahedron, 1 Gauss point */
+#define DNL_ELTET10N3D 4 /* ElTet10n3D: 10-node tetrahedron, 4 Gauss points (the reference's tables) */
 
 /* time-step methods (Solver::setTimeStepMethod, Solver.C:312-321) */
 #define DNL_COURANT 0
@@ -60,7 +62,7 @@ typedef struct dnl_handle dnl_handle;
 /* Mesh and boundary conditions (Structure::createNode/createElement, attachInitialBC,
  * attachConstantBC).  Node and element order is the reference's Id order. */
 typedef struct {
-  int etype;            /* DNL_ELQUA4NAX, DNL_ELHEX8N3D or DNL_ELQUA4N2D */
+  int etype;            /* DNL_ELQUA4NAX, DNL_ELHEX8N3D, DNL_ELQUA4N2D, DNL_ELTET4N3D, DNL_ELTET10N3D */
   int num_nodes;        /* N */
   int num_elements;     /* E */
   const double *coords; /* N*3, node-major (x, y, z) like Node::coords */

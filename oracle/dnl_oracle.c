@@ -78,8 +78,8 @@ struct dnlo {
   double fmax0;
   long pulse_iter, pulse_total;
   long *n2e_start, *n2e;
-  double Nt[8][8];
-  double dNxi[8][8][3];
+  double Nt[8][10];
+  double dNxi[8][10][3];
   double weight[8];
   int bad_elem;
   int mass_done;
@@ -95,9 +95,56 @@ static const int HX_XI[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
 static const int HX_ETA[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
 static const int HX_ZETA[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
 
+/* ElTet10n3D's tables (ElTet10n3D.C:45-72) as the compiled reference holds them.  At Gauss point p
+ * (0: (a,a,a), 1: (b,a,a), 2: (a,b,a), 3: (a,a,b)) the barycentric coordinate L_p is b and the
+ * others a; the corner shape functions L_i (2 L_i - 1) are +-0.1, the mid-edge ones 4 L_i L_j
+ * (nodes 4..9 on the edges 01 12 02 03 13 23) are (1 + sqrt 5)/10 or (3 - sqrt 5)/10.  The
+ * derivatives are the reference's named constants 3/sqrt5, 1/sqrt5, 4/sqrt5, 1 - 1/sqrt5 (4a) and
+ * 1 + 3/sqrt5 (4b); the last two are unparenthesised macros, so where the reference negates them
+ * the stored values are -1 - 1/sqrt5 and -1 + 3/sqrt5 instead of -4a and -4b. */
+static void tet10_tables(dnlo *h)
+{
+  const double r5 = sqrt(5.0);
+  const int e0[6] = {0, 1, 0, 0, 1, 2}, e1[6] = {1, 2, 2, 3, 3, 3};
+  for (int p = 0; p < 4; p++) {
+    h->weight[p] = 1.0 / 24.0;
+    for (int i = 0; i < 4; i++) h->Nt[p][i] = i == p ? 0.1 : -0.1;
+    for (int m = 0; m < 6; m++)
+      h->Nt[p][4 + m] = (e0[m] == p || e1[m] == p) ? (1.0 + r5) / 10.0 : (3.0 - r5) / 10.0;
+    for (int c = 0; c < 3; c++) {
+      /* d L_0 / d xi_c = -1, d L_i / d xi_c = 1 if c == i - 1 */
+      h->dNxi[p][0][c] = p == 0 ? -(3.0 / r5) : 1.0 / r5;
+      for (int i = 1; i < 4; i++)
+        h->dNxi[p][i][c] = c != i - 1 ? 0.0 : (p == i ? 3.0 / r5 : -(1.0 / r5));
+      for (int m = 0; m < 6; m++) {
+        const int A = e0[m], B = e1[m];
+        const int gA = A == 0 ? -1 : (c == A - 1), gB = c == B - 1;
+        double v;
+        if (!gA && !gB)
+          v = 0.0;
+        else if (gA == -1 && gB) /* 4 (L0 - L_B) */
+          v = p == 0 ? 4.0 / r5 : (p == B ? -(4.0 / r5) : 0.0);
+        else if (gA == -1) /* -4 L_B, as the macro expansion evaluates it */
+          v = p == B ? -1.0 + 3.0 / r5 : -1.0 - 1.0 / r5;
+        else /* 4 L_B or 4 L_A */
+          v = p == (gA ? B : A) ? 1.0 + 3.0 / r5 : 1.0 - 1.0 / r5;
+        h->dNxi[p][4 + m][c] = v;
+      }
+    }
+  }
+}
+
 static void build_tables(dnlo *h)
 {
-  if (h->etype != 1) { /* ElQua4nAx and ElQua4n2D share their tables (ElQua4n2D.C:26-70) */
+  if (h->etype == 3) { /* ElTet4n3D (ElTet4n3D.C:33-57): one point, weight 1/6 */
+    h->weight[0] = 1. / 6.;
+    for (int k = 0; k < 4; k++) {
+      h->Nt[0][k] = 0.25;
+      for (int c = 0; c < 3; c++) h->dNxi[0][k][c] = k == 0 ? -1.0 : (k - 1 == c ? 1.0 : 0.0);
+    }
+  } else if (h->etype == 4) {
+    tet10_tables(h);
+  } else if (h->etype != 1) { /* ElQua4nAx and ElQua4n2D share their tables (ElQua4n2D.C:26-70) */
     const double cN[3] = {(2.0 + sqrt(3.0)) / 6.0, 1.0 / 6.0, (2.0 - sqrt(3.0)) / 6.0};
     const double cD[2] = {(3.0 + sqrt(3.0)) / 12.0, (3.0 - sqrt(3.0)) / 12.0};
     for (int pt = 0; pt < 4; pt++) {
@@ -352,7 +399,7 @@ static int elem_matrices(dnlo *h, long e, int reference)
         }
     } else {
       double J[3][3] = {{0., 0., 0.}, {0., 0., 0.}, {0., 0., 0.}};
-      for (int k = 0; k < 8; k++) {
+      for (int k = 0; k < h->nen; k++) {
         const double *x = h->coords + cn[k] * 3;
         for (int r = 0; r < 3; r++)
           for (int c = 0; c < 3; c++) J[r][c] += h->dNxi[pt][k][c] * x[r];
@@ -367,7 +414,7 @@ static int elem_matrices(dnlo *h, long e, int reference)
       for (int r = 0; r < 3; r++)
         for (int c = 0; c < 3; c++) a[c * 3 + r] = J[r][c];
       if (inv3_lapack(a)) err = DNLO_ERR_SINGULAR;
-      for (int k = 0; k < 8; k++)
+      for (int k = 0; k < h->nen; k++)
         for (int c = 0; c < 3; c++) {
           double acc = 0.;
           for (int l = 0; l < 3; l++)
@@ -411,7 +458,7 @@ static void elem_F(const dnlo *h, long e, int pt, double *F)
       F[8] += v / R;
     }
   } else {
-    for (int k = 0; k < 8; k++) {
+    for (int k = 0; k < h->nen; k++) {
       const double *d = du + cn[k] * 3;
       for (int r = 0; r < 3; r++)
         for (int c = 0; c < 3; c++) F[r * 3 + c] += DN(h, e, pt, k, c) * d[r];
@@ -637,7 +684,7 @@ int dnlo_mass(dnlo *h)
   const long nd = (long)h->dim * h->N;
   for (long i = 0; i < nd; i++) h->Mass[i] = 0.;
   for (long e = 0; e < h->E; e++) {
-    double Me[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double Me[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int pt = 0; pt < h->nip; pt++) {
       double WxdJ = h->weight[pt] * h->detJ[IPX(h, e, pt)];
       if (h->etype == 0) {
@@ -656,20 +703,40 @@ int dnlo_mass(dnlo *h)
   return 0;
 }
 
+/* Vec3D::distance (Vec3D.h:380-430): the norm of (b - a) */
+static double dist3(const double *a, const double *b)
+{
+  const double x = b[0] - a[0], y = b[1] - a[1], z = b[2] - a[2];
+  return sqrt(x * x + y * y + z * z);
+}
+#define MIN2(i, j) ((i) < (j) ? (i) : (j)) /* Math.h:62 */
+
 /* Domain::computeCourantTimeStep (Domain.C:1613-1646) with ElQua4nAx::getLength
- * (ElQua4nAx.C:131-143) and Element::getSoundSpeed (Element.C:607-621). */
+ * (ElQua4nAx.C:131-143, also ElQua4n2D's), ElTet4n3D::getLength (ElTet4n3D.C:151-166, also
+ * ElTet10n3D's) and Element::getSoundSpeed (Element.C:607-621). */
 static double elem_courant(const dnlo *h, long e)
 {
-  const long *cn = h->conn + e * 4;
+  const long *cn = h->conn + e * h->nen;
   const double *x0 = h->coords + cn[0] * 3, *x1 = h->coords + cn[1] * 3;
   const double *x2 = h->coords + cn[2] * 3, *x3 = h->coords + cn[3] * 3;
-  const double x31 = x2[0] - x0[0], x24 = x1[0] - x3[0];
-  const double y42 = x3[1] - x1[1], y31 = x2[1] - x0[1];
-  const double len = ((x31 * y42 + x24 * y31) / sqrt(2. * ((x24) * (x24) + (y42) * (y42) + (x31) * (x31) + (y31) * (y31))));
+  double len;
+  if (h->dim == 2) {
+    const double x31 = x2[0] - x0[0], x24 = x1[0] - x3[0];
+    const double y42 = x3[1] - x1[1], y31 = x2[1] - x0[1];
+    len = ((x31 * y42 + x24 * y31) / sqrt(2. * ((x24) * (x24) + (y42) * (y42) + (x31) * (x31) + (y31) * (y31))));
+  } else {
+    const double l1 = dist3(x0, x1), l2 = dist3(x0, x2), l3 = dist3(x1, x2);
+    const double l4 = dist3(x0, x3), l5 = dist3(x1, x3), l6 = dist3(x2, x3);
+    len = MIN2(l1, l2);
+    len = MIN2(len, l3);
+    len = MIN2(len, l4);
+    len = MIN2(len, l5);
+    len = MIN2(len, l6);
+  }
   const double *ro = h->ro[h->cur];
   double r = 0.;
-  for (int i = 0; i < 4; i++) r += ro[cn[i]];
-  r /= 4;
+  for (int i = 0; i < h->nen; i++) r += ro[cn[i]];
+  r /= h->nen;
   const double E = h->mE[MATOF(h, e)], Nu = h->mNu[MATOF(h, e)];
   const double Cs = sqrt((E * (1 - Nu)) / (r * (1 + Nu) * (1 - 2 * Nu)));
   return len / (Cs);
@@ -697,7 +764,7 @@ static void elem_stiffness(const dnlo *h, long e, double *Ke)
   double C[6][6];
   memset(C, 0, sizeof C);
   const int axi = h->etype == 0;
-  if (h->etype != 1) {
+  if (h->dim == 2) {
     C[0][0] = 1; C[1][1] = 1;
     C[1][0] = Nu / (1. - Nu); C[0][1] = Nu / (1. - Nu);
     if (axi) {
@@ -722,12 +789,12 @@ static void elem_stiffness(const dnlo *h, long e, double *Ke)
       for (int j = 0; j < 6; j++) C[i][j] *= f;
   }
   for (int k = 0; k < nd * nd; k++) Ke[k] = 0;
-  double CB[6][24];
+  double CB[6][30];
   for (int pt = 0; pt < h->nip; pt++) {
     const long ix = IPX(h, e, pt);
     double WxdJ = h->weight[pt] * h->detJ[ix];
     double R = 0.;
-    if (h->etype != 1) {
+    if (h->dim == 2) {
       if (axi) {
         R = elem_radius(h, e, pt);
         WxdJ *= 2 * DNL_PI * R;
@@ -762,7 +829,7 @@ static void elem_stiffness(const dnlo *h, long e, double *Ke)
           Ke[I * nd + J + 1] += CB[3][J + 1] * Ni / R * WxdJ;
         }
     } else {
-      for (int i = 0; i < 8; i++) {
+      for (int i = 0; i < nen; i++) {
         const int I = 3 * i;
         const double d0 = DN(h, e, pt, i, 0), d1 = DN(h, e, pt, i, 1), d2 = DN(h, e, pt, i, 2);
         for (int r = 0; r < 6; r++) {
@@ -771,8 +838,8 @@ static void elem_stiffness(const dnlo *h, long e, double *Ke)
           CB[r][I + 2] = (C[r][2] * d2 + C[r][4] * d1 + C[r][5] * d0);
         }
       }
-      for (int i = 0; i < 8; i++)
-        for (int j = 0; j < 8; j++) {
+      for (int i = 0; i < nen; i++)
+        for (int j = 0; j < nen; j++) {
           const int I = 3 * i, J = 3 * j;
           const double d0 = DN(h, e, pt, i, 0), d1 = DN(h, e, pt, i, 1), d2 = DN(h, e, pt, i, 2);
           for (int c = 0; c < 3; c++) {
@@ -807,7 +874,7 @@ int dnlo_max_frequency(dnlo *h, double *out)
     for (long e = 0; e < h->E; e++) {
       const double *Ke = h->Ke + e * (long)nd * nd;
       const long *cn = h->conn + e * h->nen;
-      double loc[24];
+      double loc[30];
       for (int I = 0; I < h->nen; I++)
         for (int j = 0; j < h->dim; j++) loc[I * h->dim + j] = 0. + EV0[cn[I] * h->dim + j];
       double *y = h->kx + e * nd; /* dgemv: y = sum_j Ke(:,j) loc_j, skipping loc_j == 0 */
@@ -1004,11 +1071,12 @@ dnlo *dnlo_create(int etype, long N, long E, const double *coords, const long *c
                   const double *bc_val, const long *bc_start, const long *bc_nodes,
                   const double *solver)
 {
-  if ((etype != 0 && etype != 1 && etype != 2) || N <= 0 || E <= 0) return NULL;
+  if (etype < 0 || etype > 4 || N <= 0 || E <= 0) return NULL;
   dnlo *h = (dnlo *)calloc(1, sizeof(dnlo));
   h->etype = etype;
-  h->dim = etype == 1 ? 3 : 2;
-  h->nen = h->nip = etype == 1 ? 8 : 4;
+  h->dim = (etype == 0 || etype == 2) ? 2 : 3;
+  h->nen = etype == 1 ? 8 : (etype == 4 ? 10 : 4);
+  h->nip = etype == 1 ? 8 : (etype == 3 ? 1 : 4);
   h->N = N;
   h->E = E;
   h->conn = (long *)malloc(sizeof(long) * E * h->nen);
@@ -1278,8 +1346,9 @@ int dnlo_tables(int etype, double *N, double *dN)
   dnlo t;
   memset(&t, 0, sizeof t);
   t.etype = etype;
-  t.dim = etype == 1 ? 3 : 2;
-  t.nen = t.nip = etype == 1 ? 8 : 4;
+  t.dim = (etype == 0 || etype == 2) ? 2 : 3;
+  t.nen = etype == 1 ? 8 : (etype == 4 ? 10 : 4);
+  t.nip = etype == 1 ? 8 : (etype == 3 ? 1 : 4);
   build_tables(&t);
   for (int pt = 0; pt < t.nip; pt++)
     for (int k = 0; k < t.nen; k++) {

@@ -63,10 +63,11 @@ def lib():
 
 def tables(etype: int):
     """(N, dN/dxi) tables the oracle builds: (nip, nen) and (nip, nen, dim)."""
-    nen = 8 if etype == 1 else 4
-    dim = 3 if etype == 1 else 2
-    N = np.zeros((nen, nen))
-    dN = np.zeros((nen, nen, dim))
+    nen = {1: 8, 4: 10}.get(etype, 4)
+    nip = {1: 8, 3: 1}.get(etype, 4)
+    dim = 2 if etype in (0, 2) else 3
+    N = np.zeros((nip, nen))
+    dN = np.zeros((nip, nen, dim))
     lib().dnlo_tables(etype, _dp(N), _dp(dN))
     return N, dN
 

@@ -15,7 +15,8 @@
 //   ref_harness forces <model> <state> <out>  inject nodal + integration-point state, then one
 //                                             computeInternalMatrices + computeInternalForces
 //   ref_harness bench  <model> <out> <K>      K steps of the loop, wall time only
-//   ref_harness tables <out>                  element tables of ElQua4nAx, ElHex8n3D, ElQua4n2D
+//   ref_harness tables <out>                  element tables of ElQua4nAx, ElHex8n3D, ElQua4n2D,
+//                                             ElTet4n3D, ElTet10n3D
 //
 // Run it with OMP_NUM_THREADS=1 for golden data: strategy 0 of Domain::computeInternalForces sums
 // element forces under `omp critical`, so with several threads the summation order (and the last
@@ -50,6 +51,8 @@
 #include <Element.h>
 #include <ElQua4nAx.h>
 #include <ElQua4n2D.h>
+#include <ElTet4n3D.h>
+#include <ElTet10n3D.h>
 #include <ElHex8n3D.h>
 #include <Material.h>
 #include <IsoHardElastoplastic.h>
@@ -149,7 +152,7 @@ struct MatLaw
 
 struct Model
 {
-  long etype; // 0 ElQua4nAx, 1 ElHex8n3D, 2 ElQua4n2D
+  long etype; // 0 ElQua4nAx, 1 ElHex8n3D, 2 ElQua4n2D, 3 ElTet4n3D, 4 ElTet10n3D
   long N, E, nen;
   std::vector<double> coords; // N*3
   std::vector<long> conn;     // E*nen, 0-based
@@ -179,7 +182,7 @@ static Model readModel(const char *path)
   m.etype = r.i64();
   m.N = r.i64();
   m.E = r.i64();
-  m.nen = (m.etype == 1 ? 8 : 4);
+  m.nen = (m.etype == 1 ? 8 : (m.etype == 4 ? 10 : 4));
   m.coords.resize(m.N * 3);
   r.f64s(m.coords.data(), m.coords.size());
   m.conn.resize(m.E * m.nen);
@@ -256,6 +259,8 @@ static Built build(const Model &m)
 
   Element *proto = (m.etype == 0   ? (Element *)new ElQua4nAx(0)
                     : m.etype == 2 ? (Element *)new ElQua4n2D(0)
+                    : m.etype == 3 ? (Element *)new ElTet4n3D(0)
+                    : m.etype == 4 ? (Element *)new ElTet10n3D(0)
                                    : (Element *)new ElHex8n3D(0));
   st->setDefaultElement(proto);
   ElementSet *els = new ElementSet;
@@ -264,9 +269,13 @@ static Built build(const Model &m)
     const long *c = &m.conn[e * m.nen];
     if (m.nen == 4)
       st->createElement(e + 1, (int)c[0] + 1, (int)c[1] + 1, (int)c[2] + 1, (int)c[3] + 1);
-    else
+    else if (m.nen == 8)
       st->createElement(e + 1, (int)c[0] + 1, (int)c[1] + 1, (int)c[2] + 1, (int)c[3] + 1,
                         (int)c[4] + 1, (int)c[5] + 1, (int)c[6] + 1, (int)c[7] + 1);
+    else
+      st->createElement(e + 1, (int)c[0] + 1, (int)c[1] + 1, (int)c[2] + 1, (int)c[3] + 1,
+                        (int)c[4] + 1, (int)c[5] + 1, (int)c[6] + 1, (int)c[7] + 1,
+                        (int)c[8] + 1, (int)c[9] + 1);
     els->add(e + 1);
   }
 
@@ -629,15 +638,17 @@ static int cmdForces(const Model &m, const char *statePath, const std::string &o
   return 0;
 }
 
-// Element tables of ElQua4nAx / ElHex8n3D / ElQua4n2D (ElQua4nAx.C:31-101, ElHex8n3D.C:26-161,
-// ElQua4n2D.C:26-70): per Gauss point its weight, N_k and dN_k/dxi_c.
+// Element tables of ElQua4nAx / ElHex8n3D / ElQua4n2D / ElTet4n3D / ElTet10n3D (ElQua4nAx.C:31-101,
+// ElHex8n3D.C:26-161, ElQua4n2D.C:26-70, ElTet4n3D.C:33-57, ElTet10n3D.C:31-77): per Gauss point
+// its weight, N_k and dN_k/dxi_c, as the compiled tables hold them.
 static int cmdTables(const std::string &out)
 {
   Writer w(out);
-  const ElementData *tabs[3] = {&ElQua4nAx::elementData, &ElHex8n3D::elementData,
-                                &ElQua4n2D::elementData};
-  const char *names[3] = {"axi", "hex", "plane"};
-  for (int t = 0; t < 3; t++)
+  const ElementData *tabs[5] = {&ElQua4nAx::elementData, &ElHex8n3D::elementData,
+                                &ElQua4n2D::elementData, &ElTet4n3D::elementData,
+                                &ElTet10n3D::elementData};
+  const char *names[5] = {"axi", "hex", "plane", "tet4", "tet10"};
+  for (int t = 0; t < 5; t++)
   {
     const ElementData *d = tabs[t];
     std::vector<double> wgt, N, dN;

@@ -116,7 +116,7 @@ int enqueue_batch_step(dnl_batch *b, long long incAfter, bool last)
   if (incAfter % b->freq == 0) {
     ElemArgs c = elem_args_of(h);
     prof_begin(h, h->stream);
-    r = launch_courant_batch(c, b->elemInst, b->tms, h->stream);
+    r = launch_courant_batch(h->etype, c, b->elemInst, b->tms, h->stream);
     prof_end(h, DNL_PROF_COURANT, h->stream);
     if (r) return r;
   }
@@ -145,9 +145,10 @@ int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material 
   if (!out || count <= 0 || !meshes || !mats || !sps) return DNL_ERR_ARG;
   *out = nullptr;
   const int etype = meshes[0].etype;
-  const int nen = etype == DNL_ELHEX8N3D ? 8 : 4;
-  // plain batched stepping needs the axisymmetric Courant step of every instance; sensitivity
-  // runs take a step schedule and accept any element type and time-step method
+  if (!etype_valid(etype)) return DNL_ERR_ARG;
+  const int nen = etype_nen(etype);
+  // plain batched stepping needs the Courant step of every instance (ElHex8n3D has no Courant
+  // length); sensitivity runs take a step schedule and accept any time-step method
   bool canStep = etype != DNL_ELHEX8N3D;
   for (int i = 0; i < count; i++) {
     if (meshes[i].etype != etype) return DNL_ERR_ARG;
@@ -236,7 +237,7 @@ int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material 
   b->hprm.resize(count);
   std::vector<DevTime> ht(count);
   for (int i = 0; i < count; i++) {
-    hm[i] = make_material(mats[i]);
+    hm[i] = make_material(mats[i], nen);
     const double rb = sps[i].rho_b;
     InstParams &p = b->hprm[i];
     p.alphaM = (2.0 * rb - 1.0) / (1.0 + rb);
@@ -299,7 +300,7 @@ int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material 
       const double val = pow(1e-10, mats[i].n);
       for (size_t q = (size_t)elemOff[i] * h->nip; q < (size_t)elemOff[i + 1] * h->nip; q++) pn[q] = val;
     }
-    const int ns = etype == DNL_ELHEX8N3D ? 6 : 4;
+    const int ns = etype_ns(etype);
     BKF(cudaMemcpy(h->ip + (size_t)(3 * ns + 2) * nIP, pn.data(), sizeof(double) * nIP, cudaMemcpyHostToDevice));
   }
   BKF(cudaDeviceSynchronize());
@@ -336,7 +337,7 @@ int dnl_batch_prologue(dnl_batch *b)
   // computeInternalForces with the initial (zero) Current field, then computeTimeStep(True)
   ElemArgs a = elem_args_of(h);
   if ((r = launch_elem_batch(h->etype, b->block, a, b->elemInst, b->mats, b->tms, h->stream))) return r;
-  if ((r = launch_courant_batch(a, b->elemInst, b->tms, h->stream))) return r;
+  if ((r = launch_courant_batch(h->etype, a, b->elemInst, b->tms, h->stream))) return r;
   if ((r = launch_dt_batch(h, b->tms, b->prm, b->count, BT_FORCE))) return r;
   std::vector<DevTime> t;
   if ((r = read_tms(b, t))) return r;
@@ -457,8 +458,7 @@ int dnl_batch_reset(dnl_batch *b)
   for (int i = 0; i < b->ngraphs; i++) cudaGraphExecDestroy(b->graphs[i].exec);
   b->ngraphs = 0;
   const long N = h->N, nIP = h->nIP;
-  const int ncomp = h->etype == DNL_ELHEX8N3D ? IpLayout<DNL_ELHEX8N3D>::NCOMP : IpLayout<DNL_ELQUA4NAX>::NCOMP;
-  const int ns = h->etype == DNL_ELHEX8N3D ? 6 : 4;
+  const int ns = etype_ns(h->etype), ncomp = 3 * ns + 3;  // IpLayout::NCOMP
   BK(cudaMemcpyAsync(h->x[0], h->x0, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
   BK(cudaMemsetAsync(h->fieldMem, 0, sizeof(double) * 24 * N, s));
   BK(cudaMemsetAsync(h->ip, 0, sizeof(double) * ncomp * nIP, s));

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 
 #include "dnl_gpu.h"
@@ -37,6 +38,74 @@ template <> struct Elem<DNL_ELQUA4N2D> {  // plane strain: the quad of ElQua4nAx
   static constexpr int DIM = 2, NEN = 4, NIP = 4;
   static constexpr int NS = 4;
 };
+template <> struct Elem<DNL_ELTET4N3D> {
+  static constexpr int DIM = 3, NEN = 4, NIP = 1;
+  static constexpr int NS = 6;
+};
+template <> struct Elem<DNL_ELTET10N3D> {
+  static constexpr int DIM = 3, NEN = 10, NIP = 4;
+  static constexpr int NS = 6;
+};
+// the same by run-time element type
+__host__ __device__ constexpr bool etype_valid(int et) { return et >= DNL_ELQUA4NAX && et <= DNL_ELTET10N3D; }
+__host__ __device__ constexpr int etype_dim(int et) { return et == DNL_ELQUA4NAX || et == DNL_ELQUA4N2D ? 2 : 3; }
+__host__ __device__ constexpr int etype_nen(int et)
+{
+  return et == DNL_ELHEX8N3D ? 8 : (et == DNL_ELTET10N3D ? 10 : 4);
+}
+__host__ __device__ constexpr int etype_nip(int et)
+{
+  return et == DNL_ELHEX8N3D ? 8 : (et == DNL_ELTET4N3D ? 1 : 4);
+}
+__host__ __device__ constexpr int etype_ns(int et) { return etype_dim(et) == 2 ? 4 : 6; }
+// element types with the forward-mode sensitivity path (tape and tangent kernels)
+__host__ __device__ constexpr bool etype_has_sens(int et) { return et <= DNL_ELQUA4N2D; }
+// element types whose time-step length is the quad's Courant length (else the tetrahedra's
+// shortest edge; ElHex8n3D has none)
+__host__ __device__ constexpr bool etype_quad(int et) { return et == DNL_ELQUA4NAX || et == DNL_ELQUA4N2D; }
+
+// The reference's ElTet10n3D tables (ElTet10n3D.C:45-72) as they evaluate: at Gauss point p the
+// barycentric coordinate L_p is beta and the others alpha (p = 0: L0 = 1 - xi - eta - zeta), the
+// shape functions are L_i (2 L_i - 1) at the corners and 4 L_i L_j at the mid-edge nodes 4..9 =
+// (0,1) (1,2) (0,2) (0,3) (1,3) (2,3), and each value is one of the reference's named constants.
+// Two of those constants are unparenthesised macros (1.0 - 1.0 / sqrt(5.0) and
+// 1.0 + 3.0 / sqrt(5.0)); where the table negates them the expansion gives -1.0 - 1.0 / sqrt(5.0)
+// and -1.0 + 3.0 / sqrt(5.0), so the derivatives -4 alpha and -4 beta are stored as those values.
+inline void tet10_tables(double N[4][10], double D[4][10][3])
+{
+  const double r5 = sqrt(5.0);
+  const double a4 = 1.0 - 1.0 / r5, b4 = 1.0 + 3.0 / r5;  // 4 alpha, 4 beta
+  const double a4neg = -1.0 - 1.0 / r5, b4neg = -1.0 + 3.0 / r5;
+  const double bm = 3.0 / r5, am = 1.0 / r5, ba = 4.0 / r5;  // 4 beta - 1, 1 - 4 alpha, 4 (beta - alpha)
+  const int ea[6] = {0, 1, 0, 0, 1, 2}, eb[6] = {1, 2, 2, 3, 3, 3};
+  for (int p = 0; p < 4; p++) {
+    for (int i = 0; i < 4; i++) N[p][i] = i == p ? 0.1 : -0.1;
+    for (int m = 0; m < 6; m++)
+      N[p][4 + m] = (ea[m] == p || eb[m] == p) ? (1.0 + r5) / 10.0 : (3.0 - r5) / 10.0;
+    for (int c = 0; c < 3; c++) {
+      // corners: dN_0/dxi_c = 1 - 4 L0, dN_i/dxi_c = (4 L_i - 1) [c == i - 1]
+      D[p][0][c] = p == 0 ? -bm : am;
+      for (int i = 1; i < 4; i++) D[p][i][c] = c == i - 1 ? (p == i ? bm : -am) : 0.0;
+      // mid-edge (a, b): 4 (L_b dL_a/dxi_c + L_a dL_b/dxi_c), dL_0/dxi_c = -1, dL_i/dxi_c = [c == i - 1]
+      for (int m = 0; m < 6; m++) {
+        const int A = ea[m], B = eb[m];
+        const int dA = A == 0 ? -1 : (c == A - 1), dB = c == B - 1;
+        double v;
+        if (dA == 0 && dB == 0) {
+          v = 0.0;
+        } else if (dA == -1 && dB == 1) {  // 4 (L0 - L_b)
+          v = p == 0 ? ba : (p == B ? -ba : 0.0);
+        } else if (dA == -1) {  // -4 L_b
+          v = p == B ? b4neg : a4neg;
+        } else {  // 4 L_b (dA) or 4 L_a (dB)
+          const int other = dA ? B : A;
+          v = p == other ? b4 : a4;
+        }
+        D[p][4 + m][c] = v;
+      }
+    }
+  }
+}
 
 // integration-point state, component-major: ip[comp * nIP + (e * NIP + pt)]
 //   S[NS] | Eps[NS] | EpsPlas[NS] | p | evp | evpn (= evp^n, cached yield term)
@@ -123,7 +192,7 @@ struct Material {
 
 // Material constants from the ABI description, in the reference's expressions.
 #include <math.h>
-inline Material make_material(const dnl_material &mt)
+inline Material make_material(const dnl_material &mt, int nen = 4)
 {
   Material m;
   m.young = mt.young;
@@ -139,10 +208,10 @@ inline Material make_material(const dnl_material &mt)
   m.nB = m.n * m.B;
   m.dfun0 = kSqrt32 * 2.0 * G;
   m.rG3 = 1.0 / m.G3;
-  // ElQua4nAx::getLength's sound speed uses the mean of the four nodal densities
+  // Element::getSoundSpeed uses the mean of the element's nodal densities
   double ro = 0.;
-  for (int i = 0; i < 4; i++) ro += m.rho;
-  ro /= 4;
+  for (int i = 0; i < nen; i++) ro += m.rho;
+  ro /= nen;
   const double Nu = m.nu;
   m.Cs = sqrt((m.young * (1 - Nu)) / (ro * (1 + Nu) * (1 - 2 * Nu)));
   m.hard.law = DNL_HARD_POWER;
@@ -310,8 +379,9 @@ struct dnl_handle {
   void *sens;
 };
 
-// CALL instantiated for the handle's element type, as ET (CALL in parentheses when it has commas)
-#define DNL_BY_ETYPE(etype, CALL)                    \
+// CALL instantiated for the handle's element type, as ET (CALL in parentheses when it has commas):
+// DNL_BY_ETYPE over every element type, DNL_BY_ETYPE_SENS over those with the sensitivity path
+#define DNL_BY_ETYPE_SENS(etype, CALL)               \
   do {                                               \
     if ((etype) == DNL_ELQUA4NAX) {                  \
       constexpr int ET = DNL_ELQUA4NAX;              \
@@ -322,6 +392,18 @@ struct dnl_handle {
     } else {                                         \
       constexpr int ET = DNL_ELHEX8N3D;              \
       CALL;                                          \
+    }                                                \
+  } while (0)
+#define DNL_BY_ETYPE(etype, CALL)                    \
+  do {                                               \
+    if ((etype) == DNL_ELTET4N3D) {                  \
+      constexpr int ET = DNL_ELTET4N3D;              \
+      CALL;                                          \
+    } else if ((etype) == DNL_ELTET10N3D) {          \
+      constexpr int ET = DNL_ELTET10N3D;             \
+      CALL;                                          \
+    } else {                                         \
+      DNL_BY_ETYPE_SENS(etype, CALL);                \
     }                                                \
   } while (0)
 
@@ -359,7 +441,8 @@ int launch_elem_batch(int etype, int block, const ElemArgs &a, const int *elemIn
                       const Material *mats, DevTime *tms, cudaStream_t s);
 int launch_mass_batch(int etype, const ElemArgs &a, double *me, const int *elemInst,
                       const Material *mats, cudaStream_t s);
-int launch_courant_batch(const ElemArgs &a, const int *elemInst, DevTime *tms, cudaStream_t s);
+int launch_courant_batch(int etype, const ElemArgs &a, const int *elemInst, DevTime *tms,
+                         cudaStream_t s);
 ElemArgs elem_args_of(dnl_handle *h);
 int launch_node_batch(dnl_handle *h, const int *nodeInst, const InstParams *prm, DevTime *tms);
 int launch_dt_batch(dnl_handle *h, DevTime *tms, const InstParams *prm, int count, int mode);

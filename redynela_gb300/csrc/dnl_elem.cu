@@ -7,12 +7,15 @@
 //              (Tensor2.C:1154-1259), the J2 radial return (Element.C:245-345), the element-mean
 //              pressure and RFI rotation (Element.C:351-401) and B^T sigma (Element.C:164-214).
 // k_mass<ET>   Element::computeMassMatrix (Element.C:411-454).
-// k_courant    ElQua4nAx::getLength (ElQua4nAx.C:131-143) min-reduced (Domain.C:1613-1646).
+// k_courant    ElQua4nAx::getLength (ElQua4nAx.C:131-143) or the tetrahedra's shortest edge
+//              (ElTet4n3D.C:151-166) over Element::getSoundSpeed, min-reduced (Domain.C:1613-1646).
 //
 // Threading: one thread per integration point; the NIP threads of an element are adjacent lanes
 // of one warp (32 % NIP == 0), so the element-mean pressure and the force sum over integration
 // points are warp-local (shuffles and a per-warp shared-memory transpose), and the
 // integration-point state, stored component-major, is read and written with coalesced accesses.
+// Where an element has more nodes than integration points (the tetrahedra), lane pt assembles
+// nodes pt, pt + NIP, ...
 //
 // Rounding: GB300 executes FP64 at a small fraction of its other rates, so the kernels are written
 // to minimise FP64 instructions with explicit fused multiply-adds (this file is compiled with
@@ -36,10 +39,12 @@ namespace dnl {
 #define RSUB __dsub_rn
 
 // Shape-function values at the Gauss points, formed by the same constant expressions as
-// ElQua4nAx.C:43-67 and ElHex8n3D.C:73-104 (e.g. (2.0 + sqrt(3.0)) / 6.0).
+// ElQua4nAx.C:43-67 and ElHex8n3D.C:73-104 (e.g. (2.0 + sqrt(3.0)) / 6.0); the 10-node
+// tetrahedron's full tables (tet10_tables).
 struct ShapeConst {
   double axN[3], axD[2];  // axi: N by number of sign disagreements, dN/dxi by the other axis
   double hxN[4], hxD[3];  // hex: likewise over three axes
+  double t10N[4][10], t10D[4][10][3];
 };
 __constant__ ShapeConst c_shape;
 
@@ -58,6 +63,7 @@ void set_shape_tables()
   s.hxD[0] = (2.0 + sqrt(3.0)) / 12.0;
   s.hxD[1] = 1.0 / 12.0;
   s.hxD[2] = (2.0 - sqrt(3.0)) / 12.0;
+  tet10_tables(s.t10N, s.t10D);
   cudaMemcpyToSymbol(c_shape, &s, sizeof s);
 }
 
@@ -111,6 +117,29 @@ template <> struct Shape<DNL_ELHEX8N3D> {
     return s ? v : flip_sign(v);
   }
 };
+
+// ElTet4n3D (ElTet4n3D.C:33-57): one point, N = 1/4, dN/dxi of the barycentric coordinates
+template <> struct Shape<DNL_ELTET4N3D> {
+  static constexpr double kWeight = 1. / 6.;
+  __device__ __forceinline__ static double N(int, int) { return 0.25; }
+  __device__ __forceinline__ static double dN(int, int k, int c)
+  {
+    return k == 0 ? -1.0 : (k - 1 == c ? 1.0 : 0.0);
+  }
+};
+template <> struct Shape<DNL_ELTET10N3D> {
+  static constexpr double kWeight = 1.0 / 24.0;
+  __device__ __forceinline__ static double N(int pt, int k) { return c_shape.t10N[pt][k]; }
+  __device__ __forceinline__ static double dN(int pt, int k, int c) { return c_shape.t10D[pt][k][c]; }
+};
+// integration weight x detJ (Element.C:183); the quads' and the hexahedron's weight is 1
+template <int ET> __device__ __forceinline__ double weighted(double detJ)
+{
+  if constexpr (ET == DNL_ELTET4N3D || ET == DNL_ELTET10N3D)
+    return RMUL(Shape<ET>::kWeight, detJ);
+  else
+    return detJ;
+}
 
 __device__ __forceinline__ void record_error(DevTime *tm, int code, int e)
 {
@@ -268,8 +297,8 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
   using SH = Shape<ET>;
   using TL = TapeLayout<ET>;
   constexpr int NIP = T::NIP, NEN = T::NEN, DIM = T::DIM, NS = T::NS;
-  constexpr bool AXI = ET == DNL_ELQUA4NAX;    // radius, hoop strain and hoop force
-  constexpr bool TWO_D = ET != DNL_ELHEX8N3D;  // the 2 + 1 block structure of F, C, R, S
+  constexpr bool AXI = ET == DNL_ELQUA4NAX;  // radius, hoop strain and hoop force
+  constexpr bool TWO_D = DIM == 2;           // the 2 + 1 block structure of F, C, R, S
   const long nIP = (long)a.E * NIP;
   const long ipx = (long)e * NIP + pt;
   auto tape = [&](int slot, double v) {
@@ -732,7 +761,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
   }
 
   // ---- forces: c_k = dN_k . Sig . W with dN = dN/dxi J^-1, i.e. M = J^-1 Sig W (Element.C:179-212)
-  double W = detJ;
+  double W = weighted<ET>(detJ);
   double hoop = 0.;
   if (AXI) {
     W = W * (kDeuxPi * Rad);
@@ -764,13 +793,30 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     }
   __syncwarp();
   if (valid) {
-    // lane pt assembles node pt of its element (NEN == NIP): Fe = - sum over Gauss points
+    // lane pt assembles node pt of its element (and pt + NIP, ... when NEN > NIP):
+    // Fe = - sum over Gauss points
+    if constexpr (NEN == NIP) {
 #pragma unroll
-    for (int i = 0; i < DIM; i++) {
-      double s = 0.0;
+      for (int i = 0; i < DIM; i++) {
+        double s = 0.0;
 #pragma unroll
-      for (int q = 0; q < NIP; q++) s -= red[q * (NEN * DIM) + pt * DIM + i];
-      a.fe[(long)i * a.E * NEN + (long)e * NEN + pt] = s;
+        for (int q = 0; q < NIP; q++) s -= red[q * (NEN * DIM) + pt * DIM + i];
+        a.fe[(long)i * a.E * NEN + (long)e * NEN + pt] = s;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < (NEN + NIP - 1) / NIP; j++) {
+        const int k = pt + j * NIP;
+        if (k < NEN) {
+#pragma unroll
+          for (int i = 0; i < DIM; i++) {
+            double s = 0.0;
+#pragma unroll
+            for (int q = 0; q < NIP; q++) s -= red[q * (NEN * DIM) + k * DIM + i];
+            a.fe[(long)i * a.E * NEN + (long)e * NEN + k] = s;
+          }
+        }
+      }
     }
   }
 }
@@ -822,7 +868,8 @@ __global__ void __launch_bounds__(BLOCK) k_elem_batch(ElemArgs a, const int *ele
 
 // ----------------------------------------------------------------------------- mass kernel
 // Element::computeMassMatrix with the reference's rounding: M_k = sum_pt (rho N_k) W,
-// W = detJ (2 pi R).  Writes me[e*NEN + k]; Domain::computeMassMatrix's assembly is the gather.
+// W = weight detJ (2 pi R).  Writes me[e*NEN + k]; Domain::computeMassMatrix's assembly is the
+// gather.
 template <int ET>
 __global__ void __launch_bounds__(128) k_mass(ElemArgs a, double *me, const int *elemInst,
                                               const Material *mats)
@@ -831,7 +878,7 @@ __global__ void __launch_bounds__(128) k_mass(ElemArgs a, double *me, const int 
   using SH = Shape<ET>;
   constexpr int NIP = T::NIP, NEN = T::NEN, DIM = T::DIM;
   constexpr bool AXI = ET == DNL_ELQUA4NAX;
-  constexpr bool TWO_D = ET != DNL_ELHEX8N3D;
+  constexpr bool TWO_D = DIM == 2;
   constexpr int EPW = 32 / NIP;
   __shared__ double red[128 / 32][EPW][NIP][NEN];
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -868,37 +915,72 @@ __global__ void __launch_bounds__(128) k_mass(ElemArgs a, double *me, const int 
     detJ = RSUB(detJ, RMUL(RMUL(J[0][0], J[2][1]), J[1][2]));
     detJ = RSUB(detJ, RMUL(RMUL(J[1][0], J[0][1]), J[2][2]));
   }
-  double W = detJ;  // weight 1
+  double W = weighted<ET>(detJ);
   if (AXI) W = RMUL(W, RMUL(RMUL(2., kPi), Rad));
   const double rho = elemInst ? mats[elemInst[e]].rho : a.mat.rho;
 #pragma unroll
   for (int k = 0; k < NEN; k++) red[wib][slot][pt][k] = RMUL(RMUL(rho, SH::N(pt, k)), W);
   __syncwarp();
   if (valid) {
-    double s = 0.;
 #pragma unroll
-    for (int q = 0; q < NIP; q++) s = RADD(s, red[wib][slot][q][pt]);
-    me[(long)e * NEN + pt] = s;
+    for (int j = 0; j < (NEN + NIP - 1) / NIP; j++) {
+      const int k = pt + j * NIP;
+      if (k < NEN) {
+        double s = 0.;
+#pragma unroll
+        for (int q = 0; q < NIP; q++) s = RADD(s, red[wib][slot][q][k]);
+        me[(long)e * NEN + k] = s;
+      }
+    }
   }
   (void)lane;
 }
 
 // ----------------------------------------------------------------------------- Courant
-// ElQua4nAx::getLength with the reference's rounding; min over elements via an unsigned atomicMin
-// on the bit pattern (positive doubles order like their bits).  A non-positive or NaN length is an
-// error: the reference would turn it into a negative or NaN time step.
+// The element's characteristic length with the reference's rounding: ElQua4nAx::getLength /
+// ElQua4n2D::getLength (ElQua4nAx.C:131-143, ElQua4n2D.C:130-143) for the quads, else the
+// tetrahedra's shortest corner edge (ElTet4n3D.C:151-166, ElTet10n3D.C:140-155; Vec3D::distance,
+// Vec3D.h:380-430, and the Min chain of Math.h:62).
+template <bool QUAD>
+__device__ __forceinline__ double elem_length(const ElemArgs &a, int e)
+{
+  const int n0 = a.conn[e], n1 = a.conn[a.E + e], n2 = a.conn[2L * a.E + e], n3 = a.conn[3L * a.E + e];
+  if constexpr (QUAD) {
+    const double x31 = RSUB(a.x[0][n2], a.x[0][n0]), x24 = RSUB(a.x[0][n1], a.x[0][n3]);
+    const double y42 = RSUB(a.x[1][n3], a.x[1][n1]), y31 = RSUB(a.x[1][n2], a.x[1][n0]);
+    const double num = RADD(RMUL(x31, y42), RMUL(x24, y31));
+    const double sq = RADD(RADD(RADD(RMUL(x24, x24), RMUL(y42, y42)), RMUL(x31, x31)), RMUL(y31, y31));
+    return num / sqrt(RMUL(2., sq));
+  } else {
+    const int n[4] = {n0, n1, n2, n3};
+    const int ea[6] = {0, 0, 1, 0, 1, 2}, eb[6] = {1, 2, 2, 3, 3, 3};
+    double ll = 0.;
+#pragma unroll
+    for (int m = 0; m < 6; m++) {
+      double q = 0.;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const double d = RSUB(a.x[c][n[eb[m]]], a.x[c][n[ea[m]]]);
+        q = c == 0 ? RMUL(d, d) : RADD(q, RMUL(d, d));
+      }
+      const double l = sqrt(q);
+      ll = m == 0 ? l : (ll < l ? ll : l);
+    }
+    return ll;
+  }
+}
+
+// Min over elements via an unsigned atomicMin on the bit pattern (positive doubles order like
+// their bits).  A non-positive or NaN length is an error: the reference would turn it into a
+// negative or NaN time step.
+template <bool QUAD>
 __global__ void __launch_bounds__(256) k_courant(ElemArgs a)
 {
   if (a.tm->done | a.tm->status) return;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   double len = 1e300;
   if (e < a.E) {
-    const int n0 = a.conn[e], n1 = a.conn[a.E + e], n2 = a.conn[2L * a.E + e], n3 = a.conn[3L * a.E + e];
-    const double x31 = RSUB(a.x[0][n2], a.x[0][n0]), x24 = RSUB(a.x[0][n1], a.x[0][n3]);
-    const double y42 = RSUB(a.x[1][n3], a.x[1][n1]), y31 = RSUB(a.x[1][n2], a.x[1][n0]);
-    const double num = RADD(RMUL(x31, y42), RMUL(x24, y31));
-    const double sq = RADD(RADD(RADD(RMUL(x24, x24), RMUL(y42, y42)), RMUL(x31, x31)), RMUL(y31, y31));
-    len = num / sqrt(RMUL(2., sq));
+    len = elem_length<QUAD>(a, e);
     if (!(len > 0.)) {
       record_error(a.tm, DNL_ERR_DT, e);
       len = 1e300;
@@ -920,6 +1002,7 @@ __global__ void __launch_bounds__(256) k_courant(ElemArgs a)
 
 // Batched Courant lengths: each element folds its length into its instance's minimum; a warp whose
 // lanes all belong to one instance reduces first and issues one atomic.
+template <bool QUAD>
 __global__ void __launch_bounds__(256) k_courant_batch(ElemArgs a, const int *elemInst, DevTime *tms)
 {
   const int eRaw = blockIdx.x * blockDim.x + threadIdx.x;
@@ -929,12 +1012,7 @@ __global__ void __launch_bounds__(256) k_courant_batch(ElemArgs a, const int *el
   DevTime *tm = tms + inst;
   double len = 1e300;
   if (eRaw < a.E && !(tm->done | tm->status)) {
-    const int n0 = a.conn[e], n1 = a.conn[a.E + e], n2 = a.conn[2L * a.E + e], n3 = a.conn[3L * a.E + e];
-    const double x31 = RSUB(a.x[0][n2], a.x[0][n0]), x24 = RSUB(a.x[0][n1], a.x[0][n3]);
-    const double y42 = RSUB(a.x[1][n3], a.x[1][n1]), y31 = RSUB(a.x[1][n2], a.x[1][n0]);
-    const double num = RADD(RMUL(x31, y42), RMUL(x24, y31));
-    const double sq = RADD(RADD(RADD(RMUL(x24, x24), RMUL(y42, y42)), RMUL(x31, x31)), RMUL(y31, y31));
-    len = num / sqrt(RMUL(2., sq));
+    len = elem_length<QUAD>(a, e);
     if (!(len > 0.)) {
       record_error(tm, DNL_ERR_DT, e);
       len = 1e300;
@@ -1002,7 +1080,8 @@ int launch_elem_tape(dnl_handle *h, cudaStream_t s, double *tape)
   const long threads = (long)h->E * h->nip;
   const int grid = (int)((threads + 127) / 128);
   prof_begin(h, s);
-  DNL_BY_ETYPE(h->etype, (k_elem<ET, true><<<grid, 128, 0, s>>>(a)));
+  if (!etype_has_sens(h->etype)) return DNL_ERR_ARG;
+  DNL_BY_ETYPE_SENS(h->etype, (k_elem<ET, true><<<grid, 128, 0, s>>>(a)));
   prof_end(h, DNL_PROF_ELEM, s);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
@@ -1010,7 +1089,7 @@ int launch_elem_tape(dnl_handle *h, cudaStream_t s, double *tape)
 
 int launch_elem_raw(int etype, const ElemArgs &a, cudaStream_t s)
 {
-  const long threads = (long)a.E * (etype == DNL_ELHEX8N3D ? 8 : 4);
+  const long threads = (long)a.E * etype_nip(etype);
   const int grid = (int)((threads + 127) / 128);
   DNL_BY_ETYPE(etype, (k_elem<ET><<<grid, 128, 0, s>>>(a)));
   launch_counter()++;
@@ -1030,10 +1109,19 @@ int launch_mass(dnl_handle *h, cudaStream_t s, double *me)
 int launch_elem_batch(int etype, int block, const ElemArgs &a, const int *elemInst,
                       const Material *mats, DevTime *tms, cudaStream_t s)
 {
-  const long threads = (long)a.E * (etype == DNL_ELHEX8N3D ? 8 : 4);
+  // the hexahedron's and the 10-node tetrahedron's shared-memory transpose fits 128 threads at most
+  if ((etype == DNL_ELHEX8N3D || etype == DNL_ELTET10N3D) && block > 128) block = 128;
+  const long threads = (long)a.E * etype_nip(etype);
   const int grid = (int)((threads + block - 1) / block);
 #define DNL_EB(ET, B) k_elem_batch<ET, B><<<grid, B, 0, s>>>(a, elemInst, mats, tms)
-  if (etype != DNL_ELHEX8N3D) {
+  if (etype == DNL_ELTET4N3D) {
+    if (block == 64) DNL_EB(DNL_ELTET4N3D, 64);
+    else if (block == 256) DNL_EB(DNL_ELTET4N3D, 256);
+    else DNL_EB(DNL_ELTET4N3D, 128);
+  } else if (etype == DNL_ELTET10N3D) {
+    if (block == 64) DNL_EB(DNL_ELTET10N3D, 64);
+    else DNL_EB(DNL_ELTET10N3D, 128);
+  } else if (etype != DNL_ELHEX8N3D) {
     if (etype == DNL_ELQUA4N2D) {
       if (block == 64) DNL_EB(DNL_ELQUA4N2D, 64);
       else if (block == 256) DNL_EB(DNL_ELQUA4N2D, 256);
@@ -1054,9 +1142,10 @@ int launch_elem_batch(int etype, int block, const ElemArgs &a, const int *elemIn
 int launch_elem_batch_tape(int etype, const ElemArgs &a, const int *elemInst, const Material *mats,
                            DevTime *tms, cudaStream_t s)
 {
-  const long threads = (long)a.E * (etype == DNL_ELHEX8N3D ? 8 : 4);
+  if (!etype_has_sens(etype)) return DNL_ERR_ARG;
+  const long threads = (long)a.E * etype_nip(etype);
   const int grid = (int)((threads + 127) / 128);
-  DNL_BY_ETYPE(etype, (k_elem_batch<ET, 128, true><<<grid, 128, 0, s>>>(a, elemInst, mats, tms)));
+  DNL_BY_ETYPE_SENS(etype, (k_elem_batch<ET, 128, true><<<grid, 128, 0, s>>>(a, elemInst, mats, tms)));
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
@@ -1064,16 +1153,20 @@ int launch_elem_batch_tape(int etype, const ElemArgs &a, const int *elemInst, co
 int launch_mass_batch(int etype, const ElemArgs &a, double *me, const int *elemInst,
                       const Material *mats, cudaStream_t s)
 {
-  const long threads = (long)a.E * (etype == DNL_ELHEX8N3D ? 8 : 4);
+  const long threads = (long)a.E * etype_nip(etype);
   const int grid = (int)((threads + 127) / 128);
   DNL_BY_ETYPE(etype, (k_mass<ET><<<grid, 128, 0, s>>>(a, me, elemInst, mats)));
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
 
-int launch_courant_batch(const ElemArgs &a, const int *elemInst, DevTime *tms, cudaStream_t s)
+int launch_courant_batch(int etype, const ElemArgs &a, const int *elemInst, DevTime *tms,
+                         cudaStream_t s)
 {
-  k_courant_batch<<<(a.E + 255) / 256, 256, 0, s>>>(a, elemInst, tms);
+  if (etype_quad(etype))
+    k_courant_batch<true><<<(a.E + 255) / 256, 256, 0, s>>>(a, elemInst, tms);
+  else
+    k_courant_batch<false><<<(a.E + 255) / 256, 256, 0, s>>>(a, elemInst, tms);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
@@ -1084,7 +1177,10 @@ int launch_courant(dnl_handle *h, cudaStream_t s)
 {
   ElemArgs a = elem_args(h);
   prof_begin(h, s);
-  k_courant<<<(h->E + 255) / 256, 256, 0, s>>>(a);
+  if (etype_quad(h->etype))
+    k_courant<true><<<(h->E + 255) / 256, 256, 0, s>>>(a);
+  else
+    k_courant<false><<<(h->E + 255) / 256, 256, 0, s>>>(a);
   prof_end(h, DNL_PROF_COURANT, s);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;

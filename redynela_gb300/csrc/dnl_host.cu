@@ -860,7 +860,7 @@ int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, con
   std::vector<double> pnIP(nIP);
   for (long e = 0; e < E; e++)
     for (int q = 0; q < h->nip; q++) pnIP[e * h->nip + q] = pn[elem_material ? elem_material[e] : 0];
-  const int ns = h->etype == DNL_ELHEX8N3D ? 6 : 4;
+  const int ns = etype_ns(h->etype);
   CK(cudaMemcpy(h->ip + (size_t)(3 * ns + 2) * nIP, pnIP.data(), sizeof(double) * nIP, cudaMemcpyHostToDevice));
   CK(cudaMalloc(&h->evpn0, sizeof(double) * nmat));
   CK(cudaMemcpy(h->evpn0, pn.data(), sizeof(double) * nmat, cudaMemcpyHostToDevice));
@@ -897,7 +897,7 @@ int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0)
   for (int i = 0; i < h->ngraphs; i++) cudaGraphExecDestroy(h->graphs[i].exec);
   h->ngraphs = 0;  // captured launches hold the old material and state by value
   if (mat) {
-    h->mat = make_material(*mat);
+    h->mat = make_material(*mat, h->nen);
     const double Nu = h->mat.nu;
     const double f = (h->mat.young * (1.0 - Nu) / ((1.0 + Nu) * (1.0 - 2.0 * Nu)));
     h->C00 = 1 * f;
@@ -919,8 +919,8 @@ int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0)
       k_fill<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(h->bank[b].v[c], N, h->v0[c]);
       launch_counter()++;
     }
-  const int ncomp = h->etype == DNL_ELHEX8N3D ? IpLayout<DNL_ELHEX8N3D>::NCOMP : IpLayout<DNL_ELQUA4NAX>::NCOMP;
-  const int ns = h->etype == DNL_ELHEX8N3D ? 6 : 4;
+  const int ncomp = 3 * etype_ns(h->etype) + 3;  // IpLayout::NCOMP
+  const int ns = etype_ns(h->etype);
   CK(cudaMemsetAsync(h->ip, 0, sizeof(double) * ncomp * nIP, s));
   k_fill<<<(unsigned)((nIP + 255) / 256), 256, 0, s>>>(h->ip + (size_t)(3 * ns + 1) * nIP, nIP, 1e-10);
   if (h->elemMat)
@@ -953,8 +953,7 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
 {
   if (!mesh || !mat || !sp || !out) return DNL_ERR_ARG;
   *out = nullptr;
-  if (mesh->etype != DNL_ELQUA4NAX && mesh->etype != DNL_ELHEX8N3D && mesh->etype != DNL_ELQUA4N2D)
-    return DNL_ERR_ARG;
+  if (!etype_valid(mesh->etype)) return DNL_ERR_ARG;
   if (mesh->num_nodes <= 0 || mesh->num_elements <= 0 || !mesh->coords || !mesh->conn) return DNL_ERR_ARG;
   if (sp->frequency < 1 || !(sp->end_time > 0) || !(sp->safety > 0)) return DNL_ERR_ARG;
   if (sp->method != DNL_COURANT && sp->method != DNL_PULSE) return DNL_ERR_ARG;
@@ -966,7 +965,7 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
   if (mesh->num_bc < 0 || (mesh->num_bc > 0 && (!mesh->bc_kind || !mesh->bc_val || !mesh->bc_start || !mesh->bc_nodes)))
     return DNL_ERR_ARG;
   const int N = mesh->num_nodes, E = mesh->num_elements;
-  const int nen = mesh->etype == DNL_ELHEX8N3D ? 8 : 4;
+  const int nen = etype_nen(mesh->etype);
   for (long i = 0; i < (long)E * nen; i++)
     if (mesh->conn[i] < 0 || mesh->conn[i] >= N) return DNL_ERR_ARG;
   for (int g = 0; g < mesh->num_bc; g++)
@@ -982,8 +981,9 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
   dnl_handle *h = new dnl_handle();
   memset(h, 0, sizeof(dnl_handle));
   h->etype = mesh->etype;
-  h->dim = mesh->etype == DNL_ELHEX8N3D ? 3 : 2;
-  h->nen = h->nip = nen;
+  h->dim = etype_dim(mesh->etype);
+  h->nen = nen;
+  h->nip = etype_nip(mesh->etype);
   h->N = N;
   h->E = E;
   h->nIP = E * h->nip;
@@ -1011,7 +1011,7 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
   CKF(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
 
   // material constants, in the reference's expressions
-  const Material m = make_material(*mat);
+  const Material m = make_material(*mat, nen);
   h->mat = m;
   // ExplicitSolverCH::computeIntegrationParameters (ExplicitSolverCH.C:336-343)
   const double rb = sp->rho_b;
@@ -1081,8 +1081,8 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
   CKF(cudaMalloc(&h->mass, sizeof(double) * N));
   CKF(cudaMemset(h->mass, 0, sizeof(double) * N));
   // ---- integration points
-  const int ncomp = h->etype == DNL_ELHEX8N3D ? IpLayout<DNL_ELHEX8N3D>::NCOMP : IpLayout<DNL_ELQUA4NAX>::NCOMP;
-  const int ns = h->etype == DNL_ELHEX8N3D ? 6 : 4;
+  const int ncomp = 3 * etype_ns(h->etype) + 3;  // IpLayout::NCOMP
+  const int ns = etype_ns(h->etype);
   CKF(cudaMalloc(&h->ip, sizeof(double) * (size_t)ncomp * h->nIP));
   CKF(cudaMemset(h->ip, 0, sizeof(double) * (size_t)ncomp * h->nIP));
   {  // evp = 1e-10 (IntegrationPoint::flush) and its cached power
@@ -1191,7 +1191,7 @@ int dnl_set_state(dnl_handle *h, const dnl_state_view *s)
   if (s->v && (r = put3(s->v, h->bank[h->cur].v))) return r;
   if (s->a && (r = put3(s->a, h->bank[h->cur].a))) return r;
   if (s->disp && (r = put3(s->disp, h->bank[h->cur].disp))) return r;
-  const int ns = h->etype == DNL_ELHEX8N3D ? 6 : 4;
+  const int ns = etype_ns(h->etype);
   const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
   const size_t nIP = h->nIP;
   CK(cudaStreamSynchronize(h->stream));
@@ -1237,7 +1237,7 @@ int dnl_get_state(dnl_handle *h, dnl_state_view *s)
   CK(cudaStreamSynchronize(h->stream));
   if (s->mass) CK(cudaMemcpy(s->mass, h->mass, sizeof(double) * N, cudaMemcpyDeviceToHost));
   if (!(s->S || s->Eps || s->EpsPlas || s->p || s->evp || s->Sig)) return 0;
-  const int ns = h->etype == DNL_ELHEX8N3D ? 6 : 4;
+  const int ns = etype_ns(h->etype);
   const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
   const size_t nIP = h->nIP;
   std::vector<double> ib(nIP), pb(nIP);

@@ -28,6 +28,7 @@ namespace dnl {
 // shape functions, same construction as dnl_elem.cu
 struct PShape {
   double axN[3], axD[2], hxN[4], hxD[3];
+  double t10N[4][10], t10D[4][10][3];
 };
 __constant__ PShape c_pshape;
 
@@ -55,6 +56,21 @@ template <> __device__ __forceinline__ double pN<DNL_ELQUA4N2D>(int pt, int k)
 template <> __device__ __forceinline__ double pdN<DNL_ELQUA4N2D>(int pt, int k, int c)
 {
   return pdN<DNL_ELQUA4NAX>(pt, k, c);
+}
+template <> __device__ __forceinline__ double pN<DNL_ELTET4N3D>(int, int) { return 0.25; }
+template <> __device__ __forceinline__ double pdN<DNL_ELTET4N3D>(int, int k, int c)
+{
+  return k == 0 ? -1.0 : (k - 1 == c ? 1.0 : 0.0);
+}
+template <> __device__ __forceinline__ double pN<DNL_ELTET10N3D>(int pt, int k) { return c_pshape.t10N[pt][k]; }
+template <> __device__ __forceinline__ double pdN<DNL_ELTET10N3D>(int pt, int k, int c)
+{
+  return c_pshape.t10D[pt][k][c];
+}
+// integration weight (ElTet4n3D.C:33, ElTet10n3D.C:30; the quads and the hexahedron: 1)
+template <int ET> constexpr double pweight()
+{
+  return ET == DNL_ELTET4N3D ? 1. / 6. : (ET == DNL_ELTET10N3D ? 1.0 / 24.0 : 1.0);
 }
 template <> __device__ __forceinline__ double pN<DNL_ELHEX8N3D>(int pt, int k)
 {
@@ -84,6 +100,7 @@ static void set_pulse_tables()
   s.hxD[0] = (2.0 + sqrt(3.0)) / 12.0;
   s.hxD[1] = 1.0 / 12.0;
   s.hxD[2] = (2.0 - sqrt(3.0)) / 12.0;
+  tet10_tables(s.t10N, s.t10D);
   cudaMemcpyToSymbol(c_pshape, &s, sizeof s);
 }
 
@@ -106,7 +123,7 @@ __global__ void __launch_bounds__(128) k_pulse_setup(PulseArgs a)
 {
   using T = Elem<ET>;
   constexpr int NIP = T::NIP, NEN = T::NEN, DIM = T::DIM;
-  constexpr bool AXI = ET == DNL_ELQUA4NAX, TWO_D = ET != DNL_ELHEX8N3D;
+  constexpr bool AXI = ET == DNL_ELQUA4NAX, TWO_D = DIM == 2;
   if (a.tm->done | a.tm->status) return;
   const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long nIP = (long)a.E * NIP;
@@ -149,7 +166,7 @@ __global__ void __launch_bounds__(128) k_pulse_setup(PulseArgs a)
     Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
     Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
   }
-  double W = detJ;
+  double W = pweight<ET>() == 1.0 ? detJ : pweight<ET>() * detJ;
   if (AXI) W *= 2 * kPi * Rad;
 #pragma unroll
   for (int l = 0; l < DIM; l++)
@@ -254,12 +271,19 @@ __global__ void __launch_bounds__(128) k_pulse_kx(PulseArgs a)
     }
   __syncwarp();
   if (valid) {
+    // lane pt sums node pt (and pt + NIP, ... when the element has more nodes than points)
 #pragma unroll
-    for (int i = 0; i < DIM; i++) {
-      double s = 0.;
+    for (int j = 0; j < (NEN + NIP - 1) / NIP; j++) {
+      const int k = pt + j * NIP;
+      if (k < NEN) {
 #pragma unroll
-      for (int q = 0; q < NIP; q++) s += red[wib][slot][q][pt * DIM + i];
-      a.kx[(long)i * a.E * NEN + (long)e * NEN + pt] = s;
+        for (int i = 0; i < DIM; i++) {
+          double s = 0.;
+#pragma unroll
+          for (int q = 0; q < NIP; q++) s += red[wib][slot][q][k * DIM + i];
+          a.kx[(long)i * a.E * NEN + (long)e * NEN + k] = s;
+        }
+      }
     }
   }
 }
@@ -388,11 +412,10 @@ int launch_pulse(dnl_handle *h, cudaStream_t s)
   for (int round = 0; round < (kPulseMaxIt + batch) / batch + 1; round++) {
     for (int b = 0; b < batch; b++) {
       prof_begin(h, s);
-      if (h->etype != DNL_ELHEX8N3D) {
-        DNL_BY_ETYPE(h->etype, (k_pulse_kx<ET><<<gridIP, 128, 0, s>>>(a)));
+      DNL_BY_ETYPE(h->etype, (k_pulse_kx<ET><<<gridIP, 128, 0, s>>>(a)));
+      if (h->dim == 2) {
         k_pulse_gather<2><<<gridN, 256, 0, s>>>(a, h->E * h->nen);
       } else {
-        k_pulse_kx<DNL_ELHEX8N3D><<<gridIP, 128, 0, s>>>(a);
         k_pulse_gather<3><<<gridN, 256, 0, s>>>(a, h->E * h->nen);
       }
       k_pulse_check<<<1, 1, 0, s>>>(h->tm);

@@ -218,7 +218,8 @@ int sens_alloc(dnl_handle *h, SensState *S)
 // scheduled step size, each followed by its tangent launch.
 int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt)
 {
-  // the tangent formulas are those of the power law, one material
+  // the tangent formulas are those of the power law, one material, quads and hexahedra
+  if (!etype_has_sens(h->etype)) return DNL_ERR_ARG;
   if (!bt && (h->elemMat || h->mat.hard.law != DNL_HARD_POWER)) return DNL_ERR_ARG;
   for (int k = 0; k < nsteps; k++)
     if (!(dts[k] > 0. && dts[k] < 1e300)) return DNL_ERR_ARG;

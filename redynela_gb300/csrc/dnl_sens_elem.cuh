@@ -31,7 +31,7 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
   using L = IpLayout<ET>;
   constexpr int NIP = T::NIP, NEN = T::NEN, DIM = T::DIM, NS = T::NS;
   constexpr bool AXI = ET == DNL_ELQUA4NAX;
-  constexpr bool TWO_D = ET != DNL_ELHEX8N3D;
+  constexpr bool TWO_D = DIM == 2;
   const long nIP = (long)a.E * NIP, ipx = (long)e * NIP + pt, N = a.N;
   const Material &m = a.elemInst ? a.mats[a.elemInst[e]] : a.mat;
   auto tp = [&](int slot) { return a.tape[(long)slot * nIP + ipx]; };
@@ -419,9 +419,10 @@ __global__ void __launch_bounds__(128) k_elem_tan(SensElemArgs a)
 
 int launch_elem_tan(int etype, const SensElemArgs &a, cudaStream_t s)
 {
-  const long threads = (long)a.E * kSensParams * (etype == DNL_ELHEX8N3D ? 8 : 4);
+  if (!etype_has_sens(etype)) return DNL_ERR_ARG;
+  const long threads = (long)a.E * kSensParams * etype_nip(etype);
   const int grid = (int)((threads + 127) / 128);
-  DNL_BY_ETYPE(etype, (k_elem_tan<ET><<<grid, 128, 0, s>>>(a)));
+  DNL_BY_ETYPE_SENS(etype, (k_elem_tan<ET><<<grid, 128, 0, s>>>(a)));
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }

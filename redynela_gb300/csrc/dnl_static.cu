@@ -56,9 +56,8 @@ extern "C" int dnl_internal_forces_static(const dnl_static_args *a, void *stream
   using namespace dnl;
   if (bad_element) *bad_element = -1;
   if (!a) return DNL_ERR_ARG;
-  if (a->etype != DNL_ELQUA4NAX && a->etype != DNL_ELHEX8N3D && a->etype != DNL_ELQUA4N2D)
-    return DNL_ERR_ARG;
-  const int nen = a->etype == DNL_ELHEX8N3D ? 8 : 4, dim = a->etype == DNL_ELHEX8N3D ? 3 : 2;
+  if (!etype_valid(a->etype)) return DNL_ERR_ARG;
+  const int nen = etype_nen(a->etype), dim = etype_dim(a->etype);
   if (a->num_nodes <= 0 || a->num_elements <= 0) return DNL_ERR_ARG;
   if ((long long)a->num_elements * nen * dim > DNL_STATIC_MAX_ELEMENT_DOFS) return DNL_ERR_ARG;
   if (!a->conn || !a->node_start || !a->node_entry || !a->coords || !a->du || !a->ip || !a->fint)
@@ -70,7 +69,7 @@ extern "C" int dnl_internal_forces_static(const dnl_static_args *a, void *stream
   // the error word starts at zero on every call; the array itself needs no clearing (fully written)
   if (cudaMemsetAsync(sp->tm, 0, sizeof(DevTime), s) != cudaSuccess) return DNL_ERR_CUDA;
 
-  const Material m = make_material(a->mat);
+  const Material m = make_material(a->mat, nen);
 
   const int N = a->num_nodes, E = a->num_elements;
   ElemArgs ea;

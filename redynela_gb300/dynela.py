@@ -714,6 +714,8 @@ class ExplicitSolverCH:
 ElQua4nAx = meshes.ELQUA4NAX
 ElHex8n3D = meshes.ELHEX8N3D
 ElQua4n2D = meshes.ELQUA4N2D
+ElTet4n3D = meshes.ELTET4N3D
+ElTet10n3D = meshes.ELTET10N3D
 
 
 class Structure:

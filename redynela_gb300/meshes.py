@@ -30,6 +30,8 @@ import numpy as np
 ELQUA4NAX = 0
 ELHEX8N3D = 1
 ELQUA4N2D = 2  # plane strain
+ELTET4N3D = 3
+ELTET10N3D = 4
 
 COURANT = 0
 PULSE = 1
@@ -121,15 +123,15 @@ class Model:
 
     @property
     def dim(self) -> int:
-        return 3 if self.etype == ELHEX8N3D else 2
+        return 2 if self.etype in (ELQUA4NAX, ELQUA4N2D) else 3
 
     @property
     def nen(self) -> int:
-        return 8 if self.etype == ELHEX8N3D else 4
+        return {ELHEX8N3D: 8, ELTET10N3D: 10}.get(self.etype, 4)
 
     @property
     def nip(self) -> int:
-        return 8 if self.etype == ELHEX8N3D else 4
+        return {ELHEX8N3D: 8, ELTET4N3D: 1}.get(self.etype, 4)
 
 
 def taylor_axi(nr: int = 5, nz: int = 50, radius: float = 3.2e-3, length: float = 32.4e-3,
@@ -212,6 +214,39 @@ def taylor_hex(ncross: int = 40, nz: int = 400, radius: float = 3.2e-3, length: 
     bcs = [BCGroup(RESTRAIN, (0.0, 0.0, 1.0), base)]
     return Model(ELHEX8N3D, coords, conn, young, poisson, density, A, B, n,
                  (0.0, 0.0, -speed), bcs, tend, rho_b, safety, freq, PULSE)
+
+
+# the six tetrahedra of a hexahedron around its diagonal 0-6 (node numbering of ElHex8n3D); on a
+# grid of hexahedra numbered alike the faces of neighbouring cells are split the same way
+_HEX_TO_TETS = ((0, 1, 2, 6), (0, 2, 3, 6), (0, 3, 7, 6), (0, 7, 4, 6), (0, 4, 5, 6), (0, 5, 1, 6))
+# ElTet10n3D's mid-edge nodes 4..9 (ElTet10n3D.C:37-47)
+_TET10_EDGES = ((0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3))
+
+
+def taylor_tet(ncross: int = 8, nz: int = 24, quadratic: bool = False, safety: float = 0.5,
+               **kw) -> Model:
+    """3D Taylor bar of tetrahedra: each cell of taylor_hex(ncross, nz) split in six (ElTet4n3D),
+    or with a node added at the middle of every edge (ElTet10n3D, quadratic=True); base
+    restrained in z, Courant time step.  The tetrahedra's Courant length is their shortest edge,
+    longer than the stable length of these elements: with the usual safety factor 0.9 the
+    reference's own run of this bar inverts elements after ~3 us, hence 0.5."""
+    m = taylor_hex(ncross, nz, safety=safety, **kw)
+    conn = np.concatenate([m.conn[:, list(t)] for t in _HEX_TO_TETS], axis=0)
+    conn = conn.reshape(6, m.E, 4).transpose(1, 0, 2).reshape(-1, 4)  # the tets of a cell together
+    coords = m.coords
+    etype = ELTET4N3D
+    base = m.bcs[0].nodes
+    if quadratic:
+        ends = np.stack([np.sort(conn[:, list(ed)], axis=1) for ed in _TET10_EDGES], axis=1)
+        uniq, inv = np.unique(ends.reshape(-1, 2), axis=0, return_inverse=True)
+        mid = m.N + inv.reshape(-1, 6)
+        coords = np.concatenate([coords, 0.5 * (coords[uniq[:, 0]] + coords[uniq[:, 1]])])
+        conn = np.concatenate([conn, mid], axis=1)
+        etype = ELTET10N3D
+        base = np.flatnonzero(coords[:, 2] == 0.0).astype(np.int64)
+    bcs = [BCGroup(RESTRAIN, (0.0, 0.0, 1.0), base)]
+    return dataclasses.replace(m, etype=etype, coords=coords, conn=conn.astype(np.int64), bcs=bcs,
+                               method=COURANT)
 
 
 def tabular_table(A: float, B: float, n: float, step: float = 0.1, stop: float = 10.0):

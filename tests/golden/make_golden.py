@@ -20,6 +20,13 @@ reference's own output on a seeded synthetic model:
 * ``steps_plane.npz``   the 5x50 bar in plane strain (ElQua4n2D), first 40 steps
 * ``run_plane.npz``     the same bar to 80 us: final coordinates, plastic strain, pressure
 * ``steps_plane_pulse.npz`` the plane-strain bar with the Pulse time step, first 30 steps
+* ``forces_tet4.npz``, ``forces_tet10.npz``  one computeInternalForces on an injected state of a
+                        4x4x3-cell bar split into ElTet4n3D / ElTet10n3D
+* ``steps_tet4.npz``    the 6x6x8-cell ElTet4n3D bar (Courant, safety 0.5), first 40 steps
+* ``run_tet4.npz``      the same bar to 80 us
+* ``steps_tet4_pulse.npz`` the same bar with the Pulse time step, first 20 steps
+* ``steps_tet10.npz``   the ElTet10n3D bar, lumped mass and its first 2 steps (the reference's run
+                        of this element ends in a singular Jacobian a few steps later)
 
     python tests/golden/make_golden.py
 """
@@ -91,6 +98,33 @@ def plane():
          final_S=r["final_S"], final_v=r["final_v"])
 
 
+def tets():
+    """The tetrahedron fixtures only: python tests/golden/make_golden.py tets"""
+    save("tables.npz", **dnl_io.reference_tables())
+    for name, q in (("forces_tet4.npz", False), ("forces_tet10.npz", True)):
+        m = meshes.taylor_tet(4, 3, quadratic=q)
+        st = states.random_state(m, seed=7)
+        r = dnl_io.run_reference("forces", m, state=st)
+        save(name, **{f"in_{k}": np.asarray(v) for k, v in st.items()}, fint=r["fint"],
+             **{k: r[k] for k in r if k.startswith("out_")})
+    m = meshes.taylor_tet(6, 8)
+    r = dnl_io.run_reference("steps", m, 40)
+    save("steps_tet4.npz", mass=r["mass"], dt0=r["dt0"], dt=r["dt"], time=r["time"],
+         kinetic=r["kinetic"], fint=np.stack([r[f"fint_{k:06d}"] for k in range(40)]),
+         final_coords=r["final_coords"], final_S=r["final_S"])
+    r = dnl_io.run_reference("steps", dataclasses.replace(m, method=meshes.PULSE), 20)
+    save("steps_tet4_pulse.npz", dt0=r["dt0"], dt=r["dt"],
+         fint=np.stack([r[f"fint_{k:06d}"] for k in range(20)]), final_coords=r["final_coords"])
+    r = dnl_io.run_reference("run", m)
+    save("run_tet4.npz", increments=r["increments"], time=r["time"],
+         final_coords=r["final_coords"], final_evp=r["final_evp"], final_p=r["final_p"])
+    m = meshes.taylor_tet(6, 8, quadratic=True)
+    r = dnl_io.run_reference("steps", m, 2)
+    save("steps_tet10.npz", mass=r["mass"], dt0=r["dt0"], dt=r["dt"], time=r["time"],
+         kinetic=r["kinetic"], fint=np.stack([r[f"fint_{k:06d}"] for k in range(2)]),
+         final_coords=r["final_coords"])
+
+
 def main():
     if not dnl_io.reference_available():
         sys.exit("compiled reference missing: run `make -C oracle ref`")
@@ -102,6 +136,9 @@ def main():
         return
     if sys.argv[1:] == ["plane"]:
         plane()
+        return
+    if sys.argv[1:] == ["tets"]:
+        tets()
         return
     t = dnl_io.reference_tables()
     save("tables.npz", **t)
@@ -138,6 +175,7 @@ def main():
     results()
     laws()
     plane()
+    tets()
 
 
 if __name__ == "__main__":

@@ -18,16 +18,25 @@ def _inject(o, g):
 
 def test_tables_match_reference():
     g = golden("tables.npz")
-    for et, nm in ((0, "axi"), (1, "hex"), (2, "plane")):
+    for et, nm in ((0, "axi"), (1, "hex"), (2, "plane"), (3, "tet4"), (4, "tet10")):
         N, dN = orc.tables(et)
         assert np.array_equal(N.ravel(), g[nm + "_N"])
         assert np.array_equal(dN.ravel(), g[nm + "_dN"])
-        assert np.all(g[nm + "_weight"] == 1.0)
+    for nm, w in (("axi", 1.0), ("hex", 1.0), ("plane", 1.0), ("tet4", 1. / 6.), ("tet10", 1.0 / 24.0)):
+        assert np.all(g[nm + "_weight"] == w)
+    # the reference's ElTet10n3D derivative tables do not sum to zero over the nodes (two negated
+    # constants are unparenthesised macros): the oracle reproduces that, it is not a mistake here
+    dN10 = g["tet10_dN"].reshape(4, 10, 3)
+    assert np.all(np.abs(dN10.sum(axis=1)) > 1.7)
+    assert np.all(np.abs(g["tet4_dN"].reshape(1, 4, 3).sum(axis=1)) == 0.0)
 
 
 @pytest.mark.parametrize("name,model", [("forces_axi.npz", lambda: meshes.taylor_axi(3, 4)),
                                         ("forces_hex.npz", lambda: meshes.taylor_hex(4, 3)),
-                                        ("forces_plane.npz", lambda: meshes.taylor_plane(3, 4))])
+                                        ("forces_plane.npz", lambda: meshes.taylor_plane(3, 4)),
+                                        ("forces_tet4.npz", lambda: meshes.taylor_tet(4, 3)),
+                                        ("forces_tet10.npz",
+                                         lambda: meshes.taylor_tet(4, 3, quadratic=True))])
 def test_internal_forces_bit_exact(name, model):
     """One Domain::computeInternalForces on an injected mid-run state: bit for bit."""
     g = golden(name)
@@ -95,6 +104,53 @@ def test_plane_strain_steps_and_run_bit_exact():
     assert np.array_equal(o.array("coords"), g["final_coords"])
     assert np.array_equal(o.array("evp"), g["final_evp"])
     assert g["final_evp"].max() > 1.0
+
+
+def test_tet4_steps_and_run_bit_exact():
+    """ElTet4n3D (one point, Courant length = shortest edge): 40 steps, then the full run."""
+    g = golden("steps_tet4.npz")
+    m = meshes.taylor_tet(6, 8)
+    o = Oracle(m)
+    o.prologue()
+    assert np.array_equal(o.array("Mass"), g["mass"])
+    assert o.get("dt") == g["dt0"][0]
+    for k in range(40):
+        o.steps(1)
+        assert np.array_equal(o.array("fint"), g["fint"][k]), k
+    assert np.array_equal(o.array("coords"), g["final_coords"])
+    g = golden("run_tet4.npz")
+    o = Oracle(m)
+    o.prologue()
+    assert o.steps(10 ** 9) == int(g["increments"][0])
+    assert np.array_equal(o.array("coords"), g["final_coords"])
+    assert np.array_equal(o.array("evp"), g["final_evp"])
+
+
+def test_tet4_pulse():
+    g = golden("steps_tet4_pulse.npz")
+    o = Oracle(dataclasses.replace(meshes.taylor_tet(6, 8), method=meshes.PULSE))
+    o.prologue()
+    assert abs(o.get("dt") - g["dt0"][0]) <= 1e-14 * g["dt0"][0]
+    for k in range(20):
+        o.steps(1)
+        r = g["fint"][k]
+        if np.linalg.norm(r) > 0:
+            assert np.linalg.norm(o.array("fint") - r) <= 1e-12 * np.linalg.norm(r), k
+
+
+def test_tet10_mass_and_first_steps_bit_exact():
+    """ElTet10n3D: the lumped mass (negative at the corner nodes: row sums of the quadratic shape
+    functions) and the two steps the reference's run of this bar survives."""
+    g = golden("steps_tet10.npz")
+    o = Oracle(meshes.taylor_tet(6, 8, quadratic=True))
+    o.prologue()
+    assert np.array_equal(o.array("Mass"), g["mass"])
+    assert np.any(g["mass"] < 0)
+    assert o.get("dt") == g["dt0"][0]
+    for k in range(2):
+        o.steps(1)
+        assert np.array_equal(o.array("fint"), g["fint"][k]), k
+    assert np.array_equal(o.array("coords"), g["final_coords"])
 
 
 def test_steps_plane_pulse():
