@@ -361,8 +361,9 @@ def main_batch(args):
         launches = dynela.kernel_launches() - launches0
     clocks = clk.summary()
     value = E * args.steps / (ms * 1e-3)
-    # the same bars one at a time through the single-mesh path (stream launches, state resident)
-    plain_ms = 0.0
+    # the same bars one at a time through the single-mesh path, state resident: stream launches
+    # (dnl_step) and graph replay (dnl_step_graph, the faster of the two, which the ratio uses)
+    plain_ms = plain_graph_ms = 0.0
     for m in models:
         d = dynela.GpuDomain(m)
         d.prologue()
@@ -371,8 +372,14 @@ def main_batch(args):
         d.step(args.steps)
         d.timer_mark(1)
         plain_ms += d.timer_elapsed_ms(0, 1)
+        d.step_graph(args.steps)  # capture and warm-up
+        d.timer_mark(0)
+        d.step_graph(args.steps)
+        d.timer_mark(1)
+        plain_graph_ms += d.timer_elapsed_ms(0, 1)
         d.close()
     plain = E * args.steps / (plain_ms * 1e-3)
+    plain_graph = E * args.steps / (plain_graph_ms * 1e-3)
     line = {"metric": "element-updates/s (batched)", "value": value, "unit": "element-updates/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -381,8 +388,14 @@ def main_batch(args):
                        "instances": args.instances, "block": block, "active_after": active,
                        "l2": "inputs larger than L2 (integration-point state "
                              f"{E * 4 * 15 * 8 / 1e6:.0f} MB)"},
-            "plain_instance_by_instance": {"value": plain, "ms_per_step": plain_ms / args.steps},
-            "batched_over_plain": value / plain, "gpu_launches": launches, "clocks": clocks}
+            "plain_instance_by_instance": {"value": max(plain, plain_graph),
+                                           "ms_per_step": min(plain_ms, plain_graph_ms) / args.steps,
+                                           "stream_launches": {"value": plain,
+                                                               "ms_per_step": plain_ms / args.steps},
+                                           "graph_replay": {"value": plain_graph,
+                                                            "ms_per_step": plain_graph_ms / args.steps}},
+            "batched_over_plain": value / max(plain, plain_graph), "gpu_launches": launches,
+            "clocks": clocks}
     print(json.dumps(line), flush=True)
 
 
@@ -429,7 +442,6 @@ def main_sens(args):
         gradient()
     launches0 = dynela.kernel_launches()
     dev_ms = 0.0
-    d.profile_begin()
     with ClockSampler(0) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
@@ -438,10 +450,26 @@ def main_sens(args):
             d.timer_mark(1)
             dev_ms += d.timer_elapsed_ms(0, 1)
         wall = time.perf_counter() - t0
-    prof = d.profile_end()
     launches = (dynela.kernel_launches() - launches0) // args.steps
     clocks = clk.summary()
     value = args.steps / (dev_ms * 1e-3)
+    # kernel shares from one more gradient with CUDA events around every launch (untimed)
+    d.profile_begin()
+    gradient()
+    prof = d.profile_end()
+    # the forward cost: the same schedule as a plain run (Courant steps recomputed, as the schedule
+    # was made) from the same initial state, graph-replayed; the mean of K runs
+    fwd_ms = 0.0
+    for _ in range(args.steps):
+        d.reset(m)
+        d.prologue()
+        d.timer_mark(0)
+        k = 0
+        while k < nst:
+            k += d.step_graph(min(100, nst - k))
+        d.timer_mark(1)
+        fwd_ms += d.timer_elapsed_ms(0, 1) / args.steps
+    grad_ms = dev_ms / args.steps
     e2e = args.steps / wall
     tan_ms, tan_n = prof["tangent"]
     elem_ms, elem_n = prof["elem"]
@@ -489,6 +517,8 @@ def main_sens(args):
                        "step": "one gradient = dnl_reset + dnl_sens_run + contraction",
                        "l2": "state of 4,000 elements fits L2; each gradient is a 4,000-step run"},
             "gradient": [float(v) for v in g],
+            "forward_run_ms": fwd_ms, "gradient_ms": grad_ms,
+            "gradient_cost_vs_forward": grad_ms / fwd_ms,
             "agreement_vs_dual_oracle": agree,
             "gpu_launches": launches,
             "kernel_time_share": {k: round(v[0] / total_ms, 4) for k, v in prof.items()} if total_ms else None,

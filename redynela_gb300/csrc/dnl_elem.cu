@@ -154,6 +154,49 @@ __device__ __forceinline__ unsigned long long abits(double a)
 }
 __device__ __forceinline__ bool abs_gt(double a, double b) { return abits(a) > abits(b); }
 
+// ln(1 + x) for |x| <= 2^-6 by the Mercator series x - x^2/2 + x^3/3 - ... to x^10/10 in Horner
+// form: the truncation is below 2^-60 |x| and the result within about an ulp (10 FP64
+// instructions where the library logarithm takes about 25).
+__device__ __forceinline__ double log1p_series(double x)
+{
+  double s = -1. / 10.;
+  s = fma(x, s, 1. / 9.);
+  s = fma(x, s, -1. / 8.);
+  s = fma(x, s, 1. / 7.);
+  s = fma(x, s, -1. / 6.);
+  s = fma(x, s, 1. / 5.);
+  s = fma(x, s, -1. / 4.);
+  s = fma(x, s, 1. / 3.);
+  s = fma(x, s, -1. / 2.);
+  s = fma(x, s, 1.);
+  return x * s;
+}
+constexpr double kSeriesMax = 0.015625;  // 2^-6
+
+// ln(l) of an eigenvalue of C = F^T F: l - 1 is exact for l in [1/2, 2], and within 2^-6 of 1
+// (strain increments below ~0.8 % per step, nearly every point of every step) the series above
+// applies; elsewhere the library logarithm.
+__device__ __forceinline__ double ln_eig(double l)
+{
+  const double x = l - 1.0;
+  return abits(x) <= abits(kSeriesMax) ? log1p_series(x) : log(l);
+}
+
+// e^t for |t| <= 2^-5 by its Taylor series to t^9/9! in Horner form (truncation below 2^-70)
+__device__ __forceinline__ double exp_series(double t)
+{
+  double s = 1. / 362880.;
+  s = fma(t, s, 1. / 40320.);
+  s = fma(t, s, 1. / 5040.);
+  s = fma(t, s, 1. / 720.);
+  s = fma(t, s, 1. / 120.);
+  s = fma(t, s, 1. / 24.);
+  s = fma(t, s, 1. / 6.);
+  s = fma(t, s, 0.5);
+  s = fma(t, s, 1.);
+  return fma(t, s, 1.);
+}
+
 // 1/x by Newton-Raphson (r <- r + r (1 - x r), quadratic convergence) from the PTX hardware seed
 // rcp.approx.ftz.f64; two steps give the double result to about an ulp (not correctly rounded).
 // For normal, finite, non-zero x.
@@ -465,7 +508,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     double lg[3], il[3];
 #pragma unroll
     for (int cc = 0; cc < 3; cc++) {
-      lg[cc] = 0.5 * log(f[cc][cc]);
+      lg[cc] = 0.5 * ln_eig(f[cc][cc]);
       il[cc] = rsqrt(f[cc][cc]);
     }
     if (TAPE) {
@@ -638,13 +681,21 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         }
     } else if (power && __double_as_longlong(Strial) > __double_as_longlong(Sigv0)) {  // both >= 0
       plastic = true;
-      double h = m.nB * evpn * nr_rcp(evp);
+      const double revp = nr_rcp(evp);
+      double h = m.nB * evpn * revp;
       double gamma = fma(-kSqrt23, Sigv0, normS) * nr_rcp(m.G2 * fma(h, m.rG3, 1.0));
       double xn = evpn;
+      // xv^n = evp^n (1 + q)^n with q = (xv - evp) / evp: by the series above from the cached
+      // evp^n when |q| <= 2^-6 and n <= 2 (|n ln(1 + q)| <= 2^-5), else exp(n ln xv)
+      const bool series = m.n <= 2.0;
       int iteration = 0;
       for (;;) {
         const double xv = RADD(evp, RMUL(kSqrt23, gamma));
-        xn = exp(m.n * log(xv));  // xv^n
+        const double q = (xv - evp) * revp;
+        if (series && abits(q) <= abits(kSeriesMax))
+          xn = evpn * exp_series(m.n * log1p_series(q));
+        else
+          xn = exp(m.n * log(xv));  // xv^n
         const double Sigv = RADD(m.A, RMUL(m.B, xn));
         h = m.nB * xn * nr_rcp(xv);  // n B xv^(n-1)
         const double dfun = fma(kSqrt23, h, m.dfun0);
