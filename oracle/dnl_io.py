@@ -105,8 +105,10 @@ def reference_available() -> bool:
 
 
 def run_reference(cmd: str, model, *extra, state: Optional[dict] = None, threads: int = 1,
-                  timeout: float = 3600.0) -> Dict[str, np.ndarray]:
-    """Run ``ref_harness <cmd>`` on ``model`` in a scratch directory and return its records."""
+                  timeout: float = 3600.0, strategy: Optional[int] = None) -> Dict[str, np.ndarray]:
+    """Run ``ref_harness <cmd>`` on ``model`` in a scratch directory and return its records.
+    ``strategy``: the reference's Domain::computeInternalForces parallelisation (0-7, the
+    ``computeInternalForces`` environment variable it reads, Domain.C:148-152); default 0."""
     if not reference_available():
         raise RuntimeError("compiled reference not found: run `make -C oracle ref` first")
     with tempfile.TemporaryDirectory(prefix="dnlref_") as tmp:
@@ -122,6 +124,8 @@ def run_reference(cmd: str, model, *extra, state: Optional[dict] = None, threads
             args += [out] + [str(x) for x in extra]
         env = dict(os.environ, OMP_NUM_THREADS=str(threads), OMP_DYNAMIC="FALSE")
         env.pop("computeInternalForces", None)
+        if strategy is not None:
+            env["computeInternalForces"] = str(int(strategy))
         r = subprocess.run(args, cwd=tmp, env=env, capture_output=True, text=True,
                            timeout=timeout)
         if r.returncode != 0:
