@@ -48,6 +48,8 @@ def workload(name: str, layers: int = 400):
         return meshes.taylor_hex(40, layers), f"taylor_hex_40x40x{layers}"
     if name == "axi":
         return meshes.taylor_axi(20, 200), "taylor_axi_20x200"
+    if name == "hex1pt":  # not the reference's formulation (see meshes.taylor_hex_1pt)
+        return meshes.taylor_hex_1pt(40, layers), f"taylor_hex_1pt_40x40x{layers}"
     raise SystemExit(f"unknown config {name}")
 
 
@@ -61,7 +63,7 @@ def elem_bytes(m) -> float:
     """Compulsory HBM bytes of one k_elem launch: integration-point state read (S, Eps, EpsPlas, p,
     evp, evp^n) and written (S, Eps, EpsPlas, p; evp and evp^n only where plastic, not counted),
     connectivity, element forces written, node coordinates and delta_disp read once."""
-    ns = 6 if m.etype == meshes.ELHEX8N3D else 4
+    ns = 6 if m.dim == 3 else 4
     ncomp = 3 * ns + 3
     per_elem = m.nip * (ncomp * 8 + (3 * ns + 1) * 8) + m.nen * 4 + m.nen * m.dim * 8
     return m.E * per_elem + m.N * 2 * m.dim * 8
@@ -271,11 +273,14 @@ def main_ours(args):
     hbm_peak, peak_src = peak_hbm()
     bytes_per_launch = elem_bytes(model)
     achieved = bytes_per_launch / (elem_ms / elem_n * 1e-3) / 1e9 if elem_n else None
-    traffic = (ELEM_TRAFFIC_BYTES_PER_ELEMENT * model.E) if ELEM_TRAFFIC_BYTES_PER_ELEMENT else None
+    # the measured per-element DRAM traffic is that of the 2x2x2-point hexahedron
+    traffic = (ELEM_TRAFFIC_BYTES_PER_ELEMENT * model.E) if model.etype == meshes.ELHEX8N3D else None
     fp64_peak = dynela.fp64_peak_tflops()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak if achieved else None, "traffic": traffic,
-                "kernel": "k_elem<ElHex8n3D>" if model.etype else "k_elem<ElQua4nAx>",
+                "kernel": {meshes.ELHEX8N3D: "k_elem<ElHex8n3D>", meshes.ELQUA4NAX: "k_elem<ElQua4nAx>",
+                           meshes.ELHEX8N3D_1PT: "k_elem<ElHex8n3D at one point + hourglass>"}
+                          .get(model.etype, "k_elem"),
                 "peak_source": peak_src,
                 "algorithmic_bytes_per_launch": bytes_per_launch,
                 "avg_launch_ms": elem_ms / elem_n if elem_n else None,
@@ -321,11 +326,15 @@ def main_ours(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded generator of the reference Taylor deck's geometry)",
                 "config": {"workload": name, "elements": model.E, "nodes": model.N,
-                           "time_step": "Pulse every 10 increments",
+                           "time_step": ("Pulse" if model.method == meshes.PULSE else "Courant")
+                                        + f" every {model.freq} increments",
+                           "formulation": ("one Gauss point + viscous hourglass control (not the "
+                                           "reference's 2x2x2-point ElHex8n3D)"
+                                           if model.etype == meshes.ELHEX8N3D_1PT else "the reference's"),
                            "window": f"{args.steps} steps from t = {window['time'] * 1e6:.2f} us "
                                      f"(increment {window['increment']}), reached untimed",
                            "l2": "inputs larger than L2 (integration-point state "
-                                 f"{model.E * model.nip * (3 * (4 if model.etype == 0 else 6) + 3) * 8 / 1e6:.0f} MB)",
+                                 f"{model.E * model.nip * (3 * (4 if model.dim == 2 else 6) + 3) * 8 / 1e6:.0f} MB)",
                            "parallelism": f"replicas x{world}"},
                 "gpu_launches": launches, "kernel_time_share": kernel_share,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
@@ -642,7 +651,7 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="hex", choices=["hex", "axi", "batch", "sens", "necking"])
+    ap.add_argument("--config", default="hex", choices=["hex", "hex1pt", "axi", "batch", "sens", "necking"])
     ap.add_argument("--necking-instances", type=int, default=32)
     ap.add_argument("--sens-steps", type=int, default=4000,
                     help="explicit steps of the gradient workload's schedule")

@@ -45,6 +45,10 @@ enum dnl_status {
 #define DNL_ELQUA4N2D 2 /* ElQua4n2D: 4-node plane-strain quad, 2x2 Gauss points (ElementPlane) */
 #define DNL_ELTET4N3D 3 /* ElTet4n3D: 4-node tetrahedron, 1 Gauss point */
 #define DNL_ELTET10N3D 4 /* ElTet10n3D: 10-node tetrahedron, 4 Gauss points (the reference's tables) */
+/* Not a reference element: ElHex8n3D's geometry integrated at its centre only, with
+ * Flanagan-Belytschko viscous hourglass control (dnl_set_hourglass) and a Courant length of
+ * volume / largest face area.  Courant time step only; no sensitivities. */
+#define DNL_ELHEX8N3D_1PT 5
 
 /* time-step methods (Solver::setTimeStepMethod, Solver.C:312-321) */
 #define DNL_COURANT 0
@@ -62,7 +66,8 @@ typedef struct dnl_handle dnl_handle;
 /* Mesh and boundary conditions (Structure::createNode/createElement, attachInitialBC,
  * attachConstantBC).  Node and element order is the reference's Id order. */
 typedef struct {
-  int etype;            /* DNL_ELQUA4NAX, DNL_ELHEX8N3D, DNL_ELQUA4N2D, DNL_ELTET4N3D, DNL_ELTET10N3D */
+  int etype;            /* DNL_ELQUA4NAX, DNL_ELHEX8N3D, DNL_ELQUA4N2D, DNL_ELTET4N3D, DNL_ELTET10N3D,
+                           DNL_ELHEX8N3D_1PT */
   int num_nodes;        /* N */
   int num_elements;     /* E */
   const double *coords; /* N*3, node-major (x, y, z) like Node::coords */
@@ -128,6 +133,11 @@ typedef struct {
 int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_solver_params *sp,
                dnl_handle **out);
 int dnl_destroy(dnl_handle *h);
+/* DNL_ELHEX8N3D_1PT: the viscous hourglass coefficient (default 0.05): the force resisting the
+ * hourglass modes is a_h = coefficient rho c V^(2/3) / 4 times the mode's velocity.  The viscosity
+ * acts on the Chung-Hulbert predicted velocity; its rate 16 coefficient c / V^(1/3) times the
+ * Courant step must stay well below 1 (0.1 diverges on a Taylor bar at safety 0.9). */
+int dnl_set_hourglass(dnl_handle *h, double coefficient);
 
 int dnl_set_state(dnl_handle *h, const dnl_state_view *s);
 int dnl_get_state(dnl_handle *h, dnl_state_view *s);

@@ -55,6 +55,7 @@ struct dnlo {
   double *p, *evp, *detJ, *detJ0;
   double *dN; /* (E, nip, nen, 3) */
   double young, nu, rho, A, B, n;
+  double hourglass; /* etype 5: viscous hourglass coefficient */
   /* materials (Structure::attachMaterialToElements): per material E, nu, rho, hardening law and
    * its parameters / table; material 0 is the one of dnlo_create */
   int nmat;
@@ -136,7 +137,15 @@ static void tet10_tables(dnlo *h)
 
 static void build_tables(dnlo *h)
 {
-  if (h->etype == 3) { /* ElTet4n3D (ElTet4n3D.C:33-57): one point, weight 1/6 */
+  if (h->etype == 5) { /* the one-point hexahedron (not a reference element): the cube's centre */
+    h->weight[0] = 8.0;
+    for (int k = 0; k < 8; k++) {
+      h->Nt[0][k] = 0.125;
+      h->dNxi[0][k][0] = HX_XI[k] * 0.125;
+      h->dNxi[0][k][1] = HX_ETA[k] * 0.125;
+      h->dNxi[0][k][2] = HX_ZETA[k] * 0.125;
+    }
+  } else if (h->etype == 3) { /* ElTet4n3D (ElTet4n3D.C:33-57): one point, weight 1/6 */
     h->weight[0] = 1. / 6.;
     for (int k = 0; k < 4; k++) {
       h->Nt[0][k] = 0.25;
@@ -521,6 +530,54 @@ static double yield_hardening(const dnlo *h, int mi, double evp, double shift)
   }
 }
 
+/* The one-point hexahedron's viscous hourglass forces, Flanagan & Belytschko (Int. J. Numer.
+ * Meth. Eng. 17, 1981): hourglass vectors h_q of the node signs (xi eta, eta zeta, zeta xi,
+ * xi eta zeta) made orthogonal to the linear fields, g_q = h_q - sum_i (h_q . x_i) b_i with b the
+ * centre-point gradients; fe_k -= a_h sum_q g_qk (g_q . v) with a_h = coefficient rho c V^(2/3)/4
+ * on the Current velocities, V = 8 detJ at the centre, c the material's sound speed.  Not a
+ * reference element: this is the restatement of the GPU element's own formulation. */
+static void elem_hourglass(const dnlo *h, long e, double *fe)
+{
+  const long *cn = h->conn + e * 8;
+  const int mi = h->elemMat ? h->elemMat[e] : 0;
+  const double *v = h->fld[h->cur][1];
+  double hs[4][8];
+  for (int k = 0; k < 8; k++) {
+    const int sx = HX_XI[k], sy = HX_ETA[k], sz = HX_ZETA[k];
+    hs[0][k] = sx * sy;
+    hs[1][k] = sy * sz;
+    hs[2][k] = sz * sx;
+    hs[3][k] = sx * sy * sz;
+  }
+  double hx[4][3];
+  for (int q = 0; q < 4; q++)
+    for (int i = 0; i < 3; i++) {
+      double s = 0.;
+      for (int k = 0; k < 8; k++) s += hs[q][k] * h->coords[cn[k] * 3 + i];
+      hx[q][i] = s;
+    }
+  double g[4][8], qv[4][3];
+  for (int q = 0; q < 4; q++) {
+    for (int i = 0; i < 3; i++) qv[q][i] = 0.;
+    for (int k = 0; k < 8; k++) {
+      double s = hs[q][k];
+      for (int i = 0; i < 3; i++) s -= hx[q][i] * DN(h, e, 0, k, i);
+      g[q][k] = s;
+      for (int i = 0; i < 3; i++) qv[q][i] += s * v[cn[k] * 3 + i];
+    }
+  }
+  const double E = h->mE[mi], Nu = h->mNu[mi], rho = h->mRho[mi];
+  const double c = sqrt((E * (1 - Nu)) / (rho * (1 + Nu) * (1 - 2 * Nu)));
+  const double V = h->weight[0] * h->detJ[IPX(h, e, 0)], cv = cbrt(V);
+  const double ah = 0.25 * h->hourglass * rho * c * (cv * cv);
+  for (int k = 0; k < 8; k++)
+    for (int i = 0; i < 3; i++) {
+      double s = 0.;
+      for (int q = 0; q < 4; q++) s += g[q][k] * qv[q][i];
+      fe[k * 3 + i] -= ah * s;
+    }
+}
+
 /* Element::computeStress (Element.C:217-403) followed by Element::computeInternalForces
  * (Element.C:164-214) for one element; writes the element force vector to fe. */
 static int elem_forces(dnlo *h, long e, double *fe)
@@ -626,6 +683,7 @@ static int elem_forces(dnlo *h, long e, double *fe)
     if (h->etype == 0)
       for (int I = 0; I < nen; I++) fe[I * dim] -= (h->Nt[pt][I] * Sig[8] / R) * WxdJ;
   }
+  if (h->etype == 5) elem_hourglass(h, e, fe);
   return err;
 }
 
@@ -724,6 +782,28 @@ static double elem_courant(const dnlo *h, long e)
     const double x31 = x2[0] - x0[0], x24 = x1[0] - x3[0];
     const double y42 = x3[1] - x1[1], y31 = x2[1] - x0[1];
     len = ((x31 * y42 + x24 * y31) / sqrt(2. * ((x24) * (x24) + (y42) * (y42) + (x31) * (x31) + (y31) * (y31))));
+  } else if (h->etype == 5) { /* centre-point volume / largest face area (half |d1 x d2|) */
+    double J[3][3] = {{0., 0., 0.}, {0., 0., 0.}, {0., 0., 0.}};
+    for (int k = 0; k < 8; k++)
+      for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) J[r][c] += h->dNxi[0][k][c] * h->coords[cn[k] * 3 + r];
+    const double V = 8. * (J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) +
+                           J[0][1] * (J[1][2] * J[2][0] - J[1][0] * J[2][2]) +
+                           J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]));
+    static const int F[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}};
+    double a2max = 0.;
+    for (int f = 0; f < 6; f++) {
+      double d1[3], d2[3];
+      for (int i = 0; i < 3; i++) {
+        d1[i] = h->coords[cn[F[f][2]] * 3 + i] - h->coords[cn[F[f][0]] * 3 + i];
+        d2[i] = h->coords[cn[F[f][3]] * 3 + i] - h->coords[cn[F[f][1]] * 3 + i];
+      }
+      const double c0 = d1[1] * d2[2] - d1[2] * d2[1], c1 = d1[2] * d2[0] - d1[0] * d2[2];
+      const double c2 = d1[0] * d2[1] - d1[1] * d2[0];
+      const double a2 = c0 * c0 + c1 * c1 + c2 * c2;
+      if (a2 > a2max) a2max = a2;
+    }
+    len = V / (0.5 * sqrt(a2max));
   } else {
     const double l1 = dist3(x0, x1), l2 = dist3(x0, x2), l3 = dist3(x1, x2);
     const double l4 = dist3(x0, x3), l5 = dist3(x1, x3), l6 = dist3(x2, x3);
@@ -1071,12 +1151,14 @@ dnlo *dnlo_create(int etype, long N, long E, const double *coords, const long *c
                   const double *bc_val, const long *bc_start, const long *bc_nodes,
                   const double *solver)
 {
-  if (etype < 0 || etype > 4 || N <= 0 || E <= 0) return NULL;
+  if (etype < 0 || etype > 5 || N <= 0 || E <= 0) return NULL;
+  if (etype == 5 && (int)solver[4] == 1) return NULL; /* the one-point hexahedron: Courant only */
   dnlo *h = (dnlo *)calloc(1, sizeof(dnlo));
   h->etype = etype;
   h->dim = (etype == 0 || etype == 2) ? 2 : 3;
-  h->nen = etype == 1 ? 8 : (etype == 4 ? 10 : 4);
-  h->nip = etype == 1 ? 8 : (etype == 3 ? 1 : 4);
+  h->nen = (etype == 1 || etype == 5) ? 8 : (etype == 4 ? 10 : 4);
+  h->nip = etype == 1 ? 8 : ((etype == 3 || etype == 5) ? 1 : 4);
+  h->hourglass = 0.05;
   h->N = N;
   h->E = E;
   h->conn = (long *)malloc(sizeof(long) * E * h->nen);
@@ -1248,6 +1330,12 @@ int dnlo_set_materials(dnlo *h, int nmat, const double *props, const long *tab_s
 
 /* Initial velocities per node (BoundarySpeed::applyInitial_V0 on node sets, Boundary.C:378-385):
  * v (N x 3) on both nodal fields. */
+int dnlo_set_hourglass(dnlo *h, double coefficient)
+{
+  h->hourglass = coefficient;
+  return 0;
+}
+
 int dnlo_set_velocity(dnlo *h, const double *v)
 {
   for (long n = 0; n < h->N; n++)
@@ -1347,8 +1435,8 @@ int dnlo_tables(int etype, double *N, double *dN)
   memset(&t, 0, sizeof t);
   t.etype = etype;
   t.dim = (etype == 0 || etype == 2) ? 2 : 3;
-  t.nen = etype == 1 ? 8 : (etype == 4 ? 10 : 4);
-  t.nip = etype == 1 ? 8 : (etype == 3 ? 1 : 4);
+  t.nen = (etype == 1 || etype == 5) ? 8 : (etype == 4 ? 10 : 4);
+  t.nip = etype == 1 ? 8 : ((etype == 3 || etype == 5) ? 1 : 4);
   build_tables(&t);
   for (int pt = 0; pt < t.nip; pt++)
     for (int k = 0; k < t.nen; k++) {

@@ -62,6 +62,8 @@ int dnlo_get_threads(void);
 int dnlo_set_materials(dnlo *h, int nmat, const double *props, const long *tab_start,
                        const double *tab_x, const double *tab_y, const long *elem_mat);
 int dnlo_set_velocity(dnlo *h, const double *v);
+/* etype 5 (the one-point hexahedron, not a reference element): viscous hourglass coefficient */
+int dnlo_set_hourglass(dnlo *h, double coefficient);
 
 #ifdef __cplusplus
 }

@@ -57,6 +57,7 @@ def lib():
         L.dnlo_tables.argtypes = [C.c_int, dp, dp]
         L.dnlo_set_materials.argtypes = [C.c_void_p, C.c_int, dp, lp, dp, dp, lp]
         L.dnlo_set_velocity.argtypes = [C.c_void_p, dp]
+        L.dnlo_set_hourglass.argtypes = [C.c_void_p, C.c_double]
         _lib = L
     return _lib
 
@@ -118,6 +119,8 @@ class Oracle:
         self.L = L
         if getattr(m, "extended", False):
             self._apply_extensions(m)
+        if m.etype == 5:
+            L.dnlo_set_hourglass(self.h, float(m.hourglass))
 
     def _apply_extensions(self, m):
         laws = m.material_laws()

@@ -46,16 +46,20 @@ template <> struct Elem<DNL_ELTET10N3D> {
   static constexpr int DIM = 3, NEN = 10, NIP = 4;
   static constexpr int NS = 6;
 };
+template <> struct Elem<DNL_ELHEX8N3D_1PT> {  // not a reference element (see dnl_gpu.h)
+  static constexpr int DIM = 3, NEN = 8, NIP = 1;
+  static constexpr int NS = 6;
+};
 // the same by run-time element type
-__host__ __device__ constexpr bool etype_valid(int et) { return et >= DNL_ELQUA4NAX && et <= DNL_ELTET10N3D; }
+__host__ __device__ constexpr bool etype_valid(int et) { return et >= DNL_ELQUA4NAX && et <= DNL_ELHEX8N3D_1PT; }
 __host__ __device__ constexpr int etype_dim(int et) { return et == DNL_ELQUA4NAX || et == DNL_ELQUA4N2D ? 2 : 3; }
 __host__ __device__ constexpr int etype_nen(int et)
 {
-  return et == DNL_ELHEX8N3D ? 8 : (et == DNL_ELTET10N3D ? 10 : 4);
+  return (et == DNL_ELHEX8N3D || et == DNL_ELHEX8N3D_1PT) ? 8 : (et == DNL_ELTET10N3D ? 10 : 4);
 }
 __host__ __device__ constexpr int etype_nip(int et)
 {
-  return et == DNL_ELHEX8N3D ? 8 : (et == DNL_ELTET4N3D ? 1 : 4);
+  return et == DNL_ELHEX8N3D ? 8 : ((et == DNL_ELTET4N3D || et == DNL_ELHEX8N3D_1PT) ? 1 : 4);
 }
 __host__ __device__ constexpr int etype_ns(int et) { return etype_dim(et) == 2 ? 4 : 6; }
 // element types with the forward-mode sensitivity path (tape and tangent kernels)
@@ -63,6 +67,12 @@ __host__ __device__ constexpr bool etype_has_sens(int et) { return et <= DNL_ELQ
 // element types whose time-step length is the quad's Courant length (else the tetrahedra's
 // shortest edge; ElHex8n3D has none)
 __host__ __device__ constexpr bool etype_quad(int et) { return et == DNL_ELQUA4NAX || et == DNL_ELQUA4N2D; }
+// Courant length kinds: 0 the quads' (ElQua4nAx::getLength), 1 the tetrahedra's shortest edge,
+// 2 the one-point hexahedron's volume / largest face area
+__host__ __device__ constexpr int etype_length_kind(int et)
+{
+  return etype_quad(et) ? 0 : (et == DNL_ELHEX8N3D_1PT ? 2 : 1);
+}
 
 // The reference's ElTet10n3D tables (ElTet10n3D.C:45-72) as they evaluate: at Gauss point p the
 // barycentric coordinate L_p is beta and the others alpha (p = 0: L0 = 1 - xi - eta - zeta), the
@@ -251,6 +261,8 @@ struct ElemArgs {
   const int *conn;     // [NEN][E]
   double *x[3];        // current coordinates
   const double *du[3]; // Current delta_disp
+  const double *v[3];  // Current mat_speed (the one-point hexahedron's hourglass viscosity)
+  double hourglass;    // its coefficient
   double *ip;          // integration-point state
   double *fe;          // element forces [DIM][E*NEN]
   double *detJ;        // [E*NIP] (written)
@@ -346,6 +358,7 @@ struct dnl_handle {
   // Pulse: per Gauss point J^-1, weight x detJ (x 2 pi R) and R; the iterated vector (raw)
   double *pj, *ev, *kx;
   double C00, C01, C33;       // Hooke matrix entries (Material::getHookeMatrix)
+  double hourglass;           // DNL_ELHEX8N3D_1PT: viscous hourglass coefficient (0.05)
   // time
   dnl::DevTime *tm;
   dnl::Material mat;
@@ -396,7 +409,10 @@ struct dnl_handle {
   } while (0)
 #define DNL_BY_ETYPE(etype, CALL)                    \
   do {                                               \
-    if ((etype) == DNL_ELTET4N3D) {                  \
+    if ((etype) == DNL_ELHEX8N3D_1PT) {              \
+      constexpr int ET = DNL_ELHEX8N3D_1PT;          \
+      CALL;                                          \
+    } else if ((etype) == DNL_ELTET4N3D) {           \
       constexpr int ET = DNL_ELTET4N3D;              \
       CALL;                                          \
     } else if ((etype) == DNL_ELTET10N3D) {          \

@@ -132,10 +132,21 @@ template <> struct Shape<DNL_ELTET10N3D> {
   __device__ __forceinline__ static double N(int pt, int k) { return c_shape.t10N[pt][k]; }
   __device__ __forceinline__ static double dN(int pt, int k, int c) { return c_shape.t10D[pt][k][c]; }
 };
+// The one-point hexahedron (not a reference element): the centre of ElHex8n3D's reference cube,
+// N = 1/8, dN/dxi = (sign of the node's coordinate) / 8, weight 8
+template <> struct Shape<DNL_ELHEX8N3D_1PT> {
+  static constexpr double kWeight = 8.0;
+  __device__ __forceinline__ static double N(int, int) { return 0.125; }
+  __device__ __forceinline__ static double dN(int, int k, int c)
+  {
+    const int s = c == 0 ? sgx(k) : (c == 1 ? sgy(k) : sgz(k));
+    return s ? 0.125 : -0.125;
+  }
+};
 // integration weight x detJ (Element.C:183); the quads' and the hexahedron's weight is 1
 template <int ET> __device__ __forceinline__ double weighted(double detJ)
 {
-  if constexpr (ET == DNL_ELTET4N3D || ET == DNL_ELTET10N3D)
+  if constexpr (ET == DNL_ELTET4N3D || ET == DNL_ELTET10N3D || ET == DNL_ELHEX8N3D_1PT)
     return RMUL(Shape<ET>::kWeight, detJ);
   else
     return detJ;
@@ -850,6 +861,68 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
       if (AXI && i == 0) s = fma(SH::N(pt, k), hoop, s);
       row[k * DIM + i] = s;
     }
+  if constexpr (ET == DNL_ELHEX8N3D_1PT) {
+    // Flanagan-Belytschko viscous hourglass control (Int. J. Numer. Meth. Eng. 17, 1981): the
+    // hourglass vectors h_a of the node signs (xi eta, eta zeta, zeta xi, xi eta zeta), made
+    // orthogonal to the linear fields, gamma_a = h_a - sum_i (h_a . x_i) b_i with b_i the
+    // centre-point gradients; the resisting force f_k = -a_h sum_a gamma_ak (gamma_a . v) with
+    // a_h = coefficient rho c V^(2/3) / 4 on the Current velocities, V = 8 detJ.
+    double hx[4][3];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) hx[q][i] = 0.;
+    auto hsign = [](int q, int k) {
+      const int sx = sgx(k), sy = sgy(k), sz = sgz(k);
+      const int par = q == 0 ? sx ^ sy : (q == 1 ? sy ^ sz : (q == 2 ? sz ^ sx : sx ^ sy ^ sz));
+      return q == 3 ? par : !par;  // +1 where the product of the (+-1) signs is +1
+    };
+#pragma unroll
+    for (int k = 0; k < NEN; k++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const double xk = a.x[i][node[k]];
+#pragma unroll
+        for (int q = 0; q < 4; q++) hx[q][i] += hsign(q, k) ? xk : ineg(xk);
+      }
+    double g[4][NEN], qv[4][3];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) qv[q][i] = 0.;
+#pragma unroll
+    for (int k = 0; k < NEN; k++) {
+      double b[3];
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        double s = 0.;
+#pragma unroll
+        for (int l = 0; l < 3; l++) s = fma(Ji[l][i], SH::dN(pt, k, l), s);
+        b[i] = s;
+      }
+      double vk[3];
+#pragma unroll
+      for (int i = 0; i < 3; i++) vk[i] = a.v[i][node[k]];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const double gq = fma(-hx[q][2], b[2], fma(-hx[q][1], b[1], fma(-hx[q][0], b[0], hsign(q, k) ? 1. : -1.)));
+        g[q][k] = gq;
+#pragma unroll
+        for (int i = 0; i < 3; i++) qv[q][i] = fma(gq, vk[i], qv[q][i]);
+      }
+    }
+    const double V = weighted<ET>(detJ), cv = cbrt(V);
+    const double ah = 0.25 * a.hourglass * m.rho * m.Cs * (cv * cv);
+#pragma unroll
+    for (int k = 0; k < NEN; k++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        double s = 0.;
+#pragma unroll
+        for (int q = 0; q < 4; q++) s = fma(g[q][k], qv[q][i], s);
+        row[k * DIM + i] = fma(ah, s, row[k * DIM + i]);
+      }
+  }
   __syncwarp();
   if (valid) {
     // lane pt assembles node pt of its element (and pt + NIP, ... when NEN > NIP):
@@ -997,14 +1070,50 @@ __global__ void __launch_bounds__(128) k_mass(ElemArgs a, double *me, const int 
 
 // ----------------------------------------------------------------------------- Courant
 // The element's characteristic length with the reference's rounding: ElQua4nAx::getLength /
-// ElQua4n2D::getLength (ElQua4nAx.C:131-143, ElQua4n2D.C:130-143) for the quads, else the
+// ElQua4n2D::getLength (ElQua4nAx.C:131-143, ElQua4n2D.C:130-143) for the quads (KIND 0), the
 // tetrahedra's shortest corner edge (ElTet4n3D.C:151-166, ElTet10n3D.C:140-155; Vec3D::distance,
-// Vec3D.h:380-430, and the Min chain of Math.h:62).
-template <bool QUAD>
+// Vec3D.h:380-430, and the Min chain of Math.h:62) (KIND 1); for the one-point hexahedron, which
+// is not a reference element, its centre-point volume over its largest face area (KIND 2; each
+// face's area half the norm of the cross product of its diagonals).
+template <int KIND>
 __device__ __forceinline__ double elem_length(const ElemArgs &a, int e)
 {
   const int n0 = a.conn[e], n1 = a.conn[a.E + e], n2 = a.conn[2L * a.E + e], n3 = a.conn[3L * a.E + e];
-  if constexpr (QUAD) {
+  if constexpr (KIND == 2) {
+    double X[8][3];
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) X[k][i] = a.x[i][a.conn[(long)k * a.E + e]];
+    double J[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        double s = 0.;
+#pragma unroll
+        for (int k = 0; k < 8; k++) s = fma(Shape<DNL_ELHEX8N3D_1PT>::dN(0, k, c), X[k][r], s);
+        J[r][c] = s;
+      }
+    const double V = 8. * fma(J[0][0], fma(J[1][1], J[2][2], -J[1][2] * J[2][1]),
+                              fma(J[0][1], fma(J[1][2], J[2][0], -J[1][0] * J[2][2]),
+                                  J[0][2] * fma(J[1][0], J[2][1], -J[1][1] * J[2][0])));
+    const int F[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}};
+    double a2max = 0.;  // (2 area)^2
+#pragma unroll
+    for (int f = 0; f < 6; f++) {
+      double d1[3], d2[3];
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        d1[i] = X[F[f][2]][i] - X[F[f][0]][i];
+        d2[i] = X[F[f][3]][i] - X[F[f][1]][i];
+      }
+      const double c0 = fma(d1[1], d2[2], -d1[2] * d2[1]), c1 = fma(d1[2], d2[0], -d1[0] * d2[2]);
+      const double c2 = fma(d1[0], d2[1], -d1[1] * d2[0]);
+      a2max = fmax(a2max, fma(c0, c0, fma(c1, c1, c2 * c2)));
+    }
+    return V / (0.5 * sqrt(a2max));
+  } else if constexpr (KIND == 0) {
     const double x31 = RSUB(a.x[0][n2], a.x[0][n0]), x24 = RSUB(a.x[0][n1], a.x[0][n3]);
     const double y42 = RSUB(a.x[1][n3], a.x[1][n1]), y31 = RSUB(a.x[1][n2], a.x[1][n0]);
     const double num = RADD(RMUL(x31, y42), RMUL(x24, y31));
@@ -1032,14 +1141,14 @@ __device__ __forceinline__ double elem_length(const ElemArgs &a, int e)
 // Min over elements via an unsigned atomicMin on the bit pattern (positive doubles order like
 // their bits).  A non-positive or NaN length is an error: the reference would turn it into a
 // negative or NaN time step.
-template <bool QUAD>
+template <int KIND>
 __global__ void __launch_bounds__(256) k_courant(ElemArgs a)
 {
   if (a.tm->done | a.tm->status) return;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   double len = 1e300;
   if (e < a.E) {
-    len = elem_length<QUAD>(a, e);
+    len = elem_length<KIND>(a, e);
     if (!(len > 0.)) {
       record_error(a.tm, DNL_ERR_DT, e);
       len = 1e300;
@@ -1061,7 +1170,7 @@ __global__ void __launch_bounds__(256) k_courant(ElemArgs a)
 
 // Batched Courant lengths: each element folds its length into its instance's minimum; a warp whose
 // lanes all belong to one instance reduces first and issues one atomic.
-template <bool QUAD>
+template <int KIND>
 __global__ void __launch_bounds__(256) k_courant_batch(ElemArgs a, const int *elemInst, DevTime *tms)
 {
   const int eRaw = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1071,7 +1180,7 @@ __global__ void __launch_bounds__(256) k_courant_batch(ElemArgs a, const int *el
   DevTime *tm = tms + inst;
   double len = 1e300;
   if (eRaw < a.E && !(tm->done | tm->status)) {
-    len = elem_length<QUAD>(a, e);
+    len = elem_length<KIND>(a, e);
     if (!(len > 0.)) {
       record_error(tm, DNL_ERR_DT, e);
       len = 1e300;
@@ -1100,6 +1209,8 @@ static ElemArgs elem_args(dnl_handle *h)
     a.x[r] = h->x[r];
     a.du[r] = h->bank[h->cur].du[r];
   }
+  for (int r = 0; r < 3; r++) a.v[r] = h->bank[h->cur].v[r];
+  a.hourglass = h->hourglass;
   a.ip = h->ip;
   a.fe = h->fe;
   a.detJ = h->detJ;
@@ -1168,12 +1279,16 @@ int launch_mass(dnl_handle *h, cudaStream_t s, double *me)
 int launch_elem_batch(int etype, int block, const ElemArgs &a, const int *elemInst,
                       const Material *mats, DevTime *tms, cudaStream_t s)
 {
-  // the hexahedron's and the 10-node tetrahedron's shared-memory transpose fits 128 threads at most
-  if ((etype == DNL_ELHEX8N3D || etype == DNL_ELTET10N3D) && block > 128) block = 128;
+  // the hexahedra's and the 10-node tetrahedron's shared-memory transpose fits 128 threads at most
+  if ((etype == DNL_ELHEX8N3D || etype == DNL_ELTET10N3D || etype == DNL_ELHEX8N3D_1PT) && block > 128)
+    block = 128;
   const long threads = (long)a.E * etype_nip(etype);
   const int grid = (int)((threads + block - 1) / block);
 #define DNL_EB(ET, B) k_elem_batch<ET, B><<<grid, B, 0, s>>>(a, elemInst, mats, tms)
-  if (etype == DNL_ELTET4N3D) {
+  if (etype == DNL_ELHEX8N3D_1PT) {
+    if (block == 64) DNL_EB(DNL_ELHEX8N3D_1PT, 64);
+    else DNL_EB(DNL_ELHEX8N3D_1PT, 128);
+  } else if (etype == DNL_ELTET4N3D) {
     if (block == 64) DNL_EB(DNL_ELTET4N3D, 64);
     else if (block == 256) DNL_EB(DNL_ELTET4N3D, 256);
     else DNL_EB(DNL_ELTET4N3D, 128);
@@ -1222,10 +1337,13 @@ int launch_mass_batch(int etype, const ElemArgs &a, double *me, const int *elemI
 int launch_courant_batch(int etype, const ElemArgs &a, const int *elemInst, DevTime *tms,
                          cudaStream_t s)
 {
-  if (etype_quad(etype))
-    k_courant_batch<true><<<(a.E + 255) / 256, 256, 0, s>>>(a, elemInst, tms);
+  const int kind = etype_length_kind(etype), grid = (a.E + 255) / 256;
+  if (kind == 0)
+    k_courant_batch<0><<<grid, 256, 0, s>>>(a, elemInst, tms);
+  else if (kind == 1)
+    k_courant_batch<1><<<grid, 256, 0, s>>>(a, elemInst, tms);
   else
-    k_courant_batch<false><<<(a.E + 255) / 256, 256, 0, s>>>(a, elemInst, tms);
+    k_courant_batch<2><<<grid, 256, 0, s>>>(a, elemInst, tms);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
@@ -1236,10 +1354,13 @@ int launch_courant(dnl_handle *h, cudaStream_t s)
 {
   ElemArgs a = elem_args(h);
   prof_begin(h, s);
-  if (etype_quad(h->etype))
-    k_courant<true><<<(h->E + 255) / 256, 256, 0, s>>>(a);
+  const int kind = etype_length_kind(h->etype), grid = (h->E + 255) / 256;
+  if (kind == 0)
+    k_courant<0><<<grid, 256, 0, s>>>(a);
+  else if (kind == 1)
+    k_courant<1><<<grid, 256, 0, s>>>(a);
   else
-    k_courant<false><<<(h->E + 255) / 256, 256, 0, s>>>(a);
+    k_courant<2><<<grid, 256, 0, s>>>(a);
   prof_end(h, DNL_PROF_COURANT, s);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;

@@ -888,6 +888,15 @@ int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, con
   return 0;
 }
 
+int dnl_set_hourglass(dnl_handle *h, double coefficient)
+{
+  if (!h || !(coefficient >= 0.) || coefficient > 1e3) return DNL_ERR_ARG;
+  h->hourglass = coefficient;
+  for (int i = 0; i < h->ngraphs; i++) cudaGraphExecDestroy(h->graphs[i].exec);
+  h->ngraphs = 0;  // captured launches hold the coefficient by value
+  return 0;
+}
+
 int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0)
 {
   if (!h) return DNL_ERR_ARG;
@@ -958,6 +967,8 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
   if (sp->frequency < 1 || !(sp->end_time > 0) || !(sp->safety > 0)) return DNL_ERR_ARG;
   if (sp->method != DNL_COURANT && sp->method != DNL_PULSE) return DNL_ERR_ARG;
   if (sp->method == DNL_COURANT && mesh->etype == DNL_ELHEX8N3D) return DNL_ERR_ARG;  // ElHex8n3D.C:188-192
+  // the one-point hexahedron's stiffness is singular in its hourglass modes: Courant only
+  if (sp->method == DNL_PULSE && mesh->etype == DNL_ELHEX8N3D_1PT) return DNL_ERR_ARG;
   // Node::Current->ro is set only on one NodalField (Domain.C:1088) and the fields swap every step,
   // so a Courant recomputation at an odd increment reads a zero density; the reference would then
   // take a zero time step.  Only even frequencies are accepted with Courant.
@@ -1020,6 +1031,7 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
   h->gamma = 1.5 - h->alphaM;
   h->omegaS = sqrt((12.0 * pow((1 + rb), 3) * (2.0 - rb)) / (10 + 15 * rb - rb * rb + pow(rb, 3) - pow(rb, 4)));
   h->safetyOmega = sp->safety * h->omegaS;
+  h->hourglass = 0.05;
 
   // ---- mesh
   std::vector<int> connT((size_t)nen * E);

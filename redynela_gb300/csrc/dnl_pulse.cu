@@ -67,10 +67,17 @@ template <> __device__ __forceinline__ double pdN<DNL_ELTET10N3D>(int pt, int k,
 {
   return c_pshape.t10D[pt][k][c];
 }
+// the one-point hexahedron's centre (compiled for the dispatch; dnl_create refuses Pulse for it)
+template <> __device__ __forceinline__ double pN<DNL_ELHEX8N3D_1PT>(int, int) { return 0.125; }
+template <> __device__ __forceinline__ double pdN<DNL_ELHEX8N3D_1PT>(int, int k, int c)
+{
+  return (c == 0 ? psgx(k) : (c == 1 ? psgy(k) : psgz(k))) ? 0.125 : -0.125;
+}
 // integration weight (ElTet4n3D.C:33, ElTet10n3D.C:30; the quads and the hexahedron: 1)
 template <int ET> constexpr double pweight()
 {
-  return ET == DNL_ELTET4N3D ? 1. / 6. : (ET == DNL_ELTET10N3D ? 1.0 / 24.0 : 1.0);
+  return ET == DNL_ELTET4N3D ? 1. / 6.
+                             : (ET == DNL_ELTET10N3D ? 1.0 / 24.0 : (ET == DNL_ELHEX8N3D_1PT ? 8.0 : 1.0));
 }
 template <> __device__ __forceinline__ double pN<DNL_ELHEX8N3D>(int pt, int k)
 {

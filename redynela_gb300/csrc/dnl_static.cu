@@ -56,7 +56,8 @@ extern "C" int dnl_internal_forces_static(const dnl_static_args *a, void *stream
   using namespace dnl;
   if (bad_element) *bad_element = -1;
   if (!a) return DNL_ERR_ARG;
-  if (!etype_valid(a->etype)) return DNL_ERR_ARG;
+  // the one-point hexahedron's hourglass viscosity needs nodal velocities this entry does not take
+  if (!etype_valid(a->etype) || a->etype == DNL_ELHEX8N3D_1PT) return DNL_ERR_ARG;
   const int nen = etype_nen(a->etype), dim = etype_dim(a->etype);
   if (a->num_nodes <= 0 || a->num_elements <= 0) return DNL_ERR_ARG;
   if ((long long)a->num_elements * nen * dim > DNL_STATIC_MAX_ELEMENT_DOFS) return DNL_ERR_ARG;

@@ -97,6 +97,7 @@ def lib():
         L.dnl_create.argtypes = [C.POINTER(MeshDesc), C.POINTER(MaterialDesc),
                                  C.POINTER(SolverParams), C.POINTER(H)]
         L.dnl_destroy.argtypes = [H]
+        L.dnl_set_hourglass.argtypes = [H, C.c_double]
         L.dnl_set_state.argtypes = [H, C.POINTER(StateView)]
         L.dnl_get_state.argtypes = [H, C.POINTER(StateView)]
         L.dnl_get_step_tensors.argtypes = [H, _dp, _dp]
@@ -236,6 +237,12 @@ class GpuDomain:
             self.set_materials(m.material_laws(), m.elem_material)
         if m.initial_velocity is not None:
             self.set_state(v=np.asarray(m.initial_velocity, dtype=np.float64))
+        if m.etype == meshes.ELHEX8N3D_1PT:
+            self.set_hourglass(m.hourglass)
+
+    def set_hourglass(self, coefficient: float) -> None:
+        """dnl_set_hourglass: the one-point hexahedron's viscous hourglass coefficient."""
+        self._check(self.L.dnl_set_hourglass(self.h, float(coefficient)))
 
     def set_materials(self, laws, elem_material=None) -> None:
         """dnl_set_materials: materials with their hardening laws, one per element."""
@@ -716,6 +723,7 @@ ElHex8n3D = meshes.ELHEX8N3D
 ElQua4n2D = meshes.ELQUA4N2D
 ElTet4n3D = meshes.ELTET4N3D
 ElTet10n3D = meshes.ELTET10N3D
+ElHex8n3D_1PT = meshes.ELHEX8N3D_1PT
 
 
 class Structure:

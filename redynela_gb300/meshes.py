@@ -32,6 +32,8 @@ ELHEX8N3D = 1
 ELQUA4N2D = 2  # plane strain
 ELTET4N3D = 3
 ELTET10N3D = 4
+# not a reference element: ElHex8n3D at its centre with viscous hourglass control
+ELHEX8N3D_1PT = 5
 
 COURANT = 0
 PULSE = 1
@@ -101,6 +103,8 @@ class Model:
     elem_material: Optional[np.ndarray] = None
     # initial velocity per node (attachInitialBC on node sets), (N, 3); None = v0 everywhere
     initial_velocity: Optional[np.ndarray] = None
+    # ELHEX8N3D_1PT only: the viscous hourglass coefficient
+    hourglass: float = 0.05
 
     def material_laws(self) -> List[MaterialLaw]:
         if self.materials:
@@ -127,11 +131,11 @@ class Model:
 
     @property
     def nen(self) -> int:
-        return {ELHEX8N3D: 8, ELTET10N3D: 10}.get(self.etype, 4)
+        return {ELHEX8N3D: 8, ELTET10N3D: 10, ELHEX8N3D_1PT: 8}.get(self.etype, 4)
 
     @property
     def nip(self) -> int:
-        return {ELHEX8N3D: 8, ELTET4N3D: 1}.get(self.etype, 4)
+        return {ELHEX8N3D: 8, ELTET4N3D: 1, ELHEX8N3D_1PT: 1}.get(self.etype, 4)
 
 
 def taylor_axi(nr: int = 5, nz: int = 50, radius: float = 3.2e-3, length: float = 32.4e-3,
@@ -247,6 +251,13 @@ def taylor_tet(ncross: int = 8, nz: int = 24, quadratic: bool = False, safety: f
     bcs = [BCGroup(RESTRAIN, (0.0, 0.0, 1.0), base)]
     return dataclasses.replace(m, etype=etype, coords=coords, conn=conn.astype(np.int64), bcs=bcs,
                                method=COURANT)
+
+
+def taylor_hex_1pt(ncross: int = 40, nz: int = 400, hourglass: float = 0.05, **kw) -> Model:
+    """taylor_hex's bar and boundary conditions on the one-point hexahedron with viscous hourglass
+    control (ELHEX8N3D_1PT, not a reference element), Courant time step."""
+    return dataclasses.replace(taylor_hex(ncross, nz, **kw), etype=ELHEX8N3D_1PT, method=COURANT,
+                               hourglass=hourglass)
 
 
 def tabular_table(A: float, B: float, n: float, step: float = 0.1, stop: float = 10.0):

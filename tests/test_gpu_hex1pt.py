@@ -1,0 +1,105 @@
+"""The one-point hexahedron with viscous hourglass control (DNL_ELHEX8N3D_1PT, not a reference
+element) on the GPU against the oracle's restatement of the same formulation: one element pass
+from identical states (1e-12), trajectories (1e-12 for the first steps, then 1e-7: the 3D Jacobi
+pivot sensitivity described in test_steps_hex_pulse), a full Taylor run (final positions 1e-6),
+batches, and the calls it refuses."""
+
+import dataclasses
+
+import numpy as np
+import pytest
+
+from oracle import states
+from oracle.oracle import Oracle
+from redynela_gb300 import meshes
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a).ravel(), np.asarray(b).ravel()
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / nb if nb > 0 else np.linalg.norm(a - b)
+
+
+@pytest.mark.parametrize("seed", [51, 52])
+def test_forces_random_states_vs_oracle(gpu_lib, seed):
+    m = meshes.taylor_hex_1pt(10, 16)
+    st = states.random_state(m, seed=seed)
+    o = Oracle(m)
+    o.inject(**st)
+    o.internal_matrices()
+    fo = o.internal_forces()
+    d = gpu_lib.GpuDomain(m)
+    d.set_state(S=st["S"], Eps=st["Eps"], EpsPlas=st["EpsPlas"], p=st["p"], evp=st["evp"],
+                v=st["v"])
+    f = d.internal_forces(coords=st["coords"], du=st["du"], dt=st["dt"])
+    assert rel(f, fo) <= 1e-12
+    out = d.get_state("S", "EpsPlas", "evp", "p")
+    for k in out:
+        assert rel(out[k], o.array(k)) <= 1e-12, k
+
+
+def test_hourglass_coefficient_reaches_the_kernel(gpu_lib):
+    m = meshes.taylor_hex_1pt(6, 8)
+    st = states.random_state(m, seed=53)
+    out = []
+    for c in (0.0, 0.05, 0.1):
+        d = gpu_lib.GpuDomain(m)
+        d.set_hourglass(c)
+        d.set_state(S=st["S"], Eps=st["Eps"], EpsPlas=st["EpsPlas"], p=st["p"], evp=st["evp"],
+                    v=st["v"])
+        out.append(d.internal_forces(coords=st["coords"], du=st["du"], dt=st["dt"]))
+    h1, h2 = out[1] - out[0], out[2] - out[0]
+    assert np.linalg.norm(h1) > 0
+    assert rel(h2, 2 * h1) <= 1e-9
+
+
+def test_steps_vs_oracle(gpu_lib):
+    m = meshes.taylor_hex_1pt(10, 16)
+    o = Oracle(m)
+    o.prologue()
+    d = gpu_lib.GpuDomain(m)
+    d.prologue()
+    assert rel(d.get_state("mass")["mass"], o.array("mass")) <= 1e-15
+    assert abs(d.time_step() - o.get("dt")) <= 1e-14 * o.get("dt")
+    for k in range(60):
+        o.steps(1)
+        assert d.step(1) == 1
+        assert rel(d.fint(), o.array("fint")) <= (1e-12 if k < 3 else 1e-7), k
+
+
+def test_full_run_vs_oracle(gpu_lib):
+    m = meshes.taylor_hex_1pt(8, 12)
+    o = Oracle(m)
+    o.prologue()
+    n_o = o.steps(10 ** 9)
+    d = gpu_lib.GpuDomain(m)
+    n = d.run()
+    info = d.time_info()
+    assert info["done"] == 1 and info["status"] == 0
+    assert abs(n - n_o) <= 2
+    x, xo = d.get_state("coords")["coords"].ravel(), o.array("coords")
+    assert np.max(np.abs(x - xo)) <= 1e-6 * np.max(np.abs(xo))
+
+
+def test_batch_matches_single_meshes_bitwise(gpu_lib):
+    models = [meshes.taylor_hex_1pt(6, 10, speed=180.0), meshes.taylor_hex_1pt(8, 12),
+              meshes.taylor_hex_1pt(7, 9, speed=260.0, A=120e6)]
+    b = gpu_lib.BatchDomain(models)
+    b.prologue()
+    assert b.step(50) == len(models)
+    for i, m in enumerate(models):
+        d = gpu_lib.GpuDomain(m)
+        assert d.step(50) == 50
+        assert np.array_equal(b.coords(i), d.get_state("coords")["coords"]), i
+
+
+def test_refused_calls(gpu_lib):
+    with pytest.raises(RuntimeError):  # Pulse: the stiffness is singular in the hourglass modes
+        gpu_lib.GpuDomain(dataclasses.replace(meshes.taylor_hex_1pt(4, 4), method=meshes.PULSE))
+    d = gpu_lib.GpuDomain(meshes.taylor_hex_1pt(4, 4))
+    with pytest.raises(RuntimeError):
+        d.sensitivities(np.full(3, 1e-8))
+    with pytest.raises(RuntimeError):
+        d.set_hourglass(-1.0)
