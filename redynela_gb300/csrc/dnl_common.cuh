@@ -392,6 +392,28 @@ struct dnl_handle {
   void *sens;
 };
 
+// 1/x by Newton-Raphson (r <- r + r (1 - x r), quadratic convergence) from the PTX hardware seed
+// rcp.approx.ftz.f64; two steps give the double result to about an ulp (not correctly rounded).
+// For normal, finite, non-zero x.
+__device__ __forceinline__ double nr_rcp(double x)
+{
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}
+
+// a / b from r = nr_rcp(b) and one residual correction (q0 = a r, q = q0 + (a - q0 b) r; Markstein's
+// sequence): the correctly rounded quotient but in rare hard cases, 3 FP64 instructions where an
+// IEEE division takes 17
+__device__ __forceinline__ double quot(double a, double b, double r)
+{
+  const double q0 = a * r;
+  return fma(fma(-q0, b, a), r, q0);
+}
+
 // CALL instantiated for the handle's element type, as ET (CALL in parentheses when it has commas):
 // DNL_BY_ETYPE over every element type, DNL_BY_ETYPE_SENS over those with the sensitivity path
 #define DNL_BY_ETYPE_SENS(etype, CALL)               \

@@ -81,14 +81,18 @@ __device__ __forceinline__ void apply_bc(int code, const double *spd, double dt,
   }
 }
 
-// one node of the Chung-Hulbert update; dt and the integration constants of its mesh
+// one node of the Chung-Hulbert update; dt and the integration constants of its mesh.  In 2D the
+// third components of the nodal fields stay 0 (nothing writes them), so only DIM are read and
+// written.  The two divisions of the corrector, F/M and (. - alphaM a)/(1 - alphaM), go through
+// a reciprocal and one residual correction (quot): the FP64 pipe bounds this kernel too.
 template <int DIM>
 __device__ __forceinline__ void node_update(const NodeArgs &g, int n, double dt, double alphaM,
                                             double beta, double gamma)
 {
-  double cdu[3], cv[3], ca[3], cd[3], ndu[3], nv[3], na[3], nd[3];
+  double cdu[3] = {0., 0., 0.}, cv[3] = {0., 0., 0.}, ca[3] = {0., 0., 0.}, cd[3] = {0., 0., 0.};
+  double ndu[3] = {0., 0., 0.}, nv[3] = {0., 0., 0.}, na[3] = {0., 0., 0.}, nd[3] = {0., 0., 0.};
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
+  for (int i = 0; i < DIM; i++) {
     cdu[i] = g.cur.du[i][n];
     cv[i] = g.cur.v[i][n];
     ca[i] = g.cur.a[i][n];
@@ -97,7 +101,7 @@ __device__ __forceinline__ void node_update(const NodeArgs &g, int n, double dt,
   // computePredictions
   const double c1 = RMUL(dt, RSUB(0.5, beta)), c2 = RMUL(dt, RSUB(1., gamma));
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
+  for (int i = 0; i < DIM; i++) {
     ndu[i] = RMUL(RADD(RMUL(ca[i], c1), cv[i]), dt);
     nd[i] = RADD(cd[i], ndu[i]);
     nv[i] = RADD(RMUL(ca[i], c2), cv[i]);
@@ -125,21 +129,21 @@ __device__ __forceinline__ void node_update(const NodeArgs &g, int n, double dt,
     for (int c = 0; c < DIM; c++) g.fint[(long)n * DIM + c] = f[c];
   }
   // explicitSolve
-  const double m = g.mass[n];
+  const double m = g.mass[n], rm = nr_rcp(m);
 #pragma unroll
-  for (int c = 0; c < DIM; c++) na[c] = f[c] / m;
+  for (int c = 0; c < DIM; c++) na[c] = quot(f[c], m, rm);
   const double cg = RMUL(dt, gamma), cb = RMUL(RMUL(dt, dt), beta);
-  const double oma = RSUB(1.0, alphaM);
+  const double oma = RSUB(1.0, alphaM), roma = nr_rcp(oma);
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
+  for (int i = 0; i < DIM; i++) {
     na[i] = RSUB(na[i], RMUL(alphaM, ca[i]));
-    na[i] = na[i] / oma;
+    na[i] = quot(na[i], oma, roma);
     nv[i] = RADD(nv[i], RMUL(cg, na[i]));
     ndu[i] = RADD(ndu[i], RMUL(cb, na[i]));
   }
   if (bc >= 0) apply_bc(code, spd, dt, cdu, ndu, cv, nv, ca, na);
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
+  for (int i = 0; i < DIM; i++) {
     nd[i] = RADD(cd[i], ndu[i]);
     g.nxt.du[i][n] = ndu[i];
     g.nxt.v[i][n] = nv[i];

@@ -97,10 +97,12 @@ __global__ void __launch_bounds__(256) k_node_tan(SensNodeArgs g)
   const double alphaM = g.nodeInst ? g.prm[inst].alphaM : g.alphaM;
   const double beta = g.nodeInst ? g.prm[inst].beta : g.beta;
   const double gamma = g.nodeInst ? g.prm[inst].gamma : g.gamma;
+  // 2D: the third components stay 0 and are neither read nor written
   const long N = g.N, base = (long)dir * 3 * N;
-  double cdu[3], cv[3], ca[3], cd[3], ndu[3], nv[3], na[3];
+  double cdu[3] = {0., 0., 0.}, cv[3] = {0., 0., 0.}, ca[3] = {0., 0., 0.}, cd[3] = {0., 0., 0.};
+  double ndu[3] = {0., 0., 0.}, nv[3] = {0., 0., 0.}, na[3] = {0., 0., 0.};
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
+  for (int i = 0; i < DIM; i++) {
     cdu[i] = g.cur[0][base + i * N + n];
     cv[i] = g.cur[1][base + i * N + n];
     ca[i] = g.cur[2][base + i * N + n];
@@ -109,7 +111,7 @@ __global__ void __launch_bounds__(256) k_node_tan(SensNodeArgs g)
   (void)cdu;
   const double c1 = dt * (0.5 - beta), c2 = dt * (1. - gamma);
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
+  for (int i = 0; i < DIM; i++) {
     ndu[i] = (ca[i] * c1 + cv[i]) * dt;
     nv[i] = ca[i] * c2 + cv[i];
     na[i] = 0.;
@@ -128,19 +130,20 @@ __global__ void __launch_bounds__(256) k_node_tan(SensNodeArgs g)
 #pragma unroll
     for (int c = 0; c < DIM; c++) f[c] += __ldg(fe + (long)c * g.EN + ent);
   }
-  const double m = g.mass[n];
+  // the tangents need no correctly rounded quotients: reciprocals (nr_rcp) times the numerators
+  const double rm = nr_rcp(g.mass[n]);
 #pragma unroll
-  for (int c = 0; c < DIM; c++) na[c] = f[c] / m;
-  const double cg = dt * gamma, cb = dt * dt * beta, oma = 1. - alphaM;
+  for (int c = 0; c < DIM; c++) na[c] = f[c] * rm;
+  const double cg = dt * gamma, cb = dt * dt * beta, roma = nr_rcp(1. - alphaM);
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
-    na[i] = (na[i] - alphaM * ca[i]) / oma;
+  for (int i = 0; i < DIM; i++) {
+    na[i] = (na[i] - alphaM * ca[i]) * roma;
     nv[i] = fma(cg, na[i], nv[i]);
     ndu[i] = fma(cb, na[i], ndu[i]);
     if ((code >> (2 * i)) & 3) na[i] = nv[i] = ndu[i] = 0.;
   }
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
+  for (int i = 0; i < DIM; i++) {
     const long o = base + i * N + n;
     g.nxt[0][o] = ndu[i];
     g.nxt[1][o] = nv[i];
