@@ -834,92 +834,113 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
       }
       M[l][i] = s * W;
     }
-  double *row = red + pt * (NEN * DIM);
+  if constexpr (NEN == NIP) {
+    // lane k assembles node k: Fe_k = -sum over Gauss points q of dN_k(q) . M(q) (+ the hoop
+    // term), with every point's M (and hoop) exchanged through the element's shared memory
+    constexpr int ST = DIM * DIM + (AXI ? 1 : 0);
+    double *mine = red + pt * ST;
 #pragma unroll
-  for (int k = 0; k < NEN; k++)
+    for (int l = 0; l < DIM; l++)
 #pragma unroll
-    for (int i = 0; i < DIM; i++) {
-      double s = 0.;
+      for (int i = 0; i < DIM; i++) mine[l * DIM + i] = M[l][i];
+    if (AXI) mine[DIM * DIM] = hoop;
+    __syncwarp();
+    if (valid) {
+      // each dN_k(q) (a lane-dependent table lookup) once, for all DIM components
+      double s[DIM];
 #pragma unroll
-      for (int l = 0; l < DIM; l++) s = fma(SH::dN(pt, k, l), M[l][i], s);
-      if (AXI && i == 0) s = fma(SH::N(pt, k), hoop, s);
-      row[k * DIM + i] = s;
+      for (int i = 0; i < DIM; i++) s[i] = 0.0;
+#pragma unroll
+      for (int q = 0; q < NIP; q++) {
+        const double *Mq = red + q * ST;
+#pragma unroll
+        for (int l = 0; l < DIM; l++) {
+          const double d = SH::dN(q, pt, l);
+#pragma unroll
+          for (int i = 0; i < DIM; i++) s[i] = fma(d, Mq[l * DIM + i], s[i]);
+        }
+        if (AXI) s[0] = fma(SH::N(q, pt), Mq[DIM * DIM], s[0]);
+      }
+#pragma unroll
+      for (int i = 0; i < DIM; i++) a.fe[(long)i * a.E * NEN + (long)e * NEN + pt] = ineg(s[i]);
     }
-  if constexpr (ET == DNL_ELHEX8N3D_1PT) {
-    // Flanagan-Belytschko viscous hourglass control (Int. J. Numer. Meth. Eng. 17, 1981): the
-    // hourglass vectors h_a of the node signs (xi eta, eta zeta, zeta xi, xi eta zeta), made
-    // orthogonal to the linear fields, gamma_a = h_a - sum_i (h_a . x_i) b_i with b_i the
-    // centre-point gradients; the resisting force f_k = -a_h sum_a gamma_ak (gamma_a . v) with
-    // a_h = coefficient rho c V^(2/3) / 4 on the Current velocities, V = 8 detJ.
-    double hx[4][3];
-#pragma unroll
-    for (int q = 0; q < 4; q++)
-#pragma unroll
-      for (int i = 0; i < 3; i++) hx[q][i] = 0.;
-    auto hsign = [](int q, int k) {
-      const int sx = sgx(k), sy = sgy(k), sz = sgz(k);
-      const int par = q == 0 ? sx ^ sy : (q == 1 ? sy ^ sz : (q == 2 ? sz ^ sx : sx ^ sy ^ sz));
-      return q == 3 ? par : !par;  // +1 where the product of the (+-1) signs is +1
-    };
+  } else {
+    double *row = red + pt * (NEN * DIM);
 #pragma unroll
     for (int k = 0; k < NEN; k++)
-#pragma unroll
-      for (int i = 0; i < 3; i++) {
-        const double xk = a.x[i][node[k]];
-#pragma unroll
-        for (int q = 0; q < 4; q++) hx[q][i] += hsign(q, k) ? xk : ineg(xk);
-      }
-    double g[4][NEN], qv[4][3];
-#pragma unroll
-    for (int q = 0; q < 4; q++)
-#pragma unroll
-      for (int i = 0; i < 3; i++) qv[q][i] = 0.;
-#pragma unroll
-    for (int k = 0; k < NEN; k++) {
-      double b[3];
-#pragma unroll
-      for (int i = 0; i < 3; i++) {
-        double s = 0.;
-#pragma unroll
-        for (int l = 0; l < 3; l++) s = fma(Ji[l][i], SH::dN(pt, k, l), s);
-        b[i] = s;
-      }
-      double vk[3];
-#pragma unroll
-      for (int i = 0; i < 3; i++) vk[i] = a.v[i][node[k]];
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const double gq = fma(-hx[q][2], b[2], fma(-hx[q][1], b[1], fma(-hx[q][0], b[0], hsign(q, k) ? 1. : -1.)));
-        g[q][k] = gq;
-#pragma unroll
-        for (int i = 0; i < 3; i++) qv[q][i] = fma(gq, vk[i], qv[q][i]);
-      }
-    }
-    const double V = weighted<ET>(detJ), cv = cbrt(V);
-    const double ah = 0.25 * a.hourglass * m.rho * m.Cs * (cv * cv);
-#pragma unroll
-    for (int k = 0; k < NEN; k++)
-#pragma unroll
-      for (int i = 0; i < 3; i++) {
-        double s = 0.;
-#pragma unroll
-        for (int q = 0; q < 4; q++) s = fma(g[q][k], qv[q][i], s);
-        row[k * DIM + i] = fma(ah, s, row[k * DIM + i]);
-      }
-  }
-  __syncwarp();
-  if (valid) {
-    // lane pt assembles node pt of its element (and pt + NIP, ... when NEN > NIP):
-    // Fe = - sum over Gauss points
-    if constexpr (NEN == NIP) {
 #pragma unroll
       for (int i = 0; i < DIM; i++) {
-        double s = 0.0;
+        double s = 0.;
 #pragma unroll
-        for (int q = 0; q < NIP; q++) s -= red[q * (NEN * DIM) + pt * DIM + i];
-        a.fe[(long)i * a.E * NEN + (long)e * NEN + pt] = s;
+        for (int l = 0; l < DIM; l++) s = fma(SH::dN(pt, k, l), M[l][i], s);
+        if (AXI && i == 0) s = fma(SH::N(pt, k), hoop, s);
+        row[k * DIM + i] = s;
       }
-    } else {
+    if constexpr (ET == DNL_ELHEX8N3D_1PT) {
+      // Flanagan-Belytschko viscous hourglass control (Int. J. Numer. Meth. Eng. 17, 1981): the
+      // hourglass vectors h_a of the node signs (xi eta, eta zeta, zeta xi, xi eta zeta), made
+      // orthogonal to the linear fields, gamma_a = h_a - sum_i (h_a . x_i) b_i with b_i the
+      // centre-point gradients; the resisting force f_k = -a_h sum_a gamma_ak (gamma_a . v) with
+      // a_h = coefficient rho c V^(2/3) / 4 on the Current velocities, V = 8 detJ.
+      double hx[4][3];
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) hx[q][i] = 0.;
+      auto hsign = [](int q, int k) {
+        const int sx = sgx(k), sy = sgy(k), sz = sgz(k);
+        const int par = q == 0 ? sx ^ sy : (q == 1 ? sy ^ sz : (q == 2 ? sz ^ sx : sx ^ sy ^ sz));
+        return q == 3 ? par : !par;  // +1 where the product of the (+-1) signs is +1
+      };
+#pragma unroll
+      for (int k = 0; k < NEN; k++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const double xk = a.x[i][node[k]];
+#pragma unroll
+          for (int q = 0; q < 4; q++) hx[q][i] += hsign(q, k) ? xk : ineg(xk);
+        }
+      double g[4][NEN], qv[4][3];
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) qv[q][i] = 0.;
+#pragma unroll
+      for (int k = 0; k < NEN; k++) {
+        double b[3];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          double s = 0.;
+#pragma unroll
+          for (int l = 0; l < 3; l++) s = fma(Ji[l][i], SH::dN(pt, k, l), s);
+          b[i] = s;
+        }
+        double vk[3];
+#pragma unroll
+        for (int i = 0; i < 3; i++) vk[i] = a.v[i][node[k]];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const double gq = fma(-hx[q][2], b[2], fma(-hx[q][1], b[1], fma(-hx[q][0], b[0], hsign(q, k) ? 1. : -1.)));
+          g[q][k] = gq;
+#pragma unroll
+          for (int i = 0; i < 3; i++) qv[q][i] = fma(gq, vk[i], qv[q][i]);
+        }
+      }
+      const double V = weighted<ET>(detJ), cv = cbrt(V);
+      const double ah = 0.25 * a.hourglass * m.rho * m.Cs * (cv * cv);
+#pragma unroll
+      for (int k = 0; k < NEN; k++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          double s = 0.;
+#pragma unroll
+          for (int q = 0; q < 4; q++) s = fma(g[q][k], qv[q][i], s);
+          row[k * DIM + i] = fma(ah, s, row[k * DIM + i]);
+        }
+    }
+    __syncwarp();
+    if (valid) {
+      // lane pt assembles nodes pt, pt + NIP, ...: Fe = - sum over Gauss points of the rows
 #pragma unroll
       for (int j = 0; j < (NEN + NIP - 1) / NIP; j++) {
         const int k = pt + j * NIP;

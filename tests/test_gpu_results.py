@@ -71,3 +71,30 @@ def test_writing_needs_the_step_tensors(gpu_lib, tmp_path):
     d.step(2)
     with pytest.raises(gpu_lib.DnlError):
         d.write_results(str(tmp_path / "x.bin"))
+
+
+@pytest.mark.parametrize("model", [lambda: meshes.taylor_plane(4, 12), lambda: meshes.taylor_tet(4, 6),
+                                   lambda: meshes.taylor_hex_1pt(4, 6)],
+                         ids=["ElQua4n2D", "ElTet4n3D", "ElHex8n3D_1pt"])
+def test_round_trip_other_elements(gpu_lib, tmp_path, model):
+    """A file written by one handle and read into another, for the other element types: the nodal
+    state comes back bit for bit and the next element pass agrees to the parity tolerance."""
+    m = model()
+    d = gpu_lib.GpuDomain(m, flags=gpu_lib.FLAG_STEP_TENSORS)
+    d.step(9)
+    path = str(tmp_path / "w.bin")
+    d.write_results(path)
+    parsed = gpu_lib.parse_results(path, m.N, m.E * m.nip)
+    e = gpu_lib.GpuDomain(m, flags=gpu_lib.FLAG_STEP_TENSORS)
+    e.read_results(path)
+    s1 = d.get_state("coords", "du", "v", "a", "disp", "p", "evp")
+    s2 = e.get_state("coords", "du", "v", "a", "disp", "p", "evp")
+    for k in s1:
+        assert np.array_equal(np.ravel(s1[k]), np.ravel(s2[k])), k
+        if k in parsed:
+            assert np.array_equal(np.ravel(parsed[k]), np.ravel(s1[k])), k
+    x, du = s1["coords"], s1["du"]
+    f1 = d.internal_forces(coords=x, du=du, dt=d.time_info()["time_step"])
+    f2 = e.internal_forces(coords=x, du=du, dt=d.time_info()["time_step"])
+    assert rel(f2, f1) <= TOL
+    assert e.step(5) == 5
