@@ -20,13 +20,11 @@
 // Rounding: GB300 executes FP64 at a small fraction of its other rates, so the kernels are written
 // to minimise FP64 instructions with explicit fused multiply-adds (this file is compiled with
 // -fmad=false: the compiler fuses nothing by itself, so every instantiation of the element code --
-// single mesh, batch, tape, caller-allocated -- rounds identically) -- except along the chain
-// whose last bits decide the strain increment: F = I + sum dN du is accumulated onto 1 with
-// separately rounded products and sums and C = F^T F uses __dmul_rn/__dadd_rn in the reference's
-// association order, so the matrix whose eigenvalues enter ln(U) carries the reference's
-// rounding; the Jacobi rotations then move the eigenvalues by a few ulps of 1 against the
-// reference's (see jacobi_rotate).  Elsewhere results differ from the reference by a few units in
-// the last place.
+// single mesh, batch, tape, caller-allocated -- rounds identically) -- except in C = F^T F, which
+// uses __dmul_rn/__dadd_rn in the reference's association order (F itself is formed as
+// I + G_u J^-1, its diagonal sums added to 1 last); the Jacobi rotations then move the eigenvalues
+// by a few ulps of 1 against the reference's (see jacobi_rotate).  Elsewhere results differ from
+// the reference by a few units in the last place; the parity tests hold them to 1e-12 per pass.
 #include <cstdio>
 #include <cstring>
 
@@ -403,44 +401,38 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     tape(TL::RAD, Rad);
   }
 
-  // ---- F = I + sum_k dN_k (x) du_k (Current field), diagonal accumulated onto 1 in node order
+  // ---- F = I + sum_k du_k (x) dN_k = I + G_u J^-1 with G_u = sum_k du_k (x) dN/dxi_k (Current
+  // field): DIM^2 (NEN + DIM) FP64 instructions instead of DIM^2 (2 NEN) forming each node's
+  // physical gradient first; the diagonal's sum is added to 1 last
   double F[3][3] = {{1., 0., 0.}, {0., 1., 0.}, {0., 0., 1.}};
   double vR = 0.;
-  double GU[DIM][DIM];  // tape only: sum_k du_k (x) dN/dxi_k
+  double GU[DIM][DIM];
 #pragma unroll
   for (int r = 0; r < DIM; r++)
 #pragma unroll
     for (int l = 0; l < DIM; l++) GU[r][l] = 0.;
 #pragma unroll
   for (int k = 0; k < NEN; k++) {
-    double dNk[DIM];
-#pragma unroll
-    for (int c = 0; c < DIM; c++) {
-      double s = 0.;
-#pragma unroll
-      for (int l = 0; l < DIM; l++) s = fma(Ji[l][c], SH::dN(pt, k, l), s);
-      dNk[c] = s;
-    }
     double uk[DIM];
 #pragma unroll
     for (int r = 0; r < DIM; r++) uk[r] = a.du[r][node[k]];
 #pragma unroll
-    for (int r = 0; r < DIM; r++)
+    for (int l = 0; l < DIM; l++) {
+      const double d = SH::dN(pt, k, l);
 #pragma unroll
-      for (int c = 0; c < DIM; c++) {
-        if (r == c)
-          F[r][c] = RADD(F[r][c], RMUL(dNk[c], uk[r]));
-        else
-          F[r][c] = fma(dNk[c], uk[r], F[r][c]);
-      }
-    if (TAPE) {
-#pragma unroll
-      for (int r = 0; r < DIM; r++)
-#pragma unroll
-        for (int l = 0; l < DIM; l++) GU[r][l] = fma(uk[r], SH::dN(pt, k, l), GU[r][l]);
+      for (int r = 0; r < DIM; r++) GU[r][l] = fma(uk[r], d, GU[r][l]);
     }
     if (AXI) vR = fma(SH::N(pt, k), uk[0], vR);
   }
+#pragma unroll
+  for (int r = 0; r < DIM; r++)
+#pragma unroll
+    for (int c = 0; c < DIM; c++) {
+      double s = 0.;
+#pragma unroll
+      for (int l = 0; l < DIM; l++) s = fma(GU[r][l], Ji[l][c], s);
+      F[r][c] = r == c ? RADD(1.0, s) : s;
+    }
   // hoop stretch u_r / R by a reciprocal and one residual correction (quot)
   double vRR = 0.;
   if (AXI) {
