@@ -116,6 +116,22 @@ template <> struct Shape<DNL_ELHEX8N3D> {
   }
 };
 
+// Edges of the quads and of the hexahedron along each reference axis (NE / DIM per axis, axis c
+// first), as (lo, hi) local nodes with hi on the + side of the axis; lo and hi packed 4 bits per
+// edge for run-time indices.  At a Gauss point the bilinear/trilinear dN/dxi_c of the two nodes of
+// an edge are opposite, so sum_k dN_k/dxi_c v_k = sum over the axis-c edges of w (v_hi - v_lo),
+// w the table value for the number of sign disagreements between the edge's other coordinates
+// and the point's (Shape::dN).
+template <int ET> struct Edges {
+  static constexpr int NE = 4;  // quads: xi edges 0-1, 3-2; eta edges 0-3, 1-2
+  static constexpr unsigned long long LO = 0x1030ull, HI = 0x2321ull;
+};
+template <> struct Edges<DNL_ELHEX8N3D> {
+  static constexpr int NE = 12;  // xi: 0-1 3-2 4-5 7-6; eta: 0-3 1-2 4-7 5-6; zeta: 0-4 1-5 2-6 3-7
+  static constexpr unsigned long long LO = 0x321054107430ull, HI = 0x765467236521ull;
+};
+__host__ __device__ constexpr int edge_node(unsigned long long packed, int e) { return (int)((packed >> (4 * e)) & 15); }
+
 // ElTet4n3D (ElTet4n3D.C:33-57): one point, N = 1/4, dN/dxi of the barycentric coordinates
 template <> struct Shape<DNL_ELTET4N3D> {
   static constexpr double kWeight = 1. / 6.;
@@ -348,23 +364,74 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
 #pragma unroll
   for (int k = 0; k < NEN; k++) node[k] = __ldg(a.conn + (long)k * a.E + e);
 
-  // ---- kinematics: J = sum_k dN/dxi (x) x_k, then J^-1
-  double J[DIM][DIM];
+  // ---- kinematics: J = sum_k dN/dxi (x) x_k and G_u = sum_k dN/dxi (x) du_k (Current field)
+  double J[DIM][DIM], GU[DIM][DIM];
 #pragma unroll
   for (int r = 0; r < DIM; r++)
 #pragma unroll
-    for (int c = 0; c < DIM; c++) J[r][c] = 0.;
+    for (int c = 0; c < DIM; c++) J[r][c] = GU[r][c] = 0.;
   double Rad = 0.;  // axisymmetric radius at the Gauss point, sum N_k x_k
+  double vR = 0.;   // axisymmetric sum N_k du_k,r
+  constexpr bool EDGES = ET == DNL_ELHEX8N3D || ET == DNL_ELQUA4NAX || ET == DNL_ELQUA4N2D;
+  if constexpr (EDGES) {
+    // the element's edge differences of x and du, a few per lane, exchanged through its shared
+    // memory (free until the force assembly): DIM^2 (NEN / 2) FMA each instead of DIM^2 NEN
+    using EG = Edges<ET>;
+    constexpr int NE = EG::NE, PER = NE / DIM;
+    double *ex = red, *eu = red + NE * DIM;
 #pragma unroll
-  for (int k = 0; k < NEN; k++) {
-    double xk[DIM];
+    for (int j = 0; j < (NE + NIP - 1) / NIP; j++) {
+      const int eg = pt + j * NIP;
+      if (eg < NE) {
+        const int lo = __ldg(a.conn + (long)edge_node(EG::LO, eg) * a.E + e);
+        const int hi = __ldg(a.conn + (long)edge_node(EG::HI, eg) * a.E + e);
 #pragma unroll
-    for (int r = 0; r < DIM; r++) xk[r] = a.x[r][node[k]];
+        for (int r = 0; r < DIM; r++) {
+          ex[eg * DIM + r] = RSUB(a.x[r][hi], a.x[r][lo]);
+          eu[eg * DIM + r] = RSUB(a.du[r][hi], a.du[r][lo]);
+        }
+      }
+    }
+    __syncwarp();
 #pragma unroll
-    for (int r = 0; r < DIM; r++)
+    for (int c = 0; c < DIM; c++)
 #pragma unroll
-      for (int c = 0; c < DIM; c++) J[r][c] = fma(SH::dN(pt, k, c), xk[r], J[r][c]);
-    if (AXI) Rad = fma(SH::N(pt, k), xk[0], Rad);
+      for (int q = 0; q < PER; q++) {
+        const int eg = c * PER + q;
+        const double w = SH::dN(pt, edge_node(EG::HI, eg), c);
+#pragma unroll
+        for (int r = 0; r < DIM; r++) {
+          J[r][c] = fma(w, ex[eg * DIM + r], J[r][c]);
+          GU[r][c] = fma(w, eu[eg * DIM + r], GU[r][c]);
+        }
+      }
+    __syncwarp();  // the force assembly reuses the buffer
+    if (AXI) {
+#pragma unroll
+      for (int k = 0; k < NEN; k++) {
+        Rad = fma(SH::N(pt, k), a.x[0][node[k]], Rad);
+        vR = fma(SH::N(pt, k), a.du[0][node[k]], vR);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < NEN; k++) {
+      double xk[DIM], uk[DIM];
+#pragma unroll
+      for (int r = 0; r < DIM; r++) {
+        xk[r] = a.x[r][node[k]];
+        uk[r] = a.du[r][node[k]];
+      }
+#pragma unroll
+      for (int c = 0; c < DIM; c++) {
+        const double d = SH::dN(pt, k, c);
+#pragma unroll
+        for (int r = 0; r < DIM; r++) {
+          J[r][c] = fma(d, xk[r], J[r][c]);
+          GU[r][c] = fma(d, uk[r], GU[r][c]);
+        }
+      }
+    }
   }
   double detJ, Ji[DIM][DIM];
   if (TWO_D) {
@@ -401,29 +468,9 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     tape(TL::RAD, Rad);
   }
 
-  // ---- F = I + sum_k du_k (x) dN_k = I + G_u J^-1 with G_u = sum_k du_k (x) dN/dxi_k (Current
-  // field): DIM^2 (NEN + DIM) FP64 instructions instead of DIM^2 (2 NEN) forming each node's
-  // physical gradient first; the diagonal's sum is added to 1 last
+  // ---- F = I + sum_k du_k (x) dN_k = I + G_u J^-1 (no per-node physical gradients); the
+  // diagonal's sums are added to 1 last
   double F[3][3] = {{1., 0., 0.}, {0., 1., 0.}, {0., 0., 1.}};
-  double vR = 0.;
-  double GU[DIM][DIM];
-#pragma unroll
-  for (int r = 0; r < DIM; r++)
-#pragma unroll
-    for (int l = 0; l < DIM; l++) GU[r][l] = 0.;
-#pragma unroll
-  for (int k = 0; k < NEN; k++) {
-    double uk[DIM];
-#pragma unroll
-    for (int r = 0; r < DIM; r++) uk[r] = a.du[r][node[k]];
-#pragma unroll
-    for (int l = 0; l < DIM; l++) {
-      const double d = SH::dN(pt, k, l);
-#pragma unroll
-      for (int r = 0; r < DIM; r++) GU[r][l] = fma(uk[r], d, GU[r][l]);
-    }
-    if (AXI) vR = fma(SH::N(pt, k), uk[0], vR);
-  }
 #pragma unroll
   for (int r = 0; r < DIM; r++)
 #pragma unroll
