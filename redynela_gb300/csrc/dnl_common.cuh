@@ -148,7 +148,8 @@ template <int ET> struct TapeLayout {
   static constexpr int GAM = NORMS + 1;     // plastic multiplier (0: elastic step)
   static constexpr int XV = GAM + 1;        // evp + sqrt(2/3) gamma
   static constexpr int XN = XV + 1;         // XV^n
-  static constexpr int NT = XN + 1;
+  static constexpr int LXV = XN + 1;        // ln XV (plastic points; the n-derivative of XV^n)
+  static constexpr int NT = LXV + 1;
 };
 
 // Tangent integration-point state per parameter direction: [dir][comp][E*NIP]

@@ -682,6 +682,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
       tape(TL::GAM, 0.);
       tape(TL::XV, evp);
       tape(TL::XN, evpn);
+      tape(TL::LXV, 0.);
     }
     if (GENERAL && !power && m.hard.law != DNL_HARD_ELASTIC && Strial > Sigv0) {
       // any other hardening law: the return of Element.C:282-345 with the law's
@@ -760,6 +761,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
       tape(TL::GAM, gamma);
       tape(TL::XV, RADD(evp, RMUL(kSqrt23, gamma)));
       tape(TL::XN, xn);
+      if (TAPE) tape(TL::LXV, log(RADD(evp, RMUL(kSqrt23, gamma))));
       evp = RADD(evp, RMUL(kSqrt23, gamma));
       evpn = xn;
       const double c2 = m.G2 * gamma;

@@ -134,7 +134,8 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
         dF[r][c] = s;
       }
   }
-  if (AXI) dF[2][2] = fma(-tp(TL::VRR), dRad, dvR) / Rad;
+  const double rRad = AXI ? nr_rcp(Rad) : 0.;  // tangents need no correctly rounded quotients
+  if (AXI) dF[2][2] = fma(-tp(TL::VRR), dRad, dvR) * rRad;
 
   // ---- dC = dF^T F + F^T dF (symmetric)
   double dC[3][3];
@@ -264,23 +265,24 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
   double devp = devp0;
   const double gam = tp(TL::GAM);
   if (gam > 0.) {
-    const double normS = tp(TL::NORMS), xv = tp(TL::XV), xn = tp(TL::XN);
+    const double normS = tp(TL::NORMS), xv = tp(TL::XV), xn = tp(TL::XN), rnorm = nr_rcp(normS);
     double nh[3][3];
-    symload(nh, [&](int k) { return tp(TL::STR + k) / normS; });
+    symload(nh, [&](int k) { return tp(TL::STR + k) * rnorm; });
     double dnorm = 0.;
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int j = 0; j < 3; j++) dnorm = fma(nh[i][j], dS[i][j], dnorm);
-    const double h = m.nB * xn / xv;  // n B xv^(n-1)
+    const double h = m.nB * xn * nr_rcp(xv);  // n B xv^(n-1)
     const double D = fma(kSqrt23, h, m.dfun0);
-    const double dsig = dir == 0 ? 1. : (dir == 1 ? xn : (dir == 2 ? m.B * xn * log(xv) : 0.));
-    const double dgam = fma(kSqrt32, dnorm, -fma(h, devp0, dsig)) / D;
+    const double dsig = dir == 0 ? 1. : (dir == 1 ? xn : (dir == 2 ? m.B * xn * tp(TL::LXV) : 0.));
+    const double dgam = fma(kSqrt32, dnorm, -fma(h, devp0, dsig)) * nr_rcp(D);
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int j = 0; j < 3; j++) {
-        const double dn = fma(-nh[i][j], dnorm, dS[i][j]) / normS;
+        if (zero(i, j)) continue;
+        const double dn = fma(-nh[i][j], dnorm, dS[i][j]) * rnorm;
         const double dflow = fma(dgam, nh[i][j], gam * dn);
         dS[i][j] = fma(-m.G2, dflow, dS[i][j]);
         dP[i][j] += dflow;
@@ -303,6 +305,32 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
   auto rfi_t = [&](int comp, double dX[3][3]) {
     double Xp[3][3];
     symload(Xp, [&](int k) { return a.ip[(comp + k) * nIP + ipx]; });
+    if (comp == L::EPSP) {  // a point that never yielded: EpsPlas and its tangent are 0
+      unsigned long long nz = 0;
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = i; j < 3; j++) nz |= abits(Xp[i][j]) | abits(dX[i][j]);
+      if (!nz) return;
+    }
+    if constexpr (TWO_D) {
+      // Omega = dR R^T is skew (R R^T = I): in the block one rate w, so Omega X' + (Omega X')^T is
+      // 2 w X'01 on the diagonal and w (X'11 - X'00) off it; R dX R^T by two 2x2 products
+      const double w = 0.5 * (Om[0][1] - Om[1][0]);
+      const double t00 = fma(dX[0][0], R[0][0], dX[0][1] * R[0][1]);
+      const double t01 = fma(dX[0][0], R[1][0], dX[0][1] * R[1][1]);
+      const double t10 = fma(dX[1][0], R[0][0], dX[1][1] * R[0][1]);
+      const double t11 = fma(dX[1][0], R[1][0], dX[1][1] * R[1][1]);
+      const double y00 = fma(R[0][0], t00, R[0][1] * t10);
+      const double y01 = fma(R[0][0], t01, R[0][1] * t11);
+      const double y11 = fma(R[1][0], t01, R[1][1] * t11);
+      const double w2x = 2. * w * Xp[0][1];
+      dX[0][0] = y00 + w2x;
+      dX[1][1] = y11 - w2x;
+      dX[0][1] = dX[1][0] = fma(w, Xp[1][1] - Xp[0][0], y01);
+      dX[2][2] = fma(2. * Om[2][2], Xp[2][2], R[2][2] * (dX[2][2] * R[2][2]));
+      return;
+    }
     double Tm[3][3], dXRt[3][3];
 #pragma unroll
     for (int i = 0; i < 3; i++)
@@ -359,8 +387,8 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
   if (AXI) {
     W = detJ * (kDeuxPi * Rad);
     dW = kDeuxPi * fma(ddetJ, Rad, detJ * dRad);
-    const double hb = sig[2][2] / Rad;
-    dhoop = fma(fma(-hb, dRad, dS[2][2]) / Rad, W, hb * dW);
+    // the primal hoop force is sigma_tt / R x W = sigma_tt detJ 2 pi
+    dhoop = kDeuxPi * fma(dS[2][2], detJ, sig[2][2] * ddetJ);
   }
   double dM[DIM][DIM];
 #pragma unroll
@@ -375,27 +403,34 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
       }
       dM[l][i] = fma(ds, W, s * dW);
     }
-  double *row = red + pt * (NEN * DIM);
+  // every point's dM (and hoop tangent) through the group's shared memory; lane k assembles node
+  // k (the quads and the hexahedron have as many nodes as points)
+  constexpr int ST = DIM * DIM + (AXI ? 1 : 0);
+  double *mine = red + pt * ST;
 #pragma unroll
-  for (int k = 0; k < NEN; k++)
+  for (int l = 0; l < DIM; l++)
 #pragma unroll
-    for (int i = 0; i < DIM; i++) {
-      double s = 0.;
-#pragma unroll
-      for (int l = 0; l < DIM; l++) s = fma(SH::dN(pt, k, l), dM[l][i], s);
-      if (AXI && i == 0) s = fma(SH::N(pt, k), dhoop, s);
-      row[k * DIM + i] = s;
-    }
+    for (int i = 0; i < DIM; i++) mine[l * DIM + i] = dM[l][i];
+  if (AXI) mine[DIM * DIM] = dhoop;
   __syncwarp();
   if (valid) {
+    double s[DIM];
+#pragma unroll
+    for (int i = 0; i < DIM; i++) s[i] = 0.0;
+#pragma unroll
+    for (int q = 0; q < NIP; q++) {
+      const double *Mq = red + q * ST;
+#pragma unroll
+      for (int l = 0; l < DIM; l++) {
+        const double d = SH::dN(q, pt, l);
+#pragma unroll
+        for (int i = 0; i < DIM; i++) s[i] = fma(d, Mq[l * DIM + i], s[i]);
+      }
+      if (AXI) s[0] = fma(SH::N(q, pt), Mq[DIM * DIM], s[0]);
+    }
     double *tfe = a.tfe + (long)dir * DIM * a.E * NEN;
 #pragma unroll
-    for (int i = 0; i < DIM; i++) {
-      double s = 0.0;
-#pragma unroll
-      for (int q = 0; q < NIP; q++) s -= red[q * (NEN * DIM) + pt * DIM + i];
-      tfe[(long)i * a.E * NEN + (long)e * NEN + pt] = s;
-    }
+    for (int i = 0; i < DIM; i++) tfe[(long)i * a.E * NEN + (long)e * NEN + pt] = ineg(s[i]);
   }
 }
 
