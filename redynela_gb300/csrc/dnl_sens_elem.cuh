@@ -59,6 +59,48 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
   for (int r = 0; r < DIM; r++)
 #pragma unroll
     for (int c = 0; c < DIM; c++) dJ[r][c] = GT[r][c] = 0.;
+  constexpr bool EDGES = ET == DNL_ELHEX8N3D || ET == DNL_ELQUA4NAX || ET == DNL_ELQUA4N2D;
+  if constexpr (EDGES) {
+    // the group's edge differences of the tangents, a few per lane, through its shared memory
+    // (as the primal pass's J and G_u)
+    using EG = Edges<ET>;
+    constexpr int NE = EG::NE, PER = NE / DIM;
+    double *ex = red, *eu = red + NE * DIM;
+#pragma unroll
+    for (int j = 0; j < (NE + NIP - 1) / NIP; j++) {
+      const int eg = pt + j * NIP;
+      if (eg < NE) {
+        const int lo = __ldg(a.conn + (long)edge_node(EG::LO, eg) * a.E + e);
+        const int hi = __ldg(a.conn + (long)edge_node(EG::HI, eg) * a.E + e);
+#pragma unroll
+        for (int r = 0; r < DIM; r++) {
+          ex[eg * DIM + r] = tx[(long)r * N + hi] - tx[(long)r * N + lo];
+          eu[eg * DIM + r] = tdu[(long)r * N + hi] - tdu[(long)r * N + lo];
+        }
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int c = 0; c < DIM; c++)
+#pragma unroll
+      for (int q = 0; q < PER; q++) {
+        const int eg = c * PER + q;
+        const double w = SH::dN(pt, edge_node(EG::HI, eg), c);
+#pragma unroll
+        for (int r = 0; r < DIM; r++) {
+          dJ[r][c] = fma(w, ex[eg * DIM + r], dJ[r][c]);
+          GT[r][c] = fma(w, eu[eg * DIM + r], GT[r][c]);
+        }
+      }
+    __syncwarp();  // the force assembly reuses the buffer
+    if (AXI) {
+#pragma unroll
+      for (int k = 0; k < NEN; k++) {
+        dRad = fma(SH::N(pt, k), tx[node[k]], dRad);
+        dvR = fma(SH::N(pt, k), tdu[node[k]], dvR);
+      }
+    }
+  } else {
 #pragma unroll
   for (int k = 0; k < NEN; k++) {
     double t[DIM], tu[DIM];
@@ -79,6 +121,7 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
       dRad = fma(SH::N(pt, k), t[0], dRad);
       dvR = fma(SH::N(pt, k), tu[0], dvR);
     }
+  }
   }
   // ---- dJ^-1 = -J^-1 dJ J^-1, d det J = det J tr(J^-1 dJ)
   double Ji[DIM][DIM];
@@ -232,17 +275,22 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
         }
         dR[i][j] = s;
       }
+    // Omega = dR R^T is skew (R R^T = I): its upper entries (and, in 2D, Omega_22) suffice
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
-      for (int j = 0; j < 3; j++) {
-        double s = 0.;
-        if (!zero(i, j)) {
+      for (int j = 0; j < 3; j++) Om[i][j] = 0.;
 #pragma unroll
-          for (int k = 0; k < 3; k++)
-            if (!zero(i, k) && !zero(j, k)) s = fma(dR[i][k], R[j][k], s);
-        }
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = i; j < 3; j++) {
+        if (zero(i, j) || (i == j && !(TWO_D && i == 2))) continue;
+        double s = 0.;
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+          if (!zero(i, k) && !zero(j, k)) s = fma(dR[i][k], R[j][k], s);
         Om[i][j] = s;
+        if (i != j) Om[j][i] = -s;
       }
   }
 
@@ -330,34 +378,26 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
       dX[0][1] = dX[1][0] = fma(w, Xp[1][1] - Xp[0][0], y01);
       dX[2][2] = fma(2. * Om[2][2], Xp[2][2], R[2][2] * (dX[2][2] * R[2][2]));
       return;
-    }
-    double Tm[3][3], dXRt[3][3];
+    } else {
+      // R dX R^T, then Omega X' + (Omega X')^T written out for the skew Omega (a, b, c) =
+      // (Omega_01, Omega_02, Omega_12)
+      double dXRt[3][3];
 #pragma unroll
-    for (int i = 0; i < 3; i++)
+      for (int i = 0; i < 3; i++)
 #pragma unroll
-      for (int j = 0; j < 3; j++) {
-        double s = 0., t = 0.;
-        if (!zero(i, j)) {
+        for (int j = 0; j < 3; j++) dXRt[i][j] = fma(dX[i][0], R[j][0], fma(dX[i][1], R[j][1], dX[i][2] * R[j][2]));
+      double Y[3][3];
 #pragma unroll
-          for (int k = 0; k < 3; k++) {
-            if (!zero(i, k) && !zero(k, j)) s = fma(Om[i][k], Xp[k][j], s);
-            if (!zero(i, k) && !zero(j, k)) t = fma(dX[i][k], R[j][k], t);
-          }
-        }
-        Tm[i][j] = s;
-        dXRt[i][j] = t;
-      }
+      for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int q = 0; q < 6; q++) {
-      const int i = I0[q], j = I1[q];
-      double y = 0.;
-      if (!zero(i, j)) {
-#pragma unroll
-        for (int k = 0; k < 3; k++)
-          if (!zero(i, k) && !zero(k, j)) y = fma(R[i][k], dXRt[k][j], y);
-      }
-      const double v = y + Tm[i][j] + Tm[j][i];
-      dX[i][j] = dX[j][i] = v;
+        for (int j = i; j < 3; j++) Y[i][j] = fma(R[i][0], dXRt[0][j], fma(R[i][1], dXRt[1][j], R[i][2] * dXRt[2][j]));
+      const double oa = Om[0][1], ob = Om[0][2], oc = Om[1][2];
+      dX[0][0] = fma(2. * oa, Xp[1][0], fma(2. * ob, Xp[2][0], Y[0][0]));
+      dX[1][1] = fma(-2. * oa, Xp[0][1], fma(2. * oc, Xp[2][1], Y[1][1]));
+      dX[2][2] = fma(-2. * ob, Xp[0][2], fma(-2. * oc, Xp[1][2], Y[2][2]));
+      dX[0][1] = dX[1][0] = fma(oa, Xp[1][1] - Xp[0][0], fma(ob, Xp[2][1], fma(oc, Xp[2][0], Y[0][1])));
+      dX[0][2] = dX[2][0] = fma(oa, Xp[1][2], fma(ob, Xp[2][2] - Xp[0][0], fma(-oc, Xp[1][0], Y[0][2])));
+      dX[1][2] = dX[2][1] = fma(-oa, Xp[0][2], fma(-ob, Xp[0][1], fma(oc, Xp[2][2] - Xp[1][1], Y[1][2])));
     }
   };
   rfi_t(L::S, dS);
