@@ -372,7 +372,8 @@ struct dnl_handle {
   dnl::GraphEntry graphs[8];
   int ngraphs;
   char lastError[256];
-  double *stage;              // N*3 staging buffer for host <-> device nodal vectors
+  double *stage;              // 5 x N*3 staging buffer for host <-> device nodal vectors (one
+                              // slot per nodal field, so the copies of a call run back to back)
   cudaEvent_t marks[8];
   // per-kernel event timing (dnl_profile_begin/end)
   bool profiling;

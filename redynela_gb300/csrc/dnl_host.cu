@@ -1093,7 +1093,7 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
         CKF(cudaMemcpy(h->bank[b].v[c], v.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
       }
   }
-  CKF(cudaMalloc(&h->stage, sizeof(double) * 3 * (size_t)N));
+  CKF(cudaMalloc(&h->stage, sizeof(double) * 15 * (size_t)N));
   CKF(cudaMalloc(&h->mass, sizeof(double) * N));
   CKF(cudaMemset(h->mass, 0, sizeof(double) * N));
   // ---- integration points
@@ -1195,18 +1195,23 @@ int dnl_set_state(dnl_handle *h, const dnl_state_view *s)
 {
   if (!h || !s) return DNL_ERR_ARG;
   const int N = h->N;
-  auto put3 = [&](const double *src, double *const dst[3]) -> int {
-    CK(cudaMemcpyAsync(h->stage, src, sizeof(double) * 3 * (size_t)N, cudaMemcpyHostToDevice, h->stream));
-    k_aos_to_soa<<<(N + 255) / 256, 256, 0, h->stream>>>(N, h->stage, dst[0], dst[1], dst[2]);
-    launch_counter()++;
-    return check_launch();
-  };
+  // the host arrays' copies first, back to back, each into its own staging slot; then the
+  // transpositions to the component-major device arrays
+  const double *src[5] = {s->coords, s->du, s->v, s->a, s->disp};
+  double *const *dst[5] = {h->x, h->bank[h->cur].du, h->bank[h->cur].v, h->bank[h->cur].a,
+                           h->bank[h->cur].disp};
+  for (int f = 0; f < 5; f++)
+    if (src[f])
+      CK(cudaMemcpyAsync(h->stage + (size_t)f * 3 * N, src[f], sizeof(double) * 3 * (size_t)N,
+                         cudaMemcpyHostToDevice, h->stream));
   int r;
-  if (s->coords && (r = put3(s->coords, h->x))) return r;
-  if (s->du && (r = put3(s->du, h->bank[h->cur].du))) return r;
-  if (s->v && (r = put3(s->v, h->bank[h->cur].v))) return r;
-  if (s->a && (r = put3(s->a, h->bank[h->cur].a))) return r;
-  if (s->disp && (r = put3(s->disp, h->bank[h->cur].disp))) return r;
+  for (int f = 0; f < 5; f++)
+    if (src[f]) {
+      k_aos_to_soa<<<(N + 255) / 256, 256, 0, h->stream>>>(N, h->stage + (size_t)f * 3 * N, dst[f][0],
+                                                            dst[f][1], dst[f][2]);
+      launch_counter()++;
+      if ((r = check_launch())) return r;
+    }
   const int ns = etype_ns(h->etype);
   const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
   const size_t nIP = h->nIP;
@@ -1236,20 +1241,22 @@ int dnl_get_state(dnl_handle *h, dnl_state_view *s)
 {
   if (!h || !s) return DNL_ERR_ARG;
   const int N = h->N;
-  auto get3 = [&](double *dst, double *const src[3]) -> int {
-    k_soa_to_aos<<<(N + 255) / 256, 256, 0, h->stream>>>(N, h->stage, src[0], src[1], src[2]);
-    launch_counter()++;
-    if (int r = check_launch()) return r;
-    CK(cudaMemcpyAsync(dst, h->stage, sizeof(double) * 3 * (size_t)N, cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    return 0;
-  };
+  // all transpositions into the staging slots, then the copies back to back, one synchronisation
+  double *out[5] = {s->coords, s->du, s->v, s->a, s->disp};
+  double *const *from[5] = {h->x, h->bank[h->cur].du, h->bank[h->cur].v, h->bank[h->cur].a,
+                            h->bank[h->cur].disp};
   int r;
-  if (s->coords && (r = get3(s->coords, h->x))) return r;
-  if (s->du && (r = get3(s->du, h->bank[h->cur].du))) return r;
-  if (s->v && (r = get3(s->v, h->bank[h->cur].v))) return r;
-  if (s->a && (r = get3(s->a, h->bank[h->cur].a))) return r;
-  if (s->disp && (r = get3(s->disp, h->bank[h->cur].disp))) return r;
+  for (int f = 0; f < 5; f++)
+    if (out[f]) {
+      k_soa_to_aos<<<(N + 255) / 256, 256, 0, h->stream>>>(N, h->stage + (size_t)f * 3 * N, from[f][0],
+                                                            from[f][1], from[f][2]);
+      launch_counter()++;
+      if ((r = check_launch())) return r;
+    }
+  for (int f = 0; f < 5; f++)
+    if (out[f])
+      CK(cudaMemcpyAsync(out[f], h->stage + (size_t)f * 3 * N, sizeof(double) * 3 * (size_t)N,
+                         cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   if (s->mass) CK(cudaMemcpy(s->mass, h->mass, sizeof(double) * N, cudaMemcpyDeviceToHost));
   if (!(s->S || s->Eps || s->EpsPlas || s->p || s->evp || s->Sig)) return 0;
