@@ -163,6 +163,7 @@ int dnl_run(dnl_handle *h, int *steps_done);
  * Courant time step only (the Pulse power iteration checks convergence on the host) */
 int dnl_step_graph(dnl_handle *h, int nsteps, int *steps_done);
 int dnl_time_step(dnl_handle *h, double *dt);
+int dnl_dt(dnl_handle *h, double *dt); /* the same as dnl_time_step */
 int dnl_get_time_info(dnl_handle *h, dnl_time_info *info);
 /* nodal internal forces of the last element pass, dim*N */
 int dnl_get_fint(dnl_handle *h, double *fint);
@@ -184,6 +185,9 @@ int dnl_batch_prologue(dnl_batch *b);
 int dnl_batch_step(dnl_batch *b, int nsteps, int *active);
 /* the same, captured once into a CUDA graph per (nsteps, phase) and replayed */
 int dnl_batch_step_graph(dnl_batch *b, int nsteps, int *active);
+/* capture (without running) the graph dnl_batch_step_graph(b, nsteps) replays from the current
+ * increment; DNL_ERR_ARG when the handle's graph cache (8 graphs) is full */
+int dnl_batch_graph_capture(dnl_batch *b, int nsteps);
 /* time live steps with 64, 128 and 256 threads per element-pass block; keep the fastest */
 int dnl_batch_autotune(dnl_batch *b, int steps_per_candidate, int *block);
 int dnl_batch_set_block(dnl_batch *b, int block);

@@ -367,12 +367,11 @@ int dnl_batch_step(dnl_batch *b, int nsteps, int *active)
   return first_status(t, nullptr);
 }
 
-int dnl_batch_step_graph(dnl_batch *b, int nsteps, int *active)
+// The graph of nsteps batched steps from the current increment (keyed by nsteps, the nodal field
+// parity and the phase in the time-step recomputation cycle): found among the captured ones or
+// captured now.  On return h->cur is the parity after the nsteps steps.
+static int batch_graph(dnl_batch *b, int nsteps, cudaGraphExec_t *out)
 {
-  if (active) *active = 0;
-  if (!b || nsteps <= 0) return DNL_ERR_ARG;
-  int r;
-  if (!b->prologueDone && (r = dnl_batch_prologue(b))) return r;
   dnl_handle *h = b->h;
   const long long inc0 = b->increment;
   const int parity = h->cur, phase = (int)(inc0 % b->freq);
@@ -400,6 +399,39 @@ int dnl_batch_step_graph(dnl_batch *b, int nsteps, int *active)
   } else {
     h->cur = (nsteps % 2) ? 1 - parity : parity;
   }
+  *out = exec;
+  return 0;
+}
+
+int dnl_batch_graph_capture(dnl_batch *b, int nsteps)
+{
+  if (!b || nsteps <= 0) return DNL_ERR_ARG;
+  int r;
+  if (!b->prologueDone && (r = dnl_batch_prologue(b))) return r;
+  dnl_handle *h = b->h;
+  const int cur0 = h->cur;
+  cudaGraphExec_t exec;
+  r = batch_graph(b, nsteps, &exec);
+  h->cur = cur0;  // captured, not run
+  if (r) return r;
+  bool cached = false;
+  for (int i = 0; i < b->ngraphs; i++) cached |= b->graphs[i].exec == exec;
+  if (!cached) {  // the cache is full: nothing to keep
+    cudaGraphExecDestroy(exec);
+    return DNL_ERR_ARG;
+  }
+  return 0;
+}
+
+int dnl_batch_step_graph(dnl_batch *b, int nsteps, int *active)
+{
+  if (active) *active = 0;
+  if (!b || nsteps <= 0) return DNL_ERR_ARG;
+  int r;
+  if (!b->prologueDone && (r = dnl_batch_prologue(b))) return r;
+  dnl_handle *h = b->h;
+  cudaGraphExec_t exec;
+  if ((r = batch_graph(b, nsteps, &exec))) return r;
   for (int i = 0; i < b->ngraphs; i++)
     if (b->graphs[i].exec == exec) launch_counter() += b->graphs[i].kernels;
   BK(cudaGraphLaunch(exec, h->stream));

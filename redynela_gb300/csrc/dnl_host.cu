@@ -1472,6 +1472,8 @@ int dnl_time_step(dnl_handle *h, double *dt)
   return 0;
 }
 
+int dnl_dt(dnl_handle *h, double *dt) { return dnl_time_step(h, dt); }
+
 int dnl_get_time_info(dnl_handle *h, dnl_time_info *info)
 {
   if (!h || !info) return DNL_ERR_ARG;

@@ -129,6 +129,7 @@ def lib():
         L.dnl_batch_prologue.argtypes = [H]
         L.dnl_batch_step.argtypes = [H, C.c_int, _ip]
         L.dnl_batch_step_graph.argtypes = [H, C.c_int, _ip]
+        L.dnl_batch_graph_capture.argtypes = [H, C.c_int]
         L.dnl_batch_autotune.argtypes = [H, C.c_int, _ip]
         L.dnl_batch_set_block.argtypes = [H, C.c_int]
         L.dnl_batch_time_info.argtypes = [H, C.c_int, C.POINTER(TimeInfo)]
@@ -566,6 +567,10 @@ class BatchDomain:
         act = C.c_int(0)
         self._check(self.L.dnl_batch_step(self.h, int(n), C.byref(act)))
         return act.value
+
+    def graph_capture(self, n: int) -> None:
+        """dnl_batch_graph_capture: capture, without running, the graph step_graph(n) replays."""
+        self._check(self.L.dnl_batch_graph_capture(self.h, int(n)))
 
     def step_graph(self, n: int) -> int:
         act = C.c_int(0)

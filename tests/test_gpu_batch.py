@@ -62,3 +62,20 @@ def test_batch_runs_each_instance_to_its_end(gpu_lib):
         x = b.coords(i).ravel()
         ref = o.array("coords")
         assert np.max(np.abs(x - ref)) <= 1e-6 * np.max(np.abs(ref))
+
+
+def test_graph_capture_then_replay(gpu_lib):
+    """dnl_batch_graph_capture prepares the graph without advancing; the replays that follow give
+    what stream launches give."""
+    models = _models()
+    a = gpu_lib.BatchDomain(models)
+    a.step(40)
+    b = gpu_lib.BatchDomain(models)
+    b.prologue()
+    b.graph_capture(20)
+    for i in range(len(models)):
+        assert b.time_info(i)["increment"] == 0
+    b.step_graph(20)
+    b.step_graph(20)
+    for i in range(len(models)):
+        assert np.array_equal(a.coords(i), b.coords(i)), i
