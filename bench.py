@@ -480,6 +480,24 @@ def main_sens(args):
         fwd_ms += d.timer_elapsed_ms(0, 1) / args.steps
     grad_ms = dev_ms / args.steps
     e2e = args.steps / wall
+    # central differences of L over the same fixed schedule, h = 1e-5, 1e-6, 1e-7 relative per
+    # parameter: the difference quotient carries the run's rounding noise in L divided by 2h, so
+    # its distance from the derivative growing as h shrinks shows that noise, not the derivative
+    pv = np.array([m.A, m.B, m.n, v0])
+
+    def loss_at(q):
+        d.reset(dynela.model_with_params(m, *q))
+        x, _ = d.sensitivities(dts)
+        return float(np.mean(np.sum((x[surf] - xt[surf]) ** 2, axis=1)))
+
+    fd_rel = {}
+    for hrel in (1e-5, 1e-6, 1e-7):
+        errs = []
+        for p in range(4):
+            h = hrel * pv[p]
+            lp, lm = (loss_at(pv + s * h * np.eye(4)[p]) for s in (1.0, -1.0))
+            errs.append(float(abs((lp - lm) / (2 * h) - g[p]) / abs(g[p])))
+        fd_rel[f"{hrel:.0e}"] = errs
     tan_ms, tan_n = prof["tangent"]
     elem_ms, elem_n = prof["elem"]
     total_ms = sum(v[0] for v in prof.values())
@@ -529,6 +547,7 @@ def main_sens(args):
             "forward_run_ms": fwd_ms, "gradient_ms": grad_ms,
             "gradient_cost_vs_forward": grad_ms / fwd_ms,
             "agreement_vs_dual_oracle": agree,
+            "agreement_vs_central_differences": {"relative_error_by_relative_h": fd_rel},
             "gpu_launches": launches,
             "kernel_time_share": {k: round(v[0] / total_ms, 4) for k, v in prof.items()} if total_ms else None,
             "roofline": {"bound": "hbm", "achieved": tan_bytes / (tan_ms / max(tan_n, 1) * 1e-3) / 1e9,

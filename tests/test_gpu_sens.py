@@ -87,8 +87,8 @@ def test_torch_autograd_function(gpu_lib):
     _, dx = gpu_lib.GpuDomain(m).sensitivities(dts)
     ref = np.einsum("pnj,nj->p", dx, 2 * (x.detach().numpy() - m.coords))
     assert np.allclose(params.grad.numpy(), ref, rtol=1e-12, atol=0)
-    # and central differences of the GPU run for the hardening parameters (h = 1e-6 relative)
-    for p in range(3):
+    # and central differences of the GPU run for all four parameters (h = 1e-6 relative, 1e-5)
+    for p in range(4):
         h = 1e-6 * float(params.detach()[p])
         vals = []
         for sgn in (1, -1):
@@ -97,7 +97,7 @@ def test_torch_autograd_function(gpu_lib):
             xq = run.apply(q, m, dts)
             vals.append(float(((xq - target) ** 2).sum()))
         fd = (vals[0] - vals[1]) / (2 * h)
-        assert abs(fd - float(params.grad[p])) <= 1e-4 * abs(float(params.grad[p])), p
+        assert abs(fd - float(params.grad[p])) <= 1e-5 * abs(float(params.grad[p])), p
 
 
 def test_reset_returns_to_the_initial_state(gpu_lib):
