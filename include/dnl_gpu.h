@@ -47,7 +47,7 @@ enum dnl_status {
 #define DNL_ELTET10N3D 4 /* ElTet10n3D: 10-node tetrahedron, 4 Gauss points (the reference's tables) */
 /* Not a reference element: ElHex8n3D's geometry integrated at its centre only, with
  * Flanagan-Belytschko viscous hourglass control (dnl_set_hourglass) and a Courant length of
- * volume / largest face area.  Courant time step only; no sensitivities. */
+ * volume / largest face area.  Courant time step only. */
 #define DNL_ELHEX8N3D_1PT 5
 
 /* time-step methods (Solver::setTimeStepMethod, Solver.C:312-321) */
@@ -281,7 +281,8 @@ int dnl_read_results(dnl_handle *h, const char *path);
  * caller's schedule (a parameter-independent dt sequence) instead of Solver::computeTimeStep, from
  * the handle's initial state (no step taken yet); the end time is not applied.  Computed in
  * forward mode (four tangent copies of the state advanced with it), which for four parameters
- * stores no trajectory.  No counterpart in the reference, which has no derivatives. */
+ * stores no trajectory.  Every element type; one power-law material.  No counterpart in the
+ * reference, which has no derivatives. */
 #define DNL_SENS_NPARAM 4 /* A, B, n, |v0| */
 /* nsteps steps with step sizes dts[0..nsteps); coords (3N, node-major, may be NULL) receives the
  * final coordinates, dcoords (4 x 3N, may be NULL) their derivatives, dcoords[p*3N + 3n + j] */

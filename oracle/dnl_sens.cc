@@ -21,6 +21,8 @@
  * eigenpairs, d f(C) = V (F o (V^T dC V)) V^T with F_ij the divided differences of
  * f = ln(sqrt(.)) and f = 1/sqrt(.) (Daleckii-Krein).  The time step is the caller's schedule (a
  * parameter-independent dt sequence), so no Courant or Pulse step enters the derivative. */
+#include "tet10_tables.h"
+
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -123,6 +125,14 @@ inline D dsqrt(const D &a)
   for (int k = 0; k < NP; k++) r.d[k] = a.d[k] / (2. * r.v);
   return r;
 }
+inline D dcbrt(const D &a)
+{
+  D r;
+  r.v = cbrt(a.v);
+  const double s = 1.0 / (3.0 * r.v * r.v);
+  for (int k = 0; k < NP; k++) r.d[k] = a.d[k] * s;
+  return r;
+}
 // x^n for x > 0: value pow(x, n); d = n x^(n-1) dx + x^n ln(x) dn
 inline D dpow(const D &x, const D &n)
 {
@@ -164,7 +174,8 @@ struct dnls {
   std::vector<int> bcn_kind;
   std::vector<double> bcn_val;
   double alphaM, beta, gamma, timeStep;
-  double Nt[8][8], dNxi[8][8][3], weight[8];
+  double Nt[8][10], dNxi[8][10][3], weight[8];
+  double rho, hourglass;  // the one-point hexahedron's hourglass force
   int err;
 };
 
@@ -175,7 +186,23 @@ namespace {
 
 void build_tables(dnls *h)
 {
-  if (h->etype != 1) {  // ElQua4nAx and ElQua4n2D share their tables
+  if (h->etype == 5) {  // the one-point hexahedron (not a reference element): the cube's centre
+    h->weight[0] = 8.0;
+    for (int k = 0; k < 8; k++) {
+      h->Nt[0][k] = 0.125;
+      h->dNxi[0][k][0] = HX_XI[k] * 0.125;
+      h->dNxi[0][k][1] = HX_ETA[k] * 0.125;
+      h->dNxi[0][k][2] = HX_ZETA[k] * 0.125;
+    }
+  } else if (h->etype == 3) {  // ElTet4n3D (ElTet4n3D.C:33-57): one point, weight 1/6
+    h->weight[0] = 1. / 6.;
+    for (int k = 0; k < 4; k++) {
+      h->Nt[0][k] = 0.25;
+      for (int c = 0; c < 3; c++) h->dNxi[0][k][c] = k == 0 ? -1.0 : (k - 1 == c ? 1.0 : 0.0);
+    }
+  } else if (h->etype == 4) {  // ElTet10n3D (ElTet10n3D.C:45-72), as the compiled reference holds it
+    dnl_tet10_tables(h->Nt, h->dNxi, h->weight);
+  } else if (h->etype != 1) {  // ElQua4nAx and ElQua4n2D share their tables
     const double cN[3] = {(2.0 + sqrt(3.0)) / 6.0, 1.0 / 6.0, (2.0 - sqrt(3.0)) / 6.0};
     const double cD[2] = {(3.0 + sqrt(3.0)) / 12.0, (3.0 - sqrt(3.0)) / 12.0};
     for (int pt = 0; pt < 4; pt++) {
@@ -496,7 +523,7 @@ int elem_matrices(dnls *h, long e)
       D J[3][3];
       for (int r = 0; r < 3; r++)
         for (int c = 0; c < 3; c++) J[r][c] = cst(0.);
-      for (int k = 0; k < 8; k++) {
+      for (int k = 0; k < h->nen; k++) {
         const D *x = h->coords.data() + cn[k] * 3;
         for (int r = 0; r < 3; r++)
           for (int c = 0; c < 3; c++) J[r][c] += h->dNxi[pt][k][c] * x[r];
@@ -509,7 +536,7 @@ int elem_matrices(dnls *h, long e)
       for (int r = 0; r < 3; r++)
         for (int c = 0; c < 3; c++) a[c * 3 + r] = J[r][c];
       if (inv3_lapack(a)) err = 7;
-      for (int k = 0; k < 8; k++)
+      for (int k = 0; k < h->nen; k++)
         for (int c = 0; c < 3; c++) {
           D acc = cst(0.);
           for (int l = 0; l < 3; l++) acc += a[c * 3 + l] * h->dNxi[pt][k][l];
@@ -548,7 +575,7 @@ void elem_F(const dnls *h, long e, int pt, D *F)
       F[8] += v / R;
     }
   } else {
-    for (int k = 0; k < 8; k++) {
+    for (int k = 0; k < h->nen; k++) {
       const D *d = du + cn[k] * 3;
       for (int r = 0; r < 3; r++)
         for (int c = 0; c < 3; c++) F[r * 3 + c] += DNS(h, e, pt, k, c) * d[r];
@@ -565,6 +592,49 @@ D yield_hardening(const dnls *h, const D &evp, const D &shift)
 {
   const D x = evp + SQRT23 * shift;
   return (h->n * h->B * dpow(x, (h->n - 1.)));
+}
+
+// the one-point hexahedron's viscous hourglass force (dnl_oracle.c elem_hourglass; Flanagan and
+// Belytschko, Int. J. Numer. Meth. Eng. 17, 1981) on the Current velocities
+void elem_hourglass(const dnls *h, long e, D *fe)
+{
+  const long *cn = h->conn.data() + e * 8;
+  const D *v = h->fld[h->cur][1].data();
+  double hs[4][8];
+  for (int k = 0; k < 8; k++) {
+    const int sx = HX_XI[k], sy = HX_ETA[k], sz = HX_ZETA[k];
+    hs[0][k] = sx * sy;
+    hs[1][k] = sy * sz;
+    hs[2][k] = sz * sx;
+    hs[3][k] = sx * sy * sz;
+  }
+  D hx[4][3];
+  for (int q = 0; q < 4; q++)
+    for (int i = 0; i < 3; i++) {
+      D s = cst(0.);
+      for (int k = 0; k < 8; k++) s += hs[q][k] * h->coords[cn[k] * 3 + i];
+      hx[q][i] = s;
+    }
+  D g[4][8], qv[4][3];
+  for (int q = 0; q < 4; q++) {
+    for (int i = 0; i < 3; i++) qv[q][i] = cst(0.);
+    for (int k = 0; k < 8; k++) {
+      D s = cst(hs[q][k]);
+      for (int i = 0; i < 3; i++) s -= hx[q][i] * DNS(h, e, 0, k, i);
+      g[q][k] = s;
+      for (int i = 0; i < 3; i++) qv[q][i] += s * v[cn[k] * 3 + i];
+    }
+  }
+  const double E = h->young, Nu = h->nu, rho = h->rho;
+  const double c = sqrt((E * (1 - Nu)) / (rho * (1 + Nu) * (1 - 2 * Nu)));
+  const D V = h->weight[0] * h->detJ[IPX(h, e, 0)], cv = dcbrt(V);
+  const D ah = (0.25 * h->hourglass * rho * c) * (cv * cv);
+  for (int k = 0; k < 8; k++)
+    for (int i = 0; i < 3; i++) {
+      D s = cst(0.);
+      for (int q = 0; q < 4; q++) s += g[q][k] * qv[q][i];
+      fe[k * 3 + i] -= ah * s;
+    }
 }
 
 // Element::computeStress + Element::computeInternalForces (dnl_oracle.c elem_forces)
@@ -668,6 +738,7 @@ int elem_forces(dnls *h, long e, D *fe)
     if (h->etype == 0)
       for (int I = 0; I < nen; I++) fe[I * dim] -= (h->Nt[pt][I] * Sig[8] / R) * WxdJ;
   }
+  if (h->etype == 5) elem_hourglass(h, e, fe);
   return err;
 }
 
@@ -778,11 +849,14 @@ dnls *dnls_create(int etype, long N, long E, const double *coords, const long *c
                   const long *bc_kind, const double *bc_val, const long *bc_start,
                   const long *bc_nodes, double rho_b)
 {
-  if ((etype != 0 && etype != 1 && etype != 2) || N <= 0 || E <= 0) return nullptr;
+  if (etype < 0 || etype > 5 || N <= 0 || E <= 0) return nullptr;
   dnls *h = new dnls();
   h->etype = etype;
-  h->dim = etype == 1 ? 3 : 2;
-  h->nen = h->nip = etype == 1 ? 8 : 4;
+  h->dim = (etype == 0 || etype == 2) ? 2 : 3;
+  h->nen = (etype == 1 || etype == 5) ? 8 : (etype == 4 ? 10 : 4);
+  h->nip = etype == 1 ? 8 : ((etype == 3 || etype == 5) ? 1 : 4);
+  h->rho = mat[2];
+  h->hourglass = 0.05;
   h->N = N;
   h->E = E;
   h->conn.assign(conn, conn + E * h->nen);
@@ -855,6 +929,14 @@ dnls *dnls_create(int etype, long N, long E, const double *coords, const long *c
 }
 
 void dnls_destroy(dnls *h) { delete h; }
+
+/* the one-point hexahedron's hourglass coefficient (dnlo_set_hourglass) */
+int dnls_set_hourglass(dnls *h, double coefficient)
+{
+  if (!(coefficient >= 0.) || coefficient > 1e300) return 1;
+  h->hourglass = coefficient;
+  return 0;
+}
 
 /* nsteps explicit steps with the step sizes dts[0..nsteps): the ExplicitSolverCH::solve loop body
  * (predictions, internal forces on the current coordinates, explicit solve, swap). */

@@ -25,7 +25,8 @@ def _stale(out, src):
 
 
 def build(force: bool = False) -> str:
-    if force or _stale(LIB_PATH, "dnl_oracle.c") or _stale(SENS_PATH, "dnl_sens.cc"):
+    if (force or _stale(LIB_PATH, "dnl_oracle.c") or _stale(SENS_PATH, "dnl_sens.cc")
+            or _stale(LIB_PATH, "tet10_tables.h") or _stale(SENS_PATH, "tet10_tables.h")):
         subprocess.run(["make", "-C", HERE, "port"], check=True, capture_output=True)
     return LIB_PATH
 
@@ -221,6 +222,7 @@ def sens_lib():
         L.dnls_destroy.argtypes = [C.c_void_p]
         L.dnls_run.argtypes = [C.c_void_p, C.c_long, dp]
         L.dnls_coords.argtypes = [C.c_void_p, dp, dp]
+        L.dnls_set_hourglass.argtypes = [C.c_void_p, C.c_double]
         _sens = L
     return _sens
 
@@ -264,6 +266,8 @@ class SensOracle:
                                _lp(nodes), float(m.rho_b))
         if not self.h:
             raise ValueError("dnls_create rejected the model")
+        if L.dnls_set_hourglass(self.h, float(m.hourglass)):
+            raise ValueError("dnls_set_hourglass rejected the coefficient")
         self.model = m
         self.L = L
 

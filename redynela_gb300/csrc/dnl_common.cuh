@@ -62,8 +62,8 @@ __host__ __device__ constexpr int etype_nip(int et)
   return et == DNL_ELHEX8N3D ? 8 : ((et == DNL_ELTET4N3D || et == DNL_ELHEX8N3D_1PT) ? 1 : 4);
 }
 __host__ __device__ constexpr int etype_ns(int et) { return etype_dim(et) == 2 ? 4 : 6; }
-// element types with the forward-mode sensitivity path (tape and tangent kernels)
-__host__ __device__ constexpr bool etype_has_sens(int et) { return et <= DNL_ELQUA4N2D; }
+// element types with the forward-mode sensitivity path (tape and tangent kernels): all of them
+__host__ __device__ constexpr bool etype_has_sens(int et) { return etype_valid(et); }
 // element types whose time-step length is the quad's Courant length (else the tetrahedra's
 // shortest edge; ElHex8n3D has none)
 __host__ __device__ constexpr bool etype_quad(int et) { return et == DNL_ELQUA4NAX || et == DNL_ELQUA4N2D; }
@@ -287,6 +287,9 @@ struct SensElemArgs {
   const double *tape;  // [TapeLayout::NT][E*NIP]
   const double *tx;    // [dir][3][N]
   const double *tdu;   // [dir][3][N]
+  const double *v[3];  // Current velocities (the one-point hexahedron's hourglass force)
+  const double *tv;    // their tangents, [dir][3][N]
+  double hourglass;    // its coefficient
   double *tip;         // [dir][TanLayout::NCOMP][E*NIP]
   double *tfe;         // [dir][DIM][E*NEN]
   DevTime *tm;
@@ -416,35 +419,23 @@ __device__ __forceinline__ double quot(double a, double b, double r)
   return fma(fma(-q0, b, a), r, q0);
 }
 
-// CALL instantiated for the handle's element type, as ET (CALL in parentheses when it has commas):
-// DNL_BY_ETYPE over every element type, DNL_BY_ETYPE_SENS over those with the sensitivity path
-#define DNL_BY_ETYPE_SENS(etype, CALL)               \
-  do {                                               \
-    if ((etype) == DNL_ELQUA4NAX) {                  \
-      constexpr int ET = DNL_ELQUA4NAX;              \
-      CALL;                                          \
-    } else if ((etype) == DNL_ELQUA4N2D) {           \
-      constexpr int ET = DNL_ELQUA4N2D;              \
-      CALL;                                          \
-    } else {                                         \
-      constexpr int ET = DNL_ELHEX8N3D;              \
-      CALL;                                          \
-    }                                                \
-  } while (0)
-#define DNL_BY_ETYPE(etype, CALL)                    \
-  do {                                               \
-    if ((etype) == DNL_ELHEX8N3D_1PT) {              \
-      constexpr int ET = DNL_ELHEX8N3D_1PT;          \
-      CALL;                                          \
-    } else if ((etype) == DNL_ELTET4N3D) {           \
-      constexpr int ET = DNL_ELTET4N3D;              \
-      CALL;                                          \
-    } else if ((etype) == DNL_ELTET10N3D) {          \
-      constexpr int ET = DNL_ELTET10N3D;             \
-      CALL;                                          \
-    } else {                                         \
-      DNL_BY_ETYPE_SENS(etype, CALL);                \
-    }                                                \
+// CALL instantiated for the handle's element type, as ET (CALL in parentheses when it has commas)
+#define DNL_ET_CASE(etype, T, CALL) \
+  if ((etype) == (T)) {             \
+    constexpr int ET = (T);         \
+    CALL;                           \
+  }
+#define DNL_BY_ETYPE(etype, CALL)                                           \
+  do {                                                                      \
+    DNL_ET_CASE(etype, DNL_ELQUA4NAX, CALL)                                 \
+    else DNL_ET_CASE(etype, DNL_ELQUA4N2D, CALL)                            \
+    else DNL_ET_CASE(etype, DNL_ELHEX8N3D_1PT, CALL)                        \
+    else DNL_ET_CASE(etype, DNL_ELTET4N3D, CALL)                            \
+    else DNL_ET_CASE(etype, DNL_ELTET10N3D, CALL)                           \
+    else {                                                                  \
+      constexpr int ET = DNL_ELHEX8N3D;                                     \
+      CALL;                                                                 \
+    }                                                                       \
   } while (0)
 
 namespace dnl {

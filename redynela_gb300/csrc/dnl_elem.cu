@@ -1297,7 +1297,7 @@ int launch_elem_tape(dnl_handle *h, cudaStream_t s, double *tape)
   const int grid = (int)((threads + 127) / 128);
   prof_begin(h, s);
   if (!etype_has_sens(h->etype)) return DNL_ERR_ARG;
-  DNL_BY_ETYPE_SENS(h->etype, (k_elem<ET, true><<<grid, 128, 0, s>>>(a)));
+  DNL_BY_ETYPE(h->etype, (k_elem<ET, true><<<grid, 128, 0, s>>>(a)));
   prof_end(h, DNL_PROF_ELEM, s);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
@@ -1365,7 +1365,7 @@ int launch_elem_batch_tape(int etype, const ElemArgs &a, const int *elemInst, co
   if (!etype_has_sens(etype)) return DNL_ERR_ARG;
   const long threads = (long)a.E * etype_nip(etype);
   const int grid = (int)((threads + 127) / 128);
-  DNL_BY_ETYPE_SENS(etype, (k_elem_batch<ET, 128, true><<<grid, 128, 0, s>>>(a, elemInst, mats, tms)));
+  DNL_BY_ETYPE(etype, (k_elem_batch<ET, 128, true><<<grid, 128, 0, s>>>(a, elemInst, mats, tms)));
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }

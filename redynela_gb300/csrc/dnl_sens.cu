@@ -185,11 +185,28 @@ __global__ void k_to_nodes(int N, double *out, const double *c0, const double *c
     if ((x) != cudaSuccess) return DNL_ERR_CUDA; \
   } while (0)
 
+// the record and tangent-state widths depend on the dimension only (TapeLayout, TanLayout)
+static_assert(TapeLayout<DNL_ELTET4N3D>::NT == TapeLayout<DNL_ELHEX8N3D>::NT &&
+                  TapeLayout<DNL_ELTET10N3D>::NT == TapeLayout<DNL_ELHEX8N3D>::NT &&
+                  TapeLayout<DNL_ELHEX8N3D_1PT>::NT == TapeLayout<DNL_ELHEX8N3D>::NT &&
+                  TapeLayout<DNL_ELQUA4N2D>::NT == TapeLayout<DNL_ELQUA4NAX>::NT,
+              "tape width by dimension");
+static_assert(TanLayout<DNL_ELTET4N3D>::NCOMP == TanLayout<DNL_ELHEX8N3D>::NCOMP &&
+                  TanLayout<DNL_ELQUA4N2D>::NCOMP == TanLayout<DNL_ELQUA4NAX>::NCOMP,
+              "tangent state width by dimension");
+static int tape_nt(int etype)
+{
+  return etype_dim(etype) == 3 ? TapeLayout<DNL_ELHEX8N3D>::NT : TapeLayout<DNL_ELQUA4NAX>::NT;
+}
+static int tan_ncomp(int etype)
+{
+  return etype_dim(etype) == 3 ? TanLayout<DNL_ELHEX8N3D>::NCOMP : TanLayout<DNL_ELQUA4NAX>::NCOMP;
+}
+
 int sens_alloc(dnl_handle *h, SensState *S)
 {
   const long nIP = (long)h->E * h->nip, N = h->N;
-  const int NT = h->etype == DNL_ELHEX8N3D ? TapeLayout<DNL_ELHEX8N3D>::NT : TapeLayout<DNL_ELQUA4NAX>::NT;
-  const int NC = h->etype == DNL_ELHEX8N3D ? TanLayout<DNL_ELHEX8N3D>::NCOMP : TanLayout<DNL_ELQUA4NAX>::NCOMP;
+  const int NT = tape_nt(h->etype), NC = tan_ncomp(h->etype);
   const long nodal = (long)kSensParams * 3 * N;
   const long total = NT * nIP + nodal * 9 + (long)kSensParams * NC * nIP +
                      (long)kSensParams * h->dim * h->E * h->nen + 3 * N;
@@ -221,7 +238,7 @@ int sens_alloc(dnl_handle *h, SensState *S)
 // scheduled step size, each followed by its tangent launch.
 int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt)
 {
-  // the tangent formulas are those of the power law, one material, quads and hexahedra
+  // the tangent formulas are those of the power law and one material (per instance in a batch)
   if (!etype_has_sens(h->etype)) return DNL_ERR_ARG;
   if (!bt && (h->elemMat || h->mat.hard.law != DNL_HARD_POWER)) return DNL_ERR_ARG;
   for (int k = 0; k < nsteps; k++)
@@ -233,7 +250,7 @@ int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt)
   cudaStream_t s = h->stream;
   const long nIP = (long)h->E * h->nip;
   {
-    const int NT = h->etype == DNL_ELHEX8N3D ? TapeLayout<DNL_ELHEX8N3D>::NT : TapeLayout<DNL_ELQUA4NAX>::NT;
+    const int NT = tape_nt(h->etype);
     const size_t bytes = sizeof(double) * (size_t)((S->out - S->mem) - NT * nIP);
     CKS(cudaMemsetAsync(S->tx, 0, bytes, s));
   }
@@ -265,6 +282,7 @@ int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt)
   ea.tfe = S->tfe;
   ea.tm = h->tm;
   ea.mat = h->mat;
+  ea.hourglass = h->hourglass;
   ea.elemInst = bt ? bt->elemInst : nullptr;
   ea.mats = bt ? bt->mats : nullptr;
   SensNodeArgs na;
@@ -311,8 +329,12 @@ int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt)
       r = launch_elem_tape(h, s, S->tape);
     }
     if (r) return r;
-    for (int c = 0; c < 3; c++) ea.du[c] = h->bank[h->cur].du[c];
+    for (int c = 0; c < 3; c++) {
+      ea.du[c] = h->bank[h->cur].du[c];
+      ea.v[c] = h->bank[h->cur].v[c];
+    }
     ea.tdu = S->tb[h->cur][0];
+    ea.tv = S->tb[h->cur][1];
     prof_begin(h, s);
     r = launch_elem_tan(h->etype, ea, s);
     prof_end(h, DNL_PROF_TANGENT, s);

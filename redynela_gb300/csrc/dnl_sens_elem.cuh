@@ -423,7 +423,8 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
     sig[i][i] += pf;
     dS[i][i] += dpn;  // now d Sig
   }
-  double W = detJ, dW = ddetJ, dhoop = 0.;
+  // the Gauss weight (1 for the quads and the hexahedron; 1/6, 1/24, 8 for the others)
+  double W = weighted<ET>(detJ), dW = weighted<ET>(ddetJ), dhoop = 0.;
   if (AXI) {
     W = detJ * (kDeuxPi * Rad);
     dW = kDeuxPi * fma(ddetJ, Rad, detJ * dRad);
@@ -443,8 +444,7 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
       }
       dM[l][i] = fma(ds, W, s * dW);
     }
-  // every point's dM (and hoop tangent) through the group's shared memory; lane k assembles node
-  // k (the quads and the hexahedron have as many nodes as points)
+  // every point's dM (and hoop tangent) through the group's shared memory
   constexpr int ST = DIM * DIM + (AXI ? 1 : 0);
   double *mine = red + pt * ST;
 #pragma unroll
@@ -453,7 +453,10 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
     for (int i = 0; i < DIM; i++) mine[l * DIM + i] = dM[l][i];
   if (AXI) mine[DIM * DIM] = dhoop;
   __syncwarp();
-  if (valid) {
+  if (!valid) return;
+  double *tfe = a.tfe + (long)dir * DIM * a.E * NEN;
+  if constexpr (NEN == NIP) {
+    // the quads and the hexahedron: lane k assembles node k
     double s[DIM];
 #pragma unroll
     for (int i = 0; i < DIM; i++) s[i] = 0.0;
@@ -468,9 +471,114 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
       }
       if (AXI) s[0] = fma(SH::N(q, pt), Mq[DIM * DIM], s[0]);
     }
-    double *tfe = a.tfe + (long)dir * DIM * a.E * NEN;
 #pragma unroll
     for (int i = 0; i < DIM; i++) tfe[(long)i * a.E * NEN + (long)e * NEN + pt] = ineg(s[i]);
+  } else {
+    // the tetrahedra and the one-point hexahedron: lane pt assembles nodes pt, pt + NIP, ...
+    constexpr bool HG = ET == DNL_ELHEX8N3D_1PT;
+    // hourglass force f_k = a_h sum_a gamma_ak (gamma_a . v) (added to the row, as in the primal
+    // pass) and its tangent: gamma_ak = h_ak - sum_i (h_a . x_i) b_ki with b_k = J^-T dN_k/dxi, so
+    // d gamma_ak = - sum_i (h_a . dx_i) b_ki + (h_a . x_i) db_ki; d a_h = (2/3) a_h dV / V
+    double hx[4][3], dhx[4][3], qv[4][3], dqv[4][3], ah = 0., dah = 0.;
+    auto hs = [](int q, int k) {
+      const int sx = sgx(k), sy = sgy(k), sz = sgz(k);
+      const int par = q == 0 ? sx ^ sy : (q == 1 ? sy ^ sz : (q == 2 ? sz ^ sx : sx ^ sy ^ sz));
+      return (q == 3 ? par : !par) ? 1. : -1.;
+    };
+    auto gam_k = [&](int k, double g[4], double dg[4]) {
+      double b[3], db[3];
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        double u = 0., du = 0.;
+#pragma unroll
+        for (int l = 0; l < 3; l++) {
+          u = fma(Ji[l][i], SH::dN(0, k, l), u);
+          du = fma(dJi[l][i], SH::dN(0, k, l), du);
+        }
+        b[i] = u;
+        db[i] = du;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        double u = hs(q, k), du = 0.;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          u = fma(-hx[q][i], b[i], u);
+          du = fma(-dhx[q][i], b[i], fma(-hx[q][i], db[i], du));
+        }
+        g[q] = u;
+        dg[q] = du;
+      }
+    };
+    if constexpr (HG) {
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) hx[q][i] = dhx[q][i] = qv[q][i] = dqv[q][i] = 0.;
+#pragma unroll
+      for (int k = 0; k < NEN; k++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const double xk = a.x[i][node[k]], txk = tx[(long)i * N + node[k]];
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            hx[q][i] = fma(hs(q, k), xk, hx[q][i]);
+            dhx[q][i] = fma(hs(q, k), txk, dhx[q][i]);
+          }
+        }
+      const double *tv = a.tv + (long)dir * 3 * N;
+#pragma unroll
+      for (int k = 0; k < NEN; k++) {
+        double g[4], dg[4];
+        gam_k(k, g, dg);
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const double vk = a.v[i][node[k]], tvk = tv[(long)i * N + node[k]];
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            qv[q][i] = fma(g[q], vk, qv[q][i]);
+            dqv[q][i] = fma(dg[q], vk, fma(g[q], tvk, dqv[q][i]));
+          }
+        }
+      }
+      const double cv = cbrt(weighted<ET>(detJ));
+      ah = 0.25 * a.hourglass * m.rho * m.Cs * (cv * cv);
+      dah = ah * (2. / 3.) * ddetJ * nr_rcp(detJ);
+    }
+#pragma unroll
+    for (int j = 0; j < (NEN + NIP - 1) / NIP; j++) {
+      const int k = pt + j * NIP;
+      if (k >= NEN) break;
+      double s[DIM];
+#pragma unroll
+      for (int i = 0; i < DIM; i++) s[i] = 0.0;
+#pragma unroll
+      for (int q = 0; q < NIP; q++) {
+        const double *Mq = red + q * ST;
+#pragma unroll
+        for (int l = 0; l < DIM; l++) {
+          const double d = SH::dN(q, k, l);
+#pragma unroll
+          for (int i = 0; i < DIM; i++) s[i] = fma(d, Mq[l * DIM + i], s[i]);
+        }
+      }
+      if constexpr (HG) {
+        double g[4], dg[4];
+        gam_k(k, g, dg);
+#pragma unroll
+        for (int i = 0; i < DIM; i++) {
+          double f = 0., df = 0.;
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            f = fma(g[q], qv[q][i], f);
+            df = fma(dg[q], qv[q][i], fma(g[q], dqv[q][i], df));
+          }
+          s[i] = fma(dah, f, fma(ah, df, s[i]));
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < DIM; i++) tfe[(long)i * a.E * NEN + (long)e * NEN + k] = ineg(s[i]);
+    }
   }
 }
 
@@ -497,7 +605,7 @@ int launch_elem_tan(int etype, const SensElemArgs &a, cudaStream_t s)
   if (!etype_has_sens(etype)) return DNL_ERR_ARG;
   const long threads = (long)a.E * kSensParams * etype_nip(etype);
   const int grid = (int)((threads + 127) / 128);
-  DNL_BY_ETYPE_SENS(etype, (k_elem_tan<ET><<<grid, 128, 0, s>>>(a)));
+  DNL_BY_ETYPE(etype, (k_elem_tan<ET><<<grid, 128, 0, s>>>(a)));
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }

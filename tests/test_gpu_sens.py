@@ -31,18 +31,34 @@ def schedule(m, nsteps):
     return np.array(dts), o.array("coords").reshape(-1, 3).copy(), o.array("mass").copy()
 
 
-@pytest.mark.parametrize("etype,nsteps", [("axi", 300), ("hex", 80)])
+def _model(etype):
+    return {"axi": lambda: meshes.taylor_axi(5, 50), "hex": lambda: meshes.taylor_hex(4, 10),
+            "tet4": lambda: meshes.taylor_tet(6, 8),
+            "tet10": lambda: meshes.taylor_tet(4, 6, quadratic=True),
+            "hex1pt": lambda: meshes.taylor_hex_1pt(6, 10)}[etype]()
+
+
+# the tetrahedra and the one-point hexahedron: the same tangent pass, the tetrahedra's node-by-node
+# kinematics and force rows, the hourglass force's tangent.  ElTet10n3D: one step -- the
+# reference's element has blown up by the end of the second (negative lumped corner masses) --
+# in which every point is still elastic, so only d/d|v0| is not zero and the hardening
+# parameters' derivatives must be exactly zero
+@pytest.mark.parametrize("etype,nsteps", [("axi", 300), ("hex", 80), ("tet4", 80), ("tet10", 1),
+                                          ("hex1pt", 80)])
 def test_sensitivities_vs_dual_oracle(gpu_lib, etype, nsteps):
-    m = meshes.taylor_axi(5, 50) if etype == "axi" else meshes.taylor_hex(4, 10)
+    m = _model(etype)
     dts, x_ref, mass = schedule(m, nsteps)
     s = SensOracle(m, mass=mass)
     s.run(dts)
     xo, dxo = s.coords()
     d = gpu_lib.GpuDomain(m)
     x, dx = d.sensitivities(dts)
-    pos_tol = 1e-12 if etype == "axi" else 1e-8
+    pos_tol = 1e-12 if etype in ("axi", "tet10") else 1e-8
     assert np.max(np.abs(x - xo)) <= pos_tol * np.max(np.abs(xo))
     for p in range(4):
+        if etype == "tet10" and p < 3:
+            assert not np.any(dxo[p]) and not np.any(dx[p]), p
+            continue
         assert np.linalg.norm(dxo[p]) > 0
         assert rel(dx[p], dxo[p]) <= SENS_TOL, (p, rel(dx[p], dxo[p]))
 
@@ -133,11 +149,17 @@ def _small_necking(count):
                                 n=float(rng.uniform(0.2, 0.5))) for _ in range(count)]
 
 
-@pytest.mark.parametrize("kind", ["hex", "axi"])
+@pytest.mark.parametrize("kind", ["hex", "axi", "tet4", "hex1pt"])
 def test_batch_sensitivities_match_single_meshes(gpu_lib, kind):
     """dnl_batch_sens_run over several instances = dnl_sens_run of each instance alone, bit for
-    bit (hex necking bars with three parameter sets; uneven axisymmetric bars)."""
-    if kind == "hex":
+    bit (hex necking bars with three parameter sets; uneven axisymmetric, tetrahedral and one-point
+    hexahedral bars)."""
+    if kind in ("tet4", "hex1pt"):
+        mk = meshes.taylor_tet if kind == "tet4" else meshes.taylor_hex_1pt
+        models = [mk(4, 6), mk(5, 7, speed=260.0, A=120e6, n=0.45), mk(4, 5, speed=150.0, B=380e6)]
+        # one schedule for all: the smallest of the instances' own stable steps
+        dts = 0.8 * np.min([schedule(m, 60)[0] for m in models], axis=0)
+    elif kind == "hex":
         models = _small_necking(3)
         d0 = gpu_lib.GpuDomain(models[0])
         d0.prologue()  # the Pulse estimate of the stable step

@@ -136,9 +136,3 @@ def test_tet4_batch_matches_single_meshes_bitwise(gpu_lib):
         assert d.step(60) == 60
         assert np.array_equal(b.coords(i), d.get_state("coords")["coords"]), i
         assert np.array_equal(b.fint(i), d.fint()), i
-
-
-def test_tet_sensitivities_are_refused(gpu_lib):
-    d = gpu_lib.GpuDomain(meshes.taylor_tet(4, 3))
-    with pytest.raises(RuntimeError):
-        d.sensitivities(np.full(5, 1e-8))
