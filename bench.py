@@ -42,6 +42,11 @@ from redynela_gb300 import meshes  # noqa: E402
 # mid-run window); bench.py scales it by the elements of the workload
 ELEM_TRAFFIC_BYTES_PER_ELEMENT = 308.85e6 / 126400
 
+# FP64 thread-instructions of one k_elem<ElHex8n3D> launch per Gauss point, from the
+# sm__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum counters of the same mid-run window
+# (571,665,728 / 140,096,488 / 256,965,144 over 1,011,200 points); a DFMA is two flops
+HEX_FP64_FLOPS_PER_POINT = (2 * 571665728 + 140096488 + 256965144) / 1011200
+
 
 def workload(name: str, layers: int = 400):
     if name == "hex":
@@ -286,6 +291,15 @@ def main_ours(args):
                 "avg_launch_ms": elem_ms / elem_n if elem_n else None,
                 "fp64_dfma_peak_tflops_measured": fp64_peak,
                 "note": "the element pass is FP64-pipe bound on GB300; see profiles/"}
+    if model.etype == meshes.ELHEX8N3D and elem_n and fp64_peak:
+        # the bound that applies: FP64 flops per launch (the counted mix per Gauss point) over the
+        # live launch time, against the DFMA peak measured on this GPU
+        fl = HEX_FP64_FLOPS_PER_POINT * model.E * 8 / (elem_ms / elem_n * 1e-3) / 1e12
+        roofline["fp64"] = {"achieved_tflops": fl, "peak_tflops": fp64_peak, "frac": fl / fp64_peak,
+                            "flops_per_gauss_point": HEX_FP64_FLOPS_PER_POINT,
+                            "source": "ncu FP64 instruction counts of the 40x40x100 bar's mid-run "
+                                      "window (profiles/k_elem_hex_40x40x100_window.md); peak: "
+                                      "a DFMA loop timed at the start of this run"}
     kernel_share = {k: round(v[0] / ms, 4) for k, v in prof.items() if v[1]}
 
     # ---- end to end through the C ABI with page-locked host buffers
