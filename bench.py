@@ -15,7 +15,7 @@ wave has crossed the bar and the impact end is plastic.
 `value` is measured with device-resident state (CUDA events on the library's stream);
 `e2e` goes through the C ABI with page-locked host buffers: each step uploads the nodal state the
 caller owns (coordinates, delta_disp, velocity, acceleration, displacement), advances one step and
-reads it back.  The reference arm (--impl reference) times the oracle's CPU restatement of the
+reads it back, over the same increments as `value` (a second handle brought to the same state).  The reference arm (--impl reference) times the oracle's CPU restatement of the
 reference (oracle/dnl_oracle.c, OpenMP on all host cores) on a bounded slice of the same bar.
 Multi-GPU: independent replicas, one per rank (the explicit step has no cross-replica exchange).
 """
@@ -243,12 +243,16 @@ def main_ours(args):
     dynela.set_device(local)
     model, name = workload(args.config, args.layers)
 
+    def to_window(dom):
+        # advance, untimed, to the start of the measured window (runs are bitwise deterministic,
+        # so every handle advanced this way holds the same state)
+        dom.prologue()
+        while dom.time_info()["time"] < args.start_us * 1e-6:
+            if dom.step(50) == 0:
+                break
+
     d = dynela.GpuDomain(model)
-    d.prologue()
-    # advance, untimed, to the start of the measured window
-    while d.time_info()["time"] < args.start_us * 1e-6:
-        if d.step(50) == 0:
-            break
+    to_window(d)
     window = d.time_info()
     snapshot = None
     if rank == 0 and not args.no_cpu:
@@ -302,22 +306,27 @@ def main_ours(args):
                                       "a DFMA loop timed at the start of this run"}
     kernel_share = {k: round(v[0] / ms, 4) for k, v in prof.items() if v[1]}
 
-    # ---- end to end through the C ABI with page-locked host buffers
-    e2e_steps = min(args.steps, 20)
+    # ---- end to end through the C ABI with page-locked host buffers, over the same increments as
+    # the timed region: a second handle brought to the same state (the cost of a step, and of the
+    # Pulse iteration most of all, grows as the impact proceeds, so a later window would not compare)
+    e2e_steps = args.steps
     N = model.N
+    d.close()
+    d = dynela.GpuDomain(model)
+    to_window(d)
+    d.step(args.warmup)
     host = {k: dynela.PinnedArray((N, 3)) for k in ("coords", "du", "v", "a", "disp")}
     st = d.get_state(*host.keys())
     for k, pa in host.items():
         pa.array[:] = st[k]
+    sv = dynela.StateView()
+    for k, pa in host.items():
+        setattr(sv, k, pa.array.ctypes.data_as(dynela._dp))
     d.timer_mark(2)
     e2e_done = 0
     for _ in range(e2e_steps):
         d.set_state(**{k: pa.array for k, pa in host.items()})
         e2e_done += d.step(1)
-        out = {k: pa.array for k, pa in host.items()}
-        sv = dynela.StateView()
-        for k, a in out.items():
-            setattr(sv, k, a.ctypes.data_as(dynela._dp))
         d._check(d.L.dnl_get_state(d.h, dynela.C.byref(sv)))
     d.timer_mark(3)
     e2e_ms = d.timer_elapsed_ms(2, 3)
