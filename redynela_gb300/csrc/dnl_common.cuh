@@ -62,6 +62,23 @@ __host__ __device__ constexpr int etype_nip(int et)
   return et == DNL_ELHEX8N3D ? 8 : ((et == DNL_ELTET4N3D || et == DNL_ELHEX8N3D_1PT) ? 1 : 4);
 }
 __host__ __device__ constexpr int etype_ns(int et) { return etype_dim(et) == 2 ? 4 : 6; }
+
+// Edges of the quads and of the hexahedron along each reference axis (NE / DIM per axis, axis c
+// first), as (lo, hi) local nodes with hi on the + side of the axis; lo and hi packed 4 bits per
+// edge for run-time indices.  At a Gauss point the bilinear/trilinear dN/dxi_c of the two nodes of
+// an edge are opposite, so sum_k dN_k/dxi_c v_k = sum over the axis-c edges of w (v_hi - v_lo),
+// w the table value for the number of sign disagreements between the edge's other coordinates
+// and the point's (Shape::dN).
+template <int ET> struct Edges {
+  static constexpr int NE = 4;  // quads: xi edges 0-1, 3-2; eta edges 0-3, 1-2
+  static constexpr unsigned long long LO = 0x1030ull, HI = 0x2321ull;
+};
+template <> struct Edges<DNL_ELHEX8N3D> {
+  static constexpr int NE = 12;  // xi: 0-1 3-2 4-5 7-6; eta: 0-3 1-2 4-7 5-6; zeta: 0-4 1-5 2-6 3-7
+  static constexpr unsigned long long LO = 0x321054107430ull, HI = 0x765467236521ull;
+};
+__host__ __device__ constexpr int edge_node(unsigned long long packed, int e) { return (int)((packed >> (4 * e)) & 15); }
+
 // element types with the forward-mode sensitivity path (tape and tangent kernels): all of them
 __host__ __device__ constexpr bool etype_has_sens(int et) { return etype_valid(et); }
 // element types whose time-step length is the quad's Courant length (else the tetrahedra's

@@ -116,21 +116,6 @@ template <> struct Shape<DNL_ELHEX8N3D> {
   }
 };
 
-// Edges of the quads and of the hexahedron along each reference axis (NE / DIM per axis, axis c
-// first), as (lo, hi) local nodes with hi on the + side of the axis; lo and hi packed 4 bits per
-// edge for run-time indices.  At a Gauss point the bilinear/trilinear dN/dxi_c of the two nodes of
-// an edge are opposite, so sum_k dN_k/dxi_c v_k = sum over the axis-c edges of w (v_hi - v_lo),
-// w the table value for the number of sign disagreements between the edge's other coordinates
-// and the point's (Shape::dN).
-template <int ET> struct Edges {
-  static constexpr int NE = 4;  // quads: xi edges 0-1, 3-2; eta edges 0-3, 1-2
-  static constexpr unsigned long long LO = 0x1030ull, HI = 0x2321ull;
-};
-template <> struct Edges<DNL_ELHEX8N3D> {
-  static constexpr int NE = 12;  // xi: 0-1 3-2 4-5 7-6; eta: 0-3 1-2 4-7 5-6; zeta: 0-4 1-5 2-6 3-7
-  static constexpr unsigned long long LO = 0x321054107430ull, HI = 0x765467236521ull;
-};
-__host__ __device__ constexpr int edge_node(unsigned long long packed, int e) { return (int)((packed >> (4 * e)) & 15); }
 
 // ElTet4n3D (ElTet4n3D.C:33-57): one point, N = 1/4, dN/dxi of the barycentric coordinates
 template <> struct Shape<DNL_ELTET4N3D> {

@@ -213,18 +213,51 @@ __global__ void __launch_bounds__(128) k_pulse_kx(PulseArgs a)
   // G(r, l) = sum_k x_k(r) dN/dxi_k(l); grad = G J^-1
   double G[DIM][DIM] = {};
   double ur = 0.;  // axi: sum N_k x_k(r)
-  int node[NEN];
+  double *buf = &red[wib][slot][0][0];  // this element's shared memory, NIP x NEN*DIM doubles
+  constexpr bool EDGES = ET == DNL_ELHEX8N3D || ET == DNL_ELQUA4NAX || ET == DNL_ELQUA4N2D;
+  if constexpr (EDGES) {
+    // from the element's edge differences (a few per lane, exchanged through its shared memory):
+    // the dN/dxi_c of an edge's two nodes are opposite at every Gauss point (Edges)
+    using EG = Edges<ET>;
+    constexpr int NE = EG::NE, PER = NE / DIM;
 #pragma unroll
-  for (int k = 0; k < NEN; k++) {
-    node[k] = a.conn[(long)k * a.E + e];
-    double xk[DIM];
+    for (int j = 0; j < (NE + NIP - 1) / NIP; j++) {
+      const int eg = pt + j * NIP;
+      if (eg < NE) {
+        const int lo = __ldg(a.conn + (long)edge_node(EG::LO, eg) * a.E + e);
+        const int hi = __ldg(a.conn + (long)edge_node(EG::HI, eg) * a.E + e);
 #pragma unroll
-    for (int r = 0; r < DIM; r++) xk[r] = a.ev[(long)node[k] * DIM + r];
+        for (int r = 0; r < DIM; r++) buf[eg * DIM + r] = a.ev[(long)hi * DIM + r] - a.ev[(long)lo * DIM + r];
+      }
+    }
+    __syncwarp();
 #pragma unroll
-    for (int r = 0; r < DIM; r++)
+    for (int c = 0; c < DIM; c++)
 #pragma unroll
-      for (int l = 0; l < DIM; l++) G[r][l] = fma(xk[r], pdN<ET>(pt, k, l), G[r][l]);
-    if (AXI) ur = fma(pN<ET>(pt, k), xk[0], ur);
+      for (int q = 0; q < PER; q++) {
+        const int eg = c * PER + q;
+        const double w = pdN<ET>(pt, edge_node(EG::HI, eg), c);
+#pragma unroll
+        for (int r = 0; r < DIM; r++) G[r][c] = fma(w, buf[eg * DIM + r], G[r][c]);
+      }
+    __syncwarp();  // the force exchange reuses the buffer
+    if (AXI) {
+#pragma unroll
+      for (int k = 0; k < NEN; k++) ur = fma(pN<ET>(pt, k), a.ev[(long)__ldg(a.conn + (long)k * a.E + e) * DIM], ur);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < NEN; k++) {
+      const int nk = a.conn[(long)k * a.E + e];
+      double xk[DIM];
+#pragma unroll
+      for (int r = 0; r < DIM; r++) xk[r] = a.ev[(long)nk * DIM + r];
+#pragma unroll
+      for (int r = 0; r < DIM; r++)
+#pragma unroll
+        for (int l = 0; l < DIM; l++) G[r][l] = fma(xk[r], pdN<ET>(pt, k, l), G[r][l]);
+      if (AXI) ur = fma(pN<ET>(pt, k), xk[0], ur);
+    }
   }
   double gr[DIM][DIM];
 #pragma unroll
@@ -265,6 +298,37 @@ __global__ void __launch_bounds__(128) k_pulse_kx(PulseArgs a)
       M[l][i] = s * W;
     }
   const double hw = AXI ? hoop / Rad * W : 0.;
+  if constexpr (NEN == NIP) {
+    // the quads and the hexahedron: every point's J^-1 S W (and hoop term) through the element's
+    // shared memory; lane k assembles node k from all of them
+    constexpr int ST = DIM * DIM + (AXI ? 1 : 0);
+    double *mine = buf + pt * ST;
+#pragma unroll
+    for (int l = 0; l < DIM; l++)
+#pragma unroll
+      for (int i = 0; i < DIM; i++) mine[l * DIM + i] = M[l][i];
+    if (AXI) mine[DIM * DIM] = hw;
+    __syncwarp();
+    if (valid) {
+      double f[DIM];
+#pragma unroll
+      for (int i = 0; i < DIM; i++) f[i] = 0.;
+#pragma unroll
+      for (int q = 0; q < NIP; q++) {
+        const double *Mq = buf + q * ST;
+#pragma unroll
+        for (int l = 0; l < DIM; l++) {
+          const double d = pdN<ET>(q, pt, l);
+#pragma unroll
+          for (int i = 0; i < DIM; i++) f[i] = fma(d, Mq[l * DIM + i], f[i]);
+        }
+        if (AXI) f[0] = fma(pN<ET>(q, pt), Mq[DIM * DIM], f[0]);
+      }
+#pragma unroll
+      for (int i = 0; i < DIM; i++) a.kx[(long)i * a.E * NEN + (long)e * NEN + pt] = f[i];
+    }
+    return;
+  }
   double *row = red[wib][slot][pt];
 #pragma unroll
   for (int k = 0; k < NEN; k++)
