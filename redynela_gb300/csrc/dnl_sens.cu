@@ -8,6 +8,7 @@
 // initial-velocity magnitude |v0|) -- four tangent copies of every nodal field and
 // integration-point variable.  Four parameters make the forward mode cheaper than a reverse
 // (adjoint) sweep: no trajectory is stored or recomputed, so no checkpoints are needed.
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -29,7 +30,24 @@ struct SensState {
   double *out = nullptr;   // N*3 staging for node-major results
   int dtsCap = 0;
   std::vector<double> schedule;  // dnl_set_dt_schedule
+  // single-mesh runs: two consecutive steps (bank parity 0 then 1, or 1 then 0) captured as a CUDA
+  // graph and replayed; the element kernels take the material by value, so a graph is valid for
+  // the material, hourglass coefficient and schedule buffer it was captured with
+  cudaGraphExec_t pair[2] = {nullptr, nullptr};
+  long long pairLaunches[2] = {0, 0};
+  Material pairMat;
+  double pairHourglass = 0.;
+  const double *pairDts = nullptr;
 };
+
+static void drop_pairs(SensState *S)
+{
+  for (int p = 0; p < 2; p++)
+    if (S->pair[p]) {
+      cudaGraphExecDestroy(S->pair[p]);
+      S->pair[p] = nullptr;
+    }
+}
 
 namespace {
 
@@ -305,7 +323,9 @@ int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt)
   na.tms = bt ? bt->tms : nullptr;
   const dim3 ngrid((h->N + 255) / 256, kSensParams);
   const int tgrid = (ninst + 127) / 128;
-  for (int k = 0; k < nsteps; k++) {
+  // one step: the primal launches with the scheduled step size, each followed by its tangent
+  auto one_step = [&]() -> int {
+    int r;
     k_sens_dt<<<tgrid, 128, 0, s>>>(tms, ninst, S->dts, 0);
     launch_counter()++;
     if (bt)
@@ -358,7 +378,49 @@ int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt)
     h->cur = 1 - h->cur;
     k_sens_dt<<<tgrid, 128, 0, s>>>(tms, ninst, S->dts, 1);
     launch_counter()++;
-    if (cudaPeekAtLastError() != cudaSuccess) return DNL_ERR_CUDA;
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
+  };
+  // single-mesh runs replay two-step graphs (launch-latency bound on small meshes); batches, odd
+  // remainders and profiled runs launch step by step
+  if (S->pairDts != S->dts || std::memcmp(&S->pairMat, &h->mat, offsetof(Material, hard)) != 0 ||
+      S->pairHourglass != h->hourglass)
+    drop_pairs(S);
+  int k = 0;
+  while (k < nsteps) {
+    if (!bt && !h->profiling && nsteps - k >= 2) {
+      const int par = h->cur;
+      if (!S->pair[par]) {
+        const long long c0 = launch_counter();
+        cudaGraph_t g;
+        if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return DNL_ERR_CUDA;
+        int rr = one_step();
+        if (!rr) rr = one_step();
+        const cudaError_t ce = cudaStreamEndCapture(s, &g);
+        h->cur = par;  // nothing ran: the host's bank parity stays with the device state
+        if (rr) {
+          if (ce == cudaSuccess) cudaGraphDestroy(g);
+          return rr;
+        }
+        if (ce != cudaSuccess) return DNL_ERR_CUDA;
+        const cudaError_t ie = cudaGraphInstantiate(&S->pair[par], g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+          S->pair[par] = nullptr;
+          return DNL_ERR_CUDA;
+        }
+        S->pairLaunches[par] = launch_counter() - c0;
+        launch_counter() = c0;
+        S->pairMat = h->mat;
+        S->pairHourglass = h->hourglass;
+        S->pairDts = S->dts;
+      }
+      if (cudaGraphLaunch(S->pair[par], s) != cudaSuccess) return DNL_ERR_CUDA;
+      launch_counter() += S->pairLaunches[par];
+      k += 2;  // two bank swaps: the parity is unchanged
+    } else {
+      if ((r = one_step())) return r;
+      k++;
+    }
   }
   std::vector<DevTime> t(ninst);
   CKS(cudaMemcpyAsync(t.data(), tms, sizeof(DevTime) * ninst, cudaMemcpyDeviceToHost, s));
@@ -397,6 +459,7 @@ void sens_free(dnl_handle *h)
 {
   SensState *S = (SensState *)h->sens;
   if (!S) return;
+  drop_pairs(S);
   if (S->mem) cudaFree(S->mem);
   if (S->dts) cudaFree(S->dts);
   delete S;

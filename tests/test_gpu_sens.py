@@ -188,3 +188,27 @@ def test_hex_batch_refuses_plain_stepping(gpu_lib):
     b = gpu_lib.BatchDomain(_small_necking(2))
     with pytest.raises(gpu_lib.DnlError):
         b.step(1)
+
+
+def test_graph_replay_matches_step_by_step(gpu_lib):
+    """dnl_sens_run replays two-step CUDA graphs on a single mesh; a profiled run launches step by
+    step.  Both, with an odd step count (the last step eager) and twice on one handle, bit for
+    bit; and after dnl_reset with another material the graphs are recaptured."""
+    m = meshes.taylor_axi(4, 30)
+    dts, _, _ = schedule(m, 61)
+    d = gpu_lib.GpuDomain(m)
+    x1, dx1 = d.sensitivities(dts)
+    d.reset(m)
+    x2, dx2 = d.sensitivities(dts)
+    ref = gpu_lib.GpuDomain(m)
+    ref.profile_begin()
+    x3, dx3 = ref.sensitivities(dts)
+    ref.profile_end()
+    for x, dx in ((x2, dx2), (x3, dx3)):
+        assert np.array_equal(x, x1) and np.array_equal(dx, dx1)
+    m2 = gpu_lib.model_with_params(m, 120e6, 280e6, 0.4, 240.0)
+    d.reset(m2)
+    x4, dx4 = d.sensitivities(dts)
+    x5, dx5 = gpu_lib.GpuDomain(m2).sensitivities(dts)
+    assert np.array_equal(x4, x5) and np.array_equal(dx4, dx5)
+    assert not np.array_equal(x4, x1)
