@@ -1,0 +1,84 @@
+"""The 3D Taylor bar at the benchmark's size (40x40 cross-section grid clipped to the radius, 400
+layers: 505,600 ElHex8n3D, 539,345 nodes, Pulse time step) against the oracle on the same mesh.
+
+The oracle cannot run the whole 80 us here, so the bar is compared where a CPU can follow it: the
+prologue and first steps from t = 0 (1e-12 on the forces, as on the small bars), and one element
+pass from the GPU's own mid-run state at t = 10 us -- the window bench.py times, with the impact
+end plastic -- injected into the oracle (1e-12 on the forces and on the updated state).  Runs are
+deterministic: the CSR assembly has no atomics, so two handles give the same trajectory bit for
+bit."""
+
+import os
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from redynela_gb300 import meshes
+
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL = 1e-12
+STATE_TOL = 1e-12
+
+
+def rel(a, b):
+    a, b = np.asarray(a).ravel(), np.asarray(b).ravel()
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.fixture(scope="module")
+def bar():
+    m = meshes.taylor_hex(40, 400)
+    assert m.E == 505600
+    return m
+
+
+def test_full_size_prologue_and_first_steps_vs_oracle(gpu_lib, bar):
+    o = Oracle(bar, threads=os.cpu_count() or 1)
+    o.prologue()
+    d = gpu_lib.GpuDomain(bar)
+    d.prologue()
+    assert rel(d.get_state("mass")["mass"], o.array("mass")) == 0.0
+    assert abs(d.time_step() - o.get("dt")) <= 1e-10 * o.get("dt")
+    for k in range(3):
+        o.steps(1)
+        assert d.step(1) == 1
+        fo = o.array("fint")
+        if np.linalg.norm(fo) > 0:
+            assert rel(d.fint(), fo) <= FORCE_TOL, k
+        assert abs(d.time_info()["time"] - o.get("time")) <= 1e-10 * o.get("time")
+    x, xo = d.get_state("coords")["coords"].ravel(), o.array("coords")
+    assert np.max(np.abs(x - xo)) <= 1e-12 * np.max(np.abs(xo))
+
+
+def test_full_size_mid_run_pass_vs_oracle(gpu_lib, bar):
+    d = gpu_lib.GpuDomain(bar)
+    d.prologue()
+    while d.time_info()["time"] < 10e-6:
+        assert d.step(50) > 0
+    info = d.time_info()
+    st = d.get_state("coords", "du", "v", "a", "disp", "S", "Eps", "EpsPlas", "p", "evp")
+    assert np.max(st["evp"]) > 1e-3  # the impact end has yielded
+    o = Oracle(bar, threads=os.cpu_count() or 1)
+    o.prologue()
+    o.inject(coords=st["coords"], du=st["du"], v=st["v"], a=st["a"], disp=st["disp"], S=st["S"],
+             Eps=st["Eps"], EpsPlas=st["EpsPlas"], p=st["p"], evp=st["evp"], dt=info["time_step"])
+    o.internal_matrices()
+    fo = o.internal_forces()
+    f = d.internal_forces(coords=st["coords"], du=st["du"], dt=info["time_step"])
+    assert rel(f, fo) <= FORCE_TOL
+    out = d.get_state("S", "EpsPlas", "evp", "p")
+    for k in out:
+        assert rel(out[k], o.array(k)) <= STATE_TOL, k
+
+
+def test_full_size_runs_are_deterministic(gpu_lib, bar):
+    runs = []
+    for _ in range(2):
+        d = gpu_lib.GpuDomain(bar)
+        d.prologue()
+        assert d.step(30) == 30
+        runs.append((d.get_state("coords")["coords"], d.fint()))
+        d.close()
+    assert np.array_equal(runs[0][0], runs[1][0]) and np.array_equal(runs[0][1], runs[1][1])
