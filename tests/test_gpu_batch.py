@@ -79,3 +79,26 @@ def test_graph_capture_then_replay(gpu_lib):
     b.step_graph(20)
     for i in range(len(models)):
         assert np.array_equal(a.coords(i), b.coords(i)), i
+
+
+def test_full_size_batch_matches_single_meshes_bitwise(gpu_lib):
+    """The benchmark's batch at full size (256 seeded uneven bars, 1.28 M elements, autotuned block,
+    graph-replayed steps): a sample of instances, the smallest and largest among them, equal bit
+    for bit to the same bars run alone after 40 steps."""
+    models = meshes.taylor_batch(256, seed=0)
+    b = gpu_lib.BatchDomain(models)
+    b.prologue()
+    b.autotune(steps=3)
+    b.reset()
+    b.prologue()
+    b.step_graph(20)
+    b.step_graph(20)
+    sizes = [m.E for m in models]
+    sample = sorted({0, 37, 101, 200, 255, int(np.argmin(sizes)), int(np.argmax(sizes))})
+    for i in sample:
+        d = gpu_lib.GpuDomain(models[i])
+        assert d.step(40) == 40
+        assert np.array_equal(b.coords(i), d.get_state("coords")["coords"]), i
+        assert np.array_equal(b.fint(i), d.fint()), i
+        assert b.time_info(i)["time"] == d.time_info()["time"], i
+        d.close()
