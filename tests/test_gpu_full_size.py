@@ -6,7 +6,8 @@ prologue and first steps from t = 0 (1e-12 on the forces, as on the small bars),
 pass from the GPU's own mid-run state at t = 10 us -- the window bench.py times, with the impact
 end plastic -- injected into the oracle (1e-12 on the forces and on the updated state).  Runs are
 deterministic: the CSR assembly has no atomics, so two handles give the same trajectory bit for
-bit."""
+bit.  The two gradient workloads at their sizes -- the 20x200 axisymmetric bar and the 209,824-element
+necking bar through the batched path -- are held to the sensitivity oracle over their first steps."""
 
 import os
 
@@ -82,3 +83,62 @@ def test_full_size_runs_are_deterministic(gpu_lib, bar):
         runs.append((d.get_state("coords")["coords"], d.fint()))
         d.close()
     assert np.array_equal(runs[0][0], runs[1][0]) and np.array_equal(runs[0][1], runs[1][1])
+
+
+def _rel_p(dx, dxo, p):
+    return np.linalg.norm(dx[p] - dxo[p]) / np.linalg.norm(dxo[p])
+
+
+def test_full_size_gradient_bar_vs_dual_oracle(gpu_lib):
+    """The gradient workload's bar (20x200 ElQua4nAx, 4,000 elements), the first 200 steps of its
+    Courant schedule: derivatives of the final coordinates w.r.t. A, B, n, |v0| vs the sensitivity
+    oracle (FP64 dual numbers) to 1e-5, coordinates to 1e-12."""
+    from oracle.oracle import SensOracle
+    m = meshes.taylor_axi(20, 200)
+    o = Oracle(m)
+    o.prologue()
+    mass = o.array("mass").copy()
+    dts = []
+    for _ in range(200):
+        dts.append(o.get("dt"))
+        o.steps(1)
+    dts = np.array(dts)
+    s = SensOracle(m, mass=mass, threads=os.cpu_count() or 1)
+    s.run(dts)
+    xo, dxo = s.coords()
+    x, dx = gpu_lib.GpuDomain(m).sensitivities(dts)
+    assert np.max(np.abs(x - xo)) <= 1e-12 * np.max(np.abs(xo))
+    for p in range(4):
+        assert np.linalg.norm(dxo[p]) > 0, p
+        assert _rel_p(dx, dxo, p) <= 1e-5, (p, _rel_p(dx, dxo, p))
+
+
+def test_full_size_necking_batch_vs_dual_oracle(gpu_lib):
+    """The batched gradient workload's bar (209,824 hex8 necking bar, mass scaling x100), two
+    parameter sets through dnl_batch_sens_run over the first steps of its 3.55e-7 s schedule: the
+    first instance's derivatives vs the sensitivity oracle on the same bar to 1e-5 (the parameters
+    whose derivative is not yet zero), the second instance equal to its own single-mesh run."""
+    from oracle.oracle import SensOracle
+    models = meshes.necking_batch(2, seed=0, nz=166)
+    assert models[0].E == 209824
+    dts = np.full(2, models[0].tend / 30000)
+    out = gpu_lib.BatchDomain(models).sensitivities(dts)
+    g = gpu_lib.GpuDomain(models[0])
+    g.prologue()
+    mass = g.get_state("mass")["mass"].ravel().copy()
+    g.close()
+    s = SensOracle(models[0], mass=mass, threads=os.cpu_count() or 1)
+    s.run(dts)
+    xo, dxo = s.coords()
+    x, dx = out[0]
+    assert np.max(np.abs(x - xo)) <= 1e-12 * np.max(np.abs(xo))
+    checked = 0
+    for p in range(4):
+        if np.linalg.norm(dxo[p]) == 0:
+            assert not np.any(dx[p]), p
+            continue
+        assert _rel_p(dx, dxo, p) <= 1e-5, (p, _rel_p(dx, dxo, p))
+        checked += 1
+    assert checked >= 1
+    x1, dx1 = gpu_lib.GpuDomain(models[1]).sensitivities(dts)
+    assert np.array_equal(out[1][0], x1) and np.array_equal(out[1][1], dx1)
