@@ -2,7 +2,7 @@
 """Element-updates/s of DynELA's explicit step on GB300 (libdnlgpu, FP64).
 
 Workload (default): the 3D Taylor impact bar of ElHex8n3D -- a 40x40 cross-section grid clipped
-to the radius, 400 layers (505,600 elements, 538,137 nodes), copper J2 material
+to the radius, 400 layers (505,600 elements, 539,345 nodes), copper J2 material
 (A 90 MPa, B 292 MPa, n 0.31), impact speed 227 m/s, Chung-Hulbert explicit integration with the
 Pulse critical time step.  A step is one full explicit increment: element pass (kinematics, polar
 decomposition, radial return, forces), CSR assembly, nodal update and the time-step logic

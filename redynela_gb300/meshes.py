@@ -182,7 +182,7 @@ def taylor_hex(ncross: int = 40, nz: int = 400, radius: float = 3.2e-3, length: 
                rho_b: float = 0.8182) -> Model:
     """3D Taylor bar of ElHex8n3D: ncross x ncross cells over [-R, R]^2, cells with centre inside R.
 
-    For ncross=40, nz=400 this gives 1264 cells per layer, 505,600 elements and 538,137 nodes.
+    For ncross=40, nz=400 this gives 1264 cells per layer, 505,600 elements and 539,345 nodes.
     Nodes are numbered layer by layer (z slowest), then y, then x; only nodes used by a kept cell
     exist.  Hex node order follows ElHex8n3D (bottom face counter-clockwise, then top face).
     """
