@@ -1275,13 +1275,13 @@ int launch_elem(dnl_handle *h, cudaStream_t s, int gate)
 // the element pass with its per-integration-point record (forward-mode sensitivities)
 int launch_elem_tape(dnl_handle *h, cudaStream_t s, double *tape)
 {
+  if (!etype_has_sens(h->etype)) return DNL_ERR_ARG;
   ElemArgs a = elem_args(h);
   a.gate = 1;
   a.tape = tape;
   const long threads = (long)h->E * h->nip;
   const int grid = (int)((threads + 127) / 128);
   prof_begin(h, s);
-  if (!etype_has_sens(h->etype)) return DNL_ERR_ARG;
   DNL_BY_ETYPE(h->etype, (k_elem<ET, true><<<grid, 128, 0, s>>>(a)));
   prof_end(h, DNL_PROF_ELEM, s);
   launch_counter()++;
