@@ -131,24 +131,60 @@ __global__ void __launch_bounds__(128) k_pulse_setup(PulseArgs a)
   using T = Elem<ET>;
   constexpr int NIP = T::NIP, NEN = T::NEN, DIM = T::DIM;
   constexpr bool AXI = ET == DNL_ELQUA4NAX, TWO_D = DIM == 2;
+  constexpr bool EDGES = ET == DNL_ELHEX8N3D || ET == DNL_ELQUA4NAX || ET == DNL_ELQUA4N2D;
+  __shared__ double ex[128 / 32][EDGES ? 32 / NIP : 1][EDGES ? Edges<ET>::NE * DIM : 1];
   if (a.tm->done | a.tm->status) return;
   const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long nIP = (long)a.E * NIP;
-  if (gtid >= nIP) return;
-  const int e = (int)(gtid / NIP), pt = (int)(gtid % NIP);
+  if ((gtid & ~31L) >= nIP) return;  // whole warps only: the element's lanes exchange through ex
+  const bool valid = gtid < nIP;
+  const long g = valid ? gtid : nIP - 1;
+  const int e = (int)(g / NIP), pt = (int)(g % NIP);
   double J[DIM][DIM] = {};
   double Rad = 0.;
+  if constexpr (EDGES) {
+    // J from the element's edge differences, a few per lane, shared by its lanes (Edges)
+    using EG = Edges<ET>;
+    constexpr int NE = EG::NE, PER = NE / DIM;
+    double *buf = ex[threadIdx.x >> 5][(threadIdx.x & 31) / NIP];
 #pragma unroll
-  for (int k = 0; k < NEN; k++) {
-    const int nd = a.conn[(long)k * a.E + e];
+    for (int j = 0; j < (NE + NIP - 1) / NIP; j++) {
+      const int eg = pt + j * NIP;
+      if (eg < NE) {
+        const int lo = __ldg(a.conn + (long)edge_node(EG::LO, eg) * a.E + e);
+        const int hi = __ldg(a.conn + (long)edge_node(EG::HI, eg) * a.E + e);
 #pragma unroll
-    for (int r = 0; r < DIM; r++) {
-      const double xr = a.x[r][nd];
-#pragma unroll
-      for (int c = 0; c < DIM; c++) J[r][c] = fma(pdN<ET>(pt, k, c), xr, J[r][c]);
+        for (int r = 0; r < DIM; r++) buf[eg * DIM + r] = a.x[r][hi] - a.x[r][lo];
+      }
     }
-    if (AXI) Rad = fma(pN<ET>(pt, k), a.x[0][nd], Rad);
+    __syncwarp();
+#pragma unroll
+    for (int c = 0; c < DIM; c++)
+#pragma unroll
+      for (int q = 0; q < PER; q++) {
+        const int eg = c * PER + q;
+        const double w = pdN<ET>(pt, edge_node(EG::HI, eg), c);
+#pragma unroll
+        for (int r = 0; r < DIM; r++) J[r][c] = fma(w, buf[eg * DIM + r], J[r][c]);
+      }
+    if (AXI) {
+#pragma unroll
+      for (int k = 0; k < NEN; k++) Rad = fma(pN<ET>(pt, k), a.x[0][__ldg(a.conn + (long)k * a.E + e)], Rad);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < NEN; k++) {
+      const int nd = a.conn[(long)k * a.E + e];
+#pragma unroll
+      for (int r = 0; r < DIM; r++) {
+        const double xr = a.x[r][nd];
+#pragma unroll
+        for (int c = 0; c < DIM; c++) J[r][c] = fma(pdN<ET>(pt, k, c), xr, J[r][c]);
+      }
+      if (AXI) Rad = fma(pN<ET>(pt, k), a.x[0][nd], Rad);
+    }
   }
+  if (!valid) return;
   double Ji[DIM][DIM], detJ;
   if (TWO_D) {
     detJ = J[0][0] * J[1][1] - J[0][1] * J[1][0];
