@@ -199,19 +199,27 @@ int dnl_batch_sizes(dnl_batch *b, int *elements, int *nodes);
 int dnl_batch_handle(dnl_batch *b, dnl_handle **h);
 
 /* ------------------------------------------------------------- no device allocation */
-/* Internal forces for callers that cannot allocate device memory: code running inside a CUDA
- * stream capture, or under a memory manager that owns all device memory and forbids the library
- * its own cudaMalloc.  No counterpart in the reference (its element loop runs on host objects).
+/* Internal forces for callers that cannot allocate device memory: a host application or framework
+ * whose memory manager owns every device byte and forbids libraries their own cudaMalloc, or a
+ * process whose device-memory budget is fixed before the solver starts.  No counterpart in the
+ * reference (its element loop runs on host objects).
  *
- * Same computation and side effects as dnl_internal_forces, but without a handle: the caller
- * passes every input and output in device memory, and the per-element force scratch
- * (num_elements * nen * dim doubles) is a fixed array inside the library, at most
- * DNL_STATIC_MAX_ELEMENT_DOFS doubles (8 MiB; e.g. 43,690 hex8 or 131,072 axisymmetric elements);
- * larger meshes are rejected with DNL_ERR_ARG.  Every GPU that loads the library holds that array
- * until the process exits.  The first call on a device resolves the array's address (make it
- * before any stream capture).  All calls share the array: calls whose GPU work overlaps race and
- * must be serialised by the caller.  The function synchronises `stream` to read the error word.
- * It calls no cudaMalloc, cudaFree or allocating library routine. */
+ * The computation of dnl_internal_forces, without a handle: the caller passes every input and
+ * output in device memory, and the per-element force scratch (num_elements * nen * dim doubles) is
+ * a fixed array inside the library, at most DNL_STATIC_MAX_ELEMENT_DOFS doubles (8 MiB; e.g.
+ * 43,690 hex8, 65,536 Tet4 or 131,072 axisymmetric elements); larger meshes are rejected with
+ * DNL_ERR_ARG.  Every GPU that loads the library holds that array until the process exits.  The
+ * first call on a device looks up the array's device address (once per device, under a lock); make
+ * that first call before any stream capture.  All calls share the array, which keeps the last
+ * call's contents: calls whose GPU work overlaps race and must be serialised by the caller.  The
+ * function synchronises `stream` to read the error word.  It calls no cudaMalloc, cudaFree or
+ * allocating library routine.
+ *
+ * Accepted element types: DNL_ELQUA4NAX, DNL_ELQUA4N2D, DNL_ELHEX8N3D, DNL_ELTET4N3D,
+ * DNL_ELTET10N3D (DNL_ELHEX8N3D_1PT needs nodal velocities and is rejected).
+ * On a non-zero status (e.g. DNL_ERR_NEG_DETJ with *bad_element the first failing element) the
+ * pass has still run over every element: fint and ip then hold that failed pass's values, where
+ * dnl_internal_forces leaves its fint output untouched. */
 #define DNL_STATIC_MAX_ELEMENT_DOFS (1 << 20)
 typedef struct {
   int etype, num_nodes, num_elements;
@@ -220,9 +228,16 @@ typedef struct {
   const int *node_entry; /* e*nen + k for each element touching the node, ascending e */
   const double *coords;  /* [3][N] current coordinates */
   const double *du;      /* [3][N] Current delta_disp */
-  double *ip;            /* integration-point state, updated in place: [ncomp][E*nip] with the
-                            components S, Eps, EpsPlas (symmetric: xx yy zz xy [xz yz]), p, evp,
-                            evp^n -- 15 components (axisymmetric) or 21 (hex8) */
+  double *ip;            /* integration-point state, updated in place: [ncomp][E*nip], point
+                            e*nip + q at column e*nip + q, components in this order:
+                              S[ns] | Eps[ns] | EpsPlas[ns] | p | evp | evp^n
+                            each tensor as its ns symmetric components,
+                              ns = 4 (xx yy zz xy) for DNL_ELQUA4NAX and DNL_ELQUA4N2D,
+                              ns = 6 (xx yy zz xy xz yz) for DNL_ELHEX8N3D, DNL_ELTET4N3D and
+                                   DNL_ELTET10N3D,
+                            so ncomp = 3 ns + 3 = 15 (quads) or 21 (3D); nip = 4 (quads, Tet10),
+                            8 (hex8), 1 (Tet4).  evp^n is the cached power-law term (pow(evp, n)
+                            for the material's n; evp starts at 1e-10) */
   double *fint;          /* out: N*dim, index n*dim + j */
   dnl_material mat;
 } dnl_static_args;
@@ -328,6 +343,21 @@ int dnl_range_pop(void);
 /* FP64 fused multiply-add throughput of the current device, measured by a dependent-chain kernel
  * over all SMs (TFLOP/s, 2 flops per DFMA) */
 int dnl_measure_fp64_peak(double *tflops);
+/* Limits of the three bounded loops of the step, for exercising the non-convergence statuses:
+ * Jacobi passes of the polar decomposition (0..29, default 29, Tensor2.C:1169-1258 ->
+ * DNL_ERR_JACOBI_NOCONV), Newton iterations of the radial return (0..2000, default 2000,
+ * Element.C:327-330 -> DNL_ERR_RR_NOCONV) and Pulse power iterations (1..1000, default 1000,
+ * Domain.C:936-939 -> DNL_ERR_PULSE_NOCONV).  A negative value restores the reference's default.
+ * Process-wide; the two element-pass limits are device constants of the current device.  Change
+ * them only between runs (no call of the library in flight).  No counterpart in the reference,
+ * whose limits are literals. */
+int dnl_set_iteration_caps(int rotations, int newton, int power);
+/* Self-check of the element and nodal kernels' division helpers on the current device: for each
+ * i < n, out[i] = the Newton-Raphson reciprocal 1/b[i] the kernels use, out[n + i] = their quotient
+ * a[i]/b[i] (reciprocal + one residual correction), out[2n + i] = CUDA's IEEE 1.0/b[i] and
+ * out[3n + i] = its IEEE a[i]/b[i], for comparison.  No counterpart in the reference (which
+ * divides in IEEE arithmetic). */
+int dnl_check_quotients(int n, const double *a, const double *b, double *out);
 
 /* --------------------------------------------------------------------------------- misc */
 /* select the CUDA device used by subsequent dnl_create calls of this thread */

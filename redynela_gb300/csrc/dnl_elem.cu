@@ -65,6 +65,18 @@ void set_shape_tables()
   cudaMemcpyToSymbol(c_shape, &s, sizeof s);
 }
 
+// Limits of the element pass's bounded loops: Jacobi passes of the polar decomposition (a
+// convergence check and a rotation each; Tensor2.C:1169, 29) and Newton iterations of the radial
+// return (Element.C:327-330, 2000).  The defaults are the reference's; dnl_set_iteration_caps lowers
+// them to exercise the non-convergence statuses.
+__constant__ int c_caps[2] = {kPolarMaxIt - 1, kRadialReturnMaxIt};
+
+int set_iteration_caps(int rotations, int newton)
+{
+  const int caps[2] = {rotations, newton};
+  return cudaMemcpyToSymbol(c_caps, caps, sizeof caps) == cudaSuccess ? 0 : DNL_ERR_CUDA;
+}
+
 long long &launch_counter()
 {
   static long long n = 0;
@@ -501,12 +513,12 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
       f[j][i] = s;
     }
 
-  // ---- Jacobi eigen-iteration (at most 29 rotations; Tensor2.C:1169)
+  // ---- Jacobi eigen-iteration (at most 29 rotations, c_caps[0]; Tensor2.C:1169)
   double rot[3][3] = {{1., 0., 0.}, {0., 1., 0.}, {0., 0., 1.}};
   bool conv = false;
   {
     double f00 = f[0][0], f11 = f[1][1], f22 = f[2][2], f01 = f[0][1], f02 = f[0][2], f12 = f[1][2];
-    for (int it = 1; it < kPolarMaxIt; it++) {
+    for (int it = 1; it <= c_caps[0]; it++) {
       // pivot of Tensor2.C:1173-1178: q = |C01| > |C02| ? 1 : 2, p = |C0q| > |C12| ? 0 : 1
       int k = 0;
       double fpq = f01;
@@ -688,7 +700,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
           break;
         }
         iteration++;
-        if (iteration > kRadialReturnMaxIt) {
+        if (iteration > c_caps[1]) {
           if (valid) record_error(tm, DNL_ERR_RR_NOCONV, e);
           break;
         }
@@ -737,7 +749,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
           break;
         }
         iteration++;
-        if (iteration > kRadialReturnMaxIt) {
+        if (iteration > c_caps[1]) {
           if (valid) record_error(tm, DNL_ERR_RR_NOCONV, e);
           break;
         }

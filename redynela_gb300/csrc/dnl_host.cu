@@ -322,6 +322,18 @@ __global__ void k_fp64_peak(double *out, double a, double b, int iters)
   if (s == 12345.678) out[0] = s;  // keeps the chains live
 }
 
+// self-check of the reciprocal and quotient helpers against CUDA's IEEE division
+__global__ void k_check_quotients(int n, const double *a, const double *b, double *out)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double r = nr_rcp(b[i]);
+  out[i] = r;
+  out[(long)n + i] = quot(a[i], b[i], r);
+  out[2L * n + i] = __drcp_rn(b[i]);
+  out[3L * n + i] = __ddiv_rn(a[i], b[i]);
+}
+
 // kinetic energy of the Current field (Domain::getTotalKineticEnergy), fixed-order block sums
 __global__ void k_kinetic(int N, NodeFields f, const double *mass, double *partial)
 {
@@ -727,6 +739,40 @@ int dnl_measure_fp64_peak(double *tflops)
   const double flops = 2.0 * 8.0 * iters * (double)threads * blocks;
   *tflops = flops / (ms * 1e-3) / 1e12;
   return 0;
+}
+
+int dnl_set_iteration_caps(int rotations, int newton, int power)
+{
+  if (rotations > kPolarMaxIt - 1 || newton > kRadialReturnMaxIt || power > kPulseMaxIt || power == 0)
+    return DNL_ERR_ARG;
+  const int rot = rotations < 0 ? kPolarMaxIt - 1 : rotations;
+  const int nwt = newton < 0 ? kRadialReturnMaxIt : newton;
+  if (int r = set_iteration_caps(rot, nwt)) {
+    snprintf(g_lastError, sizeof g_lastError, "cudaMemcpyToSymbol of the iteration caps failed");
+    return r;
+  }
+  pulse_cap() = power < 0 ? kPulseMaxIt : power;
+  return 0;
+}
+
+int dnl_check_quotients(int n, const double *a, const double *b, double *out)
+{
+  if (n <= 0 || !a || !b || !out) return DNL_ERR_ARG;
+  double *d;
+  CK(cudaMalloc(&d, sizeof(double) * 6 * (size_t)n));
+  int r = 0;
+  auto run = [&]() -> int {
+    CK(cudaMemcpy(d, a, sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d + n, b, sizeof(double) * n, cudaMemcpyHostToDevice));
+    k_check_quotients<<<(n + 255) / 256, 256>>>(n, d, d + n, d + 2 * (size_t)n);
+    launch_counter()++;
+    if (int c = check_launch()) return c;
+    CK(cudaMemcpy(out, d + 2 * (size_t)n, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToHost));
+    return 0;
+  };
+  r = run();
+  cudaFree(d);
+  return r;
 }
 
 int dnl_range_push(const char *name)

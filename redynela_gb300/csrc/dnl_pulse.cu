@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(256) k_pulse_gather(PulseArgs a, int EN)
   }
 }
 
-__global__ void k_pulse_check(DevTime *tm)
+__global__ void k_pulse_check(DevTime *tm, int maxIt)
 {
   if (tm->done | tm->status | tm->pulseDone) return;
   const double fmax = __longlong_as_double((long long)tm->pulseMaxBits);
@@ -446,7 +446,7 @@ __global__ void k_pulse_check(DevTime *tm)
   if (convergence < kPulseConvergence) tm->pulseDone = 1;
   tm->fmax0 = fmax;
   tm->pulseScale = fmax;
-  if (tm->pulseIter > kPulseMaxIt) {
+  if (tm->pulseIter > maxIt) {
     tm->status = DNL_ERR_PULSE_NOCONV;
     tm->badElem = -1;
     return;
@@ -456,6 +456,14 @@ __global__ void k_pulse_check(DevTime *tm)
     tm->status = DNL_ERR_PULSE_NOCONV;
     tm->badElem = -1;
   }
+}
+
+// Limit of the power iteration (Domain.C:936-939, 1000 iterations); dnl_set_iteration_caps lowers
+// it to exercise the non-convergence status.
+int &pulse_cap()
+{
+  static int cap = kPulseMaxIt;
+  return cap;
 }
 
 __global__ void k_pulse_begin(DevTime *tm)
@@ -516,7 +524,7 @@ int launch_pulse(dnl_handle *h, cudaStream_t s)
   prof_end(h, DNL_PROF_PULSE, s);
   launch_counter() += 2;
   const int batch = 4;
-  for (int round = 0; round < (kPulseMaxIt + batch) / batch + 1; round++) {
+  for (int round = 0; round < (pulse_cap() + batch) / batch + 1; round++) {
     for (int b = 0; b < batch; b++) {
       prof_begin(h, s);
       DNL_BY_ETYPE(h->etype, (k_pulse_kx<ET><<<gridIP, 128, 0, s>>>(a)));
@@ -525,7 +533,7 @@ int launch_pulse(dnl_handle *h, cudaStream_t s)
       } else {
         k_pulse_gather<3><<<gridN, 256, 0, s>>>(a, h->E * h->nen);
       }
-      k_pulse_check<<<1, 1, 0, s>>>(h->tm);
+      k_pulse_check<<<1, 1, 0, s>>>(h->tm, pulse_cap());
       prof_end(h, DNL_PROF_PULSE, s);
       launch_counter() += 3;
     }

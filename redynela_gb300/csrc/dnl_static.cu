@@ -1,25 +1,28 @@
 // dnl_internal_forces_static: the internal-force pass for callers that cannot allocate device
 // memory.
 //
-// Who needs it: code that runs where cudaMalloc is off limits -- inside a CUDA stream capture
-// (allocation is not a capturable operation), under an external memory manager that owns every
-// device byte (a host application or framework pool that hands out buffers but forbids the
-// library from taking its own), or in a process whose device-memory budget is fixed before the
-// solver starts.  Such a caller owns and passes every input and output buffer; the only other
+// Who needs it: a host application or framework whose memory manager owns every device byte and
+// hands out buffers from its own pool, forbidding libraries their own cudaMalloc (a solver embedded
+// in such a framework, or a process whose device-memory budget is fixed before the solver starts
+// and must not grow).  Such a caller owns and passes every input and output buffer; the only other
 // device memory this entry point uses is the fixed array below, which is part of the library image.
 //
 // Scratch: the per-element force vectors that the element pass writes and the node-centric
 // assembly reads (E * nen * dim doubles) live in g_static_fe, a file-scope device array of
 // DNL_STATIC_MAX_ELEMENT_DOFS doubles (8 MiB).  Every GPU that loads the library holds this array
-// until the process exits.  The first call on a device looks up the array's device address with
-// cudaGetSymbolAddress while that device is current and caches it; make that first call before
-// any stream capture.  All calls share the array and it keeps the last call's contents; the error
-// word is reset at the start of each call.  Calls whose GPU work overlaps (two streams, or two
-// host threads) race on the array and must be serialised by the caller.
+// until the process exits.  Host code cannot use the array's name as a device address (on the host
+// it names a host-side stand-in), so the first call on a device looks up the array's device address
+// with cudaGetSymbolAddress while that device is current, checks the result and caches it, once per
+// device under a lock; that first call should come before any stream capture.  All calls share the
+// array and it keeps the last call's contents: every entry is written before it is read, and the
+// error word, which must start clear, is reset at the start of each call.  Calls whose GPU work
+// overlaps (two streams, or two host threads) race on the array and on the error word and must be
+// serialised by the caller.
 //
 // No cudaMalloc, cudaFree or allocating library routine is called on this path.
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "dnl_common.cuh"
 
@@ -33,16 +36,24 @@ struct StaticPtrs {
   dnl::DevTime *tm;
   bool ready;
 };
-StaticPtrs g_ptrs[64];
+constexpr int kMaxDevices = 64;
+StaticPtrs g_ptrs[kMaxDevices];
+std::mutex g_ptrs_lock;
 
+// the device addresses of the two arrays on the current device, looked up once per device
 int static_setup(StaticPtrs **out)
 {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DNL_ERR_CUDA;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return DNL_ERR_CUDA;
+  std::lock_guard<std::mutex> guard(g_ptrs_lock);
   StaticPtrs &p = g_ptrs[dev];
   if (!p.ready) {
-    if (cudaGetSymbolAddress((void **)&p.fe, g_static_fe) != cudaSuccess) return DNL_ERR_CUDA;
-    if (cudaGetSymbolAddress((void **)&p.tm, g_static_tm) != cudaSuccess) return DNL_ERR_CUDA;
+    double *fe = nullptr;
+    dnl::DevTime *tm = nullptr;
+    if (cudaGetSymbolAddress((void **)&fe, g_static_fe) != cudaSuccess) return DNL_ERR_CUDA;
+    if (cudaGetSymbolAddress((void **)&tm, g_static_tm) != cudaSuccess) return DNL_ERR_CUDA;
+    p.fe = fe;
+    p.tm = tm;
     p.ready = true;
   }
   *out = &p;
@@ -67,8 +78,10 @@ extern "C" int dnl_internal_forces_static(const dnl_static_args *a, void *stream
   if (int r = static_setup(&sp)) return r;
   cudaStream_t s = (cudaStream_t)stream;
 
-  // the error word starts at zero on every call; the array itself needs no clearing (fully written)
+  // the error word starts clear on every call (status 0, element -1); the force array needs no
+  // clearing (the element pass writes every entry the assembly reads)
   if (cudaMemsetAsync(sp->tm, 0, sizeof(DevTime), s) != cudaSuccess) return DNL_ERR_CUDA;
+  if (cudaMemsetAsync(&sp->tm->badElem, 0xff, sizeof(int), s) != cudaSuccess) return DNL_ERR_CUDA;
 
   const Material m = make_material(a->mat, nen);
 

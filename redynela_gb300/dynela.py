@@ -119,6 +119,8 @@ def lib():
         L.dnl_timer_mark.argtypes = [H, C.c_int]
         L.dnl_timer_elapsed.argtypes = [H, C.c_int, C.c_int, _dp]
         L.dnl_measure_fp64_peak.argtypes = [_dp]
+        L.dnl_check_quotients.argtypes = [C.c_int, _dp, _dp, _dp]
+        L.dnl_set_iteration_caps.argtypes = [C.c_int, C.c_int, C.c_int]
         L.dnl_set_device.argtypes = [C.c_int]
         L.dnl_host_alloc.argtypes = [C.c_ulonglong, C.POINTER(C.c_void_p)]
         L.dnl_host_free.argtypes = [C.c_void_p]
@@ -172,6 +174,28 @@ def range_push(name: str) -> None:
 
 def range_pop() -> None:
     lib().dnl_range_pop()
+
+
+def set_iteration_caps(rotations: int = -1, newton: int = -1, power: int = -1) -> None:
+    """dnl_set_iteration_caps: limits of the Jacobi passes, the radial return's Newton iterations
+    and the Pulse power iteration (-1: the reference's 29, 2000, 1000)."""
+    rc = lib().dnl_set_iteration_caps(int(rotations), int(newton), int(power))
+    if rc != DNL_OK:
+        raise DnlError(rc, lib().dnl_error_string(rc).decode())
+
+
+def check_quotients(a: np.ndarray, b: np.ndarray) -> Dict[str, np.ndarray]:
+    """dnl_check_quotients: the kernels' Newton-Raphson reciprocal and quotient of a / b next to
+    CUDA's IEEE 1 / b and a / b, computed on the current device."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    n = a.size
+    out = np.zeros(4 * n)
+    rc = lib().dnl_check_quotients(n, _ptr(a), _ptr(b), _ptr(out))
+    if rc != DNL_OK:
+        raise DnlError(rc, lib().dnl_error_string(rc).decode())
+    o = out.reshape(4, n)
+    return {"rcp": o[0], "quot": o[1], "ieee_rcp": o[2], "ieee_quot": o[3]}
 
 
 def fp64_peak_tflops() -> float:

@@ -27,6 +27,11 @@ reference's own output on a seeded synthetic model:
 * ``steps_tet4_pulse.npz`` the same bar with the Pulse time step, first 20 steps
 * ``steps_tet10.npz``   the ElTet10n3D bar, lumped mass and its first 2 steps (the reference's run
                         of this element ends in a singular Jacobian a few steps later)
+* ``steps_speed.npz``   a coarse tensile bar of ElHex8n3D (necking_bar(4, 12): one end clamped by
+                        BoundaryRestrain 1 1 1, the other pulled by BoundarySpeed 0 0 1 m/s), Pulse
+                        time step, lumped mass and its first 30 steps
+* ``run_speed.npz``     the same bar pulled at 5 m/s to 2 ms: final coordinates, velocities, plastic
+                        strain
 
     python tests/golden/make_golden.py
 """
@@ -125,6 +130,19 @@ def tets():
          final_coords=r["final_coords"])
 
 
+def speed():
+    """The imposed-velocity (BoundarySpeed) fixtures only: python tests/golden/make_golden.py speed"""
+    m = meshes.necking_bar(4, 12)
+    r = dnl_io.run_reference("steps", m, 30)
+    save("steps_speed.npz", mass=r["mass"], dt0=r["dt0"], dt=r["dt"], time=r["time"],
+         kinetic=r["kinetic"], fint=np.stack([r[f"fint_{k:06d}"] for k in range(30)]),
+         final_coords=r["final_coords"], final_v=r["final_v"], final_S=r["final_S"])
+    m = meshes.necking_bar(4, 12, speed=5.0, tend=2e-3)
+    r = dnl_io.run_reference("run", m)
+    save("run_speed.npz", increments=r["increments"], time=r["time"],
+         final_coords=r["final_coords"], final_v=r["final_v"], final_evp=r["final_evp"])
+
+
 def main():
     if not dnl_io.reference_available():
         sys.exit("compiled reference missing: run `make -C oracle ref`")
@@ -139,6 +157,9 @@ def main():
         return
     if sys.argv[1:] == ["tets"]:
         tets()
+        return
+    if sys.argv[1:] == ["speed"]:
+        speed()
         return
     t = dnl_io.reference_tables()
     save("tables.npz", **t)
@@ -176,6 +197,7 @@ def main():
     laws()
     plane()
     tets()
+    speed()
 
 
 if __name__ == "__main__":

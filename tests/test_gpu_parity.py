@@ -193,6 +193,40 @@ def test_full_run_hex_final_positions(gpu_lib):
     assert err <= POS_TOL, err
 
 
+def test_imposed_speed_bar_vs_reference(gpu_lib):
+    """The tensile bar pulled by BoundarySpeed (Boundary.C:478-525) on one end and clamped by
+    BoundaryRestrain 1 1 1 on the other, Pulse time step, against the reference's own outputs:
+    lumped mass bitwise, 30 steps (the first 3 at 1e-12, then the 3D trajectory tolerance of
+    test_steps_hex_pulse), the imposed velocity exact on the pulled nodes; then the bar pulled at
+    5 m/s to 2 ms (373 increments, plastic): final positions <= 1e-6."""
+    g = golden("steps_speed.npz")
+    m = meshes.necking_bar(4, 12)
+    d = gpu_lib.GpuDomain(m)
+    d.prologue()
+    assert rel(d.get_state("mass")["mass"], g["mass"][::3]) == 0.0
+    assert abs(d.time_step() - g["dt0"][0]) <= 1e-10 * g["dt0"][0]
+    for k in range(30):
+        assert d.step(1) == 1
+        r = g["fint"][k]
+        if np.linalg.norm(r) > 0:
+            assert rel(d.fint(), r) <= (FORCE_TOL if k < 3 else 1e-7), k
+        info = d.time_info()
+        assert abs(info["time"] - g["time"][k]) <= 1e-10 * g["time"][k]
+    st = d.get_state("coords", "v")
+    x = st["coords"].ravel()
+    assert np.max(np.abs(x - g["final_coords"])) <= 1e-9 * np.max(np.abs(g["final_coords"]))
+    top = m.bcs[1].nodes
+    assert np.array_equal(st["v"][top, 2], np.full(top.size, 1.0))
+    r = golden("run_speed.npz")
+    d = gpu_lib.GpuDomain(meshes.necking_bar(4, 12, speed=5.0, tend=2e-3))
+    n = d.run()
+    assert d.time_info()["done"] == 1
+    assert abs(n - int(r["increments"][0])) <= 2
+    x = d.get_state("coords")["coords"].ravel()
+    err = np.max(np.abs(x - r["final_coords"])) / np.max(np.abs(r["final_coords"]))
+    assert err <= POS_TOL, err
+
+
 def test_pulse_time_step_vs_oracle_medium(gpu_lib):
     """A 16x16x40 hex bar: the Pulse step after the prologue and after 25 steps vs the oracle."""
     m = meshes.taylor_hex(16, 40)

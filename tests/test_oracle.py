@@ -185,6 +185,43 @@ def test_steps_hex_pulse():
     assert np.max(np.abs(x - g["final_coords"])) <= 1e-12 * np.max(np.abs(g["final_coords"]))
 
 
+def test_imposed_speed_steps_and_run_vs_reference():
+    """The tensile bar with BoundarySpeed::applyConstant on its pulled end (Boundary.C:478-525:
+    a = 0, v = the imposed speed and delta_disp = v dt on both nodal fields) and BoundaryRestrain
+    1 1 1 on the other: lumped mass bitwise, 30 Pulse steps (K x summed in element order, so to
+    rounding), then a full run pulled at 5 m/s to 2 ms (373 increments, plastic) vs the reference."""
+    g = golden("steps_speed.npz")
+    m = meshes.necking_bar(4, 12)
+    o = Oracle(m)
+    o.prologue()
+    assert np.array_equal(o.array("Mass"), g["mass"])
+    assert abs(o.get("dt") - g["dt0"][0]) <= 1e-14 * g["dt0"][0]
+    for k in range(30):
+        o.steps(1)
+        f, r = o.array("fint"), g["fint"][k]
+        if np.linalg.norm(r) > 0:
+            assert np.linalg.norm(f - r) <= 1e-11 * np.linalg.norm(r), k
+    x = o.array("coords")
+    assert np.max(np.abs(x - g["final_coords"])) <= 1e-12 * np.max(np.abs(g["final_coords"]))
+    top = m.bcs[1].nodes
+    assert np.array_equal(o.array("v").reshape(-1, 3)[top, 2], np.full(top.size, 1.0))
+    assert np.array_equal(g["final_v"].reshape(-1, 3)[top, 2], np.full(top.size, 1.0))
+    r = golden("run_speed.npz")
+    o = Oracle(meshes.necking_bar(4, 12, speed=5.0, tend=2e-3))
+    o.prologue()
+    total = 0
+    while True:
+        k = o.steps(100)
+        total += k
+        if k < 100:
+            break
+    assert total == int(r["increments"][0])
+    x = o.array("coords")
+    assert np.max(np.abs(x - r["final_coords"])) <= 1e-12 * np.max(np.abs(r["final_coords"]))
+    assert np.max(np.abs(o.array("evp") - r["final_evp"])) <= 1e-12 * np.max(r["final_evp"])
+    assert r["final_evp"].max() > 0.1  # the run is plastic
+
+
 # ---------------------------------------------------------------------- known answers
 def test_chung_hulbert_parameters():
     o = Oracle(meshes.taylor_axi(2, 2))
