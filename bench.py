@@ -37,15 +37,30 @@ sys.path.insert(0, ROOT)
 
 from redynela_gb300 import meshes  # noqa: E402
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_elem launch per element, from the ncu capture
-# summarised in profiles/k_elem_hex_40x40x100_window.md (308.85 MB on the 126,400-element bar's
-# mid-run window); bench.py scales it by the elements of the workload
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_elem<ElHex8n3D> launch per element,
+# measured by ncu on the 126,400-element bar's mid-run window (308.85 MB); scaled by the elements
+# of the workload
 ELEM_TRAFFIC_BYTES_PER_ELEMENT = 308.85e6 / 126400
 
-# FP64 thread-instructions of one k_elem<ElHex8n3D> launch per Gauss point, from the
-# sm__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum counters of the same mid-run window
-# (571,665,728 / 140,096,488 / 256,965,144 over 1,011,200 points); a DFMA is two flops
-HEX_FP64_FLOPS_PER_POINT = (2 * 571665728 + 140096488 + 256965144) / 1011200
+# FP64 thread-instructions of one k_elem<ElHex8n3D> launch per Gauss point in the timed window of
+# the 505,600-element bar (t = 10 us, increment 1,550), from ncu's
+# sm__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum counters of that launch
+# (2,242,452,912 / 544,438,768 / 997,932,972 over the launch's 4,044,800 points, one counter per
+# capture, each a one-pass capture)
+HEX_FP64_INSTR_PER_POINT = {"dfma": 2242452912 / 4044800, "dadd": 544438768 / 4044800,
+                            "dmul": 997932972 / 4044800}
+HEX_FP64_SOURCE = "the 505,600-element bar's timed window (t = 10 us, increment 1,550)"
+
+
+def hex_fp64_flops_per_point() -> float:
+    """FP64 flops per Gauss point (a DFMA counted as two)."""
+    c = HEX_FP64_INSTR_PER_POINT
+    return 2 * c["dfma"] + c["dadd"] + c["dmul"]
+
+
+def hex_fp64_instr_per_point() -> float:
+    c = HEX_FP64_INSTR_PER_POINT
+    return c["dfma"] + c["dadd"] + c["dmul"]
 
 
 def workload(name: str, layers: int = 400):
@@ -152,10 +167,87 @@ def barrier_and_max(value: float, world: int) -> float:
     return float(t.item())
 
 
+def aggregate_rate(units: float, seconds: float, world: int) -> float:
+    """Whole-job rate of independent replicas: the units every rank processed, summed, over the
+    slowest rank's time."""
+    if world == 1:
+        return units / seconds
+    import torch
+    import torch.distributed as dist
+    u = torch.tensor([units], dtype=torch.float64)
+    t = torch.tensor([seconds], dtype=torch.float64)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(u.item()) / float(t.item())
+
+
 def barrier(world: int):
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
+
+
+def hex_config(model, name: str, args, world: int) -> dict:
+    """The `config` of the element-update line, identical for both arms (it names the workload)."""
+    ns = 4 if model.dim == 2 else 6
+    return {"workload": name, "elements": model.E, "nodes": model.N,
+            "time_step": ("Pulse" if model.method == meshes.PULSE else "Courant")
+                         + f" every {model.freq} increments",
+            "formulation": ("one Gauss point + viscous hourglass control (not the reference's "
+                            "2x2x2-point ElHex8n3D)" if model.etype == meshes.ELHEX8N3D_1PT
+                            else "the reference's"),
+            "window": f"{args.steps} steps from t = {args.start_us:g} us of the impact, reached "
+                      "untimed",
+            "l2": "inputs larger than L2 (integration-point state "
+                  f"{model.E * model.nip * (3 * ns + 3) * 8 / 1e6:.0f} MB)",
+            "parallelism": f"replicas x{world}"}
+
+
+def sm_count(device: int = 0) -> int:
+    import torch
+    return int(torch.cuda.get_device_properties(device).multi_processor_count)
+
+
+def fp64_roofline(model, launch_s, clocks, device: int = 0):
+    """Roofline of one k_elem launch of `model` taking `launch_s` seconds (CUDA events).
+
+    Bound: the FP64 pipe.  achieved = FP64 flops per launch (the counted mix per Gauss point, a
+    DFMA as two) / launch time, against the DFMA peak measured at the start of this run on this
+    GPU (`dnl_measure_fp64_peak`: independent DFMA chains on every SM); the same launch as FP64
+    instructions issued per second against the pipe's issue ceiling (2 FP64 thread-instructions per
+    SM per cycle at the sampled SM clock).  HBM: the algorithmic bytes per launch over the launch
+    time against the measured copy bandwidth, and the DRAM traffic ncu counted."""
+    from redynela_gb300 import dynela
+    hbm_peak, peak_src = peak_hbm()
+    bytes_per_launch = elem_bytes(model)
+    traffic = (ELEM_TRAFFIC_BYTES_PER_ELEMENT * model.E) if model.etype == meshes.ELHEX8N3D else None
+    hbm = {"achieved": bytes_per_launch / launch_s / 1e9 if launch_s else None, "peak": hbm_peak,
+           "unit": "GB/s", "peak_source": peak_src, "algorithmic_bytes_per_launch": bytes_per_launch,
+           "traffic": traffic}
+    hbm["frac"] = hbm["achieved"] / hbm_peak if hbm["achieved"] else None
+    kernel = {meshes.ELHEX8N3D: "k_elem<ElHex8n3D>", meshes.ELQUA4NAX: "k_elem<ElQua4nAx>",
+              meshes.ELHEX8N3D_1PT: "k_elem<ElHex8n3D at one point + hourglass>"}.get(model.etype, "k_elem")
+    if model.etype != meshes.ELHEX8N3D or not launch_s:
+        return dict(hbm, bound="hbm", kernel=kernel, avg_launch_ms=launch_s * 1e3 if launch_s else None)
+    points = model.E * model.nip
+    dfma_peak = dynela.fp64_peak_tflops()
+    achieved = hex_fp64_flops_per_point() * points / launch_s / 1e12
+    sms = sm_count(device)
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 0.0
+    ceiling = sms * 2.0 * mhz * 1e6  # FP64 thread-instructions per second
+    issued = hex_fp64_instr_per_point() * points / launch_s
+    return {"bound": "fp64", "achieved": achieved, "peak": dfma_peak, "unit": "TFLOP/s",
+            "frac": achieved / dfma_peak if dfma_peak else None, "traffic": traffic,
+            "kernel": kernel, "avg_launch_ms": launch_s * 1e3,
+            "peak_source": "measured on this GPU at the start of the run (DFMA loop); "
+                           "MEASURED_PEAKS.json has no FP64 figure",
+            "flops_per_gauss_point": hex_fp64_flops_per_point(),
+            "fp64_instructions_per_gauss_point": dict(HEX_FP64_INSTR_PER_POINT),
+            "counted_on": HEX_FP64_SOURCE,
+            "issue": {"achieved_instr_per_s": issued, "ceiling_instr_per_s": ceiling,
+                      "frac": issued / ceiling if ceiling else None, "sms": sms,
+                      "sm_mhz": mhz, "per_sm_per_cycle": 2},
+            "hbm": hbm}
 
 
 def run_cpu_baseline(model, sample_desc, min_seconds=10.0, max_steps=400, threads=None,
@@ -210,6 +302,7 @@ def main_reference(args):
     while o.get("time") < args.start_us * 1e-6:  # untimed, to the window start
         if o.steps(50) == 0:
             break
+    t_start, inc_start = o.get("time"), int(o.get("increment"))
     if args.warmup:
         o.steps(args.warmup)
     t0 = time.perf_counter()
@@ -222,7 +315,8 @@ def main_reference(args):
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(done, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": name, "sample": sample, "window_start_us": args.start_us},
+            "config": hex_config(model, name, args, args.gpus),
+            "window_start": {"time_us": t_start * 1e6, "increment": inc_start},
             "cpu_baseline": {"value": rate, "unit": "element-updates/s", "cores": threads,
                              "kind": "port",
                              "sample": f"{sample}; the oracle's C restatement of the reference "
@@ -275,35 +369,12 @@ def main_ours(args):
     clocks = clk.summary()
     barrier(world)
     ms_max = barrier_and_max(ms, world)
-    value = world * model.E * done / (ms_max * 1e-3)
+    value = aggregate_rate(model.E * done, ms * 1e-3, world)
 
-    # ---- roofline of the dominant kernel (k_elem)
+    # ---- roofline of the dominant kernel (k_elem): the FP64 pipe binds it, HBM is reported beside
     elem_ms, elem_n = prof["elem"]
-    hbm_peak, peak_src = peak_hbm()
-    bytes_per_launch = elem_bytes(model)
-    achieved = bytes_per_launch / (elem_ms / elem_n * 1e-3) / 1e9 if elem_n else None
-    # the measured per-element DRAM traffic is that of the 2x2x2-point hexahedron
-    traffic = (ELEM_TRAFFIC_BYTES_PER_ELEMENT * model.E) if model.etype == meshes.ELHEX8N3D else None
-    fp64_peak = dynela.fp64_peak_tflops()
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak if achieved else None, "traffic": traffic,
-                "kernel": {meshes.ELHEX8N3D: "k_elem<ElHex8n3D>", meshes.ELQUA4NAX: "k_elem<ElQua4nAx>",
-                           meshes.ELHEX8N3D_1PT: "k_elem<ElHex8n3D at one point + hourglass>"}
-                          .get(model.etype, "k_elem"),
-                "peak_source": peak_src,
-                "algorithmic_bytes_per_launch": bytes_per_launch,
-                "avg_launch_ms": elem_ms / elem_n if elem_n else None,
-                "fp64_dfma_peak_tflops_measured": fp64_peak,
-                "note": "the element pass is FP64-pipe bound on GB300; see profiles/"}
-    if model.etype == meshes.ELHEX8N3D and elem_n and fp64_peak:
-        # the bound that applies: FP64 flops per launch (the counted mix per Gauss point) over the
-        # live launch time, against the DFMA peak measured on this GPU
-        fl = HEX_FP64_FLOPS_PER_POINT * model.E * 8 / (elem_ms / elem_n * 1e-3) / 1e12
-        roofline["fp64"] = {"achieved_tflops": fl, "peak_tflops": fp64_peak, "frac": fl / fp64_peak,
-                            "flops_per_gauss_point": HEX_FP64_FLOPS_PER_POINT,
-                            "source": "ncu FP64 instruction counts of the 40x40x100 bar's mid-run "
-                                      "window (profiles/k_elem_hex_40x40x100_window.md); peak: "
-                                      "a DFMA loop timed at the start of this run"}
+    launch_s = elem_ms / elem_n * 1e-3 if elem_n else None
+    roofline = fp64_roofline(model, launch_s, clocks, local)
     kernel_share = {k: round(v[0] / ms, 4) for k, v in prof.items() if v[1]}
 
     # ---- end to end through the C ABI with page-locked host buffers, over the same increments as
@@ -330,9 +401,10 @@ def main_ours(args):
         d._check(d.L.dnl_get_state(d.h, dynela.C.byref(sv)))
     d.timer_mark(3)
     e2e_ms = d.timer_elapsed_ms(2, 3)
+    e2e_rate = aggregate_rate(model.E * e2e_done, e2e_ms * 1e-3, world)
     e2e_ms = barrier_and_max(e2e_ms, world)
     nodal_bytes = 5 * N * 3 * 8
-    e2e = {"value": world * model.E * e2e_done / (e2e_ms * 1e-3), "unit": "element-updates/s",
+    e2e = {"value": e2e_rate, "unit": "element-updates/s",
            "h2d_bytes_per_step": nodal_bytes, "d2h_bytes_per_step": nodal_bytes,
            "steps": e2e_done, "path": "dnl_set_state + dnl_step(1) + dnl_get_state per step"}
 
@@ -348,27 +420,25 @@ def main_ours(args):
                 "ms_per_step": ms_max / max(done, 1), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded generator of the reference Taylor deck's geometry)",
-                "config": {"workload": name, "elements": model.E, "nodes": model.N,
-                           "time_step": ("Pulse" if model.method == meshes.PULSE else "Courant")
-                                        + f" every {model.freq} increments",
-                           "formulation": ("one Gauss point + viscous hourglass control (not the "
-                                           "reference's 2x2x2-point ElHex8n3D)"
-                                           if model.etype == meshes.ELHEX8N3D_1PT else "the reference's"),
-                           "window": f"{args.steps} steps from t = {window['time'] * 1e6:.2f} us "
-                                     f"(increment {window['increment']}), reached untimed",
-                           "l2": "inputs larger than L2 (integration-point state "
-                                 f"{model.E * model.nip * (3 * (4 if model.dim == 2 else 6) + 3) * 8 / 1e6:.0f} MB)",
-                           "parallelism": f"replicas x{world}"},
+                "config": hex_config(model, name, args, world),
+                "window_start": {"time_us": window["time"] * 1e6, "increment": window["increment"]},
                 "gpu_launches": launches, "kernel_time_share": kernel_share,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
-        print(json.dumps(line), flush=True)
     d.close()
+    if rank == 0 and world == 1 and not args.no_extras and args.config == "hex":
+        # the batched and the gradient workloads, timed in the same run: their own lines, kept
+        # under two keys of this one
+        line["batched"] = batch_line(argparse.Namespace(**dict(vars(args), steps=20, warmup=3)))
+        line["gradients"] = sens_line(argparse.Namespace(**dict(vars(args), steps=3, warmup=3,
+                                                                no_cpu=True)), fd_steps=(1e-5,))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
 
 
-def main_batch(args):
+def batch_line(args) -> dict:
     """Batched mode: 256 seeded axisymmetric Taylor bars (radial x axial divisions 4-40 x 40-400,
     v 150-300 m/s, A 60-150 MPa, B 200-400 MPa, n 0.2-0.5), every instance advancing K steps with
     its own time step in one graph-captured launch sequence per step, against the same bars run
@@ -428,10 +498,14 @@ def main_batch(args):
                                                             "ms_per_step": plain_graph_ms / args.steps}},
             "batched_over_plain": value / max(plain, plain_graph), "gpu_launches": launches,
             "clocks": clocks}
-    print(json.dumps(line), flush=True)
+    return line
 
 
-def main_sens(args):
+def main_batch(args):
+    print(json.dumps(batch_line(args)), flush=True)
+
+
+def sens_line(args, fd_steps=(1e-5, 1e-6, 1e-7)) -> dict:
     """Gradient workload: the 20x200 axisymmetric Taylor bar (4,000 ElQua4nAx elements) advanced
     with a fixed step-size schedule -- the nominal run's own Courant steps, at most 4,000 -- and
     L = |x_final(p) - x_target|^2 with x_target the final shape for (A, B, n) = (110 MPa, 310 MPa,
@@ -514,13 +588,43 @@ def main_sens(args):
         return float(np.mean(np.sum((x[surf] - xt[surf]) ** 2, axis=1)))
 
     fd_rel = {}
-    for hrel in (1e-5, 1e-6, 1e-7):
+    for hrel in fd_steps:
         errs = []
         for p in range(4):
             h = hrel * pv[p]
             lp, lm = (loss_at(pv + s * h * np.eye(4)[p]) for s in (1.0, -1.0))
             errs.append(float(abs((lp - lm) / (2 * h) - g[p]) / abs(g[p])))
         fd_rel[f"{hrel:.0e}"] = errs
+    # reverse mode: the same gradient by dnl_adjoint_forward (the run with a checkpoint every
+    # ceil(sqrt(steps)) steps, the final shape), the loss's dL/dx on the host, then
+    # dnl_adjoint_backward (the reverse sweep); CUDA events around the whole sequence
+    def gradient_reverse():
+        d.reset(m)
+        x = d.adjoint_forward(dts, 0)
+        w[:] = 0.
+        w[surf] = 2.0 * (x[surf] - xt[surf]) / len(surf)
+        return d.adjoint_backward(w)
+
+    gradient_reverse()
+    rev_ms = 0.0
+    for _ in range(args.steps):
+        d.timer_mark(0)
+        g_rev = gradient_reverse()
+        d.timer_mark(1)
+        rev_ms += d.timer_elapsed_ms(0, 1)
+    rev_ms /= args.steps
+    ast = d.adjoint_stats()
+    # the device memory a stored trajectory would take: every step's state record
+    per_record = ast["record_bytes"] / max(ast["stride"], 1)
+    reverse = {"value": 1e3 / rev_ms, "unit": "gradients/s", "gradient_ms": rev_ms,
+               "gradient_cost_vs_forward": rev_ms / fwd_ms,
+               "agreement_vs_forward_mode": float(np.max(np.abs(g_rev - g) / np.abs(g))),
+               "gradient": [float(v) for v in g_rev],
+               "checkpoints": ast["checkpoints"], "steps_per_checkpoint": ast["stride"],
+               "recomputed_steps": ast["recomputed_steps"], "device_bytes": ast["bytes"],
+               "checkpoint_bytes": ast["checkpoint_bytes"], "segment_record_bytes": ast["record_bytes"],
+               "stored_trajectory_bytes": int(per_record * nst),
+               "path": "dnl_adjoint_forward + dL/dx on the host + dnl_adjoint_backward"}
     tan_ms, tan_n = prof["tangent"]
     elem_ms, elem_n = prof["elem"]
     total_ms = sum(v[0] for v in prof.values())
@@ -571,6 +675,7 @@ def main_sens(args):
             "gradient_cost_vs_forward": grad_ms / fwd_ms,
             "agreement_vs_dual_oracle": agree,
             "agreement_vs_central_differences": {"relative_error_by_relative_h": fd_rel},
+            "reverse_mode": reverse,
             "gpu_launches": launches,
             "kernel_time_share": {k: round(v[0] / total_ms, 4) for k, v in prof.items()} if total_ms else None,
             "roofline": {"bound": "hbm", "achieved": tan_bytes / (tan_ms / max(tan_n, 1) * 1e-3) / 1e9,
@@ -584,32 +689,49 @@ def main_sens(args):
             "e2e": {"value": e2e, "unit": "gradients/s", "h2d_bytes_per_step": 8 * (nst + 9),
                     "d2h_bytes_per_step": 8 * 3 * m.N * 5},
             "clocks": clocks}
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def main_sens(args):
+    print(json.dumps(sens_line(args)), flush=True)
 
 
 def main_necking(args):
     """Batched sensitivities: 32 parameter sets (A, B, n drawn as for the batched Taylor bars) of
     the tensile necking bar (ElHex8n3D, gauge radius 6.4 mm, length 53.3 mm, 209,824 elements each,
     6.7 M in the batch; clamped end, the other pulled at 1 m/s, mass scaling x100) run as one batch
-    with their forward-mode derivatives, over a 30,000-step schedule of 3.55e-7 s.  The timed
-    region is K steps of that schedule (the full run is ~6 h of GPU time); `value` extrapolates
-    to gradients of the whole schedule: instances / (time per step x 30,000).  Loss: the
-    mid-length cross-section, mean over its nodes of x^2 + y^2 (the necking measure)."""
+    with their forward-mode derivatives, over a 30,000-step schedule of 3.55e-7 s.  The timed window
+    is K steps of that schedule from its middle, where the bar is plastic: one bar is run to step
+    15,000 (the plain scheduled run, untimed), its state is copied into every instance
+    (dnl_batch_broadcast_state) and the batched tangent run is timed from there.  `value` = instances
+    / (time per step of the window x 30,000).  Loss: the mid-length cross-section, mean over its
+    nodes of x^2 + y^2 (the necking measure)."""
     from redynela_gb300 import build, dynela
     build.build()
     nz = 166
     models = meshes.necking_batch(args.necking_instances, seed=0, nz=nz)
     total_steps = 30000
+    start_step = args.necking_start
     dt = models[0].tend / total_steps
     probe = dynela.GpuDomain(models[0])
     probe.prologue()
     dt_stable = probe.time_step()
     probe.close()
+    # the window's starting state: one bar run plainly to mid-schedule
+    src = dynela.GpuDomain(models[0])
+    t0 = time.perf_counter()
+    src.run_schedule(np.full(start_step, dt))
+    advance_s = time.perf_counter() - t0
+    evp_mid = src.get_state("evp")["evp"]
+    plastic_frac = float(np.mean(evp_mid > 1e-9))
     E = sum(m.E for m in models)
     b = dynela.BatchDomain(models)
     dts = np.full(max(args.warmup, args.steps), dt)
+    b.broadcast_state(src)
     b.sensitivities(dts[:args.warmup], outputs=False)  # allocations, first launches
     b.reset()
+    b.broadcast_state(src)
+    src.close()
     hv = b.handle_view()
     launches0 = dynela.kernel_launches()
     hv.profile_begin()
@@ -654,7 +776,7 @@ def main_necking(args):
         cpu = {"value": 1.0 / (tc * total_steps), "unit": "gradients/s", "cores": threads,
                "kind": "port",
                "sample": f"the sensitivity oracle (FP64 dual numbers, OpenMP) on one bar "
-                         f"({m0.E:,} elements), {k} steps, {tc:.2f} s per step, scaled to one "
+                         f"({m0.E:,} elements), its first {k} steps, {tc:.2f} s per step, scaled to one "
                          f"gradient of the 30,000-step schedule"}
     line = {"metric": "gradients/s (batched, 3D)", "value": value, "unit": "gradients/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -665,8 +787,10 @@ def main_necking(args):
                        "instances": len(models), "elements_per_instance": models[0].E,
                        "schedule": f"{total_steps} steps of {dt:.4g} s (stable step at t=0: "
                                    f"{dt_stable:.4g} s)",
-                       "timed": f"{args.steps} steps of the schedule, extrapolated to "
-                                f"{total_steps}",
+                       "timed": f"{args.steps} steps of the schedule from step {start_step} "
+                                f"(the state one bar reached there, {plastic_frac:.0%} of its Gauss "
+                                f"points plastic, copied into every instance; reached in "
+                                f"{advance_s:.0f} s untimed), extrapolated to {total_steps}",
                        "parameters": ["A", "B", "n", "|v0| (0: starts at rest)"],
                        "l2": "inputs larger than L2 (tangent state "
                              f"{E * 8 * 4 * 20 * 8 / 1e9:.0f} GB)"},
@@ -674,12 +798,15 @@ def main_necking(args):
             "agreement_vs_dual_oracle": agree,
             "gpu_launches": launches,
             "kernel_time_share": {k: round(v[0] / total_ms, 4) for k, v in prof.items()} if total_ms else None,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak_hbm()[0], "unit": "GB/s",
-                         "frac": achieved / peak_hbm()[0] if achieved else None, "traffic": None,
-                         "kernel": "k_elem_tan<ElHex8n3D>", "peak_source": peak_hbm()[1],
+            "roofline": {"bound": "fp64", "achieved": None, "peak": None, "unit": "TFLOP/s",
+                         "frac": None, "traffic": None,
+                         "kernel": "k_elem_tan<ElHex8n3D>",
                          "avg_launch_ms": tan_ms / max(tan_n, 1),
-                         "algorithmic_bytes_per_launch": tan_bytes,
-                         "note": "the tangent pass is FP64-pipe bound"},
+                         "hbm": {"achieved": achieved, "peak": peak_hbm()[0], "unit": "GB/s",
+                                 "frac": achieved / peak_hbm()[0] if achieved else None,
+                                 "peak_source": peak_hbm()[1],
+                                 "algorithmic_bytes_per_launch": tan_bytes},
+                         "note": "the tangent pass is FP64-pipe bound; no FP64 count is taken here"},
             "cpu_baseline": cpu,
             "e2e": {"value": 1.0 / (wall / args.steps * total_steps) * len(models), "unit": "gradients/s",
                     "h2d_bytes_per_step": 8, "d2h_bytes_per_step": 0},
@@ -695,6 +822,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="hex", choices=["hex", "hex1pt", "axi", "batch", "sens", "necking"])
     ap.add_argument("--necking-instances", type=int, default=32)
+    ap.add_argument("--necking-start", type=int, default=15000,
+                    help="schedule step at which the necking window starts (reached untimed)")
     ap.add_argument("--sens-steps", type=int, default=4000,
                     help="explicit steps of the gradient workload's schedule")
     ap.add_argument("--instances", type=int, default=256)
@@ -703,6 +832,8 @@ def main():
                     help="simulated time at which the timed window starts (reached untimed), so "
                          "the window sees the deformed, partly plastic bar of a real run")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched and gradient workloads that the default line also reports")
     ap.add_argument("--layers", type=int, default=400,
                     help="axial layers of the hex bar (400 = the benchmark workload; fewer for "
                          "profiling captures)")

@@ -188,8 +188,18 @@ int dnl_batch_step_graph(dnl_batch *b, int nsteps, int *active);
 /* capture (without running) the graph dnl_batch_step_graph(b, nsteps) replays from the current
  * increment; DNL_ERR_ARG when the handle's graph cache (8 graphs) is full */
 int dnl_batch_graph_capture(dnl_batch *b, int nsteps);
-/* time live steps with 64, 128 and 256 threads per element-pass block; keep the fastest */
+/* How a batched step is launched: DNL_BATCH_LAUNCHES, the sequence of kernels of the single-mesh
+ * step (time logic, boundary conditions, element pass, nodal update, Courant reduction), each once
+ * for all instances; DNL_BATCH_PERSISTENT, one persistent cooperative kernel per step running the
+ * same phases separated by grid-wide barriers (bounded waits: DNL_ERR_TIMEOUT if one runs out).
+ * Results are bit for bit the same either way. */
+#define DNL_BATCH_LAUNCHES 0
+#define DNL_BATCH_PERSISTENT 1
+int dnl_batch_set_mode(dnl_batch *b, int mode);
+/* time live steps of both modes with 64, 128 and 256 threads per element-pass block; keep the
+ * fastest (*block: its block size; dnl_batch_get_tuning gives both) */
 int dnl_batch_autotune(dnl_batch *b, int steps_per_candidate, int *block);
+int dnl_batch_get_tuning(dnl_batch *b, int *mode, int *block);
 int dnl_batch_set_block(dnl_batch *b, int block);
 int dnl_batch_time_info(dnl_batch *b, int instance, dnl_time_info *info);
 int dnl_batch_get_coords(dnl_batch *b, int instance, double *coords);
@@ -304,11 +314,41 @@ int dnl_read_results(dnl_handle *h, const char *path);
 int dnl_sens_run(dnl_handle *h, int nsteps, const double *dts, double *coords, double *dcoords);
 /* step-size schedule used by dnl_adjoint */
 int dnl_set_dt_schedule(dnl_handle *h, const double *dts, int nsteps);
-/* gradient of L(x_final) for a given dL/dx_final (3N): grad[p] = sum dL/dx . dx/dp, p = A, B, n,
- * |v0|, over the schedule set by dnl_set_dt_schedule.  ckpt_stride (>= 0) is accepted for
- * interface compatibility with checkpointed reverse-mode adjoints and unused: the forward mode
- * keeps no checkpoints. */
+/* The gradient of a loss L(x_final) in reverse mode: grad[p] = sum dL/dx . dx/dp for p = A, B, n,
+ * |v0|, given dL/dx_final (3N, node-major), over the schedule set by dnl_set_dt_schedule, from the
+ * handle's initial state (no step taken yet, as dnl_sens_run).  One forward sweep stores the state
+ * every ckpt_stride steps (ckpt_stride = 0: ceil(sqrt(nsteps))); the reverse sweep restores each
+ * segment from its checkpoint, runs it again storing its steps' states, and undoes its steps in
+ * reverse order through the adjoints of the nodal update, the element pass (kinematics, polar
+ * decomposition, J2 return, RFI rotation, forces) and the assembly.  Memory: ceil(nsteps /
+ * ckpt_stride) checkpoints plus ckpt_stride step states (dnl_adjoint_stats), so O(sqrt(nsteps))
+ * with the default; cost: about three forward runs.  The same linearisation as the forward mode
+ * (dnl_sens_run), so the two gradients agree to rounding.  One power-law material; every element
+ * type but DNL_ELHEX8N3D_1PT.  The handle is back at its initial state afterwards.  No counterpart
+ * in the reference, which has no derivatives. */
 int dnl_adjoint(dnl_handle *h, const double *dL_dx, double *grad, int ckpt_stride);
+/* dnl_adjoint in two calls, for a caller that needs the final coordinates to form dL/dx: the
+ * forward sweep (the scheduled run from the initial state with its checkpoints; coords, 3N
+ * node-major, may be NULL, receives the final coordinates; the handle is left at the final state),
+ * then the reverse sweep over those checkpoints (the handle is back at its initial state after).
+ * dnl_adjoint_backward without a preceding forward sweep returns DNL_ERR_ARG. */
+int dnl_adjoint_forward(dnl_handle *h, int ckpt_stride, double *coords);
+int dnl_adjoint_backward(dnl_handle *h, const double *dL_dx, double *grad);
+typedef struct {
+  int nsteps;                  /* steps of the schedule */
+  int stride;                  /* steps per checkpoint segment */
+  int checkpoints;             /* states stored by the forward sweep */
+  long long recomputed_steps;  /* steps run again by the reverse sweep */
+  long long bytes;             /* device memory of the adjoint (checkpoints, step states, adjoints) */
+  long long checkpoint_bytes;  /* of which the checkpoints */
+  long long record_bytes;      /* of which one segment's step states */
+} dnl_adjoint_info;
+/* figures of the last dnl_adjoint on this handle */
+int dnl_adjoint_stats(dnl_handle *h, dnl_adjoint_info *info);
+/* The scheduled run alone (no derivatives): nsteps steps of sizes dts from the handle's initial
+ * state; coords (3N, node-major, may be NULL) receives the final coordinates.  The primal of
+ * dnl_sens_run and of dnl_adjoint, bit for bit. */
+int dnl_run_schedule(dnl_handle *h, int nsteps, const double *dts, double *coords);
 /* The same for every instance of a batch at once, all with the schedule dts, from the batch's
  * initial state; coords (3 x total nodes) and dcoords (4 x 3 x total nodes) in the union's node
  * order (instance after instance, see dnl_batch_sizes).  A batch created for this may hold
@@ -316,6 +356,12 @@ int dnl_adjoint(dnl_handle *h, const double *dL_dx, double *grad, int ckpt_strid
 int dnl_batch_sens_run(dnl_batch *b, int nsteps, const double *dts, double *coords, double *dcoords);
 /* every instance back to its initial state (as dnl_batch_create left it), device buffers kept */
 int dnl_batch_reset(dnl_batch *b);
+/* the state of a single-mesh handle of the same mesh (coordinates, Current nodal field,
+ * integration-point state; evp^n recomputed with each instance's n) copied into every instance,
+ * on the device; the time records are kept.  For starting a batch from a state one run reached,
+ * e.g. timing the plastic phase of a long schedule.  DNL_ERR_ARG unless every instance has the
+ * handle's element type and sizes. */
+int dnl_batch_broadcast_state(dnl_batch *b, dnl_handle *src);
 
 /* -------------------------------------------------------------------------- measurement */
 /* Per-kernel device time: between dnl_profile_begin and dnl_profile_end the library brackets each

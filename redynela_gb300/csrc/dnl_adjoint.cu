@@ -1,0 +1,614 @@
+// Reverse-mode gradients of an explicit run (dnl_adjoint), with checkpointing.
+//
+// The run is the scheduled explicit run of dnl_sens_run (ExplicitSolverCH.C:179-274 with the step
+// sizes of dnl_set_dt_schedule).  dnl_adjoint returns grad = (dx_final/dp)^T dL/dx_final for the
+// hardening parameters A, B, n and the initial-velocity magnitude |v0|, by one forward sweep and
+// one reverse sweep:
+//
+//  * forward: the run from the handle's initial state, with the state (coordinates, the Current
+//    nodal field, integration-point state, time record) copied aside before every `stride`-th step
+//    -- ceil(n / stride) checkpoints (stride = ceil(sqrt(n)) by default);
+//  * reverse: for each segment from the last, the state is restored from its checkpoint and the
+//    segment's steps run again, each saving the coordinates, the Current delta_disp the element
+//    pass reads and the integration-point state before it (stride records); then the segment's
+//    steps are undone in reverse order, each by
+//      - the element pass again from its saved state with its per-point record (k_elem<ET, true>),
+//      - the adjoint of the nodal update (k_node_adj): Chung-Hulbert corrector and predictor and
+//        the constant boundary conditions, whose formulas are linear in the state,
+//      - the adjoint of the element pass (k_elem_adj), and
+//      - the reverse gather (k_gather_adj): each node sums its element nodes' coordinate and
+//        delta_disp adjoints in ascending element order, no atomics.
+//    The hardening parameters' derivatives accumulate per integration point over the steps; the
+//    initial velocity's is the adjoint of the first step's Current velocity along v0's direction.
+//
+// Memory: ceil(n / stride) checkpoints plus stride step records, each of the size of the nodal
+// fields and integration-point state -- O(sqrt(n)) states instead of the n of a stored trajectory
+// -- for one extra forward run of every segment (the recomputation).  The derivative is that of the
+// run as computed at the converged return-mapping multipliers and computed eigenpairs, the same
+// linearisation as the forward-mode tangent (dnl_sens_run), so the two agree to rounding.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "dnl_common.cuh"
+
+namespace dnl {
+
+namespace {
+
+struct AdjState {
+  int E = 0, N = 0, nsteps = 0, stride = 0, nseg = 0, etype = -1;
+  size_t ckptDoubles = 0, slotDoubles = 0;
+  double *mem = nullptr;
+  double *ckpt = nullptr;       // nseg x [x(3N) | Current du, v, a, disp (12N) | ip (NCOMP nIP)]
+  DevTime *ckptTm = nullptr;    // nseg time records
+  std::vector<int> ckptCur;     // Current bank index at each checkpoint
+  double *slot = nullptr;       // stride x [x(3N) | Current du (3N) | ip (NCOMP nIP)]
+  double *tape = nullptr;       // [NT][nIP]
+  double *ipWork = nullptr;     // [NCOMP][nIP]: a step's state, the pass run on it in place
+  double *feWork = nullptr;     // [DIM][E NEN]
+  DevTime *tmWork = nullptr;
+  double *lam[2] = {nullptr, nullptr};  // nodal adjoints [du, v, a, disp][3][N]
+  double *xbar = nullptr, *fbar = nullptr;  // [3][N]
+  double *ipAdj = nullptr;      // [TanLayout::NCOMP][nIP]
+  double *xe = nullptr, *ue = nullptr;  // [DIM][E NEN]
+  double *gpar = nullptr;       // [3][nIP]
+  double *dts = nullptr;        // the schedule on the device
+  double *host = nullptr;       // page-locked staging, 3 max(N, nIP) doubles
+  size_t bytes = 0;
+  long long recomputed = 0;
+  dnl_adjoint_info info;        // figures of the last dnl_adjoint
+  bool hasInfo = false;
+  double *runDts = nullptr;     // dnl_run_schedule's schedule on the device
+  double *runOut = nullptr;     // and its staging for the coordinates (3N)
+  int runCap = 0, runN = 0;
+  std::vector<double> sched;    // the schedule of the last forward sweep (host)
+  bool ready = false;           // a forward sweep's checkpoints await the reverse sweep
+};
+
+__global__ void k_adj_dt(DevTime *tm, const double *dts, int phase)
+{
+  if (tm->status) return;
+  if (phase == 0) {  // initStep with the scheduled step
+    const double dt = dts[tm->increment];
+    tm->timeStep = dt;
+    tm->nextTime = __dadd_rn(tm->currentTime, dt);
+    tm->increment++;
+  } else {  // updateTime
+    tm->currentTime = __dadd_rn(tm->currentTime, tm->timeStep);
+  }
+}
+
+struct AdjNodeArgs {
+  int N;
+  const double *mass;
+  const int *bcIdx, *bcCode;
+  const double *ln;  // adjoints of the New field after the step, [du, v, a, disp][3][N]
+  double *lc;        // adjoints of the Current field before it (v, a, disp written here)
+  const double *xbar;
+  double *fbar;
+  double dt, alphaM, beta, gamma;
+};
+
+// Adjoint of node_update (dnl_host.cu) for one node.  Per free component, with
+// u = adj(New du) + adj(New disp) + adj(x') (delta_disp feeds the New field, the displacement and
+// the coordinates) and a' = adj(New a) + dt gamma adj(New v) + dt^2 beta u:
+//   adj(F) = a' / (m (1 - alphaM)),
+//   adj(Current a) = -alphaM / (1 - alphaM) a' + dt (1 - gamma) adj(New v) + dt^2 (1/2 - beta) u,
+//   adj(Current v) = adj(New v) + dt u,  adj(Current disp) = adj(New disp).
+// A restrained or imposed-speed component's New du, v, a are constants: no force or Current
+// velocity / acceleration adjoint from it.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_node_adj(AdjNodeArgs g)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= g.N) return;
+  const long N = g.N;
+  const int bc = g.bcIdx[n];
+  const int code = bc >= 0 ? g.bcCode[bc] : 0;
+  const double rm = 1.0 / g.mass[n], roma = 1.0 / (1.0 - g.alphaM);
+  const double c1 = g.dt * (0.5 - g.beta), c2 = g.dt * (1.0 - g.gamma);
+  const double cg = g.dt * g.gamma, cb = g.dt * g.dt * g.beta;
+#pragma unroll
+  for (int i = 0; i < DIM; i++) {
+    const long o = (long)i * N + n;
+    const double nu = g.ln[o], nv = g.ln[3 * N + o], na = g.ln[6 * N + o], nd = g.ln[9 * N + o];
+    const double u = nu + nd + g.xbar[o];
+    double fb = 0., cv = 0., ca = 0.;
+    if (!((code >> (2 * i)) & 3)) {
+      const double ab = fma(cb, u, fma(cg, nv, na));
+      fb = ab * rm * roma;
+      ca = fma(-g.alphaM * roma, ab, fma(c2, nv, g.dt * c1 * u));
+      cv = fma(g.dt, u, nv);
+    }
+    g.fbar[o] = fb;
+    g.lc[3 * N + o] = cv;
+    g.lc[6 * N + o] = ca;
+    g.lc[9 * N + o] = nd;
+  }
+}
+
+// Reverse gather: adj(x) += sum of the element nodes' coordinate adjoints, adj(Current du) = sum of
+// their delta_disp adjoints (ascending element order, as k_gather); then the constant boundary
+// conditions, which overwrite the Current du, v, a of their components before the element pass
+// reads them (k_bc_current), zero those components' adjoints.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_gather_adj(int N, int EN, const int *start, const int *entry,
+                                                    const double *xe, const double *ue, double *xbar,
+                                                    double *lc, const int *bcIdx, const int *bcCode)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  double sx[DIM], su[DIM];
+#pragma unroll
+  for (int c = 0; c < DIM; c++) sx[c] = su[c] = 0.;
+  for (int q = start[n]; q < start[n + 1]; q++) {
+    const int ent = __ldg(entry + q);
+#pragma unroll
+    for (int c = 0; c < DIM; c++) {
+      sx[c] += __ldg(xe + (long)c * EN + ent);
+      su[c] += __ldg(ue + (long)c * EN + ent);
+    }
+  }
+  const int bc = bcIdx[n];
+  const int code = bc >= 0 ? bcCode[bc] : 0;
+#pragma unroll
+  for (int c = 0; c < DIM; c++) {
+    const long o = (long)c * N + n;
+    xbar[o] += sx[c];
+    const bool fixed = (code >> (2 * c)) & 3;
+    lc[o] = fixed ? 0. : su[c];
+    if (fixed) {
+      lc[3L * N + o] = 0.;
+      lc[6L * N + o] = 0.;
+    }
+  }
+}
+
+// dL/d|v0| = sum over nodes of adj(Current v) at the first step . u (u = v0 / |v0|), and the
+// per-point parameter sums, reduced in a fixed order by one block
+__global__ void k_adj_reduce(int N, long nIP, const double *lcv, double u0, double u1, double u2,
+                             const double *gpar, double *out)
+{
+  __shared__ double sh[4][256];
+  double s[4] = {0., 0., 0., 0.};
+  for (long i = threadIdx.x; i < nIP; i += blockDim.x)
+    for (int p = 0; p < 3; p++) s[p] += gpar[p * nIP + i];
+  for (int n = threadIdx.x; n < N; n += blockDim.x)
+    s[3] += fma(lcv[n], u0, fma(lcv[(long)N + n], u1, lcv[2L * N + n] * u2));
+  for (int p = 0; p < 4; p++) sh[p][threadIdx.x] = s[p];
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o)
+      for (int p = 0; p < 4; p++) sh[p][threadIdx.x] += sh[p][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) out[threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void k_aos3(int N, const double *soa, double *aos)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+#pragma unroll
+  for (int c = 0; c < 3; c++) aos[3L * n + c] = soa[(long)c * N + n];
+}
+
+__global__ void k_soa3(int N, const double *aos, double *soa)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+#pragma unroll
+  for (int c = 0; c < 3; c++) soa[(long)c * N + n] = aos[3L * n + c];
+}
+
+#define CKA(x)                                      \
+  do {                                              \
+    if ((x) != cudaSuccess) return DNL_ERR_CUDA;    \
+  } while (0)
+
+int ip_ncomp(int etype) { return 3 * etype_ns(etype) + 3; }
+int tan_ncomp_of(int etype) { return 3 * etype_ns(etype) + 2; }
+int tape_nt_of(int etype)
+{
+  return etype_dim(etype) == 3 ? TapeLayout<DNL_ELHEX8N3D>::NT : TapeLayout<DNL_ELQUA4NAX>::NT;
+}
+
+void adj_release(AdjState *A)
+{
+  if (A->runDts) cudaFree(A->runDts);
+  if (A->runOut) cudaFree(A->runOut);
+  if (A->mem) cudaFree(A->mem);
+  if (A->ckptTm) cudaFree(A->ckptTm);
+  if (A->tmWork) cudaFree(A->tmWork);
+  if (A->dts) cudaFree(A->dts);
+  if (A->host) cudaFreeHost(A->host);
+  *A = AdjState();
+}
+
+int adj_alloc(dnl_handle *h, AdjState *A, int nsteps, int stride)
+{
+  const int nseg = (nsteps + stride - 1) / stride;
+  if (A->mem && A->E == h->E && A->N == h->N && A->etype == h->etype && A->stride == stride &&
+      A->nsteps == nsteps)
+    return 0;
+  {
+    double *rd = A->runDts, *ro = A->runOut;
+    const int rc = A->runCap, rn = A->runN;
+    A->runDts = A->runOut = nullptr;
+    adj_release(A);
+    A->runDts = rd;
+    A->runOut = ro;
+    A->runCap = rc;
+    A->runN = rn;
+  }
+  const size_t N = h->N, nIP = h->nIP, EN = (size_t)h->E * h->nen;
+  const int NC = ip_ncomp(h->etype), NT = tape_nt_of(h->etype), TC = tan_ncomp_of(h->etype);
+  A->E = h->E;
+  A->N = h->N;
+  A->etype = h->etype;
+  A->nsteps = nsteps;
+  A->stride = stride;
+  A->nseg = nseg;
+  A->ckptDoubles = 15 * N + NC * nIP;
+  A->slotDoubles = 6 * N + NC * nIP;
+  const size_t total = nseg * A->ckptDoubles + stride * A->slotDoubles + NT * nIP + NC * nIP +
+                       h->dim * EN + 2 * 12 * N + 6 * N + TC * nIP + 2 * h->dim * EN + 3 * nIP;
+  CKA(cudaMalloc(&A->mem, sizeof(double) * total));
+  CKA(cudaMalloc(&A->ckptTm, sizeof(DevTime) * nseg));
+  CKA(cudaMalloc(&A->tmWork, sizeof(DevTime)));
+  CKA(cudaMalloc(&A->dts, sizeof(double) * nsteps));
+  const size_t hostN = 4 * (N > nIP ? N : nIP);
+  CKA(cudaMallocHost(&A->host, sizeof(double) * hostN));
+  double *p = A->mem;
+  A->ckpt = p;
+  p += nseg * A->ckptDoubles;
+  A->slot = p;
+  p += stride * A->slotDoubles;
+  A->tape = p;
+  p += NT * nIP;
+  A->ipWork = p;
+  p += NC * nIP;
+  A->feWork = p;
+  p += h->dim * EN;
+  A->lam[0] = p;
+  p += 12 * N;
+  A->lam[1] = p;
+  p += 12 * N;
+  A->xbar = p;
+  p += 3 * N;
+  A->fbar = p;
+  p += 3 * N;
+  A->ipAdj = p;
+  p += TC * nIP;
+  A->xe = p;
+  p += h->dim * EN;
+  A->ue = p;
+  p += h->dim * EN;
+  A->gpar = p;
+  A->ckptCur.assign(nseg, 0);
+  A->bytes = sizeof(double) * total + sizeof(DevTime) * (nseg + 1) + sizeof(double) * nsteps;
+  return 0;
+}
+
+// one scheduled explicit step of the handle (the launches of dnl_sens_run's primal); with `rec`,
+// the coordinates, the Current delta_disp and the integration-point state the element pass reads
+// are copied there first
+int adj_primal_step(dnl_handle *h, const double *dtsDev, double *rec)
+{
+  cudaStream_t s = h->stream;
+  const size_t N = h->N, nIP = h->nIP;
+  k_adj_dt<<<1, 1, 0, s>>>(h->tm, dtsDev, 0);
+  launch_counter()++;
+  int r;
+  if ((r = enqueue_bc_current(h))) return r;
+  if (rec) {
+    CKA(cudaMemcpyAsync(rec, h->x[0], sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
+    CKA(cudaMemcpyAsync(rec + 3 * N, h->bank[h->cur].du[0], sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
+    CKA(cudaMemcpyAsync(rec + 6 * N, h->ip, sizeof(double) * ip_ncomp(h->etype) * nIP, cudaMemcpyDeviceToDevice, s));
+  }
+  if ((r = launch_elem(h, s, 1))) return r;
+  if ((r = enqueue_node(h))) return r;
+  h->cur = 1 - h->cur;
+  k_adj_dt<<<1, 1, 0, s>>>(h->tm, dtsDev, 1);
+  launch_counter()++;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
+}
+
+int adj_save(dnl_handle *h, AdjState *A, int seg)
+{
+  cudaStream_t s = h->stream;
+  const size_t N = h->N, nIP = h->nIP;
+  double *c = A->ckpt + seg * A->ckptDoubles;
+  CKA(cudaMemcpyAsync(c, h->x[0], sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
+  CKA(cudaMemcpyAsync(c + 3 * N, h->bank[h->cur].du[0], sizeof(double) * 12 * N, cudaMemcpyDeviceToDevice, s));
+  CKA(cudaMemcpyAsync(c + 15 * N, h->ip, sizeof(double) * ip_ncomp(h->etype) * nIP, cudaMemcpyDeviceToDevice, s));
+  CKA(cudaMemcpyAsync(A->ckptTm + seg, h->tm, sizeof(DevTime), cudaMemcpyDeviceToDevice, s));
+  A->ckptCur[seg] = h->cur;
+  return 0;
+}
+
+int adj_restore(dnl_handle *h, AdjState *A, int seg)
+{
+  cudaStream_t s = h->stream;
+  const size_t N = h->N, nIP = h->nIP;
+  h->cur = A->ckptCur[seg];
+  const double *c = A->ckpt + seg * A->ckptDoubles;
+  CKA(cudaMemcpyAsync(h->x[0], c, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
+  CKA(cudaMemcpyAsync(h->bank[h->cur].du[0], c + 3 * N, sizeof(double) * 12 * N, cudaMemcpyDeviceToDevice, s));
+  CKA(cudaMemcpyAsync(h->ip, c + 15 * N, sizeof(double) * ip_ncomp(h->etype) * nIP, cudaMemcpyDeviceToDevice, s));
+  CKA(cudaMemcpyAsync(h->tm, A->ckptTm + seg, sizeof(DevTime), cudaMemcpyDeviceToDevice, s));
+  return 0;
+}
+
+// undo one step from its record: the pass again with its per-point record, then the adjoints of the
+// nodal update, the element pass and the gather; ln / lc: the New / Current nodal adjoints
+int adj_reverse_step(dnl_handle *h, AdjState *A, const double *rec, double dt, const double *ln, double *lc)
+{
+  cudaStream_t s = h->stream;
+  const size_t N = h->N, nIP = h->nIP;
+  const int NC = ip_ncomp(h->etype);
+  CKA(cudaMemcpyAsync(A->ipWork, rec + 6 * N, sizeof(double) * NC * nIP, cudaMemcpyDeviceToDevice, s));
+  ElemArgs ea = elem_args_of(h);
+  ea.gate = 0;
+  for (int r = 0; r < 3; r++) {
+    ea.x[r] = const_cast<double *>(rec) + r * N;
+    ea.du[r] = rec + 3 * N + r * N;
+  }
+  ea.ip = A->ipWork;
+  ea.fe = A->feWork;
+  ea.detJ = nullptr;
+  ea.stepT = nullptr;
+  ea.tape = A->tape;
+  ea.tm = A->tmWork;
+  int r;
+  prof_begin(h, s);
+  r = launch_elem_tape_raw(h->etype, ea, s);
+  prof_end(h, DNL_PROF_ELEM, s);
+  if (r) return r;
+  AdjNodeArgs g;
+  g.N = h->N;
+  g.mass = h->mass;
+  g.bcIdx = h->bcIdx;
+  g.bcCode = h->bcCode;
+  g.ln = ln;
+  g.lc = lc;
+  g.xbar = A->xbar;
+  g.fbar = A->fbar;
+  g.dt = dt;
+  g.alphaM = h->alphaM;
+  g.beta = h->beta;
+  g.gamma = h->gamma;
+  const int gridN = (h->N + 255) / 256;
+  prof_begin(h, s);
+  if (h->dim == 2)
+    k_node_adj<2><<<gridN, 256, 0, s>>>(g);
+  else
+    k_node_adj<3><<<gridN, 256, 0, s>>>(g);
+  prof_end(h, DNL_PROF_NODE, s);
+  launch_counter()++;
+  AdjElemArgs aa;
+  aa.E = h->E;
+  aa.N = h->N;
+  aa.conn = h->conn;
+  for (int c = 0; c < 3; c++) aa.x[c] = rec + c * N;
+  aa.tape = A->tape;
+  aa.ipOut = A->ipWork;
+  aa.fbar = A->fbar;
+  aa.ipAdj = A->ipAdj;
+  aa.xe = A->xe;
+  aa.ue = A->ue;
+  aa.gpar = A->gpar;
+  aa.mat = h->mat;
+  prof_begin(h, s);
+  r = launch_elem_adj(h->etype, aa, s);
+  prof_end(h, DNL_PROF_TANGENT, s);
+  if (r) return r;
+  prof_begin(h, s);
+  if (h->dim == 2)
+    k_gather_adj<2><<<gridN, 256, 0, s>>>(h->N, h->E * h->nen, h->n2eStart, h->n2e, A->xe, A->ue,
+                                          A->xbar, lc, h->bcIdx, h->bcCode);
+  else
+    k_gather_adj<3><<<gridN, 256, 0, s>>>(h->N, h->E * h->nen, h->n2eStart, h->n2e, A->xe, A->ue,
+                                          A->xbar, lc, h->bcIdx, h->bcCode);
+  prof_end(h, DNL_PROF_NODE, s);
+  launch_counter()++;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
+}
+
+}  // namespace
+
+void adj_free(dnl_handle *h)
+{
+  AdjState *A = (AdjState *)h->adj;
+  if (!A) return;
+  adj_release(A);
+  delete A;
+  h->adj = nullptr;
+}
+
+// forward sweep: the scheduled run from the initial state with a checkpoint before every
+// `stride`-th step; the final coordinates are left in the handle
+int adjoint_forward(dnl_handle *h, const double *dts, int nsteps, int stride)
+{
+  if (!etype_has_sens(h->etype) || h->etype == DNL_ELHEX8N3D_1PT) return DNL_ERR_ARG;
+  if (h->elemMat || h->mat.hard.law != DNL_HARD_POWER) return DNL_ERR_ARG;
+  if (stride <= 0) stride = (int)ceil(sqrt((double)nsteps));
+  if (stride > nsteps) stride = nsteps;
+  if (!h->adj) h->adj = new AdjState();
+  AdjState *A = (AdjState *)h->adj;
+  int r;
+  A->ready = false;
+  if ((r = adj_alloc(h, A, nsteps, stride))) return r;
+  cudaStream_t s = h->stream;
+  CKA(cudaMemcpyAsync(A->dts, dts, sizeof(double) * nsteps, cudaMemcpyHostToDevice, s));
+  A->sched.assign(dts, dts + nsteps);
+  A->recomputed = 0;
+  for (int seg = 0; seg < A->nseg; seg++) {
+    if ((r = adj_save(h, A, seg))) return r;
+    const int len = seg == A->nseg - 1 ? nsteps - seg * stride : stride;
+    for (int j = 0; j < len; j++)
+      if ((r = adj_primal_step(h, A->dts, nullptr))) return r;
+  }
+  DevTime t;
+  CKA(cudaMemcpyAsync(&t, h->tm, sizeof t, cudaMemcpyDeviceToHost, s));
+  CKA(cudaStreamSynchronize(s));
+  if (t.status) return t.status;
+  A->ready = true;
+  return 0;
+}
+
+// reverse sweep over the checkpoints of the last forward sweep, from dL/dx_final (3N node-major);
+// the handle is back at its initial state afterwards
+int adjoint_backward(dnl_handle *h, const double *dL_dx, double *grad, dnl_adjoint_info *info)
+{
+  AdjState *A = (AdjState *)h->adj;
+  if (!A || !A->ready) return DNL_ERR_ARG;
+  A->ready = false;
+  int r;
+  cudaStream_t s = h->stream;
+  const size_t N = h->N, nIP = h->nIP;
+  const int nsteps = A->nsteps, stride = A->stride;
+  const double *dts = A->sched.data();
+  memcpy(A->host, dL_dx, sizeof(double) * 3 * N);
+  CKA(cudaMemcpyAsync(A->fbar, A->host, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s));
+  k_soa3<<<(unsigned)((N + 255) / 256), 256, 0, s>>>((int)N, A->fbar, A->xbar);
+  launch_counter()++;
+  CKA(cudaMemsetAsync(A->lam[0], 0, sizeof(double) * 24 * N, s));
+  CKA(cudaMemsetAsync(A->ipAdj, 0, sizeof(double) * tan_ncomp_of(h->etype) * nIP, s));
+  CKA(cudaMemsetAsync(A->gpar, 0, sizeof(double) * 3 * nIP, s));
+  if (h->dim == 2) CKA(cudaMemsetAsync(A->xbar + 2 * N, 0, sizeof(double) * N, s));
+
+  int nw = 0;  // lam[nw]: adjoints of the New field after the step being undone
+  for (int seg = A->nseg - 1; seg >= 0; seg--) {
+    if ((r = adj_restore(h, A, seg))) return r;
+    const int len = seg == A->nseg - 1 ? nsteps - seg * stride : stride;
+    for (int j = 0; j < len; j++)
+      if ((r = adj_primal_step(h, A->dts, A->slot + j * A->slotDoubles))) return r;
+    A->recomputed += len;
+    for (int j = len - 1; j >= 0; j--) {
+      const int step = seg * stride + j;
+      if ((r = adj_reverse_step(h, A, A->slot + j * A->slotDoubles, dts[step], A->lam[nw], A->lam[1 - nw])))
+        return r;
+      nw = 1 - nw;
+    }
+  }
+  // lam[nw] now holds the adjoints of the first step's Current field
+  k_adj_reduce<<<1, 256, 0, s>>>((int)N, (long)nIP, A->lam[nw] + 3 * N, h->v0dir[0], h->v0dir[1],
+                                 h->v0dir[2], A->gpar, A->fbar);
+  launch_counter()++;
+  double out[4];
+  CKA(cudaMemcpyAsync(out, A->fbar, sizeof out, cudaMemcpyDeviceToHost, s));
+  CKA(cudaStreamSynchronize(s));
+  CKA(cudaGetLastError());
+  for (int p = 0; p < 4; p++) grad[p] = out[p];
+  // back to the initial state: the first checkpoint
+  if ((r = adj_restore(h, A, 0))) return r;
+  CKA(cudaStreamSynchronize(s));
+  if (info) {
+    info->checkpoints = A->nseg;
+    info->stride = stride;
+    info->nsteps = nsteps;
+    info->recomputed_steps = A->recomputed;
+    info->bytes = (long long)A->bytes;
+    info->checkpoint_bytes = (long long)(sizeof(double) * A->nseg * A->ckptDoubles);
+    info->record_bytes = (long long)(sizeof(double) * A->stride * A->slotDoubles);
+  }
+  return 0;
+}
+
+}  // namespace dnl
+
+using namespace dnl;
+
+extern "C" {
+
+int dnl_adjoint_forward(dnl_handle *h, int ckpt_stride, double *coords)
+{
+  if (!h || ckpt_stride < 0) return DNL_ERR_ARG;
+  const double *dts;
+  int n;
+  if (sens_schedule(h, &dts, &n)) return DNL_ERR_ARG;
+  if (h->hostIncrement != 0) return DNL_ERR_ARG;  // starts from the initial state
+  int r;
+  if (!h->prologueDone && (r = dnl_prologue(h))) return r;
+  if ((r = adjoint_forward(h, dts, n, ckpt_stride))) return r;
+  AdjState *A = (AdjState *)h->adj;
+  h->hostIncrement = n;
+  if (coords) {
+    cudaStream_t s = h->stream;
+    k_aos3<<<(unsigned)((h->N + 255) / 256), 256, 0, s>>>(h->N, h->x[0], A->fbar);
+    launch_counter()++;
+    CKA(cudaMemcpyAsync(coords, A->fbar, sizeof(double) * 3 * (size_t)h->N, cudaMemcpyDeviceToHost, s));
+    CKA(cudaStreamSynchronize(s));
+  }
+  return 0;
+}
+
+int dnl_adjoint_backward(dnl_handle *h, const double *dL_dx, double *grad)
+{
+  if (!h || !dL_dx || !grad || !h->adj || !((AdjState *)h->adj)->ready) return DNL_ERR_ARG;
+  dnl_adjoint_info info;
+  memset(&info, 0, sizeof info);
+  int r = adjoint_backward(h, dL_dx, grad, &info);
+  if (r) return r;
+  AdjState *A = (AdjState *)h->adj;
+  A->info = info;
+  A->hasInfo = true;
+  h->hostIncrement = 0;
+  return 0;
+}
+
+int dnl_adjoint(dnl_handle *h, const double *dL_dx, double *grad, int ckpt_stride)
+{
+  if (!h || !dL_dx || !grad || ckpt_stride < 0) return DNL_ERR_ARG;
+  int r;
+  if ((r = dnl_adjoint_forward(h, ckpt_stride, nullptr))) return r;
+  return dnl_adjoint_backward(h, dL_dx, grad);
+}
+
+int dnl_adjoint_stats(dnl_handle *h, dnl_adjoint_info *info)
+{
+  if (!h || !info || !h->adj || !((AdjState *)h->adj)->hasInfo) return DNL_ERR_ARG;
+  *info = ((AdjState *)h->adj)->info;
+  return 0;
+}
+
+int dnl_run_schedule(dnl_handle *h, int nsteps, const double *dts, double *coords)
+{
+  if (!h || nsteps <= 0 || !dts) return DNL_ERR_ARG;
+  for (int k = 0; k < nsteps; k++)
+    if (!(dts[k] > 0. && dts[k] < 1e300)) return DNL_ERR_ARG;
+  if (h->hostIncrement != 0) return DNL_ERR_ARG;  // starts from the initial state
+  int r;
+  if (!h->prologueDone && (r = dnl_prologue(h))) return r;
+  if (!h->adj) h->adj = new AdjState();
+  AdjState *A = (AdjState *)h->adj;
+  cudaStream_t s = h->stream;
+  if (A->runCap < nsteps || A->runN != h->N) {
+    if (A->runDts) cudaFree(A->runDts);
+    if (A->runOut) cudaFree(A->runOut);
+    A->runDts = A->runOut = nullptr;
+    A->runCap = 0;
+    CKA(cudaMalloc(&A->runDts, sizeof(double) * nsteps));
+    CKA(cudaMalloc(&A->runOut, sizeof(double) * 3 * (size_t)h->N));
+    A->runCap = nsteps;
+    A->runN = h->N;
+  }
+  CKA(cudaMemcpyAsync(A->runDts, dts, sizeof(double) * nsteps, cudaMemcpyHostToDevice, s));
+  for (int k = 0; k < nsteps; k++)
+    if ((r = adj_primal_step(h, A->runDts, nullptr))) return r;
+  DevTime t;
+  CKA(cudaMemcpyAsync(&t, h->tm, sizeof t, cudaMemcpyDeviceToHost, s));
+  if (coords) {
+    k_aos3<<<(unsigned)((h->N + 255) / 256), 256, 0, s>>>(h->N, h->x[0], A->runOut);
+    launch_counter()++;
+    CKA(cudaMemcpyAsync(coords, A->runOut, sizeof(double) * 3 * (size_t)h->N, cudaMemcpyDeviceToHost, s));
+  }
+  CKA(cudaStreamSynchronize(s));
+  h->hostIncrement = t.increment;
+  return t.status;
+}
+
+}  // extern "C"

@@ -35,6 +35,9 @@ struct dnl_batch {
   std::vector<InstParams> hprm;
   int freq;
   int block;
+  int mode;             // DNL_BATCH_LAUNCHES or DNL_BATCH_PERSISTENT
+  unsigned *bar;        // persistent mode: grid barrier (arrival count, generation) and
+  int *barErr;          // its time-out flag
   long long increment;  // host copy (all instances advance in lockstep until they finish)
   bool prologueDone;
   bool massDone;
@@ -101,6 +104,50 @@ int first_status(const std::vector<DevTime> &t, int *inst)
   return 0;
 }
 
+// one step as a single persistent cooperative launch (the same phases as the launch sequence
+// below, separated by grid barriers); first: the step opens with initStep
+int enqueue_batch_step_persistent(dnl_batch *b, long long incAfter, bool first, bool last)
+{
+  dnl_handle *h = b->h;
+  BatchStepArgs a;
+  memset(&a, 0, sizeof a);
+  a.ea = elem_args_of(h);
+  NodeArgs &g = a.na;
+  g.N = h->N;
+  g.EN = h->E * h->nen;
+  g.start = h->n2eStart;
+  g.entry = h->n2e;
+  g.fe = h->fe;
+  g.mass = h->mass;
+  g.cur = h->bank[h->cur];
+  g.nxt = h->bank[1 - h->cur];
+  for (int i = 0; i < 3; i++) g.x[i] = h->x[i];
+  g.bcIdx = h->bcIdx;
+  g.bcCode = h->bcCode;
+  g.bcSpeed = h->bcSpeed;
+  g.fint = h->fint;
+  g.tm = nullptr;
+  a.cur = h->bank[h->cur];
+  a.elemInst = b->elemInst;
+  a.nodeInst = b->nodeInst;
+  a.mats = b->mats;
+  a.prm = b->prm;
+  a.tms = b->tms;
+  a.count = b->count;
+  a.nbc = h->nbcNodes;
+  a.bcNodes = h->bcNodeList;
+  a.preFirst = first ? 1 : 0;
+  a.courant = incAfter % b->freq == 0 ? 1 : 0;
+  a.postMode = last ? BT_POST : (BT_POST | BT_PRE);
+  a.bar = b->bar;
+  a.err = b->barErr;
+  prof_begin(h, h->stream);
+  const int r = launch_batch_persistent(h->etype, b->block, a, h->stream);
+  prof_end(h, DNL_PROF_ELEM, h->stream);
+  h->cur = 1 - h->cur;
+  return r;
+}
+
 int enqueue_batch_step(dnl_batch *b, long long incAfter, bool last)
 {
   dnl_handle *h = b->h;
@@ -123,6 +170,47 @@ int enqueue_batch_step(dnl_batch *b, long long incAfter, bool last)
   return launch_dt_batch(h, b->tms, b->prm, b->count, last ? BT_POST : (BT_POST | BT_PRE));
 }
 
+// evp^n of every integration point with its instance's n (the cached yield term), after a state
+// copy
+__global__ void k_batch_evpn(long nIP, int nip, const int *elemInst, const Material *mats,
+                             const double *evp, double *evpn)
+{
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nIP) return;
+  evpn[i] = pow(evp[i], mats[elemInst[i / nip]].n);
+}
+
+// the launches of nsteps steps from increment inc0 in the batch's mode
+int enqueue_steps(dnl_batch *b, long long inc0, int nsteps)
+{
+  dnl_handle *h = b->h;
+  int r;
+  if (b->mode == DNL_BATCH_PERSISTENT) {
+    for (int s = 0; s < nsteps; s++)
+      if ((r = enqueue_batch_step_persistent(b, inc0 + s + 1, s == 0, s == nsteps - 1))) return r;
+    return 0;
+  }
+  if ((r = launch_dt_batch(h, b->tms, b->prm, b->count, BT_PRE))) return r;
+  for (int s = 0; s < nsteps; s++)
+    if ((r = enqueue_batch_step(b, inc0 + s + 1, s == nsteps - 1))) return r;
+  return 0;
+}
+
+// after a run of persistent steps: a barrier that ran out is reported (and its words cleared)
+int barrier_status(dnl_batch *b)
+{
+  if (b->mode != DNL_BATCH_PERSISTENT) return 0;
+  int err = 0;
+  BK(cudaMemcpyAsync(&err, b->barErr, sizeof err, cudaMemcpyDeviceToHost, b->h->stream));
+  BK(cudaStreamSynchronize(b->h->stream));
+  if (!err) return 0;
+  BK(cudaMemsetAsync(b->bar, 0, sizeof(unsigned) * 2, b->h->stream));
+  BK(cudaMemsetAsync(b->barErr, 0, sizeof(int), b->h->stream));
+  BK(cudaStreamSynchronize(b->h->stream));
+  snprintf(g_batchError, sizeof g_batchError, "persistent batch step: a grid barrier wait ran out");
+  return DNL_ERR_TIMEOUT;
+}
+
 }  // namespace
 
 extern "C" {
@@ -131,7 +219,8 @@ int dnl_batch_destroy(dnl_batch *b)
 {
   if (!b) return DNL_ERR_ARG;
   for (int i = 0; i < b->ngraphs; i++) cudaGraphExecDestroy(b->graphs[i].exec);
-  void *ptrs[] = {b->elemInst, b->nodeInst, b->mats, b->prm, b->tms, b->v0dir, b->v0, b->evpn0};
+  void *ptrs[] = {b->elemInst, b->nodeInst, b->mats, b->prm, b->tms, b->v0dir, b->v0, b->evpn0,
+                  b->bar, b->barErr};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (b->h) dnl_destroy(b->h);
@@ -210,6 +299,9 @@ int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material 
   b->elemOff = elemOff;
   b->freq = sps[0].frequency;
   b->block = 128;
+  b->mode = DNL_BATCH_LAUNCHES;
+  b->bar = nullptr;
+  b->barErr = nullptr;
   b->ngraphs = 0;
   b->increment = 0;
   b->prologueDone = false;
@@ -260,6 +352,10 @@ int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material 
   BKF(cudaMalloc(&b->mats, sizeof(Material) * count));
   BKF(cudaMalloc(&b->prm, sizeof(InstParams) * count));
   BKF(cudaMalloc(&b->tms, sizeof(DevTime) * count));
+  BKF(cudaMalloc(&b->bar, sizeof(unsigned) * 2));
+  BKF(cudaMemset(b->bar, 0, sizeof(unsigned) * 2));
+  BKF(cudaMalloc(&b->barErr, sizeof(int)));
+  BKF(cudaMemset(b->barErr, 0, sizeof(int)));
   BKF(cudaMemcpy(b->elemInst, elemInst.data(), sizeof(int) * E, cudaMemcpyHostToDevice));
   BKF(cudaMemcpy(b->nodeInst, nodeInst.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
   BKF(cudaMemcpy(b->mats, hm.data(), sizeof(Material) * count, cudaMemcpyHostToDevice));
@@ -354,11 +450,10 @@ int dnl_batch_step(dnl_batch *b, int nsteps, int *active)
   dnl_handle *h = b->h;
   if (nsteps > 0) {
     const long long inc0 = b->increment;
-    if ((r = launch_dt_batch(h, b->tms, b->prm, b->count, BT_PRE))) return r;
-    for (int s = 0; s < nsteps; s++)
-      if ((r = enqueue_batch_step(b, inc0 + s + 1, s == nsteps - 1))) return r;
+    if ((r = enqueue_steps(b, inc0, nsteps))) return r;
     b->increment += nsteps;
   }
+  if ((r = barrier_status(b))) return r;
   std::vector<DevTime> t;
   if ((r = read_tms(b, t))) return r;
   int n = 0;
@@ -383,8 +478,7 @@ static int batch_graph(dnl_batch *b, int nsteps, cudaGraphExec_t *out)
     cudaGraph_t graph;
     const long long k0 = launch_counter();
     BK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    int rr = launch_dt_batch(h, b->tms, b->prm, b->count, BT_PRE);
-    for (int s = 0; s < nsteps && !rr; s++) rr = enqueue_batch_step(b, inc0 + s + 1, s == nsteps - 1);
+    int rr = enqueue_steps(b, inc0, nsteps);
     cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
     if (rr) return rr;
     if (ce != cudaSuccess) {
@@ -436,6 +530,7 @@ int dnl_batch_step_graph(dnl_batch *b, int nsteps, int *active)
     if (b->graphs[i].exec == exec) launch_counter() += b->graphs[i].kernels;
   BK(cudaGraphLaunch(exec, h->stream));
   b->increment += nsteps;
+  if ((r = barrier_status(b))) return r;
   std::vector<DevTime> t;
   if ((r = read_tms(b, t))) return r;
   int n = 0;
@@ -454,31 +549,54 @@ int dnl_batch_autotune(dnl_batch *b, int steps_per_candidate, int *block)
   if (!b->prologueDone && (r = dnl_batch_prologue(b))) return r;
   const int cands[3] = {64, 128, 256};
   double best = 1e300;
-  int bestB = b->block;
+  int bestB = b->block, bestM = b->mode;
   cudaEvent_t e0, e1;
   BK(cudaEventCreate(&e0));
   BK(cudaEventCreate(&e1));
-  for (int c = 0; c < 3; c++) {
-    b->block = cands[c];
-    BK(cudaEventRecord(e0, b->h->stream));
-    int active = 0;
-    if ((r = dnl_batch_step(b, steps_per_candidate, &active))) break;
-    BK(cudaEventRecord(e1, b->h->stream));
-    BK(cudaEventSynchronize(e1));
-    float ms = 0.f;
-    BK(cudaEventElapsedTime(&ms, e0, e1));
-    if (ms < best) {
-      best = ms;
-      bestB = cands[c];
+  r = 0;
+  for (int mode = DNL_BATCH_LAUNCHES; mode <= DNL_BATCH_PERSISTENT && !r; mode++)
+    for (int c = 0; c < 3; c++) {
+      b->mode = mode;
+      b->block = cands[c];
+      BK(cudaEventRecord(e0, b->h->stream));
+      int active = 0;
+      if ((r = dnl_batch_step(b, steps_per_candidate, &active))) break;
+      BK(cudaEventRecord(e1, b->h->stream));
+      BK(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      BK(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best) {
+        best = ms;
+        bestB = cands[c];
+        bestM = mode;
+      }
     }
-  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   b->block = bestB;
+  b->mode = bestM;
   for (int i = 0; i < b->ngraphs; i++) cudaGraphExecDestroy(b->graphs[i].exec);
   b->ngraphs = 0;
   if (block) *block = bestB;
   return r;
+}
+
+int dnl_batch_set_mode(dnl_batch *b, int mode)
+{
+  if (!b || (mode != DNL_BATCH_LAUNCHES && mode != DNL_BATCH_PERSISTENT)) return DNL_ERR_ARG;
+  if (mode == DNL_BATCH_PERSISTENT && b->h->etype != DNL_ELQUA4NAX) return DNL_ERR_ARG;
+  b->mode = mode;
+  for (int i = 0; i < b->ngraphs; i++) cudaGraphExecDestroy(b->graphs[i].exec);
+  b->ngraphs = 0;
+  return 0;
+}
+
+int dnl_batch_get_tuning(dnl_batch *b, int *mode, int *block)
+{
+  if (!b) return DNL_ERR_ARG;
+  if (mode) *mode = b->mode;
+  if (block) *block = b->block;
+  return 0;
 }
 
 int dnl_batch_reset(dnl_batch *b)
@@ -527,6 +645,47 @@ int dnl_batch_sens_run(dnl_batch *b, int nsteps, const double *dts, double *coor
   b->increment = nsteps;
   if (r) return r;
   return sens_outputs(b->h, coords, dcoords);
+}
+
+int dnl_batch_broadcast_state(dnl_batch *b, dnl_handle *src)
+{
+  if (!b || !src) return DNL_ERR_ARG;
+  dnl_handle *h = b->h;
+  if (src->etype != h->etype) return DNL_ERR_ARG;
+  for (int i = 0; i < b->count; i++)
+    if (b->nodeOff[i + 1] - b->nodeOff[i] != src->N || b->elemOff[i + 1] - b->elemOff[i] != src->E)
+      return DNL_ERR_ARG;
+  // the lumped mass is that of the initial mesh (Domain::computeMassMatrix at t = 0): form it
+  // before the coordinates are replaced
+  int r;
+  if ((r = batch_mass(b))) return r;
+  cudaStream_t s = h->stream;
+  BK(cudaStreamSynchronize(src->stream));
+  const size_t N = src->N, nIP = src->nIP, uN = h->N, unIP = h->nIP;
+  const int ncomp = 3 * etype_ns(h->etype) + 3;
+  for (int i = 0; i < b->count; i++) {
+    const size_t n0 = b->nodeOff[i], q0 = (size_t)b->elemOff[i] * h->nip;
+    for (int c = 0; c < 3; c++) {
+      BK(cudaMemcpyAsync(h->x[c] + n0, src->x[c], sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+      const double *from[4] = {src->bank[src->cur].du[c], src->bank[src->cur].v[c],
+                               src->bank[src->cur].a[c], src->bank[src->cur].disp[c]};
+      double *to[4] = {h->bank[h->cur].du[c], h->bank[h->cur].v[c], h->bank[h->cur].a[c],
+                       h->bank[h->cur].disp[c]};
+      for (int f = 0; f < 4; f++)
+        BK(cudaMemcpyAsync(to[f] + n0, from[f], sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+    }
+    for (int k = 0; k < ncomp - 1; k++)  // all but evp^n, formed below with each instance's n
+      BK(cudaMemcpyAsync(h->ip + k * unIP + q0, src->ip + k * nIP, sizeof(double) * nIP,
+                         cudaMemcpyDeviceToDevice, s));
+  }
+  k_batch_evpn<<<(unsigned)((unIP + 255) / 256), 256, 0, s>>>((long)unIP, h->nip, b->elemInst, b->mats,
+                                                             h->ip + (size_t)(ncomp - 2) * unIP,
+                                                             h->ip + (size_t)(ncomp - 1) * unIP);
+  launch_counter()++;
+  BK(cudaStreamSynchronize(s));
+  BK(cudaGetLastError());
+  (void)uN;
+  return 0;
 }
 
 int dnl_batch_set_block(dnl_batch *b, int block)

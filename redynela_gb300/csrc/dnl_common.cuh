@@ -315,6 +315,23 @@ struct SensElemArgs {
   const Material *mats;
 };
 
+// Adjoint (reverse mode) of the element pass: the pass's record and output state, the adjoints of
+// its outputs, and where the adjoints of its inputs go (dnl_adj_elem.cuh).
+struct AdjElemArgs {
+  int E, N;
+  const int *conn;        // [NEN][E]
+  const double *x[3];     // coordinates the pass read
+  const double *tape;     // [TapeLayout::NT][E*NIP], written by the tape instance of k_elem
+  const double *ipOut;    // integration-point state after the pass [IpLayout::NCOMP][E*NIP]
+  const double *fbar;     // adjoint of the assembled nodal forces, [3][N]
+  double *ipAdj;          // [TanLayout::NCOMP][E*NIP]: in, adjoint of the state after the pass;
+                          // out, of the state before it
+  double *xe, *ue;        // [DIM][E*NEN]: adjoints of the element nodes' coordinates and
+                          // Current delta_disp from this pass
+  double *gpar;           // [3][E*NIP]: d L / d(A, B, n) accumulated per integration point
+  Material mat;
+};
+
 struct GatherArgs {
   int N, EN;              // EN = E*NEN
   const int *start;       // node -> CSR offsets, N+1
@@ -342,6 +359,27 @@ struct NodeArgs {
 struct InstParams {
   double alphaM, beta, gamma, safetyOmega, Cs;
   int freq, method;
+};
+
+// One batched explicit step as a single persistent (cooperative) launch: the phases of the
+// launch sequence -- time logic, boundary conditions, element pass, nodal update, Courant
+// reduction when due, time logic -- separated by grid-wide barriers (dnl_elem.cu).
+struct BatchStepArgs {
+  ElemArgs ea;              // the union mesh; du / v of the Current bank
+  NodeArgs na;              // nodal update Current -> New (tm unused: per-instance records)
+  NodeFields cur;           // Current bank, for the boundary-condition writes
+  const int *elemInst, *nodeInst;
+  const Material *mats;
+  const InstParams *prm;
+  DevTime *tms;
+  int count;
+  int nbc;                  // boundary-condition nodes
+  const int *bcNodes;
+  int preFirst;             // 1: the time logic's initStep (DT_PRE) opens the step
+  int courant;              // 1: the Courant lengths are due after the nodal update
+  int postMode;             // DT_POST, or DT_POST | DT_PRE when another step follows
+  unsigned *bar;            // barrier: arrival count, generation
+  int *err;                 // 1 when a barrier wait ran out (DNL_ERR_TIMEOUT)
 };
 
 // ------------------------------------------------------------------------ handle
@@ -412,6 +450,8 @@ struct dnl_handle {
   // forward-mode sensitivities (dnl_sens.cu)
   double v0dir[3];            // unit vector of the initial velocity
   void *sens;
+  // reverse-mode adjoint: checkpoints, step records and adjoint state (dnl_adjoint.cu)
+  void *adj;
 };
 
 // 1/x by the Newton-Raphson iteration for the reciprocal (the root of f(r) = 1/r - x: r <- r (2 - x r),
@@ -480,6 +520,13 @@ struct SensBatch {
   const double *v0dir;  // [count][3]
 };
 int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt);
+// reverse mode (dnl_adjoint.cu, dnl_adj_elem.cuh)
+int launch_elem_adj(int etype, const AdjElemArgs &a, cudaStream_t s);
+int launch_elem_tape_raw(int etype, const ElemArgs &a, cudaStream_t s);
+void adj_free(dnl_handle *h);
+int adjoint_forward(dnl_handle *h, const double *dts, int nsteps, int stride);
+int adjoint_backward(dnl_handle *h, const double *dL_dx, double *grad, dnl_adjoint_info *info);
+int sens_schedule(dnl_handle *h, const double **dts, int *n);
 int sens_outputs(dnl_handle *h, double *coords, double *dcoords);
 void sens_free(dnl_handle *h);
 // primal per-step launches (dnl_host.cu) used by the sensitivity run
@@ -503,6 +550,8 @@ int launch_mass_batch(int etype, const ElemArgs &a, double *me, const int *elemI
                       const Material *mats, cudaStream_t s);
 int launch_courant_batch(int etype, const ElemArgs &a, const int *elemInst, DevTime *tms,
                          cudaStream_t s);
+// one batched step as a persistent cooperative launch (ElQua4nAx); grid from the occupancy
+int launch_batch_persistent(int etype, int block, const BatchStepArgs &a, cudaStream_t s);
 ElemArgs elem_args_of(dnl_handle *h);
 int launch_node_batch(dnl_handle *h, const int *nodeInst, const InstParams *prm, DevTime *tms);
 int launch_dt_batch(dnl_handle *h, DevTime *tms, const InstParams *prm, int count, int mode);

@@ -29,6 +29,7 @@
 #include <cstring>
 
 #include "dnl_common.cuh"
+#include "dnl_node.cuh"
 
 namespace dnl {
 
@@ -1041,6 +1042,9 @@ __global__ void __launch_bounds__(BLOCK) k_elem_batch(ElemArgs a, const int *ele
 // ----------------------------------------------------------------------------- tangent pass
 #include "dnl_sens_elem.cuh"
 
+// ----------------------------------------------------------------------------- adjoint pass
+#include "dnl_adj_elem.cuh"
+
 // ----------------------------------------------------------------------------- mass kernel
 // Element::computeMassMatrix with the reference's rounding: M_k = sum_pt (rho N_k) W,
 // W = weight detJ (2 pi R).  Writes me[e*NEN + k]; Domain::computeMassMatrix's assembly is the
@@ -1238,6 +1242,168 @@ __global__ void __launch_bounds__(256) k_courant_batch(ElemArgs a, const int *el
   } else if (len < 1e300) {
     atomicMin(&tm->lenMinBits, (unsigned long long)__double_as_longlong(len));
   }
+}
+
+// ----------------------------------------------------------------------------- persistent batch step
+// Grid-wide barrier of a cooperative launch (every block resident): thread 0 of each block arrives
+// on a counter; the last arrival resets it and advances the generation the others wait on.  The
+// wait is bounded: past kBarrierSpins polls it sets *err and gives up, and every block leaves the
+// kernel at its next barrier.  Fences order each phase's global writes before the next phase.
+constexpr long long kBarrierSpins = 1ll << 25;
+
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err)
+{
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *gen = bar + 1;
+    const unsigned g = *gen;
+    __threadfence();
+    if (atomicAdd(bar, 1u) + 1u == gridDim.x) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      long long spins = 0;
+      while (*gen == g) {
+        if (++spins > kBarrierSpins) {
+          atomicExch(err, 1);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *(volatile int *)err == 0;
+}
+
+template <int ET, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_batch_persistent(BatchStepArgs a)
+{
+  constexpr int NIP = Elem<ET>::NIP, NEN = Elem<ET>::NEN, DIM = Elem<ET>::DIM;
+  constexpr int EPW = 32 / NIP;
+  __shared__ double red[BLOCK / 32][EPW][NIP * NEN * DIM];
+  const int tid = blockIdx.x * BLOCK + threadIdx.x, nthreads = gridDim.x * BLOCK;
+  // ---- time logic: initStep of every unfinished instance
+  if (a.preFirst) {
+    for (int i = tid; i < a.count; i += nthreads) {
+      const InstParams &p = a.prm[i];
+      dt_update(a.tms + i, DT_PRE, p.freq, p.method, p.safetyOmega, p.Cs);
+    }
+    if (!grid_barrier(a.bar, a.err)) return;
+  }
+  // ---- constant boundary conditions on the Current field (k_bc_current)
+  for (int i = tid; i < a.nbc; i += nthreads) {
+    const int n = a.bcNodes[i];
+    const DevTime *tm = a.tms + a.nodeInst[n];
+    if (tm->done | tm->status) continue;
+    const double dt = tm->timeStep;
+    const int cd = a.na.bcCode[i];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const int act = (cd >> (2 * c)) & 3;
+      if (act == 1) {
+        a.cur.du[c][n] = 0.;
+        a.cur.v[c][n] = 0.;
+        a.cur.a[c][n] = 0.;
+      } else if (act == 2) {
+        const double sp = a.na.bcSpeed[3 * i + c];
+        a.cur.a[c][n] = 0.;
+        a.cur.v[c][n] = sp;
+        a.cur.du[c][n] = __dmul_rn(sp, dt);
+      }
+    }
+  }
+  if (!grid_barrier(a.bar, a.err)) return;
+  // ---- element pass: warp-aligned tiles of Gauss points, grid-stride (as k_elem_batch)
+  {
+    const long total = ((long)a.ea.E * NIP + 31) & ~31L;
+    const int lane = threadIdx.x & 31;
+    for (long base = (long)blockIdx.x * BLOCK; base < total; base += (long)gridDim.x * BLOCK) {
+      const long gtid = base + threadIdx.x;
+      if ((gtid & ~31L) / NIP >= a.ea.E) continue;  // the whole warp
+      const int eRaw = (int)(gtid / NIP);
+      const int e = eRaw < a.ea.E ? eRaw : a.ea.E - 1;
+      const int inst = a.elemInst[e];
+      DevTime *tm = a.tms + inst;
+      const bool valid = eRaw < a.ea.E && !(tm->done | tm->status);
+      elem_ip<ET>(a.ea, a.mats[inst], tm, e, (int)(gtid % NIP), valid, lane,
+                  red[threadIdx.x >> 5][lane / NIP]);
+      __syncwarp();
+    }
+  }
+  if (!grid_barrier(a.bar, a.err)) return;
+  // ---- assembly + nodal update (k_node_batch)
+  for (int n = tid; n < a.na.N; n += nthreads) {
+    const int i = a.nodeInst[n];
+    const DevTime *tm = a.tms + i;
+    if (tm->done | tm->status) continue;
+    node_update<DIM>(a.na, n, tm->timeStep, a.prm[i].alphaM, a.prm[i].beta, a.prm[i].gamma);
+  }
+  if (!grid_barrier(a.bar, a.err)) return;
+  // ---- Courant lengths of the updated mesh into each instance's minimum (k_courant_batch)
+  if (a.courant) {
+    for (int base = blockIdx.x * BLOCK; base < ((a.ea.E + 31) & ~31); base += gridDim.x * BLOCK) {
+      const int eRaw = base + threadIdx.x;
+      if ((eRaw & ~31) >= a.ea.E) continue;
+      const int e = eRaw < a.ea.E ? eRaw : a.ea.E - 1;
+      const int inst = a.elemInst[e];
+      DevTime *tm = a.tms + inst;
+      double len = 1e300;
+      if (eRaw < a.ea.E && !(tm->done | tm->status)) {
+        len = elem_length<etype_length_kind(ET)>(a.ea, e);
+        if (!(len > 0.)) {
+          record_error(tm, DNL_ERR_DT, e);
+          len = 1e300;
+        }
+      }
+      const int first = __shfl_sync(0xffffffffu, inst, 0);
+      if (__all_sync(0xffffffffu, inst == first)) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) len = fmin(len, __shfl_xor_sync(0xffffffffu, len, o));
+        if ((threadIdx.x & 31) == 0 && len < 1e300)
+          atomicMin(&tm->lenMinBits, (unsigned long long)__double_as_longlong(len));
+      } else if (len < 1e300) {
+        atomicMin(&tm->lenMinBits, (unsigned long long)__double_as_longlong(len));
+      }
+    }
+    if (!grid_barrier(a.bar, a.err)) return;
+  }
+  // ---- time logic: updateTime, the time step (recomputed when due), initStep of the next step
+  for (int i = tid; i < a.count; i += nthreads) {
+    const InstParams &p = a.prm[i];
+    dt_update(a.tms + i, a.postMode, p.freq, p.method, p.safetyOmega, p.Cs);
+  }
+}
+
+int launch_batch_persistent(int etype, int block, const BatchStepArgs &a, cudaStream_t s)
+{
+  if (etype != DNL_ELQUA4NAX) return DNL_ERR_ARG;  // the batched stepping's element type
+  void *fn;
+  if (block == 64)
+    fn = (void *)k_batch_persistent<DNL_ELQUA4NAX, 64>;
+  else if (block == 256)
+    fn = (void *)k_batch_persistent<DNL_ELQUA4NAX, 256>;
+  else {
+    block = 128;
+    fn = (void *)k_batch_persistent<DNL_ELQUA4NAX, 128>;
+  }
+  int dev = 0, sms = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return DNL_ERR_CUDA;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return DNL_ERR_CUDA;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, 0) != cudaSuccess || per < 1)
+    return DNL_ERR_CUDA;
+  // no more blocks than the element pass has tiles
+  const long tiles = ((long)a.ea.E * etype_nip(etype) + block - 1) / block;
+  int grid = sms * per;
+  if (grid > tiles) grid = (int)tiles;
+  if (grid < 1) grid = 1;
+  BatchStepArgs args = a;
+  void *params[] = {&args};
+  const cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(block), params, 0, s);
+  launch_counter()++;
+  return e == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
 
 // ----------------------------------------------------------------------------- launchers

@@ -23,6 +23,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include "dnl_common.cuh"
+#include "dnl_node.cuh"
 
 using namespace dnl;
 
@@ -62,96 +63,7 @@ __global__ void __launch_bounds__(256) k_gather1(int N, const int *start, const 
   out[n] = s;
 }
 
-// ----------------------------------------------------------------------------- nodal update
-__device__ __forceinline__ void apply_bc(int code, const double *spd, double dt, double cdu[3],
-                                         double ndu[3], double cv[3], double nv[3], double ca[3],
-                                         double na[3])
-{
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    const int act = (code >> (2 * i)) & 3;
-    if (act == 1) {
-      cdu[i] = ndu[i] = cv[i] = nv[i] = ca[i] = na[i] = 0.;
-    } else if (act == 2) {
-      ca[i] = na[i] = 0.;
-      cv[i] = nv[i] = spd[i];
-      cdu[i] = RMUL(cv[i], dt);
-      ndu[i] = RMUL(nv[i], dt);
-    }
-  }
-}
-
-// one node of the Chung-Hulbert update; dt and the integration constants of its mesh.  In 2D the
-// third components of the nodal fields stay 0 (nothing writes them), so only DIM are read and
-// written.  The two divisions of the corrector, F/M and (. - alphaM a)/(1 - alphaM), go through
-// a reciprocal and one residual correction (quot): the FP64 pipe bounds this kernel too.
-template <int DIM>
-__device__ __forceinline__ void node_update(const NodeArgs &g, int n, double dt, double alphaM,
-                                            double beta, double gamma)
-{
-  double cdu[3] = {0., 0., 0.}, cv[3] = {0., 0., 0.}, ca[3] = {0., 0., 0.}, cd[3] = {0., 0., 0.};
-  double ndu[3] = {0., 0., 0.}, nv[3] = {0., 0., 0.}, na[3] = {0., 0., 0.}, nd[3] = {0., 0., 0.};
-#pragma unroll
-  for (int i = 0; i < DIM; i++) {
-    cdu[i] = g.cur.du[i][n];
-    cv[i] = g.cur.v[i][n];
-    ca[i] = g.cur.a[i][n];
-    cd[i] = g.cur.disp[i][n];
-  }
-  // computePredictions
-  const double c1 = RMUL(dt, RSUB(0.5, beta)), c2 = RMUL(dt, RSUB(1., gamma));
-#pragma unroll
-  for (int i = 0; i < DIM; i++) {
-    ndu[i] = RMUL(RADD(RMUL(ca[i], c1), cv[i]), dt);
-    nd[i] = RADD(cd[i], ndu[i]);
-    nv[i] = RADD(RMUL(ca[i], c2), cv[i]);
-    na[i] = 0.0;
-  }
-  const int bc = g.bcIdx[n];
-  int code = 0;
-  const double *spd = nullptr;
-  if (bc >= 0) {
-    code = g.bcCode[bc];
-    spd = g.bcSpeed + 3 * bc;
-    apply_bc(code, spd, dt, cdu, ndu, cv, nv, ca, na);
-  }
-  // assembled internal forces of this node
-  double f[DIM];
-#pragma unroll
-  for (int c = 0; c < DIM; c++) f[c] = 0.0;
-  for (int q = g.start[n]; q < g.start[n + 1]; q++) {
-    const int ent = __ldg(g.entry + q);
-#pragma unroll
-    for (int c = 0; c < DIM; c++) f[c] = RADD(f[c], __ldg(g.fe + (long)c * g.EN + ent));
-  }
-  if (g.fint) {
-#pragma unroll
-    for (int c = 0; c < DIM; c++) g.fint[(long)n * DIM + c] = f[c];
-  }
-  // explicitSolve
-  const double m = g.mass[n], rm = nr_rcp(m);
-#pragma unroll
-  for (int c = 0; c < DIM; c++) na[c] = quot(f[c], m, rm);
-  const double cg = RMUL(dt, gamma), cb = RMUL(RMUL(dt, dt), beta);
-  const double oma = RSUB(1.0, alphaM), roma = nr_rcp(oma);
-#pragma unroll
-  for (int i = 0; i < DIM; i++) {
-    na[i] = RSUB(na[i], RMUL(alphaM, ca[i]));
-    na[i] = quot(na[i], oma, roma);
-    nv[i] = RADD(nv[i], RMUL(cg, na[i]));
-    ndu[i] = RADD(ndu[i], RMUL(cb, na[i]));
-  }
-  if (bc >= 0) apply_bc(code, spd, dt, cdu, ndu, cv, nv, ca, na);
-#pragma unroll
-  for (int i = 0; i < DIM; i++) {
-    nd[i] = RADD(cd[i], ndu[i]);
-    g.nxt.du[i][n] = ndu[i];
-    g.nxt.v[i][n] = nv[i];
-    g.nxt.a[i][n] = na[i];
-    g.nxt.disp[i][n] = nd[i];
-    g.x[i][n] = RADD(g.x[i][n], ndu[i]);
-  }
-}
+// nodal update (node_update, apply_bc) and time-step logic (dt_update): dnl_node.cuh
 
 template <int DIM>
 __global__ void __launch_bounds__(256) k_node(NodeArgs g)
@@ -205,66 +117,11 @@ __global__ void k_bc_current(int nb, const int *nodes, const int *code, const do
 }
 
 // ----------------------------------------------------------------------------- time step
-enum { DT_FORCE = 1, DT_POST = 2, DT_PRE = 4 };
-
 struct DtArgs {
   DevTime *tm;
   int mode, freq, method;
   double safetyOmega, Cs;
 };
-
-__device__ __forceinline__ bool in_bounds(const DevTime *tm)
-{
-  const double up = tm->endTime < tm->upTime ? tm->endTime : tm->upTime;
-  return tm->currentTime >= tm->startTime && tm->currentTime < up;
-}
-
-__device__ void recompute_dt(DevTime *tm, int method, double safetyOmega, double Cs)
-{
-  double fmax;
-  if (method == DNL_COURANT) {
-    const double crit = __longlong_as_double((long long)tm->lenMinBits) / Cs;
-    fmax = 2.0 / crit;
-    tm->lenMinBits = 0x7ff0000000000000ull;  // +inf for the next reduction
-  } else {
-    fmax = tm->fmax;
-  }
-  tm->timeStep = safetyOmega / fmax;
-  tm->lastTsDate = tm->tsDate;
-  tm->lastTimeStep = tm->computedTimeStep;
-  tm->tsDate = tm->currentTime;
-  tm->computedTimeStep = tm->timeStep;
-}
-
-__device__ void dt_update(DevTime *tm, int mode, int freq, int method, double safetyOmega, double Cs)
-{
-  if (tm->status) return;
-  if (mode & DT_FORCE) recompute_dt(tm, method, safetyOmega, Cs);
-  if ((mode & DT_POST) && !tm->done) {
-    tm->currentTime = RADD(tm->currentTime, tm->timeStep);  // ExplicitSolverCH::updateTime
-    if (!in_bounds(tm)) {
-      tm->done = 1;
-    } else if (tm->increment % freq == 0) {
-      recompute_dt(tm, method, safetyOmega, Cs);
-    } else if (tm->tsDate != tm->lastTsDate) {  // LINEARdbl extrapolation (Math.h:91)
-      const double dx = RSUB(tm->currentTime, tm->lastTsDate) / RSUB(tm->tsDate, tm->lastTsDate);
-      tm->timeStep = RADD(RMUL(dx, tm->computedTimeStep), RMUL(RSUB(1.0, dx), tm->lastTimeStep));
-    }
-  }
-  if ((mode & DT_PRE) && !tm->done) {
-    if (!in_bounds(tm)) {
-      tm->done = 1;
-    } else {
-      if (RADD(tm->currentTime, tm->timeStep) > tm->upTime) tm->timeStep = RSUB(tm->upTime, tm->currentTime);
-      tm->nextTime = RADD(tm->currentTime, tm->timeStep);
-      tm->increment++;
-    }
-  }
-  if (!tm->done && !(tm->timeStep > 0. && tm->timeStep < 1e300)) {
-    tm->status = DNL_ERR_DT;
-    tm->badElem = -1;
-  }
-}
 
 __global__ void k_dt(DtArgs a)
 {
@@ -817,6 +674,7 @@ int dnl_destroy(dnl_handle *h)
 {
   if (!h) return DNL_ERR_ARG;
   dnl::sens_free(h);
+  dnl::adj_free(h);
   for (int i = 0; i < h->ngraphs; i++) cudaGraphExecDestroy(h->graphs[i].exec);
   void *ptrs[] = {h->conn, h->x[0], h->n2eStart, h->n2e, h->mass, h->fieldMem, h->ip, h->detJ,
                   h->stepT, h->fe, h->fint, h->stage, h->bcIdx, h->bcCode, h->bcNodeList, h->bcSpeed,

@@ -1,4 +1,4 @@
-// Forward-mode sensitivities of an explicit run (dnl_sens_run, dnl_adjoint).
+// Forward-mode sensitivities of an explicit run (dnl_sens_run, dnl_batch_sens_run).
 //
 // The run advances the primal state exactly as dnl_step does (boundary conditions, element pass,
 // nodal Chung-Hulbert update of ExplicitSolverCH.C:387-567), except that the step sizes come from
@@ -6,8 +6,9 @@
 // per-integration-point record.  After each primal launch a tangent launch carries the derivative
 // of the state with respect to the four parameters (A, B, n of IsoHardElastoplastic and the
 // initial-velocity magnitude |v0|) -- four tangent copies of every nodal field and
-// integration-point variable.  Four parameters make the forward mode cheaper than a reverse
-// (adjoint) sweep: no trajectory is stored or recomputed, so no checkpoints are needed.
+// integration-point variable.  It stores no trajectory: the derivatives of every final coordinate
+// come out of one run, where the reverse sweep of dnl_adjoint (dnl_adjoint.cu) gives one loss's
+// gradient from checkpoints and recomputation.
 #include <cstddef>
 #include <cmath>
 #include <cstdio>
@@ -455,6 +456,20 @@ int sens_outputs(dnl_handle *h, double *coords, double *dcoords)
   return 0;
 }
 
+// the schedule dnl_set_dt_schedule stored (nullptr / 0 when none)
+int sens_schedule(dnl_handle *h, const double **dts, int *n)
+{
+  SensState *S = (SensState *)h->sens;
+  if (!S || S->schedule.empty()) {
+    *dts = nullptr;
+    *n = 0;
+    return DNL_ERR_ARG;
+  }
+  *dts = S->schedule.data();
+  *n = (int)S->schedule.size();
+  return 0;
+}
+
 void sens_free(dnl_handle *h)
 {
   SensState *S = (SensState *)h->sens;
@@ -490,23 +505,6 @@ int dnl_sens_run(dnl_handle *h, int nsteps, const double *dts, double *coords, d
   if (!h->prologueDone && (r = dnl_prologue(h))) return r;
   if ((r = sens_run(h, nsteps, dts, nullptr))) return r;
   return sens_outputs(h, coords, dcoords);
-}
-
-int dnl_adjoint(dnl_handle *h, const double *dL_dx, double *grad, int ckpt_stride)
-{
-  if (!h || !dL_dx || !grad || ckpt_stride < 0 || !h->sens) return DNL_ERR_ARG;
-  SensState *S = (SensState *)h->sens;
-  if (S->schedule.empty()) return DNL_ERR_ARG;
-  const long n3 = 3L * h->N;
-  std::vector<double> dx((size_t)kSensParams * n3);
-  int r = dnl_sens_run(h, (int)S->schedule.size(), S->schedule.data(), nullptr, dx.data());
-  if (r) return r;
-  for (int p = 0; p < kSensParams; p++) {
-    double s = 0.;
-    for (long i = 0; i < n3; i++) s += dL_dx[i] * dx[(size_t)p * n3 + i];
-    grad[p] = s;
-  }
-  return 0;
 }
 
 }  // extern "C"

@@ -77,6 +77,12 @@ class StateView(C.Structure):
                                    "evp", "Sig", "mass")]
 
 
+class AdjointInfo(C.Structure):
+    _fields_ = [("nsteps", C.c_int), ("stride", C.c_int), ("checkpoints", C.c_int),
+                ("recomputed_steps", C.c_longlong), ("bytes", C.c_longlong),
+                ("checkpoint_bytes", C.c_longlong), ("record_bytes", C.c_longlong)]
+
+
 class TimeInfo(C.Structure):
     _fields_ = [("time", C.c_double), ("time_step", C.c_double), ("computed_step", C.c_double),
                 ("kinetic", C.c_double), ("increment", C.c_longlong), ("done", C.c_int),
@@ -130,6 +136,9 @@ def lib():
         L.dnl_batch_destroy.argtypes = [H]
         L.dnl_batch_prologue.argtypes = [H]
         L.dnl_batch_step.argtypes = [H, C.c_int, _ip]
+        L.dnl_batch_broadcast_state.argtypes = [H, H]
+        L.dnl_batch_set_mode.argtypes = [H, C.c_int]
+        L.dnl_batch_get_tuning.argtypes = [H, _ip, _ip]
         L.dnl_batch_step_graph.argtypes = [H, C.c_int, _ip]
         L.dnl_batch_graph_capture.argtypes = [H, C.c_int]
         L.dnl_batch_autotune.argtypes = [H, C.c_int, _ip]
@@ -142,6 +151,10 @@ def lib():
         L.dnl_sens_run.argtypes = [H, C.c_int, _dp, _dp, _dp]
         L.dnl_set_dt_schedule.argtypes = [H, _dp, C.c_int]
         L.dnl_adjoint.argtypes = [H, _dp, _dp, C.c_int]
+        L.dnl_adjoint_stats.argtypes = [H, C.POINTER(AdjointInfo)]
+        L.dnl_adjoint_forward.argtypes = [H, C.c_int, _dp]
+        L.dnl_adjoint_backward.argtypes = [H, _dp, _dp]
+        L.dnl_run_schedule.argtypes = [H, C.c_int, _dp, _dp]
         L.dnl_reset.argtypes = [H, C.POINTER(MaterialDesc), _dp]
         L.dnl_set_materials.argtypes = [H, C.c_int, C.POINTER(MaterialLawDesc), _ip]
         L.dnl_write_results.argtypes = [H, C.c_char_p]
@@ -440,7 +453,9 @@ class GpuDomain:
         return x, dx
 
     def adjoint(self, dL_dx, dts, ckpt_stride: int = 0) -> np.ndarray:
-        """dnl_set_dt_schedule + dnl_adjoint: gradient of L(x_final) given dL/dx_final (N, 3)."""
+        """dnl_set_dt_schedule + dnl_adjoint: the reverse-mode gradient of L(x_final) with respect to
+        SENS_PARAMS given dL/dx_final (N, 3), from the handle's initial state, checkpoints every
+        ``ckpt_stride`` steps (0: ceil(sqrt(steps))).  The handle is at its initial state after."""
         dts = np.ascontiguousarray(dts, dtype=np.float64)
         g = np.ascontiguousarray(dL_dx, dtype=np.float64)
         assert g.size == 3 * self.model.N
@@ -448,6 +463,38 @@ class GpuDomain:
         grad = np.zeros(SENS_NPARAM)
         self._check_run(self.L.dnl_adjoint(self.h, _ptr(g), _ptr(grad), int(ckpt_stride)))
         return grad
+
+    def adjoint_forward(self, dts, ckpt_stride: int = 0) -> np.ndarray:
+        """dnl_set_dt_schedule + dnl_adjoint_forward: the scheduled run from the initial state with
+        its checkpoints; returns the final coordinates (N, 3)."""
+        dts = np.ascontiguousarray(dts, dtype=np.float64)
+        self._check(self.L.dnl_set_dt_schedule(self.h, _ptr(dts), len(dts)))
+        x = np.zeros((self.model.N, 3))
+        self._check_run(self.L.dnl_adjoint_forward(self.h, int(ckpt_stride), _ptr(x)))
+        return x
+
+    def adjoint_backward(self, dL_dx) -> np.ndarray:
+        """dnl_adjoint_backward: the reverse sweep over the last forward sweep's checkpoints."""
+        g = np.ascontiguousarray(dL_dx, dtype=np.float64)
+        assert g.size == 3 * self.model.N
+        grad = np.zeros(SENS_NPARAM)
+        self._check_run(self.L.dnl_adjoint_backward(self.h, _ptr(g), _ptr(grad)))
+        return grad
+
+    def adjoint_stats(self) -> dict:
+        """dnl_adjoint_stats: checkpoints, stride, recomputed steps and device bytes of the last
+        adjoint."""
+        info = AdjointInfo()
+        self._check(self.L.dnl_adjoint_stats(self.h, C.byref(info)))
+        return {k: getattr(info, k) for k, _ in AdjointInfo._fields_}
+
+    def run_schedule(self, dts) -> np.ndarray:
+        """dnl_run_schedule: the run with step sizes ``dts`` from the initial state, no derivatives;
+        returns the final coordinates (N, 3)."""
+        dts = np.ascontiguousarray(dts, dtype=np.float64)
+        x = np.zeros((self.model.N, 3))
+        self._check_run(self.L.dnl_run_schedule(self.h, len(dts), _ptr(dts), _ptr(x)))
+        return x
 
 
 def parse_results(path: str, num_nodes: int, num_points: int) -> Dict[str, np.ndarray]:
@@ -475,6 +522,9 @@ def parse_results(path: str, num_nodes: int, num_points: int) -> Dict[str, np.nd
     return out
 
 
+BATCH_LAUNCHES = 0
+BATCH_PERSISTENT = 1
+
 SENS_NPARAM = 4
 SENS_PARAMS = ("A", "B", "n", "v0")
 
@@ -488,12 +538,15 @@ def model_with_params(model: Model, A: float, B: float, n: float, v0: float) -> 
                                v0=tuple(u / nu * float(v0)) if nu > 0 else tuple(u))
 
 
-def taylor_autograd():
+def taylor_autograd(mode: str = "reverse", ckpt_stride: int = 0):
     """torch.autograd.Function over the GPU run: forward(params, model, dts) -> final coordinates.
 
-    ``params`` is a float64 tensor (A, B, n, |v0|); the forward pass runs dnl_sens_run, which
-    returns the final coordinates and their derivatives, and the backward pass contracts the
-    incoming gradient with those derivatives (forward-mode Jacobian, reverse-mode interface)."""
+    ``params`` is a float64 tensor (A, B, n, |v0|).  mode "reverse": the forward pass runs the
+    scheduled run with its checkpoints (dnl_adjoint_forward, ``ckpt_stride`` steps per checkpoint,
+    0: ceil(sqrt(steps))) and the backward pass the reverse sweep over them
+    (dnl_adjoint_backward) with the incoming gradient as dL/dx_final.  mode "forward": the forward pass runs dnl_sens_run, which returns the
+    final coordinates and their derivatives, and the backward pass contracts the incoming gradient
+    with those (forward-mode Jacobian)."""
     import torch
 
     class TaylorRun(torch.autograd.Function):
@@ -501,18 +554,29 @@ def taylor_autograd():
         def forward(ctx, params, model, dts):
             A, B, n, v0 = (float(v) for v in params.detach().cpu().tolist())
             d = GpuDomain(model_with_params(model, A, B, n, v0))
-            try:
-                x, dx = d.sensitivities(dts)
-            finally:
-                d.close()
-            ctx.dx = torch.from_numpy(dx).to(params.device)
+            if mode == "forward":
+                try:
+                    x, dx = d.sensitivities(dts)
+                finally:
+                    d.close()
+                ctx.dx = torch.from_numpy(dx).to(params.device)
+            else:
+                x = d.adjoint_forward(dts, ckpt_stride)
+                ctx.domain = d
             return torch.from_numpy(x).to(params.device)
 
         @staticmethod
         def backward(ctx, grad_x):
-            dx = ctx.dx
-            g = (dx * grad_x.to(dx.dtype).unsqueeze(0)).sum(dim=(1, 2))
-            return g, None, None
+            if mode == "forward":
+                dx = ctx.dx
+                g = (dx * grad_x.to(dx.dtype).unsqueeze(0)).sum(dim=(1, 2))
+                return g, None, None
+            d = ctx.domain
+            try:
+                g = d.adjoint_backward(grad_x.detach().to(torch.float64).cpu().numpy())
+            finally:
+                d.close()
+            return torch.from_numpy(g).to(grad_x.device), None, None
 
     return TaylorRun
 
@@ -609,6 +673,17 @@ class BatchDomain:
     def set_block(self, block: int):
         self._check(self.L.dnl_batch_set_block(self.h, int(block)))
 
+    def set_mode(self, mode: int):
+        """dnl_batch_set_mode: BATCH_LAUNCHES (a launch sequence per step) or BATCH_PERSISTENT
+        (one persistent cooperative kernel per step)."""
+        self._check(self.L.dnl_batch_set_mode(self.h, int(mode)))
+
+    def tuning(self):
+        """dnl_batch_get_tuning: (mode, block) in use."""
+        mo, bl = C.c_int(0), C.c_int(0)
+        self._check(self.L.dnl_batch_get_tuning(self.h, C.byref(mo), C.byref(bl)))
+        return mo.value, bl.value
+
     def time_info(self, i: int) -> dict:
         t = TimeInfo()
         self._check(self.L.dnl_batch_time_info(self.h, int(i), C.byref(t)))
@@ -627,6 +702,11 @@ class BatchDomain:
     def reset(self) -> None:
         """dnl_batch_reset: every instance back to its initial state."""
         self._check(self.L.dnl_batch_reset(self.h))
+
+    def broadcast_state(self, domain: "GpuDomain") -> None:
+        """dnl_batch_broadcast_state: the state of a single-mesh handle (same mesh as every
+        instance) copied into every instance."""
+        self._check(self.L.dnl_batch_broadcast_state(self.h, domain.h))
 
     def sensitivities(self, dts, outputs: bool = True):
         """dnl_batch_sens_run: every instance with step sizes ``dts``; returns, per instance, the

@@ -36,20 +36,45 @@ def test_batch_graph_and_autotune_keep_results(gpu_lib):
     a = gpu_lib.BatchDomain(models)
     a.step(60)
     b = gpu_lib.BatchDomain(models)
-    blk = b.autotune(steps=10)  # 3 candidates x 10 live steps = 30 steps
+    blk = b.autotune(steps=5)  # 2 modes x 3 block sizes x 5 live steps = 30 steps
     assert blk in (64, 128, 256)
+    assert b.tuning() in {(mode, blk) for mode in (gpu_lib.BATCH_LAUNCHES, gpu_lib.BATCH_PERSISTENT)}
     for _ in range(3):
         b.step_graph(10)
     for i in range(len(models)):
         assert np.array_equal(a.coords(i), b.coords(i)), i
 
 
-def test_batch_runs_each_instance_to_its_end(gpu_lib):
+def test_persistent_step_matches_launch_sequence(gpu_lib):
+    """One persistent cooperative kernel per step (grid barriers between the phases) gives the
+    launch sequence's results bit for bit, stream-launched and graph-replayed, with every block
+    size; so it also equals each bar run alone."""
+    models = _models()
+    ref = gpu_lib.BatchDomain(models)
+    ref.step(70)
+    for block in (64, 128, 256):
+        b = gpu_lib.BatchDomain(models)
+        b.set_mode(gpu_lib.BATCH_PERSISTENT)
+        b.set_block(block)
+        assert b.tuning() == (gpu_lib.BATCH_PERSISTENT, block)
+        b.step(30)
+        b.step_graph(20)
+        b.step_graph(20)
+        for i in range(len(models)):
+            assert np.array_equal(ref.coords(i), b.coords(i)), (block, i)
+            assert np.array_equal(ref.fint(i), b.fint(i)), (block, i)
+            assert ref.time_info(i)["time"] == b.time_info(i)["time"], (block, i)
+        b.close()
+
+
+@pytest.mark.parametrize("mode", ["launches", "persistent"])
+def test_batch_runs_each_instance_to_its_end(gpu_lib, mode):
     """Two small bars with different end times: each stops at its own end time; final positions
     vs the oracle within the full-run tolerance."""
     m1 = meshes.taylor_axi(4, 40, tend=6e-6)
     m2 = meshes.taylor_axi(5, 50, speed=200.0, tend=9e-6)
     b = gpu_lib.BatchDomain([m1, m2])
+    b.set_mode(gpu_lib.BATCH_PERSISTENT if mode == "persistent" else gpu_lib.BATCH_LAUNCHES)
     active = 2
     while active:
         active = b.step(200)
