@@ -450,6 +450,8 @@ def batch_line(args) -> dict:
     b = dynela.BatchDomain(models)
     b.prologue()
     block = b.autotune(steps=3)
+    mode = ("persistent kernel per step" if b.tuning()[0] == dynela.BATCH_PERSISTENT
+            else "launch sequence per step")
     b.step_graph(args.steps)  # capture + warm-up
     for _ in range(max(0, args.warmup - 1)):
         b.step_graph(args.steps)
@@ -487,7 +489,8 @@ def batch_line(args) -> dict:
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, numpy default_rng(0))",
             "config": {"workload": f"taylor_axi_batch_{args.instances}", "elements": E,
-                       "instances": args.instances, "block": block, "active_after": active,
+                       "instances": args.instances, "block": block, "mode": mode,
+                       "active_after": active,
                        "l2": "inputs larger than L2 (integration-point state "
                              f"{E * 4 * 15 * 8 / 1e6:.0f} MB)"},
             "plain_instance_by_instance": {"value": max(plain, plain_graph),

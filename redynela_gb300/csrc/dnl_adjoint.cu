@@ -27,6 +27,7 @@
 // run as computed at the converged return-mapping multipliers and computed eigenpairs, the same
 // linearisation as the forward-mode tangent (dnl_sens_run), so the two agree to rounding.
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -65,7 +66,22 @@ struct AdjState {
   int runCap = 0, runN = 0;
   std::vector<double> sched;    // the schedule of the last forward sweep (host)
   bool ready = false;           // a forward sweep's checkpoints await the reverse sweep
+  // segments replayed from captured graphs: kind (0 forward, 1 recomputation with records,
+  // 2 reverse), length, the handle's bank parity and the adjoint bank at the segment's start
+  struct SegGraph {
+    int kind, len, cur, nw;
+    cudaGraphExec_t exec;
+    long long kernels;
+  };
+  std::vector<SegGraph> graphs;
+  Material graphMat;            // the material the graphs hold by value
 };
+
+void adj_drop_graphs(AdjState *A)
+{
+  for (auto &g : A->graphs) cudaGraphExecDestroy(g.exec);
+  A->graphs.clear();
+}
 
 __global__ void k_adj_dt(DevTime *tm, const double *dts, int phase)
 {
@@ -88,7 +104,9 @@ struct AdjNodeArgs {
   double *lc;        // adjoints of the Current field before it (v, a, disp written here)
   const double *xbar;
   double *fbar;
-  double dt, alphaM, beta, gamma;
+  const double *dts; // the schedule; the step undone is the time record's increment - 1
+  const DevTime *tm;
+  double alphaM, beta, gamma;
 };
 
 // Adjoint of node_update (dnl_host.cu) for one node.  Per free component, with
@@ -107,9 +125,10 @@ __global__ void __launch_bounds__(256) k_node_adj(AdjNodeArgs g)
   const long N = g.N;
   const int bc = g.bcIdx[n];
   const int code = bc >= 0 ? g.bcCode[bc] : 0;
+  const double dt = g.dts[g.tm->increment - 1];
   const double rm = 1.0 / g.mass[n], roma = 1.0 / (1.0 - g.alphaM);
-  const double c1 = g.dt * (0.5 - g.beta), c2 = g.dt * (1.0 - g.gamma);
-  const double cg = g.dt * g.gamma, cb = g.dt * g.dt * g.beta;
+  const double c1 = dt * (0.5 - g.beta), c2 = dt * (1.0 - g.gamma);
+  const double cg = dt * g.gamma, cb = dt * dt * g.beta;
 #pragma unroll
   for (int i = 0; i < DIM; i++) {
     const long o = (long)i * N + n;
@@ -119,8 +138,8 @@ __global__ void __launch_bounds__(256) k_node_adj(AdjNodeArgs g)
     if (!((code >> (2 * i)) & 3)) {
       const double ab = fma(cb, u, fma(cg, nv, na));
       fb = ab * rm * roma;
-      ca = fma(-g.alphaM * roma, ab, fma(c2, nv, g.dt * c1 * u));
-      cv = fma(g.dt, u, nv);
+      ca = fma(-g.alphaM * roma, ab, fma(c2, nv, dt * c1 * u));
+      cv = fma(dt, u, nv);
     }
     g.fbar[o] = fb;
     g.lc[3 * N + o] = cv;
@@ -132,13 +151,16 @@ __global__ void __launch_bounds__(256) k_node_adj(AdjNodeArgs g)
 // Reverse gather: adj(x) += sum of the element nodes' coordinate adjoints, adj(Current du) = sum of
 // their delta_disp adjoints (ascending element order, as k_gather); then the constant boundary
 // conditions, which overwrite the Current du, v, a of their components before the element pass
-// reads them (k_bc_current), zero those components' adjoints.
+// reads them (k_bc_current), zero those components' adjoints.  The time record's increment steps
+// back to the step undone next, whose size the next k_node_adj reads from the schedule.
 template <int DIM>
 __global__ void __launch_bounds__(256) k_gather_adj(int N, int EN, const int *start, const int *entry,
                                                     const double *xe, const double *ue, double *xbar,
-                                                    double *lc, const int *bcIdx, const int *bcCode)
+                                                    double *lc, const int *bcIdx, const int *bcCode,
+                                                    DevTime *tm)
 {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n == 0) tm->increment--;  // the step undone; nothing else in this kernel reads the record
   if (n >= N) return;
   double sx[DIM], su[DIM];
 #pragma unroll
@@ -217,6 +239,7 @@ int tape_nt_of(int etype)
 
 void adj_release(AdjState *A)
 {
+  adj_drop_graphs(A);
   if (A->runDts) cudaFree(A->runDts);
   if (A->runOut) cudaFree(A->runOut);
   if (A->mem) cudaFree(A->mem);
@@ -344,7 +367,7 @@ int adj_restore(dnl_handle *h, AdjState *A, int seg)
 
 // undo one step from its record: the pass again with its per-point record, then the adjoints of the
 // nodal update, the element pass and the gather; ln / lc: the New / Current nodal adjoints
-int adj_reverse_step(dnl_handle *h, AdjState *A, const double *rec, double dt, const double *ln, double *lc)
+int adj_reverse_step(dnl_handle *h, AdjState *A, const double *rec, const double *ln, double *lc)
 {
   cudaStream_t s = h->stream;
   const size_t N = h->N, nIP = h->nIP;
@@ -376,7 +399,8 @@ int adj_reverse_step(dnl_handle *h, AdjState *A, const double *rec, double dt, c
   g.lc = lc;
   g.xbar = A->xbar;
   g.fbar = A->fbar;
-  g.dt = dt;
+  g.dts = A->dts;
+  g.tm = h->tm;
   g.alphaM = h->alphaM;
   g.beta = h->beta;
   g.gamma = h->gamma;
@@ -408,13 +432,70 @@ int adj_reverse_step(dnl_handle *h, AdjState *A, const double *rec, double dt, c
   prof_begin(h, s);
   if (h->dim == 2)
     k_gather_adj<2><<<gridN, 256, 0, s>>>(h->N, h->E * h->nen, h->n2eStart, h->n2e, A->xe, A->ue,
-                                          A->xbar, lc, h->bcIdx, h->bcCode);
+                                          A->xbar, lc, h->bcIdx, h->bcCode, h->tm);
   else
     k_gather_adj<3><<<gridN, 256, 0, s>>>(h->N, h->E * h->nen, h->n2eStart, h->n2e, A->xe, A->ue,
-                                          A->xbar, lc, h->bcIdx, h->bcCode);
+                                          A->xbar, lc, h->bcIdx, h->bcCode, h->tm);
   prof_end(h, DNL_PROF_NODE, s);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
+}
+
+// `len` steps of one kind from the handle's bank parity h->cur and adjoint bank nw: 0 the forward
+// steps, 1 the recomputation writing the step records, 2 the reverse steps (from the last record).
+// Segments of two steps or more replay a graph captured on first use (one per kind, length, parity
+// and adjoint bank: every full segment of a run shares them); profiled runs launch step by step.
+int adj_segment(dnl_handle *h, AdjState *A, int kind, int len, int &nw)
+{
+  auto enqueue = [&]() -> int {
+    int r;
+    if (kind == 2) {
+      for (int j = len - 1; j >= 0; j--) {
+        if ((r = adj_reverse_step(h, A, A->slot + j * A->slotDoubles, A->lam[nw], A->lam[1 - nw]))) return r;
+        nw = 1 - nw;
+      }
+      return 0;
+    }
+    for (int j = 0; j < len; j++)
+      if ((r = adj_primal_step(h, A->dts, kind == 1 ? A->slot + j * A->slotDoubles : nullptr))) return r;
+    return 0;
+  };
+  if (h->profiling || len < 2) return enqueue();
+  if (!A->graphs.empty() && memcmp(&A->graphMat, &h->mat, offsetof(Material, hard)) != 0) adj_drop_graphs(A);
+  cudaStream_t s = h->stream;
+  const int cur0 = h->cur, nw0 = nw;
+  AdjState::SegGraph *g = nullptr;
+  for (auto &x : A->graphs)
+    if (x.kind == kind && x.len == len && x.cur == cur0 && x.nw == nw0) g = &x;
+  if (!g) {
+    const long long k0 = launch_counter();
+    cudaGraph_t graph;
+    CKA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const int rr = enqueue();
+    const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    h->cur = cur0;  // captured, not run
+    nw = nw0;
+    if (rr) {
+      if (ce == cudaSuccess) cudaGraphDestroy(graph);
+      return rr;
+    }
+    if (ce != cudaSuccess) return DNL_ERR_CUDA;
+    cudaGraphExec_t exec;
+    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) return DNL_ERR_CUDA;
+    A->graphs.push_back(AdjState::SegGraph{kind, len, cur0, nw0, exec, launch_counter() - k0});
+    launch_counter() = k0;
+    A->graphMat = h->mat;
+    g = &A->graphs.back();
+  }
+  CKA(cudaGraphLaunch(g->exec, s));
+  launch_counter() += g->kernels;
+  if (kind == 2)
+    nw = (len & 1) ? 1 - nw0 : nw0;
+  else
+    h->cur = (len & 1) ? 1 - cur0 : cur0;
+  return 0;
 }
 
 }  // namespace
@@ -434,7 +515,12 @@ int adjoint_forward(dnl_handle *h, const double *dts, int nsteps, int stride)
 {
   if (!etype_has_sens(h->etype) || h->etype == DNL_ELHEX8N3D_1PT) return DNL_ERR_ARG;
   if (h->elemMat || h->mat.hard.law != DNL_HARD_POWER) return DNL_ERR_ARG;
-  if (stride <= 0) stride = (int)ceil(sqrt((double)nsteps));
+  if (stride <= 0) {
+    // ceil(sqrt(n)), made even so that every full segment starts on the same nodal-field bank and
+    // replays the same graphs
+    stride = (int)ceil(sqrt((double)nsteps));
+    stride += stride & 1;
+  }
   if (stride > nsteps) stride = nsteps;
   if (!h->adj) h->adj = new AdjState();
   AdjState *A = (AdjState *)h->adj;
@@ -445,11 +531,11 @@ int adjoint_forward(dnl_handle *h, const double *dts, int nsteps, int stride)
   CKA(cudaMemcpyAsync(A->dts, dts, sizeof(double) * nsteps, cudaMemcpyHostToDevice, s));
   A->sched.assign(dts, dts + nsteps);
   A->recomputed = 0;
+  int nw = 0;
   for (int seg = 0; seg < A->nseg; seg++) {
     if ((r = adj_save(h, A, seg))) return r;
     const int len = seg == A->nseg - 1 ? nsteps - seg * stride : stride;
-    for (int j = 0; j < len; j++)
-      if ((r = adj_primal_step(h, A->dts, nullptr))) return r;
+    if ((r = adj_segment(h, A, 0, len, nw))) return r;
   }
   DevTime t;
   CKA(cudaMemcpyAsync(&t, h->tm, sizeof t, cudaMemcpyDeviceToHost, s));
@@ -470,7 +556,6 @@ int adjoint_backward(dnl_handle *h, const double *dL_dx, double *grad, dnl_adjoi
   cudaStream_t s = h->stream;
   const size_t N = h->N, nIP = h->nIP;
   const int nsteps = A->nsteps, stride = A->stride;
-  const double *dts = A->sched.data();
   memcpy(A->host, dL_dx, sizeof(double) * 3 * N);
   CKA(cudaMemcpyAsync(A->fbar, A->host, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s));
   k_soa3<<<(unsigned)((N + 255) / 256), 256, 0, s>>>((int)N, A->fbar, A->xbar);
@@ -484,15 +569,9 @@ int adjoint_backward(dnl_handle *h, const double *dL_dx, double *grad, dnl_adjoi
   for (int seg = A->nseg - 1; seg >= 0; seg--) {
     if ((r = adj_restore(h, A, seg))) return r;
     const int len = seg == A->nseg - 1 ? nsteps - seg * stride : stride;
-    for (int j = 0; j < len; j++)
-      if ((r = adj_primal_step(h, A->dts, A->slot + j * A->slotDoubles))) return r;
+    if ((r = adj_segment(h, A, 1, len, nw))) return r;
     A->recomputed += len;
-    for (int j = len - 1; j >= 0; j--) {
-      const int step = seg * stride + j;
-      if ((r = adj_reverse_step(h, A, A->slot + j * A->slotDoubles, dts[step], A->lam[nw], A->lam[1 - nw])))
-        return r;
-      nw = 1 - nw;
-    }
+    if ((r = adj_segment(h, A, 2, len, nw))) return r;
   }
   // lam[nw] now holds the adjoints of the first step's Current field
   k_adj_reduce<<<1, 256, 0, s>>>((int)N, (long)nIP, A->lam[nw] + 3 * N, h->v0dir[0], h->v0dir[1],

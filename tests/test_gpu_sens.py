@@ -130,7 +130,8 @@ def test_reverse_mode_checkpoint_strides(gpu_lib):
         stats[stride] = d.adjoint_stats()
     for stride in (1, 7, 120):
         assert np.array_equal(grads[stride], grads[0]), stride
-    assert stats[0]["stride"] == 11 and stats[0]["checkpoints"] == 11
+    # the default: ceil(sqrt(120)) = 11, made even so every segment replays the same graphs
+    assert stats[0]["stride"] == 12 and stats[0]["checkpoints"] == 10
     assert stats[7]["checkpoints"] == 18 and stats[120]["checkpoints"] == 1
     assert stats[1]["checkpoints"] == 120 and stats[1]["recomputed_steps"] == 120
     # O(sqrt(n)) states with the default stride, against n for a stored trajectory
