@@ -452,8 +452,12 @@ def batch_line(args) -> dict:
     block = b.autotune(steps=3)
     mode = ("persistent kernel per step" if b.tuning()[0] == dynela.BATCH_PERSISTENT
             else "launch sequence per step")
-    b.step_graph(args.steps)  # capture + warm-up
-    for _ in range(max(0, args.warmup - 1)):
+    # every arm is timed over the same increments [W K, (W + 1) K) of each bar (a run's cost per
+    # step grows as the impact wave spreads): the batch back at t = 0 after the tuning, W untimed
+    # graph replays of K steps (the first captures), then the timed one
+    b.reset()
+    b.prologue()
+    for _ in range(max(1, args.warmup)):
         b.step_graph(args.steps)
     hv = b.handle_view()
     with ClockSampler(0) as clk:
@@ -465,18 +469,22 @@ def batch_line(args) -> dict:
         launches = dynela.kernel_launches() - launches0
     clocks = clk.summary()
     value = E * args.steps / (ms * 1e-3)
-    # the same bars one at a time through the single-mesh path, state resident: stream launches
-    # (dnl_step) and graph replay (dnl_step_graph, the faster of the two, which the ratio uses)
+    # the same bars one at a time through the single-mesh path, state resident, over the same
+    # increments: stream launches (dnl_step) and graph replay (dnl_step_graph; the faster of the two
+    # is the ratio's denominator)
+    start = max(1, args.warmup) * args.steps
     plain_ms = plain_graph_ms = 0.0
     for m in models:
         d = dynela.GpuDomain(m)
         d.prologue()
-        d.step(args.warmup)
+        d.step(start)
         d.timer_mark(0)
         d.step(args.steps)
         d.timer_mark(1)
         plain_ms += d.timer_elapsed_ms(0, 1)
-        d.step_graph(args.steps)  # capture and warm-up
+        d.reset()
+        for _ in range(max(1, args.warmup)):
+            d.step_graph(args.steps)  # the first captures
         d.timer_mark(0)
         d.step_graph(args.steps)
         d.timer_mark(1)
@@ -490,6 +498,8 @@ def batch_line(args) -> dict:
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, numpy default_rng(0))",
             "config": {"workload": f"taylor_axi_batch_{args.instances}", "elements": E,
                        "instances": args.instances, "block": block, "mode": mode,
+                       "window": f"increments {start} to {start + args.steps} of every bar, "
+                                 "the same for the batch and the bars run alone",
                        "active_after": active,
                        "l2": "inputs larger than L2 (integration-point state "
                              f"{E * 4 * 15 * 8 / 1e6:.0f} MB)"},

@@ -196,8 +196,10 @@ int dnl_batch_graph_capture(dnl_batch *b, int nsteps);
 #define DNL_BATCH_LAUNCHES 0
 #define DNL_BATCH_PERSISTENT 1
 int dnl_batch_set_mode(dnl_batch *b, int mode);
-/* time live steps of both modes with 64, 128 and 256 threads per element-pass block; keep the
- * fastest (*block: its block size; dnl_batch_get_tuning gives both) */
+/* time live steps of both modes with 64, 128 and 256 threads per element-pass block (one untimed
+ * step each, then steps_per_candidate rounds of one step per candidate in turn, so 6 * (1 +
+ * steps_per_candidate) increments in all); keep the fastest (*block: its block size;
+ * dnl_batch_get_tuning gives both) */
 int dnl_batch_autotune(dnl_batch *b, int steps_per_candidate, int *block);
 int dnl_batch_get_tuning(dnl_batch *b, int *mode, int *block);
 int dnl_batch_set_block(dnl_batch *b, int block);

@@ -11,10 +11,11 @@
 // the per-step launch cost is paid once for the batch; `dnl_batch_step_graph` captures a run of
 // steps into a CUDA graph and replays it.
 //
-// Tile autotuning: the element pass is launched with 64, 128 or 256 threads per block (16, 32 or
-// 64 axisymmetric elements per block); `dnl_batch_autotune` times live steps with each and keeps
-// the fastest.  Every element's arithmetic is independent of the block size, so the choice does
-// not change results.
+// Autotuning: the element pass is launched with 64, 128 or 256 threads per block (16, 32 or 64
+// axisymmetric elements per block), and a step is either the launch sequence or one persistent
+// kernel; `dnl_batch_autotune` times live steps of the six candidates taken in turn and keeps the
+// fastest.  Every element's arithmetic is independent of both choices, so they do not change
+// results.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -547,32 +548,38 @@ int dnl_batch_autotune(dnl_batch *b, int steps_per_candidate, int *block)
   if (!b || steps_per_candidate <= 0) return DNL_ERR_ARG;
   int r;
   if (!b->prologueDone && (r = dnl_batch_prologue(b))) return r;
+  // candidates (mode, block): each first runs one untimed step (the first launch of its kernels
+  // loads them), then the candidates are timed one step each in turn, steps_per_candidate rounds:
+  // a run's cost per step drifts as it proceeds (the wave spreads, points yield), and taking the
+  // candidates in turn lets that drift fall on all of them alike
   const int cands[3] = {64, 128, 256};
-  double best = 1e300;
-  int bestB = b->block, bestM = b->mode;
+  constexpr int NC = 2 * 3;
+  double total[NC] = {};
+  const int mode0 = b->mode, block0 = b->block;
   cudaEvent_t e0, e1;
   BK(cudaEventCreate(&e0));
   BK(cudaEventCreate(&e1));
   r = 0;
-  for (int mode = DNL_BATCH_LAUNCHES; mode <= DNL_BATCH_PERSISTENT && !r; mode++)
-    for (int c = 0; c < 3; c++) {
-      b->mode = mode;
-      b->block = cands[c];
-      BK(cudaEventRecord(e0, b->h->stream));
+  for (int round = -1; round < steps_per_candidate && !r; round++)
+    for (int c = 0; c < NC && !r; c++) {
+      b->mode = c < 3 ? DNL_BATCH_LAUNCHES : DNL_BATCH_PERSISTENT;
+      b->block = cands[c % 3];
       int active = 0;
-      if ((r = dnl_batch_step(b, steps_per_candidate, &active))) break;
-      BK(cudaEventRecord(e1, b->h->stream));
-      BK(cudaEventSynchronize(e1));
       float ms = 0.f;
-      BK(cudaEventElapsedTime(&ms, e0, e1));
-      if (ms < best) {
-        best = ms;
-        bestB = cands[c];
-        bestM = mode;
-      }
+      if (cudaEventRecord(e0, b->h->stream) != cudaSuccess) r = DNL_ERR_CUDA;
+      if (!r) r = dnl_batch_step(b, 1, &active);
+      if (!r && cudaEventRecord(e1, b->h->stream) != cudaSuccess) r = DNL_ERR_CUDA;
+      if (!r && cudaEventSynchronize(e1) != cudaSuccess) r = DNL_ERR_CUDA;
+      if (!r && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) r = DNL_ERR_CUDA;
+      if (round >= 0) total[c] += ms;
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  int bestC = -1;
+  for (int c = 0; c < NC && !r; c++)
+    if (bestC < 0 || total[c] < total[bestC]) bestC = c;
+  const int bestM = bestC < 0 ? mode0 : (bestC < 3 ? DNL_BATCH_LAUNCHES : DNL_BATCH_PERSISTENT);
+  const int bestB = bestC < 0 ? block0 : cands[bestC % 3];
   b->block = bestB;
   b->mode = bestM;
   for (int i = 0; i < b->ngraphs; i++) cudaGraphExecDestroy(b->graphs[i].exec);

@@ -177,18 +177,42 @@ __device__ __forceinline__ unsigned long long abits(double a)
 }
 __device__ __forceinline__ bool abs_gt(double a, double b) { return abits(a) > abits(b); }
 
-// ln(1 + x) for |x| <= 2^-6 by the Mercator series x - x^2/2 + x^3/3 - ... to x^10/10 in Horner
-// form: the truncation is below 2^-60 |x| and the result within about an ulp (10 FP64
-// instructions where the library logarithm takes about 25).
+constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
+
+// x * 2^K by adding K to the exponent field (integer pipe): the product's exact value for +-0 and
+// for normal x whose product is normal, which is every call site's case (eigenvalue logarithms,
+// sums of strain traces, pivot entries and diagonal differences of C, all far from the ends of the
+// range); infinite and NaN x are returned unchanged (as the product would be, NaN payload aside).
+template <int K>
+__device__ __forceinline__ double scale2(double x)
+{
+  const int hi = __double2hiint(x);
+  const int ef = (hi >> 20) & 0x7ff;
+  const double y = __hiloint2double(hi + K * (1 << 20), __double2loint(x));
+  return ef == 0 || ef == 0x7ff ? x : y;
+}
+
+// ln(1 + x) for |x| <= 2^-6 by the Mercator series x - x^2/2 + x^3/3 - ... in Horner form, to
+// x^9/9, to x^6/6 when |x| <= 2^-9, to x^4/4 when |x| <= 2^-14: the alternating series' truncation,
+// at most the first omitted term, is below 2^-56 |x| in each case (2^-54 / 10, 2^-54 / 7,
+// 2^-56 / 5), under a tenth of an ulp of the result, which is within about an ulp (9, 6 or 4 FP64
+// instructions where the library logarithm takes 28).  The length depends on the point's own x
+// only, so a point's result does not depend on the other points of its warp; a warp runs the
+// longest form any of its points needs.
 __device__ __forceinline__ double log1p_series(double x)
 {
-  double s = -1. / 10.;
-  s = fma(x, s, 1. / 9.);
-  s = fma(x, s, -1. / 8.);
-  s = fma(x, s, 1. / 7.);
-  s = fma(x, s, -1. / 6.);
-  s = fma(x, s, 1. / 5.);
-  s = fma(x, s, -1. / 4.);
+  double s = -1. / 4.;
+  if (abits(x) > abits(0x1p-14)) {
+    double u = -1. / 6.;
+    if (abits(x) > abits(0x1p-9)) {
+      double v = 1. / 9.;
+      v = fma(x, v, -1. / 8.);
+      v = fma(x, v, 1. / 7.);
+      u = fma(x, v, -1. / 6.);
+    }
+    u = fma(x, u, 1. / 5.);
+    s = fma(x, u, -1. / 4.);
+  }
   s = fma(x, s, 1. / 3.);
   s = fma(x, s, -1. / 2.);
   s = fma(x, s, 1.);
@@ -205,16 +229,18 @@ __device__ __forceinline__ double ln_eig(double l)
   return abits(x) <= abits(kSeriesMax) ? log1p_series(x) : log(l);
 }
 
-// e^t for |t| <= 2^-5 by its Taylor series to t^9/9! in Horner form (truncation below 2^-70)
+// e^t for |t| <= 2^-5 by its Taylor series in Horner form, to t^7/7!, to t^5/5! when |t| <= 2^-9,
+// to t^3/3! when |t| <= 2^-14: the truncation is below 2^-55 (2^-40 / 8!, 2^-54 / 6!,
+// 2^-56 / 4!), with e^t within 4 % of 1 a tenth of an ulp (7, 5 or 3 FP64 instructions where the
+// library exponential takes 15); the length depends on t only (as log1p_series).
 __device__ __forceinline__ double exp_series(double t)
 {
-  double s = 1. / 362880.;
-  s = fma(t, s, 1. / 40320.);
-  s = fma(t, s, 1. / 5040.);
-  s = fma(t, s, 1. / 720.);
-  s = fma(t, s, 1. / 120.);
-  s = fma(t, s, 1. / 24.);
-  s = fma(t, s, 1. / 6.);
+  double s = 1. / 6.;
+  if (abits(t) > abits(0x1p-14)) {
+    double u = 1. / 120.;
+    if (abits(t) > abits(0x1p-9)) u = fma(t, fma(t, 1. / 5040., 1. / 720.), 1. / 120.);
+    s = fma(t, fma(t, u, 1. / 24.), 1. / 6.);
+  }
   s = fma(t, s, 0.5);
   s = fma(t, s, 1.);
   return fma(t, s, 1.);
@@ -273,8 +299,8 @@ __device__ __forceinline__ void jacobi_angle(double fpp, double fqq, double fpq,
                                              double &t)
 {
   const double d = fqq - fpp;
-  const double w = rsqrt(fma(d, d, (4.0 * fpq) * fpq));
-  const double h = fma(0.5 * iabs(d), w, 0.5);  // cos^2(theta)
+  const double w = rsqrt(fma(d, d, scale2<2>(fpq) * fpq));
+  const double h = fma(scale2<-1>(iabs(d)), w, 0.5);  // cos^2(theta)
   const double r = rsqrt(h);                    // 1 / c
   c = h * r;
   const double sv = iabs(fpq) * w * r;
@@ -296,7 +322,10 @@ __device__ __forceinline__ void jacobi_angle(double fpp, double fqq, double fpq,
 // of 1 (at most 9 in 4e5 random 3x3 cases, the same order as the angle's own effect) and the
 // pivot sequences are the same (x' is below the 1e-9 stop either way).
 // TWO_D (axisymmetric and plane strain): C is block diagonal and the pivot is always (0, 1).
-template <bool TWO_D>
+// FIRST: Rot is still the identity, so Rot R is R itself, whose entries are c, s, -s, 0 and 1:
+// selected, not multiplied (the products by 0 and 1 that the general update forms are exact and
+// give the same doubles, +0 included).
+template <bool TWO_D, bool FIRST = false>
 __device__ __forceinline__ void jacobi_rotate(int k, double &f00, double &f11, double &f22, double &f01,
                                               double &f02, double &f12, double rot[3][3], double x)
 {
@@ -322,6 +351,20 @@ __device__ __forceinline__ void jacobi_rotate(int k, double &f00, double &f11, d
     f01 = k == 0 ? x2 : y2;
     f02 = k == 0 ? y2 : (k == 1 ? x2 : z2);
     f12 = k == 2 ? x2 : z2;
+  }
+  if (FIRST) {
+    // pivot (p, q): R_pp = R_qq = c, R_pq = s, R_qp = -s, R_oo = 1, zero elsewhere
+    const int p = k == 2 ? 1 : 0, q = k == 0 ? 1 : 2;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+        rot[i][j] = (i == p && j == p) || (i == q && j == q) ? c
+                    : (i == p && j == q)                     ? s
+                    : (i == q && j == p)                     ? ms
+                    : (i != p && i != q && i == j)           ? 1.
+                                                             : 0.;
+    return;
   }
 #pragma unroll
   for (int i = 0; i < (TWO_D ? 2 : 3); i++) {
@@ -434,7 +477,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
   double detJ, Ji[DIM][DIM];
   if (TWO_D) {
     detJ = fma(J[0][0], J[1][1], -J[0][1] * J[1][0]);
-    const double r = 1. / detJ;
+    const double r = nr_rcp(detJ);  // the IEEE reciprocal but in rare hard cases (within an ulp)
     Ji[0][0] = J[1][1] * r;
     Ji[0][1] = -J[0][1] * r;
     Ji[1][0] = -J[1][0] * r;
@@ -445,7 +488,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     const double c01 = fma(J[1][2], J[2][0], -J[1][0] * J[2][2]);
     const double c02 = fma(J[1][0], J[2][1], -J[1][1] * J[2][0]);
     detJ = fma(J[0][0], c00, fma(J[0][1], c01, J[0][2] * c02));
-    const double r = 1. / detJ;
+    const double r = nr_rcp(detJ);  // the IEEE reciprocal but in rare hard cases (within an ulp)
     Ji[0][0] = c00 * r;
     Ji[1][0] = c01 * r;
     Ji[2][0] = c02 * r;
@@ -534,7 +577,11 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         conv = true;
         break;
       }
-      jacobi_rotate<TWO_D>(k, f00, f11, f22, f01, f02, f12, rot, fpq);
+      // the lanes still in the loop are all at the same iteration: a uniform branch
+      if (it == 1)
+        jacobi_rotate<TWO_D, true>(k, f00, f11, f22, f01, f02, f12, rot, fpq);
+      else
+        jacobi_rotate<TWO_D>(k, f00, f11, f22, f01, f02, f12, rot, fpq);
     }
     f[0][0] = f00;
     f[1][1] = f11;
@@ -548,7 +595,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     double lg[3], il[3];
 #pragma unroll
     for (int cc = 0; cc < 3; cc++) {
-      lg[cc] = 0.5 * ln_eig(f[cc][cc]);
+      lg[cc] = scale2<-1>(ln_eig(f[cc][cc]));
       il[cc] = rsqrt(f[cc][cc]);
     }
     if (TAPE) {
@@ -575,6 +622,10 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         tape(TL::HD + k, hh);
       }
     }
+    // 2 + 1 block: Rot is the identity or the one rotation's [[c, s], [-s, c]], so the products
+    // Rot_ic Rot_jc of the block are c c, s s and +-c s (the same doubles, three multiplications)
+    const double pcc = TWO_D ? rot[0][0] * rot[0][0] : 0., pss = TWO_D ? rot[0][1] * rot[0][1] : 0.;
+    const double pcs = TWO_D ? rot[0][0] * rot[0][1] : 0.;
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -588,7 +639,10 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         } else {
 #pragma unroll
           for (int cc = 0; cc < (TWO_D ? 2 : 3); cc++) {
-            const double ext = rot[i][cc] * rot[j][cc];
+            const double ext = !TWO_D      ? rot[i][cc] * rot[j][cc]
+                               : i != j    ? (cc == 0 ? ineg(pcs) : pcs)
+                               : (i == cc) ? pcc
+                                           : pss;
             su = fma(lg[cc], ext, su);
             sr = fma(il[cc], ext, sr);
           }
@@ -755,7 +809,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
           break;
         }
       }
-      const double inv = 1. / normS;
+      const double inv = nr_rcp(normS);  // normS > 0: the trial stress is above A > 0
       tape(TL::GAM, gamma);
       tape(TL::XV, RADD(evp, RMUL(kSqrt23, gamma)));
       tape(TL::XN, xn);
@@ -783,7 +837,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     const int base = lane - pt;
 #pragma unroll
     for (int k = 0; k < NIP; k++) pressure += __shfl_sync(0xffffffffu, trace, base + k);
-    pressure *= 1.0 / NIP;  // exact: NIP is a power of two
+    pressure = scale2<-ilog2(NIP)>(pressure);  // exact: NIP is a power of two
   }
   const double p = fma(m.K, pressure, a.ip[L::P * nIP + ipx]);
 
