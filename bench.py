@@ -452,54 +452,72 @@ def batch_line(args) -> dict:
     block = b.autotune(steps=3)
     mode = ("persistent kernel per step" if b.tuning()[0] == dynela.BATCH_PERSISTENT
             else "launch sequence per step")
-    # every arm is timed over the same increments [W K, (W + 1) K) of each bar (a run's cost per
-    # step grows as the impact wave spreads): the batch back at t = 0 after the tuning, W untimed
-    # graph replays of K steps (the first captures), then the timed one
+    # every arm is timed over the same increments [S, S + K) of each bar, S = --batch-start (400:
+    # every bar still running, the impact wave across most of them, their impact ends plastic; a
+    # run's cost per step grows as the wave spreads and points yield).  The batch, back at t = 0
+    # after the tuning: S - W K launch-sequence steps, W graph replays of K steps (the first
+    # captures), then the timed replay.
+    K, W = args.steps, max(1, args.warmup)
+    start = max(args.batch_start, W * K)
     b.reset()
     b.prologue()
-    for _ in range(max(1, args.warmup)):
-        b.step_graph(args.steps)
+    if start > W * K:
+        b.step(start - W * K)
+    for _ in range(W):
+        b.step_graph(K)
+    inc0 = [b.time_info(i)["increment"] for i in range(len(models))]
     hv = b.handle_view()
     with ClockSampler(0) as clk:
         launches0 = dynela.kernel_launches()
         hv.timer_mark(0)
-        active = b.step_graph(args.steps)
+        active = b.step_graph(K)
         hv.timer_mark(1)
         ms = hv.timer_elapsed_ms(0, 1)
         launches = dynela.kernel_launches() - launches0
     clocks = clk.summary()
-    value = E * args.steps / (ms * 1e-3)
+    # element-updates: each bar's elements times the increments it made (a bar at its end time
+    # makes none)
+    done = sum(m.E * (b.time_info(i)["increment"] - inc0[i]) for i, m in enumerate(models))
+    value = done / (ms * 1e-3)
     # the same bars one at a time through the single-mesh path, state resident, over the same
     # increments: stream launches (dnl_step) and graph replay (dnl_step_graph; the faster of the two
     # is the ratio's denominator)
-    start = max(1, args.warmup) * args.steps
     plain_ms = plain_graph_ms = 0.0
+    plain_done = plain_graph_done = 0
     for m in models:
         d = dynela.GpuDomain(m)
         d.prologue()
         d.step(start)
+        i0 = d.time_info()["increment"]
         d.timer_mark(0)
-        d.step(args.steps)
+        d.step(K)
         d.timer_mark(1)
         plain_ms += d.timer_elapsed_ms(0, 1)
+        plain_done += m.E * (d.time_info()["increment"] - i0)
         d.reset()
-        for _ in range(max(1, args.warmup)):
-            d.step_graph(args.steps)  # the first captures
+        d.prologue()
+        if start > W * K:
+            d.step(start - W * K)
+        for _ in range(W):
+            d.step_graph(K)  # the first captures
+        i0 = d.time_info()["increment"]
         d.timer_mark(0)
-        d.step_graph(args.steps)
+        d.step_graph(K)
         d.timer_mark(1)
         plain_graph_ms += d.timer_elapsed_ms(0, 1)
+        plain_graph_done += m.E * (d.time_info()["increment"] - i0)
         d.close()
-    plain = E * args.steps / (plain_ms * 1e-3)
-    plain_graph = E * args.steps / (plain_graph_ms * 1e-3)
+    plain = plain_done / (plain_ms * 1e-3)
+    plain_graph = plain_graph_done / (plain_graph_ms * 1e-3)
     line = {"metric": "element-updates/s (batched)", "value": value, "unit": "element-updates/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, numpy default_rng(0))",
             "config": {"workload": f"taylor_axi_batch_{args.instances}", "elements": E,
                        "instances": args.instances, "block": block, "mode": mode,
-                       "window": f"increments {start} to {start + args.steps} of every bar, "
+                       "window": f"increments {start} to {start + K} of every bar, "
                                  "the same for the batch and the bars run alone",
+                       "element_updates_timed": done,
                        "active_after": active,
                        "l2": "inputs larger than L2 (integration-point state "
                              f"{E * 4 * 15 * 8 / 1e6:.0f} MB)"},
@@ -840,6 +858,8 @@ def main():
     ap.add_argument("--sens-steps", type=int, default=4000,
                     help="explicit steps of the gradient workload's schedule")
     ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--batch-start", type=int, default=400,
+                    help="increment at which the batched line's timed window starts")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--start-us", type=float, default=10.0,
                     help="simulated time at which the timed window starts (reached untimed), so "
