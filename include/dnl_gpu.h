@@ -132,6 +132,15 @@ typedef struct {
  * shape-function derivatives. */
 int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_solver_params *sp,
                dnl_handle **out);
+/* Structure::setDefaultElement + Structure::createElement (Structure.C:204-256, 1032-1036) for a
+ * further element type in the same domain, which Domain::initSolve accepts within one family
+ * (Domain.C:1042-1060): num_elements elements of etype, conn (E*nen, node indices) in the
+ * handle's node numbering, numbered after the elements already there.  Before dnl_prologue or the
+ * first step; 3D reference elements (ElHex8n3D, ElTet4n3D, ElTet10n3D) with one power-law
+ * material, ElHex8n3D with the Pulse time step only.  Integration-point arrays of
+ * dnl_get/set_state then cover every group in element order; the sensitivity, adjoint, schedule,
+ * results-restart and several-material entry points return DNL_ERR_ARG on such a handle. */
+int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn);
 int dnl_destroy(dnl_handle *h);
 /* DNL_ELHEX8N3D_1PT: the viscous hourglass coefficient (default 0.05): the force resisting the
  * hourglass modes is a_h = coefficient rho c V^(2/3) / 4 times the mode's velocity.  The viscosity

@@ -24,14 +24,26 @@ REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
 MODEL_MAGIC = 0x4D4C4E44  # "DNLM"
 EXT_MAGIC = 0x584C4E44  # "DNLX": optional block after the solver settings
 STATE_MAGIC = 0x54534E44  # "DNST"
+MIXED = 9  # model file etype: the elements' own types follow
 
 
 def write_model(path: str, m) -> None:
     """Serialise a :class:`redynela_gb300.meshes.Model` for the harness."""
+    groups = m.element_groups() if hasattr(m, "element_groups") else [(m.etype, m.conn)]
     with open(path, "wb") as f:
-        f.write(struct.pack("<4q", MODEL_MAGIC, m.etype, m.N, m.E))
-        f.write(np.ascontiguousarray(m.coords, dtype="<f8").tobytes())
-        f.write(np.ascontiguousarray(m.conn, dtype="<i8").tobytes())
+        if len(groups) == 1:
+            f.write(struct.pack("<4q", MODEL_MAGIC, m.etype, m.N, m.E))
+            f.write(np.ascontiguousarray(m.coords, dtype="<f8").tobytes())
+            f.write(np.ascontiguousarray(m.conn, dtype="<i8").tobytes())
+        else:
+            # etype 9: the type of each element, then every element's nodes
+            E = sum(c.shape[0] for _, c in groups)
+            f.write(struct.pack("<4q", MODEL_MAGIC, MIXED, m.N, E))
+            f.write(np.ascontiguousarray(m.coords, dtype="<f8").tobytes())
+            types = np.concatenate([np.full(c.shape[0], t, dtype="<i8") for t, c in groups])
+            f.write(types.tobytes())
+            for _, c in groups:
+                f.write(np.ascontiguousarray(c, dtype="<i8").tobytes())
         f.write(struct.pack("<6d", m.young, m.poisson, m.density, m.A, m.B, m.n))
         f.write(struct.pack("<3d", *m.v0))
         f.write(struct.pack("<q", len(m.bcs)))
@@ -62,12 +74,12 @@ def write_model(path: str, m) -> None:
 
 
 def write_state(path: str, coords, du, v, a, disp, S, Eps, EpsPlas, p, evp, dt) -> None:
-    """Nodal arrays are (N, 3); tensors are (E, nip, 3, 3); p, evp are (E, nip)."""
+    """Nodal arrays are (N, 3); tensors are (E, nip, 3, 3) or, for any mix of element types,
+    (nIP, 3, 3) in element order; p, evp are (E, nip) or (nIP,)."""
     N = coords.shape[0]
     node = np.concatenate([coords, du, v, a, disp], axis=1).reshape(N, 15)
-    E, nip = p.shape
-    ip = np.concatenate([S.reshape(E, nip, 9), Eps.reshape(E, nip, 9), EpsPlas.reshape(E, nip, 9),
-                         p.reshape(E, nip, 1), evp.reshape(E, nip, 1)], axis=2)
+    ip = np.concatenate([S.reshape(-1, 9), Eps.reshape(-1, 9), EpsPlas.reshape(-1, 9),
+                         p.reshape(-1, 1), evp.reshape(-1, 1)], axis=1)
     with open(path, "wb") as f:
         f.write(struct.pack("<q", STATE_MAGIC))
         f.write(np.ascontiguousarray(node, dtype="<f8").tobytes())

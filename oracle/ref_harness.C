@@ -150,12 +150,16 @@ struct MatLaw
   std::vector<double> tx, ty;
 };
 
+static long nenOf(long etype) { return etype == 1 ? 8 : (etype == 4 ? 10 : 4); }
+
 struct Model
 {
-  long etype; // 0 ElQua4nAx, 1 ElHex8n3D, 2 ElQua4n2D, 3 ElTet4n3D, 4 ElTet10n3D
+  long etype; // 0 ElQua4nAx, 1 ElHex8n3D, 2 ElQua4n2D, 3 ElTet4n3D, 4 ElTet10n3D, 9 per element
   long N, E, nen;
   std::vector<double> coords; // N*3
-  std::vector<long> conn;     // E*nen, 0-based
+  std::vector<long> conn;     // the elements' nodes one after another, 0-based
+  std::vector<long> etypes;   // per element (etype 9: a domain of several element types)
+  std::vector<long> first;    // E+1 offsets into conn
   double mat[6];              // E, nu, rho, A, B, n
   double v0[3];               // initial speed of every node
   std::vector<BCGroup> bcs;
@@ -182,10 +186,19 @@ static Model readModel(const char *path)
   m.etype = r.i64();
   m.N = r.i64();
   m.E = r.i64();
-  m.nen = (m.etype == 1 ? 8 : (m.etype == 4 ? 10 : 4));
   m.coords.resize(m.N * 3);
   r.f64s(m.coords.data(), m.coords.size());
-  m.conn.resize(m.E * m.nen);
+  // etype 9: the type of each element follows (a domain of one family mixing element types,
+  // Domain.C:1042-1060), then each element's nodes
+  m.etypes.assign(m.E, m.etype);
+  if (m.etype == 9)
+    for (long e = 0; e < m.E; e++)
+      m.etypes[e] = r.i64();
+  m.first.assign(m.E + 1, 0);
+  for (long e = 0; e < m.E; e++)
+    m.first[e + 1] = m.first[e] + nenOf(m.etypes[e]);
+  m.nen = m.etype == 9 ? 0 : nenOf(m.etype);
+  m.conn.resize(m.first[m.E]);
   for (size_t i = 0; i < m.conn.size(); i++)
     m.conn[i] = r.i64();
   r.f64s(m.mat, 6);
@@ -257,19 +270,26 @@ static Built build(const Model &m)
   for (long n = 0; n < m.N; n++)
     st->createNode(n + 1, m.coords[3 * n], m.coords[3 * n + 1], m.coords[3 * n + 2]);
 
-  Element *proto = (m.etype == 0   ? (Element *)new ElQua4nAx(0)
-                    : m.etype == 2 ? (Element *)new ElQua4n2D(0)
-                    : m.etype == 3 ? (Element *)new ElTet4n3D(0)
-                    : m.etype == 4 ? (Element *)new ElTet10n3D(0)
-                                   : (Element *)new ElHex8n3D(0));
-  st->setDefaultElement(proto);
+  // as a deck does: setDefaultElement, then createElement; again at each change of element type
+  long protoType = -1;
   ElementSet *els = new ElementSet;
   for (long e = 0; e < m.E; e++)
   {
-    const long *c = &m.conn[e * m.nen];
-    if (m.nen == 4)
+    const long et = m.etypes[e], nen = nenOf(et);
+    if (et != protoType)
+    {
+      Element *proto = (et == 0   ? (Element *)new ElQua4nAx(0)
+                        : et == 2 ? (Element *)new ElQua4n2D(0)
+                        : et == 3 ? (Element *)new ElTet4n3D(0)
+                        : et == 4 ? (Element *)new ElTet10n3D(0)
+                                  : (Element *)new ElHex8n3D(0));
+      st->setDefaultElement(proto);
+      protoType = et;
+    }
+    const long *c = &m.conn[m.first[e]];
+    if (nen == 4)
       st->createElement(e + 1, (int)c[0] + 1, (int)c[1] + 1, (int)c[2] + 1, (int)c[3] + 1);
-    else if (m.nen == 8)
+    else if (nen == 8)
       st->createElement(e + 1, (int)c[0] + 1, (int)c[1] + 1, (int)c[2] + 1, (int)c[3] + 1,
                         (int)c[4] + 1, (int)c[5] + 1, (int)c[6] + 1, (int)c[7] + 1);
     else

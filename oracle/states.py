@@ -26,6 +26,10 @@ def random_state(model, seed: int = 0, du_scale: float = 2e-3, dt: float = 1e-8)
     axi = m.etype == 0
     two_d = m.etype != 1
     dim, N, E, nip = m.dim, m.N, m.E, m.nip
+    if getattr(m, "groups", None):
+        # several element types (3D): per-IP arrays flat over every group's points, element order
+        two_d = False
+        E, nip = m.nIP_all, 1
     x = m.coords[m.conn]  # (E, nen, 3)
     h = float(np.min(np.linalg.norm(x[:, 1] - x[:, 0], axis=1)))
     coords = m.coords.copy()
@@ -58,5 +62,8 @@ def random_state(model, seed: int = 0, du_scale: float = 2e-3, dt: float = 1e-8)
     Eps = _sym(rng, (E, nip), 2e-2, two_d)
     EpsPlas = _sym(rng, (E, nip), 1e-2, two_d)
     p = rng.normal(scale=1e8, size=(E, nip))
+    if getattr(m, "groups", None):
+        S, Eps, EpsPlas = S[:, 0], Eps[:, 0], EpsPlas[:, 0]
+        p, evp = p[:, 0], evp[:, 0]
     return dict(coords=coords, du=du, v=v, a=a, disp=disp, S=S, Eps=Eps, EpsPlas=EpsPlas, p=p,
                 evp=evp, dt=dt)

@@ -513,7 +513,7 @@ void adj_free(dnl_handle *h)
 // `stride`-th step; the final coordinates are left in the handle
 int adjoint_forward(dnl_handle *h, const double *dts, int nsteps, int stride)
 {
-  if (!etype_has_sens(h->etype) || h->etype == DNL_ELHEX8N3D_1PT) return DNL_ERR_ARG;
+  if (!etype_has_sens(h->etype) || h->etype == DNL_ELHEX8N3D_1PT || h->nextra) return DNL_ERR_ARG;
   if (h->elemMat || h->mat.hard.law != DNL_HARD_POWER) return DNL_ERR_ARG;
   if (stride <= 0) {
     // ceil(sqrt(n)), made even so that every full segment starts on the same nodal-field bank and
@@ -656,7 +656,7 @@ int dnl_adjoint_stats(dnl_handle *h, dnl_adjoint_info *info)
 
 int dnl_run_schedule(dnl_handle *h, int nsteps, const double *dts, double *coords)
 {
-  if (!h || nsteps <= 0 || !dts) return DNL_ERR_ARG;
+  if (!h || nsteps <= 0 || !dts || h->nextra) return DNL_ERR_ARG;
   for (int k = 0; k < nsteps; k++)
     if (!(dts[k] > 0. && dts[k] < 1e300)) return DNL_ERR_ARG;
   if (h->hostIncrement != 0) return DNL_ERR_ARG;  // starts from the initial state

@@ -282,7 +282,8 @@ struct ElemArgs {
   const double *v[3];  // Current mat_speed (the one-point hexahedron's hourglass viscosity)
   double hourglass;    // its coefficient
   double *ip;          // integration-point state
-  double *fe;          // element forces [DIM][E*NEN]
+  double *fe;          // element forces: component i of element e's node k at fe[i feStride + e NEN + k]
+  long feStride;       // element-node slots of the handle's element groups (E*NEN with one type)
   double *detJ;        // [E*NIP] (written)
   double *stepT;       // optional dEps|R per IP, [18][E*NIP] or nullptr
   double *tape;        // [TapeLayout::NT][E*NIP], written by the tape instance of k_elem
@@ -390,8 +391,24 @@ struct GraphEntry {
 
 }  // namespace dnl
 
+namespace dnl {
+// A further group of elements of another type in the same domain (dnl_add_elements): its elements
+// are numbered after those of the handle's first group and of the groups added before it.  Its
+// element-node slots in fe / kx / the lumped-mass vector start at feOff.
+struct ElemGroup {
+  int etype, nen, nip, E;
+  long nIP, feOff;
+  int *conn;     // [NEN][E]
+  double *ip;    // integration-point state [NCOMP][nIP]
+  double *detJ;  // [nIP]
+  double *pj;    // Pulse per-Gauss-point kinematics, or nullptr
+  double *Cs;    // Courant: the sound speed of each element when the groups' differ, or nullptr
+};
+}  // namespace dnl
+
 struct dnl_handle {
-  int etype, dim, nen, nip, N, E, nIP;
+  int etype, dim, nen, nip, N, E, nIP;  // the first element group (the only one unless
+                                         // dnl_add_elements added others)
   int flags;
   cudaStream_t stream;
   // mesh
@@ -407,7 +424,10 @@ struct dnl_handle {
   double *ip;
   double *detJ;
   double *stepT;
-  double *fe;                 // [DIM][E*NEN]
+  double *fe;                 // [DIM][EN]
+  long EN;                    // element-node slots of all element groups
+  int nextra;                 // further element groups (dnl_add_elements)
+  dnl::ElemGroup *extra;
   double *fint;               // [N*DIM]
   // boundary conditions
   int nbcNodes;

@@ -955,7 +955,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         if (AXI) s[0] = fma(SH::N(q, pt), Mq[DIM * DIM], s[0]);
       }
 #pragma unroll
-      for (int i = 0; i < DIM; i++) a.fe[(long)i * a.E * NEN + (long)e * NEN + pt] = ineg(s[i]);
+      for (int i = 0; i < DIM; i++) a.fe[(long)i * a.feStride + (long)e * NEN + pt] = ineg(s[i]);
     }
   } else {
     double *row = red + pt * (NEN * DIM);
@@ -1043,7 +1043,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
             double s = 0.0;
 #pragma unroll
             for (int q = 0; q < NIP; q++) s -= red[q * (NEN * DIM) + k * DIM + i];
-            a.fe[(long)i * a.E * NEN + (long)e * NEN + k] = s;
+            a.fe[(long)i * a.feStride + (long)e * NEN + k] = s;
           }
         }
       }
@@ -1476,6 +1476,7 @@ static ElemArgs elem_args(dnl_handle *h)
   a.hourglass = h->hourglass;
   a.ip = h->ip;
   a.fe = h->fe;
+  a.feStride = h->EN;
   a.detJ = h->detJ;
   a.stepT = h->stepT;
   a.tm = h->tm;
@@ -1484,6 +1485,23 @@ static ElemArgs elem_args(dnl_handle *h)
   a.mats = h->dmats;
   a.elemCs = h->elemCs;
   a.gate = 1;
+  return a;
+}
+
+// the element arguments of a further element group g: its connectivity, integration points and
+// slots of the handle's element-force array (one material; no step tensors)
+static ElemArgs group_args(dnl_handle *h, const ElemGroup &g)
+{
+  ElemArgs a = elem_args(h);
+  a.E = g.E;
+  a.conn = g.conn;
+  a.ip = g.ip;
+  a.fe = h->fe + g.feOff;
+  a.detJ = g.detJ;
+  a.stepT = nullptr;
+  a.elemMat = nullptr;
+  a.mats = nullptr;
+  a.elemCs = g.Cs;
   return a;
 }
 
@@ -1499,15 +1517,28 @@ int launch_elem(dnl_handle *h, cudaStream_t s, int gate)
     DNL_BY_ETYPE(h->etype, (k_elem<ET, false, true><<<grid, 128, 0, s>>>(a)));
   else
     DNL_BY_ETYPE(h->etype, (k_elem<ET><<<grid, 128, 0, s>>>(a)));
-  prof_end(h, DNL_PROF_ELEM, s);
   launch_counter()++;
+  // further element groups: same pass, their own element type (one material: the power law or
+  // the general instance as above)
+  for (int gi = 0; gi < h->nextra; gi++) {
+    const ElemGroup &g = h->extra[gi];
+    ElemArgs b = group_args(h, g);
+    b.gate = gate;
+    const int gg = (int)(((long)g.E * g.nip + 127) / 128);
+    if (general)
+      DNL_BY_ETYPE(g.etype, (k_elem<ET, false, true><<<gg, 128, 0, s>>>(b)));
+    else
+      DNL_BY_ETYPE(g.etype, (k_elem<ET><<<gg, 128, 0, s>>>(b)));
+    launch_counter()++;
+  }
+  prof_end(h, DNL_PROF_ELEM, s);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
 
 // the element pass with its per-integration-point record (forward-mode sensitivities)
 int launch_elem_tape(dnl_handle *h, cudaStream_t s, double *tape)
 {
-  if (!etype_has_sens(h->etype)) return DNL_ERR_ARG;
+  if (!etype_has_sens(h->etype) || h->nextra) return DNL_ERR_ARG;
   ElemArgs a = elem_args(h);
   a.gate = 1;
   a.tape = tape;
@@ -1536,6 +1567,13 @@ int launch_mass(dnl_handle *h, cudaStream_t s, double *me)
   const int grid = (int)((threads + 127) / 128);
   DNL_BY_ETYPE(h->etype, (k_mass<ET><<<grid, 128, 0, s>>>(a, me, h->elemMat, h->dmats)));
   launch_counter()++;
+  for (int gi = 0; gi < h->nextra; gi++) {
+    const ElemGroup &g = h->extra[gi];
+    ElemArgs b = group_args(h, g);
+    const int gg = (int)(((long)g.E * g.nip + 127) / 128);
+    DNL_BY_ETYPE(g.etype, (k_mass<ET><<<gg, 128, 0, s>>>(b, me + g.feOff, nullptr, nullptr)));
+    launch_counter()++;
+  }
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
 
@@ -1615,17 +1653,21 @@ ElemArgs elem_args_of(dnl_handle *h) { return elem_args(h); }
 
 int launch_courant(dnl_handle *h, cudaStream_t s)
 {
-  ElemArgs a = elem_args(h);
   prof_begin(h, s);
-  const int kind = etype_length_kind(h->etype), grid = (h->E + 255) / 256;
-  if (kind == 0)
-    k_courant<0><<<grid, 256, 0, s>>>(a);
-  else if (kind == 1)
-    k_courant<1><<<grid, 256, 0, s>>>(a);
-  else
-    k_courant<2><<<grid, 256, 0, s>>>(a);
+  // every element group's lengths into the one minimum (its kernels reduce into the time record)
+  for (int gi = -1; gi < h->nextra; gi++) {
+    const ElemArgs a = gi < 0 ? elem_args(h) : group_args(h, h->extra[gi]);
+    const int et = gi < 0 ? h->etype : h->extra[gi].etype;
+    const int kind = etype_length_kind(et), grid = (a.E + 255) / 256;
+    if (kind == 0)
+      k_courant<0><<<grid, 256, 0, s>>>(a);
+    else if (kind == 1)
+      k_courant<1><<<grid, 256, 0, s>>>(a);
+    else
+      k_courant<2><<<grid, 256, 0, s>>>(a);
+    launch_counter()++;
+  }
   prof_end(h, DNL_PROF_COURANT, s);
-  launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
 

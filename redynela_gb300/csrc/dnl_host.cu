@@ -235,7 +235,7 @@ GatherArgs gather_args(dnl_handle *h)
 {
   GatherArgs g;
   g.N = h->N;
-  g.EN = h->E * h->nen;
+  g.EN = (int)h->EN;
   g.start = h->n2eStart;
   g.entry = h->n2e;
   g.fe = h->fe;
@@ -261,7 +261,7 @@ int launch_node(dnl_handle *h, bool keepFint)
 {
   NodeArgs g;
   g.N = h->N;
-  g.EN = h->E * h->nen;
+  g.EN = (int)h->EN;
   g.start = h->n2eStart;
   g.entry = h->n2e;
   g.fe = h->fe;
@@ -359,7 +359,7 @@ int launch_node_batch(dnl_handle *h, const int *nodeInst, const InstParams *prm,
 {
   NodeArgs g;
   g.N = h->N;
-  g.EN = h->E * h->nen;
+  g.EN = (int)h->EN;
   g.start = h->n2eStart;
   g.entry = h->n2e;
   g.fe = h->fe;
@@ -682,6 +682,12 @@ int dnl_destroy(dnl_handle *h)
                   h->matTab, h->evpn0};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  for (int gi = 0; gi < h->nextra; gi++) {
+    void *gp[] = {h->extra[gi].conn, h->extra[gi].ip, h->extra[gi].detJ, h->extra[gi].pj, h->extra[gi].Cs};
+    for (void *p : gp)
+      if (p) cudaFree(p);
+  }
+  delete[] h->extra;
   for (int i = 0; i < 8; i++)
     if (h->marks[i]) cudaEventDestroy(h->marks[i]);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -701,6 +707,7 @@ int dnl_destroy(dnl_handle *h)
 
 int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, const int *elem_material)
 {
+  if (h && h->nextra) return DNL_ERR_ARG;  // a domain of several element types holds one material
   if (!h || nmat < 1 || !mats || h->prologueDone) return DNL_ERR_ARG;
   if (nmat > 1 && !elem_material) return DNL_ERR_ARG;
   if (nmat > 1 && h->method == DNL_PULSE) return DNL_ERR_ARG;  // one Hooke matrix per handle
@@ -808,7 +815,7 @@ int dnl_set_hourglass(dnl_handle *h, double coefficient)
 int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0)
 {
   if (!h) return DNL_ERR_ARG;
-  if (mat && (h->nmat > 1 || h->mat.hard.law != DNL_HARD_POWER)) return DNL_ERR_ARG;
+  if (mat && (h->nmat > 1 || h->mat.hard.law != DNL_HARD_POWER || h->nextra)) return DNL_ERR_ARG;
   cudaStream_t s = h->stream;
   CK(cudaStreamSynchronize(s));
   for (int i = 0; i < h->ngraphs; i++) cudaGraphExecDestroy(h->graphs[i].exec);
@@ -847,6 +854,15 @@ int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0)
     k_fill<<<(unsigned)((nIP + 255) / 256), 256, 0, s>>>(h->ip + (size_t)(3 * ns + 2) * nIP, nIP,
                                                          h->mat.hard.law == DNL_HARD_POWER ? pow(1e-10, h->mat.n) : 0.);
   launch_counter() += 2;
+  for (int gi = 0; gi < h->nextra; gi++) {  // further element groups: one power-law material
+    const ElemGroup &g = h->extra[gi];
+    const int gns = etype_ns(g.etype), gnc = 3 * gns + 3;
+    CK(cudaMemsetAsync(g.ip, 0, sizeof(double) * gnc * g.nIP, s));
+    k_fill<<<(unsigned)((g.nIP + 255) / 256), 256, 0, s>>>(g.ip + (size_t)(3 * gns + 1) * g.nIP, g.nIP, 1e-10);
+    k_fill<<<(unsigned)((g.nIP + 255) / 256), 256, 0, s>>>(g.ip + (size_t)(3 * gns + 2) * g.nIP, g.nIP,
+                                                           pow(1e-10, h->mat.n));
+    launch_counter() += 2;
+  }
   CK(cudaMemsetAsync(h->fint, 0, sizeof(double) * h->dim * N, s));
   if (h->stepT) CK(cudaMemsetAsync(h->stepT, 0, sizeof(double) * 18 * nIP, s));
   DevTime t;
@@ -906,6 +922,7 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
   h->N = N;
   h->E = E;
   h->nIP = E * h->nip;
+  h->EN = (long)E * nen;
   h->flags = sp->flags;
   h->freq = sp->frequency;
   h->method = sp->method;
@@ -1094,7 +1111,215 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
   return 0;
 }
 
+// ------------------------------------------------------------------------------ element groups
+namespace {
+bool solid_reference_element(int etype)
+{
+  return etype == DNL_ELHEX8N3D || etype == DNL_ELTET4N3D || etype == DNL_ELTET10N3D;
+}
+
+// every element group's connectivity, node-major per element, in element order
+int all_connectivity(dnl_handle *h, std::vector<int> &conn, std::vector<int> &nenOf)
+{
+  conn.clear();
+  nenOf.clear();
+  for (int gi = -1; gi < h->nextra; gi++) {
+    const int E = gi < 0 ? h->E : h->extra[gi].E, nen = gi < 0 ? h->nen : h->extra[gi].nen;
+    const int *dc = gi < 0 ? h->conn : h->extra[gi].conn;
+    std::vector<int> t((size_t)nen * E);
+    CK(cudaMemcpy(t.data(), dc, sizeof(int) * t.size(), cudaMemcpyDeviceToHost));
+    for (int e = 0; e < E; e++) {
+      for (int k = 0; k < nen; k++) conn.push_back(t[(size_t)k * E + e]);
+      nenOf.push_back(nen);
+    }
+  }
+  return 0;
+}
+}  // namespace
+
+int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn)
+{
+  if (!h || !conn || num_elements <= 0 || !etype_valid(etype)) return DNL_ERR_ARG;
+  // before the run starts: the lumped mass, the first time step and the element numbering cover
+  // every group
+  if (h->prologueDone || h->hostIncrement) return DNL_ERR_ARG;
+  // one family (Domain.C:1042-1060): the 3D reference elements; ElHex8n3D has no Courant length
+  if (!solid_reference_element(h->etype) || !solid_reference_element(etype)) return DNL_ERR_ARG;
+  if (h->method == DNL_COURANT && etype == DNL_ELHEX8N3D) return DNL_ERR_ARG;
+  // one material; no sensitivity or adjoint state, no per-step tensors
+  if (h->elemMat || h->nmat > 1 || h->mat.hard.law != DNL_HARD_POWER || h->sens || h->adj || h->stepT)
+    return DNL_ERR_ARG;
+  const int nen = etype_nen(etype), nip = etype_nip(etype), N = h->N, E = num_elements;
+  for (long i = 0; i < (long)E * nen; i++)
+    if (conn[i] < 0 || conn[i] >= N) return DNL_ERR_ARG;
+  CK(cudaStreamSynchronize(h->stream));
+  for (int i = 0; i < h->ngraphs; i++) cudaGraphExecDestroy(h->graphs[i].exec);
+  h->ngraphs = 0;
+
+  ElemGroup g;
+  memset(&g, 0, sizeof g);
+  g.etype = etype;
+  g.nen = nen;
+  g.nip = nip;
+  g.E = E;
+  g.nIP = (long)E * nip;
+  g.feOff = h->EN;
+  auto fail = [&](int code) {
+    void *gp[] = {g.conn, g.ip, g.detJ, g.pj, g.Cs};
+    for (void *p : gp)
+      if (p) cudaFree(p);
+    return code;
+  };
+#define CKG(call)                                                                             \
+  do {                                                                                        \
+    cudaError_t err_ = (call);                                                                \
+    if (err_ != cudaSuccess) {                                                                \
+      snprintf(g_lastError, sizeof g_lastError, "%s: %s", #call, cudaGetErrorString(err_));  \
+      return fail(DNL_ERR_CUDA);                                                              \
+    }                                                                                         \
+  } while (0)
+  {
+    std::vector<int> connT((size_t)nen * E);
+    for (int e = 0; e < E; e++)
+      for (int k = 0; k < nen; k++) connT[(size_t)k * E + e] = conn[(size_t)e * nen + k];
+    CKG(cudaMalloc(&g.conn, sizeof(int) * connT.size()));
+    CKG(cudaMemcpy(g.conn, connT.data(), sizeof(int) * connT.size(), cudaMemcpyHostToDevice));
+  }
+  // integration points at rest: zero stresses and strains, evp = 1e-10 (IntegrationPoint.C:117)
+  const int ns = etype_ns(etype), ncomp = 3 * ns + 3;  // IpLayout::NCOMP (ns = 6 for every solid)
+  CKG(cudaMalloc(&g.ip, sizeof(double) * (size_t)ncomp * g.nIP));
+  CKG(cudaMemset(g.ip, 0, sizeof(double) * (size_t)ncomp * g.nIP));
+  {
+    std::vector<double> v(g.nIP, 1e-10);
+    CKG(cudaMemcpy(g.ip + (size_t)(3 * ns + 1) * g.nIP, v.data(), sizeof(double) * g.nIP, cudaMemcpyHostToDevice));
+    const double pn = pow(1e-10, h->mat.n);
+    for (auto &x : v) x = pn;
+    CKG(cudaMemcpy(g.ip + (size_t)(3 * ns + 2) * g.nIP, v.data(), sizeof(double) * g.nIP, cudaMemcpyHostToDevice));
+  }
+  CKG(cudaMalloc(&g.detJ, sizeof(double) * g.nIP));
+  if (h->method == DNL_PULSE) CKG(cudaMalloc(&g.pj, sizeof(double) * (size_t)(h->dim * h->dim + 2) * g.nIP));
+  // Courant: Element::getSoundSpeed averages the element's nodal densities over its own node
+  // count, which can round differently for another element type; then every element's length is
+  // divided by its own group's speed before the minimum (Domain::computeCourantTimeStep)
+  dnl_material dm;
+  dm.young = h->mat.young;
+  dm.poisson = h->mat.nu;
+  dm.density = h->mat.rho;
+  dm.A = h->mat.A;
+  dm.B = h->mat.B;
+  dm.n = h->mat.n;
+  const double csG = make_material(dm, nen).Cs;
+  bool perElementCs = h->method == DNL_COURANT && csG != h->mat.Cs;
+  for (int gi = 0; gi < h->nextra; gi++) perElementCs |= h->extra[gi].Cs != nullptr;
+
+  // element-force and Pulse-product arrays over the slots of every group; the node -> slot map
+  const long EN = h->EN + (long)E * nen;
+  double *fe = nullptr, *kx = nullptr, *cs0 = nullptr;
+  int *start = nullptr, *entry = nullptr;
+  auto freeNew = [&]() {
+    void *np[] = {fe, kx, cs0, start, entry};
+    for (void *p : np)
+      if (p) cudaFree(p);
+  };
+#define CKN(call)                                                                             \
+  do {                                                                                        \
+    cudaError_t err_ = (call);                                                                \
+    if (err_ != cudaSuccess) {                                                                \
+      snprintf(g_lastError, sizeof g_lastError, "%s: %s", #call, cudaGetErrorString(err_));  \
+      freeNew();                                                                              \
+      return fail(DNL_ERR_CUDA);                                                              \
+    }                                                                                         \
+  } while (0)
+  CKN(cudaMalloc(&fe, sizeof(double) * (size_t)h->dim * EN));
+  if (h->method == DNL_PULSE) CKN(cudaMalloc(&kx, sizeof(double) * (size_t)h->dim * EN));
+  {
+    std::vector<int> all, nenOf;
+    if (all_connectivity(h, all, nenOf)) {
+      freeNew();
+      return fail(DNL_ERR_CUDA);
+    }
+    for (int e = 0; e < E; e++) {
+      for (int k = 0; k < nen; k++) all.push_back(conn[(size_t)e * nen + k]);
+      nenOf.push_back(nen);
+    }
+    // node -> element-node slot, ascending element order (the slots of element e are its first
+    // slot + k, elements of every group one after another)
+    std::vector<int> st(N + 1, 0), en(all.size()), fill(N, 0);
+    for (size_t i = 0; i < all.size(); i++) st[all[i] + 1]++;
+    for (int n = 0; n < N; n++) st[n + 1] += st[n];
+    size_t slot = 0;
+    for (size_t e = 0; e < nenOf.size(); e++)
+      for (int k = 0; k < nenOf[e]; k++, slot++) {
+        const int n = all[slot];
+        en[st[n] + fill[n]++] = (int)slot;
+      }
+    CKN(cudaMalloc(&start, sizeof(int) * (N + 1)));
+    CKN(cudaMalloc(&entry, sizeof(int) * en.size()));
+    CKN(cudaMemcpy(start, st.data(), sizeof(int) * (N + 1), cudaMemcpyHostToDevice));
+    CKN(cudaMemcpy(entry, en.data(), sizeof(int) * en.size(), cudaMemcpyHostToDevice));
+  }
+  if (perElementCs) {
+    // the first group's and each group's own speed per element
+    if (!h->elemCs) {
+      std::vector<double> v(h->E, h->mat.Cs);
+      CKN(cudaMalloc(&cs0, sizeof(double) * h->E));
+      CKN(cudaMemcpy(cs0, v.data(), sizeof(double) * h->E, cudaMemcpyHostToDevice));
+    }
+    std::vector<double> v(E, csG);
+    CKN(cudaMalloc(&g.Cs, sizeof(double) * E));
+    CKN(cudaMemcpy(g.Cs, v.data(), sizeof(double) * E, cudaMemcpyHostToDevice));
+    for (int gi = 0; gi < h->nextra; gi++)
+      if (!h->extra[gi].Cs) {
+        dnl_material dg = dm;
+        std::vector<double> w(h->extra[gi].E, make_material(dg, h->extra[gi].nen).Cs);
+        CKN(cudaMalloc(&h->extra[gi].Cs, sizeof(double) * w.size()));
+        CKN(cudaMemcpy(h->extra[gi].Cs, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice));
+      }
+  }
+#undef CKN
+#undef CKG
+  // commit
+  cudaFree(h->fe);
+  h->fe = fe;
+  if (kx) {
+    cudaFree(h->kx);
+    h->kx = kx;
+  }
+  if (cs0) h->elemCs = cs0;
+  cudaFree(h->n2eStart);
+  cudaFree(h->n2e);
+  h->n2eStart = start;
+  h->n2e = entry;
+  ElemGroup *grown = new ElemGroup[h->nextra + 1];
+  for (int gi = 0; gi < h->nextra; gi++) grown[gi] = h->extra[gi];
+  grown[h->nextra] = g;
+  delete[] h->extra;
+  h->extra = grown;
+  h->nextra++;
+  h->EN = EN;
+  return 0;
+}
+
 // ------------------------------------------------------------------------------ state access
+namespace {
+// the integration points of each element group: its device state (component-major over its own
+// points) and its first point in the element order of the host arrays
+struct IpSeg {
+  double *ip;
+  size_t nIP, off;
+};
+std::vector<IpSeg> ip_segments(dnl_handle *h)
+{
+  std::vector<IpSeg> v{{h->ip, (size_t)h->nIP, 0}};
+  size_t off = h->nIP;
+  for (int gi = 0; gi < h->nextra; gi++) {
+    v.push_back({h->extra[gi].ip, (size_t)h->extra[gi].nIP, off});
+    off += h->extra[gi].nIP;
+  }
+  return v;
+}
+}  // namespace
+
 int dnl_set_state(dnl_handle *h, const dnl_state_view *s)
 {
   if (!h || !s) return DNL_ERR_ARG;
@@ -1116,27 +1341,29 @@ int dnl_set_state(dnl_handle *h, const dnl_state_view *s)
       launch_counter()++;
       if ((r = check_launch())) return r;
     }
-  const int ns = etype_ns(h->etype);
+  const int ns = etype_ns(h->etype);  // the same for every group of a domain (one family)
   const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
-  const size_t nIP = h->nIP;
   CK(cudaStreamSynchronize(h->stream));
   if (!(s->S || s->Eps || s->EpsPlas || s->p || s->evp)) return 0;
-  std::vector<double> ib(nIP);
-  auto putT = [&](const double *src, int base) -> int {
-    for (int k = 0; k < ns; k++) {
-      for (size_t i = 0; i < nIP; i++) ib[i] = src[9 * i + 3 * I0[k] + I1[k]];
-      CK(cudaMemcpy(h->ip + (size_t)(base + k) * nIP, ib.data(), sizeof(double) * nIP, cudaMemcpyHostToDevice));
+  for (const IpSeg &g : ip_segments(h)) {
+    const size_t nIP = g.nIP, o = g.off;
+    std::vector<double> ib(nIP);
+    auto putT = [&](const double *src, int base) -> int {
+      for (int k = 0; k < ns; k++) {
+        for (size_t i = 0; i < nIP; i++) ib[i] = src[9 * (o + i) + 3 * I0[k] + I1[k]];
+        CK(cudaMemcpy(g.ip + (size_t)(base + k) * nIP, ib.data(), sizeof(double) * nIP, cudaMemcpyHostToDevice));
+      }
+      return 0;
+    };
+    if (s->S && (r = putT(s->S, 0))) return r;
+    if (s->Eps && (r = putT(s->Eps, ns))) return r;
+    if (s->EpsPlas && (r = putT(s->EpsPlas, 2 * ns))) return r;
+    if (s->p) CK(cudaMemcpy(g.ip + (size_t)(3 * ns) * nIP, s->p + o, sizeof(double) * nIP, cudaMemcpyHostToDevice));
+    if (s->evp) {
+      CK(cudaMemcpy(g.ip + (size_t)(3 * ns + 1) * nIP, s->evp + o, sizeof(double) * nIP, cudaMemcpyHostToDevice));
+      for (size_t i = 0; i < nIP; i++) ib[i] = pow(s->evp[o + i], h->mat.n);
+      CK(cudaMemcpy(g.ip + (size_t)(3 * ns + 2) * nIP, ib.data(), sizeof(double) * nIP, cudaMemcpyHostToDevice));
     }
-    return 0;
-  };
-  if (s->S && (r = putT(s->S, 0))) return r;
-  if (s->Eps && (r = putT(s->Eps, ns))) return r;
-  if (s->EpsPlas && (r = putT(s->EpsPlas, 2 * ns))) return r;
-  if (s->p) CK(cudaMemcpy(h->ip + (size_t)(3 * ns) * nIP, s->p, sizeof(double) * nIP, cudaMemcpyHostToDevice));
-  if (s->evp) {
-    CK(cudaMemcpy(h->ip + (size_t)(3 * ns + 1) * nIP, s->evp, sizeof(double) * nIP, cudaMemcpyHostToDevice));
-    for (size_t i = 0; i < nIP; i++) ib[i] = pow(s->evp[i], h->mat.n);
-    CK(cudaMemcpy(h->ip + (size_t)(3 * ns + 2) * nIP, ib.data(), sizeof(double) * nIP, cudaMemcpyHostToDevice));
   }
   return 0;
 }
@@ -1164,31 +1391,34 @@ int dnl_get_state(dnl_handle *h, dnl_state_view *s)
   CK(cudaStreamSynchronize(h->stream));
   if (s->mass) CK(cudaMemcpy(s->mass, h->mass, sizeof(double) * N, cudaMemcpyDeviceToHost));
   if (!(s->S || s->Eps || s->EpsPlas || s->p || s->evp || s->Sig)) return 0;
-  const int ns = etype_ns(h->etype);
+  const int ns = etype_ns(h->etype);  // the same for every group of a domain (one family)
   const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
-  const size_t nIP = h->nIP;
-  std::vector<double> ib(nIP), pb(nIP);
-  auto getT = [&](double *dst, int base, const double *addP) -> int {
-    for (size_t i = 0; i < 9 * nIP; i++) dst[i] = 0.;
-    for (int k = 0; k < ns; k++) {
-      CK(cudaMemcpy(ib.data(), h->ip + (size_t)(base + k) * nIP, sizeof(double) * nIP, cudaMemcpyDeviceToHost));
-      for (size_t i = 0; i < nIP; i++) {
-        dst[9 * i + 3 * I0[k] + I1[k]] = ib[i];
-        dst[9 * i + 3 * I1[k] + I0[k]] = ib[i];
+  for (const IpSeg &g : ip_segments(h)) {
+    const size_t nIP = g.nIP, o = g.off;
+    std::vector<double> ib(nIP), pb(nIP);
+    auto getT = [&](double *dst, int base, const double *addP) -> int {
+      dst += 9 * o;
+      for (size_t i = 0; i < 9 * nIP; i++) dst[i] = 0.;
+      for (int k = 0; k < ns; k++) {
+        CK(cudaMemcpy(ib.data(), g.ip + (size_t)(base + k) * nIP, sizeof(double) * nIP, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < nIP; i++) {
+          dst[9 * i + 3 * I0[k] + I1[k]] = ib[i];
+          dst[9 * i + 3 * I1[k] + I0[k]] = ib[i];
+        }
       }
-    }
-    if (addP)
-      for (size_t i = 0; i < nIP; i++)
-        for (int d = 0; d < 3; d++) dst[9 * i + 4 * d] += addP[i];
-    return 0;
-  };
-  if (s->S && (r = getT(s->S, 0, nullptr))) return r;
-  if (s->Eps && (r = getT(s->Eps, ns, nullptr))) return r;
-  if (s->EpsPlas && (r = getT(s->EpsPlas, 2 * ns, nullptr))) return r;
-  if (s->p || s->Sig) CK(cudaMemcpy(pb.data(), h->ip + (size_t)(3 * ns) * nIP, sizeof(double) * nIP, cudaMemcpyDeviceToHost));
-  if (s->p) memcpy(s->p, pb.data(), sizeof(double) * nIP);
-  if (s->Sig && (r = getT(s->Sig, 0, pb.data()))) return r;
-  if (s->evp) CK(cudaMemcpy(s->evp, h->ip + (size_t)(3 * ns + 1) * nIP, sizeof(double) * nIP, cudaMemcpyDeviceToHost));
+      if (addP)
+        for (size_t i = 0; i < nIP; i++)
+          for (int d = 0; d < 3; d++) dst[9 * i + 4 * d] += addP[i];
+      return 0;
+    };
+    if (s->S && (r = getT(s->S, 0, nullptr))) return r;
+    if (s->Eps && (r = getT(s->Eps, ns, nullptr))) return r;
+    if (s->EpsPlas && (r = getT(s->EpsPlas, 2 * ns, nullptr))) return r;
+    if (s->p || s->Sig) CK(cudaMemcpy(pb.data(), g.ip + (size_t)(3 * ns) * nIP, sizeof(double) * nIP, cudaMemcpyDeviceToHost));
+    if (s->p) memcpy(s->p + o, pb.data(), sizeof(double) * nIP);
+    if (s->Sig && (r = getT(s->Sig, 0, pb.data()))) return r;
+    if (s->evp) CK(cudaMemcpy(s->evp + o, g.ip + (size_t)(3 * ns + 1) * nIP, sizeof(double) * nIP, cudaMemcpyDeviceToHost));
+  }
   return 0;
 }
 
@@ -1249,7 +1479,7 @@ int dnl_prologue(dnl_handle *h)
   int r;
   // computeMassMatrix (ExplicitSolverCH.C:145): per-element lumped masses, gathered per node
   double *me;
-  CK(cudaMalloc(&me, sizeof(double) * (size_t)h->E * h->nen));
+  CK(cudaMalloc(&me, sizeof(double) * (size_t)h->EN));
   if ((r = launch_mass(h, h->stream, me))) {
     cudaFree(me);
     return r;

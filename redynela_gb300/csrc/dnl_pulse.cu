@@ -117,7 +117,8 @@ struct PulseArgs {
   const double *x[3];
   double *pj;        // [DIM*DIM + 2][nIP]: J^-1 (row-major), W, R
   double *ev;        // raw iterate [N*DIM]; the normalised vector is ev / tm->pulseScale
-  double *kx;        // element products [DIM][E*NEN]
+  double *kx;        // element products: component i of element e's node k at kx[i kxStride + e NEN + k]
+  long kxStride;     // element-node slots of the handle's element groups
   const int *start, *entry;
   const double *mass;
   DevTime *tm;
@@ -361,7 +362,7 @@ __global__ void __launch_bounds__(128) k_pulse_kx(PulseArgs a)
         if (AXI) f[0] = fma(pN<ET>(q, pt), Mq[DIM * DIM], f[0]);
       }
 #pragma unroll
-      for (int i = 0; i < DIM; i++) a.kx[(long)i * a.E * NEN + (long)e * NEN + pt] = f[i];
+      for (int i = 0; i < DIM; i++) a.kx[(long)i * a.kxStride + (long)e * NEN + pt] = f[i];
     }
     return;
   }
@@ -388,7 +389,7 @@ __global__ void __launch_bounds__(128) k_pulse_kx(PulseArgs a)
           double s = 0.;
 #pragma unroll
           for (int q = 0; q < NIP; q++) s += red[wib][slot][q][k * DIM + i];
-          a.kx[(long)i * a.E * NEN + (long)e * NEN + k] = s;
+          a.kx[(long)i * a.kxStride + (long)e * NEN + k] = s;
         }
       }
     }
@@ -491,6 +492,7 @@ int launch_pulse(dnl_handle *h, cudaStream_t s)
   a.pj = h->pj;
   a.ev = h->ev;
   a.kx = h->kx;
+  a.kxStride = h->EN;
   a.start = h->n2eStart;
   a.entry = h->n2e;
   a.mass = h->mass;
@@ -518,24 +520,39 @@ int launch_pulse(dnl_handle *h, cudaStream_t s)
   const long nthreads = (long)h->E * h->nip;
   const int gridIP = (int)((nthreads + 127) / 128);
   const int gridN = (h->N + 255) / 256;
+  // further element groups: their own element type, connectivity, kinematics and product slots
+  std::vector<PulseArgs> ga(h->nextra, a);
+  for (int gi = 0; gi < h->nextra; gi++) {
+    const ElemGroup &g = h->extra[gi];
+    ga[gi].E = g.E;
+    ga[gi].conn = g.conn;
+    ga[gi].pj = g.pj;
+    ga[gi].kx = h->kx + g.feOff;
+    if (!g.pj) return DNL_ERR_ARG;
+  }
+  auto gridOf = [](const ElemGroup &g) { return (int)(((long)g.E * g.nip + 127) / 128); };
   prof_begin(h, s);
   k_pulse_begin<<<1, 1, 0, s>>>(h->tm);
   DNL_BY_ETYPE(h->etype, (k_pulse_setup<ET><<<gridIP, 128, 0, s>>>(a)));
+  for (int gi = 0; gi < h->nextra; gi++)
+    DNL_BY_ETYPE(h->extra[gi].etype, (k_pulse_setup<ET><<<gridOf(h->extra[gi]), 128, 0, s>>>(ga[gi])));
   prof_end(h, DNL_PROF_PULSE, s);
-  launch_counter() += 2;
+  launch_counter() += 2 + h->nextra;
   const int batch = 4;
   for (int round = 0; round < (pulse_cap() + batch) / batch + 1; round++) {
     for (int b = 0; b < batch; b++) {
       prof_begin(h, s);
       DNL_BY_ETYPE(h->etype, (k_pulse_kx<ET><<<gridIP, 128, 0, s>>>(a)));
+      for (int gi = 0; gi < h->nextra; gi++)
+        DNL_BY_ETYPE(h->extra[gi].etype, (k_pulse_kx<ET><<<gridOf(h->extra[gi]), 128, 0, s>>>(ga[gi])));
       if (h->dim == 2) {
-        k_pulse_gather<2><<<gridN, 256, 0, s>>>(a, h->E * h->nen);
+        k_pulse_gather<2><<<gridN, 256, 0, s>>>(a, (int)h->EN);
       } else {
-        k_pulse_gather<3><<<gridN, 256, 0, s>>>(a, h->E * h->nen);
+        k_pulse_gather<3><<<gridN, 256, 0, s>>>(a, (int)h->EN);
       }
       k_pulse_check<<<1, 1, 0, s>>>(h->tm, pulse_cap());
       prof_end(h, DNL_PROF_PULSE, s);
-      launch_counter() += 3;
+      launch_counter() += 3 + h->nextra;
     }
     if (cudaPeekAtLastError() != cudaSuccess) return DNL_ERR_CUDA;
     if (cudaMemcpyAsync(&t, h->tm, sizeof t, cudaMemcpyDeviceToHost, s) != cudaSuccess) return DNL_ERR_CUDA;

@@ -150,7 +150,7 @@ int dnl_write_results(dnl_handle *h, const char *path)
 
 int dnl_read_results(dnl_handle *h, const char *path)
 {
-  if (!h || !path) return DNL_ERR_ARG;
+  if (!h || !path || h->nextra) return DNL_ERR_ARG;
   FILE *f = fopen(path, "rb");
   if (!f) return DNL_ERR_ARG;
   std::vector<double> data;

@@ -258,7 +258,7 @@ int sens_alloc(dnl_handle *h, SensState *S)
 int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt)
 {
   // the tangent formulas are those of the power law and one material (per instance in a batch)
-  if (!etype_has_sens(h->etype)) return DNL_ERR_ARG;
+  if (!etype_has_sens(h->etype) || h->nextra) return DNL_ERR_ARG;
   if (!bt && (h->elemMat || h->mat.hard.law != DNL_HARD_POWER)) return DNL_ERR_ARG;
   for (int k = 0; k < nsteps; k++)
     if (!(dts[k] > 0. && dts[k] < 1e300)) return DNL_ERR_ARG;

@@ -98,6 +98,7 @@ extern "C" int dnl_internal_forces_static(const dnl_static_args *a, void *stream
   }
   ea.ip = a->ip;
   ea.fe = sp->fe;
+  ea.feStride = (long)E * nen;
   ea.detJ = nullptr;
   ea.stepT = nullptr;
   ea.tm = sp->tm;

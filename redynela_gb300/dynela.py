@@ -104,6 +104,7 @@ def lib():
                                  C.POINTER(SolverParams), C.POINTER(H)]
         L.dnl_destroy.argtypes = [H]
         L.dnl_set_hourglass.argtypes = [H, C.c_double]
+        L.dnl_add_elements.argtypes = [H, C.c_int, C.c_int, _ip]
         L.dnl_set_state.argtypes = [H, C.POINTER(StateView)]
         L.dnl_get_state.argtypes = [H, C.POINTER(StateView)]
         L.dnl_get_step_tensors.argtypes = [H, _dp, _dp]
@@ -277,6 +278,16 @@ class GpuDomain:
             self.set_state(v=np.asarray(m.initial_velocity, dtype=np.float64))
         if m.etype == meshes.ELHEX8N3D_1PT:
             self.set_hourglass(m.hourglass)
+        self._groups = []
+        for etype, conn in (m.groups or []):
+            self.add_elements(etype, conn)
+
+    def add_elements(self, etype: int, conn) -> None:
+        """dnl_add_elements: a further group of elements of another type in this domain, numbered
+        after the elements already there (before the prologue)."""
+        c = np.ascontiguousarray(conn, dtype=np.int32)
+        self._groups.append(c)
+        self._check(self.L.dnl_add_elements(self.h, int(etype), int(c.shape[0]), c.ctypes.data_as(_ip)))
 
     def set_hourglass(self, coefficient: float) -> None:
         """dnl_set_hourglass: the one-point hexahedron's viscous hourglass coefficient."""
@@ -335,12 +346,15 @@ class GpuDomain:
         self._check(self.L.dnl_set_state(self.h, C.byref(sv)))
 
     def get_state(self, *names: str) -> Dict[str, np.ndarray]:
+        """Nodal fields (N, 3); integration-point fields (E, nip, ...) with one element type, or
+        (nIP, ...) over every group in element order with several."""
         m = self.model
         nI = m.E * m.nip
+        ip = (m.nIP_all,) if m.groups else (m.E, m.nip)
         shapes = {"coords": (m.N, 3), "du": (m.N, 3), "v": (m.N, 3), "a": (m.N, 3),
-                  "disp": (m.N, 3), "S": (m.E, m.nip, 3, 3), "Eps": (m.E, m.nip, 3, 3),
-                  "EpsPlas": (m.E, m.nip, 3, 3), "Sig": (m.E, m.nip, 3, 3), "p": (m.E, m.nip),
-                  "evp": (m.E, m.nip), "mass": (m.N,)}
+                  "disp": (m.N, 3), "S": ip + (3, 3), "Eps": ip + (3, 3),
+                  "EpsPlas": ip + (3, 3), "Sig": ip + (3, 3), "p": ip,
+                  "evp": ip, "mass": (m.N,)}
         names = names or tuple(shapes)
         out = {n: np.zeros(shapes[n]) for n in names}
         sv = StateView()

@@ -17,13 +17,15 @@ Generators:
   z; base restrained in z; Pulse time step (hex8 has no Courant length in the reference,
   finiteElement/ElHex8n3D.C:188-192).
 * :func:`taylor_batch` -- seeded parameter draws for many independent axisymmetric Taylor bars.
+* :func:`taylor_mixed` -- a 3D bar of two element types in one domain: hexahedra at the impact
+  end, tetrahedra above.
 """
 
 from __future__ import annotations
 
 import dataclasses
 from dataclasses import dataclass, field
-from typing import List, Optional, Sequence
+from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -34,6 +36,8 @@ ELTET4N3D = 3
 ELTET10N3D = 4
 # not a reference element: ElHex8n3D at its centre with viscous hourglass control
 ELHEX8N3D_1PT = 5
+NEN_OF = {ELQUA4NAX: 4, ELHEX8N3D: 8, ELQUA4N2D: 4, ELTET4N3D: 4, ELTET10N3D: 10, ELHEX8N3D_1PT: 8}
+NIP_OF = {ELQUA4NAX: 4, ELHEX8N3D: 8, ELQUA4N2D: 4, ELTET4N3D: 1, ELTET10N3D: 4, ELHEX8N3D_1PT: 1}
 
 COURANT = 0
 PULSE = 1
@@ -105,6 +109,10 @@ class Model:
     initial_velocity: Optional[np.ndarray] = None
     # ELHEX8N3D_1PT only: the viscous hourglass coefficient
     hourglass: float = 0.05
+    # further element groups of other types of the same family, [(etype, conn (E_g, nen_g))],
+    # numbered after the elements of `conn` in this order (a deck's setDefaultElement +
+    # createElement for each further type); etype/conn above are the first group
+    groups: Optional[List[Tuple[int, np.ndarray]]] = None
 
     def material_laws(self) -> List[MaterialLaw]:
         if self.materials:
@@ -120,6 +128,20 @@ class Model:
     @property
     def N(self) -> int:
         return int(self.coords.shape[0])
+
+    def element_groups(self) -> List[Tuple[int, np.ndarray]]:
+        """Every element group, the first one included: [(etype, conn)]."""
+        return [(self.etype, self.conn)] + list(self.groups or [])
+
+    @property
+    def E_all(self) -> int:
+        """Elements of all groups."""
+        return int(sum(c.shape[0] for _, c in self.element_groups()))
+
+    @property
+    def nIP_all(self) -> int:
+        """Integration points of all groups."""
+        return int(sum(c.shape[0] * NIP_OF[t] for t, c in self.element_groups()))
 
     @property
     def E(self) -> int:
@@ -258,6 +280,40 @@ def taylor_hex_1pt(ncross: int = 40, nz: int = 400, hourglass: float = 0.05, **k
     control (ELHEX8N3D_1PT, not a reference element), Courant time step."""
     return dataclasses.replace(taylor_hex(ncross, nz, **kw), etype=ELHEX8N3D_1PT, method=COURANT,
                                hourglass=hourglass)
+
+
+def taylor_mixed(ncross: int = 6, nz: int = 12, nz_lower: int = 6, lower: int = ELTET4N3D,
+                 upper: int = ELTET10N3D, **kw) -> Model:
+    """One 3D domain of two element types (Domain::initSolve accepts any mix of one family,
+    Domain.C:1042-1060): the cells of taylor_hex(ncross, nz) in the `nz_lower` layers at the
+    impact end (z = 0) are of type `lower`, the others of type `upper`; a cell of tetrahedra is
+    split in six as in taylor_tet, so the triangles on the interface plane are halves of the faces
+    below or above and the two parts share the interface's corner nodes (ElTet10n3D's mid-edge
+    nodes there belong to its side only).  Elements of `lower` first, then `upper` (a deck's
+    second setDefaultElement); base restrained in z.  Time step: Pulse when a group is ElHex8n3D
+    (no Courant length), else Courant with the safety factor of taylor_tet."""
+    m = taylor_hex(ncross, nz, **kw)
+    ncell = m.E // nz
+    layer = np.arange(m.E) // ncell
+    coords = m.coords
+    groups = []
+    for etype, cells in ((lower, m.conn[layer < nz_lower]), (upper, m.conn[layer >= nz_lower])):
+        if etype == ELHEX8N3D:
+            groups.append((etype, cells.astype(np.int64)))
+            continue
+        tets = np.stack([cells[:, list(t)] for t in _HEX_TO_TETS], axis=1).reshape(-1, 4)
+        if etype == ELTET10N3D:
+            ends = np.stack([np.sort(tets[:, list(ed)], axis=1) for ed in _TET10_EDGES], axis=1)
+            uniq, inv = np.unique(ends.reshape(-1, 2), axis=0, return_inverse=True)
+            mid = coords.shape[0] + inv.reshape(-1, 6)
+            coords = np.concatenate([coords, 0.5 * (coords[uniq[:, 0]] + coords[uniq[:, 1]])])
+            tets = np.concatenate([tets, mid], axis=1)
+        groups.append((etype, tets.astype(np.int64)))
+    hexes = ELHEX8N3D in (lower, upper)
+    method = PULSE if hexes else COURANT
+    safety = kw.get("safety", 0.9 if hexes else 0.5)
+    return dataclasses.replace(m, etype=groups[0][0], coords=coords, conn=groups[0][1],
+                               groups=groups[1:], method=method, safety=safety)
 
 
 def tabular_table(A: float, B: float, n: float, step: float = 0.1, stop: float = 10.0):

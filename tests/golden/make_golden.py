@@ -32,6 +32,11 @@ reference's own output on a seeded synthetic model:
                         time step, lumped mass and its first 30 steps
 * ``run_speed.npz``     the same bar pulled at 5 m/s to 2 ms: final coordinates, velocities, plastic
                         strain
+* ``forces_mixed.npz``  one computeInternalForces on an injected state of a 4x4x3-cell bar of
+                        ElTet4n3D (first layer) and ElHex8n3D (the others) in one domain
+* ``steps_mixed.npz``   the 6x6x12-cell bar of ElTet4n3D (6 layers) and ElTet10n3D (6 layers) in one
+                        domain, Courant time step: lumped mass and its first 5 steps (its ElTet10n3D
+                        part ends in a singular Jacobian a few steps later, as the ElTet10n3D bar)
 
     python tests/golden/make_golden.py
 """
@@ -143,6 +148,25 @@ def speed():
          final_coords=r["final_coords"], final_v=r["final_v"], final_evp=r["final_evp"])
 
 
+def mixed():
+    """The mixed element-type fixtures only: python tests/golden/make_golden.py mixed
+
+    Only what the reference computes soundly: a hexahedron + tetrahedron domain is pinned by one
+    force pass (elements created tetrahedra first; the reverse order, and its Pulse loop, make
+    Vector::redim copy a longer vector into a shorter one, a heap overflow), and the time steps by
+    the ElTet4n3D + ElTet10n3D domain with the Courant step."""
+    m = meshes.taylor_mixed(4, 3, nz_lower=1, lower=meshes.ELTET4N3D, upper=meshes.ELHEX8N3D)
+    st = states.random_state(m, seed=7)
+    r = dnl_io.run_reference("forces", m, state=st)
+    save("forces_mixed.npz", **{f"in_{k}": np.asarray(v) for k, v in st.items()}, fint=r["fint"],
+         **{k: r[k] for k in r if k.startswith("out_")})
+    m = meshes.taylor_mixed(6, 12)
+    r = dnl_io.run_reference("steps", m, 5)
+    save("steps_mixed.npz", mass=r["mass"], dt0=r["dt0"], dt=r["dt"], time=r["time"],
+         kinetic=r["kinetic"], fint=np.stack([r[f"fint_{k:06d}"] for k in range(5)]),
+         final_coords=r["final_coords"], final_S=r["final_S"], final_p=r["final_p"])
+
+
 def main():
     if not dnl_io.reference_available():
         sys.exit("compiled reference missing: run `make -C oracle ref`")
@@ -160,6 +184,9 @@ def main():
         return
     if sys.argv[1:] == ["speed"]:
         speed()
+        return
+    if sys.argv[1:] == ["mixed"]:
+        mixed()
         return
     t = dnl_io.reference_tables()
     save("tables.npz", **t)
@@ -198,6 +225,7 @@ def main():
     plane()
     tets()
     speed()
+    mixed()
 
 
 if __name__ == "__main__":

@@ -1,0 +1,164 @@
+"""Domains of several element types on the GPU (dnl_add_elements): the element pass, the lumped mass,
+the Courant reduction and the Pulse power iteration run once per element group and assemble through
+one node -> element-node map.
+
+Against the reference's own outputs where the reference computes them soundly (tests/golden,
+*mixed*): one force pass on an injected state of an ElTet4n3D + ElHex8n3D domain, and the lumped
+mass, time steps and first steps of an ElTet4n3D + ElTet10n3D domain with the Courant step.  (The
+reference's Pulse loop, and its force loop when a larger element precedes a smaller one, copy a
+longer Vector into a shorter one on such domains -- Vector::redim, linearAlgebra/Vector.C:213-229 --
+a heap overflow, so its hexahedron + tetrahedron runs pin nothing.)  The rest by identities: a
+mesh split into two groups of its own element type runs bit for bit as the single group, and the
+forces of a hexahedron + tetrahedron domain are those of its two parts as separate domains.
+Tolerances as in test_gpu_tets."""
+
+import dataclasses
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import states
+from redynela_gb300 import meshes
+
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL = 1e-12
+STATE_TOL = 1e-12
+TRAJ_TOL = 1e-7
+
+
+def rel(a, b):
+    a, b = np.asarray(a).ravel(), np.asarray(b).ravel()
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / nb if nb > 0 else np.linalg.norm(a - b)
+
+
+def tet_hex_bar():
+    return meshes.taylor_mixed(4, 3, nz_lower=1, lower=meshes.ELTET4N3D, upper=meshes.ELHEX8N3D)
+
+
+def test_mixed_forces_injected_state_vs_reference(gpu_lib):
+    """ElTet4n3D (first layer) + ElHex8n3D (two layers) in one domain, one computeInternalForces
+    on the reference's injected mid-run state: forces and every integration point's new state."""
+    g = golden("forces_mixed.npz")
+    d = gpu_lib.GpuDomain(tet_hex_bar())
+    st = {k[3:]: g[k] for k in g.files if k.startswith("in_")}
+    d.set_state(S=st["S"], Eps=st["Eps"], EpsPlas=st["EpsPlas"], p=st["p"], evp=st["evp"],
+                v=st["v"], a=st["a"], disp=st["disp"])
+    f = d.internal_forces(coords=st["coords"], du=st["du"], dt=float(st["dt"]))
+    assert rel(f, g["fint"]) <= FORCE_TOL
+    out = d.get_state("S", "Eps", "EpsPlas", "p", "evp", "Sig")
+    for k in out:
+        assert rel(out[k], g["out_" + k]) <= STATE_TOL, k
+
+
+def test_mixed_tet4_tet10_steps_vs_reference(gpu_lib):
+    """ElTet4n3D (6 layers) + ElTet10n3D (6 layers), Courant: the lumped mass of both groups
+    assembled bit for bit, the first time step bit for bit (the minimum of both groups' lengths
+    over their sound speeds), then 5 steps: forces and time steps (the second step onwards from the
+    ill-conditioned state ElTet10n3D's tables leave, as in test_tet10_mass_and_first_steps).  The
+    forces stay within 1e-10 to 2e-9 of the reference's over the 5 steps; positions after them to
+    the trajectory tolerance: the tables give some ElTet10n3D nodes negative lumped masses, whose
+    accelerations turn those last-bit differences into 1.6e-8 of the coordinates."""
+    g = golden("steps_mixed.npz")
+    m = meshes.taylor_mixed(6, 12)
+    d = gpu_lib.GpuDomain(m)
+    d.prologue()
+    assert rel(d.get_state("mass")["mass"], g["mass"][::3]) == 0.0
+    assert d.time_step() == g["dt0"][0]
+    for k in range(5):
+        assert d.step(1) == 1
+        assert rel(d.fint(), g["fint"][k]) <= (FORCE_TOL if k == 0 else TRAJ_TOL), k
+        info = d.time_info()
+        assert abs(info["time"] - g["time"][k]) <= 1e-12 * g["time"][k], k
+    st = d.get_state("coords", "S", "p")
+    assert rel(st["coords"], g["final_coords"]) <= TRAJ_TOL
+    assert rel(st["S"], g["final_S"]) <= 1e-6
+    assert rel(st["p"], g["final_p"]) <= 1e-6
+
+
+@pytest.mark.parametrize("kind", ["hex_pulse", "tet4_courant"])
+def test_split_into_groups_is_bitwise_the_single_group(gpu_lib, kind):
+    """A mesh given as two groups of its own element type (the first 40 % of its elements, then
+    the rest through dnl_add_elements) numbers its element-node slots as the single group does, so
+    every kernel sees the same data: 30 steps bit for bit (coordinates, forces, time, state)."""
+    m = meshes.taylor_hex(6, 8) if kind == "hex_pulse" else meshes.taylor_tet(6, 8)
+    cut = int(0.4 * m.E)
+    split = dataclasses.replace(m, conn=m.conn[:cut], groups=[(m.etype, m.conn[cut:])])
+    a = gpu_lib.GpuDomain(m)
+    b = gpu_lib.GpuDomain(split)
+    assert a.step(30) == 30 and b.step(30) == 30
+    sa, sb = a.get_state("coords", "v", "S", "evp"), b.get_state("coords", "v", "S", "evp")
+    for k in ("coords", "v"):
+        assert np.array_equal(sa[k], sb[k]), k
+    for k in ("S", "evp"):
+        assert np.array_equal(sa[k].reshape(-1), sb[k].reshape(-1)), k
+    assert np.array_equal(a.fint(), b.fint())
+    assert a.time_info()["time"] == b.time_info()["time"]
+
+
+def test_hex_tet_forces_are_the_sum_of_both_parts(gpu_lib):
+    """On a random mid-run state, the forces of the ElTet4n3D + ElHex8n3D domain equal those of its
+    tetrahedra and of its hexahedra as two separate domains over the same nodes, to rounding (the
+    mixed domain sums each node's slots in one pass, the sum of two domains adds two partial
+    sums); the new integration-point states are the parts' own."""
+    m = tet_hex_bar()
+    st = states.random_state(m, seed=11)
+    d = gpu_lib.GpuDomain(m)
+    ip = dict(S=st["S"], Eps=st["Eps"], EpsPlas=st["EpsPlas"], p=st["p"], evp=st["evp"])
+    d.set_state(**ip)
+    f = d.internal_forces(coords=st["coords"], du=st["du"], dt=st["dt"])
+    out = d.get_state("S", "evp")
+    n0 = m.E * m.nip  # integration points of the first group (tetrahedra, one each)
+    parts, outs = [], []
+    for (etype, conn), sl in zip(m.element_groups(), (slice(0, n0), slice(n0, None))):
+        pm = dataclasses.replace(m, etype=etype, conn=conn, groups=None)
+        p = gpu_lib.GpuDomain(pm)
+        nip = meshes.NIP_OF[etype]
+        p.set_state(**{k: v[sl].reshape((conn.shape[0], nip) + v.shape[1:]) for k, v in ip.items()})
+        parts.append(p.internal_forces(coords=st["coords"], du=st["du"], dt=st["dt"]))
+        outs.append(p.get_state("S", "evp"))
+    assert rel(f, parts[0] + parts[1]) <= 1e-14
+    for k in ("S", "evp"):
+        whole = np.concatenate([o[k].reshape((-1,) + out[k].shape[1:]) for o in outs])
+        assert np.array_equal(out[k], whole), k
+
+
+def test_hex_tet_bar_runs_with_pulse(gpu_lib):
+    """The 6x6x12-cell bar, ElHex8n3D at the impact end and ElTet4n3D above, Pulse time step over
+    both groups, 10 us of the impact: no error status, finite coordinates, and the same run bit
+    for bit after dnl_reset on the same handle."""
+    m = meshes.taylor_mixed(6, 12, lower=meshes.ELHEX8N3D, upper=meshes.ELTET4N3D, tend=10e-6)
+    d = gpu_lib.GpuDomain(m)
+    n = d.run()
+    info = d.time_info()
+    assert info["done"] == 1 and info["status"] == 0 and n > 10
+    x1 = d.get_state("coords")["coords"]
+    assert np.all(np.isfinite(x1))
+    d.reset()
+    assert d.run() == n
+    assert np.array_equal(d.get_state("coords")["coords"], x1)
+
+
+def test_add_elements_refusals(gpu_lib):
+    """dnl_add_elements only before the run, only 3D reference elements of one family, ElHex8n3D
+    only with the Pulse step; a domain of several types refuses several materials and the
+    sensitivity entry points."""
+    t = meshes.taylor_tet(4, 3)
+    d = gpu_lib.GpuDomain(t)
+    with pytest.raises(gpu_lib.DnlError):
+        d.add_elements(meshes.ELHEX8N3D, meshes.taylor_hex(4, 3).conn[:2])  # Courant handle
+    with pytest.raises(gpu_lib.DnlError):
+        d.add_elements(meshes.ELQUA4NAX, np.zeros((1, 4), dtype=np.int64))  # another family
+    d.add_elements(meshes.ELTET4N3D, t.conn[:3])
+    with pytest.raises(gpu_lib.DnlError):
+        d.set_materials(t.material_laws(), np.zeros(t.E + 3, dtype=np.int64))
+    with pytest.raises(gpu_lib.DnlError):
+        d.sensitivities(np.full(3, 1e-9))
+    d.step(2)
+    with pytest.raises(gpu_lib.DnlError):
+        d.add_elements(meshes.ELTET4N3D, t.conn[:3])  # after the run started
+    a = gpu_lib.GpuDomain(meshes.taylor_axi(3, 4))
+    with pytest.raises(gpu_lib.DnlError):
+        a.add_elements(meshes.ELQUA4NAX, meshes.taylor_axi(3, 4).conn[:2])
