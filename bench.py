@@ -43,13 +43,13 @@ from redynela_gb300 import meshes  # noqa: E402
 ELEM_TRAFFIC_BYTES_PER_ELEMENT = 308.85e6 / 126400
 
 # FP64 thread-instructions of one k_elem<ElHex8n3D> launch per Gauss point in the timed window of
-# the 505,600-element bar (t = 10 us, increment 1,550), from ncu's
+# the 505,600-element bar (t = 10 us, increment 1,553), from ncu's
 # sm__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum counters of that launch
-# (2,242,452,912 / 544,438,768 / 997,932,972 over the launch's 4,044,800 points, one counter per
+# (2,145,155,470 / 573,527,287 / 914,639,971 over the launch's 4,044,800 points, one counter per
 # capture, each a one-pass capture)
-HEX_FP64_INSTR_PER_POINT = {"dfma": 2242452912 / 4044800, "dadd": 544438768 / 4044800,
-                            "dmul": 997932972 / 4044800}
-HEX_FP64_SOURCE = "the 505,600-element bar's timed window (t = 10 us, increment 1,550)"
+HEX_FP64_INSTR_PER_POINT = {"dfma": 2145155470 / 4044800, "dadd": 573527287 / 4044800,
+                            "dmul": 914639971 / 4044800}
+HEX_FP64_SOURCE = "the 505,600-element bar's timed window (t = 10 us, increment 1,553)"
 
 
 def hex_fp64_flops_per_point() -> float:
