@@ -1216,9 +1216,12 @@ int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn
   const long EN = h->EN + (long)E * nen;
   double *fe = nullptr, *kx = nullptr, *cs0 = nullptr;
   int *start = nullptr, *entry = nullptr;
+  std::vector<double *> csOld(h->nextra, nullptr);  // speeds for earlier groups that had none
   auto freeNew = [&]() {
     void *np[] = {fe, kx, cs0, start, entry};
     for (void *p : np)
+      if (p) cudaFree(p);
+    for (double *p : csOld)
       if (p) cudaFree(p);
   };
 #define CKN(call)                                                                             \
@@ -1270,10 +1273,9 @@ int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn
     CKN(cudaMemcpy(g.Cs, v.data(), sizeof(double) * E, cudaMemcpyHostToDevice));
     for (int gi = 0; gi < h->nextra; gi++)
       if (!h->extra[gi].Cs) {
-        dnl_material dg = dm;
-        std::vector<double> w(h->extra[gi].E, make_material(dg, h->extra[gi].nen).Cs);
-        CKN(cudaMalloc(&h->extra[gi].Cs, sizeof(double) * w.size()));
-        CKN(cudaMemcpy(h->extra[gi].Cs, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice));
+        std::vector<double> w(h->extra[gi].E, make_material(dm, h->extra[gi].nen).Cs);
+        CKN(cudaMalloc(&csOld[gi], sizeof(double) * w.size()));
+        CKN(cudaMemcpy(csOld[gi], w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice));
       }
   }
 #undef CKN
@@ -1286,6 +1288,8 @@ int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn
     h->kx = kx;
   }
   if (cs0) h->elemCs = cs0;
+  for (int gi = 0; gi < h->nextra; gi++)
+    if (csOld[gi]) h->extra[gi].Cs = csOld[gi];
   cudaFree(h->n2eStart);
   cudaFree(h->n2e);
   h->n2eStart = start;

@@ -125,6 +125,27 @@ def test_hex_tet_forces_are_the_sum_of_both_parts(gpu_lib):
         assert np.array_equal(out[k], whole), k
 
 
+def test_courant_step_takes_each_groups_sound_speed(gpu_lib):
+    """Element::getSoundSpeed averages the element's nodal densities over its own node count, so
+    with this density ElTet4n3D's and ElTet10n3D's speeds differ in the last bit; the Courant
+    critical time is the minimum of every element's length over its own speed
+    (Domain::computeCourantTimeStep), so the domain's first step is the smaller of its two parts'
+    steps, bit for bit; and a graph-replayed run of the mixed domain is the stream-launched one."""
+    m = meshes.taylor_mixed(4, 6, nz_lower=3, density=8930.0137)
+    d = gpu_lib.GpuDomain(m)
+    d.prologue()
+    steps = []
+    for etype, conn in m.element_groups():
+        p = gpu_lib.GpuDomain(dataclasses.replace(m, etype=etype, conn=conn, groups=None))
+        p.prologue()
+        steps.append(p.time_step())
+    assert d.time_step() == min(steps)
+    a, b = gpu_lib.GpuDomain(m), gpu_lib.GpuDomain(m)
+    assert a.step(4) == 4 and b.step_graph(4) == 4  # ElTet10n3D's tables: a few steps only
+    assert np.array_equal(a.get_state("coords")["coords"], b.get_state("coords")["coords"])
+    assert a.time_info()["time"] == b.time_info()["time"]
+
+
 def test_hex_tet_bar_runs_with_pulse(gpu_lib):
     """The 6x6x12-cell bar, ElHex8n3D at the impact end and ElTet4n3D above, Pulse time step over
     both groups, 10 us of the impact: no error status, finite coordinates, and the same run bit
