@@ -284,6 +284,7 @@ struct ElemArgs {
   double *ip;          // integration-point state
   double *fe;          // element forces: component i of element e's node k at fe[i feStride + e NEN + k]
   long feStride;       // element-node slots of the handle's element groups (E*NEN with one type)
+  int eBase;           // the domain's number of element 0 of these arguments (error reports)
   double *detJ;        // [E*NIP] (written)
   double *stepT;       // optional dEps|R per IP, [18][E*NIP] or nullptr
   double *tape;        // [TapeLayout::NT][E*NIP], written by the tape instance of k_elem
@@ -397,6 +398,7 @@ namespace dnl {
 // element-node slots in fe / kx / the lumped-mass vector start at feOff.
 struct ElemGroup {
   int etype, nen, nip, E;
+  int eOff;      // the domain's number of the group's first element
   long nIP, feOff;
   int *conn;     // [NEN][E]
   double *ip;    // integration-point state [NCOMP][nIP]

@@ -482,7 +482,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     Ji[0][1] = -J[0][1] * r;
     Ji[1][0] = -J[1][0] * r;
     Ji[1][1] = J[0][0] * r;
-    if (detJ < 0. && valid) record_error(tm, DNL_ERR_NEG_DETJ, e);
+    if (detJ < 0. && valid) record_error(tm, DNL_ERR_NEG_DETJ, a.eBase + e);
   } else {
     const double c00 = fma(J[1][1], J[2][2], -J[1][2] * J[2][1]);
     const double c01 = fma(J[1][2], J[2][0], -J[1][0] * J[2][2]);
@@ -498,7 +498,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     Ji[0][2] = fma(J[0][1], J[1][2], -J[0][2] * J[1][1]) * r;
     Ji[1][2] = fma(J[0][2], J[1][0], -J[0][0] * J[1][2]) * r;
     Ji[2][2] = fma(J[0][0], J[1][1], -J[0][1] * J[1][0]) * r;
-    if (detJ == 0. && valid) record_error(tm, DNL_ERR_SINGULAR, e);
+    if (detJ == 0. && valid) record_error(tm, DNL_ERR_SINGULAR, a.eBase + e);
   }
   if (TAPE) {
 #pragma unroll
@@ -587,7 +587,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
     f[1][1] = f11;
     f[2][2] = f22;
   }
-  if (!conv && valid) record_error(tm, DNL_ERR_JACOBI_NOCONV, e);
+  if (!conv && valid) record_error(tm, DNL_ERR_JACOBI_NOCONV, a.eBase + e);
 
   // ---- ln U = sum ln(l)/2 v v^T,  R = F sum l^-1/2 v v^T
   double dE[3][3], Rr[3][3];
@@ -756,7 +756,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         }
         iteration++;
         if (iteration > c_caps[1]) {
-          if (valid) record_error(tm, DNL_ERR_RR_NOCONV, e);
+          if (valid) record_error(tm, DNL_ERR_RR_NOCONV, a.eBase + e);
           break;
         }
       }
@@ -805,7 +805,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         }
         iteration++;
         if (iteration > c_caps[1]) {
-          if (valid) record_error(tm, DNL_ERR_RR_NOCONV, e);
+          if (valid) record_error(tm, DNL_ERR_RR_NOCONV, a.eBase + e);
           break;
         }
       }
@@ -1251,7 +1251,7 @@ __global__ void __launch_bounds__(256) k_courant(ElemArgs a)
   if (e < a.E) {
     len = elem_length<KIND>(a, e);
     if (!(len > 0.)) {
-      record_error(a.tm, DNL_ERR_DT, e);
+      record_error(a.tm, DNL_ERR_DT, a.eBase + e);
       len = 1e300;
     } else if (a.elemCs) {
       len = len / a.elemCs[e];  // several materials: the critical time of this element
@@ -1502,6 +1502,7 @@ static ElemArgs group_args(dnl_handle *h, const ElemGroup &g)
   a.elemMat = nullptr;
   a.mats = nullptr;
   a.elemCs = g.Cs;
+  a.eBase = g.eOff;
   return a;
 }
 

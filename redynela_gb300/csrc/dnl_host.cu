@@ -1162,6 +1162,8 @@ int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn
   g.nen = nen;
   g.nip = nip;
   g.E = E;
+  g.eOff = h->E;
+  for (int gi = 0; gi < h->nextra; gi++) g.eOff += h->extra[gi].E;
   g.nIP = (long)E * nip;
   g.feOff = h->EN;
   auto fail = [&](int code) {

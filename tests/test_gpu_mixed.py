@@ -162,6 +162,21 @@ def test_hex_tet_bar_runs_with_pulse(gpu_lib):
     assert np.array_equal(d.get_state("coords")["coords"], x1)
 
 
+def test_failure_in_an_added_group_reports_the_domains_element_number(gpu_lib):
+    """A flat ElTet4n3D (four nodes of the base plane: det J = 0) added after a bar's elements and
+    a first added group: the element pass reports DNL_ERR_SINGULAR with that element's number in
+    the domain (after every element before it), and the handle, reset, runs again."""
+    t = meshes.taylor_tet(4, 3)
+    base = t.bcs[0].nodes  # the z = 0 layer
+    flat = np.array([[base[0], base[1], base[2], base[3]]], dtype=np.int64)
+    d = gpu_lib.GpuDomain(t)
+    d.add_elements(meshes.ELTET4N3D, t.conn[:5])
+    d.add_elements(meshes.ELTET4N3D, flat)
+    with pytest.raises(gpu_lib.DnlError) as err:
+        d.internal_forces(coords=t.coords, du=np.zeros((t.N, 3)), dt=1e-8)
+    assert err.value.code == 8 and err.value.element == t.E + 5
+
+
 def test_add_elements_refusals(gpu_lib):
     """dnl_add_elements only before the run, only 3D reference elements of one family, ElHex8n3D
     only with the Pulse step; a domain of several types refuses several materials and the
