@@ -590,12 +590,7 @@ def sens_line(args, fd_steps=(1e-5, 1e-6, 1e-7)) -> dict:
             dev_ms += d.timer_elapsed_ms(0, 1)
         wall = time.perf_counter() - t0
     launches = (dynela.kernel_launches() - launches0) // args.steps
-    clocks = clk.summary()
     value = args.steps / (dev_ms * 1e-3)
-    # kernel shares from one more gradient with CUDA events around every launch (untimed)
-    d.profile_begin()
-    gradient()
-    prof = d.profile_end()
     # the forward cost: the same schedule as a plain run (Courant steps recomputed, as the schedule
     # was made) from the same initial state, graph-replayed; the mean of K runs
     fwd_ms = 0.0
@@ -638,29 +633,41 @@ def sens_line(args, fd_steps=(1e-5, 1e-6, 1e-7)) -> dict:
         w[surf] = 2.0 * (x[surf] - xt[surf]) / len(surf)
         return d.adjoint_backward(w)
 
-    gradient_reverse()
+    for _ in range(args.warmup):
+        gradient_reverse()
     rev_ms = 0.0
-    for _ in range(args.steps):
-        d.timer_mark(0)
-        g_rev = gradient_reverse()
-        d.timer_mark(1)
-        rev_ms += d.timer_elapsed_ms(0, 1)
+    with ClockSampler(0) as clk_rev:
+        launches0 = dynela.kernel_launches()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            d.timer_mark(0)
+            g_rev = gradient_reverse()
+            d.timer_mark(1)
+            rev_ms += d.timer_elapsed_ms(0, 1)
+        rev_wall = time.perf_counter() - t0
+        rev_launches = (dynela.kernel_launches() - launches0) // args.steps
     rev_ms /= args.steps
     ast = d.adjoint_stats()
+    # kernel shares of one more reverse-mode gradient with CUDA events around every launch
+    # (untimed; profiled sweeps launch step by step instead of replaying their graphs)
+    d.profile_begin()
+    gradient_reverse()
+    prof_rev = d.profile_end()
     # the device memory a stored trajectory would take: every step's state record
     per_record = ast["record_bytes"] / max(ast["stride"], 1)
-    reverse = {"value": 1e3 / rev_ms, "unit": "gradients/s", "gradient_ms": rev_ms,
-               "gradient_cost_vs_forward": rev_ms / fwd_ms,
-               "agreement_vs_forward_mode": float(np.max(np.abs(g_rev - g) / np.abs(g))),
-               "gradient": [float(v) for v in g_rev],
-               "checkpoints": ast["checkpoints"], "steps_per_checkpoint": ast["stride"],
-               "recomputed_steps": ast["recomputed_steps"], "device_bytes": ast["bytes"],
-               "checkpoint_bytes": ast["checkpoint_bytes"], "segment_record_bytes": ast["record_bytes"],
-               "stored_trajectory_bytes": int(per_record * nst),
-               "path": "dnl_adjoint_forward + dL/dx on the host + dnl_adjoint_backward"}
-    tan_ms, tan_n = prof["tangent"]
-    elem_ms, elem_n = prof["elem"]
-    total_ms = sum(v[0] for v in prof.values())
+    checkpointing = {"checkpoints": ast["checkpoints"], "steps_per_checkpoint": ast["stride"],
+                     "recomputed_steps": ast["recomputed_steps"], "device_bytes": ast["bytes"],
+                     "checkpoint_bytes": ast["checkpoint_bytes"],
+                     "segment_record_bytes": ast["record_bytes"],
+                     "stored_trajectory_bytes": int(per_record * nst)}
+    forward_mode = {"value": value, "unit": "gradients/s", "gradient_ms": grad_ms,
+                    "gradient_cost_vs_forward": grad_ms / fwd_ms,
+                    "gradient": [float(v) for v in g], "gpu_launches": launches,
+                    "e2e": e2e,
+                    "path": "dnl_reset + dnl_sens_run (the run with four tangent copies) + contraction"}
+    # the reverse sweep's dominant kernel, the element pass's adjoint (profiled as "tangent")
+    adj_ms, adj_n = prof_rev["tangent"]
+    total_ms = sum(v[0] for v in prof_rev.values())
     # agreement with the sensitivity oracle (FP64 dual numbers) over a bounded prefix, which is
     # also the CPU baseline's sample
     cpu = None
@@ -688,40 +695,46 @@ def sens_line(args, fd_steps=(1e-5, 1e-6, 1e-7)) -> dict:
         cpu = {"value": 1.0 / (tc * nst / k), "unit": "gradients/s", "cores": threads, "kind": "port",
                "sample": f"the sensitivity oracle (FP64 dual numbers, OpenMP) over the first {k} of "
                          f"the {nst} steps, {tc:.1f} s, scaled to the full schedule"}
-    # tangent element pass: compulsory bytes per launch -- the per-point record (64 doubles,
-    # axisymmetric) and the rotated state (3 tensors + p) read once, the four tangent states read
-    # and written, the element forces written -- over its mean launch time
-    nip, ns, nt = 4, 4, 64
-    tan_bytes = m.E * nip * 8 * (nt + 3 * ns + 1 + 4 * 2 * (3 * ns + 2)) + m.E * 4 * 2 * 8 * 4
-    line = {"metric": "gradients/s", "value": value, "unit": "gradients/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
+    # adjoint element pass: compulsory bytes per launch -- the step's per-point record (64 doubles,
+    # axisymmetric) and the integration-point state read, the state adjoints (15 doubles per point)
+    # read and written, the parameter adjoints (4 per point) accumulated, the element-node adjoints
+    # of coordinates and delta_disp written -- over its mean launch time
+    nip, nt = 4, 64
+    adj_bytes = m.E * nip * 8 * (nt + 15 + 2 * 15 + 2 * 4) + m.E * 4 * 2 * 8 * 2
+    line = {"metric": "adjoint gradients/s", "value": 1e3 / rev_ms, "unit": "gradients/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": rev_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (the reference Taylor deck's geometry)",
             "config": {"workload": "taylor_axi_20x200_sensitivities", "elements": m.E,
                        "explicit_steps": nst, "parameters": ["A", "B", "n", "|v0|"],
                        "loss": "mean over the free-surface nodes (outer radius, impact-free end) of "
                                "|x_final - x_final(A=110 MPa, B=310 MPa, n=0.28)|^2",
-                       "step": "one gradient = dnl_reset + dnl_sens_run + contraction",
+                       "step": "one gradient = dnl_reset + dnl_adjoint_forward (the run, a "
+                               "checkpoint every ceil(sqrt(steps)) steps, made even) + dL/dx on "
+                               "the host + dnl_adjoint_backward (the reverse sweep)",
                        "l2": "state of 4,000 elements fits L2; each gradient is a 4,000-step run"},
-            "gradient": [float(v) for v in g],
-            "forward_run_ms": fwd_ms, "gradient_ms": grad_ms,
-            "gradient_cost_vs_forward": grad_ms / fwd_ms,
+            "gradient": [float(v) for v in g_rev],
+            "forward_run_ms": fwd_ms, "gradient_ms": rev_ms,
+            "gradient_cost_vs_forward": rev_ms / fwd_ms,
+            "checkpointing": checkpointing,
+            "agreement_vs_forward_mode": float(np.max(np.abs(g_rev - g) / np.abs(g))),
             "agreement_vs_dual_oracle": agree,
-            "agreement_vs_central_differences": {"relative_error_by_relative_h": fd_rel},
-            "reverse_mode": reverse,
-            "gpu_launches": launches,
-            "kernel_time_share": {k: round(v[0] / total_ms, 4) for k, v in prof.items()} if total_ms else None,
-            "roofline": {"bound": "hbm", "achieved": tan_bytes / (tan_ms / max(tan_n, 1) * 1e-3) / 1e9,
+            "agreement_vs_central_differences": {"relative_error_by_relative_h": fd_rel,
+                                                 "of": "the forward-mode gradient"},
+            "forward_mode": forward_mode,
+            "gpu_launches": rev_launches,
+            "kernel_time_share": {k: round(v[0] / total_ms, 4) for k, v in prof_rev.items()} if total_ms else None,
+            "roofline": {"bound": "hbm", "achieved": adj_bytes / (adj_ms / max(adj_n, 1) * 1e-3) / 1e9,
                          "peak": peak_hbm()[0], "unit": "GB/s",
-                         "frac": tan_bytes / (tan_ms / max(tan_n, 1) * 1e-3) / 1e9 / peak_hbm()[0],
-                         "avg_launch_ms": tan_ms / max(tan_n, 1), "algorithmic_bytes_per_launch": tan_bytes,
-                         "traffic": None, "kernel": "k_elem_tan<ElQua4nAx>",
+                         "frac": adj_bytes / (adj_ms / max(adj_n, 1) * 1e-3) / 1e9 / peak_hbm()[0],
+                         "avg_launch_ms": adj_ms / max(adj_n, 1), "algorithmic_bytes_per_launch": adj_bytes,
+                         "traffic": None, "kernel": "k_elem_adj<ElQua4nAx>",
                          "peak_source": peak_hbm()[1],
-                         "note": "4,000 elements: launch-latency bound; the tangent pass is FP64 work"},
+                         "note": "4,000 elements: launch-latency bound; the adjoint pass is FP64 work"},
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e, "unit": "gradients/s", "h2d_bytes_per_step": 8 * (nst + 9),
-                    "d2h_bytes_per_step": 8 * 3 * m.N * 5},
-            "clocks": clocks}
+            "e2e": {"value": args.steps / rev_wall, "unit": "gradients/s",
+                    "h2d_bytes_per_step": 8 * (nst + 3 * m.N), "d2h_bytes_per_step": 8 * (3 * m.N + 4)},
+            "clocks": clk_rev.summary()}
     return line
 
 
