@@ -659,6 +659,7 @@ def sens_line(args, fd_steps=(1e-5, 1e-6, 1e-7)) -> dict:
                      "recomputed_steps": ast["recomputed_steps"], "device_bytes": ast["bytes"],
                      "checkpoint_bytes": ast["checkpoint_bytes"],
                      "segment_record_bytes": ast["record_bytes"],
+                     "kept_per_point_record_bytes": ast["kept_record_bytes"],
                      "stored_trajectory_bytes": int(per_record * nst)}
     forward_mode = {"value": value, "unit": "gradients/s", "gradient_ms": grad_ms,
                     "gradient_cost_vs_forward": grad_ms / fwd_ms,

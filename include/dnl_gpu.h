@@ -329,11 +329,12 @@ int dnl_set_dt_schedule(dnl_handle *h, const double *dts, int nsteps);
  * |v0|, given dL/dx_final (3N, node-major), over the schedule set by dnl_set_dt_schedule, from the
  * handle's initial state (no step taken yet, as dnl_sens_run).  One forward sweep stores the state
  * every ckpt_stride steps (ckpt_stride = 0: ceil(sqrt(nsteps))); the reverse sweep restores each
- * segment from its checkpoint, runs it again storing its steps' states, and undoes its steps in
- * reverse order through the adjoints of the nodal update, the element pass (kinematics, polar
- * decomposition, J2 return, RFI rotation, forces) and the assembly.  Memory: ceil(nsteps /
- * ckpt_stride) checkpoints plus ckpt_stride step states (dnl_adjoint_stats), so O(sqrt(nsteps))
- * with the default; cost: about three forward runs.  The same linearisation as the forward mode
+ * segment from its checkpoint, runs it again storing its steps' states (and, within
+ * dnl_set_adjoint_record_budget, their per-point records), and undoes its steps in reverse order
+ * through the adjoints of the nodal update, the element pass (kinematics, polar decomposition, J2
+ * return, RFI rotation, forces) and the assembly.  Memory: ceil(nsteps / ckpt_stride) checkpoints
+ * plus ckpt_stride step states (dnl_adjoint_stats), so O(sqrt(nsteps)) with the default; cost:
+ * about three forward runs.  The same linearisation as the forward mode
  * (dnl_sens_run), so the two gradients agree to rounding.  One power-law material; every element
  * type but DNL_ELHEX8N3D_1PT.  The handle is back at its initial state afterwards.  No counterpart
  * in the reference, which has no derivatives. */
@@ -353,9 +354,16 @@ typedef struct {
   long long bytes;             /* device memory of the adjoint (checkpoints, step states, adjoints) */
   long long checkpoint_bytes;  /* of which the checkpoints */
   long long record_bytes;      /* of which one segment's step states */
+  long long kept_record_bytes; /* of which one segment's per-point records (0: regenerated) */
 } dnl_adjoint_info;
 /* figures of the last dnl_adjoint on this handle */
 int dnl_adjoint_stats(dnl_handle *h, dnl_adjoint_info *info);
+/* Device memory the reverse sweep may spend (per handle) on keeping a segment's per-point records,
+ * which its recomputation writes, so that undoing a step does not run the element pass again:
+ * used when ckpt_stride x the records of one step fit (default 2 GiB; 0: every record is
+ * regenerated).  Gradients are the same bit for bit either way.  Applies to sweeps started after
+ * the call.  No counterpart in the reference. */
+int dnl_set_adjoint_record_budget(unsigned long long bytes);
 /* The scheduled run alone (no derivatives): nsteps steps of sizes dts from the handle's initial
  * state; coords (3N, node-major, may be NULL) receives the final coordinates.  The primal of
  * dnl_sens_run and of dnl_adjoint, bit for bit. */

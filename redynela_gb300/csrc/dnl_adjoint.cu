@@ -55,6 +55,11 @@ struct AdjState {
   double *ipAdj = nullptr;      // [TanLayout::NCOMP][nIP]
   double *xe = nullptr, *ue = nullptr;  // [DIM][E NEN]
   double *gpar = nullptr;       // [3][nIP]
+  // each step's per-point record [NT][nIP] of the segment being undone, written by its
+  // recomputation when stride x NT x nIP doubles fit kept_record_budget(); otherwise the reverse
+  // step runs the element pass again from the step's stored state to regenerate it
+  double *tapes = nullptr;
+  size_t tapeDoubles = 0;
   double *dts = nullptr;        // the schedule on the device
   double *host = nullptr;       // page-locked staging, 3 max(N, nIP) doubles
   size_t bytes = 0;
@@ -250,11 +255,21 @@ void adj_release(AdjState *A)
   *A = AdjState();
 }
 
+// device memory the reverse sweep may spend on keeping a segment's per-point records
+// (dnl_set_adjoint_record_budget; 2 GiB by default)
+size_t &kept_record_budget()
+{
+  static size_t bytes = size_t(2) << 30;
+  return bytes;
+}
+
 int adj_alloc(dnl_handle *h, AdjState *A, int nsteps, int stride)
 {
   const int nseg = (nsteps + stride - 1) / stride;
+  const size_t nIP0 = h->nIP;
+  const bool keep = sizeof(double) * (size_t)stride * tape_nt_of(h->etype) * nIP0 <= kept_record_budget();
   if (A->mem && A->E == h->E && A->N == h->N && A->etype == h->etype && A->stride == stride &&
-      A->nsteps == nsteps)
+      A->nsteps == nsteps && (A->tapes != nullptr) == keep)
     return 0;
   {
     double *rd = A->runDts, *ro = A->runOut;
@@ -276,8 +291,10 @@ int adj_alloc(dnl_handle *h, AdjState *A, int nsteps, int stride)
   A->nseg = nseg;
   A->ckptDoubles = 15 * N + NC * nIP;
   A->slotDoubles = 6 * N + NC * nIP;
+  A->tapeDoubles = NT * nIP;
   const size_t total = nseg * A->ckptDoubles + stride * A->slotDoubles + NT * nIP + NC * nIP +
-                       h->dim * EN + 2 * 12 * N + 6 * N + TC * nIP + 2 * h->dim * EN + 3 * nIP;
+                       h->dim * EN + 2 * 12 * N + 6 * N + TC * nIP + 2 * h->dim * EN + 3 * nIP +
+                       (keep ? stride * A->tapeDoubles : 0);
   CKA(cudaMalloc(&A->mem, sizeof(double) * total));
   CKA(cudaMalloc(&A->ckptTm, sizeof(DevTime) * nseg));
   CKA(cudaMalloc(&A->tmWork, sizeof(DevTime)));
@@ -310,6 +327,8 @@ int adj_alloc(dnl_handle *h, AdjState *A, int nsteps, int stride)
   A->ue = p;
   p += h->dim * EN;
   A->gpar = p;
+  p += 3 * nIP;
+  A->tapes = keep ? p : nullptr;
   A->ckptCur.assign(nseg, 0);
   A->bytes = sizeof(double) * total + sizeof(DevTime) * (nseg + 1) + sizeof(double) * nsteps;
   return 0;
@@ -318,7 +337,7 @@ int adj_alloc(dnl_handle *h, AdjState *A, int nsteps, int stride)
 // one scheduled explicit step of the handle (the launches of dnl_sens_run's primal); with `rec`,
 // the coordinates, the Current delta_disp and the integration-point state the element pass reads
 // are copied there first
-int adj_primal_step(dnl_handle *h, const double *dtsDev, double *rec)
+int adj_primal_step(dnl_handle *h, const double *dtsDev, double *rec, double *tapeOut = nullptr)
 {
   cudaStream_t s = h->stream;
   const size_t N = h->N, nIP = h->nIP;
@@ -331,7 +350,8 @@ int adj_primal_step(dnl_handle *h, const double *dtsDev, double *rec)
     CKA(cudaMemcpyAsync(rec + 3 * N, h->bank[h->cur].du[0], sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
     CKA(cudaMemcpyAsync(rec + 6 * N, h->ip, sizeof(double) * ip_ncomp(h->etype) * nIP, cudaMemcpyDeviceToDevice, s));
   }
-  if ((r = launch_elem(h, s, 1))) return r;
+  // with tapeOut: the same pass (bit for bit) also writing its per-point record there
+  if ((r = tapeOut ? launch_elem_tape(h, s, tapeOut) : launch_elem(h, s, 1))) return r;
   if ((r = enqueue_node(h))) return r;
   h->cur = 1 - h->cur;
   k_adj_dt<<<1, 1, 0, s>>>(h->tm, dtsDev, 1);
@@ -365,31 +385,38 @@ int adj_restore(dnl_handle *h, AdjState *A, int seg)
   return 0;
 }
 
-// undo one step from its record: the pass again with its per-point record, then the adjoints of the
-// nodal update, the element pass and the gather; ln / lc: the New / Current nodal adjoints
-int adj_reverse_step(dnl_handle *h, AdjState *A, const double *rec, const double *ln, double *lc)
+// undo one step from its record: its per-point record (kept from the recomputation in `tape`, or
+// regenerated by running the pass again on the step's stored state), then the adjoints of the
+// nodal update, the element pass and the gather; ln / lc: the New / Current nodal adjoints; ipOut:
+// the integration-point state after the step (with a kept record)
+int adj_reverse_step(dnl_handle *h, AdjState *A, const double *rec, const double *ln, double *lc,
+                     const double *tape = nullptr, const double *ipOut = nullptr)
 {
   cudaStream_t s = h->stream;
   const size_t N = h->N, nIP = h->nIP;
   const int NC = ip_ncomp(h->etype);
-  CKA(cudaMemcpyAsync(A->ipWork, rec + 6 * N, sizeof(double) * NC * nIP, cudaMemcpyDeviceToDevice, s));
-  ElemArgs ea = elem_args_of(h);
-  ea.gate = 0;
-  for (int r = 0; r < 3; r++) {
-    ea.x[r] = const_cast<double *>(rec) + r * N;
-    ea.du[r] = rec + 3 * N + r * N;
-  }
-  ea.ip = A->ipWork;
-  ea.fe = A->feWork;
-  ea.detJ = nullptr;
-  ea.stepT = nullptr;
-  ea.tape = A->tape;
-  ea.tm = A->tmWork;
   int r;
-  prof_begin(h, s);
-  r = launch_elem_tape_raw(h->etype, ea, s);
-  prof_end(h, DNL_PROF_ELEM, s);
-  if (r) return r;
+  if (!tape) {
+    CKA(cudaMemcpyAsync(A->ipWork, rec + 6 * N, sizeof(double) * NC * nIP, cudaMemcpyDeviceToDevice, s));
+    ElemArgs ea = elem_args_of(h);
+    ea.gate = 0;
+    for (int c = 0; c < 3; c++) {
+      ea.x[c] = const_cast<double *>(rec) + c * N;
+      ea.du[c] = rec + 3 * N + c * N;
+    }
+    ea.ip = A->ipWork;
+    ea.fe = A->feWork;
+    ea.detJ = nullptr;
+    ea.stepT = nullptr;
+    ea.tape = A->tape;
+    ea.tm = A->tmWork;
+    prof_begin(h, s);
+    r = launch_elem_tape_raw(h->etype, ea, s);
+    prof_end(h, DNL_PROF_ELEM, s);
+    if (r) return r;
+    tape = A->tape;
+    ipOut = A->ipWork;
+  }
   AdjNodeArgs g;
   g.N = h->N;
   g.mass = h->mass;
@@ -417,8 +444,8 @@ int adj_reverse_step(dnl_handle *h, AdjState *A, const double *rec, const double
   aa.N = h->N;
   aa.conn = h->conn;
   for (int c = 0; c < 3; c++) aa.x[c] = rec + c * N;
-  aa.tape = A->tape;
-  aa.ipOut = A->ipWork;
+  aa.tape = tape;
+  aa.ipOut = ipOut;
   aa.fbar = A->fbar;
   aa.ipAdj = A->ipAdj;
   aa.xe = A->xe;
@@ -451,13 +478,21 @@ int adj_segment(dnl_handle *h, AdjState *A, int kind, int len, int &nw)
     int r;
     if (kind == 2) {
       for (int j = len - 1; j >= 0; j--) {
-        if ((r = adj_reverse_step(h, A, A->slot + j * A->slotDoubles, A->lam[nw], A->lam[1 - nw]))) return r;
+        // with kept records: step j's record, and the state after it -- the next step's stored
+        // state, or the handle's own after the segment's last step
+        const double *tape = A->tapes ? A->tapes + j * A->tapeDoubles : nullptr;
+        const double *ipOut = j < len - 1 ? A->slot + (j + 1) * A->slotDoubles + 6 * (size_t)h->N : h->ip;
+        if ((r = adj_reverse_step(h, A, A->slot + j * A->slotDoubles, A->lam[nw], A->lam[1 - nw], tape,
+                                  tape ? ipOut : nullptr)))
+          return r;
         nw = 1 - nw;
       }
       return 0;
     }
     for (int j = 0; j < len; j++)
-      if ((r = adj_primal_step(h, A->dts, kind == 1 ? A->slot + j * A->slotDoubles : nullptr))) return r;
+      if ((r = adj_primal_step(h, A->dts, kind == 1 ? A->slot + j * A->slotDoubles : nullptr,
+                               kind == 1 && A->tapes ? A->tapes + j * A->tapeDoubles : nullptr)))
+        return r;
     return 0;
   };
   if (h->profiling || len < 2) return enqueue();
@@ -593,6 +628,7 @@ int adjoint_backward(dnl_handle *h, const double *dL_dx, double *grad, dnl_adjoi
     info->bytes = (long long)A->bytes;
     info->checkpoint_bytes = (long long)(sizeof(double) * A->nseg * A->ckptDoubles);
     info->record_bytes = (long long)(sizeof(double) * A->stride * A->slotDoubles);
+    info->kept_record_bytes = A->tapes ? (long long)(sizeof(double) * A->stride * A->tapeDoubles) : 0;
   }
   return 0;
 }
@@ -645,6 +681,12 @@ int dnl_adjoint(dnl_handle *h, const double *dL_dx, double *grad, int ckpt_strid
   int r;
   if ((r = dnl_adjoint_forward(h, ckpt_stride, nullptr))) return r;
   return dnl_adjoint_backward(h, dL_dx, grad);
+}
+
+int dnl_set_adjoint_record_budget(unsigned long long bytes)
+{
+  kept_record_budget() = (size_t)bytes;
+  return 0;
 }
 
 int dnl_adjoint_stats(dnl_handle *h, dnl_adjoint_info *info)

@@ -80,7 +80,8 @@ class StateView(C.Structure):
 class AdjointInfo(C.Structure):
     _fields_ = [("nsteps", C.c_int), ("stride", C.c_int), ("checkpoints", C.c_int),
                 ("recomputed_steps", C.c_longlong), ("bytes", C.c_longlong),
-                ("checkpoint_bytes", C.c_longlong), ("record_bytes", C.c_longlong)]
+                ("checkpoint_bytes", C.c_longlong), ("record_bytes", C.c_longlong),
+                ("kept_record_bytes", C.c_longlong)]
 
 
 class TimeInfo(C.Structure):
@@ -127,6 +128,7 @@ def lib():
         L.dnl_timer_elapsed.argtypes = [H, C.c_int, C.c_int, _dp]
         L.dnl_measure_fp64_peak.argtypes = [_dp]
         L.dnl_check_quotients.argtypes = [C.c_int, _dp, _dp, _dp]
+        L.dnl_set_adjoint_record_budget.argtypes = [C.c_ulonglong]
         L.dnl_set_iteration_caps.argtypes = [C.c_int, C.c_int, C.c_int]
         L.dnl_set_device.argtypes = [C.c_int]
         L.dnl_host_alloc.argtypes = [C.c_ulonglong, C.POINTER(C.c_void_p)]
@@ -210,6 +212,14 @@ def check_quotients(a: np.ndarray, b: np.ndarray) -> Dict[str, np.ndarray]:
         raise DnlError(rc, lib().dnl_error_string(rc).decode())
     o = out.reshape(4, n)
     return {"rcp": o[0], "quot": o[1], "ieee_rcp": o[2], "ieee_quot": o[3]}
+
+
+def set_adjoint_record_budget(nbytes: int) -> None:
+    """dnl_set_adjoint_record_budget: device bytes a reverse sweep may keep for one segment's
+    per-point records (0: regenerate each by running the element pass again)."""
+    rc = lib().dnl_set_adjoint_record_budget(int(nbytes))
+    if rc != DNL_OK:
+        raise DnlError(rc, lib().dnl_error_string(rc).decode())
 
 
 def fp64_peak_tflops() -> float:

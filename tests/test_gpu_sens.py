@@ -144,6 +144,31 @@ def test_reverse_mode_checkpoint_strides(gpu_lib):
     assert np.array_equal(x_after, x_sens)  # the scheduled run is the primal of dnl_sens_run
 
 
+@pytest.mark.parametrize("kind", ["axi", "hex"])
+def test_reverse_mode_kept_records_equal_regenerated(gpu_lib, kind):
+    """The reverse sweep keeps each segment's per-point records from its recomputation when they
+    fit dnl_set_adjoint_record_budget, and otherwise runs each step's element pass again to
+    regenerate them: the same records, so the same gradient bit for bit; the kept records are
+    reported and the regenerating sweep holds none."""
+    m = meshes.taylor_axi(4, 30) if kind == "axi" else meshes.taylor_hex(4, 10)
+    dts, _, _ = schedule(m, 60)
+    rng = np.random.default_rng(5)
+    w = np.zeros((m.N, 3))
+    w[:, :m.dim] = rng.normal(size=(m.N, m.dim))
+    d = gpu_lib.GpuDomain(m)
+    kept = d.adjoint(w, dts, ckpt_stride=0)
+    st_kept = d.adjoint_stats()
+    try:
+        gpu_lib.set_adjoint_record_budget(0)
+        regen = d.adjoint(w, dts, ckpt_stride=0)
+        st_regen = d.adjoint_stats()
+    finally:
+        gpu_lib.set_adjoint_record_budget(2 << 30)
+    assert np.array_equal(kept, regen)
+    assert st_kept["kept_record_bytes"] > 0 and st_regen["kept_record_bytes"] == 0
+    assert st_kept["bytes"] - st_regen["bytes"] == st_kept["kept_record_bytes"]
+
+
 def test_torch_autograd_function(gpu_lib):
     torch = pytest.importorskip("torch")
     m = meshes.taylor_axi(4, 30)
