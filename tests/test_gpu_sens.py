@@ -94,14 +94,16 @@ def _rev_vs_fwd(g, ref):
 
 
 @pytest.mark.parametrize("etype,nsteps", [("axi", 120), ("plane", 120), ("hex", 80), ("tet4", 80),
-                                          ("tet10", 1)])
+                                          ("tet10", 1), ("neck", 60)])
 def test_reverse_mode_matches_forward_mode(gpu_lib, etype, nsteps):
     """dnl_adjoint (reverse sweep with checkpoints) = the forward-mode contraction (dx/dp)^T w to
     1e-10 per parameter, for a random w = dL/dx_final; plastic runs for every element type (the
-    10-node tetrahedron: the one step its reference element survives, elastic)."""
+    10-node tetrahedron: the one step its reference element survives, elastic), and a tensile bar
+    pulled by an imposed end velocity (BoundarySpeed; starting at rest, so d/d|v0| is zero)."""
     m = {"axi": lambda: meshes.taylor_axi(4, 30), "plane": lambda: meshes.taylor_plane(4, 30),
          "hex": lambda: meshes.taylor_hex(4, 10), "tet4": lambda: meshes.taylor_tet(6, 8),
-         "tet10": lambda: meshes.taylor_tet(4, 6, quadratic=True)}[etype]()
+         "tet10": lambda: meshes.taylor_tet(4, 6, quadratic=True),
+         "neck": lambda: meshes.necking_bar(4, 12, speed=5.0)}[etype]()
     dts, _, _ = schedule(m, nsteps)
     rng = np.random.default_rng(3)
     w = np.zeros((m.N, 3))
@@ -110,7 +112,9 @@ def test_reverse_mode_matches_forward_mode(gpu_lib, etype, nsteps):
     ref = np.einsum("pnj,nj->p", dx, w)
     g = gpu_lib.GpuDomain(m).adjoint(w, dts, ckpt_stride=0)
     assert _rev_vs_fwd(g, ref) <= REV_TOL, (g, ref)
-    if etype != "tet10":
+    if etype == "neck":
+        assert np.all(ref[:3] != 0.0) and ref[3] == 0.0  # plastic; no initial velocity
+    elif etype != "tet10":
         assert np.all(ref != 0.0)  # the run reaches the plastic range: all four derivatives live
 
 
