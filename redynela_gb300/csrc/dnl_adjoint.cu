@@ -88,17 +88,29 @@ void adj_drop_graphs(AdjState *A)
   A->graphs.clear();
 }
 
+// the time record between scheduled steps: phase 0 initStep with the scheduled step, 1 updateTime,
+// 2 both (updateTime of one step then initStep of the next: one launch between two steps)
 __global__ void k_adj_dt(DevTime *tm, const double *dts, int phase)
 {
   if (tm->status) return;
-  if (phase == 0) {  // initStep with the scheduled step
+  if (phase != 0)  // updateTime
+    tm->currentTime = __dadd_rn(tm->currentTime, tm->timeStep);
+  if (phase != 1) {  // initStep with the scheduled step
     const double dt = dts[tm->increment];
     tm->timeStep = dt;
     tm->nextTime = __dadd_rn(tm->currentTime, dt);
     tm->increment++;
-  } else {  // updateTime
-    tm->currentTime = __dadd_rn(tm->currentTime, tm->timeStep);
   }
+}
+
+// a step's record: the coordinates (3N), the Current delta_disp (3N) and the integration-point
+// state (n doubles) copied into rec one after another, in one launch
+__global__ void k_adj_record(long N, long nip, const double *x, const double *du, const double *ip,
+                             double *rec)
+{
+  const long total = 6 * N + nip;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x)
+    rec[i] = i < 3 * N ? x[i] : (i < 6 * N ? du[i - 3 * N] : ip[i - 6 * N]);
 }
 
 struct AdjNodeArgs {
@@ -337,24 +349,30 @@ int adj_alloc(dnl_handle *h, AdjState *A, int nsteps, int stride)
 // one scheduled explicit step of the handle (the launches of dnl_sens_run's primal); with `rec`,
 // the coordinates, the Current delta_disp and the integration-point state the element pass reads
 // are copied there first
-int adj_primal_step(dnl_handle *h, const double *dtsDev, double *rec, double *tapeOut = nullptr)
+// `first`: the step opens with initStep; `last`: it ends with updateTime; between two steps of a
+// sequence one launch does both (the same operations in the same order)
+int adj_primal_step(dnl_handle *h, const double *dtsDev, double *rec, double *tapeOut = nullptr,
+                    bool first = true, bool last = true)
 {
   cudaStream_t s = h->stream;
   const size_t N = h->N, nIP = h->nIP;
-  k_adj_dt<<<1, 1, 0, s>>>(h->tm, dtsDev, 0);
-  launch_counter()++;
+  if (first) {
+    k_adj_dt<<<1, 1, 0, s>>>(h->tm, dtsDev, 0);
+    launch_counter()++;
+  }
   int r;
   if ((r = enqueue_bc_current(h))) return r;
   if (rec) {
-    CKA(cudaMemcpyAsync(rec, h->x[0], sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
-    CKA(cudaMemcpyAsync(rec + 3 * N, h->bank[h->cur].du[0], sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
-    CKA(cudaMemcpyAsync(rec + 6 * N, h->ip, sizeof(double) * ip_ncomp(h->etype) * nIP, cudaMemcpyDeviceToDevice, s));
+    const long total = 6 * (long)N + (long)ip_ncomp(h->etype) * nIP;
+    k_adj_record<<<(unsigned)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096), 256, 0, s>>>(
+        (long)N, (long)ip_ncomp(h->etype) * nIP, h->x[0], h->bank[h->cur].du[0], h->ip, rec);
+    launch_counter()++;
   }
   // with tapeOut: the same pass (bit for bit) also writing its per-point record there
   if ((r = tapeOut ? launch_elem_tape(h, s, tapeOut) : launch_elem(h, s, 1))) return r;
   if ((r = enqueue_node(h))) return r;
   h->cur = 1 - h->cur;
-  k_adj_dt<<<1, 1, 0, s>>>(h->tm, dtsDev, 1);
+  k_adj_dt<<<1, 1, 0, s>>>(h->tm, dtsDev, last ? 1 : 2);
   launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
@@ -491,7 +509,8 @@ int adj_segment(dnl_handle *h, AdjState *A, int kind, int len, int &nw)
     }
     for (int j = 0; j < len; j++)
       if ((r = adj_primal_step(h, A->dts, kind == 1 ? A->slot + j * A->slotDoubles : nullptr,
-                               kind == 1 && A->tapes ? A->tapes + j * A->tapeDoubles : nullptr)))
+                               kind == 1 && A->tapes ? A->tapes + j * A->tapeDoubles : nullptr, j == 0,
+                               j == len - 1)))
         return r;
     return 0;
   };
@@ -719,7 +738,7 @@ int dnl_run_schedule(dnl_handle *h, int nsteps, const double *dts, double *coord
   }
   CKA(cudaMemcpyAsync(A->runDts, dts, sizeof(double) * nsteps, cudaMemcpyHostToDevice, s));
   for (int k = 0; k < nsteps; k++)
-    if ((r = adj_primal_step(h, A->runDts, nullptr))) return r;
+    if ((r = adj_primal_step(h, A->runDts, nullptr, nullptr, k == 0, k == nsteps - 1))) return r;
   DevTime t;
   CKA(cudaMemcpyAsync(&t, h->tm, sizeof t, cudaMemcpyDeviceToHost, s));
   if (coords) {
