@@ -344,13 +344,28 @@ class GpuDomain:
     def nip(self) -> int:
         return self.model.nip
 
+    def _state_shapes(self) -> Dict[str, tuple]:
+        """Nodal fields (N, 3); integration-point fields (E, nip, ...) with one element type, or
+        (nIP, ...) over every group in element order with several."""
+        m = self.model
+        ip = (m.nIP_all,) if m.groups else (m.E, m.nip)
+        return {"coords": (m.N, 3), "du": (m.N, 3), "v": (m.N, 3), "a": (m.N, 3),
+                "disp": (m.N, 3), "S": ip + (3, 3), "Eps": ip + (3, 3),
+                "EpsPlas": ip + (3, 3), "Sig": ip + (3, 3), "p": ip,
+                "evp": ip, "mass": (m.N,)}
+
     def set_state(self, **arrays) -> None:
+        """dnl_set_state; each array must hold as many values as its field (_state_shapes): the
+        library reads that many."""
+        shapes = self._state_shapes()
         keep = {}
         sv = StateView()
         for k, v in arrays.items():
             if v is None:
                 continue
             a = np.ascontiguousarray(v, dtype=np.float64)
+            if k not in shapes or k in ("Sig", "mass") or a.size != int(np.prod(shapes[k])):
+                raise ValueError(f"set_state: {k} must be a writable field of {shapes.get(k)} values")
             keep[k] = a
             setattr(sv, k, a.ctypes.data_as(_dp))
         self._check(self.L.dnl_set_state(self.h, C.byref(sv)))
@@ -358,20 +373,13 @@ class GpuDomain:
     def get_state(self, *names: str) -> Dict[str, np.ndarray]:
         """Nodal fields (N, 3); integration-point fields (E, nip, ...) with one element type, or
         (nIP, ...) over every group in element order with several."""
-        m = self.model
-        nI = m.E * m.nip
-        ip = (m.nIP_all,) if m.groups else (m.E, m.nip)
-        shapes = {"coords": (m.N, 3), "du": (m.N, 3), "v": (m.N, 3), "a": (m.N, 3),
-                  "disp": (m.N, 3), "S": ip + (3, 3), "Eps": ip + (3, 3),
-                  "EpsPlas": ip + (3, 3), "Sig": ip + (3, 3), "p": ip,
-                  "evp": ip, "mass": (m.N,)}
+        shapes = self._state_shapes()
         names = names or tuple(shapes)
         out = {n: np.zeros(shapes[n]) for n in names}
         sv = StateView()
         for n, a in out.items():
             setattr(sv, n, a.ctypes.data_as(_dp))
         self._check(self.L.dnl_get_state(self.h, C.byref(sv)))
-        del nI
         return out
 
     def step_tensors(self):
