@@ -861,6 +861,37 @@ def main_necking(args):
     print(json.dumps(line), flush=True)
 
 
+def main_full_run(args):
+    """The whole run of a bar (`--config hex` or `hex1pt`) from t = 0 to its end time (80 us), not a
+    window: the prologue, then dnl_run, CUDA events on the library's stream around the run.
+    `value` = elements x increments / run time; the early elastic steps are cheaper per element
+    than the window of the default line, the late ones dearer (the impact end crushed, the Pulse
+    iteration longer)."""
+    from redynela_gb300 import build, dynela
+    build.build()
+    model, name = workload(args.config, args.layers)
+    d = dynela.GpuDomain(model)
+    d.prologue()
+    with ClockSampler(0) as clk:
+        launches0 = dynela.kernel_launches()
+        d.timer_mark(0)
+        n = d.run()
+        d.timer_mark(1)
+        launches = dynela.kernel_launches() - launches0
+    ms = d.timer_elapsed_ms(0, 1)
+    info = d.time_info()
+    line = {"metric": "element-updates/s (full run)", "value": model.E * n / (ms * 1e-3),
+            "unit": "element-updates/s", "n_gpus": 1, "steps": n, "warmup": 0,
+            "ms_per_step": ms / max(n, 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator of the "
+            "reference Taylor deck's geometry)",
+            "config": {"workload": name, "elements": model.E, "nodes": model.N,
+                       "run": f"t = 0 to {model.tend * 1e6:g} us, {n} increments",
+                       "end_time_us": info["time"] * 1e6, "status": info["status"]},
+            "run_s": ms * 1e-3, "gpu_launches": launches, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -881,6 +912,8 @@ def main():
                     help="simulated time at which the timed window starts (reached untimed), so "
                          "the window sees the deformed, partly plastic bar of a real run")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--full-run", action="store_true",
+                    help="time the bar's whole run to its end time instead of a window")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched and gradient workloads that the default line also reports")
     ap.add_argument("--layers", type=int, default=400,
@@ -897,6 +930,8 @@ def main():
         main_sens(args)
     elif args.config == "necking":
         main_necking(args)
+    elif args.full_run:
+        main_full_run(args)
     else:
         main_ours(args)
 
