@@ -1150,6 +1150,8 @@ int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn
   if (h->elemMat || h->nmat > 1 || h->mat.hard.law != DNL_HARD_POWER || h->sens || h->adj || h->stepT)
     return DNL_ERR_ARG;
   const int nen = etype_nen(etype), nip = etype_nip(etype), N = h->N, E = num_elements;
+  // element-node slots are int32 indices in the node -> slot map
+  if (h->EN + (long)E * nen > 2147483647L) return DNL_ERR_ARG;
   for (long i = 0; i < (long)E * nen; i++)
     if (conn[i] < 0 || conn[i] >= N) return DNL_ERR_ARG;
   CK(cudaStreamSynchronize(h->stream));
