@@ -138,8 +138,9 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
  * handle's node numbering, numbered after the elements already there.  Before dnl_prologue or the
  * first step; 3D reference elements (ElHex8n3D, ElTet4n3D, ElTet10n3D) with one power-law
  * material, ElHex8n3D with the Pulse time step only.  Integration-point arrays of
- * dnl_get/set_state then cover every group in element order; the sensitivity, adjoint, schedule,
- * results-restart and several-material entry points return DNL_ERR_ARG on such a handle. */
+ * dnl_get/set_state, dnl_get_step_tensors and the results files then cover every group in element
+ * order; the sensitivity, adjoint, schedule and several-material entry points return DNL_ERR_ARG
+ * on such a handle. */
 int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn);
 int dnl_destroy(dnl_handle *h);
 /* DNL_ELHEX8N3D_1PT: the viscous hourglass coefficient (default 0.05): the force resisting the
@@ -150,7 +151,8 @@ int dnl_set_hourglass(dnl_handle *h, double coefficient);
 
 int dnl_set_state(dnl_handle *h, const dnl_state_view *s);
 int dnl_get_state(dnl_handle *h, dnl_state_view *s);
-/* dEps and R of the last element pass, (E, nip, 9); needs DNL_FLAG_STEP_TENSORS */
+/* dEps and R of the last element pass, (E, nip, 9) (every group's points in element order on a
+ * domain of several element types); needs DNL_FLAG_STEP_TENSORS */
 int dnl_get_step_tensors(dnl_handle *h, double *dEps, double *R);
 
 /* The drop-in of Domain::computeInternalForces(): one pass of the element loop (kinematics,
@@ -300,8 +302,9 @@ int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, con
 /* -------------------------------------------------------------- results / restart files */
 /* The reference's binary results file (Structure::writeData, Structure.C:936-952, through
  * io_Data::structure_write, io_Data.C:486-506): version header, time, per node the coordinates
- * and the Current NodalField, per integration point p, evp, S, Sig, Eps, dEps, EpsPlas.  Writing
- * needs the last step's strain increments: a handle created with DNL_FLAG_STEP_TENSORS
+ * and the Current NodalField, per integration point p, evp, S, Sig, Eps, dEps, EpsPlas (each
+ * element's own points, elements in the domain's order, on a domain of several element types).
+ * Writing needs the last step's strain increments: a handle created with DNL_FLAG_STEP_TENSORS
  * (DNL_ERR_ARG otherwise). */
 int dnl_write_results(dnl_handle *h, const char *path);
 /* Load such a file into the handle (same mesh) and continue from its time: coordinates, Current

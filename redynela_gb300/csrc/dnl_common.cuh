@@ -405,6 +405,7 @@ struct ElemGroup {
   double *detJ;  // [nIP]
   double *pj;    // Pulse per-Gauss-point kinematics, or nullptr
   double *Cs;    // Courant: the sound speed of each element when the groups' differ, or nullptr
+  double *stepT; // dEps|R per IP [18][nIP] when the handle keeps them, or nullptr
 };
 }  // namespace dnl
 

@@ -1498,7 +1498,7 @@ static ElemArgs group_args(dnl_handle *h, const ElemGroup &g)
   a.ip = g.ip;
   a.fe = h->fe + g.feOff;
   a.detJ = g.detJ;
-  a.stepT = nullptr;
+  a.stepT = g.stepT;
   a.elemMat = nullptr;
   a.mats = nullptr;
   a.elemCs = g.Cs;

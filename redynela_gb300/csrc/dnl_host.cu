@@ -683,7 +683,8 @@ int dnl_destroy(dnl_handle *h)
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int gi = 0; gi < h->nextra; gi++) {
-    void *gp[] = {h->extra[gi].conn, h->extra[gi].ip, h->extra[gi].detJ, h->extra[gi].pj, h->extra[gi].Cs};
+    void *gp[] = {h->extra[gi].conn, h->extra[gi].ip,  h->extra[gi].detJ,
+                  h->extra[gi].pj,   h->extra[gi].Cs, h->extra[gi].stepT};
     for (void *p : gp)
       if (p) cudaFree(p);
   }
@@ -862,6 +863,7 @@ int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0)
     k_fill<<<(unsigned)((g.nIP + 255) / 256), 256, 0, s>>>(g.ip + (size_t)(3 * gns + 2) * g.nIP, g.nIP,
                                                            pow(1e-10, h->mat.n));
     launch_counter() += 2;
+    if (g.stepT) CK(cudaMemsetAsync(g.stepT, 0, sizeof(double) * 18 * g.nIP, s));
   }
   CK(cudaMemsetAsync(h->fint, 0, sizeof(double) * h->dim * N, s));
   if (h->stepT) CK(cudaMemsetAsync(h->stepT, 0, sizeof(double) * 18 * nIP, s));
@@ -1146,9 +1148,8 @@ int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn
   // one family (Domain.C:1042-1060): the 3D reference elements; ElHex8n3D has no Courant length
   if (!solid_reference_element(h->etype) || !solid_reference_element(etype)) return DNL_ERR_ARG;
   if (h->method == DNL_COURANT && etype == DNL_ELHEX8N3D) return DNL_ERR_ARG;
-  // one material; no sensitivity or adjoint state, no per-step tensors
-  if (h->elemMat || h->nmat > 1 || h->mat.hard.law != DNL_HARD_POWER || h->sens || h->adj || h->stepT)
-    return DNL_ERR_ARG;
+  // one material; no sensitivity or adjoint state
+  if (h->elemMat || h->nmat > 1 || h->mat.hard.law != DNL_HARD_POWER || h->sens || h->adj) return DNL_ERR_ARG;
   const int nen = etype_nen(etype), nip = etype_nip(etype), N = h->N, E = num_elements;
   // element-node slots are int32 indices in the node -> slot map
   if (h->EN + (long)E * nen > 2147483647L) return DNL_ERR_ARG;
@@ -1169,7 +1170,7 @@ int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn
   g.nIP = (long)E * nip;
   g.feOff = h->EN;
   auto fail = [&](int code) {
-    void *gp[] = {g.conn, g.ip, g.detJ, g.pj, g.Cs};
+    void *gp[] = {g.conn, g.ip, g.detJ, g.pj, g.Cs, g.stepT};
     for (void *p : gp)
       if (p) cudaFree(p);
     return code;
@@ -1201,6 +1202,10 @@ int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn
     CKG(cudaMemcpy(g.ip + (size_t)(3 * ns + 2) * g.nIP, v.data(), sizeof(double) * g.nIP, cudaMemcpyHostToDevice));
   }
   CKG(cudaMalloc(&g.detJ, sizeof(double) * g.nIP));
+  if (h->stepT) {  // the handle keeps each step's dEps and R (results files): for this group too
+    CKG(cudaMalloc(&g.stepT, sizeof(double) * 18 * (size_t)g.nIP));
+    CKG(cudaMemset(g.stepT, 0, sizeof(double) * 18 * (size_t)g.nIP));
+  }
   if (h->method == DNL_PULSE) CKG(cudaMalloc(&g.pj, sizeof(double) * (size_t)(h->dim * h->dim + 2) * g.nIP));
   // Courant: Element::getSoundSpeed averages the element's nodal densities over its own node
   // count, which can round differently for another element type; then every element's length is
@@ -1313,15 +1318,15 @@ namespace {
 // the integration points of each element group: its device state (component-major over its own
 // points) and its first point in the element order of the host arrays
 struct IpSeg {
-  double *ip;
+  double *ip, *stepT;
   size_t nIP, off;
 };
 std::vector<IpSeg> ip_segments(dnl_handle *h)
 {
-  std::vector<IpSeg> v{{h->ip, (size_t)h->nIP, 0}};
+  std::vector<IpSeg> v{{h->ip, h->stepT, (size_t)h->nIP, 0}};
   size_t off = h->nIP;
   for (int gi = 0; gi < h->nextra; gi++) {
-    v.push_back({h->extra[gi].ip, (size_t)h->extra[gi].nIP, off});
+    v.push_back({h->extra[gi].ip, h->extra[gi].stepT, (size_t)h->extra[gi].nIP, off});
     off += h->extra[gi].nIP;
   }
   return v;
@@ -1434,13 +1439,15 @@ int dnl_get_step_tensors(dnl_handle *h, double *dEps, double *R)
 {
   if (!h || !h->stepT) return DNL_ERR_ARG;
   CK(cudaStreamSynchronize(h->stream));
-  const size_t nIP = h->nIP;
-  std::vector<double> ib(nIP);
-  for (int k = 0; k < 18; k++) {
-    double *dst = k < 9 ? dEps : R;
-    if (!dst) continue;
-    CK(cudaMemcpy(ib.data(), h->stepT + (size_t)k * nIP, sizeof(double) * nIP, cudaMemcpyDeviceToHost));
-    for (size_t i = 0; i < nIP; i++) dst[9 * i + (k % 9)] = ib[i];
+  for (const IpSeg &g : ip_segments(h)) {  // every group's points, in element order
+    const size_t nIP = g.nIP, o = g.off;
+    std::vector<double> ib(nIP);
+    for (int k = 0; k < 18; k++) {
+      double *dst = k < 9 ? dEps : R;
+      if (!dst) continue;
+      CK(cudaMemcpy(ib.data(), g.stepT + (size_t)k * nIP, sizeof(double) * nIP, cudaMemcpyDeviceToHost));
+      for (size_t i = 0; i < nIP; i++) dst[9 * (o + i) + (k % 9)] = ib[i];
+    }
   }
   return 0;
 }

@@ -37,6 +37,11 @@ reference's own output on a seeded synthetic model:
 * ``steps_mixed.npz``   the 6x6x12-cell bar of ElTet4n3D (6 layers) and ElTet10n3D (6 layers) in one
                         domain, Courant time step: lumped mass and its first 5 steps (its ElTet10n3D
                         part ends in a singular Jacobian a few steps later, as the ElTet10n3D bar)
+* ``results_mixed.bin`` the reference's results file of the 3x3x4-cell bar of ElTet4n3D (2 layers)
+                        and ElTet10n3D (2 layers) after its first 2 steps (the first step's
+                        element pass sees the bar at rest): each element's own integration points,
+                        elements in the domain's order (its ElTet10n3D part ends in a singular
+                        Jacobian at the fourth step)
 
     python tests/golden/make_golden.py
 """
@@ -70,6 +75,15 @@ def results():
     r = dnl_io.run_reference("steps", m, 13, path)
     print(f"results_axi.bin: {os.path.getsize(path)} bytes")
     save("results_axi.npz", **{k: r[k] for k in r if k.startswith("final_")}, time=r["time"])
+    results_mixed()
+
+
+def results_mixed():
+    """The mixed-domain results file only: python tests/golden/make_golden.py results_mixed"""
+    m = meshes.taylor_mixed(3, 4, nz_lower=2)
+    path = os.path.join(HERE, "results_mixed.bin")
+    dnl_io.run_reference("steps", m, 2, path)
+    print(f"results_mixed.bin: {os.path.getsize(path)} bytes")
 
 
 def laws():
@@ -172,6 +186,9 @@ def main():
         sys.exit("compiled reference missing: run `make -C oracle ref`")
     if sys.argv[1:] == ["results"]:
         results()
+        return
+    if sys.argv[1:] == ["results_mixed"]:
+        results_mixed()
         return
     if sys.argv[1:] == ["laws"]:
         laws()

@@ -7,7 +7,8 @@ Against the reference's own outputs where the reference computes them soundly (t
 mass, time steps and first steps of an ElTet4n3D + ElTet10n3D domain with the Courant step.  (The
 reference's Pulse loop, and its force loop when a larger element precedes a smaller one, copy a
 longer Vector into a shorter one on such domains -- Vector::redim, linearAlgebra/Vector.C:213-229 --
-a heap overflow, so its hexahedron + tetrahedron runs pin nothing.)  The rest by identities: a
+a heap overflow, so its hexahedron + tetrahedron runs pin nothing.)  The results file of an
+ElTet4n3D + ElTet10n3D domain against the reference's own file.  The rest by identities: a
 mesh split into two groups of its own element type runs bit for bit as the single group, and the
 forces of a hexahedron + tetrahedron domain are those of its two parts as separate domains.
 Tolerances as in test_gpu_tets."""
@@ -17,7 +18,7 @@ import dataclasses
 import numpy as np
 import pytest
 
-from conftest import golden
+from conftest import GOLDEN, golden
 from oracle import states
 from redynela_gb300 import meshes
 
@@ -198,3 +199,61 @@ def test_add_elements_refusals(gpu_lib):
     a = gpu_lib.GpuDomain(meshes.taylor_axi(3, 4))
     with pytest.raises(gpu_lib.DnlError):
         a.add_elements(meshes.ELQUA4NAX, meshes.taylor_axi(3, 4).conn[:2])
+
+
+def test_mixed_results_file_vs_reference_file(gpu_lib, tmp_path):
+    """ElTet4n3D (2 layers) + ElTet10n3D (2 layers) after 2 steps, written by dnl_write_results,
+    against the reference's Structure::writeData file of the same run (tests/golden,
+    results_mixed.bin): each element's own integration points, elements in the domain's order;
+    layout, headers, separators and time exactly, the mechanical fields per field to the
+    trajectory tolerance of this domain's steps (test_mixed_tet4_tet10_steps_vs_reference).  The
+    reference's file read into a fresh handle gives back its state exactly."""
+    m = meshes.taylor_mixed(3, 4, nz_lower=2)
+    d = gpu_lib.GpuDomain(m, flags=gpu_lib.FLAG_STEP_TENSORS)
+    assert d.step(2) == 2
+    path = str(tmp_path / "gpu.bin")
+    d.write_results(path)
+    ours = gpu_lib.parse_results(path, m.N, m.nIP_all)
+    ref = gpu_lib.parse_results(f"{GOLDEN}/results_mixed.bin", m.N, m.nIP_all)
+    for k in ("header", "domain_header", "thermal", "fe"):
+        assert np.array_equal(ours[k], ref[k]), k
+    for a, b in zip(ours["separators"], ref["separators"]):
+        assert np.array_equal(a, b)
+    assert abs(ours["time"] - ref["time"]) <= 1e-15 * ref["time"]
+    errs = {k: rel(ours[k], ref[k]) for k in ("coords", "du", "disp", "v", "a", "S", "Sig", "Eps",
+                                                "dEps", "EpsPlas", "p", "evp")}
+    assert max(errs.values()) <= TRAJ_TOL, errs
+    r = gpu_lib.GpuDomain(m)
+    r.read_results(f"{GOLDEN}/results_mixed.bin")
+    st = r.get_state("coords", "du", "v", "a", "disp", "S", "Eps", "EpsPlas", "p", "evp")
+    for k in st:
+        assert np.array_equal(np.ravel(st[k]), np.ravel(ref[k])), k
+    assert r.time_info()["time"] == ref["time"]
+
+
+def test_mixed_restart_continues_the_run(gpu_lib, tmp_path):
+    """The ElHex8n3D + ElTet4n3D bar with the Pulse step: a file written after 12 steps and read
+    into a fresh handle gives back every group's state bit for bit (the file's per-point records
+    against both handles' states) and the same next element pass to the parity tolerance (the
+    cached evp^n is recomputed from evp on loading); the run then continues."""
+    m = meshes.taylor_mixed(4, 8, lower=meshes.ELHEX8N3D, upper=meshes.ELTET4N3D)
+    d = gpu_lib.GpuDomain(m, flags=gpu_lib.FLAG_STEP_TENSORS)
+    assert d.step(12) == 12
+    path = str(tmp_path / "w.bin")
+    d.write_results(path)
+    parsed = gpu_lib.parse_results(path, m.N, m.nIP_all)
+    e = gpu_lib.GpuDomain(m, flags=gpu_lib.FLAG_STEP_TENSORS)
+    e.read_results(path)
+    keys = ("coords", "du", "v", "a", "disp", "S", "Eps", "EpsPlas", "p", "evp")
+    s1, s2 = d.get_state(*keys), e.get_state(*keys)
+    for k in keys:
+        assert np.array_equal(np.ravel(s1[k]), np.ravel(s2[k])), k
+        assert np.array_equal(np.ravel(parsed[k]), np.ravel(s1[k])), k
+    assert np.any(parsed["evp"] > 1e-10)  # the impact end is plastic
+    x, du = s1["coords"], s1["du"]
+    f1 = d.internal_forces(coords=x, du=du, dt=d.time_info()["time_step"])
+    f2 = e.internal_forces(coords=x, du=du, dt=d.time_info()["time_step"])
+    assert rel(f2, f1) <= FORCE_TOL
+    assert e.step(10) == 10
+    assert e.time_info()["status"] == 0
+    assert np.all(np.isfinite(e.get_state("coords")["coords"]))
