@@ -138,9 +138,9 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
  * handle's node numbering, numbered after the elements already there.  Before dnl_prologue or the
  * first step; 3D reference elements (ElHex8n3D, ElTet4n3D, ElTet10n3D) with one power-law
  * material, ElHex8n3D with the Pulse time step only.  Integration-point arrays of
- * dnl_get/set_state, dnl_get_step_tensors and the results files then cover every group in element
- * order; the sensitivity, adjoint, schedule and several-material entry points return DNL_ERR_ARG
- * on such a handle. */
+ * dnl_get/set_state, dnl_get_step_tensors, the results files, the forward-mode sensitivities and
+ * the reverse-mode adjoint then cover every group in element order; dnl_set_materials returns
+ * DNL_ERR_ARG on such a handle, and so does this call on a batch's union mesh (dnl_batch_handle). */
 int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn);
 int dnl_destroy(dnl_handle *h);
 /* DNL_ELHEX8N3D_1PT: the viscous hourglass coefficient (default 0.05): the force resisting the

@@ -285,8 +285,8 @@ __device__ __forceinline__ void elem_adj(const AdjElemArgs &a, int e, int pt, bo
     a.ipAdj[TN::EVP * nIP + ipx] = evp0b;
     if (gam > 0.) {
       a.gpar[ipx] += gA;
-      a.gpar[nIP + ipx] += gB;
-      a.gpar[2 * nIP + ipx] += gN;
+      a.gpar[a.gStride + ipx] += gB;
+      a.gpar[2 * a.gStride + ipx] += gN;
     }
   }
 
@@ -493,8 +493,8 @@ __device__ __forceinline__ void elem_adj(const AdjElemArgs &a, int e, int pt, bo
     }
 #pragma unroll
     for (int r = 0; r < DIM; r++) {
-      a.xe[(long)r * a.E * NEN + (long)e * NEN + k] = sx[r];
-      a.ue[(long)r * a.E * NEN + (long)e * NEN + k] = su[r];
+      a.xe[(long)r * a.feStride + (long)e * NEN + k] = sx[r];
+      a.ue[(long)r * a.feStride + (long)e * NEN + k] = su[r];
     }
   }
 }

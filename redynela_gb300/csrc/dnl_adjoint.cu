@@ -40,6 +40,7 @@ namespace {
 
 struct AdjState {
   int E = 0, N = 0, nsteps = 0, stride = 0, nseg = 0, etype = -1;
+  long nIP = 0;                 // integration points of every element group
   size_t ckptDoubles = 0, slotDoubles = 0;
   double *mem = nullptr;
   double *ckpt = nullptr;       // nseg x [x(3N) | Current du, v, a, disp (12N) | ip (NCOMP nIP)]
@@ -278,10 +279,10 @@ size_t &kept_record_budget()
 int adj_alloc(dnl_handle *h, AdjState *A, int nsteps, int stride)
 {
   const int nseg = (nsteps + stride - 1) / stride;
-  const size_t nIP0 = h->nIP;
+  const size_t nIP0 = ip_total(h);
   const bool keep = sizeof(double) * (size_t)stride * tape_nt_of(h->etype) * nIP0 <= kept_record_budget();
-  if (A->mem && A->E == h->E && A->N == h->N && A->etype == h->etype && A->stride == stride &&
-      A->nsteps == nsteps && (A->tapes != nullptr) == keep)
+  if (A->mem && A->E == h->E && A->N == h->N && A->nIP == (long)nIP0 && A->etype == h->etype &&
+      A->stride == stride && A->nsteps == nsteps && (A->tapes != nullptr) == keep)
     return 0;
   {
     double *rd = A->runDts, *ro = A->runOut;
@@ -293,10 +294,13 @@ int adj_alloc(dnl_handle *h, AdjState *A, int nsteps, int stride)
     A->runCap = rc;
     A->runN = rn;
   }
-  const size_t N = h->N, nIP = h->nIP, EN = (size_t)h->E * h->nen;
+  // per-point arrays over every element group's points (each group's block at its ipOff; one
+  // layout width per dimension), element-node arrays over every group's slots
+  const size_t N = h->N, nIP = nIP0, EN = (size_t)h->EN;
   const int NC = ip_ncomp(h->etype), NT = tape_nt_of(h->etype), TC = tan_ncomp_of(h->etype);
   A->E = h->E;
   A->N = h->N;
+  A->nIP = (long)nIP;
   A->etype = h->etype;
   A->nsteps = nsteps;
   A->stride = stride;
@@ -355,7 +359,7 @@ int adj_primal_step(dnl_handle *h, const double *dtsDev, double *rec, double *ta
                     bool first = true, bool last = true)
 {
   cudaStream_t s = h->stream;
-  const size_t N = h->N, nIP = h->nIP;
+  const size_t N = h->N, nIP = ip_total(h);  // one allocation holds every group's state
   if (first) {
     k_adj_dt<<<1, 1, 0, s>>>(h->tm, dtsDev, 0);
     launch_counter()++;
@@ -380,7 +384,7 @@ int adj_primal_step(dnl_handle *h, const double *dtsDev, double *rec, double *ta
 int adj_save(dnl_handle *h, AdjState *A, int seg)
 {
   cudaStream_t s = h->stream;
-  const size_t N = h->N, nIP = h->nIP;
+  const size_t N = h->N, nIP = A->nIP;
   double *c = A->ckpt + seg * A->ckptDoubles;
   CKA(cudaMemcpyAsync(c, h->x[0], sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
   CKA(cudaMemcpyAsync(c + 3 * N, h->bank[h->cur].du[0], sizeof(double) * 12 * N, cudaMemcpyDeviceToDevice, s));
@@ -393,7 +397,7 @@ int adj_save(dnl_handle *h, AdjState *A, int seg)
 int adj_restore(dnl_handle *h, AdjState *A, int seg)
 {
   cudaStream_t s = h->stream;
-  const size_t N = h->N, nIP = h->nIP;
+  const size_t N = h->N, nIP = A->nIP;
   h->cur = A->ckptCur[seg];
   const double *c = A->ckpt + seg * A->ckptDoubles;
   CKA(cudaMemcpyAsync(h->x[0], c, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
@@ -411,25 +415,28 @@ int adj_reverse_step(dnl_handle *h, AdjState *A, const double *rec, const double
                      const double *tape = nullptr, const double *ipOut = nullptr)
 {
   cudaStream_t s = h->stream;
-  const size_t N = h->N, nIP = h->nIP;
-  const int NC = ip_ncomp(h->etype);
-  int r;
+  const size_t N = h->N, nIP = A->nIP;
+  const int NC = ip_ncomp(h->etype), NT = tape_nt_of(h->etype), TC = tan_ncomp_of(h->etype);
+  int r = 0;
   if (!tape) {
     CKA(cudaMemcpyAsync(A->ipWork, rec + 6 * N, sizeof(double) * NC * nIP, cudaMemcpyDeviceToDevice, s));
-    ElemArgs ea = elem_args_of(h);
-    ea.gate = 0;
-    for (int c = 0; c < 3; c++) {
-      ea.x[c] = const_cast<double *>(rec) + c * N;
-      ea.du[c] = rec + 3 * N + c * N;
-    }
-    ea.ip = A->ipWork;
-    ea.fe = A->feWork;
-    ea.detJ = nullptr;
-    ea.stepT = nullptr;
-    ea.tape = A->tape;
-    ea.tm = A->tmWork;
     prof_begin(h, s);
-    r = launch_elem_tape_raw(h->etype, ea, s);
+    for (int gi = -1; gi < h->nextra && !r; gi++) {
+      const long ipOff = gi < 0 ? 0 : h->extra[gi].ipOff, feOff = gi < 0 ? 0 : h->extra[gi].feOff;
+      ElemArgs ea = group_args_of(h, gi);
+      ea.gate = 0;
+      for (int c = 0; c < 3; c++) {
+        ea.x[c] = const_cast<double *>(rec) + c * N;
+        ea.du[c] = rec + 3 * N + c * N;
+      }
+      ea.ip = A->ipWork + NC * ipOff;
+      ea.fe = A->feWork + feOff;
+      ea.detJ = nullptr;
+      ea.stepT = nullptr;
+      ea.tape = A->tape + NT * ipOff;
+      ea.tm = A->tmWork;
+      r = launch_elem_tape_raw(gi < 0 ? h->etype : h->extra[gi].etype, ea, s);
+    }
     prof_end(h, DNL_PROF_ELEM, s);
     if (r) return r;
     tape = A->tape;
@@ -458,28 +465,34 @@ int adj_reverse_step(dnl_handle *h, AdjState *A, const double *rec, const double
   prof_end(h, DNL_PROF_NODE, s);
   launch_counter()++;
   AdjElemArgs aa;
-  aa.E = h->E;
   aa.N = h->N;
-  aa.conn = h->conn;
   for (int c = 0; c < 3; c++) aa.x[c] = rec + c * N;
-  aa.tape = tape;
-  aa.ipOut = ipOut;
   aa.fbar = A->fbar;
-  aa.ipAdj = A->ipAdj;
-  aa.xe = A->xe;
-  aa.ue = A->ue;
-  aa.gpar = A->gpar;
+  aa.feStride = h->EN;
+  aa.gStride = (long)nIP;
   aa.mat = h->mat;
   prof_begin(h, s);
-  r = launch_elem_adj(h->etype, aa, s);
+  // each element group on its own blocks of the per-point arrays and its own element-node slots
+  for (int gi = -1; gi < h->nextra && !r; gi++) {
+    const long ipOff = gi < 0 ? 0 : h->extra[gi].ipOff, feOff = gi < 0 ? 0 : h->extra[gi].feOff;
+    aa.E = gi < 0 ? h->E : h->extra[gi].E;
+    aa.conn = gi < 0 ? h->conn : h->extra[gi].conn;
+    aa.tape = tape + NT * ipOff;
+    aa.ipOut = ipOut + NC * ipOff;
+    aa.ipAdj = A->ipAdj + TC * ipOff;
+    aa.xe = A->xe + feOff;
+    aa.ue = A->ue + feOff;
+    aa.gpar = A->gpar + ipOff;
+    r = launch_elem_adj(gi < 0 ? h->etype : h->extra[gi].etype, aa, s);
+  }
   prof_end(h, DNL_PROF_TANGENT, s);
   if (r) return r;
   prof_begin(h, s);
   if (h->dim == 2)
-    k_gather_adj<2><<<gridN, 256, 0, s>>>(h->N, h->E * h->nen, h->n2eStart, h->n2e, A->xe, A->ue,
+    k_gather_adj<2><<<gridN, 256, 0, s>>>(h->N, (int)h->EN, h->n2eStart, h->n2e, A->xe, A->ue,
                                           A->xbar, lc, h->bcIdx, h->bcCode, h->tm);
   else
-    k_gather_adj<3><<<gridN, 256, 0, s>>>(h->N, h->E * h->nen, h->n2eStart, h->n2e, A->xe, A->ue,
+    k_gather_adj<3><<<gridN, 256, 0, s>>>(h->N, (int)h->EN, h->n2eStart, h->n2e, A->xe, A->ue,
                                           A->xbar, lc, h->bcIdx, h->bcCode, h->tm);
   prof_end(h, DNL_PROF_NODE, s);
   launch_counter()++;
@@ -567,7 +580,7 @@ void adj_free(dnl_handle *h)
 // `stride`-th step; the final coordinates are left in the handle
 int adjoint_forward(dnl_handle *h, const double *dts, int nsteps, int stride)
 {
-  if (!etype_has_sens(h->etype) || h->etype == DNL_ELHEX8N3D_1PT || h->nextra) return DNL_ERR_ARG;
+  if (!etype_has_sens(h->etype) || h->etype == DNL_ELHEX8N3D_1PT) return DNL_ERR_ARG;
   if (h->elemMat || h->mat.hard.law != DNL_HARD_POWER) return DNL_ERR_ARG;
   if (stride <= 0) {
     // ceil(sqrt(n)), made even so that every full segment starts on the same nodal-field bank and
@@ -608,7 +621,7 @@ int adjoint_backward(dnl_handle *h, const double *dL_dx, double *grad, dnl_adjoi
   A->ready = false;
   int r;
   cudaStream_t s = h->stream;
-  const size_t N = h->N, nIP = h->nIP;
+  const size_t N = h->N, nIP = A->nIP;
   const int nsteps = A->nsteps, stride = A->stride;
   memcpy(A->host, dL_dx, sizeof(double) * 3 * N);
   CKA(cudaMemcpyAsync(A->fbar, A->host, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s));
@@ -717,7 +730,7 @@ int dnl_adjoint_stats(dnl_handle *h, dnl_adjoint_info *info)
 
 int dnl_run_schedule(dnl_handle *h, int nsteps, const double *dts, double *coords)
 {
-  if (!h || nsteps <= 0 || !dts || h->nextra) return DNL_ERR_ARG;
+  if (!h || nsteps <= 0 || !dts) return DNL_ERR_ARG;
   for (int k = 0; k < nsteps; k++)
     if (!(dts[k] > 0. && dts[k] < 1e300)) return DNL_ERR_ARG;
   if (h->hostIncrement != 0) return DNL_ERR_ARG;  // starts from the initial state

@@ -293,6 +293,7 @@ int dnl_batch_create(int count, const dnl_mesh_desc *meshes, const dnl_material 
   dnl_handle *h = nullptr;
   int r = dnl_create(&u, &mats[0], &sp0, &h);
   if (r) return r;
+  h->batchUnion = true;  // its kernels cover one element group: no dnl_add_elements
   dnl_batch *b = new dnl_batch();
   b->count = count;
   b->h = h;
@@ -658,7 +659,7 @@ int dnl_batch_broadcast_state(dnl_batch *b, dnl_handle *src)
 {
   if (!b || !src) return DNL_ERR_ARG;
   dnl_handle *h = b->h;
-  if (src->etype != h->etype) return DNL_ERR_ARG;
+  if (src->etype != h->etype || src->nextra) return DNL_ERR_ARG;
   for (int i = 0; i < b->count; i++)
     if (b->nodeOff[i + 1] - b->nodeOff[i] != src->N || b->elemOff[i + 1] - b->elemOff[i] != src->E)
       return DNL_ERR_ARG;

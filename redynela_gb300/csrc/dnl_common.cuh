@@ -310,7 +310,8 @@ struct SensElemArgs {
   const double *tv;    // their tangents, [dir][3][N]
   double hourglass;    // its coefficient
   double *tip;         // [dir][TanLayout::NCOMP][E*NIP]
-  double *tfe;         // [dir][DIM][E*NEN]
+  double *tfe;         // [dir][DIM][feStride]: the element's slots from e NEN
+  long feStride;       // element-node slots of the handle's element groups (E*NEN with one type)
   DevTime *tm;
   Material mat;
   const int *elemInst; // batched: instance of each element (its material), or nullptr
@@ -328,9 +329,11 @@ struct AdjElemArgs {
   const double *fbar;     // adjoint of the assembled nodal forces, [3][N]
   double *ipAdj;          // [TanLayout::NCOMP][E*NIP]: in, adjoint of the state after the pass;
                           // out, of the state before it
-  double *xe, *ue;        // [DIM][E*NEN]: adjoints of the element nodes' coordinates and
-                          // Current delta_disp from this pass
-  double *gpar;           // [3][E*NIP]: d L / d(A, B, n) accumulated per integration point
+  double *xe, *ue;        // [DIM][feStride]: adjoints of the element nodes' coordinates and
+                          // Current delta_disp from this pass (the element's slots from e NEN)
+  long feStride;          // element-node slots of the handle's element groups (E*NEN with one type)
+  double *gpar;           // [3][gStride]: d L / d(A, B, n) accumulated per integration point
+  long gStride;           // integration points of the handle's element groups (E*NIP with one type)
   Material mat;
 };
 
@@ -400,8 +403,10 @@ struct ElemGroup {
   int etype, nen, nip, E;
   int eOff;      // the domain's number of the group's first element
   long nIP, feOff;
+  long ipOff;    // the group's first integration point in element order (its state is the block
+                 // at ip + NCOMP ipOff of the handle's one integration-point allocation)
   int *conn;     // [NEN][E]
-  double *ip;    // integration-point state [NCOMP][nIP]
+  double *ip;    // integration-point state [NCOMP][nIP], inside the handle's allocation
   double *detJ;  // [nIP]
   double *pj;    // Pulse per-Gauss-point kinematics, or nullptr
   double *Cs;    // Courant: the sound speed of each element when the groups' differ, or nullptr
@@ -431,6 +436,7 @@ struct dnl_handle {
   long EN;                    // element-node slots of all element groups
   int nextra;                 // further element groups (dnl_add_elements)
   dnl::ElemGroup *extra;
+  bool batchUnion;            // the union mesh of a dnl_batch
   double *fint;               // [N*DIM]
   // boundary conditions
   int nbcNodes;
@@ -476,6 +482,17 @@ struct dnl_handle {
   // reverse-mode adjoint: checkpoints, step records and adjoint state (dnl_adjoint.cu)
   void *adj;
 };
+
+namespace dnl {
+// integration points of every element group, in element order (the first group's, then each
+// added group's)
+inline long ip_total(const dnl_handle *h)
+{
+  long n = h->nIP;
+  for (int gi = 0; gi < h->nextra; gi++) n += h->extra[gi].nIP;
+  return n;
+}
+}  // namespace dnl
 
 // 1/x by the Newton-Raphson iteration for the reciprocal (the root of f(r) = 1/r - x: r <- r (2 - x r),
 // written r + r e with the residual e = 1 - x r in one fused multiply-add; the relative error
@@ -576,6 +593,8 @@ int launch_courant_batch(int etype, const ElemArgs &a, const int *elemInst, DevT
 // one batched step as a persistent cooperative launch (ElQua4nAx); grid from the occupancy
 int launch_batch_persistent(int etype, int block, const BatchStepArgs &a, cudaStream_t s);
 ElemArgs elem_args_of(dnl_handle *h);
+// the element pass's arguments for element group gi (-1: the first group, as elem_args_of)
+ElemArgs group_args_of(dnl_handle *h, int gi);
 int launch_node_batch(dnl_handle *h, const int *nodeInst, const InstParams *prm, DevTime *tms);
 int launch_dt_batch(dnl_handle *h, DevTime *tms, const InstParams *prm, int count, int mode);
 int launch_bc_batch(dnl_handle *h, DevTime *tms, const int *nodeInst);

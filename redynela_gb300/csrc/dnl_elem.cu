@@ -1536,19 +1536,24 @@ int launch_elem(dnl_handle *h, cudaStream_t s, int gate)
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
 
-// the element pass with its per-integration-point record (forward-mode sensitivities)
+// the element pass with its per-integration-point record (forward-mode sensitivities, the
+// adjoint's recomputation): each element group's record is the block at tape + NT ipOff of the
+// [NT][points] record (one layout width NT per dimension)
 int launch_elem_tape(dnl_handle *h, cudaStream_t s, double *tape)
 {
-  if (!etype_has_sens(h->etype) || h->nextra) return DNL_ERR_ARG;
-  ElemArgs a = elem_args(h);
-  a.gate = 1;
-  a.tape = tape;
-  const long threads = (long)h->E * h->nip;
-  const int grid = (int)((threads + 127) / 128);
+  if (!etype_has_sens(h->etype)) return DNL_ERR_ARG;
   prof_begin(h, s);
-  DNL_BY_ETYPE(h->etype, (k_elem<ET, true><<<grid, 128, 0, s>>>(a)));
+  for (int gi = -1; gi < h->nextra; gi++) {
+    ElemArgs a = gi < 0 ? elem_args(h) : group_args(h, h->extra[gi]);
+    const int et = gi < 0 ? h->etype : h->extra[gi].etype;
+    a.gate = 1;
+    a.tape = tape + (gi < 0 ? 0 : (long)TapeLayout<DNL_ELHEX8N3D>::NT * h->extra[gi].ipOff);
+    const long threads = (long)a.E * etype_nip(et);
+    const int grid = (int)((threads + 127) / 128);
+    DNL_BY_ETYPE(et, (k_elem<ET, true><<<grid, 128, 0, s>>>(a)));
+    launch_counter()++;
+  }
   prof_end(h, DNL_PROF_ELEM, s);
-  launch_counter()++;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
 
@@ -1651,6 +1656,7 @@ int launch_courant_batch(int etype, const ElemArgs &a, const int *elemInst, DevT
 }
 
 ElemArgs elem_args_of(dnl_handle *h) { return elem_args(h); }
+ElemArgs group_args_of(dnl_handle *h, int gi) { return gi < 0 ? elem_args(h) : group_args(h, h->extra[gi]); }
 
 int launch_courant(dnl_handle *h, cudaStream_t s)
 {

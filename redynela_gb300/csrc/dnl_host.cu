@@ -683,8 +683,9 @@ int dnl_destroy(dnl_handle *h)
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int gi = 0; gi < h->nextra; gi++) {
-    void *gp[] = {h->extra[gi].conn, h->extra[gi].ip,  h->extra[gi].detJ,
-                  h->extra[gi].pj,   h->extra[gi].Cs, h->extra[gi].stepT};
+    // (the integration-point state is inside h->ip)
+    void *gp[] = {h->extra[gi].conn, h->extra[gi].detJ, h->extra[gi].pj, h->extra[gi].Cs,
+                  h->extra[gi].stepT};
     for (void *p : gp)
       if (p) cudaFree(p);
   }
@@ -816,7 +817,7 @@ int dnl_set_hourglass(dnl_handle *h, double coefficient)
 int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0)
 {
   if (!h) return DNL_ERR_ARG;
-  if (mat && (h->nmat > 1 || h->mat.hard.law != DNL_HARD_POWER || h->nextra)) return DNL_ERR_ARG;
+  if (mat && (h->nmat > 1 || h->mat.hard.law != DNL_HARD_POWER)) return DNL_ERR_ARG;
   cudaStream_t s = h->stream;
   CK(cudaStreamSynchronize(s));
   for (int i = 0; i < h->ngraphs; i++) cudaGraphExecDestroy(h->graphs[i].exec);
@@ -828,6 +829,18 @@ int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0)
     h->C00 = 1 * f;
     h->C01 = (Nu / (1. - Nu)) * f;
     h->C33 = ((1.0 - 2.0 * Nu) / (2. * (1.0 - Nu))) * f;
+    // a domain of several element types: each group's Courant sound speed with its own node count
+    // (one material, so h->elemCs holds the first group's speed when it exists)
+    if (h->nextra && h->elemCs) {
+      k_fill<<<(unsigned)((h->E + 255) / 256), 256, 0, s>>>(h->elemCs, h->E, h->mat.Cs);
+      launch_counter()++;
+    }
+    for (int gi = 0; gi < h->nextra; gi++)
+      if (h->extra[gi].Cs) {
+        const ElemGroup &g = h->extra[gi];
+        k_fill<<<(unsigned)((g.E + 255) / 256), 256, 0, s>>>(g.Cs, g.E, make_material(*mat, g.nen).Cs);
+        launch_counter()++;
+      }
   }
   if (v0) {
     const double vn = sqrt(v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2]);
@@ -1144,7 +1157,7 @@ int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn
   if (!h || !conn || num_elements <= 0 || !etype_valid(etype)) return DNL_ERR_ARG;
   // before the run starts: the lumped mass, the first time step and the element numbering cover
   // every group
-  if (h->prologueDone || h->hostIncrement) return DNL_ERR_ARG;
+  if (h->prologueDone || h->hostIncrement || h->batchUnion) return DNL_ERR_ARG;
   // one family (Domain.C:1042-1060): the 3D reference elements; ElHex8n3D has no Courant length
   if (!solid_reference_element(h->etype) || !solid_reference_element(etype)) return DNL_ERR_ARG;
   if (h->method == DNL_COURANT && etype == DNL_ELHEX8N3D) return DNL_ERR_ARG;
@@ -1169,8 +1182,10 @@ int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn
   for (int gi = 0; gi < h->nextra; gi++) g.eOff += h->extra[gi].E;
   g.nIP = (long)E * nip;
   g.feOff = h->EN;
+  g.ipOff = ip_total(h);
+  double *ipAll = nullptr;  // every group's integration-point state, this group's block last
   auto fail = [&](int code) {
-    void *gp[] = {g.conn, g.ip, g.detJ, g.pj, g.Cs, g.stepT};
+    void *gp[] = {g.conn, ipAll, g.detJ, g.pj, g.Cs, g.stepT};
     for (void *p : gp)
       if (p) cudaFree(p);
     return code;
@@ -1190,9 +1205,13 @@ int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn
     CKG(cudaMalloc(&g.conn, sizeof(int) * connT.size()));
     CKG(cudaMemcpy(g.conn, connT.data(), sizeof(int) * connT.size(), cudaMemcpyHostToDevice));
   }
-  // integration points at rest: zero stresses and strains, evp = 1e-10 (IntegrationPoint.C:117)
+  // one allocation for every group's integration points, each group's [NCOMP][nIP] block after
+  // the previous one (a state copy is then one copy); this group's at rest: zero stresses and
+  // strains, evp = 1e-10 (IntegrationPoint.C:117)
   const int ns = etype_ns(etype), ncomp = 3 * ns + 3;  // IpLayout::NCOMP (ns = 6 for every solid)
-  CKG(cudaMalloc(&g.ip, sizeof(double) * (size_t)ncomp * g.nIP));
+  CKG(cudaMalloc(&ipAll, sizeof(double) * (size_t)ncomp * (g.ipOff + g.nIP)));
+  CKG(cudaMemcpy(ipAll, h->ip, sizeof(double) * (size_t)ncomp * g.ipOff, cudaMemcpyDeviceToDevice));
+  g.ip = ipAll + (size_t)ncomp * g.ipOff;
   CKG(cudaMemset(g.ip, 0, sizeof(double) * (size_t)ncomp * g.nIP));
   {
     std::vector<double> v(g.nIP, 1e-10);
@@ -1218,19 +1237,17 @@ int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn
   dm.B = h->mat.B;
   dm.n = h->mat.n;
   const double csG = make_material(dm, nen).Cs;
-  bool perElementCs = h->method == DNL_COURANT && csG != h->mat.Cs;
-  for (int gi = 0; gi < h->nextra; gi++) perElementCs |= h->extra[gi].Cs != nullptr;
+  // (kept per element whenever the step is Courant's: a later dnl_reset with another material can
+  // make speeds differ that are equal now)
+  const bool perElementCs = h->method == DNL_COURANT;
 
   // element-force and Pulse-product arrays over the slots of every group; the node -> slot map
   const long EN = h->EN + (long)E * nen;
   double *fe = nullptr, *kx = nullptr, *cs0 = nullptr;
   int *start = nullptr, *entry = nullptr;
-  std::vector<double *> csOld(h->nextra, nullptr);  // speeds for earlier groups that had none
   auto freeNew = [&]() {
     void *np[] = {fe, kx, cs0, start, entry};
     for (void *p : np)
-      if (p) cudaFree(p);
-    for (double *p : csOld)
       if (p) cudaFree(p);
   };
 #define CKN(call)                                                                             \
@@ -1280,16 +1297,13 @@ int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn
     std::vector<double> v(E, csG);
     CKN(cudaMalloc(&g.Cs, sizeof(double) * E));
     CKN(cudaMemcpy(g.Cs, v.data(), sizeof(double) * E, cudaMemcpyHostToDevice));
-    for (int gi = 0; gi < h->nextra; gi++)
-      if (!h->extra[gi].Cs) {
-        std::vector<double> w(h->extra[gi].E, make_material(dm, h->extra[gi].nen).Cs);
-        CKN(cudaMalloc(&csOld[gi], sizeof(double) * w.size()));
-        CKN(cudaMemcpy(csOld[gi], w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice));
-      }
   }
 #undef CKN
 #undef CKG
   // commit
+  cudaFree(h->ip);
+  h->ip = ipAll;
+  for (int gi = 0; gi < h->nextra; gi++) h->extra[gi].ip = ipAll + (size_t)ncomp * h->extra[gi].ipOff;
   cudaFree(h->fe);
   h->fe = fe;
   if (kx) {
@@ -1297,8 +1311,6 @@ int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn
     h->kx = kx;
   }
   if (cs0) h->elemCs = cs0;
-  for (int gi = 0; gi < h->nextra; gi++)
-    if (csOld[gi]) h->extra[gi].Cs = csOld[gi];
   cudaFree(h->n2eStart);
   cudaFree(h->n2e);
   h->n2eStart = start;

@@ -81,15 +81,6 @@ struct In {
   }
 };
 
-// integration points of every element group (a domain of several element types writes each
-// element's own points, elements in the domain's order)
-long all_points(const dnl_handle *h)
-{
-  long n = h->nIP;
-  for (int gi = 0; gi < h->nextra; gi++) n += h->extra[gi].nIP;
-  return n;
-}
-
 }  // namespace
 
 extern "C" {
@@ -97,7 +88,7 @@ extern "C" {
 int dnl_write_results(dnl_handle *h, const char *path)
 {
   if (!h || !path || !h->stepT) return DNL_ERR_ARG;
-  const long N = h->N, nIP = all_points(h);
+  const long N = h->N, nIP = dnl::ip_total(h);  // every group's points, in element order
   std::vector<double> x(3 * N), du(3 * N), v(3 * N), a(3 * N), disp(3 * N);
   std::vector<double> S(9 * nIP), Eps(9 * nIP), EpsPlas(9 * nIP), p(nIP), evp(nIP), dE(9 * nIP);
   dnl_state_view sv;
@@ -167,7 +158,7 @@ int dnl_read_results(dnl_handle *h, const char *path)
   size_t got;
   while ((got = fread(buf, sizeof(double), 4096, f)) > 0) data.insert(data.end(), buf, buf + got);
   fclose(f);
-  const long N = h->N, nIP = all_points(h);
+  const long N = h->N, nIP = dnl::ip_total(h);  // every group's points, in element order
   if (data.size() != (size_t)(6 + 1 + 6 + 1 + 23 * N + 3 + 47 * nIP + 3 + 3)) return DNL_ERR_ARG;
   In in(data);
   in.header();

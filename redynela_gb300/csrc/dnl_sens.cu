@@ -222,13 +222,15 @@ static int tan_ncomp(int etype)
   return etype_dim(etype) == 3 ? TanLayout<DNL_ELHEX8N3D>::NCOMP : TanLayout<DNL_ELQUA4NAX>::NCOMP;
 }
 
+// per-point arrays cover every element group's points (each group's block at its ipOff), the
+// element-node tangents every group's slots (component stride EN)
 int sens_alloc(dnl_handle *h, SensState *S)
 {
-  const long nIP = (long)h->E * h->nip, N = h->N;
+  const long nIP = ip_total(h), N = h->N;
   const int NT = tape_nt(h->etype), NC = tan_ncomp(h->etype);
   const long nodal = (long)kSensParams * 3 * N;
   const long total = NT * nIP + nodal * 9 + (long)kSensParams * NC * nIP +
-                     (long)kSensParams * h->dim * h->E * h->nen + 3 * N;
+                     (long)kSensParams * h->dim * h->EN + 3 * N;
   CKS(cudaMalloc(&S->mem, sizeof(double) * total));
   double *p = S->mem;
   S->tape = p;
@@ -243,7 +245,7 @@ int sens_alloc(dnl_handle *h, SensState *S)
   S->tip = p;
   p += (long)kSensParams * NC * nIP;
   S->tfe = p;
-  p += (long)kSensParams * h->dim * h->E * h->nen;
+  p += (long)kSensParams * h->dim * h->EN;
   S->out = p;
   S->E = h->E;
   S->N = h->N;
@@ -258,7 +260,7 @@ int sens_alloc(dnl_handle *h, SensState *S)
 int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt)
 {
   // the tangent formulas are those of the power law and one material (per instance in a batch)
-  if (!etype_has_sens(h->etype) || h->nextra) return DNL_ERR_ARG;
+  if (!etype_has_sens(h->etype)) return DNL_ERR_ARG;
   if (!bt && (h->elemMat || h->mat.hard.law != DNL_HARD_POWER)) return DNL_ERR_ARG;
   for (int k = 0; k < nsteps; k++)
     if (!(dts[k] > 0. && dts[k] < 1e300)) return DNL_ERR_ARG;
@@ -267,7 +269,7 @@ int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt)
   SensState *S = (SensState *)h->sens;
   if (!S->mem && (r = sens_alloc(h, S))) return r;
   cudaStream_t s = h->stream;
-  const long nIP = (long)h->E * h->nip;
+  const long nIP = ip_total(h);
   {
     const int NT = tape_nt(h->etype);
     const size_t bytes = sizeof(double) * (size_t)((S->out - S->mem) - NT * nIP);
@@ -299,6 +301,7 @@ int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt)
   ea.tx = S->tx;
   ea.tip = S->tip;
   ea.tfe = S->tfe;
+  ea.feStride = h->EN;
   ea.tm = h->tm;
   ea.mat = h->mat;
   ea.hourglass = h->hourglass;
@@ -307,7 +310,7 @@ int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt)
   SensNodeArgs na;
   memset(&na, 0, sizeof na);
   na.N = h->N;
-  na.EN = h->E * h->nen;
+  na.EN = (int)h->EN;
   na.start = h->n2eStart;
   na.entry = h->n2e;
   na.tfe = S->tfe;
@@ -358,6 +361,18 @@ int sens_run(dnl_handle *h, int nsteps, const double *dts, const SensBatch *bt)
     ea.tv = S->tb[h->cur][1];
     prof_begin(h, s);
     r = launch_elem_tan(h->etype, ea, s);
+    // further element groups: their own connectivity, state, records and element-node slots
+    for (int gi = 0; gi < h->nextra && !r; gi++) {
+      const ElemGroup &g = h->extra[gi];
+      SensElemArgs eg = ea;
+      eg.E = g.E;
+      eg.conn = g.conn;
+      eg.ip = g.ip;
+      eg.tape = S->tape + (long)tape_nt(g.etype) * g.ipOff;
+      eg.tip = S->tip + (long)kSensParams * tan_ncomp(g.etype) * g.ipOff;
+      eg.tfe = S->tfe + g.feOff;
+      r = launch_elem_tan(g.etype, eg, s);
+    }
     prof_end(h, DNL_PROF_TANGENT, s);
     if (r) return r;
     if (bt)

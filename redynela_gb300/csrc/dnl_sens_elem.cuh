@@ -454,7 +454,7 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
   if (AXI) mine[DIM * DIM] = dhoop;
   __syncwarp();
   if (!valid) return;
-  double *tfe = a.tfe + (long)dir * DIM * a.E * NEN;
+  double *tfe = a.tfe + (long)dir * DIM * a.feStride;
   if constexpr (NEN == NIP) {
     // the quads and the hexahedron: lane k assembles node k
     double s[DIM];
@@ -472,7 +472,7 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
       if (AXI) s[0] = fma(SH::N(q, pt), Mq[DIM * DIM], s[0]);
     }
 #pragma unroll
-    for (int i = 0; i < DIM; i++) tfe[(long)i * a.E * NEN + (long)e * NEN + pt] = ineg(s[i]);
+    for (int i = 0; i < DIM; i++) tfe[(long)i * a.feStride + (long)e * NEN + pt] = ineg(s[i]);
   } else {
     // the tetrahedra and the one-point hexahedron: lane pt assembles nodes pt, pt + NIP, ...
     constexpr bool HG = ET == DNL_ELHEX8N3D_1PT;
@@ -577,7 +577,7 @@ __device__ __forceinline__ void elem_tan(const SensElemArgs &a, int e, int dir, 
         }
       }
 #pragma unroll
-      for (int i = 0; i < DIM; i++) tfe[(long)i * a.E * NEN + (long)e * NEN + k] = ineg(s[i]);
+      for (int i = 0; i < DIM; i++) tfe[(long)i * a.feStride + (long)e * NEN + k] = ineg(s[i]);
     }
   }
 }

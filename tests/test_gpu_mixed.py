@@ -1,6 +1,7 @@
 """Domains of several element types on the GPU (dnl_add_elements): the element pass, the lumped mass,
 the Courant reduction and the Pulse power iteration run once per element group and assemble through
-one node -> element-node map.
+one node -> element-node map; so do the forward-mode tangents and the reverse-mode adjoint, on one
+integration-point allocation in which each group has its block.
 
 Against the reference's own outputs where the reference computes them soundly (tests/golden,
 *mixed*): one force pass on an injected state of an ElTet4n3D + ElHex8n3D domain, and the lumped
@@ -11,7 +12,10 @@ a heap overflow, so its hexahedron + tetrahedron runs pin nothing.)  The results
 ElTet4n3D + ElTet10n3D domain against the reference's own file.  The rest by identities: a
 mesh split into two groups of its own element type runs bit for bit as the single group, and the
 forces of a hexahedron + tetrahedron domain are those of its two parts as separate domains.
-Tolerances as in test_gpu_tets."""
+Gradients by identities and differences: the split mesh's tangents and adjoint are the single
+group's bit for bit, the adjoint of a hexahedron + tetrahedron run is its forward-mode
+contraction, and both match central differences of the scheduled run.  Tolerances as in
+test_gpu_tets and test_gpu_sens."""
 
 import dataclasses
 
@@ -180,8 +184,8 @@ def test_failure_in_an_added_group_reports_the_domains_element_number(gpu_lib):
 
 def test_add_elements_refusals(gpu_lib):
     """dnl_add_elements only before the run, only 3D reference elements of one family, ElHex8n3D
-    only with the Pulse step; a domain of several types refuses several materials and the
-    sensitivity entry points."""
+    only with the Pulse step, not on a batch's union mesh; a domain of several types refuses
+    several materials and a batch does not take its state."""
     t = meshes.taylor_tet(4, 3)
     d = gpu_lib.GpuDomain(t)
     with pytest.raises(gpu_lib.DnlError):
@@ -191,8 +195,12 @@ def test_add_elements_refusals(gpu_lib):
     d.add_elements(meshes.ELTET4N3D, t.conn[:3])
     with pytest.raises(gpu_lib.DnlError):
         d.set_materials(t.material_laws(), np.zeros(t.E + 3, dtype=np.int64))
+    batch = gpu_lib.BatchDomain([t, t])
     with pytest.raises(gpu_lib.DnlError):
-        d.sensitivities(np.full(3, 1e-9))
+        batch.broadcast_state(d)
+    view = batch.handle_view()
+    c = np.ascontiguousarray(t.conn[:3], dtype=np.int32)
+    assert gpu_lib.lib().dnl_add_elements(view.h, meshes.ELTET4N3D, 3, c.ctypes.data_as(gpu_lib._ip)) != 0
     d.step(2)
     with pytest.raises(gpu_lib.DnlError):
         d.add_elements(meshes.ELTET4N3D, t.conn[:3])  # after the run started
@@ -257,3 +265,93 @@ def test_mixed_restart_continues_the_run(gpu_lib, tmp_path):
     assert e.step(10) == 10
     assert e.time_info()["status"] == 0
     assert np.all(np.isfinite(e.get_state("coords")["coords"]))
+
+
+def plain_schedule(gpu_lib, m, nsteps):
+    """The step sizes of the domain's own plain run (its Courant or Pulse estimate)."""
+    d = gpu_lib.GpuDomain(m)
+    d.prologue()
+    dts = []
+    for _ in range(nsteps):
+        dts.append(d.time_info()["time_step"])
+        assert d.step(1) == 1
+    return np.array(dts), d.get_state("coords")["coords"]
+
+
+@pytest.mark.parametrize("kind", ["hex_pulse", "tet4_courant"])
+def test_split_mesh_gradients_are_bitwise_the_single_groups(gpu_lib, kind):
+    """The mesh given as two groups of its own element type: dnl_sens_run's final coordinates and
+    tangents, and dnl_adjoint's gradient (its per-point parameter sums run over the points in
+    element order either way), are those of the single group bit for bit."""
+    m = meshes.taylor_hex(4, 8) if kind == "hex_pulse" else meshes.taylor_tet(4, 8)
+    cut = int(0.4 * m.E)
+    split = dataclasses.replace(m, conn=m.conn[:cut], groups=[(m.etype, m.conn[cut:])])
+    dts, _ = plain_schedule(gpu_lib, m, 40)
+    xa, dxa = gpu_lib.GpuDomain(m).sensitivities(dts)
+    xb, dxb = gpu_lib.GpuDomain(split).sensitivities(dts)
+    assert np.array_equal(xa, xb) and np.array_equal(dxa, dxb)
+    assert np.all(np.abs(dxa).reshape(4, -1).max(axis=1) > 0)
+    w = np.random.default_rng(5).normal(size=(m.N, 3))
+    ga = gpu_lib.GpuDomain(m).adjoint(w, dts)
+    gb = gpu_lib.GpuDomain(split).adjoint(w, dts)
+    assert np.array_equal(ga, gb)
+
+
+def hex_tet_gradient_bar():
+    return meshes.taylor_mixed(4, 8, lower=meshes.ELHEX8N3D, upper=meshes.ELTET4N3D)
+
+
+def test_mixed_sens_primal_is_the_plain_run(gpu_lib):
+    """On the ElHex8n3D + ElTet4n3D bar, dnl_sens_run and dnl_run_schedule given the plain run's
+    own step sizes are the plain run, bit for bit."""
+    m = hex_tet_gradient_bar()
+    dts, x_plain = plain_schedule(gpu_lib, m, 60)
+    x, _ = gpu_lib.GpuDomain(m).sensitivities(dts)
+    assert np.array_equal(x, x_plain)
+    assert np.array_equal(gpu_lib.GpuDomain(m).run_schedule(dts), x_plain)
+
+
+def test_mixed_reverse_mode_matches_forward_mode(gpu_lib):
+    """The ElHex8n3D + ElTet4n3D bar, 60 scheduled steps (plastic at the impact end): dnl_adjoint
+    with checkpoints, with kept and with regenerated per-point records, equals the forward-mode
+    contraction (dx/dp)^T w to 1e-10 per parameter."""
+    m = hex_tet_gradient_bar()
+    dts, _ = plain_schedule(gpu_lib, m, 60)
+    w = np.random.default_rng(3).normal(size=(m.N, 3))
+    _, dx = gpu_lib.GpuDomain(m).sensitivities(dts)
+    ref = np.einsum("pnj,nj->p", dx, w)
+    assert np.all(ref != 0.0)
+    d = gpu_lib.GpuDomain(m)
+    g = d.adjoint(w, dts, ckpt_stride=0)
+    assert d.adjoint_stats()["kept_record_bytes"] > 0
+    assert np.max(np.abs(g - ref) / np.abs(ref)) <= 1e-10, (g, ref)
+    gpu_lib.set_adjoint_record_budget(0)
+    try:
+        e = gpu_lib.GpuDomain(m)
+        g2 = e.adjoint(w, dts, ckpt_stride=8)
+        assert e.adjoint_stats()["kept_record_bytes"] == 0
+    finally:
+        gpu_lib.set_adjoint_record_budget(2 << 30)
+    assert np.array_equal(g, g2) or np.max(np.abs(g2 - ref) / np.abs(ref)) <= 1e-10
+
+
+def test_mixed_tangents_match_central_differences(gpu_lib):
+    """The forward-mode tangents of the ElHex8n3D + ElTet4n3D bar's final coordinates against
+    central differences of the scheduled run (dnl_run_schedule, the same steps) at 1e-4 relative
+    steps of A, B, n and |v0|: 1e-4 relative (2-norm) per parameter; a domain of several types
+    takes a new material and speed through dnl_reset."""
+    m = hex_tet_gradient_bar()
+    dts, _ = plain_schedule(gpu_lib, m, 40)
+    _, dx = gpu_lib.GpuDomain(m).sensitivities(dts)
+    d = gpu_lib.GpuDomain(m)
+    base = np.array([m.A, m.B, m.n, np.linalg.norm(m.v0)])
+    for p in range(4):
+        h = 1e-4 * base[p]
+        xs = []
+        for sgn in (1.0, -1.0):
+            q = base.copy()
+            q[p] += sgn * h
+            d.reset(gpu_lib.model_with_params(m, *q))
+            xs.append(d.run_schedule(dts))
+        fd = (xs[0] - xs[1]) / (2 * h)
+        assert rel(dx[p], fd) <= 1e-4, (p, rel(dx[p], fd))
