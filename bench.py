@@ -15,7 +15,8 @@ wave has crossed the bar and the impact end is plastic.
 `value` is measured with device-resident state (CUDA events on the library's stream);
 `e2e` goes through the C ABI with page-locked host buffers: each step uploads the nodal state the
 caller owns (coordinates, delta_disp, velocity, acceleration, displacement), advances one step and
-reads it back, over the same increments as `value` (a second handle brought to the same state).  The reference arm (--impl reference) times the oracle's CPU restatement of the
+reads it back in one dnl_step_host call (v, a and disp travel beside the element pass), over the
+same increments as `value` (a second handle brought to the same state).  The reference arm (--impl reference) times the oracle's CPU restatement of the
 reference (oracle/dnl_oracle.c, OpenMP on all host cores) on a bounded slice of the same bar.
 Multi-GPU: independent replicas, one per rank (the explicit step has no cross-replica exchange).
 """
@@ -390,15 +391,11 @@ def main_ours(args):
     st = d.get_state(*host.keys())
     for k, pa in host.items():
         pa.array[:] = st[k]
-    sv = dynela.StateView()
-    for k, pa in host.items():
-        setattr(sv, k, pa.array.ctypes.data_as(dynela._dp))
+    arrays = {k: pa.array for k, pa in host.items()}
     d.timer_mark(2)
     e2e_done = 0
     for _ in range(e2e_steps):
-        d.set_state(**{k: pa.array for k, pa in host.items()})
-        e2e_done += d.step(1)
-        d._check(d.L.dnl_get_state(d.h, dynela.C.byref(sv)))
+        e2e_done += d.step_host(1, inputs=arrays, outputs=arrays)
     d.timer_mark(3)
     e2e_ms = d.timer_elapsed_ms(2, 3)
     e2e_rate = aggregate_rate(model.E * e2e_done, e2e_ms * 1e-3, world)
@@ -406,7 +403,8 @@ def main_ours(args):
     nodal_bytes = 5 * N * 3 * 8
     e2e = {"value": e2e_rate, "unit": "element-updates/s",
            "h2d_bytes_per_step": nodal_bytes, "d2h_bytes_per_step": nodal_bytes,
-           "steps": e2e_done, "path": "dnl_set_state + dnl_step(1) + dnl_get_state per step"}
+           "steps": e2e_done, "path": "dnl_step_host(in, 1, out) per step: the five nodal fields in, "
+           "one step, the five out"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

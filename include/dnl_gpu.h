@@ -168,6 +168,13 @@ int dnl_internal_forces(dnl_handle *h, const double *coords, const double *du, d
 int dnl_prologue(dnl_handle *h);
 /* up to nsteps passes of the ExplicitSolverCH loop, all on the device; stops at the end time */
 int dnl_step(dnl_handle *h, int nsteps, int *steps_done);
+/* dnl_set_state(in) + dnl_step(nsteps) + dnl_get_state(out) in one call, with the same results,
+ * for a host that owns the nodal state between steps: the non-NULL nodal fields of `in` (coords,
+ * du, v, a, disp; N*3 each) are uploaded and those of `out` downloaded after the last step
+ * (integration-point fields and mass: DNL_ERR_ARG).  v, a and disp travel on a second stream while
+ * the first element pass runs, and the download overlaps the next time step's computation
+ * (page-locked host buffers keep the copies asynchronous).  in or out may be NULL. */
+int dnl_step_host(dnl_handle *h, const dnl_state_view *in, int nsteps, dnl_state_view *out, int *steps_done);
 /* the whole run to end_time */
 int dnl_run(dnl_handle *h, int *steps_done);
 /* nsteps steps captured once into a CUDA graph and replayed (same results as dnl_step);

@@ -462,6 +462,11 @@ struct dnl_handle {
   double *stage;              // 5 x N*3 staging buffer for host <-> device nodal vectors (one
                               // slot per nodal field, so the copies of a call run back to back)
   cudaEvent_t marks[8];
+  // dnl_step_host: the second stream its transfers run on, its events, the boundary conditions'
+  // device flag (created on first use)
+  cudaStream_t ioStream;
+  cudaEvent_t ioEv[3];
+  int *bcApplied;
   // per-kernel event timing (dnl_profile_begin/end)
   bool profiling;
   void *prof;

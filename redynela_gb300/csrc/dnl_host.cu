@@ -116,6 +116,50 @@ __global__ void k_bc_current(int nb, const int *nodes, const int *code, const do
   }
 }
 
+// k_bc_current split in two for dnl_step_host, whose Current v and a arrive on a second stream
+// beside the element pass: the delta_disp writes before the pass (recording whether they were
+// made: the run neither done nor in error), then the v and a writes, made iff the first were, once
+// those fields are on the device.  Together the same writes as k_bc_current.
+__global__ void k_bc_current_du(int nb, const int *nodes, const int *code, const double *speed,
+                                NodeFields cur, const DevTime *tm, int *applied)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = !(tm->done | tm->status);
+  if (i == 0) *applied = live;
+  if (i >= nb || !live) return;
+  const int n = nodes[i];
+  const double dt = tm->timeStep;
+  const int cd = code[i];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const int act = (cd >> (2 * c)) & 3;
+    if (act == 1)
+      cur.du[c][n] = 0.;
+    else if (act == 2)
+      cur.du[c][n] = RMUL(speed[3 * i + c], dt);
+  }
+}
+
+__global__ void k_bc_current_va(int nb, const int *nodes, const int *code, const double *speed,
+                                NodeFields cur, const int *applied)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb || !*applied) return;
+  const int n = nodes[i];
+  const int cd = code[i];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const int act = (cd >> (2 * c)) & 3;
+    if (act == 1) {
+      cur.v[c][n] = 0.;
+      cur.a[c][n] = 0.;
+    } else if (act == 2) {
+      cur.a[c][n] = 0.;
+      cur.v[c][n] = speed[3 * i + c];
+    }
+  }
+}
+
 // ----------------------------------------------------------------------------- time step
 struct DtArgs {
   DevTime *tm;
@@ -692,6 +736,10 @@ int dnl_destroy(dnl_handle *h)
   delete[] h->extra;
   for (int i = 0; i < 8; i++)
     if (h->marks[i]) cudaEventDestroy(h->marks[i]);
+  for (int i = 0; i < 3; i++)
+    if (h->ioEv[i]) cudaEventDestroy(h->ioEv[i]);
+  if (h->ioStream) cudaStreamDestroy(h->ioStream);
+  if (h->bcApplied) cudaFree(h->bcApplied);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->prof) {
     Prof *p = (Prof *)h->prof;
@@ -1550,6 +1598,126 @@ int dnl_step(dnl_handle *h, int nsteps, int *steps_done)
   if (t.increment - inc0 != nsteps) {
     const long long extra = nsteps - (t.increment - inc0);
     if (extra % 2) h->cur = 1 - h->cur;
+  }
+  return t.status;
+}
+
+// nsteps steps with the nodal state exchanged with host memory (dnl_set_state + dnl_step +
+// dnl_get_state in one call, the same results).  Coordinates and delta_disp, which the element
+// pass reads, are uploaded first on the handle's stream (and v for the one-point hexahedron, whose
+// hourglass force reads it); v, a and disp on a second stream while the first element pass runs,
+// the boundary conditions' v and a writes after them (k_bc_current_du / _va), and the first nodal
+// update waits for that stream.  The download is queued on the second stream as soon as the last
+// nodal update has run, beside the next time step's computation.
+int dnl_step_host(dnl_handle *h, const dnl_state_view *in, int nsteps, dnl_state_view *out, int *steps_done)
+{
+  if (steps_done) *steps_done = 0;
+  if (!h || nsteps < 1) return DNL_ERR_ARG;
+  for (const dnl_state_view *sv : {in, (const dnl_state_view *)out})
+    if (sv && (sv->S || sv->Eps || sv->EpsPlas || sv->p || sv->evp || sv->Sig || sv->mass)) return DNL_ERR_ARG;
+  int r;
+  if (!h->prologueDone && (r = dnl_prologue(h))) return r;
+  cudaStream_t s = h->stream;
+  if (!h->ioStream) {
+    CK(cudaStreamCreateWithFlags(&h->ioStream, cudaStreamNonBlocking));
+    for (int i = 0; i < 3; i++) CK(cudaEventCreateWithFlags(&h->ioEv[i], cudaEventDisableTiming));
+    CK(cudaMalloc(&h->bcApplied, sizeof(int)));
+  }
+  cudaStream_t io = h->ioStream;
+  const int N = h->N;
+  const size_t n3 = 3 * (size_t)N;
+  const int grid = (N + 255) / 256;
+  // fields: 0 coords, 1 du, 2 v, 3 a, 4 disp (staging slot f)
+  const double *src[5] = {in ? in->coords : nullptr, in ? in->du : nullptr, in ? in->v : nullptr,
+                          in ? in->a : nullptr, in ? in->disp : nullptr};
+  auto dev = [&](int f, double **c) {
+    NodeFields &b = h->bank[h->cur];
+    double *const *p = f == 0 ? h->x : f == 1 ? b.du : f == 2 ? b.v : f == 3 ? b.a : b.disp;
+    for (int k = 0; k < 3; k++) c[k] = p[k];
+  };
+  auto upload = [&](int f, cudaStream_t st) -> int {
+    double *c[3];
+    dev(f, c);
+    CK(cudaMemcpyAsync(h->stage + f * n3, src[f], sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+    k_aos_to_soa<<<grid, 256, 0, st>>>(N, h->stage + f * n3, c[0], c[1], c[2]);
+    launch_counter()++;
+    return check_launch();
+  };
+  const bool vFirst = h->etype == DNL_ELHEX8N3D_1PT;  // its element pass reads Current v
+  const bool side = src[3] || src[4] || (src[2] && !vFirst);
+  const bool bc = h->nbcNodes > 0;
+  for (int f = 0; f < 3; f++)
+    if (src[f] && (f < 2 || vFirst) && (r = upload(f, s))) return r;
+  CK(cudaEventRecord(h->ioEv[0], s));  // the handle's earlier work and these uploads
+  const long long inc0 = h->hostIncrement;
+  if ((r = launch_dt(h, DT_PRE))) return r;
+  for (int k = 0; k < nsteps; k++) {
+    const long long incAfter = inc0 + k + 1;
+    const bool last = k == nsteps - 1;
+    if (k == 0 && side) {
+      if (bc) {
+        k_bc_current_du<<<(h->nbcNodes + 127) / 128, 128, 0, s>>>(h->nbcNodes, h->bcNodeList, h->bcCode,
+                                                                   h->bcSpeed, h->bank[h->cur], h->tm,
+                                                                   h->bcApplied);
+        launch_counter()++;
+        if ((r = check_launch())) return r;
+      }
+      CK(cudaEventRecord(h->ioEv[1], s));
+      if ((r = launch_elem(h, s, 1))) return r;
+      // the second stream: v, a, disp beside the element pass, then the boundary conditions'
+      // writes to v and a
+      CK(cudaStreamWaitEvent(io, h->ioEv[0], 0));
+      for (int f = 2; f < 5; f++)
+        if (src[f] && !(f == 2 && vFirst) && (r = upload(f, io))) return r;
+      if (bc) {
+        CK(cudaStreamWaitEvent(io, h->ioEv[1], 0));
+        k_bc_current_va<<<(h->nbcNodes + 127) / 128, 128, 0, io>>>(h->nbcNodes, h->bcNodeList, h->bcCode,
+                                                                    h->bcSpeed, h->bank[h->cur], h->bcApplied);
+        launch_counter()++;
+        if ((r = check_launch())) return r;
+      }
+      CK(cudaEventRecord(h->ioEv[2], io));
+      CK(cudaStreamWaitEvent(s, h->ioEv[2], 0));
+    } else {
+      if (bc && (r = launch_bc_current(h))) return r;
+      if ((r = launch_elem(h, s, 1))) return r;
+    }
+    if ((r = launch_node(h, true))) return r;
+    h->cur = 1 - h->cur;
+    if (last && out) {  // the download, beside the time step's computation
+      CK(cudaEventRecord(h->ioEv[1], s));
+      CK(cudaStreamWaitEvent(io, h->ioEv[1], 0));
+      double *dst[5] = {out->coords, out->du, out->v, out->a, out->disp};
+      for (int f = 0; f < 5; f++)
+        if (dst[f]) {
+          double *c[3];
+          dev(f, c);
+          k_soa_to_aos<<<grid, 256, 0, io>>>(N, h->stage + f * n3, c[0], c[1], c[2]);
+          launch_counter()++;
+          if ((r = check_launch())) return r;
+        }
+      for (int f = 0; f < 5; f++)
+        if (dst[f]) CK(cudaMemcpyAsync(dst[f], h->stage + f * n3, sizeof(double) * n3, cudaMemcpyDeviceToHost, io));
+    }
+    if (incAfter % h->freq == 0 && (r = launch_time_step_source(h))) return r;
+    if ((r = launch_dt(h, last ? DT_POST : (DT_POST | DT_PRE)))) return r;
+  }
+  // the handle's later work waits for the second stream (its staging slots, the Current fields)
+  CK(cudaEventRecord(h->ioEv[2], io));
+  CK(cudaStreamWaitEvent(s, h->ioEv[2], 0));
+  DevTime t;
+  if ((r = read_time(h, &t))) return r;
+  CK(cudaStreamSynchronize(io));
+  if (steps_done) *steps_done = (int)(t.increment - inc0);
+  h->hostIncrement = t.increment;
+  if (t.increment - inc0 != nsteps) {
+    // the run ended early: the bank parity follows the steps done, and the fields downloaded
+    // above came from the other bank -- download again from the Current one
+    if ((nsteps - (t.increment - inc0)) % 2) h->cur = 1 - h->cur;
+    if (out) {
+      dnl_state_view o = *out;
+      if ((r = dnl_get_state(h, &o))) return r;
+    }
   }
   return t.status;
 }

@@ -113,6 +113,7 @@ def lib():
         L.dnl_prologue.argtypes = [H]
         L.dnl_step.argtypes = [H, C.c_int, _ip]
         L.dnl_run.argtypes = [H, _ip]
+        L.dnl_step_host.argtypes = [H, C.POINTER(StateView), C.c_int, C.POINTER(StateView), _ip]
         L.dnl_step_graph.argtypes = [H, C.c_int, _ip]
         L.dnl_time_step.argtypes = [H, _dp]
         L.dnl_get_time_info.argtypes = [H, C.POINTER(TimeInfo)]
@@ -383,9 +384,10 @@ class GpuDomain:
         return out
 
     def step_tensors(self):
-        m = self.model
-        dE = np.zeros((m.E, m.nip, 3, 3))
-        R = np.zeros((m.E, m.nip, 3, 3))
+        """dEps and R of the last element pass, shaped as the integration-point tensors."""
+        shape = self._state_shapes()["S"]
+        dE = np.zeros(shape)
+        R = np.zeros(shape)
         self._check(self.L.dnl_get_step_tensors(self.h, _ptr(dE), _ptr(R)))
         return dE, R
 
@@ -414,6 +416,35 @@ class GpuDomain:
     def step_graph(self, n: int) -> int:
         done = C.c_int(0)
         self._check_run(self.L.dnl_step_graph(self.h, int(n), C.byref(done)))
+        return done.value
+
+    NODAL = ("coords", "du", "v", "a", "disp")
+
+    def step_host(self, n: int = 1, inputs: Optional[Dict[str, np.ndarray]] = None,
+                  outputs: Optional[Dict[str, np.ndarray]] = None) -> int:
+        """dnl_step_host: upload the nodal fields of ``inputs`` ((N, 3) each), run n steps and
+        download into the arrays of ``outputs`` ((N, 3) float64, C-contiguous, written in place;
+        page-locked arrays such as PinnedArray keep the copies asynchronous).  The same results as
+        set_state + step + get_state."""
+        shape = (self.model.N, 3)
+        views, keep = [], []
+        for fields, writable in ((inputs, False), (outputs, True)):
+            if fields is None:
+                views.append(None)
+                continue
+            sv = StateView()
+            for k, v in fields.items():
+                if k not in self.NODAL:
+                    raise ValueError(f"step_host: {k} is not a nodal field")
+                a = v if writable else np.ascontiguousarray(v, dtype=np.float64)
+                if a.dtype != np.float64 or a.shape != shape or not a.flags.c_contiguous:
+                    raise ValueError(f"step_host: {k} must be a C-contiguous float64 array {shape}")
+                keep.append(a)
+                setattr(sv, k, a.ctypes.data_as(_dp))
+            views.append(sv)
+        done = C.c_int(0)
+        self._check_run(self.L.dnl_step_host(self.h, C.byref(views[0]) if views[0] else None, int(n),
+                                             C.byref(views[1]) if views[1] else None, C.byref(done)))
         return done.value
 
     def run(self) -> int:
