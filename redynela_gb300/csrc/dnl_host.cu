@@ -75,28 +75,6 @@ __global__ void __launch_bounds__(256) k_node(NodeArgs g)
   node_update<DIM>(g, n, tm->timeStep, g.alphaM, g.beta, g.gamma);
 }
 
-// k_node writing the new nodal fields also into host memory the device can address (page-locked
-// buffers of dnl_step_host, node-major N*3; null: not wanted), so the download overlaps the update
-struct HostOut {
-  double *f[5];  // coords, du, v, a, disp
-};
-template <int DIM>
-__global__ void __launch_bounds__(256) k_node_out(NodeArgs g, HostOut o)
-{
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= g.N) return;
-  DevTime *tm = g.tm;
-  if (tm->done | tm->status) return;
-  node_update<DIM>(g, n, tm->timeStep, g.alphaM, g.beta, g.gamma);
-  double *const *src[5] = {g.x, g.nxt.du, g.nxt.v, g.nxt.a, g.nxt.disp};
-#pragma unroll
-  for (int f = 0; f < 5; f++)
-    if (o.f[f]) {
-#pragma unroll
-      for (int c = 0; c < 3; c++) o.f[f][3L * n + c] = src[f][c][n];
-    }
-}
-
 // batched: node n belongs to instance nodeInst[n] with its own time record and constants
 template <int DIM>
 __global__ void __launch_bounds__(256) k_node_batch(NodeArgs g, const int *nodeInst,
@@ -323,7 +301,7 @@ int launch_gather(dnl_handle *h)
   return check_launch();
 }
 
-int launch_node(dnl_handle *h, bool keepFint, const HostOut *out = nullptr)
+int launch_node(dnl_handle *h, bool keepFint)
 {
   NodeArgs g;
   g.N = h->N;
@@ -345,11 +323,7 @@ int launch_node(dnl_handle *h, bool keepFint, const HostOut *out = nullptr)
   g.gamma = h->gamma;
   const int grid = (h->N + 255) / 256;
   prof_begin(h, h->stream);
-  if (out && h->dim == 2)
-    k_node_out<2><<<grid, 256, 0, h->stream>>>(g, *out);
-  else if (out)
-    k_node_out<3><<<grid, 256, 0, h->stream>>>(g, *out);
-  else if (h->dim == 2)
+  if (h->dim == 2)
     k_node<2><<<grid, 256, 0, h->stream>>>(g);
   else
     k_node<3><<<grid, 256, 0, h->stream>>>(g);
@@ -1708,32 +1682,12 @@ int dnl_step_host(dnl_handle *h, const dnl_state_view *in, int nsteps, dnl_state
       if (bc && (r = launch_bc_current(h))) return r;
       if ((r = launch_elem(h, s, 1))) return r;
     }
-    // the download: written by the nodal update itself into page-locked buffers when no time-step
-    // computation follows it in this step; otherwise (and for other buffers) copied on the second
-    // stream beside that computation
-    const bool source = incAfter % h->freq == 0;
-    double *dst[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    HostOut zc = {{nullptr, nullptr, nullptr, nullptr, nullptr}};
-    bool anyZc = false;
-    if (last && out) {
-      double *want[5] = {out->coords, out->du, out->v, out->a, out->disp};
-      for (int f = 0; f < 5; f++) {
-        cudaPointerAttributes at;
-        if (want[f] && !source && cudaPointerGetAttributes(&at, want[f]) == cudaSuccess &&
-            at.type == cudaMemoryTypeHost && at.devicePointer) {
-          zc.f[f] = (double *)at.devicePointer;
-          anyZc = true;
-        } else {
-          dst[f] = want[f];
-        }
-      }
-      cudaGetLastError();  // a pageable pointer's query may leave an error behind
-    }
-    if ((r = launch_node(h, true, anyZc ? &zc : nullptr))) return r;
+    if ((r = launch_node(h, true))) return r;
     h->cur = 1 - h->cur;
-    if (dst[0] || dst[1] || dst[2] || dst[3] || dst[4]) {
+    if (last && out) {  // the download, beside the time step's computation
       CK(cudaEventRecord(h->ioEv[1], s));
       CK(cudaStreamWaitEvent(io, h->ioEv[1], 0));
+      double *dst[5] = {out->coords, out->du, out->v, out->a, out->disp};
       for (int f = 0; f < 5; f++)
         if (dst[f]) {
           double *c[3];
@@ -1745,7 +1699,7 @@ int dnl_step_host(dnl_handle *h, const dnl_state_view *in, int nsteps, dnl_state
       for (int f = 0; f < 5; f++)
         if (dst[f]) CK(cudaMemcpyAsync(dst[f], h->stage + f * n3, sizeof(double) * n3, cudaMemcpyDeviceToHost, io));
     }
-    if (source && (r = launch_time_step_source(h))) return r;
+    if (incAfter % h->freq == 0 && (r = launch_time_step_source(h))) return r;
     if ((r = launch_dt(h, last ? DT_POST : (DT_POST | DT_PRE)))) return r;
   }
   // the handle's later work waits for the second stream (its staging slots, the Current fields)
@@ -1756,10 +1710,9 @@ int dnl_step_host(dnl_handle *h, const dnl_state_view *in, int nsteps, dnl_state
   CK(cudaStreamSynchronize(io));
   if (steps_done) *steps_done = (int)(t.increment - inc0);
   h->hostIncrement = t.increment;
-  if (t.increment - inc0 != nsteps || t.status) {
-    // the run ended early or failed: the bank parity follows the steps done, and the fields
-    // downloaded above may come from the other bank or from a nodal update that did not run --
-    // download again from the Current one
+  if (t.increment - inc0 != nsteps) {
+    // the run ended early: the bank parity follows the steps done, and the fields downloaded
+    // above came from the other bank -- download again from the Current one
     if ((nsteps - (t.increment - inc0)) % 2) h->cur = 1 - h->cur;
     if (out) {
       dnl_state_view o = *out;
