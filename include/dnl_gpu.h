@@ -168,7 +168,8 @@ int dnl_internal_forces(dnl_handle *h, const double *coords, const double *du, d
 int dnl_prologue(dnl_handle *h);
 /* up to nsteps passes of the ExplicitSolverCH loop, all on the device; stops at the end time */
 int dnl_step(dnl_handle *h, int nsteps, int *steps_done);
-/* dnl_set_state(in) + dnl_step(nsteps) + dnl_get_state(out) in one call, with the same results,
+/* dnl_set_state(in) + dnl_step(nsteps) + dnl_get_state(out) in one call, with the same results
+ * (the ExplicitSolverCH::solve loop, ExplicitSolverCH.C:115-278, between the Node field copies),
  * for a host that owns the nodal state between steps: the non-NULL nodal fields of `in` (coords,
  * du, v, a, disp; N*3 each) are uploaded and those of `out` downloaded after the last step
  * (integration-point fields and mass: DNL_ERR_ARG).  v, a and disp travel on a second stream while
