@@ -360,3 +360,24 @@ def test_mixed_tangents_match_central_differences(gpu_lib):
             xs.append(d.run_schedule(dts))
         fd = (xs[0] - xs[1]) / (2 * h)
         assert rel(dx[p], fd) <= 1e-4, (p, rel(dx[p], fd))
+
+
+def test_mixed_torch_autograd_function(gpu_lib):
+    """The torch.autograd.Function over a domain of several element types (the model's groups are
+    added when its handle is made): the reverse-mode backward gives the forward-mode contraction
+    of the same loss, and the forward-mode Function the same gradient."""
+    torch = pytest.importorskip("torch")
+    m = hex_tet_gradient_bar()
+    dts, _ = plain_schedule(gpu_lib, m, 40)
+    params = torch.tensor([m.A, m.B, m.n, float(np.linalg.norm(m.v0))], dtype=torch.float64,
+                          requires_grad=True)
+    target = torch.from_numpy(m.coords.copy())
+    x = gpu_lib.taylor_autograd().apply(params, m, dts)
+    ((x - target) ** 2).sum().backward()
+    _, dx = gpu_lib.GpuDomain(m).sensitivities(dts)
+    ref = np.einsum("pnj,nj->p", dx, 2 * (x.detach().numpy() - m.coords))
+    assert np.all(ref != 0.0)
+    assert np.max(np.abs(params.grad.numpy() - ref) / np.abs(ref)) <= 1e-10
+    pf = params.detach().clone().requires_grad_(True)
+    ((gpu_lib.taylor_autograd("forward").apply(pf, m, dts) - target) ** 2).sum().backward()
+    assert np.allclose(pf.grad.numpy(), ref, rtol=1e-12, atol=0)
