@@ -179,23 +179,42 @@ __global__ void k_dt_batch(DevTime *tms, const InstParams *prm, int count, int m
   dt_update(tms + i, mode, prm[i].freq, prm[i].method, prm[i].safetyOmega, prm[i].Cs);
 }
 
-// node-major (x,y,z) host layout <-> component arrays on the device
-__global__ void k_aos_to_soa(int N, const double *aos, double *c0, double *c1, double *c2)
+// node-major (x,y,z) host layout <-> component arrays on the device, several nodal fields in one
+// launch: field blockIdx.y of the set, its node-major staging slot and its three component arrays
+struct FieldSet {
+  double *aos[5];
+  double *c[5][3];
+  int nf;
+};
+__global__ void k_aos_to_soa_set(int N, FieldSet s)
 {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
-  c0[n] = aos[3L * n];
-  c1[n] = aos[3L * n + 1];
-  c2[n] = aos[3L * n + 2];
+  const int f = blockIdx.y;
+  const double *a = s.aos[f];
+#pragma unroll
+  for (int k = 0; k < 3; k++) s.c[f][k][n] = a[3L * n + k];
 }
-__global__ void k_soa_to_aos(int N, double *aos, const double *c0, const double *c1, const double *c2)
+__global__ void k_soa_to_aos_set(int N, FieldSet s)
 {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
-  aos[3L * n] = c0[n];
-  aos[3L * n + 1] = c1[n];
-  aos[3L * n + 2] = c2[n];
+  const int f = blockIdx.y;
+  double *a = s.aos[f];
+#pragma unroll
+  for (int k = 0; k < 3; k++) a[3L * n + k] = s.c[f][k][n];
 }
+// the handle's nodal field f (0 coords, 1 du, 2 v, 3 a, 4 disp of the Current bank) with staging
+// slot f, appended to a set
+void add_field(dnl_handle *h, FieldSet &s, int f)
+{
+  NodeFields &b = h->bank[h->cur];
+  double *const *p = f == 0 ? h->x : f == 1 ? b.du : f == 2 ? b.v : f == 3 ? b.a : b.disp;
+  s.aos[s.nf] = h->stage + (size_t)f * 3 * h->N;
+  for (int k = 0; k < 3; k++) s.c[s.nf][k] = p[k];
+  s.nf++;
+}
+int transpose_set(dnl_handle *h, const FieldSet &s, bool toDevice, cudaStream_t st);
 
 // FP64 throughput probe: 8 independent DFMA chains per thread, ITER rounds
 __global__ void k_fill(double *p, long n, double v)
@@ -273,6 +292,19 @@ int check_launch()
     return DNL_ERR_CUDA;
   }
   return 0;
+}
+
+// node-major staging slots <-> component arrays for every field of the set, one launch
+int transpose_set(dnl_handle *h, const FieldSet &s, bool toDevice, cudaStream_t st)
+{
+  if (!s.nf) return 0;
+  const dim3 grid((h->N + 255) / 256, s.nf);
+  if (toDevice)
+    k_aos_to_soa_set<<<grid, 256, 0, st>>>(h->N, s);
+  else
+    k_soa_to_aos_set<<<grid, 256, 0, st>>>(h->N, s);
+  launch_counter()++;
+  return check_launch();
 }
 
 GatherArgs gather_args(dnl_handle *h)
@@ -1400,20 +1432,16 @@ int dnl_set_state(dnl_handle *h, const dnl_state_view *s)
   // the host arrays' copies first, back to back, each into its own staging slot; then the
   // transpositions to the component-major device arrays
   const double *src[5] = {s->coords, s->du, s->v, s->a, s->disp};
-  double *const *dst[5] = {h->x, h->bank[h->cur].du, h->bank[h->cur].v, h->bank[h->cur].a,
-                           h->bank[h->cur].disp};
-  for (int f = 0; f < 5; f++)
-    if (src[f])
-      CK(cudaMemcpyAsync(h->stage + (size_t)f * 3 * N, src[f], sizeof(double) * 3 * (size_t)N,
-                         cudaMemcpyHostToDevice, h->stream));
-  int r;
+  FieldSet fs;
+  fs.nf = 0;
   for (int f = 0; f < 5; f++)
     if (src[f]) {
-      k_aos_to_soa<<<(N + 255) / 256, 256, 0, h->stream>>>(N, h->stage + (size_t)f * 3 * N, dst[f][0],
-                                                            dst[f][1], dst[f][2]);
-      launch_counter()++;
-      if ((r = check_launch())) return r;
+      CK(cudaMemcpyAsync(h->stage + (size_t)f * 3 * N, src[f], sizeof(double) * 3 * (size_t)N,
+                         cudaMemcpyHostToDevice, h->stream));
+      add_field(h, fs, f);
     }
+  int r;
+  if ((r = transpose_set(h, fs, true, h->stream))) return r;
   const int ns = etype_ns(h->etype);  // the same for every group of a domain (one family)
   const int I0[6] = {0, 1, 2, 0, 0, 1}, I1[6] = {0, 1, 2, 1, 2, 2};
   CK(cudaStreamSynchronize(h->stream));
@@ -1447,16 +1475,12 @@ int dnl_get_state(dnl_handle *h, dnl_state_view *s)
   const int N = h->N;
   // all transpositions into the staging slots, then the copies back to back, one synchronisation
   double *out[5] = {s->coords, s->du, s->v, s->a, s->disp};
-  double *const *from[5] = {h->x, h->bank[h->cur].du, h->bank[h->cur].v, h->bank[h->cur].a,
-                            h->bank[h->cur].disp};
-  int r;
+  FieldSet fs;
+  fs.nf = 0;
   for (int f = 0; f < 5; f++)
-    if (out[f]) {
-      k_soa_to_aos<<<(N + 255) / 256, 256, 0, h->stream>>>(N, h->stage + (size_t)f * 3 * N, from[f][0],
-                                                            from[f][1], from[f][2]);
-      launch_counter()++;
-      if ((r = check_launch())) return r;
-    }
+    if (out[f]) add_field(h, fs, f);
+  int r;
+  if ((r = transpose_set(h, fs, false, h->stream))) return r;
   for (int f = 0; f < 5; f++)
     if (out[f])
       CK(cudaMemcpyAsync(out[f], h->stage + (size_t)f * 3 * N, sizeof(double) * 3 * (size_t)N,
@@ -1626,28 +1650,28 @@ int dnl_step_host(dnl_handle *h, const dnl_state_view *in, int nsteps, dnl_state
   cudaStream_t io = h->ioStream;
   const int N = h->N;
   const size_t n3 = 3 * (size_t)N;
-  const int grid = (N + 255) / 256;
   // fields: 0 coords, 1 du, 2 v, 3 a, 4 disp (staging slot f)
   const double *src[5] = {in ? in->coords : nullptr, in ? in->du : nullptr, in ? in->v : nullptr,
                           in ? in->a : nullptr, in ? in->disp : nullptr};
-  auto dev = [&](int f, double **c) {
-    NodeFields &b = h->bank[h->cur];
-    double *const *p = f == 0 ? h->x : f == 1 ? b.du : f == 2 ? b.v : f == 3 ? b.a : b.disp;
-    for (int k = 0; k < 3; k++) c[k] = p[k];
+  // the fields of `in` that `pick` selects: copied into their staging slots, then one transposition
+  auto upload = [&](bool (*pick)(int, bool), bool vFirstArg, cudaStream_t st) -> int {
+    FieldSet fs;
+    fs.nf = 0;
+    for (int f = 0; f < 5; f++)
+      if (src[f] && pick(f, vFirstArg)) {
+        CK(cudaMemcpyAsync(h->stage + f * n3, src[f], sizeof(double) * n3, cudaMemcpyHostToDevice, st));
+        add_field(h, fs, f);
+      }
+    return transpose_set(h, fs, true, st);
   };
-  auto upload = [&](int f, cudaStream_t st) -> int {
-    double *c[3];
-    dev(f, c);
-    CK(cudaMemcpyAsync(h->stage + f * n3, src[f], sizeof(double) * n3, cudaMemcpyHostToDevice, st));
-    k_aos_to_soa<<<grid, 256, 0, st>>>(N, h->stage + f * n3, c[0], c[1], c[2]);
-    launch_counter()++;
-    return check_launch();
-  };
+  // before the element pass: coordinates and delta_disp (and v when the pass reads it); beside it
+  // the rest
+  auto early = [](int f, bool vf) { return f < 2 || (f == 2 && vf); };
+  auto late = [](int f, bool vf) { return f >= 2 && !(f == 2 && vf); };
   const bool vFirst = h->etype == DNL_ELHEX8N3D_1PT;  // its element pass reads Current v
   const bool side = src[3] || src[4] || (src[2] && !vFirst);
   const bool bc = h->nbcNodes > 0;
-  for (int f = 0; f < 3; f++)
-    if (src[f] && (f < 2 || vFirst) && (r = upload(f, s))) return r;
+  if ((r = upload(early, vFirst, s))) return r;
   CK(cudaEventRecord(h->ioEv[0], s));  // the handle's earlier work and these uploads
   const long long inc0 = h->hostIncrement;
   if ((r = launch_dt(h, DT_PRE))) return r;
@@ -1667,8 +1691,7 @@ int dnl_step_host(dnl_handle *h, const dnl_state_view *in, int nsteps, dnl_state
       // the second stream: v, a, disp beside the element pass, then the boundary conditions'
       // writes to v and a
       CK(cudaStreamWaitEvent(io, h->ioEv[0], 0));
-      for (int f = 2; f < 5; f++)
-        if (src[f] && !(f == 2 && vFirst) && (r = upload(f, io))) return r;
+      if ((r = upload(late, vFirst, io))) return r;
       if (bc) {
         CK(cudaStreamWaitEvent(io, h->ioEv[1], 0));
         k_bc_current_va<<<(h->nbcNodes + 127) / 128, 128, 0, io>>>(h->nbcNodes, h->bcNodeList, h->bcCode,
@@ -1688,14 +1711,11 @@ int dnl_step_host(dnl_handle *h, const dnl_state_view *in, int nsteps, dnl_state
       CK(cudaEventRecord(h->ioEv[1], s));
       CK(cudaStreamWaitEvent(io, h->ioEv[1], 0));
       double *dst[5] = {out->coords, out->du, out->v, out->a, out->disp};
+      FieldSet fs;
+      fs.nf = 0;
       for (int f = 0; f < 5; f++)
-        if (dst[f]) {
-          double *c[3];
-          dev(f, c);
-          k_soa_to_aos<<<grid, 256, 0, io>>>(N, h->stage + f * n3, c[0], c[1], c[2]);
-          launch_counter()++;
-          if ((r = check_launch())) return r;
-        }
+        if (dst[f]) add_field(h, fs, f);
+      if ((r = transpose_set(h, fs, false, io))) return r;
       for (int f = 0; f < 5; f++)
         if (dst[f]) CK(cudaMemcpyAsync(dst[f], h->stage + f * n3, sizeof(double) * n3, cudaMemcpyDeviceToHost, io));
     }
