@@ -395,12 +395,12 @@ def main_ours(args):
     sv = dynela.StateView()
     for k, pa in host.items():
         setattr(sv, k, pa.array.ctypes.data_as(dynela._dp))
-    done = dynela.C.c_int(0)
+    stepped = dynela.C.c_int(0)
     d.timer_mark(2)
     e2e_done = 0
     for _ in range(e2e_steps):
-        d._check_run(d.L.dnl_step_host(d.h, dynela.C.byref(sv), 1, dynela.C.byref(sv), dynela.C.byref(done)))
-        e2e_done += done.value
+        d._check_run(d.L.dnl_step_host(d.h, dynela.C.byref(sv), 1, dynela.C.byref(sv), dynela.C.byref(stepped)))
+        e2e_done += stepped.value
     d.timer_mark(3)
     e2e_ms = d.timer_elapsed_ms(2, 3)
     e2e_rate = aggregate_rate(model.E * e2e_done, e2e_ms * 1e-3, world)
