@@ -1633,7 +1633,17 @@ int dnl_step(dnl_handle *h, int nsteps, int *steps_done)
 // the boundary conditions' v and a writes after them (k_bc_current_du / _va), and the first nodal
 // update waits for that stream.  The download is queued on the second stream as soon as the last
 // nodal update has run, beside the next time step's computation.
+static int step_host(dnl_handle *h, const dnl_state_view *in, int nsteps, dnl_state_view *out, int *steps_done);
+
 int dnl_step_host(dnl_handle *h, const dnl_state_view *in, int nsteps, dnl_state_view *out, int *steps_done)
+{
+  const int r = step_host(h, in, nsteps, out, steps_done);
+  // a failed launch leaves no work of this call running on the second stream
+  if (r == DNL_ERR_CUDA && h && h->ioStream) cudaStreamSynchronize(h->ioStream);
+  return r;
+}
+
+static int step_host(dnl_handle *h, const dnl_state_view *in, int nsteps, dnl_state_view *out, int *steps_done)
 {
   if (steps_done) *steps_done = 0;
   if (!h || nsteps < 1) return DNL_ERR_ARG;
