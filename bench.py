@@ -429,11 +429,13 @@ def main_ours(args):
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
     d.close()
     if rank == 0 and world == 1 and not args.no_extras and args.config == "hex":
-        # the batched and the gradient workloads, timed in the same run: their own lines, kept
-        # under two keys of this one
+        # the batched, the gradient and the batched-gradient workloads, timed in the same run:
+        # their own lines, kept under three keys of this one
         line["batched"] = batch_line(argparse.Namespace(**dict(vars(args), steps=20, warmup=3)))
         line["gradients"] = sens_line(argparse.Namespace(**dict(vars(args), steps=3, warmup=3,
                                                                 no_cpu=True)), fd_steps=(1e-5,))
+        line["necking"] = necking_line(argparse.Namespace(**dict(vars(args), steps=3, warmup=3,
+                                                                 no_cpu=True)))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -747,6 +749,10 @@ def main_sens(args):
 
 
 def main_necking(args):
+    print(json.dumps(necking_line(args)), flush=True)
+
+
+def necking_line(args) -> dict:
     """Batched sensitivities: 32 parameter sets (A, B, n drawn as for the batched Taylor bars) of
     the tensile necking bar (ElHex8n3D, gauge radius 6.4 mm, length 53.3 mm, 209,824 elements each,
     6.7 M in the batch; clamped end, the other pulled at 1 m/s, mass scaling x100) run as one batch
@@ -861,7 +867,7 @@ def main_necking(args):
             "e2e": {"value": 1.0 / (wall / args.steps * total_steps) * len(models), "unit": "gradients/s",
                     "h2d_bytes_per_step": 8, "d2h_bytes_per_step": 0},
             "clocks": clocks}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def main_full_run(args):
@@ -918,7 +924,8 @@ def main():
     ap.add_argument("--full-run", action="store_true",
                     help="time the bar's whole run to its end time instead of a window")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the batched and gradient workloads that the default line also reports")
+                    help="skip the batched, gradient and necking workloads that the default line "
+                         "also reports")
     ap.add_argument("--layers", type=int, default=400,
                     help="axial layers of the hex bar (400 = the benchmark workload; fewer for "
                          "profiling captures)")
