@@ -628,6 +628,28 @@ def sens_line(args, fd_steps=(1e-5, 1e-6, 1e-7)) -> dict:
             lp, lm = (loss_at(pv + s * h * np.eye(4)[p]) for s in (1.0, -1.0))
             errs.append(float(abs((lp - lm) / (2 * h) - g[p]) / abs(g[p])))
         fd_rel[f"{hrel:.0e}"] = errs
+    # the quotients at h = 1e-6 with the two iterations' stopping tests tightened
+    # (dnl_set_stop_tolerances): with the reference's tolerances a change of 1e-6 in a parameter
+    # can add or remove an iteration somewhere in the run, a jump of the tolerance's order in L
+    # that the quotient divides by h; with tight ones the run's map is smooth at that scale and the
+    # quotients meet the derivative (recomputed under the same tolerances)
+    tight = {"polar": 1e-15, "radial_return": 1e-13}
+    dynela.set_stop_tolerances(tight["polar"], tight["radial_return"])
+    try:
+        d.reset(m)
+        xs, dxs = d.sensitivities(dts)
+        ws = np.zeros((m.N, 3))
+        ws[surf] = 2.0 * (xs[surf] - xt[surf]) / len(surf)
+        gs = np.einsum("pnj,nj->p", dxs, ws)
+        errs = []
+        for p in range(4):
+            h = 1e-6 * pv[p]
+            lp, lm = (loss_at(pv + s * h * np.eye(4)[p]) for s in (1.0, -1.0))
+            errs.append(float(abs((lp - lm) / (2 * h) - gs[p]) / abs(gs[p])))
+    finally:
+        dynela.set_stop_tolerances()
+    fd_tight = {"h": 1e-6, "relative_error": errs, "stop_tolerances": tight,
+                "derivative_change_vs_reference_tolerances": float(np.max(np.abs(gs - g) / np.abs(g)))}
     # reverse mode: the same gradient by dnl_adjoint_forward (the run with a checkpoint every
     # ceil(sqrt(steps)) steps, the final shape), the loss's dL/dx on the host, then
     # dnl_adjoint_backward (the reverse sweep); CUDA events around the whole sequence
@@ -726,6 +748,7 @@ def sens_line(args, fd_steps=(1e-5, 1e-6, 1e-7)) -> dict:
             "agreement_vs_forward_mode": float(np.max(np.abs(g_rev - g) / np.abs(g))),
             "agreement_vs_dual_oracle": agree,
             "agreement_vs_central_differences": {"relative_error_by_relative_h": fd_rel,
+                                                 "with_tight_stopping_tests": fd_tight,
                                                  "of": "the forward-mode gradient"},
             "forward_mode": forward_mode,
             "gpu_launches": rev_launches,

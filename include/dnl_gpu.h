@@ -428,6 +428,17 @@ int dnl_measure_fp64_peak(double *tflops);
  * them only between runs (no call of the library in flight).  No counterpart in the reference,
  * whose limits are literals. */
 int dnl_set_iteration_caps(int rotations, int newton, int power);
+/* Stopping tests of the element pass's two iterations: the polar decomposition stops once every
+ * off-diagonal |C_pq| < polar (Tensor2.C:1180, default 1e-9) and the radial return once
+ * |f / sigma_y| <= radial (Element.C:315, default 1e-8).  A negative value restores the reference's
+ * default; 0 or >= 1 is refused.  Tighter tolerances move results away from the reference's, which
+ * the parity tests hold at the defaults; they exist to check derivatives (dnl_sens_run,
+ * dnl_adjoint) against difference quotients of the run: with the reference's tolerances a
+ * parameter change of 1e-6 relative can add or remove an iteration somewhere, a jump in the run's
+ * map of the tolerance's order that a difference quotient divides by h.  Process-wide device
+ * constants of the current device; change them only between runs.  No counterpart in the
+ * reference, whose tolerances are literals. */
+int dnl_set_stop_tolerances(double polar, double radial);
 /* Self-check of the element and nodal kernels' division helpers on the current device: for each
  * i < n, out[i] = the Newton-Raphson reciprocal 1/b[i] the kernels use, out[n + i] = their quotient
  * a[i]/b[i] (reciprocal + one residual correction), out[2n + i] = CUDA's IEEE 1.0/b[i] and

@@ -586,6 +586,7 @@ void set_shape_tables();
 // loop limits of the element pass (Jacobi passes, Newton iterations; device constants of the
 // current device) and of the Pulse power iteration (host-side)
 int set_iteration_caps(int rotations, int newton);
+int set_stop_tolerances(double polar, double radial);
 int &pulse_cap();
 long long &launch_counter();
 // batched launches (dnl_batch.cu)

@@ -78,6 +78,22 @@ int set_iteration_caps(int rotations, int newton)
   return cudaMemcpyToSymbol(c_caps, caps, sizeof caps) == cudaSuccess ? 0 : DNL_ERR_CUDA;
 }
 
+// Stopping tests of the same two loops: the polar decomposition stops once every off-diagonal
+// |C_pq| is below c_polarTol (Tensor2.C:1180, 1e-9), the radial return once |f / sigma_y| is at
+// most c_returnTol (Element.C:315, 1e-8).  The defaults are the reference's; dnl_set_stop_tolerances
+// tightens them for checks of derivatives against difference quotients, which these tests make
+// non-smooth (a parameter change can add or remove an iteration).
+__constant__ double c_polarTol = kPolarPrecision;
+__constant__ double c_returnTol = kRadialReturnPrecision;
+
+int set_stop_tolerances(double polar, double radial)
+{
+  return cudaMemcpyToSymbol(c_polarTol, &polar, sizeof polar) == cudaSuccess &&
+                 cudaMemcpyToSymbol(c_returnTol, &radial, sizeof radial) == cudaSuccess
+             ? 0
+             : DNL_ERR_CUDA;
+}
+
 long long &launch_counter()
 {
   static long long n = 0;
@@ -573,7 +589,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         k = p0 ? (q1 ? 0 : 1) : 2;
         fpq = p0 ? f0q : f12;
       }
-      if (abits(fpq) < abits(kPolarPrecision)) {
+      if (abits(fpq) < abits(c_polarTol)) {
         conv = true;
         break;
       }
@@ -747,7 +763,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         hardening_law(m.hard, RADD(evp, RMUL(kSqrt23, gamma)), Sigv, h);
         const double dfun = kSqrt32 * m.G2 + kSqrt23 * h;
         const double fun = dfun * gamma - (Strial - Sigv + h * kSqrt23 * gamma);
-        if (fabs(fun / Sigv) > kRadialReturnPrecision) {
+        if (fabs(fun / Sigv) > c_returnTol) {
           double dgamma = -fun / dfun;
           if (dgamma < 0 && fabs(dgamma) > gamma) dgamma = -gamma * 0.9;
           gamma += dgamma;
@@ -795,7 +811,7 @@ __device__ __forceinline__ void elem_ip(const ElemArgs &a, const Material &m, De
         h = m.nB * xn * nr_rcp(xv);  // n B xv^(n-1)
         const double dfun = fma(kSqrt23, h, m.dfun0);
         const double fun = fma(dfun, gamma, -fma(h * kSqrt23, gamma, Strial - Sigv));
-        if (abs_gt(fun, kRadialReturnPrecision * Sigv)) {  // |fun / Sigv| > 1e-8, Sigv > 0
+        if (abs_gt(fun, c_returnTol * Sigv)) {  // |fun / Sigv| > 1e-8, Sigv > 0
           double dgamma = -fun * nr_rcp(dfun);
           // dgamma < 0 && |dgamma| > gamma, with gamma > 0
           if (__double_as_longlong(dgamma) < 0 && abs_gt(dgamma, gamma)) dgamma = -gamma * 0.9;

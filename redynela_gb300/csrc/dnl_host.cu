@@ -688,6 +688,16 @@ int dnl_set_iteration_caps(int rotations, int newton, int power)
   return 0;
 }
 
+int dnl_set_stop_tolerances(double polar, double radial)
+{
+  if (!(polar < 1.0) || !(radial < 1.0) || polar == 0.0 || radial == 0.0) return DNL_ERR_ARG;
+  if (int r = set_stop_tolerances(polar < 0 ? kPolarPrecision : polar, radial < 0 ? kRadialReturnPrecision : radial)) {
+    snprintf(g_lastError, sizeof g_lastError, "cudaMemcpyToSymbol of the stop tolerances failed");
+    return r;
+  }
+  return 0;
+}
+
 int dnl_check_quotients(int n, const double *a, const double *b, double *out)
 {
   if (n <= 0 || !a || !b || !out) return DNL_ERR_ARG;

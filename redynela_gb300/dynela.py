@@ -130,6 +130,7 @@ def lib():
         L.dnl_measure_fp64_peak.argtypes = [_dp]
         L.dnl_check_quotients.argtypes = [C.c_int, _dp, _dp, _dp]
         L.dnl_set_adjoint_record_budget.argtypes = [C.c_ulonglong]
+        L.dnl_set_stop_tolerances.argtypes = [C.c_double, C.c_double]
         L.dnl_set_iteration_caps.argtypes = [C.c_int, C.c_int, C.c_int]
         L.dnl_set_device.argtypes = [C.c_int]
         L.dnl_host_alloc.argtypes = [C.c_ulonglong, C.POINTER(C.c_void_p)]
@@ -213,6 +214,15 @@ def check_quotients(a: np.ndarray, b: np.ndarray) -> Dict[str, np.ndarray]:
         raise DnlError(rc, lib().dnl_error_string(rc).decode())
     o = out.reshape(4, n)
     return {"rcp": o[0], "quot": o[1], "ieee_rcp": o[2], "ieee_quot": o[3]}
+
+
+def set_stop_tolerances(polar: float = -1.0, radial: float = -1.0) -> None:
+    """dnl_set_stop_tolerances: the polar decomposition's and the radial return's stopping
+    tolerances (negative: the reference's 1e-9 and 1e-8), for derivative checks against
+    difference quotients."""
+    rc = lib().dnl_set_stop_tolerances(float(polar), float(radial))
+    if rc:
+        raise DnlError(rc, lib().dnl_error_string(rc).decode())
 
 
 def set_adjoint_record_budget(nbytes: int) -> None:

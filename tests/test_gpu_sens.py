@@ -300,3 +300,47 @@ def test_graph_replay_matches_step_by_step(gpu_lib):
     x5, dx5 = gpu_lib.GpuDomain(m2).sensitivities(dts)
     assert np.array_equal(x4, x5) and np.array_equal(dx4, dx5)
     assert not np.array_equal(x4, x1)
+
+
+def test_gradient_workload_central_differences_with_tight_stopping_tests(gpu_lib):
+    """The gradient workload (20x200 axisymmetric bar, its 4,000-step schedule, the squared
+    distance of the free surface to the shape of (110 MPa, 310 MPa, 0.28)) at the configured
+    h = 1e-6 relative: with the polar decomposition's and the radial return's stopping tests
+    tightened (dnl_set_stop_tolerances 1e-15, 1e-13) the run's map is smooth at that scale and the
+    central differences meet the forward-mode derivative to 1e-5 for all four parameters (measured
+    2e-7 and below; with the reference's 1e-9 and 1e-8 a parameter change of 1e-6 can add or remove
+    an iteration somewhere in the run and the quotient for n is 2.6e-5 away).  The default
+    tolerances are restored afterwards and give the reference's results again."""
+    m = meshes.taylor_axi(20, 200)
+    v0 = float(np.linalg.norm(m.v0))
+    d = gpu_lib.GpuDomain(m)
+    d.prologue()
+    dts = []
+    for _ in range(4000):
+        dts.append(d.time_info()["time_step"])
+        d.step(1)
+    dts = np.array(dts)
+    surf = meshes.taylor_axi_free_surface(20, 200)
+    xt = gpu_lib.GpuDomain(gpu_lib.model_with_params(m, 110e6, 310e6, 0.28, v0)).run_schedule(dts)
+    pv = np.array([m.A, m.B, m.n, v0])
+    x_default = gpu_lib.GpuDomain(m).run_schedule(dts)
+    gpu_lib.set_stop_tolerances(1e-15, 1e-13)
+    try:
+        x, dx = gpu_lib.GpuDomain(m).sensitivities(dts)
+        w = np.zeros((m.N, 3))
+        w[surf] = 2.0 * (x[surf] - xt[surf]) / len(surf)
+        g = np.einsum("pnj,nj->p", dx, w)
+        e = gpu_lib.GpuDomain(m)
+
+        def loss(q):
+            e.reset(gpu_lib.model_with_params(m, *q))
+            xq = e.run_schedule(dts)
+            return float(np.mean(np.sum((xq[surf] - xt[surf]) ** 2, axis=1)))
+
+        for p in range(4):
+            h = 1e-6 * pv[p]
+            fd = (loss(pv + h * np.eye(4)[p]) - loss(pv - h * np.eye(4)[p])) / (2 * h)
+            assert abs(fd - g[p]) <= 1e-5 * abs(g[p]), (p, fd, g[p])
+    finally:
+        gpu_lib.set_stop_tolerances()
+    assert np.array_equal(gpu_lib.GpuDomain(m).run_schedule(dts), x_default)
