@@ -344,3 +344,51 @@ def test_gradient_workload_central_differences_with_tight_stopping_tests(gpu_lib
     finally:
         gpu_lib.set_stop_tolerances()
     assert np.array_equal(gpu_lib.GpuDomain(m).run_schedule(dts), x_default)
+
+
+@pytest.mark.parametrize("etype,nsteps", [("axi", 120), ("plane", 120), ("hex", 80), ("tet4", 80),
+                                          ("hex1pt", 80), ("neck", 60), ("hex_tet", 60)])
+def test_tangents_vs_central_differences_with_tight_stopping_tests(gpu_lib, etype, nsteps):
+    """Every element type (and a domain of two, and the bar pulled by an imposed speed): the
+    forward-mode tangents of a linear functional of the final coordinates against central
+    differences of the GPU's own scheduled run at h = 1e-5 relative, with the stopping tests
+    tightened (1e-15, 1e-13), to 1e-5 per parameter (measured 3.3e-7 and below).  At the
+    reference's tolerances the 3D quotients carry the iterations' jumps divided by h (up to 1e-2 at
+    this h on these bars), which is why the oracle's own checks of 3D tangents need h = 1e-3."""
+    m = {"axi": lambda: meshes.taylor_axi(4, 30), "plane": lambda: meshes.taylor_plane(4, 30),
+         "hex": lambda: meshes.taylor_hex(4, 10), "tet4": lambda: meshes.taylor_tet(6, 8),
+         "hex1pt": lambda: meshes.taylor_hex_1pt(6, 10),
+         "neck": lambda: meshes.necking_bar(4, 12, speed=5.0),
+         "hex_tet": lambda: meshes.taylor_mixed(4, 8, lower=meshes.ELHEX8N3D,
+                                                upper=meshes.ELTET4N3D)}[etype]()
+    gpu_lib.set_stop_tolerances(1e-15, 1e-13)
+    try:
+        d = gpu_lib.GpuDomain(m)
+        d.prologue()
+        dts = []
+        for _ in range(nsteps):
+            dts.append(d.time_info()["time_step"])
+            d.step(1)
+        dts = np.array(dts)
+        w = np.zeros((m.N, 3))
+        w[:, :m.dim] = np.random.default_rng(3).normal(size=(m.N, m.dim))
+        _, dx = gpu_lib.GpuDomain(m).sensitivities(dts)
+        g = np.einsum("pnj,nj->p", dx, w)
+        pv = np.array([m.A, m.B, m.n, np.linalg.norm(m.v0)])
+        e = gpu_lib.GpuDomain(m)
+        live = 0
+        for p in range(4):
+            if pv[p] == 0.0:  # the pulled bar starts at rest: no initial-speed derivative
+                assert g[p] == 0.0
+                continue
+            h = 1e-5 * pv[p]
+            ls = []
+            for sgn in (1.0, -1.0):
+                e.reset(gpu_lib.model_with_params(m, *(pv + sgn * h * np.eye(4)[p])))
+                ls.append(float(np.sum(e.run_schedule(dts) * w)))
+            fd = (ls[0] - ls[1]) / (2 * h)
+            assert abs(fd - g[p]) <= 1e-5 * abs(g[p]), (p, fd, g[p])
+            live += 1
+        assert live >= 3
+    finally:
+        gpu_lib.set_stop_tolerances()
