@@ -893,6 +893,61 @@ def necking_line(args) -> dict:
     return line
 
 
+def main_fd_sweep(args):
+    """Forward-mode tangents against central differences, every element type: a small bar of each
+    (and a domain of two, and the tensile bar pulled by an imposed speed) over its own plain run's
+    step sizes, L = a seeded random linear functional of the final coordinates, the largest
+    relative distance over A, B, n, |v0| of the central quotient of L (dnl_run_schedule at
+    p +- h p) from the tangent, at h = 1e-5, 1e-6, 1e-7 relative; with the reference's stopping
+    tests and with them tightened (dnl_set_stop_tolerances 1e-15, 1e-13).  One JSON line; not a
+    throughput measurement."""
+    from redynela_gb300 import build, dynela
+    build.build()
+    bars = {"axi_4x30": (meshes.taylor_axi(4, 30), 120), "plane_4x30": (meshes.taylor_plane(4, 30), 120),
+            "hex_4x4x10_pulse": (meshes.taylor_hex(4, 10), 80), "tet4_6x6x8": (meshes.taylor_tet(6, 8), 80),
+            "hex1pt_6x6x10": (meshes.taylor_hex_1pt(6, 10), 80),
+            "tensile_4x4x12_speed": (meshes.necking_bar(4, 12, speed=5.0), 60),
+            "hex_tet_4x4x8": (meshes.taylor_mixed(4, 8, lower=meshes.ELHEX8N3D, upper=meshes.ELTET4N3D), 60)}
+    steps = (1e-5, 1e-6, 1e-7)
+    out = {}
+    try:
+        for tight in (False, True):
+            dynela.set_stop_tolerances(*((1e-15, 1e-13) if tight else (-1.0, -1.0)))
+            for name, (m, n) in bars.items():
+                d = dynela.GpuDomain(m)
+                d.prologue()
+                dts = []
+                for _ in range(n):
+                    dts.append(d.time_info()["time_step"])
+                    d.step(1)
+                dts = np.array(dts)
+                w = np.zeros((m.N, 3))
+                w[:, :m.dim] = np.random.default_rng(3).normal(size=(m.N, m.dim))
+                _, dx = dynela.GpuDomain(m).sensitivities(dts)
+                g = np.einsum("pnj,nj->p", dx, w)
+                pv = np.array([m.A, m.B, m.n, np.linalg.norm(m.v0)])
+                e = dynela.GpuDomain(m)
+                worst = {}
+                for hrel in steps:
+                    errs = []
+                    for p in range(4):
+                        if pv[p] == 0.0 or g[p] == 0.0:
+                            continue
+                        h = hrel * pv[p]
+                        ls = []
+                        for sgn in (1.0, -1.0):
+                            e.reset(dynela.model_with_params(m, *(pv + sgn * h * np.eye(4)[p])))
+                            ls.append(float(np.sum(e.run_schedule(dts) * w)))
+                        errs.append(abs((ls[0] - ls[1]) / (2 * h) - g[p]) / abs(g[p]))
+                    worst[f"{hrel:.0e}"] = max(errs)
+                out.setdefault(name, {})["tight" if tight else "reference"] = worst
+    finally:
+        dynela.set_stop_tolerances()
+    print(json.dumps({"metric": "max relative distance of central differences from the tangents",
+                      "stop_tolerances": {"reference": [1e-9, 1e-8], "tight": [1e-15, 1e-13]},
+                      "by_bar": out}), flush=True)
+
+
 def main_full_run(args):
     """The whole run of a bar (`--config hex` or `hex1pt`) from t = 0 to its end time (80 us), not a
     window: the prologue, then dnl_run, CUDA events on the library's stream around the run.
@@ -930,7 +985,8 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="hex", choices=["hex", "hex1pt", "axi", "batch", "sens", "necking"])
+    ap.add_argument("--config", default="hex",
+                    choices=["hex", "hex1pt", "axi", "batch", "sens", "necking", "fdsweep"])
     ap.add_argument("--necking-instances", type=int, default=32)
     ap.add_argument("--necking-start", type=int, default=15000,
                     help="schedule step at which the necking window starts (reached untimed)")
@@ -963,6 +1019,8 @@ def main():
         main_sens(args)
     elif args.config == "necking":
         main_necking(args)
+    elif args.config == "fdsweep":
+        main_fd_sweep(args)
     elif args.full_run:
         main_full_run(args)
     else:
