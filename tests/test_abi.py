@@ -73,3 +73,16 @@ def test_create_rejects_bad_arguments_on_host(libpath):
     md.etype = 1  # hex8 has no Courant length (ElHex8n3D.C:188-192)
     assert L.dnl_create(C.byref(md), C.byref(mat), C.byref(sp_hex), C.byref(h)) == 6
     assert L.dnl_destroy(None) == 6
+
+
+def test_host_side_refusals_of_the_newer_entry_points(libpath):
+    """dnl_step_host, dnl_add_elements and dnl_set_stop_tolerances check their arguments before any
+    device call: a null handle, a step count below 1, integration-point fields in a host-step view,
+    tolerances of 0 or at least 1 are DNL_ERR_ARG without a GPU."""
+    from redynela_gb300 import dynela
+    L = dynela.lib()
+    done = C.c_int(0)
+    assert L.dnl_step_host(None, None, 1, None, C.byref(done)) == 6
+    assert L.dnl_add_elements(None, 1, 1, None) == 6
+    for polar, radial in ((0.0, 1e-8), (1e-9, 0.0), (1.0, 1e-8), (1e-9, 2.0), (float("nan"), 1e-8)):
+        assert L.dnl_set_stop_tolerances(polar, radial) == 6, (polar, radial)
