@@ -303,8 +303,9 @@ typedef struct {
 /* Several materials in one mesh (Structure::attachMaterialToElements per ElementSet) and any of
  * the hardening laws: element e gets mats[elem_material[e]] (elem_material NULL: one material for
  * all).  As Domain::initSolve, each node's density is that of the last element holding it and the
- * Courant sound speed of an element averages those densities.  Before the prologue; with the
- * Pulse time step one material only.  Sensitivity runs need one power-law material. */
+ * Courant sound speed of an element averages those densities; the Pulse power iteration forms
+ * each element's K x with its own material's Hooke matrix (Element3D.C:242-333).  Before the
+ * prologue.  Sensitivity runs need one power-law material. */
 int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, const int *elem_material);
 
 /* -------------------------------------------------------------- results / restart files */

@@ -477,6 +477,8 @@ struct dnl_handle {
   double *elemCs;             // device, E: sound speed with the nodal densities of Domain::initSolve
   double *matTab;             // device: the tabular laws' points
   double *evpn0;              // device, nmat: (1e-10)^n of power-law materials (dnl_reset)
+  double *hooke;              // device, nmat x 3: each material's Hooke entries C00, C01, C33 for
+                              // the Pulse products, with several materials and the Pulse step
   double *nodeRo;             // host, N: Current ro of the first nodal field (results files)
   // initial state (dnl_reset)
   double *x0;                 // initial coordinates [3][N]

@@ -294,6 +294,17 @@ int check_launch()
   return 0;
 }
 
+// Material::getHookeMatrix (Material.C:270-331): the diagonal f = E (1 - nu) / ((1 + nu) (1 - 2 nu)),
+// the off-diagonal nu / (1 - nu) f and the shear (1 - 2 nu) / (2 (1 - nu)) f, in the reference's
+// expressions
+void hooke_entries(double young, double nu, double c[3])
+{
+  const double f = (young * (1.0 - nu) / ((1.0 + nu) * (1.0 - 2.0 * nu)));
+  c[0] = 1 * f;
+  c[1] = (nu / (1. - nu)) * f;
+  c[2] = ((1.0 - 2.0 * nu) / (2. * (1.0 - nu))) * f;
+}
+
 // node-major staging slots <-> component arrays for every field of the set, one launch
 int transpose_set(dnl_handle *h, const FieldSet &s, bool toDevice, cudaStream_t st)
 {
@@ -765,7 +776,7 @@ int dnl_destroy(dnl_handle *h)
   void *ptrs[] = {h->conn, h->x[0], h->n2eStart, h->n2e, h->mass, h->fieldMem, h->ip, h->detJ,
                   h->stepT, h->fe, h->fint, h->stage, h->bcIdx, h->bcCode, h->bcNodeList, h->bcSpeed,
                   h->pj, h->ev, h->kx, h->tm, h->x0, h->elemMat, h->dmats, h->elemCs,
-                  h->matTab, h->evpn0};
+                  h->matTab, h->evpn0, h->hooke};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int gi = 0; gi < h->nextra; gi++) {
@@ -802,7 +813,6 @@ int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, con
   if (h && h->nextra) return DNL_ERR_ARG;  // a domain of several element types holds one material
   if (!h || nmat < 1 || !mats || h->prologueDone) return DNL_ERR_ARG;
   if (nmat > 1 && !elem_material) return DNL_ERR_ARG;
-  if (nmat > 1 && h->method == DNL_PULSE) return DNL_ERR_ARG;  // one Hooke matrix per handle
   const long N = h->N, E = h->E, nIP = h->nIP;
   if (elem_material)
     for (long e = 0; e < E; e++)
@@ -820,7 +830,7 @@ int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, con
     }
   }
   // drop an earlier assignment
-  void *old[] = {h->elemMat, h->dmats, h->elemCs, h->matTab, h->evpn0};
+  void *old[] = {h->elemMat, h->dmats, h->elemCs, h->matTab, h->evpn0, h->hooke};
   for (void *p : old)
     if (p) cudaFree(p);
   h->elemMat = nullptr;
@@ -828,6 +838,7 @@ int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, con
   h->elemCs = nullptr;
   h->matTab = nullptr;
   h->evpn0 = nullptr;
+  h->hooke = nullptr;
   delete[] h->nodeRo;
   h->nodeRo = nullptr;
   if (ntab) CK(cudaMalloc(&h->matTab, sizeof(double) * ntab));
@@ -848,12 +859,19 @@ int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, con
   }
   h->nmat = nmat;
   h->mat = hm[0];
-  {  // Material::getHookeMatrix of material 0 for the Pulse estimate
-    const double Nu = h->mat.nu;
-    const double f = (h->mat.young * (1.0 - Nu) / ((1.0 + Nu) * (1.0 - 2.0 * Nu)));
-    h->C00 = 1 * f;
-    h->C01 = (Nu / (1. - Nu)) * f;
-    h->C33 = ((1.0 - 2.0 * Nu) / (2. * (1.0 - Nu))) * f;
+  {  // Material::getHookeMatrix of material 0 for the Pulse estimate, and of every material when
+     // the Pulse products take each element's
+    double c[3];
+    hooke_entries(h->mat.young, h->mat.nu, c);
+    h->C00 = c[0];
+    h->C01 = c[1];
+    h->C33 = c[2];
+    if (nmat > 1 && h->method == DNL_PULSE) {
+      std::vector<double> hk(3 * (size_t)nmat);
+      for (int i = 0; i < nmat; i++) hooke_entries(hm[i].young, hm[i].nu, &hk[3 * (size_t)i]);
+      CK(cudaMalloc(&h->hooke, sizeof(double) * hk.size()));
+      CK(cudaMemcpy(h->hooke, hk.data(), sizeof(double) * hk.size(), cudaMemcpyHostToDevice));
+    }
   }
   // nodal densities as Domain::initSolve assigns them: element order, the last element wins
   std::vector<int> conn((size_t)E * h->nen);
@@ -914,11 +932,11 @@ int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0)
   h->ngraphs = 0;  // captured launches hold the old material and state by value
   if (mat) {
     h->mat = make_material(*mat, h->nen);
-    const double Nu = h->mat.nu;
-    const double f = (h->mat.young * (1.0 - Nu) / ((1.0 + Nu) * (1.0 - 2.0 * Nu)));
-    h->C00 = 1 * f;
-    h->C01 = (Nu / (1. - Nu)) * f;
-    h->C33 = ((1.0 - 2.0 * Nu) / (2. * (1.0 - Nu))) * f;
+    double c[3];
+    hooke_entries(h->mat.young, h->mat.nu, c);
+    h->C00 = c[0];
+    h->C01 = c[1];
+    h->C33 = c[2];
     // a domain of several element types: each group's Courant sound speed with its own node count
     // (one material, so h->elemCs holds the first group's speed when it exists)
     if (h->nextra && h->elemCs) {
@@ -1192,12 +1210,11 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
     CKF(cudaMalloc(&h->pj, sizeof(double) * (size_t)npj * h->nIP));
     CKF(cudaMalloc(&h->ev, sizeof(double) * (size_t)h->dim * N));
     CKF(cudaMalloc(&h->kx, sizeof(double) * (size_t)h->dim * E * nen));
-    // Material::getHookeMatrix (Material.C:270-331): entries times E(1-nu)/((1+nu)(1-2nu))
-    const double Nu = m.nu;
-    const double f = (m.young * (1.0 - Nu) / ((1.0 + Nu) * (1.0 - 2.0 * Nu)));
-    h->C00 = 1 * f;
-    h->C01 = (Nu / (1. - Nu)) * f;
-    h->C33 = ((1.0 - 2.0 * Nu) / (2. * (1.0 - Nu))) * f;
+    double c[3];
+    hooke_entries(m.young, m.nu, c);
+    h->C00 = c[0];
+    h->C01 = c[1];
+    h->C33 = c[2];
   }
   // ---- time state
   CKF(cudaMalloc(&h->tm, sizeof(DevTime)));

@@ -123,6 +123,10 @@ struct PulseArgs {
   const double *mass;
   DevTime *tm;
   double C00, C01, C33;
+  // several materials: each element's material (elemMat) and the materials' Hooke entries
+  // (hooke, 3 per material: C00, C01, C33), or nullptr (one material: C00, C01, C33 above)
+  const int *elemMat;
+  const double *hooke;
 };
 
 // ------------------------------------------------------------------ per-Gauss-point kinematics
@@ -307,22 +311,30 @@ __global__ void __launch_bounds__(128) k_pulse_kx(PulseArgs a)
       gr[r][c] = s;
     }
   // Hooke stress S of the in-plane components and, axisymmetric, the hoop stress (plane strain:
-  // the upper-left block of the axisymmetric matrix, no hoop strain)
+  // the upper-left block of the axisymmetric matrix, no hoop strain); with several materials the
+  // element's own matrix (Element2D/3D::computeElasticStiffnessMatrix reads the element's material)
+  double C00 = a.C00, C01 = a.C01, C33 = a.C33;
+  if (a.elemMat) {
+    const double *c = a.hooke + 3 * __ldg(a.elemMat + e);
+    C00 = c[0];
+    C01 = c[1];
+    C33 = c[2];
+  }
   double S[DIM][DIM], hoop = 0.;
   if (DIM == 2) {
     const double e0 = gr[0][0], e1 = gr[1][1], e2 = gr[0][1] + gr[1][0], e3 = AXI ? ur / Rad : 0.;
-    S[0][0] = a.C00 * e0 + a.C01 * (e1 + e3);
-    S[1][1] = a.C00 * e1 + a.C01 * (e0 + e3);
-    S[0][1] = S[1][0] = a.C33 * e2;
-    hoop = a.C00 * e3 + a.C01 * (e0 + e1);
+    S[0][0] = C00 * e0 + C01 * (e1 + e3);
+    S[1][1] = C00 * e1 + C01 * (e0 + e3);
+    S[0][1] = S[1][0] = C33 * e2;
+    hoop = C00 * e3 + C01 * (e0 + e1);
   } else {
     const double e0 = gr[0][0], e1 = gr[1][1], e2 = gr[2][2];
-    S[0][0] = a.C00 * e0 + a.C01 * (e1 + e2);
-    S[1][1] = a.C00 * e1 + a.C01 * (e0 + e2);
-    S[2][2] = a.C00 * e2 + a.C01 * (e0 + e1);
-    S[0][1] = S[1][0] = a.C33 * (gr[0][1] + gr[1][0]);
-    S[1][2] = S[2][1] = a.C33 * (gr[1][2] + gr[2][1]);
-    S[0][2] = S[2][0] = a.C33 * (gr[0][2] + gr[2][0]);
+    S[0][0] = C00 * e0 + C01 * (e1 + e2);
+    S[1][1] = C00 * e1 + C01 * (e0 + e2);
+    S[2][2] = C00 * e2 + C01 * (e0 + e1);
+    S[0][1] = S[1][0] = C33 * (gr[0][1] + gr[1][0]);
+    S[1][2] = S[2][1] = C33 * (gr[1][2] + gr[2][1]);
+    S[0][2] = S[2][0] = C33 * (gr[0][2] + gr[2][0]);
   }
   double M[DIM][DIM];
 #pragma unroll
@@ -500,6 +512,8 @@ int launch_pulse(dnl_handle *h, cudaStream_t s)
   a.C00 = h->C00;
   a.C01 = h->C01;
   a.C33 = h->C33;
+  a.elemMat = h->hooke ? h->elemMat : nullptr;
+  a.hooke = h->hooke;
   // Domain::fmax0 == 0: the vector starts as the ramp EV(0) = 1, EV(i) = EV(i-1) - 2/(noddl-1)
   DevTime t;
   if (cudaMemcpyAsync(&t, h->tm, sizeof t, cudaMemcpyDeviceToHost, s) != cudaSuccess) return DNL_ERR_CUDA;
@@ -528,6 +542,7 @@ int launch_pulse(dnl_handle *h, cudaStream_t s)
     ga[gi].conn = g.conn;
     ga[gi].pj = g.pj;
     ga[gi].kx = h->kx + g.feOff;
+    ga[gi].elemMat = nullptr;  // one material on a domain of several element types
     if (!g.pj) return DNL_ERR_ARG;
   }
   auto gridOf = [](const ElemGroup &g) { return (int)(((long)g.E * g.nip + 127) / 128); };

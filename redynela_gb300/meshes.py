@@ -352,6 +352,27 @@ def impact_two_materials(nr: int = 5, nz: int = 50, radius: float = 3.2e-3,
                                initial_velocity=v)
 
 
+def impact_two_materials_hex(ncross: int = 6, nz: int = 12, radius: float = 3.2e-3,
+                             length: float = 32.4e-3, split: float = 0.5, speed: float = 80.0,
+                             tend: float = 40e-6, freq: int = 10) -> Model:
+    """impact_two_materials' bonded pair on taylor_hex's 3D bar of ElHex8n3D, Pulse time step:
+    the layers below split*nz are the tabular-hardening target, those above the elastic projectile,
+    whose nodes (the interface plane's included) start at `speed` towards the base; the base is
+    restrained in z."""
+    m = taylor_hex(ncross, nz, radius, length, 0.0, tend=tend, freq=freq)
+    tx, ty = tabular_table(360e6, 316e6, 0.28)
+    target = MaterialLaw(74.2e9, 0.33, 2784.0, HARD_TABULAR, (), tx, ty)
+    projectile = MaterialLaw(193.6e9, 0.3, 7800.0, HARD_ELASTIC, ())
+    js = int(round(split * nz))
+    dz = length / nz
+    em = (m.coords[m.conn[:, 0], 2] >= js * dz - 0.5 * dz).astype(np.int64)  # bottom face's layer
+    v = np.zeros((m.N, 3))
+    v[m.coords[:, 2] >= js * dz - 0.5 * dz, 2] = -speed
+    return dataclasses.replace(m, young=74.2e9, poisson=0.33, density=2784.0,
+                               materials=[target, projectile], elem_material=em,
+                               initial_velocity=v)
+
+
 def metafor_bar(nr: int = 5, nz: int = 50, speed: float = 227.0, tend: float = 40e-6,
                 P=(90e6, 200e6, 10.0, 50e6, 0.5, 1.0, 0.1, 1e8)) -> Model:
     """The copper Taylor bar with an IsoHardMetafor law (P1..P8):

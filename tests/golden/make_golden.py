@@ -14,6 +14,9 @@ reference's own output on a seeded synthetic model:
 * ``steps_two.npz``     two bonded materials in the pattern of Samples/Traction (tabular target,
                         elastic projectile with its own initial velocity), first 40 steps
 * ``steps_metafor.npz`` the 5x50 bar with an IsoHardMetafor law, first 40 steps
+* ``steps_two_hex.npz`` the same two bonded materials on a 4x4x12-cell ElHex8n3D bar with the Pulse
+                        time step (each element's own Hooke matrix in the power iteration), first 30
+                        steps
 * ``results_axi.bin``   the reference's binary results file (Structure::writeData) of the 3x4 axi bar
                         after 13 steps, and ``results_axi.npz`` its state from the harness
 * ``forces_plane.npz``  one Domain::computeInternalForces on an injected state, 3x4 ElQua4n2D bar
@@ -95,6 +98,15 @@ def laws():
              fint=np.stack([r[f"fint_{k:06d}"] for k in range(40)]),
              final_coords=r["final_coords"], final_evp=r["final_evp"], final_S=r["final_S"],
              final_p=r["final_p"])
+
+
+def laws3d():
+    """The 3D two-material fixture only: python tests/golden/make_golden.py laws3d"""
+    m = meshes.impact_two_materials_hex(4, 12)
+    r = dnl_io.run_reference("steps", m, 30)
+    save("steps_two_hex.npz", mass=r["mass"], dt0=r["dt0"], dt=r["dt"], time=r["time"],
+         fint=np.stack([r[f"fint_{k:06d}"] for k in range(30)]), final_coords=r["final_coords"],
+         final_evp=r["final_evp"], final_S=r["final_S"])
 
 
 def plane():
@@ -196,6 +208,9 @@ def main():
     if sys.argv[1:] == ["plane"]:
         plane()
         return
+    if sys.argv[1:] == ["laws3d"]:
+        laws3d()
+        return
     if sys.argv[1:] == ["tets"]:
         tets()
         return
@@ -239,6 +254,7 @@ def main():
 
     results()
     laws()
+    laws3d()
     plane()
     tets()
     speed()

@@ -1,8 +1,9 @@
 """Hardening laws other than the power law and several materials per mesh on the GPU
 (dnl_set_materials), against the reference's own outputs (tests/golden, generated from the
 compiled reference): a two-material impact in the pattern of Samples/Traction/Traction.dyn
-(tabular-hardening target, projectile without hardening carrying its own initial velocity) and the
-Taylor bar with an IsoHardMetafor law.  One element pass from identical (injected) states within
+(tabular-hardening target, projectile without hardening carrying its own initial velocity), the
+same pair on a hexahedral bar with the Pulse time step, and the Taylor bar with an IsoHardMetafor
+law.  One element pass from identical (injected) states within
 the per-step tolerance (1e-12 relative 2-norm); along the 40-step trajectories the forces of the
 first 20 steps within 1e-12 and of the next 20 within 1e-11 (the few-ulp differences of each pass
 accumulate); the lumped mass exactly, the first step size to 1e-12."""
@@ -75,6 +76,29 @@ def test_two_materials_longer_run_vs_oracle(gpu_lib):
     x = d.get_state("coords")["coords"].ravel()
     ref = o.array("coords")
     assert np.max(np.abs(x - ref)) <= 1e-9 * np.max(np.abs(ref))
+
+
+def test_two_materials_hex_pulse_vs_reference(gpu_lib):
+    """The two bonded materials on a 4x4x12-cell ElHex8n3D bar with the Pulse time step, whose
+    power iteration forms K x with each element's own Hooke matrix (Element3D.C:242-333 reads the
+    element's material): lumped mass bit for bit, the first step size and the times to 1e-10 (the
+    power iteration sums K x in another order than the reference's assembled Ke), forces of the
+    first 3 steps to 1e-12 and of the next 27 to 1e-7 (3D Jacobi pivot ties, as in
+    test_steps_hex_pulse), final positions to 1e-9; the tabular target yields."""
+    g = golden("steps_two_hex.npz")
+    m = meshes.impact_two_materials_hex(4, 12)
+    d = gpu_lib.GpuDomain(m)
+    d.prologue()
+    assert np.array_equal(d.get_state("mass")["mass"], g["mass"][::3])
+    assert abs(d.time_step() - g["dt0"][0]) <= 1e-10 * g["dt0"][0]
+    for k in range(30):
+        assert d.step(1) == 1
+        if np.linalg.norm(g["fint"][k]) > 0:
+            assert rel(d.fint(), g["fint"][k]) <= (TOL if k < 3 else 1e-7), k
+        assert abs(d.time_info()["time"] - g["time"][k]) <= 1e-10 * g["time"][k], k
+    x = d.get_state("coords")["coords"].ravel()
+    assert np.max(np.abs(x - g["final_coords"])) <= 1e-9 * np.max(np.abs(g["final_coords"]))
+    assert d.get_state("evp")["evp"].max() > 1e-3
 
 
 def test_material_arguments_are_checked(gpu_lib):

@@ -185,6 +185,26 @@ def test_steps_hex_pulse():
     assert np.max(np.abs(x - g["final_coords"])) <= 1e-12 * np.max(np.abs(g["final_coords"]))
 
 
+def test_steps_hex_pulse_two_materials():
+    """The two bonded materials on a hex8 bar with the Pulse time step: the power iteration's
+    element stiffness takes each element's own Hooke matrix (Element3D.C:242-333 reads the
+    element's material); lumped mass bitwise, 30 steps to rounding (K.x summed in element order),
+    the tabular target past yield."""
+    g = golden("steps_two_hex.npz")
+    o = Oracle(meshes.impact_two_materials_hex(4, 12))
+    o.prologue()
+    assert np.array_equal(o.array("Mass"), g["mass"])
+    assert abs(o.get("dt") - g["dt0"][0]) <= 1e-14 * g["dt0"][0]
+    for k in range(30):
+        o.steps(1)
+        f, r = o.array("fint"), g["fint"][k]
+        if np.linalg.norm(r) > 0:
+            assert np.linalg.norm(f - r) <= 1e-12 * np.linalg.norm(r), k
+    x = o.array("coords")
+    assert np.max(np.abs(x - g["final_coords"])) <= 1e-12 * np.max(np.abs(g["final_coords"]))
+    assert g["final_evp"].max() > 1e-3
+
+
 def test_imposed_speed_steps_and_run_vs_reference():
     """The tensile bar with BoundarySpeed::applyConstant on its pulled end (Boundary.C:478-525:
     a = 0, v = the imposed speed and delta_disp = v dt on both nodal fields) and BoundaryRestrain
