@@ -1515,8 +1515,8 @@ static ElemArgs group_args(dnl_handle *h, const ElemGroup &g)
   a.fe = h->fe + g.feOff;
   a.detJ = g.detJ;
   a.stepT = g.stepT;
-  a.elemMat = nullptr;
-  a.mats = nullptr;
+  a.elemMat = h->elemMat ? h->elemMat + g.eOff : nullptr;  // several materials: over all groups
+  a.mats = h->elemMat ? h->dmats : nullptr;
   a.elemCs = g.Cs;
   a.eBase = g.eOff;
   return a;
@@ -1593,7 +1593,7 @@ int launch_mass(dnl_handle *h, cudaStream_t s, double *me)
     const ElemGroup &g = h->extra[gi];
     ElemArgs b = group_args(h, g);
     const int gg = (int)(((long)g.E * g.nip + 127) / 128);
-    DNL_BY_ETYPE(g.etype, (k_mass<ET><<<gg, 128, 0, s>>>(b, me + g.feOff, nullptr, nullptr)));
+    DNL_BY_ETYPE(g.etype, (k_mass<ET><<<gg, 128, 0, s>>>(b, me + g.feOff, b.elemMat, b.mats)));
     launch_counter()++;
   }
   return cudaPeekAtLastError() == cudaSuccess ? 0 : DNL_ERR_CUDA;

@@ -417,11 +417,6 @@ int read_time(dnl_handle *h, DevTime *out)
   return 0;
 }
 
-int status_of(dnl_handle *h, const DevTime &t)
-{
-  (void)h;
-  return t.status;
-}
 
 // one explicit step's launches; post = complete this step's time update afterwards
 int enqueue_step(dnl_handle *h, long long incAfter, bool last)
@@ -578,6 +573,32 @@ void prof_end(dnl_handle *h, int kind, cudaStream_t s)
 }  // namespace dnl
 
 // =============================================================================== C ABI
+// ------------------------------------------------------------------------------ element groups
+namespace {
+bool solid_reference_element(int etype)
+{
+  return etype == DNL_ELHEX8N3D || etype == DNL_ELTET4N3D || etype == DNL_ELTET10N3D;
+}
+
+// every element group's connectivity, node-major per element, in element order
+int all_connectivity(dnl_handle *h, std::vector<int> &conn, std::vector<int> &nenOf)
+{
+  conn.clear();
+  nenOf.clear();
+  for (int gi = -1; gi < h->nextra; gi++) {
+    const int E = gi < 0 ? h->E : h->extra[gi].E, nen = gi < 0 ? h->nen : h->extra[gi].nen;
+    const int *dc = gi < 0 ? h->conn : h->extra[gi].conn;
+    std::vector<int> t((size_t)nen * E);
+    CK(cudaMemcpy(t.data(), dc, sizeof(int) * t.size(), cudaMemcpyDeviceToHost));
+    for (int e = 0; e < E; e++) {
+      for (int k = 0; k < nen; k++) conn.push_back(t[(size_t)k * E + e]);
+      nenOf.push_back(nen);
+    }
+  }
+  return 0;
+}
+}  // namespace
+
 extern "C" {
 
 const char *dnl_error_string(int status)
@@ -810,12 +831,13 @@ int dnl_destroy(dnl_handle *h)
 
 int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, const int *elem_material)
 {
-  if (h && h->nextra) return DNL_ERR_ARG;  // a domain of several element types holds one material
-  if (!h || nmat < 1 || !mats || h->prologueDone) return DNL_ERR_ARG;
+  if (!h || nmat < 1 || !mats || h->prologueDone || h->batchUnion) return DNL_ERR_ARG;
   if (nmat > 1 && !elem_material) return DNL_ERR_ARG;
   const long N = h->N, E = h->E, nIP = h->nIP;
+  long Eall = E;  // elements of every group, in element order
+  for (int gi = 0; gi < h->nextra; gi++) Eall += h->extra[gi].E;
   if (elem_material)
-    for (long e = 0; e < E; e++)
+    for (long e = 0; e < Eall; e++)
       if (elem_material[e] < 0 || elem_material[e] >= nmat) return DNL_ERR_ARG;
   long ntab = 0;
   for (int i = 0; i < nmat; i++) {
@@ -873,40 +895,59 @@ int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, con
       CK(cudaMemcpy(h->hooke, hk.data(), sizeof(double) * hk.size(), cudaMemcpyHostToDevice));
     }
   }
-  // nodal densities as Domain::initSolve assigns them: element order, the last element wins
-  std::vector<int> conn((size_t)E * h->nen);
-  CK(cudaMemcpy(conn.data(), h->conn, sizeof(int) * conn.size(), cudaMemcpyDeviceToHost));  // [NEN][E]
+  // nodal densities as Domain::initSolve assigns them: element order over every group, the last
+  // element wins
+  std::vector<int> conn, nenOf;  // every element's nodes, node-major per element, element order
+  if (all_connectivity(h, conn, nenOf)) return DNL_ERR_CUDA;
+  std::vector<size_t> first(Eall + 1, 0);
+  for (long e = 0; e < Eall; e++) first[e + 1] = first[e] + nenOf[e];
+  auto matOf = [&](long e) { return elem_material ? elem_material[e] : 0; };
   h->nodeRo = new double[N];
   for (long n = 0; n < N; n++) h->nodeRo[n] = hm[0].rho;
-  for (long e = 0; e < E; e++) {
-    const int mi = elem_material ? elem_material[e] : 0;
-    for (int k = 0; k < h->nen; k++) h->nodeRo[conn[(size_t)k * E + e]] = hm[mi].rho;
+  for (long e = 0; e < Eall; e++)
+    for (size_t k = first[e]; k < first[e + 1]; k++) h->nodeRo[conn[k]] = hm[matOf(e)].rho;
+  // the cached evp^n of each group's points at rest, (1e-10)^n of its element's material
+  const int ns = etype_ns(h->etype);  // the same for every group of a domain (one family)
+  for (int gi = -1; gi < h->nextra; gi++) {
+    const long gE = gi < 0 ? E : h->extra[gi].E, gOff = gi < 0 ? 0 : h->extra[gi].eOff;
+    const int gnip = gi < 0 ? h->nip : h->extra[gi].nip;
+    const long gIP = gE * gnip;
+    double *gip = gi < 0 ? h->ip : h->extra[gi].ip;
+    std::vector<double> pnIP(gIP);
+    for (long e = 0; e < gE; e++)
+      for (int q = 0; q < gnip; q++) pnIP[e * gnip + q] = pn[matOf(gOff + e)];
+    CK(cudaMemcpy(gip + (size_t)(3 * ns + 2) * gIP, pnIP.data(), sizeof(double) * gIP, cudaMemcpyHostToDevice));
   }
-  std::vector<double> pnIP(nIP);
-  for (long e = 0; e < E; e++)
-    for (int q = 0; q < h->nip; q++) pnIP[e * h->nip + q] = pn[elem_material ? elem_material[e] : 0];
-  const int ns = etype_ns(h->etype);
-  CK(cudaMemcpy(h->ip + (size_t)(3 * ns + 2) * nIP, pnIP.data(), sizeof(double) * nIP, cudaMemcpyHostToDevice));
+  (void)nIP;
   CK(cudaMalloc(&h->evpn0, sizeof(double) * nmat));
   CK(cudaMemcpy(h->evpn0, pn.data(), sizeof(double) * nmat, cudaMemcpyHostToDevice));
-  if (nmat > 1) {
-    // Element::getSoundSpeed: the element's E and nu, the mean of its nodes' densities
-    std::vector<double> cs(E);
-    for (long e = 0; e < E; e++) {
-      const Material &m = hm[elem_material[e]];
-      double ro = 0.;
-      for (int k = 0; k < h->nen; k++) ro += h->nodeRo[conn[(size_t)k * E + e]];
-      ro /= h->nen;
-      const double Nu = m.nu;
-      cs[e] = sqrt((m.young * (1 - Nu)) / (ro * (1 + Nu) * (1 - 2 * Nu)));
-    }
-    std::vector<int> em(elem_material, elem_material + E);
-    CK(cudaMalloc(&h->elemMat, sizeof(int) * E));
-    CK(cudaMemcpy(h->elemMat, em.data(), sizeof(int) * E, cudaMemcpyHostToDevice));
-    CK(cudaMalloc(&h->dmats, sizeof(Material) * nmat));
-    CK(cudaMemcpy(h->dmats, hm.data(), sizeof(Material) * nmat, cudaMemcpyHostToDevice));
+  // Element::getSoundSpeed: the element's E and nu, the mean of its nodes' densities; kept per
+  // element with several materials, and on a domain of several element types (each group's
+  // array, the first group's in h->elemCs) whatever the materials
+  std::vector<double> cs(Eall);
+  for (long e = 0; e < Eall; e++) {
+    const Material &m = hm[matOf(e)];
+    double ro = 0.;
+    for (size_t k = first[e]; k < first[e + 1]; k++) ro += h->nodeRo[conn[k]];
+    ro /= nenOf[e];
+    const double Nu = m.nu;
+    cs[e] = sqrt((m.young * (1 - Nu)) / (ro * (1 + Nu) * (1 - 2 * Nu)));
+  }
+  if (nmat > 1 || (h->nextra && h->method == DNL_COURANT)) {
     CK(cudaMalloc(&h->elemCs, sizeof(double) * E));
     CK(cudaMemcpy(h->elemCs, cs.data(), sizeof(double) * E, cudaMemcpyHostToDevice));
+    for (int gi = 0; gi < h->nextra; gi++) {
+      ElemGroup &g = h->extra[gi];
+      if (!g.Cs) CK(cudaMalloc(&g.Cs, sizeof(double) * g.E));
+      CK(cudaMemcpy(g.Cs, cs.data() + g.eOff, sizeof(double) * g.E, cudaMemcpyHostToDevice));
+    }
+  }
+  if (nmat > 1) {
+    std::vector<int> em(elem_material, elem_material + Eall);
+    CK(cudaMalloc(&h->elemMat, sizeof(int) * Eall));
+    CK(cudaMemcpy(h->elemMat, em.data(), sizeof(int) * Eall, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&h->dmats, sizeof(Material) * nmat));
+    CK(cudaMemcpy(h->dmats, hm.data(), sizeof(Material) * nmat, cudaMemcpyHostToDevice));
   }
   for (int i = 0; i < h->ngraphs; i++) cudaGraphExecDestroy(h->graphs[i].exec);
   h->ngraphs = 0;
@@ -976,13 +1017,17 @@ int dnl_reset(dnl_handle *h, const dnl_material *mat, const double *v0)
     k_fill<<<(unsigned)((nIP + 255) / 256), 256, 0, s>>>(h->ip + (size_t)(3 * ns + 2) * nIP, nIP,
                                                          h->mat.hard.law == DNL_HARD_POWER ? pow(1e-10, h->mat.n) : 0.);
   launch_counter() += 2;
-  for (int gi = 0; gi < h->nextra; gi++) {  // further element groups: one power-law material
+  for (int gi = 0; gi < h->nextra; gi++) {  // further element groups, as the first
     const ElemGroup &g = h->extra[gi];
     const int gns = etype_ns(g.etype), gnc = 3 * gns + 3;
     CK(cudaMemsetAsync(g.ip, 0, sizeof(double) * gnc * g.nIP, s));
     k_fill<<<(unsigned)((g.nIP + 255) / 256), 256, 0, s>>>(g.ip + (size_t)(3 * gns + 1) * g.nIP, g.nIP, 1e-10);
-    k_fill<<<(unsigned)((g.nIP + 255) / 256), 256, 0, s>>>(g.ip + (size_t)(3 * gns + 2) * g.nIP, g.nIP,
-                                                           pow(1e-10, h->mat.n));
+    if (h->elemMat)
+      k_fill_evpn<<<(unsigned)((g.nIP + 255) / 256), 256, 0, s>>>(g.nIP, g.nip, h->elemMat + g.eOff, h->evpn0,
+                                                                  g.ip + (size_t)(3 * gns + 2) * g.nIP);
+    else
+      k_fill<<<(unsigned)((g.nIP + 255) / 256), 256, 0, s>>>(g.ip + (size_t)(3 * gns + 2) * g.nIP, g.nIP,
+                                                             h->mat.hard.law == DNL_HARD_POWER ? pow(1e-10, h->mat.n) : 0.);
     launch_counter() += 2;
     if (g.stepT) CK(cudaMemsetAsync(g.stepT, 0, sizeof(double) * 18 * g.nIP, s));
   }
@@ -1233,31 +1278,6 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
   return 0;
 }
 
-// ------------------------------------------------------------------------------ element groups
-namespace {
-bool solid_reference_element(int etype)
-{
-  return etype == DNL_ELHEX8N3D || etype == DNL_ELTET4N3D || etype == DNL_ELTET10N3D;
-}
-
-// every element group's connectivity, node-major per element, in element order
-int all_connectivity(dnl_handle *h, std::vector<int> &conn, std::vector<int> &nenOf)
-{
-  conn.clear();
-  nenOf.clear();
-  for (int gi = -1; gi < h->nextra; gi++) {
-    const int E = gi < 0 ? h->E : h->extra[gi].E, nen = gi < 0 ? h->nen : h->extra[gi].nen;
-    const int *dc = gi < 0 ? h->conn : h->extra[gi].conn;
-    std::vector<int> t((size_t)nen * E);
-    CK(cudaMemcpy(t.data(), dc, sizeof(int) * t.size(), cudaMemcpyDeviceToHost));
-    for (int e = 0; e < E; e++) {
-      for (int k = 0; k < nen; k++) conn.push_back(t[(size_t)k * E + e]);
-      nenOf.push_back(nen);
-    }
-  }
-  return 0;
-}
-}  // namespace
 
 int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn)
 {

@@ -542,7 +542,7 @@ int launch_pulse(dnl_handle *h, cudaStream_t s)
     ga[gi].conn = g.conn;
     ga[gi].pj = g.pj;
     ga[gi].kx = h->kx + g.feOff;
-    ga[gi].elemMat = nullptr;  // one material on a domain of several element types
+    ga[gi].elemMat = h->hooke ? h->elemMat + g.eOff : nullptr;  // element materials over all groups
     if (!g.pj) return DNL_ERR_ARG;
   }
   auto gridOf = [](const ElemGroup &g) { return (int)(((long)g.E * g.nip + 127) / 128); };

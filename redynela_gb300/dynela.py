@@ -293,22 +293,23 @@ class GpuDomain:
         self._check(L.dnl_create(C.byref(desc), C.byref(mat), C.byref(sp), C.byref(h)))
         self.h = h
         self.L = L
+        # further element groups first: the materials then cover every group's elements
+        self._groups = []
+        for etype, conn in (m.groups or []):
+            self.add_elements(etype, conn)
         if m.materials or m.elem_material is not None:
             self.set_materials(m.material_laws(), m.elem_material)
         if m.initial_velocity is not None:
             self.set_state(v=np.asarray(m.initial_velocity, dtype=np.float64))
         if m.etype == meshes.ELHEX8N3D_1PT:
             self.set_hourglass(m.hourglass)
-        self._groups = []
-        for etype, conn in (m.groups or []):
-            self.add_elements(etype, conn)
 
     def add_elements(self, etype: int, conn) -> None:
         """dnl_add_elements: a further group of elements of another type in this domain, numbered
         after the elements already there (before the prologue)."""
         c = np.ascontiguousarray(conn, dtype=np.int32)
-        self._groups.append(c)
         self._check(self.L.dnl_add_elements(self.h, int(etype), int(c.shape[0]), c.ctypes.data_as(_ip)))
+        self._groups.append(c)
 
     def set_hourglass(self, coefficient: float) -> None:
         """dnl_set_hourglass: the one-point hexahedron's viscous hourglass coefficient."""
@@ -327,6 +328,9 @@ class GpuDomain:
             arr[i] = MaterialLawDesc(ml.young, ml.poisson, ml.density, int(ml.law), (C.c_double * 8)(*prm),
                                      npts, tx.ctypes.data_as(_dp), ty.ctypes.data_as(_dp))
         em = None if elem_material is None else np.ascontiguousarray(elem_material, dtype=np.int32)
+        nel = self.model.E + sum(c.shape[0] for c in getattr(self, "_groups", []))
+        if em is not None and em.size != nel:  # the library reads one index per element
+            raise ValueError(f"set_materials: {em.size} element materials for {nel} elements")
         self._check(self.L.dnl_set_materials(self.h, len(laws), arr,
                                              em.ctypes.data_as(_ip) if em is not None else None))
 

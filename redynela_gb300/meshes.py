@@ -373,6 +373,15 @@ def impact_two_materials_hex(ncross: int = 6, nz: int = 12, radius: float = 3.2e
                                initial_velocity=v)
 
 
+def group_materials(m: Model, laws: Sequence[MaterialLaw]) -> Model:
+    """The model with material i on the elements of element group i (element_groups order): a
+    domain of several element types whose parts are also of several materials."""
+    groups = m.element_groups()
+    assert len(laws) == len(groups)
+    em = np.concatenate([np.full(c.shape[0], i, dtype=np.int64) for i, (_, c) in enumerate(groups)])
+    return dataclasses.replace(m, materials=list(laws), elem_material=em)
+
+
 def metafor_bar(nr: int = 5, nz: int = 50, speed: float = 227.0, tend: float = 40e-6,
                 P=(90e6, 200e6, 10.0, 50e6, 0.5, 1.0, 0.1, 1e8)) -> Model:
     """The copper Taylor bar with an IsoHardMetafor law (P1..P8):

@@ -40,6 +40,11 @@ reference's own output on a seeded synthetic model:
 * ``steps_mixed.npz``   the 6x6x12-cell bar of ElTet4n3D (6 layers) and ElTet10n3D (6 layers) in one
                         domain, Courant time step: lumped mass and its first 5 steps (its ElTet10n3D
                         part ends in a singular Jacobian a few steps later, as the ElTet10n3D bar)
+* ``forces_mixed_two.npz`` the force pass of ``forces_mixed.npz`` with the ElTet4n3D layer of a
+                        tabular-hardening material and the ElHex8n3D layers of a power-law one
+* ``steps_mixed_two.npz`` the ElTet4n3D + ElTet10n3D bar of ``steps_mixed.npz`` with the two parts
+                        of two materials (other E, nu, rho and hardening above): lumped mass, time
+                        steps and its first 3 steps
 * ``results_mixed.bin`` the reference's results file of the 3x3x4-cell bar of ElTet4n3D (2 layers)
                         and ElTet10n3D (2 layers) after its first 2 steps (the first step's
                         element pass sees the bar at rest): each element's own integration points,
@@ -193,6 +198,26 @@ def mixed():
          final_coords=r["final_coords"], final_S=r["final_S"], final_p=r["final_p"])
 
 
+def mixed_materials():
+    """The mixed element-type, two-material fixtures only:
+    python tests/golden/make_golden.py mixed_materials"""
+    tx, ty = meshes.tabular_table(360e6, 316e6, 0.28)
+    target = meshes.MaterialLaw(74.2e9, 0.33, 2784.0, meshes.HARD_TABULAR, (), tx, ty)
+    copper = meshes.MaterialLaw(117e9, 0.35, 8930.0, meshes.HARD_POWER, (90e6, 292e6, 0.31))
+    m = meshes.group_materials(meshes.taylor_mixed(4, 3, nz_lower=1, lower=meshes.ELTET4N3D,
+                                                   upper=meshes.ELHEX8N3D), [target, copper])
+    st = states.random_state(m, seed=7)
+    r = dnl_io.run_reference("forces", m, state=st)
+    save("forces_mixed_two.npz", **{f"in_{k}": np.asarray(v) for k, v in st.items()}, fint=r["fint"],
+         **{k: r[k] for k in r if k.startswith("out_")})
+    steel = meshes.MaterialLaw(193.6e9, 0.3, 7800.0, meshes.HARD_POWER, (250e6, 400e6, 0.4))
+    m = meshes.group_materials(meshes.taylor_mixed(6, 12), [copper, steel])
+    r = dnl_io.run_reference("steps", m, 3)
+    save("steps_mixed_two.npz", mass=r["mass"], dt0=r["dt0"], dt=r["dt"], time=r["time"],
+         fint=np.stack([r[f"fint_{k:06d}"] for k in range(3)]), final_coords=r["final_coords"],
+         final_S=r["final_S"])
+
+
 def main():
     if not dnl_io.reference_available():
         sys.exit("compiled reference missing: run `make -C oracle ref`")
@@ -219,6 +244,9 @@ def main():
         return
     if sys.argv[1:] == ["mixed"]:
         mixed()
+        return
+    if sys.argv[1:] == ["mixed_materials"]:
+        mixed_materials()
         return
     t = dnl_io.reference_tables()
     save("tables.npz", **t)
@@ -259,6 +287,7 @@ def main():
     tets()
     speed()
     mixed()
+    mixed_materials()
 
 
 if __name__ == "__main__":

@@ -58,6 +58,51 @@ def test_mixed_forces_injected_state_vs_reference(gpu_lib):
         assert rel(out[k], g["out_" + k]) <= STATE_TOL, k
 
 
+def _two_materials():
+    tx, ty = meshes.tabular_table(360e6, 316e6, 0.28)
+    target = meshes.MaterialLaw(74.2e9, 0.33, 2784.0, meshes.HARD_TABULAR, (), tx, ty)
+    copper = meshes.MaterialLaw(117e9, 0.35, 8930.0, meshes.HARD_POWER, (90e6, 292e6, 0.31))
+    steel = meshes.MaterialLaw(193.6e9, 0.3, 7800.0, meshes.HARD_POWER, (250e6, 400e6, 0.4))
+    return target, copper, steel
+
+
+def test_mixed_two_materials_forces_vs_reference(gpu_lib):
+    """The ElTet4n3D + ElHex8n3D domain of test_mixed_forces_injected_state_vs_reference with its
+    tetrahedra of a tabular-hardening material and its hexahedra of a power-law one (materials
+    and the element map over every group, dnl_set_materials after dnl_add_elements): one force pass
+    on the reference's injected state, forces and every point's new state to 1e-12."""
+    target, copper, _ = _two_materials()
+    g = golden("forces_mixed_two.npz")
+    d = gpu_lib.GpuDomain(meshes.group_materials(tet_hex_bar(), [target, copper]))
+    st = {k[3:]: g[k] for k in g.files if k.startswith("in_")}
+    d.set_state(S=st["S"], Eps=st["Eps"], EpsPlas=st["EpsPlas"], p=st["p"], evp=st["evp"],
+                v=st["v"], a=st["a"], disp=st["disp"])
+    f = d.internal_forces(coords=st["coords"], du=st["du"], dt=float(st["dt"]))
+    assert rel(f, g["fint"]) <= FORCE_TOL
+    out = d.get_state("S", "Eps", "EpsPlas", "p", "evp", "Sig")
+    for k in out:
+        assert rel(out[k], g["out_" + k]) <= STATE_TOL, k
+
+
+def test_mixed_two_materials_steps_vs_reference(gpu_lib):
+    """The ElTet4n3D + ElTet10n3D bar with its parts of two materials (other E, nu, rho and
+    hardening), Courant: the lumped mass bit for bit (each element's density), the first time
+    step bit for bit (each element's length over the sound speed of its own material and its
+    nodes' densities, the interface nodes holding the last element's), then 3 steps: forces and
+    times as in test_mixed_tet4_tet10_steps_vs_reference."""
+    _, copper, steel = _two_materials()
+    g = golden("steps_mixed_two.npz")
+    d = gpu_lib.GpuDomain(meshes.group_materials(meshes.taylor_mixed(6, 12), [copper, steel]))
+    d.prologue()
+    assert rel(d.get_state("mass")["mass"], g["mass"][::3]) == 0.0
+    assert d.time_step() == g["dt0"][0]
+    for k in range(3):
+        assert d.step(1) == 1
+        assert rel(d.fint(), g["fint"][k]) <= (FORCE_TOL if k == 0 else TRAJ_TOL), k
+        assert abs(d.time_info()["time"] - g["time"][k]) <= 1e-12 * g["time"][k], k
+    assert rel(d.get_state("coords")["coords"], g["final_coords"]) <= TRAJ_TOL
+
+
 def test_mixed_tet4_tet10_steps_vs_reference(gpu_lib):
     """ElTet4n3D (6 layers) + ElTet10n3D (6 layers), Courant: the lumped mass of both groups
     assembled bit for bit, the first time step bit for bit (the minimum of both groups' lengths
@@ -184,8 +229,9 @@ def test_failure_in_an_added_group_reports_the_domains_element_number(gpu_lib):
 
 def test_add_elements_refusals(gpu_lib):
     """dnl_add_elements only before the run, only 3D reference elements of one family, ElHex8n3D
-    only with the Pulse step, not on a batch's union mesh; a domain of several types refuses
-    several materials and a batch does not take its state."""
+    only with the Pulse step, not on a batch's union mesh, not after several materials (they are
+    set after the groups, over every group's elements); a batch does not take a domain of several
+    types' state."""
     t = meshes.taylor_tet(4, 3)
     d = gpu_lib.GpuDomain(t)
     with pytest.raises(gpu_lib.DnlError):
@@ -193,8 +239,11 @@ def test_add_elements_refusals(gpu_lib):
     with pytest.raises(gpu_lib.DnlError):
         d.add_elements(meshes.ELQUA4NAX, np.zeros((1, 4), dtype=np.int64))  # another family
     d.add_elements(meshes.ELTET4N3D, t.conn[:3])
+    with pytest.raises(ValueError):  # one material index per element of every group
+        d.set_materials(t.material_laws() * 2, np.zeros(t.E, dtype=np.int64))
+    d.set_materials(t.material_laws() * 2, np.r_[np.zeros(t.E), np.ones(3)].astype(np.int64))
     with pytest.raises(gpu_lib.DnlError):
-        d.set_materials(t.material_laws(), np.zeros(t.E + 3, dtype=np.int64))
+        d.add_elements(meshes.ELTET4N3D, t.conn[:3])  # after several materials
     batch = gpu_lib.BatchDomain([t, t])
     with pytest.raises(gpu_lib.DnlError):
         batch.broadcast_state(d)
