@@ -480,6 +480,11 @@ struct dnl_handle {
   double *hooke;              // device, nmat x 3: each material's Hooke entries C00, C01, C33 for
                               // the Pulse products, with several materials and the Pulse step
   double *nodeRo;             // host, N: Current ro of the first nodal field (results files)
+  // several materials, host copies: each element's material (every group, element order) and
+  // each material's power-law exponent (0 for the other laws), for the cached evp^n of
+  // dnl_set_state
+  int *elemMatHost;
+  double *matExpHost;
   // initial state (dnl_reset)
   double *x0;                 // initial coordinates [3][N]
   double v0[3];               // initial velocity

@@ -14,6 +14,7 @@
 //   k_dt         Solver::computeTimeStep (Solver.C:220-267), ExplicitSolverCH::initStep (:434-447),
 //                updateTime and Solver::betweenTimeBounds in one thread, so a run needs no
 //                host round trip per step.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -825,6 +826,8 @@ int dnl_destroy(dnl_handle *h)
     delete p;
   }
   delete[] h->nodeRo;
+  delete[] h->elemMatHost;
+  delete[] h->matExpHost;
   delete h;
   return 0;
 }
@@ -863,6 +866,10 @@ int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, con
   h->hooke = nullptr;
   delete[] h->nodeRo;
   h->nodeRo = nullptr;
+  delete[] h->elemMatHost;
+  h->elemMatHost = nullptr;
+  delete[] h->matExpHost;
+  h->matExpHost = nullptr;
   if (ntab) CK(cudaMalloc(&h->matTab, sizeof(double) * ntab));
   std::vector<Material> hm(nmat);
   std::vector<double> pn(nmat, 0.);
@@ -943,6 +950,10 @@ int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, con
     }
   }
   if (nmat > 1) {
+    h->elemMatHost = new int[Eall];
+    std::copy(elem_material, elem_material + Eall, h->elemMatHost);
+    h->matExpHost = new double[nmat];
+    for (int i = 0; i < nmat; i++) h->matExpHost[i] = mats[i].law == DNL_HARD_POWER ? mats[i].params[2] : 0.;
     std::vector<int> em(elem_material, elem_material + Eall);
     CK(cudaMalloc(&h->elemMat, sizeof(int) * Eall));
     CK(cudaMemcpy(h->elemMat, em.data(), sizeof(int) * Eall, cudaMemcpyHostToDevice));
@@ -1459,14 +1470,17 @@ namespace {
 struct IpSeg {
   double *ip, *stepT;
   size_t nIP, off;
+  long eOff;  // the domain's number of the group's first element
+  int nip;
 };
 std::vector<IpSeg> ip_segments(dnl_handle *h)
 {
-  std::vector<IpSeg> v{{h->ip, h->stepT, (size_t)h->nIP, 0}};
+  std::vector<IpSeg> v{{h->ip, h->stepT, (size_t)h->nIP, 0, 0, h->nip}};
   size_t off = h->nIP;
   for (int gi = 0; gi < h->nextra; gi++) {
-    v.push_back({h->extra[gi].ip, h->extra[gi].stepT, (size_t)h->extra[gi].nIP, off});
-    off += h->extra[gi].nIP;
+    const ElemGroup &g = h->extra[gi];
+    v.push_back({g.ip, g.stepT, (size_t)g.nIP, off, g.eOff, g.nip});
+    off += g.nIP;
   }
   return v;
 }
@@ -1509,7 +1523,10 @@ int dnl_set_state(dnl_handle *h, const dnl_state_view *s)
     if (s->p) CK(cudaMemcpy(g.ip + (size_t)(3 * ns) * nIP, s->p + o, sizeof(double) * nIP, cudaMemcpyHostToDevice));
     if (s->evp) {
       CK(cudaMemcpy(g.ip + (size_t)(3 * ns + 1) * nIP, s->evp + o, sizeof(double) * nIP, cudaMemcpyHostToDevice));
-      for (size_t i = 0; i < nIP; i++) ib[i] = pow(s->evp[o + i], h->mat.n);
+      // the cached evp^n: the exponent of each point's element's material
+      for (size_t i = 0; i < nIP; i++)
+        ib[i] = pow(s->evp[o + i], h->elemMatHost ? h->matExpHost[h->elemMatHost[g.eOff + (long)(i / g.nip)]]
+                                                   : h->mat.n);
       CK(cudaMemcpy(g.ip + (size_t)(3 * ns + 2) * nIP, ib.data(), sizeof(double) * nIP, cudaMemcpyHostToDevice));
     }
   }
