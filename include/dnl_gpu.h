@@ -136,11 +136,12 @@ int dnl_create(const dnl_mesh_desc *mesh, const dnl_material *mat, const dnl_sol
  * further element type in the same domain, which Domain::initSolve accepts within one family
  * (Domain.C:1042-1060): num_elements elements of etype, conn (E*nen, node indices) in the
  * handle's node numbering, numbered after the elements already there.  Before dnl_prologue or the
- * first step; 3D reference elements (ElHex8n3D, ElTet4n3D, ElTet10n3D) with one power-law
- * material, ElHex8n3D with the Pulse time step only.  Integration-point arrays of
- * dnl_get/set_state, dnl_get_step_tensors, the results files, the forward-mode sensitivities and
- * the reverse-mode adjoint then cover every group in element order; dnl_set_materials returns
- * DNL_ERR_ARG on such a handle, and so does this call on a batch's union mesh (dnl_batch_handle). */
+ * first step and before dnl_set_materials (which then takes one material per element of every
+ * group); 3D reference elements (ElHex8n3D, ElTet4n3D, ElTet10n3D), ElHex8n3D with the Pulse time
+ * step only.  Integration-point arrays of dnl_get/set_state, dnl_get_step_tensors, the results
+ * files, the forward-mode sensitivities and the reverse-mode adjoint then cover every group in
+ * element order.  DNL_ERR_ARG after several materials or another hardening law were set, and on a
+ * batch's union mesh (dnl_batch_handle). */
 int dnl_add_elements(dnl_handle *h, int etype, int num_elements, const int *conn);
 int dnl_destroy(dnl_handle *h);
 /* DNL_ELHEX8N3D_1PT: the viscous hourglass coefficient (default 0.05): the force resisting the
