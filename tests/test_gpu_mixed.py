@@ -128,12 +128,15 @@ def test_mixed_tet4_tet10_steps_vs_reference(gpu_lib):
     assert rel(st["p"], g["final_p"]) <= 1e-6
 
 
-@pytest.mark.parametrize("kind", ["hex_pulse", "tet4_courant"])
+@pytest.mark.parametrize("kind", ["hex_pulse", "tet4_courant", "hex_two_materials_pulse"])
 def test_split_into_groups_is_bitwise_the_single_group(gpu_lib, kind):
     """A mesh given as two groups of its own element type (the first 40 % of its elements, then
     the rest through dnl_add_elements) numbers its element-node slots as the single group does, so
-    every kernel sees the same data: 30 steps bit for bit (coordinates, forces, time, state)."""
-    m = meshes.taylor_hex(6, 8) if kind == "hex_pulse" else meshes.taylor_tet(6, 8)
+    every kernel sees the same data: 30 steps bit for bit (coordinates, forces, time, state); with
+    two materials (tabular and elastic, Pulse) the groups read their elements' materials and Hooke
+    entries from the one element map."""
+    m = {"hex_pulse": lambda: meshes.taylor_hex(6, 8), "tet4_courant": lambda: meshes.taylor_tet(6, 8),
+         "hex_two_materials_pulse": lambda: meshes.impact_two_materials_hex(4, 12)}[kind]()
     cut = int(0.4 * m.E)
     split = dataclasses.replace(m, conn=m.conn[:cut], groups=[(m.etype, m.conn[cut:])])
     a = gpu_lib.GpuDomain(m)
