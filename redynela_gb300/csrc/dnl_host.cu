@@ -836,7 +836,7 @@ int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, con
 {
   if (!h || nmat < 1 || !mats || h->prologueDone || h->batchUnion) return DNL_ERR_ARG;
   if (nmat > 1 && !elem_material) return DNL_ERR_ARG;
-  const long N = h->N, E = h->E, nIP = h->nIP;
+  const long N = h->N, E = h->E;
   long Eall = E;  // elements of every group, in element order
   for (int gi = 0; gi < h->nextra; gi++) Eall += h->extra[gi].E;
   if (elem_material)
@@ -925,7 +925,6 @@ int dnl_set_materials(dnl_handle *h, int nmat, const dnl_material_law *mats, con
       for (int q = 0; q < gnip; q++) pnIP[e * gnip + q] = pn[matOf(gOff + e)];
     CK(cudaMemcpy(gip + (size_t)(3 * ns + 2) * gIP, pnIP.data(), sizeof(double) * gIP, cudaMemcpyHostToDevice));
   }
-  (void)nIP;
   CK(cudaMalloc(&h->evpn0, sizeof(double) * nmat));
   CK(cudaMemcpy(h->evpn0, pn.data(), sizeof(double) * nmat, cudaMemcpyHostToDevice));
   // Element::getSoundSpeed: the element's E and nu, the mean of its nodes' densities; kept per
