@@ -68,3 +68,26 @@ def test_random_state_covers_every_group():
     assert st["S"].shape == (n, 3, 3) and st["p"].shape == (n,) and st["evp"].shape == (n,)
     assert np.allclose(st["S"], np.swapaxes(st["S"], -1, -2))
     assert np.allclose(np.trace(st["S"], axis1=-2, axis2=-1), 0.0, atol=1e-3)
+
+
+def test_group_materials_assign_one_material_per_group():
+    a = meshes.MaterialLaw(117e9, 0.35, 8930.0)
+    b = meshes.MaterialLaw(193.6e9, 0.3, 7800.0)
+    m = meshes.group_materials(meshes.taylor_mixed(4, 6, nz_lower=3), [a, b])
+    (_, c0), (_, c1) = m.element_groups()
+    assert m.elem_material.shape == (m.E_all,)
+    assert np.all(m.elem_material[:c0.shape[0]] == 0) and np.all(m.elem_material[c0.shape[0]:] == 1)
+    assert m.material_laws() == [a, b]
+
+
+def test_two_material_hex_bar_layers_and_speeds():
+    """impact_two_materials_hex: the lower half of the layers is the target (material 0), the upper
+    half the projectile, whose nodes (the interface plane's included) alone move."""
+    m = meshes.impact_two_materials_hex(4, 12)
+    z_bottom = m.coords[m.conn[:, 0], 2]
+    zi = 6 * (m.coords[:, 2].max() / 12)
+    assert np.all(m.elem_material[z_bottom < zi - 1e-12] == 0)
+    assert np.all(m.elem_material[z_bottom >= zi - 1e-12] == 1)
+    moving = m.initial_velocity[:, 2] != 0
+    assert np.all(m.coords[moving, 2] >= zi - 1e-12) and np.all(m.coords[~moving, 2] < zi - 1e-12)
+    assert m.method == meshes.PULSE and len(m.material_laws()) == 2
