@@ -41,6 +41,9 @@ namespace {
 struct AdjState {
   int E = 0, N = 0, nsteps = 0, stride = 0, nseg = 0, etype = -1;
   long nIP = 0;                 // integration points of every element group
+  // Per-point arrays below ([X][nIP]) hold one block per element group, [X][nIP_g] at X ipOff, as
+  // the handle's integration-point state; gpar alone is [3][nIP] over all points (its sum runs in
+  // element order); element-node arrays ([DIM][E NEN]) span every group's slots (EN).
   size_t ckptDoubles = 0, slotDoubles = 0;
   double *mem = nullptr;
   double *ckpt = nullptr;       // nseg x [x(3N) | Current du, v, a, disp (12N) | ip (NCOMP nIP)]
