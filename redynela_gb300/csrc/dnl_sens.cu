@@ -22,11 +22,11 @@ namespace dnl {
 struct SensState {
   int E, N;
   double *mem = nullptr;
-  double *tape = nullptr;  // [NT][E*NIP]
+  double *tape = nullptr;  // [NT][nIP_g] per element group, at NT ipOff
   double *tx = nullptr;    // [dir][3][N]
   double *tb[2][4];        // [bank][du, v, a, disp] -> [dir][3][N]
-  double *tip = nullptr;   // [dir][NCOMP][E*NIP]
-  double *tfe = nullptr;   // [dir][DIM][E*NEN]
+  double *tip = nullptr;   // [dir][NCOMP][nIP_g] per element group, at 4 NCOMP ipOff
+  double *tfe = nullptr;   // [dir][DIM][EN]: every group's element-node slots
   double *dts = nullptr;   // step sizes on the device
   double *out = nullptr;   // N*3 staging for node-major results
   int dtsCap = 0;
