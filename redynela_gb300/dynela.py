@@ -810,7 +810,8 @@ class BatchDomain:
 
 # ====================================================================== deck-level mirror
 class Material:
-    """Material (finiteElement/Material.h:61-156): setYoung, setPoisson, setDensity, setHardening."""
+    """Material (finiteElement/Material.h:61-156): setYoung, setPoisson, setDensity, setHardening
+    (no hardening attached: elastic)."""
 
     def __init__(self):
         self.young = 0.0
@@ -830,6 +831,16 @@ class Material:
     def setHardening(self, h):
         self.hardening = h
 
+    def setColor(self, r, g, b):
+        pass  # post-processing colour
+
+    def law(self) -> meshes.MaterialLaw:
+        """The library's description of this material and its hardening."""
+        h = self.hardening
+        if h is None:
+            return meshes.MaterialLaw(self.young, self.poisson, self.density, meshes.HARD_ELASTIC)
+        return h._law(self)
+
 
 class IsoHardElastoplastic:
     """sigma_y = A + B evp^n (finiteElement/IsoHardElastoplastic.C:171-184)."""
@@ -846,6 +857,50 @@ class IsoHardElastoplastic:
 
     def setHardExponent(self, v):
         self.n = float(v)
+
+    def _law(self, m: Material) -> meshes.MaterialLaw:
+        return meshes.MaterialLaw(m.young, m.poisson, m.density, meshes.HARD_POWER, (self.A, self.B, self.n))
+
+
+class DiscreteFunction:
+    """DiscreteFunction (basicTools/DiscreteFunction.C): points (x, y) kept sorted by x."""
+
+    def __init__(self):
+        self.points: List[tuple] = []
+
+    def add(self, x, y):
+        self.points.append((float(x), float(y)))
+        self.points.sort(key=lambda q: q[0])
+
+
+class IsoHardElastoplasticTabular:
+    """sigma_y tabulated against evp by a DiscreteFunction
+    (finiteElement/IsoHardElastoplasticTabular.C:103-116)."""
+
+    def __init__(self):
+        self.function = None
+
+    def setFunction(self, f: DiscreteFunction):
+        self.function = f
+
+    def _law(self, m: Material) -> meshes.MaterialLaw:
+        xs = np.array([q[0] for q in self.function.points])
+        ys = np.array([q[1] for q in self.function.points])
+        return meshes.MaterialLaw(m.young, m.poisson, m.density, meshes.HARD_TABULAR, (), xs, ys)
+
+
+class IsoHardMetafor:
+    """sigma_y = (P2 - P1)(1 - exp(-P3 evp)) + P4 evp^P5 + P1 (1 + P6 evp)^P7 + P8 evp
+    (finiteElement/IsoHardMetafor.C:132-153); set(k, value) is getConstitutiveParameter(k) = value."""
+
+    def __init__(self):
+        self.P = [0.0] * 8
+
+    def set(self, k, v):
+        self.P[int(k)] = float(v)
+
+    def _law(self, m: Material) -> meshes.MaterialLaw:
+        return meshes.MaterialLaw(m.young, m.poisson, m.density, meshes.HARD_METAFOR, tuple(self.P))
 
 
 class NodeSet:
@@ -901,6 +956,9 @@ class ExplicitSolverCH:
         self.frequency = int(v)
 
     def setTimeStepMethod(self, name):
+        """Solver::setTimeStepMethod (Solver.C:312-322): "Courant" or "Pulse"."""
+        if name not in ("Courant", "Pulse"):
+            raise ValueError(f"setTimeStepMethod: unknown method {name}")
         self.method = {"Courant": meshes.COURANT, "Pulse": meshes.PULSE}[name]
 
 
@@ -913,13 +971,20 @@ ElHex8n3D_1PT = meshes.ELHEX8N3D_1PT
 
 
 class Structure:
-    """The model-building calls of a .dyn deck (finiteElement/Structure.h), solved on the GPU."""
+    """The model-building calls of a .dyn deck (finiteElement/Structure.h), solved on the GPU.
+
+    Elements are numbered in creation order (Structure::createElement); a setDefaultElement of
+    another type between createElement calls starts a further element group (3D reference
+    elements; dnl_add_elements).  Each attachMaterialToElements sets the material of its set's
+    elements (later attachments win), each attachInitialBC the initial velocity of its set's
+    nodes (BoundarySpeed::applyInitial_V0), each attachConstantBC a restraint (BoundaryRestrain) or
+    an imposed speed (BoundarySpeed) on its set's nodes."""
 
     def __init__(self):
         self._nodes: Dict[int, Sequence[float]] = {}
-        self._elements: Dict[int, Sequence[int]] = {}
+        self._elements: List[tuple] = []  # (number, etype, node numbers) in creation order
         self._etype = None
-        self._material = None
+        self._materials: List[tuple] = []  # (Material, ElementSet)
         self._initial = []
         self._constant = []
         self._solver = None
@@ -932,13 +997,15 @@ class Structure:
         self._etype = etype
 
     def createElement(self, num, *nodes):
-        self._elements[int(num)] = tuple(int(n) for n in nodes)
+        if self._etype is None:
+            raise ValueError("createElement: no default element type (setDefaultElement)")
+        self._elements.append((int(num), self._etype, tuple(int(n) for n in nodes)))
 
     def addMaterial(self, mat):
-        self._material = mat
+        pass  # materials enter through attachMaterialToElements
 
     def attachMaterialToElements(self, mat, els):
-        self._material = mat
+        self._materials.append((mat, els))
 
     def attachInitialBC(self, bnd, nodes):
         self._initial.append((bnd, nodes))
@@ -956,18 +1023,57 @@ class Structure:
         nums = sorted(self._nodes)
         index = {n: i for i, n in enumerate(nums)}
         coords = np.array([self._nodes[n] for n in nums], dtype=np.float64)
-        conn = np.array([[index[n] for n in self._elements[e]] for e in sorted(self._elements)],
-                        dtype=np.int64)
-        v0 = (0.0, 0.0, 0.0)
+        N = len(nums)
+        # element groups: runs of one type in creation order
+        runs: List[tuple] = []
+        for num, et, nodes in self._elements:
+            if not runs or runs[-1][0] != et:
+                runs.append((et, []))
+            runs[-1][1].append([index[n] for n in nodes])
+        if not runs:
+            raise ValueError("model: no elements")
+        conns = [(et, np.array(c, dtype=np.int64)) for et, c in runs]
+        enum = {num: i for i, (num, _, _) in enumerate(self._elements)}
+        E = len(self._elements)
+        # materials: each attachment sets its elements' material, later ones win
+        if not self._materials:
+            raise ValueError("model: no material attached")
+        mats: List[Material] = []
+        em = np.full(E, -1, dtype=np.int64)
+        for mat, els in self._materials:
+            if mat not in mats:
+                mats.append(mat)
+            em[[enum[n] for n in els.numbers]] = mats.index(mat)
+        if np.any(em < 0):
+            raise ValueError("model: elements without a material")
+        used = sorted(set(em.tolist()))
+        mats = [mats[i] for i in used]
+        em = np.searchsorted(used, em)
+        laws = [m.law() for m in mats]
+        first = laws[0]
+        A, B, n = (first.params if first.law == meshes.HARD_POWER else (0.0, 0.0, 1.0))
+        single = len(laws) == 1 and first.law == meshes.HARD_POWER
+        # initial velocities per node, later attachments win; one speed on every node is v0
+        vel = np.zeros((N, 3))
+        covered = np.zeros(N, dtype=bool)
         for bnd, ns in self._initial:
-            v0 = bnd.val
+            idx = [index[k] for k in ns.numbers]
+            vel[idx] = bnd.val
+            covered[idx] = True
+        uniform = bool(covered.all()) and bool(np.all(vel == vel[0])) if N else True
+        v0 = tuple(vel[0]) if uniform else (0.0, 0.0, 0.0)
         bcs = []
         for bnd, ns in self._constant:
             kind = meshes.RESTRAIN if isinstance(bnd, BoundaryRestrain) else meshes.SPEED
-            bcs.append(BCGroup(kind, bnd.val, np.array([index[n] for n in ns.numbers])))
-        mat, hard, s = self._material, self._material.hardening, self._solver
-        return Model(self._etype, coords, conn, mat.young, mat.poisson, mat.density, hard.A,
-                     hard.B, hard.n, v0, bcs, s.end, s.rho_b, s.safety, s.frequency, s.method)
+            bcs.append(BCGroup(kind, bnd.val, np.array([index[k] for k in ns.numbers], dtype=np.int64)))
+        s = self._solver
+        if s is None:
+            raise ValueError("model: no solver (addSolver)")
+        (et0, conn0), rest = conns[0], conns[1:]
+        return Model(et0, coords, conn0, first.young, first.poisson, first.density, A, B, n, v0, bcs,
+                     s.end, s.rho_b, s.safety, s.frequency, s.method,
+                     materials=None if single else laws, elem_material=None if single else em,
+                     initial_velocity=None if uniform else vel, groups=rest or None)
 
     def initSolve(self, flags: int = 0) -> GpuDomain:
         self.domain = GpuDomain(self.model(), flags)
